@@ -1,0 +1,169 @@
+/*
+ * f8.h — C ABI of the GB300 SMAC + FENE-P + immersed-boundary time step.
+ *
+ * The reference (machapin/fortran8) has no library interface: its "API" is the
+ * set of subroutines that each solver's main loop calls on whole grid arrays
+ * (fenep.f90:2477-2527, fenep_2d.f90:1912-1966, fenep_mpi.f90:2929-2967).
+ * This header replaces that loop body with one opaque context and a handful of
+ * entry points that take the reference's own array layouts, so a Fortran main
+ * program can bind them with iso_c_binding (fortran/f8_gpu.f90) and keep its
+ * init / output code unchanged.
+ *
+ * Array layouts (all double precision, column-major as in the reference):
+ *   U, V, W, P, Phi : (0:NX+1, 0:NY+1, 0:NZ+1), x fastest, one halo layer
+ *                     (fenep.f90:2424, 2437-2438).  In 2D NZ = 1 and the z halo
+ *                     planes are copies of plane 1.
+ *   C               : (NC, 0:NX+1, 0:NY+1, 0:NZ+1), component fastest;
+ *                     NC = 6 in 3D (xx,xy,xz,yy,yz,zz; fenep.f90:2425) and
+ *                     NC = 3 in 2D (xx,xy,yy; fenep_2d.f90:1877).
+ *   Ax0..Az0, Tx0..Tz0, Fx..Fz : (1:NX, 1:NY, 1:NZ), no halo (fenep.f90:2430-2439).
+ *
+ * Every call is synchronous on return.  A context is not thread-safe.  No call
+ * aborts the host process: failures are reported by the returned status.
+ *
+ * The same entry points with the prefix f8o_ are exported by the CPU oracle
+ * (oracle/liboracle_f8.so), so one harness drives both.
+ */
+#ifndef F8_H
+#define F8_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F8_ABI_VERSION 1
+
+/* Status codes.  F8_WARN_* are non-fatal: the step completed. */
+enum f8_status {
+    F8_OK = 0,
+    F8_ERR_ARG = 1,         /* bad grid / parameter / pointer                     */
+    F8_ERR_STATE = 2,       /* call out of order (step before load, ...)          */
+    F8_ERR_NOMEM = 3,       /* device or host allocation failed                   */
+    F8_ERR_CUDA = 4,        /* a CUDA runtime call failed                          */
+    F8_ERR_NAN = 5,         /* NaN/Inf found in the velocity after a step
+                               (reference: stop 'NaN value', fenep_2d.f90:1974)   */
+    F8_ERR_UNSUPPORTED = 6, /* option combination not built                        */
+    F8_ERR_NO_DEVICE = 7,   /* no CUDA device / extension not usable               */
+    F8_WARN_NEWTON = 16,    /* some cells reached newton_itrmax without meeting
+                               newton_eps (reference continues silently,
+                               fenep.f90:556-577)                                  */
+    F8_WARN_SOR = 17        /* SOR reached sor_itrmax (fenep.f90:885-901)          */
+};
+
+enum f8_precision {
+    F8_FP64 = 0,   /* every operation in FP64, same operation order as the oracle */
+    F8_MIXED = 1   /* FP32 bulk stencils, FP64 state / Peterlin / reductions /
+                      Poisson defect correction                                  */
+};
+
+enum f8_poisson {
+    F8_POISSON_FFT = 0, /* periodic: 3D FFT (fenep.f90:1529-1560);
+                           y-walls: FFT(x,z) + tridiagonal in y
+                           (fenep_2d.f90:1294-1342)                            */
+    F8_POISSON_SOR = 1  /* red-black SOR (fenep.f90:848-905, smac_kabe.f90:302-374) */
+};
+
+enum f8_bc_y {
+    F8_BC_PERIODIC = 0, /* PBM (fenep.f90:147-166)                         */
+    F8_BC_WALLS = 1     /* no-slip walls at y = 0 and y = NY*dY
+                           (fenep_2d.f90:1098-1143 with NA = 0, NB = NY)  */
+};
+
+typedef struct f8_grid {
+    int dim;            /* 2 or 3                                         */
+    int nx, ny, nz;     /* cell counts; powers of two for the FFT solver;
+                           nz = 1 when dim == 2                           */
+    double lx, ly, lz;  /* box lengths: dX = lx/nx ... (fenep.f90:13)     */
+    int bc_y;           /* enum f8_bc_y                                   */
+    double uwall;       /* upper-wall speed when bc_y == F8_BC_WALLS
+                           (fenep_2d.f90:1084, 1103)                      */
+} f8_grid;
+
+typedef struct f8_phys {
+    double re, wi, beta;    /* Re, Wi, beta (fenep.f90:23-25)                          */
+    double lp2;             /* L^2 of the Peterlin factor; the reference's Lp**2
+                               (fenep.f90:513)                                         */
+    double dt;
+    double newton_dc;       /* finite-difference step of the Jacobian (fenep.f90:526)  */
+    double newton_eps;      /* relative step tolerance (fenep.f90:528)                 */
+    int newton_itrmax;      /* fenep.f90:527                                           */
+    double sor_omega;       /* SOR relaxation factor                                   */
+    double sor_eps;         /* relative residual tolerance (fenep.f90:856)             */
+    int sor_itrmax;         /* fenep.f90:857                                           */
+    int ab2_start;          /* 1: the first step copies A->A0, T->T0 (input_type == 0,
+                               fenep.f90:1445-1452)                                    */
+} f8_phys;
+
+typedef struct f8_cyl {
+    double xc, yc;  /* centre in the x-y plane; the cylinder spans z            */
+    double r;       /* radius (the reference's DC/2, fenep.f90:19)             */
+    double spin;    /* marker surface speed of a rotating cylinder; 0 = fixed
+                       (fenep.f90:1847-1854, 1882-1889)                         */
+    int filled;     /* 1: markers on concentric shells (ibm_type 2x,
+                       fenep.f90:1791-1801); 0: surface ring (ibm_type 1x)      */
+} f8_cyl;
+
+typedef struct f8_fields {
+    double *u, *v, *w, *p, *phi;    /* halo layout, see above                   */
+    double *c;                      /* component-fastest halo layout            */
+    double *ax0, *ay0, *az0;        /* AB2 history of the convection term       */
+    double *tx0, *ty0, *tz0;        /* trapezoid history of the polymer stress  */
+    double *fx, *fy, *fz;           /* body force (fenep.f90:96-120)            */
+} f8_fields;
+
+typedef struct f8_diag {
+    int step;                   /* steps taken since f8_load's step0            */
+    double ke;                  /* 0.5 <|u|^2> on cell centres (fenep.f90:2266-2300) */
+    double cfl;                 /* max(|u|dt/dX + |v|dt/dY + |w|dt/dZ)           */
+    double trc_min, trc_max, trc_mean;
+    double div_max;             /* max |div u| after the projection             */
+    long long newton_iters;     /* Newton iterations summed over cells, last step */
+    long long newton_unconverged; /* cells at newton_itrmax, last step           */
+    int poisson_iters;          /* SOR iterations of the last step (-1: FFT)     */
+    int nan_found;
+} f8_diag;
+
+typedef struct f8_ctx f8_ctx;
+
+/* Create a solver context.  cyls may be NULL when ncyl == 0 (no IBM; the
+ * predictor is the plain CN/AB2 FFT step, fenep.f90:1430-1527).  precision is
+ * enum f8_precision, poisson enum f8_poisson.
+ * Replaces: fft_init + ibm_init (fenep.f90:2459-2462, 1374-1377, 1769-1900). */
+int f8_create(f8_ctx **ctx, const f8_grid *grid, const f8_phys *phys,
+              const f8_cyl *cyls, int ncyl, int precision, int poisson);
+
+/* Copy a state in from host arrays in the reference layouts.  Any pointer of
+ * the A0/T0/F/phi groups may be NULL (zeros).  step0 is the number of steps
+ * already taken (0 = fresh start; the AB2 start rule applies when
+ * step0 == 0 and phys->ab2_start).
+ * Replaces: init / input (fenep.f90:52-145, 1186-1233). */
+int f8_load(f8_ctx *ctx, const f8_fields *in, int step0);
+
+/* Advance nsteps time steps.  drag may be NULL; otherwise it receives
+ * nsteps * ncyl * 3 doubles: for each step and cylinder the force of the
+ * fluid on the body, -sum_markers(Fc) * dV (x, y, z), dV = dX*dY*dZ (3D) or
+ * dX*dY (2D).  Returns the worst status of the steps.
+ * Replaces: the body of the step loop (fenep.f90:2477-2527). */
+int f8_step(f8_ctx *ctx, int nsteps, double *drag);
+
+/* Copy the state out to host arrays (same layouts as f8_load).  NULL
+ * pointers are skipped.  Replaces: output (fenep.f90:1186-1233). */
+int f8_store(f8_ctx *ctx, f8_fields *out);
+
+/* Diagnostics of the current state (log_progress, fenep.f90:2266-2342). */
+int f8_diagnostics(f8_ctx *ctx, f8_diag *out);
+
+/* Number of Lagrangian markers per z-plane and their host-side positions
+ * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */
+int f8_markers(f8_ctx *ctx, int *n_per_plane, double *xy);
+
+const char *f8_strerror(int status);
+void f8_destroy(f8_ctx *ctx);
+
+/* Fill a phys struct with the reference's defaults (fenep.f90:526-528, 855-857). */
+void f8_default_phys(f8_phys *phys);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* F8_H */
