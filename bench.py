@@ -1,0 +1,304 @@
+"""Benchmark of the SMAC + FENE-P + IBM time step (Mcell-steps/s).
+
+Workload: the 256 x 128 x 128 channel with no-slip walls in y and 2 x 2
+spanwise cylinders (Re 500, Wi 5, beta 0.9, L^2 900, dt 2e-4), synthetic
+seeded initial state (Poiseuille + noise), see fortran8_gb300/configs.py.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision auto|fp64|mixed] [--workload c3_channel]
+
+ours:      K steps through the C ABI with the state resident in HBM, timed by
+           CUDA events that the library records on its own stream; the e2e
+           number times load-from-host + K single-step calls that read the
+           drag history back every step + store-to-host.
+reference: the CPU oracle (the reference's algorithm restated in C++, the
+           reference itself cannot be compiled here) on all host cores.
+Multi-GPU: the step does not shard (one domain per GPU); N ranks run N
+independent replicas ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from fortran8_gb300 import abi, configs  # noqa: E402
+from fortran8_gb300.solver import Solver  # noqa: E402
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+# Algorithmic bytes per cell of each stage of the FP64 step (words of 8 B):
+# every field a stage must read once and write once.
+FP64_STAGE_WORDS = {
+    "eigen": 6.125,      # C (6) read, 1-byte selection code written
+    "newton": 16.125,    # C, U, V, W read (9) + code; C (6) and f(C) (1) written
+    "momentum": 32.0,    # U V W P, C (6), f, A0 (3), T0 (3), F (3) read; Ua (3), B (3), A0, T0 written
+    "ibm": 9.0,          # Ua (3), B (3) read, Q (3) written (marker traffic excluded)
+    "helmholtz": 6.0,    # Q (3) read, U* (3) written (FFT-internal passes excluded)
+    "poisson": 5.0,      # U* (3) read, RHS, Phi written (FFT-internal passes excluded)
+    "project": 9.0,      # U*, Phi, P read (5); U, V, W, P written (4)
+}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"])}, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"f8_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def state_bytes(st):
+    return int(sum(a.nbytes for a in st.arrays.values()))
+
+
+def pinned_state(st):
+    """Copy a state into page-locked host memory (numpy views of pinned tensors)."""
+    import torch
+    out = {}
+    for k, a in st.arrays.items():
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        v = t.numpy()
+        v[...] = a
+        out[k] = (t, v)
+    from fortran8_gb300.solver import State
+    return State({k: v for k, (t, v) in out.items()}), [t for t, _ in out.values()]
+
+
+def oracle_fns():
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    lib = C.CDLL(str(ROOT / "oracle" / "liboracle_f8.so"))
+    lib.f8o_max_threads.restype = C.c_int
+    return abi.bind(lib, "f8o_"), lib
+
+
+def cpu_baseline(w, steps_cap=2, budget_s=30.0):
+    """Oracle on the host cores (all threads) on a bounded sample of the workload."""
+    fns, lib = oracle_fns()
+    threads = int(lib.f8o_max_threads())
+    st0 = configs.initial_state(w)
+    with Solver(fns, w.grid, w.phys, w.cyls) as s:
+        s.load(st0)
+        t0 = time.perf_counter()
+        n = 0
+        while n < steps_cap:
+            s.step(1, want_drag=True)
+            n += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        el = time.perf_counter() - t0
+    return {"value": w.cells * n / el / 1e6, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} full step(s) of {w.grid.nx}x{w.grid.ny}x{w.grid.nz} from the seeded initial state, "
+                      f"FP64, {threads} OpenMP threads, {el:.1f} s"}
+
+
+def run_reference(args, w):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return 0
+    fns, lib = oracle_fns()
+    threads = int(lib.f8o_max_threads())
+    with Solver(fns, w.grid, w.phys, w.cyls) as s:
+        s.load(configs.initial_state(w))
+        s.step(args.warmup)
+        t0 = time.perf_counter()
+        s.step(args.steps)
+        el = time.perf_counter() - t0
+    v = w.cells * args.steps / el / 1e6
+    line = {"impl": "reference", "metric": "Mcell-steps/s", "value": v, "unit": "Mcell-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
+                       "poisson": "fft+tridiagonal"},
+            "cpu_baseline": {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps after {args.warmup} warm-up, FP64, {threads} threads"},
+            "e2e": {"value": v, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, w):
+    import torch
+    ws, rank, local = dist_init()
+    from fortran8_gb300 import build as b, lib as flib
+    if rank == 0:
+        b.build()
+    barrier(ws)
+    torch.cuda.set_device(local)
+    fns = flib.functions()
+    prec = {"fp64": abi.F8_FP64, "mixed": abi.F8_MIXED}[args.precision]
+    st0 = configs.initial_state(w)
+    cells = w.cells
+    peaks, peak_kind = load_peaks()
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+        s.load(st0)
+        s.step(args.warmup)
+        s.set_timing(True)
+        s.timing_reset()
+        torch.cuda.synchronize()
+        barrier(ws)
+        with ClockSampler(local) as clk:
+            status, drag = s.step(args.steps)
+        torch.cuda.synchronize()
+        barrier(ws)
+        tot_ms, stage_ms, nst = s.timing()
+        clocks = clk.summary()
+        diag = s.diagnostics()
+    ms = max_over_ranks(ws, tot_ms)
+    value = cells * args.steps * ws / (ms / 1e3) / 1e6
+    # e2e: host arrays in, K single-step calls reading the drag every step, host arrays out
+    pst, _keep = pinned_state(st0)
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+        s.load(pst)
+        s.step(args.warmup)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        s.load(pst, step0=0)
+        for _ in range(args.steps):
+            s.step(1)
+        out = s.store()
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
+    sb = state_bytes(st0)
+    ncyl = len(w.cyls)
+    e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s",
+           "h2d_bytes_per_step": int(sb / args.steps),
+           "d2h_bytes_per_step": int(sb / args.steps + ncyl * 3 * 8 + 8)}
+    if rank != 0:
+        return 0
+    # roofline of the dominant stage
+    per_step = stage_ms / max(nst, 1)
+    names = abi.STAGE_NAMES
+    top = int(np.argmax(per_step))
+    words = FP64_STAGE_WORDS[names[top]]
+    achieved = words * 8 * cells / (per_step[top] / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel_stage": names[top], "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
+            "traffic": None, "stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)}}
+    line = {"metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == abi.F8_FP64 else "f32+f64",
+            "data": "synthetic (seeded Poiseuille + noise, C = I)",
+            "config": {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": ncyl,
+                       "precision": args.precision, "poisson": "fft+tridiagonal",
+                       "l2": "inputs larger than L2 (state %.2f GB)" % (sb / 1e9), "parallelism": f"replicas{ws}"},
+            "status": int(status), "div_max": diag.div_max, "newton_iters_per_cell": diag.newton_iters / cells,
+            "drag_last": drag[-1].tolist() if drag is not None else None,
+            "gpu_launches": None, "clocks": clocks, "roofline": roof, "e2e": e2e}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w)
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.precision == "auto":
+        args.precision = "fp64"
+    w = configs.WORKLOADS[args.workload]()
+    if args.impl == "reference":
+        return run_reference(args, w)
+    return run_ours(args, w)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -76,7 +76,13 @@ ABI_FUNCTIONS = {
     "strerror": (C.c_char_p, [C.c_int]),
     "destroy": (None, [C.c_void_p]),
     "default_phys": (None, [C.POINTER(Phys)]),
+    "set_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_longlong)]),
+    "timing_reset": (C.c_int, [C.c_void_p]),
 }
+
+NSTAGE = 7
+STAGE_NAMES = ("eigen", "newton", "momentum", "ibm", "helmholtz", "poisson", "project")
 
 
 def bind(lib: C.CDLL, prefix: str) -> dict:

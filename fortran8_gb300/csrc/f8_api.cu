@@ -1,0 +1,540 @@
+// f8_api.cu — the C ABI of include/f8.h on one GB300.
+//
+// One context owns the device state of one solver instance (one CUDA stream).
+// Host arrays cross the boundary only in f8_load / f8_store / f8_step's drag
+// history; between calls the state stays resident in HBM.  The step loop body
+// replaces the reference's main loop (fenep.f90:2477-2527).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+#include "../../include/f8.h"
+#include "f8_kernels.h"
+
+using namespace f8;
+
+namespace {
+
+const double PI = 3.141592653589793238462643383279502884;
+
+struct Marker { double x, y, u, v; int cyl; };
+
+// Marker set of one z-plane from the cylinder list, following ibm_init
+// (fenep.f90:1784-1899, fenep_2d.f90:1472-1629): surface rings of
+// nint(pi*DC/dX) points, or concentric shells i = 0..int(DC/(2dX)) of
+// nint(pi*(DC-2 i dX)/dX) points with one centre point; ordered marker-major,
+// cylinder-minor like the reference's (NC, NL, NZ) arrays.
+std::vector<Marker> build_markers(const std::vector<f8_cyl> &cyl, double dX, int dim) {
+    std::vector<std::vector<Marker>> per(cyl.size());
+    for (size_t l = 0; l < cyl.size(); ++l) {
+        const f8_cyl &cy = cyl[l];
+        const double DC = 2.0 * cy.r;
+        if (!cy.filled) {
+            int NL = (int)std::lround(PI * DC / dX);
+            if (NL < 1) NL = 1;
+            for (int j = 1; j <= NL; ++j) {
+                double ang = 2 * PI / NL * j;
+                per[l].push_back({cy.xc + DC / 2 * std::cos(ang), cy.yc + DC / 2 * std::sin(ang),
+                                  cy.spin * std::sin(ang), -cy.spin * std::cos(ang), (int)l});
+            }
+        } else {
+            int NL_lap = (int)(DC / (2 * dX));
+            std::vector<int> shell(NL_lap + 1);
+            for (int i = 0; i <= NL_lap; ++i) shell[i] = (int)std::lround(PI * (DC - 2 * i * dX) / dX);
+            if (shell[NL_lap] == 0) shell[NL_lap] = 1;
+            for (int i = 0; i <= NL_lap; ++i)
+                for (int j = 1; j <= shell[i]; ++j) {
+                    double ang = 2 * PI / shell[i] * j;
+                    double rr = (DC - 2 * i * dX) / 2;
+                    per[l].push_back({cy.xc + rr * std::cos(ang), cy.yc + rr * std::sin(ang),
+                                      cy.spin * ((DC - 2 * i * dX) / DC * std::sin(ang)),
+                                      -cy.spin * ((DC - 2 * i * dX) / DC * std::cos(ang)), (int)l});
+                }
+        }
+    }
+    std::vector<Marker> out;
+    size_t maxn = 0;
+    for (auto &p : per) maxn = std::max(maxn, p.size());
+    for (size_t m = 0; m < maxn; ++m)
+        for (size_t l = 0; l < per.size(); ++l)
+            if (m < per[l].size()) out.push_back(per[l][m]);
+    if (dim == 2)  // fenep_2d.f90:1628-1629
+        for (auto &m : out) { m.x = m.x + 10e-10 * dX; m.y = m.y + 10e-10 * dX; }
+    return out;
+}
+
+void stencil_origin_h(int comp, double xc, double yc, double dX, double dY, int &i0, int &j0) {
+    if (comp == 0) { j0 = (int)(yc / dY); i0 = (int)(xc / dX - 0.5); }
+    else if (comp == 1) { j0 = (int)(yc / dY - 0.5); i0 = (int)(xc / dX); }
+    else { j0 = (int)(yc / dY); i0 = (int)(xc / dX); }
+}
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+}  // namespace
+
+struct f8_ctx {
+    f8_grid grid{};
+    f8_phys phys{};
+    std::vector<f8_cyl> cyl;
+    std::vector<Marker> mk;
+    int precision = 0, poisson = 0;
+    Dev d{};
+    cudaStream_t s = nullptr;
+    bool loaded = false;
+    int step = 0;            // steps taken (absolute, includes step0)
+    int step0 = 0;
+    std::vector<void *> allocs;
+    double *drag_dev = nullptr;
+    int drag_cap = 0;
+    double *scratch_aos = nullptr;   // ncomp * cs doubles (C transposes)
+    unsigned long long *nan_dev = nullptr;
+    long long last_newton_iters = 0, last_newton_unconv = 0;
+    int last_poisson_iters = -1;
+    std::string last_error;
+    // device timing
+    bool timing = false;
+    std::vector<cudaEvent_t> evpool;
+    cudaEvent_t tot0 = nullptr, tot1 = nullptr;
+    double total_ms = 0.0, stage_ms[NSTAGE] = {};
+    long long timed_steps = 0;
+
+    template <typename T>
+    cudaError_t alloc(T **p, size_t n) {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        allocs.push_back(q);
+        *p = static_cast<T *>(q);
+        return cudaMemsetAsync(q, 0, std::max<size_t>(n, 1) * sizeof(T), s);
+    }
+    void release() {
+        for (cudaEvent_t e : evpool) cudaEventDestroy(e);
+        evpool.clear();
+        if (tot0) cudaEventDestroy(tot0);
+        if (tot1) cudaEventDestroy(tot1);
+        tot0 = tot1 = nullptr;
+        for (void *p : allocs) cudaFree(p);
+        allocs.clear();
+        if (s) cudaStreamDestroy(s);
+        s = nullptr;
+    }
+};
+
+namespace {
+
+int fail(f8_ctx *c, cudaError_t e, const char *where) {
+    if (c) c->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? F8_ERR_NOMEM : F8_ERR_CUDA;
+}
+
+#define API_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e__ = (call);                             \
+        if (e__ != cudaSuccess) return fail(ctx, e__, #call); \
+    } while (0)
+
+int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, int prec, int poisson) {
+    if (!g || !ph) return F8_ERR_ARG;
+    if (g->dim != 2 && g->dim != 3) return F8_ERR_ARG;
+    if (g->nx < 4 || g->ny < 4 || g->nz < 1) return F8_ERR_ARG;
+    if (g->dim == 2 && g->nz != 1) return F8_ERR_ARG;
+    if (g->dim == 3 && g->nz < 4) return F8_ERR_ARG;
+    if (!(g->lx > 0 && g->ly > 0 && g->lz > 0)) return F8_ERR_ARG;
+    if (g->bc_y != F8_BC_PERIODIC && g->bc_y != F8_BC_WALLS) return F8_ERR_ARG;
+    if (!is_pow2(g->nx) || !is_pow2(g->ny) || !is_pow2(g->nz)) return F8_ERR_ARG;  // spectral solves
+    if (g->nx > 1024 || g->ny > 1024 || g->nz > 1024) return F8_ERR_ARG;
+    if ((long)(g->nx + 2) * (g->ny + 2) * (g->nz + 2) > (1L << 31) / 8) return F8_ERR_ARG;
+    if (poisson != F8_POISSON_FFT && poisson != F8_POISSON_SOR) return F8_ERR_ARG;
+    if (prec != F8_FP64 && prec != F8_MIXED) return F8_ERR_ARG;
+    if (!(ph->dt > 0) || !(ph->re > 0) || !(ph->wi > 0)) return F8_ERR_ARG;
+    if (ph->newton_itrmax < 1 || ph->sor_itrmax < 1) return F8_ERR_ARG;
+    if (ncyl < 0 || (ncyl > 0 && !cy)) return F8_ERR_ARG;
+    return F8_OK;
+}
+
+void make_tw(int n, std::vector<double> &r, std::vector<double> &i) {
+    int h = std::max(1, n / 2);
+    r.assign(h, 1.0); i.assign(h, 0.0);
+    for (int t = 0; t < n / 2; ++t) {
+        double a = 2.0 * PI * t / n;
+        r[t] = std::cos(a);
+        i[t] = -std::sin(a);
+    }
+}
+
+int upload(f8_ctx *c, double **dst, const std::vector<double> &v) {
+    API_CUDA(c, c->alloc(dst, v.size()));
+    API_CUDA(c, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, c->s));
+    return F8_OK;
+}
+
+int setup(f8_ctx *c) {
+    const f8_grid &G = c->grid;
+    Dev &d = c->d;
+    Geo &g = d.g;
+    g.nx = G.nx; g.ny = G.ny; g.nz = G.nz;
+    g.sx = G.nx + 2; g.sy = G.ny + 2; g.sz = G.nz + 2;
+    g.dim = G.dim; g.walls = G.bc_y == F8_BC_WALLS;
+    g.dx = G.lx / G.nx; g.dy = G.ly / G.ny; g.dz = G.dim == 3 ? G.lz / G.nz : g.dx;
+    g.dt = c->phys.dt; g.uwall = G.uwall;
+    d.ph = Phys{c->phys.re, c->phys.wi, c->phys.beta, c->phys.lp2, c->phys.dt,
+                c->phys.newton_dc, c->phys.newton_eps, c->phys.newton_itrmax};
+    d.ncomp = G.dim == 3 ? 6 : 3;
+    d.cs = g.sx * g.sy * g.sz;
+    d.ni = g.nx * g.ny * g.nz;
+    API_CUDA(c, cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+    API_CUDA(c, init_kernels_fp64());
+    API_CUDA(c, cudaEventCreate(&c->tot0));
+    API_CUDA(c, cudaEventCreate(&c->tot1));
+    const size_t cs = d.cs, ni = d.ni;
+    for (double **p : {&d.U, &d.V, &d.W, &d.P, &d.Phi, &d.fpet, &d.Up, &d.Vp, &d.Wp, &d.Ua, &d.Va, &d.Wa})
+        API_CUDA(c, c->alloc(p, cs));
+    API_CUDA(c, c->alloc(&d.C, cs * d.ncomp));
+    API_CUDA(c, c->alloc(&d.Cn, cs * d.ncomp));
+    API_CUDA(c, c->alloc(&c->scratch_aos, cs * d.ncomp));
+    API_CUDA(c, c->alloc(&d.codes, ni));
+    for (double **p : {&d.Ax0, &d.Ay0, &d.Az0, &d.Tx0, &d.Ty0, &d.Tz0, &d.Fx, &d.Fy, &d.Fz, &d.Bx, &d.By, &d.Bz,
+                       &d.Q[0], &d.Q[1], &d.Q[2], &d.E})
+        API_CUDA(c, c->alloc(p, ni));
+    const size_t nxh = g.nx / 2 + 1;
+    const size_t nspec = 2 * nxh * (size_t)(g.ny + 2) * g.nz;
+    API_CUDA(c, c->alloc(&d.H, nspec));
+    API_CUDA(c, c->alloc(&d.H2, nspec));
+    API_CUDA(c, c->alloc(&d.red, 4096));
+    API_CUDA(c, c->alloc(&d.scal, 64));
+    API_CUDA(c, c->alloc(&d.flag, 4));
+    API_CUDA(c, c->alloc(&d.cnt, 1));
+    API_CUDA(c, c->alloc(&c->nan_dev, 1));
+    std::vector<double> tr, ti;
+    make_tw(g.nx, tr, ti);
+    if (int st = upload(c, &d.twx_r, tr)) return st;
+    if (int st = upload(c, &d.twx_i, ti)) return st;
+    make_tw(g.ny, tr, ti);
+    if (int st = upload(c, &d.twy_r, tr)) return st;
+    if (int st = upload(c, &d.twy_i, ti)) return st;
+    make_tw(g.nz, tr, ti);
+    if (int st = upload(c, &d.twz_r, tr)) return st;
+    if (int st = upload(c, &d.twz_i, ti)) return st;
+    // modified wavenumbers 2(1-cos(m 2pi/N))/d^2 (fenep.f90:1458-1460 with
+    // the angle step 2 pi/N, identical to (i-1)*dX in the reference's 2 pi box)
+    const double thx = 2 * PI / g.nx, thy = 2 * PI / g.ny, thz = 2 * PI / g.nz;
+    std::vector<double> kx2(nxh), ky2(g.ny), kz2(g.nz);
+    for (int i = 1; i <= (int)nxh; ++i) kx2[i - 1] = 2 * (1 - std::cos((i - 1) * thx)) / (g.dx * g.dx);
+    for (int j = 1; j <= g.ny; ++j) ky2[j - 1] = 2 * (1 - std::cos((j - 1) * thy)) / (g.dy * g.dy);
+    for (int k = 1; k <= g.nz; ++k) kz2[k - 1] = 2 * (1 - std::cos((k - 1) * thz)) / (g.dz * g.dz);
+    if (int st = upload(c, &d.kx2, kx2)) return st;
+    if (int st = upload(c, &d.ky2, ky2)) return st;
+    if (int st = upload(c, &d.kz2, kz2)) return st;
+    // IBM markers and the gather lists of the spreading kernel
+    d.ncyl = (int)c->cyl.size();
+    if (!c->cyl.empty()) {
+        if (std::fabs(g.dx - g.dy) > 1e-14 * g.dx || (g.dim == 3 && std::fabs(g.dx - g.dz) > 1e-14 * g.dx))
+            return F8_ERR_ARG;  // fenep.f90:1808-1810
+        c->mk = build_markers(c->cyl, g.dx, g.dim);
+        const int nm = (int)c->mk.size();
+        d.nm = nm;
+        std::vector<double> mx(nm), my(nm), mu(nm), mv(nm);
+        std::vector<int> mc(nm);
+        for (int m = 0; m < nm; ++m) { mx[m] = c->mk[m].x; my[m] = c->mk[m].y; mu[m] = c->mk[m].u; mv[m] = c->mk[m].v; mc[m] = c->mk[m].cyl; }
+        if (int st = upload(c, &d.mx, mx)) return st;
+        if (int st = upload(c, &d.my, my)) return st;
+        if (int st = upload(c, &d.mu, mu)) return st;
+        if (int st = upload(c, &d.mv, mv)) return st;
+        API_CUDA(c, c->alloc(&d.mcyl, nm));
+        API_CUDA(c, cudaMemcpyAsync(d.mcyl, mc.data(), nm * sizeof(int), cudaMemcpyHostToDevice, c->s));
+        const int ncomp = g.dim == 3 ? 3 : 2;
+        const int ncol = g.sx * g.sy;
+        for (int comp = 0; comp < 3; ++comp) {
+            API_CUDA(c, c->alloc(&d.Fc[comp], (size_t)nm * g.nz));
+            std::vector<int> off(ncol + 1, 0), idx;
+            std::vector<std::vector<int>> lists(ncol);
+            if (comp < ncomp)
+                for (int m = 0; m < nm; ++m) {
+                    int i0, j0;
+                    stencil_origin_h(comp, mx[m], my[m], g.dx, g.dy, i0, j0);
+                    for (int jj = j0; jj <= j0 + 2; ++jj)
+                        for (int ii = i0; ii <= i0 + 2; ++ii) {
+                            if (ii < 0 || ii >= g.sx || jj < 0 || jj >= g.sy) return F8_ERR_ARG;  // marker too close to the edge
+                            lists[ii + g.sx * jj].push_back(m);
+                        }
+                }
+            for (int q = 0; q < ncol; ++q) off[q + 1] = off[q] + (int)lists[q].size();
+            idx.reserve(off[ncol]);
+            for (int q = 0; q < ncol; ++q) idx.insert(idx.end(), lists[q].begin(), lists[q].end());
+            API_CUDA(c, c->alloc(&d.csr_off[comp], off.size()));
+            API_CUDA(c, cudaMemcpyAsync(d.csr_off[comp], off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, c->alloc(&d.csr_idx[comp], std::max<size_t>(idx.size(), 1)));
+            if (!idx.empty())
+                API_CUDA(c, cudaMemcpyAsync(d.csr_idx[comp], idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, c->s));
+        }
+        // the interpolation stencil reads k = n-1 .. n+1 and marker columns
+        // inside the halo box; validated above through the gather lists
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+int ensure_drag(f8_ctx *c, int nsteps) {
+    if (c->cyl.empty() || nsteps <= c->drag_cap) return F8_OK;
+    int cap = std::max(nsteps, 64);
+    double *p = nullptr;
+    API_CUDA(c, c->alloc(&p, (size_t)cap * c->cyl.size() * 3));
+    c->drag_dev = p;
+    c->drag_cap = cap;
+    return F8_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void f8_default_phys(f8_phys *ph) {
+    std::memset(ph, 0, sizeof(*ph));
+    ph->re = 1.0; ph->wi = 1.0; ph->beta = 1.0; ph->lp2 = 100.0; ph->dt = 1.0e-3;
+    ph->newton_dc = 1.0e-5; ph->newton_eps = 1.0e-6; ph->newton_itrmax = 10000;
+    ph->sor_omega = 1.8; ph->sor_eps = 1.0e-5; ph->sor_itrmax = 10000;
+    ph->ab2_start = 1;
+}
+
+int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *cy, int ncyl, int prec, int poisson) {
+    if (!out) return F8_ERR_ARG;
+    *out = nullptr;
+    int st = validate(g, ph, ncyl, cy, prec, poisson);
+    if (st) return st;
+    if (prec == F8_MIXED) return F8_ERR_UNSUPPORTED;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return F8_ERR_NO_DEVICE;
+    }
+    f8_ctx *c = new (std::nothrow) f8_ctx();
+    if (!c) return F8_ERR_NOMEM;
+    c->grid = *g; c->phys = *ph; c->precision = prec; c->poisson = poisson;
+    if (ncyl > 0) c->cyl.assign(cy, cy + ncyl);
+    st = setup(c);
+    if (st) {
+        c->release();
+        delete c;
+        return st;
+    }
+    *out = c;
+    return F8_OK;
+}
+
+int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
+    if (!c || !in || !in->u || !in->v || !in->p || !in->c || step0 < 0) return F8_ERR_ARG;
+    if (c->grid.dim == 3 && !in->w) return F8_ERR_ARG;
+    Dev &d = c->d;
+    const size_t cs = d.cs, ni = d.ni;
+    auto put = [&](double *dst, const double *src, size_t n) -> cudaError_t {
+        if (src) return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, c->s);
+        return cudaMemsetAsync(dst, 0, n * sizeof(double), c->s);
+    };
+    API_CUDA(c, put(d.U, in->u, cs));
+    API_CUDA(c, put(d.V, in->v, cs));
+    API_CUDA(c, put(d.W, c->grid.dim == 3 ? in->w : nullptr, cs));
+    API_CUDA(c, put(d.P, in->p, cs));
+    API_CUDA(c, put(d.Phi, in->phi, cs));
+    API_CUDA(c, put(c->scratch_aos, in->c, cs * d.ncomp));
+    API_CUDA(c, aos_to_soa(c->scratch_aos, d.C, d.ncomp, (int)cs, c->s));
+    API_CUDA(c, put(d.Ax0, in->ax0, ni)); API_CUDA(c, put(d.Ay0, in->ay0, ni)); API_CUDA(c, put(d.Az0, in->az0, ni));
+    API_CUDA(c, put(d.Tx0, in->tx0, ni)); API_CUDA(c, put(d.Ty0, in->ty0, ni)); API_CUDA(c, put(d.Tz0, in->tz0, ni));
+    API_CUDA(c, put(d.Fx, in->fx, ni)); API_CUDA(c, put(d.Fy, in->fy, ni)); API_CUDA(c, put(d.Fz, in->fz, ni));
+    // boundary values of the loaded state (init calls PBM, fenep.f90:139-143)
+    API_CUDA(c, bc_all_state_fp64(d, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    c->step = step0;
+    c->step0 = step0;
+    c->loaded = true;
+    return F8_OK;
+}
+
+int f8_step(f8_ctx *c, int nsteps, double *drag) {
+    if (!c || nsteps < 0) return F8_ERR_ARG;
+    if (!c->loaded) return F8_ERR_STATE;
+    if (nsteps == 0) return F8_OK;
+    if (int st = ensure_drag(c, nsteps)) return st;
+    Dev &d = c->d;
+    const int ncyl = (int)c->cyl.size();
+    API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
+    API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
+    const size_t per = NSTAGE + 1;
+    if (c->timing && c->evpool.size() < per * nsteps) {
+        size_t have = c->evpool.size();
+        c->evpool.resize(per * nsteps, nullptr);
+        for (size_t q = have; q < c->evpool.size(); ++q) API_CUDA(c, cudaEventCreate(&c->evpool[q]));
+    }
+    API_CUDA(c, cudaEventRecord(c->tot0, c->s));
+    int worst = F8_OK;
+    for (int s = 0; s < nsteps; ++s) {
+        StepOpts o{};
+        o.polymer = c->phys.beta != 1.0;
+        o.ab2_first = (c->step + 1 == 1) && c->phys.ab2_start;
+        o.ibm = ncyl > 0;
+        o.poisson = c->poisson;
+        o.sor_omega = c->phys.sor_omega; o.sor_eps = c->phys.sor_eps; o.sor_itrmax = c->phys.sor_itrmax;
+        o.ev = c->timing ? &c->evpool[per * s] : nullptr;
+        if (!o.polymer && s == 0) {
+            // beta == 1: C and T vanish (fenep.f90:2479-2485)
+            API_CUDA(c, cudaMemsetAsync(d.C, 0, (size_t)d.cs * d.ncomp * sizeof(double), c->s));
+        }
+        int sor_iters = -1;
+        double *dg = (ncyl && drag) ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
+        cudaError_t e = step_fp64(d, o, dg, &sor_iters, c->s);
+        if (e != cudaSuccess) return fail(c, e, "step");
+        c->last_poisson_iters = sor_iters;
+        if (c->poisson == F8_POISSON_SOR && sor_iters > c->phys.sor_itrmax) worst = std::max(worst, (int)F8_WARN_SOR);
+        c->step += 1;
+    }
+    API_CUDA(c, cudaEventRecord(c->tot1, c->s));
+    API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
+    StepCounters cnt{};
+    unsigned long long nan = 0;
+    API_CUDA(c, cudaMemcpyAsync(&cnt, d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaMemcpyAsync(&nan, c->nan_dev, sizeof(nan), cudaMemcpyDeviceToHost, c->s));
+    if (drag && ncyl)
+        API_CUDA(c, cudaMemcpyAsync(drag, c->drag_dev, (size_t)nsteps * ncyl * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    {
+        float ms = 0.f;
+        API_CUDA(c, cudaEventElapsedTime(&ms, c->tot0, c->tot1));
+        c->total_ms += ms;
+        c->timed_steps += nsteps;
+        if (c->timing)
+            for (int s2 = 0; s2 < nsteps; ++s2)
+                for (int q = 0; q < NSTAGE; ++q) {
+                    API_CUDA(c, cudaEventElapsedTime(&ms, c->evpool[per * s2 + q], c->evpool[per * s2 + q + 1]));
+                    c->stage_ms[q] += ms;
+                }
+    }
+    c->last_newton_iters = (long long)cnt.newton_iters;
+    c->last_newton_unconv = (long long)cnt.newton_unconverged;
+    if (nan) return F8_ERR_NAN;
+    if (cnt.newton_unconverged) worst = std::max(worst, (int)F8_WARN_NEWTON);
+    return worst;
+}
+
+int f8_store(f8_ctx *c, f8_fields *out) {
+    if (!c || !out) return F8_ERR_ARG;
+    Dev &d = c->d;
+    const size_t cs = d.cs, ni = d.ni;
+    auto get = [&](double *dst, const double *src, size_t n) -> cudaError_t {
+        if (!dst) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+    };
+    API_CUDA(c, get(out->u, d.U, cs));
+    API_CUDA(c, get(out->v, d.V, cs));
+    if (c->grid.dim == 3) API_CUDA(c, get(out->w, d.W, cs));
+    API_CUDA(c, get(out->p, d.P, cs));
+    API_CUDA(c, get(out->phi, d.Phi, cs));
+    if (out->c) {
+        API_CUDA(c, soa_to_aos(d.C, c->scratch_aos, d.ncomp, (int)cs, c->s));
+        API_CUDA(c, get(out->c, c->scratch_aos, cs * d.ncomp));
+    }
+    API_CUDA(c, get(out->ax0, d.Ax0, ni)); API_CUDA(c, get(out->ay0, d.Ay0, ni)); API_CUDA(c, get(out->az0, d.Az0, ni));
+    API_CUDA(c, get(out->tx0, d.Tx0, ni)); API_CUDA(c, get(out->ty0, d.Ty0, ni)); API_CUDA(c, get(out->tz0, d.Tz0, ni));
+    API_CUDA(c, get(out->fx, d.Fx, ni)); API_CUDA(c, get(out->fy, d.Fy, ni)); API_CUDA(c, get(out->fz, d.Fz, ni));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
+    if (!c || !dg) return F8_ERR_ARG;
+    const Geo &g = c->d.g;
+    const size_t cs = c->d.cs;
+    const int nc = c->d.ncomp;
+    std::vector<double> U(cs), V(cs), W(cs, 0.0), C(cs * nc);
+    f8_fields f{};
+    f.u = U.data(); f.v = V.data(); f.w = W.data(); f.c = C.data();
+    if (int st = f8_store(c, &f)) return st;
+    std::memset(dg, 0, sizeof(*dg));
+    dg->step = c->step;
+    const bool d3 = g.dim == 3;
+    auto h = [&](int i, int j, int k) { return (size_t)i + (size_t)g.sx * ((size_t)j + (size_t)g.sy * k); };
+    double ke = 0, tmin = 1e300, tmax = -1e300, tsum = 0, dmax = 0, umax = -1e300, vmax = -1e300, wmax = -1e300;
+    for (int k = 1; k <= g.nz; ++k)
+        for (int j = 1; j <= g.ny; ++j)
+            for (int i = 1; i <= g.nx; ++i) {
+                double ur = (U[h(i, j, k)] + U[h(i - 1, j, k)]) / 2.0, vr = (V[h(i, j, k)] + V[h(i, j - 1, k)]) / 2.0;
+                double wr = d3 ? (W[h(i, j, k)] + W[h(i, j, k - 1)]) / 2.0 : 0.0;
+                ke += ur * ur + vr * vr + wr * wr;
+                const double *cc = &C[nc * h(i, j, k)];
+                double tr = d3 ? cc[0] + cc[3] + cc[5] : cc[0] + cc[2];
+                tmin = std::min(tmin, tr); tmax = std::max(tmax, tr); tsum += tr;
+                double dv = (U[h(i, j, k)] - U[h(i - 1, j, k)]) / g.dx + (V[h(i, j, k)] - V[h(i, j - 1, k)]) / g.dy;
+                if (d3) dv += (W[h(i, j, k)] - W[h(i, j, k - 1)]) / g.dz;
+                dmax = std::max(dmax, std::fabs(dv));
+                if (std::isnan(ur) || std::isnan(vr) || std::isnan(wr)) dg->nan_found = 1;
+            }
+    for (size_t n = 0; n < cs; ++n) { umax = std::max(umax, U[n]); vmax = std::max(vmax, V[n]); if (d3) wmax = std::max(wmax, W[n]); }
+    const double N = (double)c->d.ni;
+    dg->ke = ke / 2.0 / N;
+    double cfl = std::max(umax * g.dt / g.dx, vmax * g.dt / g.dy);
+    if (d3) cfl = std::max(cfl, wmax * g.dt / g.dz);
+    dg->cfl = cfl * 6.0;
+    dg->trc_min = tmin; dg->trc_max = tmax; dg->trc_mean = tsum / N;
+    dg->div_max = dmax;
+    dg->newton_iters = c->last_newton_iters;
+    dg->newton_unconverged = c->last_newton_unconv;
+    dg->poisson_iters = c->last_poisson_iters;
+    return F8_OK;
+}
+
+int f8_markers(f8_ctx *c, int *n, double *xy) {
+    if (!c) return F8_ERR_ARG;
+    if (n) *n = (int)c->mk.size();
+    if (xy)
+        for (size_t m = 0; m < c->mk.size(); ++m) { xy[2 * m] = c->mk[m].x; xy[2 * m + 1] = c->mk[m].y; }
+    return F8_OK;
+}
+
+int f8_set_timing(f8_ctx *c, int enable) {
+    if (!c) return F8_ERR_ARG;
+    c->timing = enable != 0;
+    return F8_OK;
+}
+
+int f8_timing(f8_ctx *c, double *total_ms, double *stage_ms, long long *steps_timed) {
+    if (!c) return F8_ERR_ARG;
+    if (total_ms) *total_ms = c->total_ms;
+    if (stage_ms)
+        for (int q = 0; q < NSTAGE; ++q) stage_ms[q] = c->stage_ms[q];
+    if (steps_timed) *steps_timed = c->timed_steps;
+    return F8_OK;
+}
+
+int f8_timing_reset(f8_ctx *c) {
+    if (!c) return F8_ERR_ARG;
+    c->total_ms = 0.0;
+    for (int q = 0; q < NSTAGE; ++q) c->stage_ms[q] = 0.0;
+    c->timed_steps = 0;
+    return F8_OK;
+}
+
+const char *f8_strerror(int st) {
+    switch (st) {
+    case F8_OK: return "ok";
+    case F8_ERR_ARG: return "invalid argument";
+    case F8_ERR_STATE: return "call out of order (load before step)";
+    case F8_ERR_NOMEM: return "device allocation failed";
+    case F8_ERR_CUDA: return "CUDA runtime error";
+    case F8_ERR_NAN: return "NaN in the velocity field";
+    case F8_ERR_UNSUPPORTED: return "unsupported option";
+    case F8_ERR_NO_DEVICE: return "no CUDA device";
+    case F8_WARN_NEWTON: return "Newton iteration limit reached in some cells";
+    case F8_WARN_SOR: return "SOR iteration limit reached";
+    default: return "unknown status";
+    }
+}
+
+void f8_destroy(f8_ctx *c) {
+    if (!c) return;
+    c->release();
+    delete c;
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// f8_common.cuh — shared device definitions of the GB300 SMAC + FENE-P + IBM step.
+//
+// Device memory layout (structure of arrays, x fastest):
+//   halo scalar fields (U, V, W, P, Phi, Ua.., Up..): (NX+2)(NY+2)(NZ+2) values,
+//     index h(i,j,k) = i + SX*(j + SY*k), i in 0..NX+1 (the reference's
+//     (0:NX+1, 0:NY+1, 0:NZ+1) Fortran layout, fenep.f90:2424).
+//   C: NC separate halo fields (SoA) instead of the reference's component-fastest
+//     C(6, 0:NX+1, ...): a warp then reads 32 consecutive x of one component.
+//   interior fields (A0, T0, F, B, Q): NX*NY*NZ values, index q(i,j,k) =
+//     (i-1) + NX*((j-1) + NY*(k-1)).
+//   spectra: complex (re, im interleaved) [k][j][kx], kx in 0..NX/2.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace f8 {
+
+struct Geo {
+    int nx, ny, nz;      // cells
+    int sx, sy, sz;      // halo extents nx+2 ...
+    int dim;             // 2 or 3
+    int walls;           // y walls (1) or periodic (0)
+    double dx, dy, dz;
+    double dt;
+    double uwall;
+};
+
+__host__ __device__ inline int hix(const Geo &g, int i, int j, int k) { return i + g.sx * (j + g.sy * k); }
+__host__ __device__ inline int qix(const Geo &g, int i, int j, int k) { return (i - 1) + g.nx * ((j - 1) + g.ny * (k - 1)); }
+__host__ __device__ inline int wrapx(const Geo &g, int i) { return i < 1 ? i + g.nx : (i > g.nx ? i - g.nx : i); }
+__host__ __device__ inline int wrapy(const Geo &g, int j) { return j < 1 ? j + g.ny : (j > g.ny ? j - g.ny : j); }
+__host__ __device__ inline int wrapz(const Geo &g, int k) { return k < 1 ? k + g.nz : (k > g.nz ? k - g.nz : k); }
+
+// Physical parameters the kernels need (copied from f8_phys).
+struct Phys {
+    double re, wi, beta, lp2, dt;
+    double newton_dc, newton_eps;
+    int newton_itrmax;
+};
+
+// Boundary-condition kinds of the halo fill kernel.
+enum BcKind { BC_U = 0, BC_V = 1, BC_W = 2, BC_P = 3, BC_C = 4, BC_CODE = 5 };
+
+// Per-step device counters (status words read by the host after a step).
+struct StepCounters {
+    unsigned long long newton_iters;
+    unsigned long long newton_unconverged;
+    unsigned long long nan_cells;
+};
+
+}  // namespace f8
+
+#define F8_CUDA_RET(call)                          \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) return e_;          \
+    } while (0)

@@ -1,0 +1,65 @@
+// f8_kernels.h — device state and kernel launchers of the step (host-visible).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "f8_common.cuh"
+
+namespace f8 {
+
+// Device pointers of one context.  Field layouts are described in f8_common.cuh.
+struct Dev {
+    Geo g;
+    Phys ph;
+    int ncomp;           // 6 (3D) or 3 (2D)
+    int cs;              // elements of one halo field, SX*SY*SZ
+    int ni;              // interior cells NX*NY*NZ
+    // state (FP64)
+    double *U, *V, *W, *P, *Phi;
+    double *C, *Cn;      // ncomp SoA halo fields each
+    double *fpet;        // Peterlin factor f(C) on every halo cell
+    uint8_t *codes;      // interior: 2 bits per direction, chosen candidate - 1
+    double *Ax0, *Ay0, *Az0, *Tx0, *Ty0, *Tz0, *Fx, *Fy, *Fz;
+    // work
+    double *Up, *Vp, *Wp, *Ua, *Va, *Wa;   // halo
+    double *Bx, *By, *Bz;                  // interior
+    double *Q[3];                          // interior right-hand sides
+    double *E;                             // interior SOR residual
+    double *H, *H2;                        // spectral scratch
+    double *twx_r, *twx_i, *twy_r, *twy_i, *twz_r, *twz_i;
+    double *kx2, *ky2, *kz2;
+    // IBM
+    int nm;                                // markers per plane
+    int ncyl;
+    double *mx, *my, *mu, *mv;
+    int *mcyl;
+    double *Fc[3];                         // nm * nz each
+    int *csr_off[3], *csr_idx[3];          // per component over (SX*SY) columns
+    double *drag;                          // per step ncyl*3
+    // reductions
+    double *red;                           // scratch partial sums (>= 4096)
+    double *scal;                          // small scalar results
+    int *flag;                             // SOR convergence flag / iteration
+    StepCounters *cnt;
+};
+
+struct StepOpts {
+    bool polymer;      // beta != 1
+    bool ab2_first;    // this step copies A->A0, T->T0 first
+    bool ibm;
+    int poisson;       // F8_POISSON_FFT / SOR
+    double sor_omega, sor_eps;
+    int sor_itrmax;
+    cudaEvent_t *ev;   // NSTAGE+1 events recorded at the stage boundaries, or null
+};
+constexpr int NSTAGE = 7;
+
+// FP64 step (f8_step_fp64.cu).  Returns a cudaError_t of the launches; SOR
+// iteration count in *sor_iters.
+cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s);
+cudaError_t bc_all_state_fp64(Dev &d, cudaStream_t s);
+cudaError_t init_kernels_fp64();
+cudaError_t aos_to_soa(const double *aos, double *soa, int ncomp, int cs, cudaStream_t s);
+cudaError_t soa_to_aos(const double *soa, double *aos, int ncomp, int cs, cudaStream_t s);
+cudaError_t count_nonfinite(const double *a, int n, unsigned long long *out, cudaStream_t s);
+
+}  // namespace f8

@@ -1,0 +1,1243 @@
+// f8_step_fp64.cu — FP64 kernels of the SMAC + FENE-P + IBM step.
+//
+// Compiled with --fmad=false: every a*b+c stays two rounded operations, in the
+// order the reference writes them, so results can be compared with the CPU
+// oracle at the 1e-10 level (and are bit-identical wherever no
+// transcendental function is involved).  The cited lines are in
+// machapin/fortran8.
+#include <algorithm>
+#include <cstdio>
+#include "f8_common.cuh"
+#include "f8_fft.cuh"
+#include "f8_kernels.h"
+
+namespace f8 {
+
+namespace {
+
+constexpr double PI_D = 3.141592653589793238462643383279502884;
+
+// ---------------------------------------------------------------------------
+// Halo fill (PBM / C_PBM, fenep.f90:147-166; walls fenep_2d.f90:1098-1143).
+// Each halo cell takes its value from an interior cell after wrapping the
+// periodic directions, which is what the reference's plane-by-plane copies
+// produce.
+
+__host__ __device__ inline long halo_count(const Geo &g) {
+    return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
+}
+
+__device__ inline bool halo_cell(const Geo &g, long t, int &i, int &j, int &k) {
+    long nf = 2L * g.sy * g.sz;
+    if (t < nf) {
+        long r = t % ((long)g.sy * g.sz);
+        i = (t / ((long)g.sy * g.sz)) ? g.sx - 1 : 0;
+        j = (int)(r % g.sy); k = (int)(r / g.sy);
+        return true;
+    }
+    t -= nf;
+    nf = 2L * g.nx * g.sz;
+    if (t < nf) {
+        long r = t % ((long)g.nx * g.sz);
+        j = (t / ((long)g.nx * g.sz)) ? g.sy - 1 : 0;
+        i = 1 + (int)(r % g.nx); k = (int)(r / g.nx);
+        return true;
+    }
+    t -= nf;
+    nf = 2L * g.nx * g.ny;
+    if (t < nf) {
+        long r = t % ((long)g.nx * g.ny);
+        k = (t / ((long)g.nx * g.ny)) ? g.sz - 1 : 0;
+        i = 1 + (int)(r % g.nx); j = 1 + (int)(r / g.nx);
+        return true;
+    }
+    return false;
+}
+
+__device__ inline double halo_value(const Geo &g, const double *A, int kind, int i, int j, int k) {
+    const int ii = wrapx(g, i), kk = wrapz(g, k);
+    if (j >= 1 && j <= g.ny) {
+        if (g.walls && kind == BC_V && j == g.ny) return 0.0;
+        return A[hix(g, ii, j, kk)];
+    }
+    if (!g.walls) return A[hix(g, ii, wrapy(g, j), kk)];
+    const bool lo = j == 0;
+    switch (kind) {
+    case BC_U: return lo ? -A[hix(g, ii, 1, kk)] : 2 * g.uwall - A[hix(g, ii, g.ny, kk)];
+    case BC_W: return lo ? -A[hix(g, ii, 1, kk)] : -A[hix(g, ii, g.ny, kk)];
+    case BC_V: return 0.0;
+    case BC_P: return lo ? A[hix(g, ii, 1, kk)] : A[hix(g, ii, g.ny, kk)];
+    default:   return lo ? 2 * A[hix(g, ii, 1, kk)] - A[hix(g, ii, 2, kk)]
+                         : 2 * A[hix(g, ii, g.ny, kk)] - A[hix(g, ii, g.ny - 1, kk)];
+    }
+}
+
+__global__ void k_bc_scalar(double *A, Geo g, int kind) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (halo_cell(g, t, i, j, k)) {
+        A[hix(g, i, j, k)] = halo_value(g, A, kind, i, j, k);
+        return;
+    }
+    // V on the upper wall face (V(:,NB) = 0, fenep_2d.f90:1114)
+    if (kind == BC_V && g.walls) {
+        t -= halo_count(g);
+        if (t >= 0 && t < (long)g.nx * g.nz) {
+            i = 1 + (int)(t % g.nx); k = 1 + (int)(t / g.nx);
+            A[hix(g, i, g.ny, k)] = 0.0;
+        }
+    }
+}
+
+// Peterlin factor (fenep.f90:510-515, fenep_2d.f90:275-280).
+__device__ inline double peterlin(const double *x, int ncomp, double lp2) {
+    return ncomp == 6 ? (lp2 - 3) / (lp2 - x[0] - x[3] - x[5]) : (lp2 - 2) / (lp2 - x[0] - x[2]);
+}
+
+// Halo fill of the SoA conformation tensor plus the Peterlin factor of every
+// halo cell (the interior f is written by the polymer update).
+__global__ void k_bc_c_pet(double *C, double *fpet, Geo g, int ncomp, int cs, double lp2) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (!halo_cell(g, t, i, j, k)) return;
+    const int h = hix(g, i, j, k);
+    double x[6];
+    for (int m = 0; m < ncomp; ++m) {
+        x[m] = halo_value(g, C + (size_t)m * cs, BC_C, i, j, k);
+        C[(size_t)m * cs + h] = x[m];
+    }
+    fpet[h] = peterlin(x, ncomp, lp2);
+}
+
+// f on every cell (after a load, or when the polymer stage is skipped)
+__global__ void k_pet_all(const double *C, double *fpet, int ncomp, int cs, double lp2) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    double x[6];
+    for (int m = 0; m < ncomp; ++m) x[m] = C[(size_t)m * cs + h];
+    fpet[h] = peterlin(x, ncomp, lp2);
+}
+
+// ---------------------------------------------------------------------------
+// Polymer, 3D.  Eigen test (Vieta, fenep.f90:425-444) and candidate selection
+// (CpxCnx, fenep.f90:169-242).
+
+__device__ inline double vieta(const double *a) {
+    double a2 = -(a[0] + a[3] + a[5]);
+    double a1 = a[0] * a[3] + a[3] * a[5] + a[5] * a[0] - a[4] * a[4] - a[2] * a[2] - a[1] * a[1];
+    double a0 = -(a[0] * a[3] * a[5] + a[1] * a[4] * a[2] + a[1] * a[4] * a[2] - a[0] * a[4] * a[4]
+                  - a[1] * a[1] * a[5] - a[2] * a[3] * a[2]);
+    double p = a1 - (a2 * a2) / 3.0;
+    double q = a0 - a1 * a2 / 3.0 + 2.0 * (a2 * a2 * a2) / 27.0;
+    double qh = q / 2.0, p3 = p / 3.0;
+    double t = qh * qh + p3 * p3 * p3;
+    if (t >= 0.0) return -100.0;
+    const double two_pi_3 = 2.0 * PI_D / 3.0;
+    return 2.0 * sqrt(-p / 3.0) * cos(acos(3.0 * q / (2.0 * p) * sqrt(-3.0 / p)) / 3.0 + two_pi_3) - a2 / 3.0;
+}
+
+__device__ inline double nanmin2(double a, double b) {
+    if (isnan(a)) return b;
+    if (isnan(b)) return a;
+    return b < a ? b : a;
+}
+
+// maxloc(minlist, 1) over four values, NaN ignored, first maximum wins.
+__device__ inline int maxloc4(const double *m) {
+    int idx = 0; double best = 0; bool found = false;
+    for (int l = 0; l < 4; ++l) {
+        if (isnan(m[l])) continue;
+        if (!found || m[l] > best) { best = m[l]; idx = l; found = true; }
+    }
+    return found ? idx + 1 : 1;
+}
+
+// candidate faces of fenep.f90:179-184 (idx 1..3), or the cell value (idx 4)
+__device__ inline double face_p(int idx, double cm, double c0, double cp) {
+    switch (idx) {
+    case 1: return c0 * 3 / 2 - cp / 2;
+    case 2: return cm / 2 + c0 / 2;
+    case 3: return cm / 4 + c0 - cp / 4;
+    default: return c0;
+    }
+}
+__device__ inline double face_n(int idx, double cm, double c0, double cp) {
+    switch (idx) {
+    case 1: return c0 / 2 + cp / 2;
+    case 2: return -cm / 2 + c0 * 3 / 2;
+    case 3: return -cm / 4 + c0 + cp / 4;
+    default: return c0;
+    }
+}
+
+__device__ inline int select3(const double *cm, const double *c0, const double *cp) {
+    double minlist[4];
+    for (int l = 1; l <= 3; ++l) {
+        double pt[6], nt[6];
+        for (int m = 0; m < 6; ++m) {
+            pt[m] = face_p(l, cm[m], c0[m], cp[m]);
+            nt[m] = face_n(l, cm[m], c0[m], cp[m]);
+        }
+        minlist[l - 1] = nanmin2(vieta(pt), vieta(nt));
+    }
+    minlist[3] = 0.0;
+    return maxloc4(minlist);
+}
+
+__global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    double c0[6], cm[6], cp[6];
+    const int h = hix(g, i, j, k);
+    for (int m = 0; m < 6; ++m) c0[m] = C[(size_t)m * cs + h];
+    const int off[3] = {1, g.sx, g.sx * g.sy};
+    int code = 0;
+    for (int d = 0; d < 3; ++d) {
+        for (int m = 0; m < 6; ++m) {
+            cm[m] = C[(size_t)m * cs + h - off[d]];
+            cp[m] = C[(size_t)m * cs + h + off[d]];
+        }
+        code |= (select3(cm, c0, cp) - 1) << (2 * d);
+    }
+    codes[qix(g, i, j, k)] = (uint8_t)code;
+}
+
+// fenep.f90:588-605
+__device__ inline void lyap_func3(const double A0[3][3], const double *b, const double *x, double *l, double lp2,
+                                  double dt, double wi) {
+    double A[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) A[r][q] = A0[r][q];
+    double fx = (lp2 - 3) / (lp2 - x[0] - x[3] - x[5]);
+    double dd = (1.0 + fx * dt / wi) / 2.0;
+    A[0][0] = A[0][0] + dd;
+    A[1][1] = A[1][1] + dd;
+    A[2][2] = A[2][2] + dd;
+    l[0] = (A[0][0] + A[0][0]) * x[0] + A[0][1] * x[1] + A[0][2] * x[2] + A[0][1] * x[1] + A[0][2] * x[2] - b[0];
+    l[1] = A[1][0] * x[0] + (A[1][1] + A[0][0]) * x[1] + A[1][2] * x[2] + A[0][1] * x[3] + A[0][2] * x[4] - b[1];
+    l[2] = A[2][0] * x[0] + A[2][1] * x[1] + (A[2][2] + A[0][0]) * x[2] + A[0][1] * x[4] + A[0][2] * x[5] - b[2];
+    l[3] = A[1][0] * x[1] + A[1][0] * x[1] + (A[1][1] + A[1][1]) * x[3] + A[1][2] * x[4] + A[1][2] * x[4] - b[3];
+    l[4] = A[1][0] * x[2] + A[2][0] * x[1] + A[2][1] * x[3] + (A[2][2] + A[1][1]) * x[4] + A[1][2] * x[5] - b[4];
+    l[5] = A[2][0] * x[2] + A[2][1] * x[4] + A[2][0] * x[2] + A[2][1] * x[4] + (A[2][2] + A[2][2]) * x[5] - b[5];
+}
+
+// Gauss-Jordan with partial pivoting (fenep.f90:608-643)
+template <int N>
+__device__ inline void gauss(double (&Ah)[N][N + 1], double *x) {
+    for (int k = 0; k < N; ++k) {
+        int maxidx = k; double maxabs = fabs(Ah[k][k]);
+        for (int r = k + 1; r < N; ++r) {
+            double a = fabs(Ah[r][k]);
+            if (a > maxabs) { maxabs = a; maxidx = r; }
+        }
+        if (maxabs == 0.0) {
+            for (int r = 0; r < N; ++r) Ah[r][N] = 0.0;
+            break;
+        }
+        if (k != maxidx)
+            for (int q = k; q <= N; ++q) { double tmp = Ah[k][q]; Ah[k][q] = Ah[maxidx][q]; Ah[maxidx][q] = tmp; }
+        double piv = Ah[k][k];
+        for (int q = k + 1; q <= N; ++q) Ah[k][q] = Ah[k][q] / piv;
+        Ah[k][k] = 1.0;
+        for (int r = 0; r < N; ++r) {
+            if (r == k) continue;
+            double f = Ah[r][k];
+            for (int q = k + 1; q <= N; ++q) Ah[r][q] = Ah[r][q] - f * Ah[k][q];
+            Ah[r][k] = 0.0;
+        }
+    }
+    for (int r = 0; r < N; ++r) x[r] = Ah[r][N];
+}
+
+__device__ inline void warp_count(unsigned long long v, unsigned long long *dst) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+// Cstar (fenep.f90:464-507) + Lyapunov Newton (fenep.f90:518-585) for one
+// cell.  The face states Cp/Cn of the three cells along each direction are
+// rebuilt from their selection codes, so no face arrays are stored.
+__global__ void __launch_bounds__(128) k_polymer_update3(const double *__restrict__ C, double *__restrict__ Cn,
+                                                         double *__restrict__ fpet, const uint8_t *__restrict__ codes,
+                                                         const double *__restrict__ U, const double *__restrict__ V,
+                                                         const double *__restrict__ W, Geo g, Phys ph, int cs,
+                                                         StepCounters *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    const bool active = i <= g.nx && j <= g.ny;
+    unsigned long long my_itr = 0, my_unconv = 0;
+    if (active) {
+        const int h = hix(g, i, j, k);
+        const double dt = ph.dt, dX = g.dx, dY = g.dy, dZ = g.dz;
+        // selection codes of the cell and its neighbours; wall ghost rows use
+        // the cell value (their faces are multiplied by zero in Cstar)
+        const int cself = codes[qix(g, i, j, k)];
+        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
+        const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
+        int cym, cyp;
+        int jm = j - 1, jp = j + 1;
+        bool ym_ghost = false, yp_ghost = false;
+        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
+        cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
+        cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
+        // centres of the neighbour cells along each direction (wrapped)
+        const int xm = wrapx(g, i - 1), xp = wrapx(g, i + 1);
+        const int zm = wrapz(g, k - 1), zp = wrapz(g, k + 1);
+        const int hxm = hix(g, xm, j, k), hxp = hix(g, xp, j, k);
+        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+        const int hzm = hix(g, i, j, zm), hzp = hix(g, i, j, zp);
+        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+
+        double u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
+        double v1 = V[hix(g, i, j - 1, k)], v2 = V[h];
+        double w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
+        double s1 = (-u2 + fabs(u2)) * dt / (2 * dX);
+        double s2 = 1.0 / 6 + (-u2 - fabs(u2)) * dt / (2 * dX);
+        double s3 = 1.0 / 6 + (u1 - fabs(u1)) * dt / (2 * dX);
+        double s4 = (u1 + fabs(u1)) * dt / (2 * dX);
+        double s5 = (-v2 + fabs(v2)) * dt / (2 * dY);
+        double s6 = 1.0 / 6 + (-v2 - fabs(v2)) * dt / (2 * dY);
+        double s7 = 1.0 / 6 + (v1 - fabs(v1)) * dt / (2 * dY);
+        double s8 = (v1 + fabs(v1)) * dt / (2 * dY);
+        double s9 = (-w2 + fabs(w2)) * dt / (2 * dZ);
+        double s10 = 1.0 / 6 + (-w2 - fabs(w2)) * dt / (2 * dZ);
+        double s11 = 1.0 / 6 + (w1 - fabs(w1)) * dt / (2 * dZ);
+        double s12 = (w1 + fabs(w1)) * dt / (2 * dZ);
+
+        double b[6], x[6];
+        for (int m = 0; m < 6; ++m) {
+            const double *Cm = C + (size_t)m * cs;
+            const double c0 = Cm[h];
+            // x
+            double pxm = face_p(isx, Cm[h - ox], c0, Cm[h + ox]);
+            double nxp = face_n(isx, Cm[h - ox], c0, Cm[h + ox]);
+            double pxp = face_p(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+            double nxm = face_n(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            // y
+            double pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
+            double nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
+            double pyp = yp_ghost ? Cm[hyp] : face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+            double nym = ym_ghost ? Cm[hym] : face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            // z
+            double pzm = face_p(isz, Cm[h - oz], c0, Cm[h + oz]);
+            double nzp = face_n(isz, Cm[h - oz], c0, Cm[h + oz]);
+            double pzp = face_p(czp + 1, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
+            double nzm = face_n(czm + 1, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
+            b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp
+                   + s11 * pzm + s9 * pzp + s12 * nzm + s10 * nzp;
+            x[m] = c0;
+        }
+        const double wi = ph.wi;
+        b[0] = b[0] + dt / wi;
+        b[3] = b[3] + dt / wi;
+        b[5] = b[5] + dt / wi;
+        auto u = [&](int a, int bb, int cc) { return U[hix(g, a, bb, cc)]; };
+        auto v = [&](int a, int bb, int cc) { return V[hix(g, a, bb, cc)]; };
+        auto w = [&](int a, int bb, int cc) { return W[hix(g, a, bb, cc)]; };
+        double A0[3][3];
+        A0[0][0] = -dt * (-u(i - 1, j, k) + u(i, j, k)) / dX;
+        A0[0][1] = -dt * (-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) / (4 * dX);
+        A0[0][2] = -dt * (-w(i - 1, j, k - 1) + w(i + 1, j, k - 1) - w(i - 1, j, k) + w(i + 1, j, k)) / (4 * dX);
+        A0[1][0] = -dt * (-u(i - 1, j - 1, k) - u(i, j - 1, k) + u(i - 1, j + 1, k) + u(i, j + 1, k)) / (4 * dY);
+        A0[1][1] = -dt * (-v(i, j - 1, k) + v(i, j, k)) / dY;
+        A0[1][2] = -dt * (-w(i, j - 1, k - 1) + w(i, j + 1, k - 1) - w(i, j - 1, k) + w(i, j + 1, k)) / (4 * dY);
+        A0[2][0] = -dt * (-u(i - 1, j, k - 1) - u(i, j, k - 1) + u(i - 1, j, k + 1) + u(i, j, k + 1)) / (4 * dZ);
+        A0[2][1] = -dt * (-v(i, j - 1, k - 1) - v(i, j, k - 1) + v(i, j - 1, k + 1) + v(i, j, k + 1)) / (4 * dZ);
+        A0[2][2] = -dt * (-w(i, j, k - 1) + w(i, j, k)) / dZ;
+        double AT[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) AT[r][q] = A0[q][r];
+        const double dc = ph.newton_dc, eps = ph.newton_eps;
+        int itr;
+        for (itr = 1; itr <= ph.newton_itrmax; ++itr) {
+            double Ah[6][7], x1[6], x2[6], l1[6], l2[6], l[6], r[6];
+            for (int col = 0; col < 6; ++col) {
+                for (int m = 0; m < 6; ++m) { x1[m] = x[m]; x2[m] = x[m]; }
+                x1[col] = x1[col] + dc;
+                x2[col] = x2[col] - dc;
+                lyap_func3(AT, b, x1, l1, ph.lp2, dt, wi);
+                lyap_func3(AT, b, x2, l2, ph.lp2, dt, wi);
+                for (int row = 0; row < 6; ++row) Ah[row][col] = (l1[row] - l2[row]) / (2.0 * dc);
+            }
+            lyap_func3(AT, b, x, l, ph.lp2, dt, wi);
+            for (int row = 0; row < 6; ++row) Ah[row][6] = l[row];
+            gauss<6>(Ah, r);
+            for (int m = 0; m < 6; ++m) x[m] = x[m] - r[m];
+            double sr = 0, sx = 0;
+            for (int m = 0; m < 6; ++m) sr = sr + r[m] * r[m];
+            for (int m = 0; m < 6; ++m) sx = sx + x[m] * x[m];
+            if (sqrt(sr / sx) < eps) break;
+        }
+        my_itr = (unsigned long long)itr;
+        my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+        for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
+        fpet[h] = (ph.lp2 - 3) / (ph.lp2 - x[0] - x[3] - x[5]);
+    }
+    const int lane_flat = threadIdx.x + blockDim.x * threadIdx.y;
+    (void)lane_flat;
+    unsigned long long a = my_itr, b2 = my_unconv;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b2 += __shfl_down_sync(0xffffffffu, b2, o);
+    }
+    if (((threadIdx.x + blockDim.x * threadIdx.y) & 31) == 0) {
+        if (a) atomicAdd(&cnt->newton_iters, a);
+        if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Polymer, 2D (fenep_2d.f90:138-393): closed-form 2x2 eigenvalues, the "last
+// candidate >= running best" rule, Cstar with 1/4 weights, 3-unknown Newton.
+
+__device__ inline void eig2(const double *a, double &re1, double &re2) {
+    double d = (a[0] - a[2]) * (a[0] - a[2]) + 4.0 * (a[1] * a[1]);
+    double s = sqrt(d);
+    re1 = (a[0] + a[2] + s) * 0.5;
+    re2 = (a[0] + a[2] - s) * 0.5;
+}
+
+// returns the reference's index (0 = none qualified -> cell value)
+__device__ inline int select2(const double *cm, const double *c0, const double *cp) {
+    int index = 0; double mintemp = 0.0;
+    for (int l = 1; l <= 3; ++l) {
+        double pt[3], nt[3], e[4];
+        for (int m = 0; m < 3; ++m) {
+            pt[m] = face_p(l, cm[m], c0[m], cp[m]);
+            nt[m] = face_n(l, cm[m], c0[m], cp[m]);
+        }
+        eig2(pt, e[0], e[1]);
+        eig2(nt, e[2], e[3]);
+        double mv = e[0];
+        bool found = !isnan(mv);
+        for (int q = 1; q < 4; ++q) {
+            if (isnan(e[q])) continue;
+            if (!found || e[q] < mv) { mv = e[q]; found = true; }
+        }
+        if (found && mv >= mintemp) { index = l; mintemp = mv; }
+    }
+    return index;
+}
+
+__global__ void k_polymer_codes2(const double *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int k = 1;
+    double c0[3], cm[3], cp[3];
+    const int h = hix(g, i, j, k);
+    for (int m = 0; m < 3; ++m) c0[m] = C[(size_t)m * cs + h];
+    const int off[2] = {1, g.sx};
+    int code = 0;
+    for (int d = 0; d < 2; ++d) {
+        for (int m = 0; m < 3; ++m) {
+            cm[m] = C[(size_t)m * cs + h - off[d]];
+            cp[m] = C[(size_t)m * cs + h + off[d]];
+        }
+        int idx = select2(cm, c0, cp);   // 0..3; 0 -> cell value (stored as 3 = "4")
+        code |= (idx == 0 ? 3 : idx - 1) << (2 * d);
+    }
+    codes[qix(g, i, j, k)] = (uint8_t)code;
+}
+
+__device__ inline void lyap_func2(const double A0[2][2], const double *b, const double *x, double *l, double lp2,
+                                  double dt, double wi) {
+    double A[2][2] = {{A0[0][0], A0[0][1]}, {A0[1][0], A0[1][1]}};
+    double fx = (lp2 - 2) / (lp2 - x[0] - x[2]);
+    double dd = (1.0 + fx * dt / wi) / 2.0;
+    A[0][0] = A[0][0] + dd;
+    A[1][1] = A[1][1] + dd;
+    l[0] = (A[0][0] + A[0][0]) * x[0] + A[0][1] * x[1] + A[0][1] * x[1] - b[0];
+    l[1] = A[1][0] * x[0] + (A[1][1] + A[0][0]) * x[1] + A[0][1] * x[2] - b[1];
+    l[2] = A[1][0] * x[1] + A[1][0] * x[1] + (A[1][1] + A[1][1]) * x[2] - b[2];
+}
+
+__global__ void k_polymer_update2(const double *__restrict__ C, double *__restrict__ Cn, double *__restrict__ fpet,
+                                  const uint8_t *__restrict__ codes, const double *__restrict__ U,
+                                  const double *__restrict__ V, Geo g, Phys ph, int cs, StepCounters *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = 1;
+    const bool active = i <= g.nx && j <= g.ny;
+    unsigned long long my_itr = 0, my_unconv = 0;
+    if (active) {
+        const int h = hix(g, i, j, k);
+        const double dt = ph.dt, dX = g.dx, dY = g.dy;
+        const int cself = codes[qix(g, i, j, k)];
+        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
+        int jm = j - 1, jp = j + 1;
+        bool ym_ghost = false, yp_ghost = false;
+        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
+        const int cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
+        const int cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1;
+        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+        const int ox = 1, oy = g.sx;
+        double u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
+        double v1 = V[hix(g, i, j - 1, k)], v2 = V[h];
+        double s1 = (-u2 + fabs(u2)) * dt / (2 * dX);
+        double s2 = 1.0 / 4 + (-u2 - fabs(u2)) * dt / (2 * dX);
+        double s3 = 1.0 / 4 + (u1 - fabs(u1)) * dt / (2 * dX);
+        double s4 = (u1 + fabs(u1)) * dt / (2 * dX);
+        double s5 = (-v2 + fabs(v2)) * dt / (2 * dY);
+        double s6 = 1.0 / 4 + (-v2 - fabs(v2)) * dt / (2 * dY);
+        double s7 = 1.0 / 4 + (v1 - fabs(v1)) * dt / (2 * dY);
+        double s8 = (v1 + fabs(v1)) * dt / (2 * dY);
+        double b[3], x[3];
+        for (int m = 0; m < 3; ++m) {
+            const double *Cm = C + (size_t)m * cs;
+            const double c0 = Cm[h];
+            double pxm = face_p(isx, Cm[h - ox], c0, Cm[h + ox]);
+            double nxp = face_n(isx, Cm[h - ox], c0, Cm[h + ox]);
+            double pxp = face_p(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+            double nxm = face_n(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            double pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
+            double nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
+            double pyp = yp_ghost ? Cm[hyp] : face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+            double nym = ym_ghost ? Cm[hym] : face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp;
+            x[m] = c0;
+        }
+        const double wi = ph.wi;
+        b[0] = b[0] + dt / wi;
+        b[2] = b[2] + dt / wi;
+        auto u = [&](int a, int bb) { return U[hix(g, a, bb, k)]; };
+        auto v = [&](int a, int bb) { return V[hix(g, a, bb, k)]; };
+        double A0[2][2];
+        A0[0][0] = -dt * (-u(i - 1, j) + u(i, j)) / dX;
+        A0[0][1] = -dt * (-v(i - 1, j - 1) + v(i + 1, j - 1) - v(i - 1, j) + v(i + 1, j)) / (4 * dX);
+        A0[1][0] = -dt * (-u(i - 1, j - 1) - u(i, j - 1) + u(i - 1, j + 1) + u(i, j + 1)) / (4 * dY);
+        A0[1][1] = -dt * (-v(i, j - 1) + v(i, j)) / dY;
+        double AT[2][2] = {{A0[0][0], A0[1][0]}, {A0[0][1], A0[1][1]}};
+        const double dc = ph.newton_dc, eps = ph.newton_eps;
+        int itr;
+        for (itr = 1; itr <= ph.newton_itrmax; ++itr) {
+            double Ah[3][4], x1[3], x2[3], l1[3], l2[3], l[3], r[3];
+            for (int col = 0; col < 3; ++col) {
+                for (int m = 0; m < 3; ++m) { x1[m] = x[m]; x2[m] = x[m]; }
+                x1[col] = x1[col] + dc;
+                x2[col] = x2[col] - dc;
+                lyap_func2(AT, b, x1, l1, ph.lp2, dt, wi);
+                lyap_func2(AT, b, x2, l2, ph.lp2, dt, wi);
+                for (int row = 0; row < 3; ++row) Ah[row][col] = (l1[row] - l2[row]) / (2.0 * dc);
+            }
+            lyap_func2(AT, b, x, l, ph.lp2, dt, wi);
+            for (int row = 0; row < 3; ++row) Ah[row][3] = l[row];
+            gauss<3>(Ah, r);
+            for (int m = 0; m < 3; ++m) x[m] = x[m] - r[m];
+            double sr = 0, sx = 0;
+            for (int m = 0; m < 3; ++m) sr = sr + r[m] * r[m];
+            for (int m = 0; m < 3; ++m) sx = sx + x[m] * x[m];
+            if (sqrt(sr / sx) < eps) break;
+        }
+        my_itr = (unsigned long long)itr;
+        my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+        for (int m = 0; m < 3; ++m) Cn[(size_t)m * cs + h] = x[m];
+        fpet[h] = (ph.lp2 - 2) / (ph.lp2 - x[0] - x[2]);
+    }
+    unsigned long long a = my_itr, b2 = my_unconv;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b2 += __shfl_down_sync(0xffffffffu, b2, o);
+    }
+    if (((threadIdx.x + blockDim.x * threadIdx.y) & 31) == 0) {
+        if (a) atomicAdd(&cnt->newton_iters, a);
+        if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Momentum: polymer_stress (fenep.f90:645-691), convection (694-734), viscous
+// (736-770) and the predictor right-hand side: the CN/AB2 Q of fft_navier
+// (fenep.f90:1469-1474) or the explicit Ua of ibm_preliminary (1997-2010, plus
+// dt*F as in fenep_2d.f90:1678).  The AB2/trapezoid history is rotated in the
+// same pass (fenep.f90:1521-1526).
+struct MomArgs {
+    const double *U, *V, *W, *P, *C, *fpet;
+    double *Ax0, *Ay0, *Az0, *Tx0, *Ty0, *Tz0;
+    const double *Fx, *Fy, *Fz;
+    double *out[3];     // Q (interior) or Ua (halo)
+    double *B[3];       // B (interior), IBM only
+    int cs;
+    int polymer, ab2_first, ibm;
+    double coef_t;      // (1-beta)/(Re Wi)
+    double vis;         // beta/Re
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_momentum(MomArgs a, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const double dX = g.dx, dY = g.dy, dZ = g.dz, dt = g.dt;
+    const double *U = a.U, *V = a.V, *W = a.W;
+    auto u = [&](int x, int y, int z) { return U[hix(g, x, y, z)]; };
+    auto v = [&](int x, int y, int z) { return V[hix(g, x, y, z)]; };
+    auto w = [&](int x, int y, int z) { return W[hix(g, x, y, z)]; };
+    const int o = qix(g, i, j, k);
+    const int h = hix(g, i, j, k);
+    // polymer stress
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    if (a.polymer) {
+        const int cs = a.cs;
+        const double *C = a.C, *fp = a.fpet;
+        if (DIM == 3) {
+            const double E[6] = {1.0, 0.0, 0.0, 1.0, 0.0, 1.0};
+            auto c0 = [&](int m, int x, int y, int z) {
+                int hh = hix(g, x, y, z);
+                return fp[hh] * C[(size_t)(m - 1) * cs + hh] - E[m - 1];
+            };
+            double sx = (-c0(1, i, j, k) + c0(1, i + 1, j, k)) / dX
+                      + (-c0(2, i, j - 1, k) - c0(2, i + 1, j - 1, k) + c0(2, i, j + 1, k) + c0(2, i + 1, j + 1, k)) / (4 * dY)
+                      + (-c0(3, i, j, k - 1) - c0(3, i + 1, j, k - 1) + c0(3, i, j, k + 1) + c0(3, i + 1, j, k + 1)) / (4 * dZ);
+            double sy = (-c0(2, i - 1, j, k) + c0(2, i + 1, j, k) - c0(2, i - 1, j + 1, k) + c0(2, i + 1, j + 1, k)) / (4 * dX)
+                      + (-c0(4, i, j, k) + c0(4, i, j + 1, k)) / dY
+                      + (-c0(5, i, j, k - 1) - c0(5, i, j + 1, k - 1) + c0(5, i, j, k + 1) + c0(5, i, j + 1, k + 1)) / (4 * dZ);
+            double sz = (-c0(3, i - 1, j, k) + c0(3, i + 1, j, k) - c0(3, i - 1, j, k + 1) + c0(3, i + 1, j, k + 1)) / (4 * dX)
+                      + (-c0(5, i, j - 1, k) + c0(5, i, j + 1, k) - c0(5, i, j - 1, k + 1) + c0(5, i, j + 1, k + 1)) / (4 * dY)
+                      + (-c0(6, i, j, k) + c0(6, i, j, k + 1)) / dZ;
+            tx = a.coef_t * sx; ty = a.coef_t * sy; tz = a.coef_t * sz;
+        } else {
+            const double E[3] = {1.0, 0.0, 1.0};
+            auto c0 = [&](int m, int x, int y) {
+                int hh = hix(g, x, y, k);
+                return fp[hh] * C[(size_t)(m - 1) * cs + hh] - E[m - 1];
+            };
+            double sx = (-c0(1, i, j) + c0(1, i + 1, j)) / dX
+                      + (-c0(2, i, j - 1) - c0(2, i + 1, j - 1) + c0(2, i, j + 1) + c0(2, i + 1, j + 1)) / (4 * dY);
+            double sy = (-c0(2, i - 1, j) + c0(2, i + 1, j) - c0(2, i - 1, j + 1) + c0(2, i + 1, j + 1)) / (4 * dX)
+                      + (-c0(3, i, j) + c0(3, i, j + 1)) / dY;
+            tx = a.coef_t * sx; ty = a.coef_t * sy;
+        }
+    }
+    // convection and viscous terms
+    double t1 = (u(i - 1, j, k) + u(i, j, k)) / 2, t2 = (u(i, j, k) + u(i + 1, j, k)) / 2;
+    double ax = (-(t1 * t1) + t2 * t2) / dX
+              + (-(v(i, j - 1, k) + v(i + 1, j - 1, k)) / 2 * (u(i, j - 1, k) + u(i, j, k)) / 2
+                 + (v(i, j, k) + v(i + 1, j, k)) / 2 * (u(i, j, k) + u(i, j + 1, k)) / 2) / dY;
+    double t3 = (v(i, j - 1, k) + v(i, j, k)) / 2, t4 = (v(i, j, k) + v(i, j + 1, k)) / 2;
+    double ay = (-(u(i - 1, j, k) + u(i - 1, j + 1, k)) / 2 * (v(i - 1, j, k) + v(i, j, k)) / 2
+                 + (u(i, j, k) + u(i, j + 1, k)) / 2 * (v(i, j, k) + v(i + 1, j, k)) / 2) / dX
+              + (-(t3 * t3) + t4 * t4) / dY;
+    double bx = (u(i - 1, j, k) - 2 * u(i, j, k) + u(i + 1, j, k)) / (dX * dX)
+              + (u(i, j - 1, k) - 2 * u(i, j, k) + u(i, j + 1, k)) / (dY * dY);
+    double by = (v(i - 1, j, k) - 2 * v(i, j, k) + v(i + 1, j, k)) / (dX * dX)
+              + (v(i, j - 1, k) - 2 * v(i, j, k) + v(i, j + 1, k)) / (dY * dY);
+    double az = 0, bz = 0;
+    if (DIM == 3) {
+        ax = ax + (-(w(i, j, k - 1) + w(i + 1, j, k - 1)) / 2 * (u(i, j, k - 1) + u(i, j, k)) / 2
+                   + (w(i, j, k) + w(i + 1, j, k)) / 2 * (u(i, j, k) + u(i, j, k + 1)) / 2) / dZ;
+        ay = ay + (-(w(i, j, k - 1) + w(i, j + 1, k - 1)) / 2 * (v(i, j, k - 1) + v(i, j, k)) / 2
+                   + (w(i, j, k) + w(i, j + 1, k)) / 2 * (v(i, j, k) + v(i, j, k + 1)) / 2) / dZ;
+        double t5 = (w(i, j, k - 1) + w(i, j, k)) / 2, t6 = (w(i, j, k) + w(i, j, k + 1)) / 2;
+        az = (-(u(i - 1, j, k) + u(i - 1, j, k + 1)) / 2 * (w(i - 1, j, k) + w(i, j, k)) / 2
+              + (u(i, j, k) + u(i, j, k + 1)) / 2 * (w(i, j, k) + w(i + 1, j, k)) / 2) / dX
+           + (-(v(i, j - 1, k) + v(i, j - 1, k + 1)) / 2 * (w(i, j - 1, k) + w(i, j, k)) / 2
+              + (v(i, j, k) + v(i, j, k + 1)) / 2 * (w(i, j, k) + w(i, j + 1, k)) / 2) / dY
+           + (-(t5 * t5) + t6 * t6) / dZ;
+        bx = bx + (u(i, j, k - 1) - 2 * u(i, j, k) + u(i, j, k + 1)) / (dZ * dZ);
+        by = by + (v(i, j, k - 1) - 2 * v(i, j, k) + v(i, j, k + 1)) / (dZ * dZ);
+        bz = (w(i - 1, j, k) - 2 * w(i, j, k) + w(i + 1, j, k)) / (dX * dX)
+           + (w(i, j - 1, k) - 2 * w(i, j, k) + w(i, j + 1, k)) / (dY * dY)
+           + (w(i, j, k - 1) - 2 * w(i, j, k) + w(i, j, k + 1)) / (dZ * dZ);
+    }
+    const double A[3] = {-ax, -ay, -az};
+    const double B[3] = {a.vis * bx, a.vis * by, a.vis * bz};
+    const double T[3] = {tx, ty, tz};
+    double *A0p[3] = {a.Ax0, a.Ay0, a.Az0};
+    double *T0p[3] = {a.Tx0, a.Ty0, a.Tz0};
+    const double *Fp[3] = {a.Fx, a.Fy, a.Fz};
+    const double *Us[3] = {U, V, W};
+    const double d[3] = {dX, dY, dZ};
+    const int hp[3] = {hix(g, i + 1, j, k), hix(g, i, j + 1, k), hix(g, i, j, k + 1)};
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+        double a0 = a.ab2_first ? A[c] : A0p[c][o];
+        double t0 = a.ab2_first ? T[c] : T0p[c][o];
+        double gp = -dt * (-a.P[h] + a.P[hp[c]]) / d[c];
+        double val;
+        if (!a.ibm)
+            val = Us[c][h] + gp + dt * (3.0 * A[c] - a0) / 2.0 + dt * B[c] / 2.0 + dt * (T[c] + t0) / 2.0 + dt * Fp[c][o];
+        else
+            val = Us[c][h] + gp + dt * (3.0 * A[c] - a0) / 2.0 + dt * B[c] + dt * (T[c] + t0) / 2.0 + dt * Fp[c][o];
+        if (!a.ibm) a.out[c][o] = val;
+        else { a.out[c][h] = val; a.B[c][o] = B[c]; }
+        A0p[c][o] = A[c];
+        T0p[c][o] = T[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// IBM (fenep_mpi.f90:1794-1929; 2D fenep_2d.f90:1726-1819).
+
+__device__ inline double roma(double r) {
+    double ar = fabs(r);
+    if (ar < 1.5 && ar >= 0.5) return (5.0 - 3.0 * ar - sqrt(-3.0 * ((1 - ar) * (1 - ar)) + 1.0)) / 6.0;
+    if (ar < 0.5) return (1.0 + sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
+    return 0.0;
+}
+
+__device__ inline void stencil_origin(int comp, double xc, double yc, double dX, double dY, int &i0, int &j0) {
+    if (comp == 0) { j0 = (int)(yc / dY); i0 = (int)(xc / dX - 0.5); }
+    else if (comp == 1) { j0 = (int)(yc / dY - 0.5); i0 = (int)(xc / dX); }
+    else { j0 = (int)(yc / dY); i0 = (int)(xc / dX); }
+}
+
+__device__ inline void grid_pos(int comp, int i, int j, int k, double dX, double dY, double dZ, double &x, double &y,
+                                double &z) {
+    x = (i - 0.5) * dX; y = (j - 0.5) * dY; z = (k - 0.5) * dZ;
+    if (comp == 0) x = x + 0.5 * dX;
+    else if (comp == 1) y = y + 0.5 * dY;
+    else z = z + 0.5 * dZ;
+}
+
+struct IbmArgs {
+    const double *mx, *my, *mu, *mv;
+    const int *mcyl;
+    int nm, ncomp, d3;
+    double dvol, dxn;
+    const double *Uf[3];
+    double *Fc[3];
+    const int *off[3], *idx[3];
+    const double *Ua[3], *B[3];
+    double *Q[3];
+};
+
+// interpolation at the markers and the marker force Fc = (Uc - Ub)/dt
+__global__ void k_ibm_interp(IbmArgs a, Geo g) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y + 1;
+    const int comp = blockIdx.z;
+    if (m >= a.nm) return;
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    const double xc = a.mx[m], yc = a.my[m];
+    const double zc = a.d3 ? (n - 0.25) * dZ : 0.0;
+    int i0, j0;
+    stencil_origin(comp, xc, yc, dX, dY, i0, j0);
+    const int klo = a.d3 ? n - 1 : 1, khi = a.d3 ? n + 1 : 1;
+    double ub = 0.0;
+    const double *Uf = a.Uf[comp];
+    for (int k = klo; k <= khi; ++k)
+        for (int j = j0; j <= j0 + 2; ++j)
+            for (int i = i0; i <= i0 + 2; ++i) {
+                double x, y, z;
+                grid_pos(comp, i, j, k, dX, dY, dZ, x, y, z);
+                double del = a.d3 ? roma((x - xc) / dX) * roma((y - yc) / dY) * roma((z - zc) / dZ) / a.dvol
+                                  : roma((x - xc) / dX) * roma((y - yc) / dY) / a.dvol;
+                ub = ub + Uf[hix(g, i, j, k)] * del * a.dxn;
+            }
+    const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
+    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = 0.0 + (uc - ub) / g.dt;
+}
+
+// pre-fold spreading sum of extended cell (ie, je, ke) (ftmp of ibm_Helmholtz)
+__device__ inline double spread_at(const IbmArgs &a, const Geo &g, int comp, int ie, int je, int ke) {
+    const int col = ie + g.sx * je;
+    const int b = a.off[comp][col], e = a.off[comp][col + 1];
+    if (b == e) return 0.0;
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    double x, y, z;
+    grid_pos(comp, ie, je, ke, dX, dY, dZ, x, y, z);
+    double acc = 0.0;
+    const int nlo = a.d3 ? max(ke - 1, 1) : 1, nhi = a.d3 ? min(ke + 1, g.nz) : 1;
+    for (int n = nlo; n <= nhi; ++n) {
+        const double zc = a.d3 ? (n - 0.25) * dZ : 0.0;
+        for (int q = b; q < e; ++q) {
+            const int m = a.idx[comp][q];
+            const double xc = a.mx[m], yc = a.my[m];
+            double del = a.d3 ? roma((x - xc) / dX) * roma((y - yc) / dY) * roma((z - zc) / dZ) / a.dvol
+                              : roma((x - xc) / dX) * roma((y - yc) / dY) / a.dvol;
+            double fcv = a.Fc[comp][m + (size_t)a.nm * (n - 1)];
+            acc = acc + fcv * del * a.dxn;
+        }
+    }
+    return acc;
+}
+
+// Spread the marker forces (with the periodic fold of ibm_PBM,
+// fenep.f90:2195-2205) and form Q = Ua + dt*f - dt*B/2 (ibm_predict,
+// fenep.f90:2229) for every interior cell.
+__global__ void k_ibm_spread_q(IbmArgs a, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int o = qix(g, i, j, k), h = hix(g, i, j, k);
+    int xs[2] = {i, -1}, ys[2] = {j, -1}, zs[2] = {k, -1};
+    if (i == 1) xs[1] = g.nx + 1; else if (i == g.nx) xs[1] = 0;
+    if (!g.walls) { if (j == 1) ys[1] = g.ny + 1; else if (j == g.ny) ys[1] = 0; }
+    if (a.d3) { if (k == 1) zs[1] = g.nz + 1; else if (k == g.nz) zs[1] = 0; }
+    for (int comp = 0; comp < a.ncomp; ++comp) {
+        double fz = 0.0;
+        for (int zz = 0; zz < 2; ++zz) {
+            if (zs[zz] < 0) continue;
+            double fy = 0.0;
+            for (int yy = 0; yy < 2; ++yy) {
+                if (ys[yy] < 0) continue;
+                double fx = 0.0;
+                for (int xx = 0; xx < 2; ++xx) {
+                    if (xs[xx] < 0) continue;
+                    double v = spread_at(a, g, comp, xs[xx], ys[yy], zs[zz]);
+                    fx = xx == 0 ? v : fx + v;
+                }
+                fy = yy == 0 ? fx : fy + fx;
+            }
+            fz = zz == 0 ? fy : fz + fy;
+        }
+        const double dt = g.dt;
+        a.Q[comp][o] = a.Ua[comp][h] + dt * fz - dt * a.B[comp][o] / 2;
+    }
+}
+
+// drag of each cylinder: -sum(Fc) * dv per component (one block per cylinder)
+__global__ void k_drag(const double *Fx, const double *Fy, const double *Fz, const int *mcyl, int nm, int nz, int ncomp,
+                       double dv, double *out) {
+    const int l = blockIdx.x;
+    __shared__ double sh[3][256];
+    double s[3] = {0.0, 0.0, 0.0};
+    const double *F[3] = {Fx, Fy, Fz};
+    for (long q = threadIdx.x; q < (long)nm * nz; q += blockDim.x) {
+        int m = (int)(q % nm);
+        if (mcyl[m] != l) continue;
+        for (int c = 0; c < ncomp; ++c) s[c] += F[c][q];
+    }
+    for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = s[c];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) out[3 * l + c] = c < ncomp ? -sh[c][0] * dv : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Poisson right-hand side (fenep.f90:1547-1555) and projection (1562-1604).
+
+__global__ void k_poisson_rhs(const double *Up, const double *Vp, const double *Wp, double *Q, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    double s = (-Up[hix(g, i - 1, j, k)] + Up[hix(g, i, j, k)]) / g.dx + (-Vp[hix(g, i, j - 1, k)] + Vp[hix(g, i, j, k)]) / g.dy;
+    if (g.dim == 3) s = s + (-Wp[hix(g, i, j, k - 1)] + Wp[hix(g, i, j, k)]) / g.dz;
+    Q[qix(g, i, j, k)] = s / g.dt;
+}
+
+__global__ void k_march(double *U, double *V, double *W, double *P, const double *Up, const double *Vp,
+                        const double *Wp, const double *Phi, Geo g, double pc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    const double dt = g.dt, dX = g.dx, dY = g.dy, dZ = g.dz;
+    const double ph = Phi[h];
+    U[h] = Up[h] - dt * (-ph + Phi[hix(g, i + 1, j, k)]) / dX;
+    V[h] = Vp[h] - dt * (-ph + Phi[hix(g, i, j + 1, k)]) / dY;
+    if (g.dim == 3) W[h] = Wp[h] - dt * (-ph + Phi[hix(g, i, j, k + 1)]) / dZ;
+    double lap = (Phi[hix(g, i - 1, j, k)] - 2 * ph + Phi[hix(g, i + 1, j, k)]) / (dX * dX)
+               + (Phi[hix(g, i, j - 1, k)] - 2 * ph + Phi[hix(g, i, j + 1, k)]) / (dY * dY);
+    if (g.dim == 3) lap = lap + (Phi[hix(g, i, j, k - 1)] - 2 * ph + Phi[hix(g, i, j, k + 1)]) / (dZ * dZ);
+    P[h] = P[h] + ph - pc * lap;
+}
+
+// ---------------------------------------------------------------------------
+// Red-black SOR (the reference's sweep, fenep.f90:885-896, is lexicographic in
+// k and j; the GPU colours by (i+j+k) parity, so it matches the reference
+// only at the converged tolerance).  A device flag stops the remaining
+// launched iterations once the tolerance is met.
+
+__global__ void k_sor_color(double *Phi, double *E, const double *Q, Geo g, int color, double om, const int *flag) {
+    if (flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    if (((i + j + k) & 1) != color) return;
+    const bool d3 = g.dim == 3;
+    const double BXM = 1.0 / (g.dx * g.dx), BXP = BXM, BYM = 1.0 / (g.dy * g.dy), BYP = BYM;
+    const double BZM = d3 ? 1.0 / (g.dz * g.dz) : 0.0, BZP = BZM;
+    const double B0 = BXM + BXP + BYM + BYP + BZM + BZP;
+    const int h = hix(g, i, j, k);
+    double e = BZM * Phi[hix(g, i, j, k - 1)] + BYM * Phi[hix(g, i, j - 1, k)] + BXM * Phi[hix(g, i - 1, j, k)]
+               - B0 * Phi[h] + BXP * Phi[hix(g, i + 1, j, k)] + BYP * Phi[hix(g, i, j + 1, k)]
+               + BZP * Phi[hix(g, i, j, k + 1)] - Q[qix(g, i, j, k)];
+    E[qix(g, i, j, k)] = e;
+    Phi[h] = Phi[h] + om * e / B0;
+}
+
+__global__ void k_bc_scalar_flag(double *A, Geo g, int kind, const int *flag) {
+    if (flag[0]) return;
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (halo_cell(g, t, i, j, k)) A[hix(g, i, j, k)] = halo_value(g, A, kind, i, j, k);
+}
+
+// Deterministic two-level reductions: partial sums per block in a fixed order,
+// then one block sums the partials.
+template <int OP>  // 0: sum of squares, 1: sum of interior values of a halo field
+__global__ void k_reduce_part(const double *A, int n, double *part, Geo g, const int *flag) {
+    if (flag && flag[0]) return;
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        if (OP == 0) { double v = A[q]; s += v * v; }
+        else {
+            int i = 1 + (int)(q % g.nx), j = 1 + (int)((q / g.nx) % g.ny), k = 1 + (int)(q / ((long)g.nx * g.ny));
+            s += A[hix(g, i, j, k)];
+        }
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// finish: scal[slot] = sum(part); mode 1 (SOR check): compare with er0 and set
+// the flag (flag[0] = 1 when converged, flag[1] = iteration count)
+__global__ void k_reduce_final(const double *part, int nparts, double *scal, int slot, int mode, int *flag, double eps,
+                               int itr) {
+    if (mode == 1 && flag[0]) return;
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        scal[slot] = sh[0];
+        if (mode == 1) {
+            flag[1] = itr;
+            double er0 = scal[0];
+            if (sqrt(sh[0] / er0) < eps) flag[0] = 1;
+        }
+        if (mode == 2) {  // er0 with the reference's zero guard
+            if (sh[0] == 0.0) scal[slot] = 1.0e-16;
+        }
+    }
+}
+
+__global__ void k_shift(double *A, int n, const double *scal, int slot, double inv_n) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    double mean = scal[slot] * inv_n;
+    A[q] = A[q] - mean;
+}
+
+__global__ void k_aos_to_soa(const double *aos, double *soa, int ncomp, int cs) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    for (int m = 0; m < ncomp; ++m) soa[(size_t)m * cs + h] = aos[(size_t)ncomp * h + m];
+}
+__global__ void k_soa_to_aos(const double *soa, double *aos, int ncomp, int cs) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    for (int m = 0; m < ncomp; ++m) aos[(size_t)ncomp * h + m] = soa[(size_t)m * cs + h];
+}
+__global__ void k_count_nonfinite(const double *a, int n, unsigned long long *out) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long c = (q < n && !isfinite(a[q])) ? 1ull : 0ull;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+
+inline dim3 cell_grid(const Geo &g, dim3 blk) {
+    return dim3((g.nx + blk.x - 1) / blk.x, (g.ny + blk.y - 1) / blk.y, g.nz);
+}
+
+cudaError_t bc(double *A, const Geo &g, int kind, cudaStream_t s) {
+    long n = halo_count(g) + ((kind == BC_V && g.walls) ? (long)g.nx * g.nz : 0);
+    k_bc_scalar<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, g, kind);
+    return cudaGetLastError();
+}
+
+// Periodic spectral solve (fft_solve): src interior -> dst halo interior.
+cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lhs0, double lhs1, cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
+    // x forward
+    {
+        int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+        int npp = ny / 2, total = npp * nz;
+        size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
+        k_fft_x_fwd<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+    }
+    DivideSpec none{};
+    // y forward (line along y: stride nxh, sets = k planes)
+    {
+        int tx = std::max(1, std::min(32, 2048 / ny));
+        size_t smem = (size_t)2 * ny * tx * sizeof(Cx<double>);
+        dim3 grid((nxh + tx - 1) / tx, nz);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, -1, 0, none);
+    }
+    // z forward + divide + z inverse (line along z: stride nxh*ny, sets = j)
+    {
+        DivideSpec dv{d.kx2, d.ky2, d.kz2, lhs0, lhs1, (double)nx * ny * nz, 1};
+        int tx = std::max(1, std::min(32, 2048 / nz));
+        size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
+        dim3 grid((nxh + tx - 1) / tx, ny);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 1, dv);
+    }
+    // y inverse
+    {
+        int tx = std::max(1, std::min(32, 2048 / ny));
+        size_t smem = (size_t)2 * ny * tx * sizeof(Cx<double>);
+        dim3 grid((nxh + tx - 1) / tx, nz);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, +1, 0, none);
+    }
+    // x inverse
+    {
+        int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+        int npp = ny / 2, total = npp * nz;
+        size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
+        k_fft_x_inv<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i);
+    }
+    return cudaGetLastError();
+}
+
+// Wall-bounded solve: FFT(x, z) of rows 1..NY, tridiagonal in y over rows
+// 0..NY+1, inverse FFT of all NY+2 rows into dst (halo rows 0..NY+1).
+cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double uwall, cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, n = ny + 2;
+    DivideSpec none{};
+    {
+        int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+        int npp = ny / 2, total = npp * nz;
+        size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
+        k_fft_x_fwd<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+    }
+    if (nz > 1) {
+        int tx = std::max(1, std::min(32, 2048 / nz));
+        size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
+        dim3 grid((nxh + tx - 1) / tx, ny);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 0, none);
+    }
+    {
+        WallSpec w{d.kx2, d.kz2, d.ph.dt, d.ph.beta, d.ph.re, g.dy, (double)nx * nz, uwall, sys};
+        int tx = 16;
+        size_t smem = (size_t)n * tx * (sizeof(Cx<double>) + sizeof(double));
+        dim3 grid((nxh + tx - 1) / tx, nz);
+        k_wall_tdma<double><<<grid, 128, smem, s>>>(d.H, d.H2, ny, nxh, tx, w);
+    }
+    if (nz > 1) {
+        int tx = std::max(1, std::min(32, 2048 / nz));
+        size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
+        dim3 grid((nxh + tx - 1) / tx, n);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H2, nz, nxh * n, nxh, nxh, tx, d.twz_r, d.twz_i, +1, 0, none);
+    }
+    {
+        int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+        int npp = n / 2, total = npp * nz;
+        size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
+        k_fft_x_inv<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t reduce_sumsq(const double *A, int n, double *part, double *scal, int slot, int mode, int *flag, double eps,
+                         int itr, const Geo &g, cudaStream_t s) {
+    int nb = std::min(1024, (n + 255) / 256);
+    k_reduce_part<0><<<nb, 256, 0, s>>>(A, n, part, g, mode == 1 ? flag : nullptr);
+    k_reduce_final<<<1, 256, 0, s>>>(part, nb, scal, slot, mode, flag, eps, itr);
+    return cudaGetLastError();
+}
+
+cudaError_t sor_solve(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
+    const Geo &g = d.g;
+    dim3 blk(32, 8);
+    dim3 grd = cell_grid(g, blk);
+    // er0 = sum(Q^2) (+1e-16 guard); flag reset
+    F8_CUDA_RET(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), s));
+    F8_CUDA_RET(reduce_sumsq(d.Q[0], d.ni, d.red, d.scal, 0, 2, d.flag, 0.0, 0, g, s));
+    const long nh = halo_count(g);
+    const unsigned hb = (unsigned)((nh + 255) / 256);
+    int done = 0, it_host[2] = {0, 0};
+    const int chunk = 25;
+    for (int it0 = 1; it0 <= o.sor_itrmax && !done; it0 += chunk) {
+        int last = std::min(o.sor_itrmax, it0 + chunk - 1);
+        for (int it = it0; it <= last; ++it) {
+            for (int color = 0; color < 2; ++color) {
+                k_sor_color<<<grd, blk, 0, s>>>(d.Phi, d.E, d.Q[0], g, color, o.sor_omega, d.flag);
+                k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag);
+            }
+            k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag);
+            F8_CUDA_RET(reduce_sumsq(d.E, d.ni, d.red, d.scal, 1, 1, d.flag, o.sor_eps, it, g, s));
+        }
+        F8_CUDA_RET(cudaMemcpyAsync(it_host, d.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        F8_CUDA_RET(cudaStreamSynchronize(s));
+        done = it_host[0];
+    }
+    *iters = done ? it_host[1] : o.sor_itrmax + 1;
+    // zero-mean shift (fenep_2d.f90:577-579)
+    int nb = std::min(1024, (d.ni + 255) / 256);
+    k_reduce_part<1><<<nb, 256, 0, s>>>(d.Phi, d.ni, d.red, g, nullptr);
+    k_reduce_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 2, 0, d.flag, 0.0, 0);
+    k_shift<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Phi, d.cs, d.scal, 2, 1.0 / ((double)g.nx * g.ny * g.nz));
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t init_kernels_fp64() {
+    const int big = 200 * 1024;
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_wall_tdma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    return cudaSuccess;
+}
+
+cudaError_t bc_all_state_fp64(Dev &d, cudaStream_t s) {
+    cudaError_t e;
+    if ((e = bc(d.U, d.g, BC_U, s))) return e;
+    if ((e = bc(d.V, d.g, BC_V, s))) return e;
+    if (d.g.dim == 3 && (e = bc(d.W, d.g, BC_W, s))) return e;
+    if ((e = bc(d.P, d.g, BC_P, s))) return e;
+    long n = halo_count(d.g);
+    k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, d.g, d.ncomp, d.cs, d.ph.lp2);
+    k_pet_all<<<(d.cs + 255) / 256, 256, 0, s>>>(d.C, d.fpet, d.ncomp, d.cs, d.ph.lp2);
+    return cudaGetLastError();
+}
+
+cudaError_t aos_to_soa(const double *aos, double *soa, int ncomp, int cs, cudaStream_t s) {
+    k_aos_to_soa<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs);
+    return cudaGetLastError();
+}
+cudaError_t soa_to_aos(const double *soa, double *aos, int ncomp, int cs, cudaStream_t s) {
+    k_soa_to_aos<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs);
+    return cudaGetLastError();
+}
+cudaError_t count_nonfinite(const double *a, int n, unsigned long long *out, cudaStream_t s) {
+    k_count_nonfinite<<<(n + 255) / 256, 256, 0, s>>>(a, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s) {
+    const Geo &g = d.g;
+    const bool d3 = g.dim == 3;
+    cudaError_t e;
+    auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
+    mark(0);
+    // 1. polymer
+    if (o.polymer) {
+        dim3 blk(32, 4);
+        dim3 grd = cell_grid(g, blk);
+        if (d3) k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs);
+        else k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs);
+        mark(1);
+        if (d3) k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt);
+        else k_polymer_update2<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, g, d.ph, d.cs, d.cnt);
+        std::swap(d.C, d.Cn);
+        long n = halo_count(g);
+        k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2);
+        if ((e = cudaGetLastError())) return e;
+    } else {
+        mark(1);
+    }
+    mark(2);
+    // 2. momentum right-hand side
+    MomArgs ma{};
+    ma.U = d.U; ma.V = d.V; ma.W = d.W; ma.P = d.P; ma.C = d.C; ma.fpet = d.fpet;
+    ma.Ax0 = d.Ax0; ma.Ay0 = d.Ay0; ma.Az0 = d.Az0; ma.Tx0 = d.Tx0; ma.Ty0 = d.Ty0; ma.Tz0 = d.Tz0;
+    ma.Fx = d.Fx; ma.Fy = d.Fy; ma.Fz = d.Fz;
+    if (o.ibm) { ma.out[0] = d.Ua; ma.out[1] = d.Va; ma.out[2] = d.Wa; }
+    else { ma.out[0] = d.Q[0]; ma.out[1] = d.Q[1]; ma.out[2] = d.Q[2]; }
+    ma.B[0] = d.Bx; ma.B[1] = d.By; ma.B[2] = d.Bz;
+    ma.cs = d.cs; ma.polymer = o.polymer; ma.ab2_first = o.ab2_first; ma.ibm = o.ibm;
+    ma.coef_t = (1.0 - d.ph.beta) / (d.ph.re * d.ph.wi);
+    ma.vis = d.ph.beta / d.ph.re;
+    {
+        dim3 blk(32, 8);
+        dim3 grd = cell_grid(g, blk);
+        if (d3) k_momentum<3><<<grd, blk, 0, s>>>(ma, g);
+        else k_momentum<2><<<grd, blk, 0, s>>>(ma, g);
+        if ((e = cudaGetLastError())) return e;
+    }
+    mark(3);
+    // 3. IBM direct forcing
+    if (o.ibm) {
+        if ((e = bc(d.Ua, g, BC_U, s))) return e;
+        if ((e = bc(d.Va, g, BC_V, s))) return e;
+        if (d3 && (e = bc(d.Wa, g, BC_W, s))) return e;
+        IbmArgs ia{};
+        ia.mx = d.mx; ia.my = d.my; ia.mu = d.mu; ia.mv = d.mv; ia.mcyl = d.mcyl;
+        ia.nm = d.nm; ia.ncomp = d3 ? 3 : 2; ia.d3 = d3;
+        ia.dvol = d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy;
+        ia.dxn = d3 ? g.dx * g.dx * g.dx : g.dx * g.dx;
+        ia.Uf[0] = d.Ua; ia.Uf[1] = d.Va; ia.Uf[2] = d.Wa;
+        for (int c = 0; c < 3; ++c) {
+            ia.Fc[c] = d.Fc[c]; ia.off[c] = d.csr_off[c]; ia.idx[c] = d.csr_idx[c];
+            ia.Q[c] = d.Q[c]; ia.B[c] = (c == 0 ? d.Bx : c == 1 ? d.By : d.Bz);
+        }
+        ia.Ua[0] = d.Ua; ia.Ua[1] = d.Va; ia.Ua[2] = d.Wa;
+        dim3 gi((d.nm + 127) / 128, g.nz, ia.ncomp);
+        k_ibm_interp<<<gi, 128, 0, s>>>(ia, g);
+        dim3 blk(32, 8);
+        k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g);
+        if (drag_out_dev) k_drag<<<d.ncyl, 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mcyl, d.nm, g.nz, ia.ncomp, ia.dvol, drag_out_dev);
+        if ((e = cudaGetLastError())) return e;
+    }
+    mark(4);
+    // 4. Helmholtz (CN viscous) solves
+    double *outs[3] = {d.Up, d.Vp, d.Wp};
+    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+    for (int c = 0; c < (d3 ? 3 : 2); ++c) {
+        if (!g.walls) e = fft_solve_periodic(d, d.Q[c], outs[c], 1.0, lhs1, s);
+        else e = wall_solve(d, d.Q[c], outs[c], c == 1 ? SYS_V : SYS_U, c == 0 ? g.uwall : 0.0, s);
+        if (e) return e;
+    }
+    if ((e = bc(d.Up, g, BC_U, s))) return e;
+    if ((e = bc(d.Vp, g, BC_V, s))) return e;
+    if (d3 && (e = bc(d.Wp, g, BC_W, s))) return e;
+    mark(5);
+    // 5. Poisson
+    {
+        dim3 blk(32, 8);
+        k_poisson_rhs<<<cell_grid(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Q[0], g);
+    }
+    if (o.poisson == 0) {
+        if (!g.walls) e = fft_solve_periodic(d, d.Q[0], d.Phi, 0.0, -1.0, s);
+        else e = wall_solve(d, d.Q[0], d.Phi, SYS_P, 0.0, s);
+        if (e) return e;
+        if ((e = bc(d.Phi, g, BC_P, s))) return e;
+        *sor_iters = -1;
+    } else {
+        if ((e = sor_solve(d, o, sor_iters, s))) return e;
+    }
+    mark(6);
+    // 6. projection and pressure update
+    {
+        dim3 blk(32, 8);
+        k_march<<<cell_grid(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, g,
+                                                  d.ph.dt * d.ph.beta / d.ph.re / 2.0);
+        if ((e = cudaGetLastError())) return e;
+    }
+    if ((e = bc(d.U, g, BC_U, s))) return e;
+    if ((e = bc(d.V, g, BC_V, s))) return e;
+    if (d3 && (e = bc(d.W, g, BC_W, s))) return e;
+    if ((e = bc(d.P, g, BC_P, s))) return e;
+    mark(7);
+    return cudaGetLastError();
+}
+
+}  // namespace f8

@@ -183,6 +183,20 @@ class Solver:
         self._check(self._fns["markers"](self._h, C.byref(n), _ptr(xy)))
         return xy[: n.value]
 
+    def set_timing(self, on: bool = True) -> None:
+        self._check(self._fns["set_timing"](self._h, 1 if on else 0))
+
+    def timing(self):
+        """(total ms of the f8_step calls, per-stage ms array, steps timed)."""
+        tot = C.c_double()
+        st = np.zeros(abi.NSTAGE)
+        n = C.c_longlong()
+        self._check(self._fns["timing"](self._h, C.byref(tot), _ptr(st), C.byref(n)))
+        return tot.value, st, n.value
+
+    def timing_reset(self) -> None:
+        self._check(self._fns["timing_reset"](self._h))
+
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             self._fns["destroy"](self._h)

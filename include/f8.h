@@ -157,6 +157,27 @@ int f8_diagnostics(f8_ctx *ctx, f8_diag *out);
  * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */
 int f8_markers(f8_ctx *ctx, int *n_per_plane, double *xy);
 
+/* Device-side timing (the reference's cpu_time buckets, fenep.f90:2478-2527,
+ * reported at 2561-2566).  With timing enabled, f8_step records CUDA events
+ * around each stage of every step on the context's stream; f8_timing returns
+ * the accumulated milliseconds per stage and the total device time of the
+ * f8_step calls since the last reset (the total is recorded even when the
+ * per-stage timing is off).  Stages: */
+enum f8_stage {
+    F8_STAGE_EIGEN = 0,      /* candidate selection by eigen test ("C+-")       */
+    F8_STAGE_NEWTON = 1,     /* Cstar + implicit Newton ("Newton")              */
+    F8_STAGE_MOMENTUM = 2,   /* stress, convection, viscous, predictor RHS      */
+    F8_STAGE_IBM = 3,        /* marker interpolation, force, spreading           */
+    F8_STAGE_HELMHOLTZ = 4,  /* CN viscous solves                                */
+    F8_STAGE_POISSON = 5,    /* divergence and pressure Poisson solve            */
+    F8_STAGE_PROJECT = 6,    /* projection, pressure update, boundary values     */
+    F8_NSTAGE = 7
+};
+int f8_set_timing(f8_ctx *ctx, int enable);
+int f8_timing(f8_ctx *ctx, double *total_ms, double *stage_ms /* F8_NSTAGE or NULL */,
+              long long *steps_timed);
+int f8_timing_reset(f8_ctx *ctx);
+
 const char *f8_strerror(int status);
 void f8_destroy(f8_ctx *ctx);
 

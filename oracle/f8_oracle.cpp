@@ -33,6 +33,7 @@
 #include <vector>
 #include <algorithm>
 #include <new>
+#include <chrono>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -73,6 +74,16 @@ struct OCtx {
     long long newton_iters = 0, newton_unconv = 0;
     int poisson_iters = -1;
     int sor_order = 0;  // 0: reference sweep order, 1: red-black
+    bool timing = false;
+    double total_ms = 0, stage_ms[7] = {};
+    long long timed_steps = 0;
+    std::chrono::steady_clock::time_point tmark;
+    void mark(int q) {
+        if (!timing) return;
+        auto now = std::chrono::steady_clock::now();
+        if (q > 0) stage_ms[q - 1] += std::chrono::duration<double, std::milli>(now - tmark).count();
+        tmark = now;
+    }
 
     size_t hidx(int i, int j, int k) const { return (size_t)i + (size_t)SX * ((size_t)j + (size_t)SY * (size_t)k); }
     size_t iidx(int i, int j, int k) const { return (size_t)(i - 1) + (size_t)NX * ((size_t)(j - 1) + (size_t)NY * (size_t)(k - 1)); }
@@ -1308,18 +1319,26 @@ int do_step(OCtx &c, double *drag) {
         std::fill(c.Tz.begin(), c.Tz.end(), 0.0);
         c.newton_iters = 0; c.newton_unconv = 0;
     } else if (d3) {
+        c.mark(0);
         polymer_faces3(c);
+        c.mark(1);
         cstar3(c);
         lyapunov3(c);
+        c.mark(2);
         polymer_stress3(c);
     } else {
+        c.mark(0);
+        c.mark(1);
         polymer2(c);
+        c.mark(2);
         polymer_stress2(c);
     }
+    if (c.ph.beta == 1.0) { c.mark(0); c.mark(1); c.mark(2); }
     convection_viscous(c);
     if (step_no == 1 && c.ph.ab2_start) save_history(c);
     predictor(c, ibm);
     save_history(c);
+    c.mark(3);
     std::vector<double> Qx, Qy, Qz;
     std::vector<double> *Qs[3] = {&Qx, &Qy, &Qz};
     const double dt = c.ph.dt;
@@ -1359,7 +1378,9 @@ int do_step(OCtx &c, double *drag) {
             }
         }
     }
+    c.mark(4);
     helmholtz(c, Qs);
+    c.mark(5);
     // Poisson
     std::vector<double> Qp;
     poisson_rhs(c, Qp);
@@ -1371,7 +1392,9 @@ int do_step(OCtx &c, double *drag) {
     } else {
         c.poisson_iters = sor(c, Qp, c.sor_order);
     }
+    c.mark(6);
     march(c);
+    c.mark(7);
     c.step += 1;
     // NaN guard (fenep_2d.f90:1974)
     for (size_t n = 0; n < c.nh(); ++n)
@@ -1511,8 +1534,12 @@ int f8o_step(f8_ctx *ctx, int nsteps, double *drag) {
     if (!c.loaded) return F8_ERR_STATE;
     int worst = F8_OK;
     const int ncyl = (int)c.cyl.size();
+    auto t0 = std::chrono::steady_clock::now();
     for (int s = 0; s < nsteps; ++s) {
         int st = do_step(c, drag ? drag + (size_t)s * ncyl * 3 : nullptr);
+        c.total_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        t0 = std::chrono::steady_clock::now();
+        c.timed_steps += 1;
         if (st == F8_ERR_NAN) return st;
         if (st > worst) worst = st;
     }
@@ -1592,6 +1619,28 @@ const char *f8o_strerror(int st) {
 }
 
 void f8o_destroy(f8_ctx *ctx) { delete reinterpret_cast<OCtx *>(ctx); }
+
+int f8o_set_timing(f8_ctx *ctx, int enable) {
+    if (!ctx) return F8_ERR_ARG;
+    reinterpret_cast<OCtx *>(ctx)->timing = enable != 0;
+    return F8_OK;
+}
+
+int f8o_timing(f8_ctx *ctx, double *total_ms, double *stage_ms, long long *steps) {
+    if (!ctx) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (total_ms) *total_ms = c.total_ms;
+    if (stage_ms) for (int q = 0; q < 7; ++q) stage_ms[q] = c.stage_ms[q];
+    if (steps) *steps = c.timed_steps;
+    return F8_OK;
+}
+
+int f8o_timing_reset(f8_ctx *ctx) {
+    if (!ctx) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    c.total_ms = 0; for (double &v : c.stage_ms) v = 0; c.timed_steps = 0;
+    return F8_OK;
+}
 
 // --- oracle-only controls and kernel-level entry points (tests) ------------
 
