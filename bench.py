@@ -250,6 +250,29 @@ def run_ours(args, w):
         out = s.store()
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(ws, time.perf_counter() - t0)
+    # the FP64 path on the same workload and the drag difference (accuracy gate)
+    cmp = None
+    if prec == abi.F8_MIXED and not args.no_fp64_compare:
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s64:
+            s64.load(st0)
+            _, d64w = s64.step(args.warmup)
+            s64.set_timing(True)
+            s64.timing_reset()
+            _, d64 = s64.step(args.steps)
+            t64, st64, n64 = s64.timing()
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as sm:
+            sm.load(st0)
+            _, dmw = sm.step(args.warmup)
+            _, dm = sm.step(args.steps)
+        dall64 = np.concatenate([d64w, d64]) if d64w is not None else d64
+        dallm = np.concatenate([dmw, dm]) if dmw is not None else dm
+        rel = None
+        if dall64 is not None:
+            rel = float(np.max(np.abs(dallm[..., 0] - dall64[..., 0])) / np.max(np.abs(dall64[..., 0])))
+        v64 = cells * args.steps / (t64 / 1e3) / 1e6
+        cmp = {"fp64_value": v64, "fp64_ms_per_step": t64 / args.steps, "mixed_over_fp64": value / v64,
+               "drag_rel_err_vs_fp64": rel, "steps_compared": args.warmup + args.steps,
+               "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s",
@@ -275,7 +298,7 @@ def run_ours(args, w):
                        "l2": "inputs larger than L2 (state %.2f GB)" % (sb / 1e9), "parallelism": f"replicas{ws}"},
             "status": int(status), "div_max": diag.div_max, "newton_iters_per_cell": diag.newton_iters / cells,
             "drag_last": drag[-1].tolist() if drag is not None else None,
-            "gpu_launches": None, "clocks": clocks, "roofline": roof, "e2e": e2e}
+            "gpu_launches": None, "clocks": clocks, "roofline": roof, "e2e": e2e, "fp64_compare": cmp}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
     print(json.dumps(line))
@@ -291,9 +314,10 @@ def main():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     args = ap.parse_args()
     if args.precision == "auto":
-        args.precision = "fp64"
+        args.precision = "mixed"
     w = configs.WORKLOADS[args.workload]()
     if args.impl == "reference":
         return run_reference(args, w)

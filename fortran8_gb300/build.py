@@ -24,6 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "f8_step_fp64.cu": ["--fmad=false"],
     "f8_api.cu": ["--fmad=false"],
+    "f8_step_mixed.cu": [],
 }
 
 

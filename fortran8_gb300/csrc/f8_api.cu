@@ -172,6 +172,29 @@ int upload(f8_ctx *c, double **dst, const std::vector<double> &v) {
     return F8_OK;
 }
 
+int upload_f(f8_ctx *c, float **dst, const std::vector<double> &v) {
+    std::vector<float> f(v.begin(), v.end());
+    API_CUDA(c, c->alloc(dst, f.size()));
+    API_CUDA(c, cudaMemcpyAsync(*dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+int upload_i(f8_ctx *c, int **dst, const std::vector<int> &v) {
+    API_CUDA(c, c->alloc(dst, std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) API_CUDA(c, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(int), cudaMemcpyHostToDevice, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+// Kernel of the IBM delta function (fenep.f90:2045-2055), host copy.
+double roma_h(double r) {
+    double ar = std::fabs(r);
+    if (ar < 1.5 && ar >= 0.5) return (5.0 - 3.0 * ar - std::sqrt(-3.0 * ((1 - ar) * (1 - ar)) + 1.0)) / 6.0;
+    if (ar < 0.5) return (1.0 + std::sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
+    return 0.0;
+}
+
 int setup(f8_ctx *c) {
     const f8_grid &G = c->grid;
     Dev &d = c->d;
@@ -191,34 +214,58 @@ int setup(f8_ctx *c) {
     API_CUDA(c, cudaEventCreate(&c->tot0));
     API_CUDA(c, cudaEventCreate(&c->tot1));
     const size_t cs = d.cs, ni = d.ni;
-    for (double **p : {&d.U, &d.V, &d.W, &d.P, &d.Phi, &d.fpet, &d.Up, &d.Vp, &d.Wp, &d.Ua, &d.Va, &d.Wa})
+    const bool mixed = c->precision == F8_MIXED;
+    if (mixed) API_CUDA(c, init_kernels_mixed());
+    for (double **p : {&d.U, &d.V, &d.W, &d.P, &d.Phi, &d.Up, &d.Vp, &d.Wp})
         API_CUDA(c, c->alloc(p, cs));
-    API_CUDA(c, c->alloc(&d.C, cs * d.ncomp));
-    API_CUDA(c, c->alloc(&d.Cn, cs * d.ncomp));
     API_CUDA(c, c->alloc(&c->scratch_aos, cs * d.ncomp));
     API_CUDA(c, c->alloc(&d.codes, ni));
-    for (double **p : {&d.Ax0, &d.Ay0, &d.Az0, &d.Tx0, &d.Ty0, &d.Tz0, &d.Fx, &d.Fy, &d.Fz, &d.Bx, &d.By, &d.Bz,
-                       &d.Q[0], &d.Q[1], &d.Q[2], &d.E})
-        API_CUDA(c, c->alloc(p, ni));
     const size_t nxh = g.nx / 2 + 1;
     const size_t nspec = 2 * nxh * (size_t)(g.ny + 2) * g.nz;
-    API_CUDA(c, c->alloc(&d.H, nspec));
-    API_CUDA(c, c->alloc(&d.H2, nspec));
+    if (!mixed) {
+        for (double **p : {&d.fpet, &d.Ua, &d.Va, &d.Wa}) API_CUDA(c, c->alloc(p, cs));
+        API_CUDA(c, c->alloc(&d.C, cs * d.ncomp));
+        API_CUDA(c, c->alloc(&d.Cn, cs * d.ncomp));
+        for (double **p : {&d.Ax0, &d.Ay0, &d.Az0, &d.Tx0, &d.Ty0, &d.Tz0, &d.Fx, &d.Fy, &d.Fz, &d.Bx, &d.By, &d.Bz,
+                           &d.Q[0], &d.Q[1], &d.Q[2], &d.E})
+            API_CUDA(c, c->alloc(p, ni));
+        API_CUDA(c, c->alloc(&d.H, nspec));
+        API_CUDA(c, c->alloc(&d.H2, nspec));
+    } else {
+        API_CUDA(c, c->alloc(&d.Cf, cs * d.ncomp));
+        API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
+        API_CUDA(c, c->alloc(&d.fpetf, cs));
+        for (int q = 0; q < 3; ++q) {
+            API_CUDA(c, c->alloc(&d.A0f[q], ni));
+            API_CUDA(c, c->alloc(&d.T0f[q], ni));
+            API_CUDA(c, c->alloc(&d.Ff[q], ni));
+            API_CUDA(c, c->alloc(&d.Qf[q], ni));
+        }
+        API_CUDA(c, c->alloc(&d.Rp, ni));
+        API_CUDA(c, c->alloc(&d.Rd, ni));
+        API_CUDA(c, c->alloc(&d.Hf, nspec));
+        API_CUDA(c, c->alloc(&d.H2f, nspec));
+        d.defect_iters = 1;
+    }
     API_CUDA(c, c->alloc(&d.red, 4096));
     API_CUDA(c, c->alloc(&d.scal, 64));
     API_CUDA(c, c->alloc(&d.flag, 4));
     API_CUDA(c, c->alloc(&d.cnt, 1));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
     std::vector<double> tr, ti;
-    make_tw(g.nx, tr, ti);
-    if (int st = upload(c, &d.twx_r, tr)) return st;
-    if (int st = upload(c, &d.twx_i, ti)) return st;
-    make_tw(g.ny, tr, ti);
-    if (int st = upload(c, &d.twy_r, tr)) return st;
-    if (int st = upload(c, &d.twy_i, ti)) return st;
-    make_tw(g.nz, tr, ti);
-    if (int st = upload(c, &d.twz_r, tr)) return st;
-    if (int st = upload(c, &d.twz_i, ti)) return st;
+    double **twd[3][2] = {{&d.twx_r, &d.twx_i}, {&d.twy_r, &d.twy_i}, {&d.twz_r, &d.twz_i}};
+    float **twf[3][2] = {{&d.twxf_r, &d.twxf_i}, {&d.twyf_r, &d.twyf_i}, {&d.twzf_r, &d.twzf_i}};
+    const int nn[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a) {
+        make_tw(nn[a], tr, ti);
+        if (!mixed) {
+            if (int st = upload(c, twd[a][0], tr)) return st;
+            if (int st = upload(c, twd[a][1], ti)) return st;
+        } else {
+            if (int st = upload_f(c, twf[a][0], tr)) return st;
+            if (int st = upload_f(c, twf[a][1], ti)) return st;
+        }
+    }
     // modified wavenumbers 2(1-cos(m 2pi/N))/d^2 (fenep.f90:1458-1460 with
     // the angle step 2 pi/N, identical to (i-1)*dX in the reference's 2 pi box)
     const double thx = 2 * PI / g.nx, thy = 2 * PI / g.ny, thz = 2 * PI / g.nz;
@@ -270,6 +317,42 @@ int setup(f8_ctx *c) {
             API_CUDA(c, c->alloc(&d.csr_idx[comp], std::max<size_t>(idx.size(), 1)));
             if (!idx.empty())
                 API_CUDA(c, cudaMemcpyAsync(d.csr_idx[comp], idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, cudaStreamSynchronize(c->s));
+            if (mixed && comp < ncomp) {
+                // separable 1D kernel weights of each marker and the interior
+                // columns that receive spreading (after the periodic fold)
+                std::vector<double> wx(3 * (size_t)nm), wy(3 * (size_t)nm);
+                std::vector<int> i0v(nm), j0v(nm);
+                for (int m = 0; m < nm; ++m) {
+                    int i0, j0;
+                    stencil_origin_h(comp, mx[m], my[m], g.dx, g.dy, i0, j0);
+                    i0v[m] = i0; j0v[m] = j0;
+                    for (int a = 0; a < 3; ++a) {
+                        double xg = (i0 + a - 0.5) * g.dx + (comp == 0 ? 0.5 * g.dx : 0.0);
+                        double yg = (j0 + a - 0.5) * g.dy + (comp == 1 ? 0.5 * g.dy : 0.0);
+                        wx[3 * m + a] = roma_h((xg - mx[m]) / g.dx);
+                        wy[3 * m + a] = roma_h((yg - my[m]) / g.dy);
+                    }
+                }
+                if (int st = upload_f(c, &d.mwx[comp], wx)) return st;
+                if (int st = upload_f(c, &d.mwy[comp], wy)) return st;
+                if (int st = upload_i(c, &d.mi0[comp], i0v)) return st;
+                if (int st = upload_i(c, &d.mj0[comp], j0v)) return st;
+                std::vector<int> act;
+                for (int j = 1; j <= g.ny; ++j)
+                    for (int i = 1; i <= g.nx; ++i) {
+                        int xs[2] = {i, -1}, ys[2] = {j, -1};
+                        if (i == 1) xs[1] = g.nx + 1; else if (i == g.nx) xs[1] = 0;
+                        if (!g.walls) { if (j == 1) ys[1] = g.ny + 1; else if (j == g.ny) ys[1] = 0; }
+                        bool any = false;
+                        for (int a = 0; a < 2 && !any; ++a)
+                            for (int b2 = 0; b2 < 2 && !any; ++b2)
+                                if (xs[a] >= 0 && ys[b2] >= 0 && !lists[xs[a] + g.sx * ys[b2]].empty()) any = true;
+                        if (any) act.push_back((i - 1) + g.nx * (j - 1));
+                    }
+                d.nact[comp] = (int)act.size();
+                if (int st = upload_i(c, &d.act_cols[comp], act)) return st;
+            }
         }
         // the interpolation stencil reads k = n-1 .. n+1 and marker columns
         // inside the halo box; validated above through the gather lists
@@ -305,7 +388,7 @@ int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *c
     *out = nullptr;
     int st = validate(g, ph, ncyl, cy, prec, poisson);
     if (st) return st;
-    if (prec == F8_MIXED) return F8_ERR_UNSUPPORTED;
+    if (prec == F8_MIXED && (g->dim != 3 || poisson != F8_POISSON_FFT)) return F8_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -340,12 +423,28 @@ int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
     API_CUDA(c, put(d.P, in->p, cs));
     API_CUDA(c, put(d.Phi, in->phi, cs));
     API_CUDA(c, put(c->scratch_aos, in->c, cs * d.ncomp));
-    API_CUDA(c, aos_to_soa(c->scratch_aos, d.C, d.ncomp, (int)cs, c->s));
-    API_CUDA(c, put(d.Ax0, in->ax0, ni)); API_CUDA(c, put(d.Ay0, in->ay0, ni)); API_CUDA(c, put(d.Az0, in->az0, ni));
-    API_CUDA(c, put(d.Tx0, in->tx0, ni)); API_CUDA(c, put(d.Ty0, in->ty0, ni)); API_CUDA(c, put(d.Tz0, in->tz0, ni));
-    API_CUDA(c, put(d.Fx, in->fx, ni)); API_CUDA(c, put(d.Fy, in->fy, ni)); API_CUDA(c, put(d.Fz, in->fz, ni));
-    // boundary values of the loaded state (init calls PBM, fenep.f90:139-143)
-    API_CUDA(c, bc_all_state_fp64(d, c->s));
+    if (c->precision == F8_FP64) {
+        API_CUDA(c, aos_to_soa(c->scratch_aos, d.C, d.ncomp, (int)cs, c->s));
+        API_CUDA(c, put(d.Ax0, in->ax0, ni)); API_CUDA(c, put(d.Ay0, in->ay0, ni)); API_CUDA(c, put(d.Az0, in->az0, ni));
+        API_CUDA(c, put(d.Tx0, in->tx0, ni)); API_CUDA(c, put(d.Ty0, in->ty0, ni)); API_CUDA(c, put(d.Tz0, in->tz0, ni));
+        API_CUDA(c, put(d.Fx, in->fx, ni)); API_CUDA(c, put(d.Fy, in->fy, ni)); API_CUDA(c, put(d.Fz, in->fz, ni));
+        // boundary values of the loaded state (init calls PBM, fenep.f90:139-143)
+        API_CUDA(c, bc_all_state_fp64(d, c->s));
+    } else {
+        API_CUDA(c, aos_to_soa_f(c->scratch_aos, d.Cf, d.ncomp, (int)cs, c->s));
+        const double *src[9] = {in->ax0, in->ay0, in->az0, in->tx0, in->ty0, in->tz0, in->fx, in->fy, in->fz};
+        float *dst[9] = {d.A0f[0], d.A0f[1], d.A0f[2], d.T0f[0], d.T0f[1], d.T0f[2], d.Ff[0], d.Ff[1], d.Ff[2]};
+        double *tmp = c->scratch_aos;  // ncomp*cs >= ni doubles
+        for (int q = 0; q < 9; ++q) {
+            if (src[q]) {
+                API_CUDA(c, cudaMemcpyAsync(tmp, src[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
+                API_CUDA(c, d2f(tmp, dst[q], (int)ni, c->s));
+            } else {
+                API_CUDA(c, cudaMemsetAsync(dst[q], 0, ni * sizeof(float), c->s));
+            }
+        }
+        API_CUDA(c, bc_all_state_mixed(d, c->s));
+    }
     API_CUDA(c, cudaStreamSynchronize(c->s));
     c->step = step0;
     c->step0 = step0;
@@ -378,13 +477,15 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         o.poisson = c->poisson;
         o.sor_omega = c->phys.sor_omega; o.sor_eps = c->phys.sor_eps; o.sor_itrmax = c->phys.sor_itrmax;
         o.ev = c->timing ? &c->evpool[per * s] : nullptr;
+        const bool mixed = c->precision == F8_MIXED;
         if (!o.polymer && s == 0) {
             // beta == 1: C and T vanish (fenep.f90:2479-2485)
-            API_CUDA(c, cudaMemsetAsync(d.C, 0, (size_t)d.cs * d.ncomp * sizeof(double), c->s));
+            if (mixed) API_CUDA(c, cudaMemsetAsync(d.Cf, 0, (size_t)d.cs * d.ncomp * sizeof(float), c->s));
+            else API_CUDA(c, cudaMemsetAsync(d.C, 0, (size_t)d.cs * d.ncomp * sizeof(double), c->s));
         }
         int sor_iters = -1;
         double *dg = (ncyl && drag) ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
-        cudaError_t e = step_fp64(d, o, dg, &sor_iters, c->s);
+        cudaError_t e = mixed ? step_mixed(d, o, dg, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
         if (e != cudaSuccess) return fail(c, e, "step");
         c->last_poisson_iters = sor_iters;
         if (c->poisson == F8_POISSON_SOR && sor_iters > c->phys.sor_itrmax) worst = std::max(worst, (int)F8_WARN_SOR);
@@ -431,13 +532,28 @@ int f8_store(f8_ctx *c, f8_fields *out) {
     if (c->grid.dim == 3) API_CUDA(c, get(out->w, d.W, cs));
     API_CUDA(c, get(out->p, d.P, cs));
     API_CUDA(c, get(out->phi, d.Phi, cs));
-    if (out->c) {
-        API_CUDA(c, soa_to_aos(d.C, c->scratch_aos, d.ncomp, (int)cs, c->s));
-        API_CUDA(c, get(out->c, c->scratch_aos, cs * d.ncomp));
+    if (c->precision == F8_FP64) {
+        if (out->c) {
+            API_CUDA(c, soa_to_aos(d.C, c->scratch_aos, d.ncomp, (int)cs, c->s));
+            API_CUDA(c, get(out->c, c->scratch_aos, cs * d.ncomp));
+        }
+        API_CUDA(c, get(out->ax0, d.Ax0, ni)); API_CUDA(c, get(out->ay0, d.Ay0, ni)); API_CUDA(c, get(out->az0, d.Az0, ni));
+        API_CUDA(c, get(out->tx0, d.Tx0, ni)); API_CUDA(c, get(out->ty0, d.Ty0, ni)); API_CUDA(c, get(out->tz0, d.Tz0, ni));
+        API_CUDA(c, get(out->fx, d.Fx, ni)); API_CUDA(c, get(out->fy, d.Fy, ni)); API_CUDA(c, get(out->fz, d.Fz, ni));
+    } else {
+        if (out->c) {
+            API_CUDA(c, soa_to_aos_f(d.Cf, c->scratch_aos, d.ncomp, (int)cs, c->s));
+            API_CUDA(c, get(out->c, c->scratch_aos, cs * d.ncomp));
+        }
+        double *dsts[9] = {out->ax0, out->ay0, out->az0, out->tx0, out->ty0, out->tz0, out->fx, out->fy, out->fz};
+        const float *srcs[9] = {d.A0f[0], d.A0f[1], d.A0f[2], d.T0f[0], d.T0f[1], d.T0f[2], d.Ff[0], d.Ff[1], d.Ff[2]};
+        for (int q = 0; q < 9; ++q) {
+            if (!dsts[q]) continue;
+            API_CUDA(c, f2d(srcs[q], c->scratch_aos, (int)ni, c->s));
+            API_CUDA(c, get(dsts[q], c->scratch_aos, ni));
+            API_CUDA(c, cudaStreamSynchronize(c->s));
+        }
     }
-    API_CUDA(c, get(out->ax0, d.Ax0, ni)); API_CUDA(c, get(out->ay0, d.Ay0, ni)); API_CUDA(c, get(out->az0, d.Az0, ni));
-    API_CUDA(c, get(out->tx0, d.Tx0, ni)); API_CUDA(c, get(out->ty0, d.Ty0, ni)); API_CUDA(c, get(out->tz0, d.Tz0, ni));
-    API_CUDA(c, get(out->fx, d.Fx, ni)); API_CUDA(c, get(out->fy, d.Fy, ni)); API_CUDA(c, get(out->fz, d.Fz, ni));
     API_CUDA(c, cudaStreamSynchronize(c->s));
     return F8_OK;
 }

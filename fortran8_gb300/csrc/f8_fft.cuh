@@ -44,8 +44,8 @@ __device__ inline void stockham_stage(const Cx<T> *x, Cx<T> *y, int n, int ns, i
 // source src (row length n, nrow_src rows per plane) become spectral rows
 // jj, jj+1 of H (nrow_h rows per plane).  One CTA handles ppc row pairs with
 // n/2 threads each.
-template <typename T>
-__global__ void k_fft_x_fwd(const T *__restrict__ src, T *__restrict__ H, int n, int nrow_src, int j0, int nrow_h,
+template <typename T, typename TS>
+__global__ void k_fft_x_fwd(const TS *__restrict__ src, T *__restrict__ H, int n, int nrow_src, int j0, int nrow_h,
                             int npairs_per_plane, int nplanes, const T *__restrict__ twr, const T *__restrict__ twi) {
     extern __shared__ unsigned char smem_raw[];
     Cx<T> *sm = reinterpret_cast<Cx<T> *>(smem_raw);
@@ -60,9 +60,9 @@ __global__ void k_fft_x_fwd(const T *__restrict__ src, T *__restrict__ H, int n,
     if (active) {
         k = (int)(pair / npairs_per_plane);
         jj = 2 * (int)(pair % npairs_per_plane);
-        const T *ra = src + (size_t)n * ((size_t)(j0 + jj - 1) + (size_t)nrow_src * k);
-        const T *rb = ra + n;
-        for (int e = t; e < n; e += tpp) { x[e].r = ra[e]; x[e].i = rb[e]; }
+        const TS *ra = src + (size_t)n * ((size_t)(j0 + jj - 1) + (size_t)nrow_src * k);
+        const TS *rb = ra + n;
+        for (int e = t; e < n; e += tpp) { x[e].r = T(ra[e]); x[e].i = T(rb[e]); }
     }
     __syncthreads();
     for (int ns = 1; ns < n; ns *= 2) {
@@ -85,9 +85,11 @@ __global__ void k_fft_x_fwd(const T *__restrict__ src, T *__restrict__ H, int n,
 }
 
 // Inverse: spectral rows jj, jj+1 (nrow_h per plane) -> real rows jdst0 + jj,
-// jdst0 + jj + 1 of a halo-layout field (x written at 1..n).
-template <typename T>
-__global__ void k_fft_x_inv(const T *__restrict__ H, T *__restrict__ dst, int n, int nrow_h, int npairs_per_plane,
+// jdst0 + jj + 1 of a halo-layout field (x written at 1..n).  With a base
+// field the result is dst = base + value (the mixed-precision path forms the
+// FP64 predicted velocity from the FP32 increment here).
+template <typename T, typename TO>
+__global__ void k_fft_x_inv(const T *__restrict__ H, TO *dst, const TO *base, int n, int nrow_h, int npairs_per_plane,
                             int nplanes, int jdst0, int sx, int sy, const T *__restrict__ twr, const T *__restrict__ twi) {
     extern __shared__ unsigned char smem_raw[];
     Cx<T> *sm = reinterpret_cast<Cx<T> *>(smem_raw);
@@ -123,9 +125,15 @@ __global__ void k_fft_x_inv(const T *__restrict__ H, T *__restrict__ dst, int n,
         Cx<T> *tmp = x; x = y; y = tmp;
     }
     if (!active) return;
-    T *ra = dst + 1 + (size_t)sx * ((size_t)(jdst0 + jj) + (size_t)sy * (k + 1));
-    T *rb = ra + sx;
-    for (int e = t; e < n; e += tpp) { ra[e] = x[e].r; rb[e] = x[e].i; }
+    const size_t oa = 1 + (size_t)sx * ((size_t)(jdst0 + jj) + (size_t)sy * (k + 1));
+    TO *ra = dst + oa;
+    TO *rb = ra + sx;
+    if (base) {
+        const TO *ba = base + oa, *bb = ba + sx;
+        for (int e = t; e < n; e += tpp) { ra[e] = ba[e] + TO(x[e].r); rb[e] = bb[e] + TO(x[e].i); }
+    } else {
+        for (int e = t; e < n; e += tpp) { ra[e] = TO(x[e].r); rb[e] = TO(x[e].i); }
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -35,6 +35,19 @@ struct Dev {
     double *Fc[3];                         // nm * nz each
     int *csr_off[3], *csr_idx[3];          // per component over (SX*SY) columns
     double *drag;                          // per step ncyl*3
+    // mixed-precision state and work (F8_MIXED)
+    float *Cf, *Cnf, *fpetf;               // FP32 conformation tensor (SoA halo) and f(C)
+    float *A0f[3], *T0f[3], *Ff[3];        // FP32 history and body force (interior)
+    float *Qf[3];                          // FP32 right-hand sides dt*(R + f)
+    double *Rp;                            // FP64 Poisson right-hand side (interior)
+    double *Rd;                            // FP64 Poisson defect (interior)
+    float *Hf, *H2f;                       // FP32 spectra
+    float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
+    float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
+    int *mi0[3], *mj0[3];                  // per-marker stencil origins
+    int *act_cols[3];                      // interior (i,j) columns that receive spreading
+    int nact[3];
+    int defect_iters;                      // Poisson defect corrections (mixed)
     // reductions
     double *red;                           // scratch partial sums (>= 4096)
     double *scal;                          // small scalar results
@@ -61,5 +74,18 @@ cudaError_t init_kernels_fp64();
 cudaError_t aos_to_soa(const double *aos, double *soa, int ncomp, int cs, cudaStream_t s);
 cudaError_t soa_to_aos(const double *soa, double *aos, int ncomp, int cs, cudaStream_t s);
 cudaError_t count_nonfinite(const double *a, int n, unsigned long long *out, cudaStream_t s);
+// FP64 helpers shared with the mixed path (f8_step_fp64.cu)
+cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s);
+cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s);
+cudaError_t launch_march(Dev &d, cudaStream_t s);
+cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s);
+// Mixed path (f8_step_mixed.cu)
+cudaError_t init_kernels_mixed();
+cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s);
+cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s);
+cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s);
+cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s);
+cudaError_t aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs, cudaStream_t s);
+cudaError_t soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs, cudaStream_t s);
 
 }  // namespace f8

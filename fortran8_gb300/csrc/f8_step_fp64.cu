@@ -979,7 +979,7 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_fwd<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
     }
     DivideSpec none{};
     // y forward (line along y: stride nxh, sets = k planes)
@@ -1009,7 +1009,7 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i);
+        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nullptr, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i);
     }
     return cudaGetLastError();
 }
@@ -1024,7 +1024,7 @@ cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double u
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_fwd<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
     }
     if (nz > 1) {
         int tx = std::max(1, std::min(32, 2048 / nz));
@@ -1049,7 +1049,7 @@ cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double u
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = n / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i);
+        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nullptr, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i);
     }
     return cudaGetLastError();
 }
@@ -1102,8 +1102,8 @@ cudaError_t init_kernels_fp64() {
     const int big = 200 * 1024;
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_wall_tdma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return cudaSuccess;
 }
 
@@ -1116,6 +1116,29 @@ cudaError_t bc_all_state_fp64(Dev &d, cudaStream_t s) {
     long n = halo_count(d.g);
     k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, d.g, d.ncomp, d.cs, d.ph.lp2);
     k_pet_all<<<(d.cs + 255) / 256, 256, 0, s>>>(d.C, d.fpet, d.ncomp, d.cs, d.ph.lp2);
+    return cudaGetLastError();
+}
+
+cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s) { return bc(A, g, kind, s); }
+
+cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s) {
+    dim3 blk(32, 8);
+    k_poisson_rhs<<<cell_grid(d.g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, out, d.g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_march(Dev &d, cudaStream_t s) {
+    dim3 blk(32, 8);
+    k_march<<<cell_grid(d.g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.g,
+                                                d.ph.dt * d.ph.beta / d.ph.re / 2.0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s) {
+    const Geo &g = d.g;
+    const bool d3 = g.dim == 3;
+    k_drag<<<d.ncyl, 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mcyl, d.nm, g.nz, d3 ? 3 : 2,
+                                  d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out);
     return cudaGetLastError();
 }
 

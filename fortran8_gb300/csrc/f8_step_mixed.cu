@@ -1,0 +1,739 @@
+// f8_step_mixed.cu — FP32-bulk / FP64-state step (F8_MIXED).
+//
+// Same discretisation as the FP64 step (fenep.f90 numerics; cited per kernel
+// in f8_step_fp64.cu), with the precision split:
+//   FP64: U, V, W, P, Phi state; the pressure gradient; the formation of the
+//         predicted velocity U* = U^n + dU; the Poisson right-hand side and its
+//         defect; the projection; marker forces and drag; the Peterlin factor
+//         when L^2 - tr C < 1% of L^2.
+//   FP32: C, f(C), the AB2/trapezoid history, stress / convection / viscous
+//         stencils, the eigen test and Newton solve of the polymer update, and
+//         every spectral transform and tridiagonal solve.
+// The predictor is solved in increment form: (1 - dt beta/(2Re) L) dU =
+// dt (R + f), with R = -grad P + (3A - A0)/2 + B + (T + T0)/2 + F.  This is
+// algebraically the reference's (1 - dt beta/(2Re) L) U* = Q (fenep.f90:
+// 1469-1479, 2229-2233) with U* = U^n + dU, but FP32 rounding now touches only
+// the O(dt) increment.  The Poisson equation is solved in FP32 and corrected
+// with FP64 residuals (iterative refinement).
+#include <algorithm>
+#include <cstdio>
+#include "f8_common.cuh"
+#include "f8_fft.cuh"
+#include "f8_kernels.h"
+
+namespace f8 {
+namespace {
+
+constexpr float TWO_PI_3F = 2.0943951023931955f;
+
+__host__ __device__ inline long halo_count_m(const Geo &g) {
+    return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
+}
+
+__device__ inline bool halo_cell_m(const Geo &g, long t, int &i, int &j, int &k) {
+    long nf = 2L * g.sy * g.sz;
+    if (t < nf) {
+        long r = t % ((long)g.sy * g.sz);
+        i = (t / ((long)g.sy * g.sz)) ? g.sx - 1 : 0;
+        j = (int)(r % g.sy); k = (int)(r / g.sy);
+        return true;
+    }
+    t -= nf;
+    nf = 2L * g.nx * g.sz;
+    if (t < nf) {
+        long r = t % ((long)g.nx * g.sz);
+        j = (t / ((long)g.nx * g.sz)) ? g.sy - 1 : 0;
+        i = 1 + (int)(r % g.nx); k = (int)(r / g.nx);
+        return true;
+    }
+    t -= nf;
+    nf = 2L * g.nx * g.ny;
+    if (t < nf) {
+        long r = t % ((long)g.nx * g.ny);
+        k = (t / ((long)g.nx * g.ny)) ? g.sz - 1 : 0;
+        i = 1 + (int)(r % g.nx); j = 1 + (int)(r / g.nx);
+        return true;
+    }
+    return false;
+}
+
+// Peterlin factor (fenep.f90:510-515) from FP32 components: FP32 normally, FP64
+// when the denominator L^2 - tr C is within 1% of L^2 of the limit.
+__device__ inline float peterlin_f(float x0, float x3, float x5, float lp2f, double lp2) {
+    float tr = x0 + x3 + x5;
+    float den = lp2f - tr;
+    if (den > 0.01f * lp2f) return (lp2f - 3.0f) / den;
+    double trd = (double)x0 + (double)x3 + (double)x5;
+    return (float)((lp2 - 3.0) / (lp2 - trd));
+}
+
+// C halo (C_PBM / linear extrapolation at walls) and f on the halo cells
+__global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (!halo_cell_m(g, t, i, j, k)) return;
+    const int h = hix(g, i, j, k);
+    const int ii = wrapx(g, i), kk = wrapz(g, k);
+    float x[6];
+    for (int m = 0; m < 6; ++m) {
+        const float *A = C + (size_t)m * cs;
+        float v;
+        if (j >= 1 && j <= g.ny) v = A[hix(g, ii, j, kk)];
+        else if (!g.walls) v = A[hix(g, ii, wrapy(g, j), kk)];
+        else if (j == 0) v = 2.0f * A[hix(g, ii, 1, kk)] - A[hix(g, ii, 2, kk)];
+        else v = 2.0f * A[hix(g, ii, g.ny, kk)] - A[hix(g, ii, g.ny - 1, kk)];
+        x[m] = v;
+        C[(size_t)m * cs + h] = v;
+    }
+    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+}
+
+__global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    fpet[h] = peterlin_f(C[h], C[3 * (size_t)cs + h], C[5 * (size_t)cs + h], (float)lp2, lp2);
+}
+
+// ---------------------------------------------------------------------------
+// Polymer (3D).  Eigen test: the smallest eigenvalue of the symmetric 3x3
+// candidate in the shifted (traceless) trigonometric form, which is the same
+// root as the reference's Vieta formula (fenep.f90:425-444) but free of the
+// cancellation in p = a1 - a2^2/3 that FP32 would suffer near C = I.  Equal
+// roots (discriminant q^2 - p^3 >= 0) return the reference's -100 sentinel.
+__device__ inline float eigmin_f(const float *a) {
+    const float m = (a[0] + a[3] + a[5]) * (1.0f / 3.0f);
+    const float b0 = a[0] - m, b1 = a[3] - m, b2 = a[5] - m;
+    const float p2 = (b0 * b0 + b1 * b1 + b2 * b2 + 2.0f * (a[1] * a[1] + a[2] * a[2] + a[4] * a[4])) * (1.0f / 6.0f);
+    const float q = 0.5f * (b0 * (b1 * b2 - a[4] * a[4]) - a[1] * (a[1] * b2 - a[4] * a[2]) + a[2] * (a[1] * a[4] - b1 * a[2]));
+    const float p3 = p2 * p2 * p2;
+    if (q * q >= p3) return -100.0f;
+    const float sp = sqrtf(p2);
+    const float r = fminf(1.0f, fmaxf(-1.0f, q / (p2 * sp)));
+    return m + 2.0f * sp * cosf(acosf(r) * (1.0f / 3.0f) + TWO_PI_3F);
+}
+
+__device__ inline float face_pf(int idx, float cm, float c0, float cp) {
+    switch (idx) {
+    case 1: return c0 * 1.5f - cp * 0.5f;
+    case 2: return cm * 0.5f + c0 * 0.5f;
+    case 3: return cm * 0.25f + c0 - cp * 0.25f;
+    default: return c0;
+    }
+}
+__device__ inline float face_nf(int idx, float cm, float c0, float cp) {
+    switch (idx) {
+    case 1: return c0 * 0.5f + cp * 0.5f;
+    case 2: return -cm * 0.5f + c0 * 1.5f;
+    case 3: return -cm * 0.25f + c0 + cp * 0.25f;
+    default: return c0;
+    }
+}
+
+__device__ inline int select3f(const float *cm, const float *c0, const float *cp) {
+    float best = 0.0f;
+    int idx = 4;
+    bool found = false;
+    float ml[3];
+    for (int l = 1; l <= 3; ++l) {
+        float pt[6], nt[6];
+        for (int m = 0; m < 6; ++m) {
+            pt[m] = face_pf(l, cm[m], c0[m], cp[m]);
+            nt[m] = face_nf(l, cm[m], c0[m], cp[m]);
+        }
+        float a = eigmin_f(pt), b = eigmin_f(nt);
+        ml[l - 1] = isnan(a) ? b : (isnan(b) ? a : fminf(a, b));
+    }
+    // maxloc over (ml1, ml2, ml3, 0): first maximum, NaN ignored
+    for (int l = 0; l < 3; ++l) {
+        if (isnan(ml[l])) continue;
+        if (!found || ml[l] > best) { best = ml[l]; idx = l + 1; found = true; }
+    }
+    if (!found || 0.0f > best) idx = 4;
+    return idx;
+}
+
+__global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    float c0[6], cm[6], cp[6];
+    for (int m = 0; m < 6; ++m) c0[m] = C[(size_t)m * cs + h];
+    const int off[3] = {1, g.sx, g.sx * g.sy};
+    int code = 0;
+    for (int d = 0; d < 3; ++d) {
+        for (int m = 0; m < 6; ++m) {
+            cm[m] = C[(size_t)m * cs + h - off[d]];
+            cp[m] = C[(size_t)m * cs + h + off[d]];
+        }
+        code |= (select3f(cm, c0, cp) - 1) << (2 * d);
+    }
+    codes[qix(g, i, j, k)] = (uint8_t)code;
+}
+
+// Cstar + implicit Newton solve of A C + C A^T = Cx + dt/Wi I with
+// A = A0 + (1 + f(C) dt/Wi)/2 I (fenep.f90:518-605) in FP32.  The Jacobian is
+// analytic: J = M(A0) + a I + (dt/Wi) f'(tr C) C e^T, with a = 1 + f dt/Wi,
+// e = (1,0,0,1,0,1) and f' = (L^2-3)/(L^2-tr C)^2; the stopping rule is the
+// reference's relative step test.
+__global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
+                                                   float *__restrict__ fpet, const uint8_t *__restrict__ codes,
+                                                   const double *__restrict__ U, const double *__restrict__ V,
+                                                   const double *__restrict__ W, Geo g, Phys ph, int cs,
+                                                   StepCounters *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    const bool active = i <= g.nx && j <= g.ny;
+    unsigned long long my_itr = 0, my_unconv = 0;
+    if (active) {
+        const int h = hix(g, i, j, k);
+        const float dt = (float)ph.dt, dX = (float)g.dx, dY = (float)g.dy, dZ = (float)g.dz;
+        const int cself = codes[qix(g, i, j, k)];
+        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
+        const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
+        int jm = j - 1, jp = j + 1;
+        bool ym_ghost = false, yp_ghost = false;
+        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
+        const int cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
+        const int cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
+        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+        const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
+        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+        const float u1 = (float)U[hix(g, i - 1, j, k)], u2 = (float)U[h];
+        const float v1 = (float)V[hix(g, i, j - 1, k)], v2 = (float)V[h];
+        const float w1 = (float)W[hix(g, i, j, k - 1)], w2 = (float)W[h];
+        const float cxs = dt / (2.0f * dX), cys = dt / (2.0f * dY), czs = dt / (2.0f * dZ);
+        const float s1 = (-u2 + fabsf(u2)) * cxs, s2 = 1.0f / 6 + (-u2 - fabsf(u2)) * cxs;
+        const float s3 = 1.0f / 6 + (u1 - fabsf(u1)) * cxs, s4 = (u1 + fabsf(u1)) * cxs;
+        const float s5 = (-v2 + fabsf(v2)) * cys, s6 = 1.0f / 6 + (-v2 - fabsf(v2)) * cys;
+        const float s7 = 1.0f / 6 + (v1 - fabsf(v1)) * cys, s8 = (v1 + fabsf(v1)) * cys;
+        const float s9 = (-w2 + fabsf(w2)) * czs, s10 = 1.0f / 6 + (-w2 - fabsf(w2)) * czs;
+        const float s11 = 1.0f / 6 + (w1 - fabsf(w1)) * czs, s12 = (w1 + fabsf(w1)) * czs;
+        float b[6], x[6];
+        for (int m = 0; m < 6; ++m) {
+            const float *Cm = C + (size_t)m * cs;
+            const float c0 = Cm[h];
+            const float xm1 = Cm[h - ox], xp1 = Cm[h + ox];
+            const float ym1 = Cm[h - oy], yp1 = Cm[h + oy];
+            const float zm1 = Cm[h - oz], zp1 = Cm[h + oz];
+            float pxm = face_pf(isx, xm1, c0, xp1), nxp = face_nf(isx, xm1, c0, xp1);
+            float pxp = face_pf(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+            float nxm = face_nf(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            float pym = face_pf(isy, ym1, c0, yp1), nyp = face_nf(isy, ym1, c0, yp1);
+            float pyp = yp_ghost ? Cm[hyp] : face_pf(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+            float nym = ym_ghost ? Cm[hym] : face_nf(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            float pzm = face_pf(isz, zm1, c0, zp1), nzp = face_nf(isz, zm1, c0, zp1);
+            float pzp = face_pf(czp + 1, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
+            float nzm = face_nf(czm + 1, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
+            b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp
+                   + s11 * pzm + s9 * pzp + s12 * nzm + s10 * nzp;
+            x[m] = c0;
+        }
+        const float dtwi = (float)(ph.dt / ph.wi);
+        b[0] += dtwi; b[3] += dtwi; b[5] += dtwi;
+        // velocity gradient (fenep.f90:541-550), differences in FP64
+        auto U_ = [&](int a, int bb, int cc) { return U[hix(g, a, bb, cc)]; };
+        auto V_ = [&](int a, int bb, int cc) { return V[hix(g, a, bb, cc)]; };
+        auto W_ = [&](int a, int bb, int cc) { return W[hix(g, a, bb, cc)]; };
+        const double ddt = ph.dt;
+        float A0[3][3];
+        A0[0][0] = (float)(-ddt * (U_(i, j, k) - U_(i - 1, j, k)) / g.dx);
+        A0[0][1] = (float)(-ddt * (-V_(i - 1, j - 1, k) + V_(i + 1, j - 1, k) - V_(i - 1, j, k) + V_(i + 1, j, k)) / (4 * g.dx));
+        A0[0][2] = (float)(-ddt * (-W_(i - 1, j, k - 1) + W_(i + 1, j, k - 1) - W_(i - 1, j, k) + W_(i + 1, j, k)) / (4 * g.dx));
+        A0[1][0] = (float)(-ddt * (-U_(i - 1, j - 1, k) - U_(i, j - 1, k) + U_(i - 1, j + 1, k) + U_(i, j + 1, k)) / (4 * g.dy));
+        A0[1][1] = (float)(-ddt * (V_(i, j, k) - V_(i, j - 1, k)) / g.dy);
+        A0[1][2] = (float)(-ddt * (-W_(i, j - 1, k - 1) + W_(i, j + 1, k - 1) - W_(i, j - 1, k) + W_(i, j + 1, k)) / (4 * g.dy));
+        A0[2][0] = (float)(-ddt * (-U_(i - 1, j, k - 1) - U_(i, j, k - 1) + U_(i - 1, j, k + 1) + U_(i, j, k + 1)) / (4 * g.dz));
+        A0[2][1] = (float)(-ddt * (-V_(i, j - 1, k - 1) - V_(i, j, k - 1) + V_(i, j - 1, k + 1) + V_(i, j, k + 1)) / (4 * g.dz));
+        A0[2][2] = (float)(-ddt * (W_(i, j, k) - W_(i, j, k - 1)) / g.dz);
+        // A = transpose(A0) (fenep.f90:550)
+        const float a00 = A0[0][0], a01 = A0[1][0], a02 = A0[2][0];
+        const float a10 = A0[0][1], a11 = A0[1][1], a12 = A0[2][1];
+        const float a20 = A0[0][2], a21 = A0[1][2], a22 = A0[2][2];
+        // linear Lyapunov part M (rows of Lyapunov_func with A = A0^T)
+        float M[6][6] = {
+            {2 * a00, 2 * a01, 2 * a02, 0, 0, 0},
+            {a10, a11 + a00, a12, a01, a02, 0},
+            {a20, a21, a22 + a00, 0, a01, a02},
+            {0, 2 * a10, 0, 2 * a11, 2 * a12, 0},
+            {0, a20, a10, a21, a22 + a11, a12},
+            {0, 0, 2 * a20, 0, 2 * a21, 2 * a22}};
+        const float lp2f = (float)ph.lp2;
+        const float epsf = (float)ph.newton_eps;
+        int itr;
+        for (itr = 1; itr <= ph.newton_itrmax; ++itr) {
+            const float f = peterlin_f(x[0], x[3], x[5], lp2f, ph.lp2);
+            const float a = 1.0f + f * dtwi;
+            const float den = lp2f - (x[0] + x[3] + x[5]);
+            const float fp = (lp2f - 3.0f) / (den * den);
+            const float cc = dtwi * fp;
+            float Ah[6][7];
+            for (int r = 0; r < 6; ++r) {
+                float l = -b[r] + a * x[r];
+                for (int q = 0; q < 6; ++q) l += M[r][q] * x[q];
+                for (int q = 0; q < 6; ++q) Ah[r][q] = M[r][q] + cc * x[r] * ((q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f);
+                Ah[r][r] += a;
+                Ah[r][6] = l;
+            }
+            // Gauss-Jordan with partial pivoting
+            for (int kk = 0; kk < 6; ++kk) {
+                int piv = kk; float best = fabsf(Ah[kk][kk]);
+                for (int r = kk + 1; r < 6; ++r) if (fabsf(Ah[r][kk]) > best) { best = fabsf(Ah[r][kk]); piv = r; }
+                if (best == 0.0f) { for (int r = 0; r < 6; ++r) Ah[r][6] = 0.0f; break; }
+                if (piv != kk)
+                    for (int q = kk; q < 7; ++q) { float t = Ah[kk][q]; Ah[kk][q] = Ah[piv][q]; Ah[piv][q] = t; }
+                const float inv = 1.0f / Ah[kk][kk];
+                for (int q = kk + 1; q < 7; ++q) Ah[kk][q] *= inv;
+                for (int r = 0; r < 6; ++r) {
+                    if (r == kk) continue;
+                    const float fr = Ah[r][kk];
+                    for (int q = kk + 1; q < 7; ++q) Ah[r][q] -= fr * Ah[kk][q];
+                }
+            }
+            float sr = 0.0f, sx = 0.0f;
+            for (int m = 0; m < 6; ++m) {
+                x[m] -= Ah[m][6];
+                sr += Ah[m][6] * Ah[m][6];
+            }
+            for (int m = 0; m < 6; ++m) sx += x[m] * x[m];
+            if (sqrtf(sr / sx) < epsf) break;
+        }
+        my_itr = (unsigned long long)itr;
+        my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+        for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
+        fpet[h] = peterlin_f(x[0], x[3], x[5], lp2f, ph.lp2);
+    }
+    unsigned long long a = my_itr, b2 = my_unconv;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b2 += __shfl_down_sync(0xffffffffu, b2, o);
+    }
+    if (((threadIdx.x + blockDim.x * threadIdx.y) & 31) == 0) {
+        if (a) atomicAdd(&cnt->newton_iters, a);
+        if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Momentum right-hand side in increment form: Q_c = dt * R_c (FP32).
+struct MomArgsF {
+    const double *U, *V, *W, *P;
+    const float *C, *fpet;
+    float *A0[3], *T0[3];
+    const float *F[3];
+    float *Q[3];
+    int cs;
+    int polymer, ab2_first;
+    float coef_t, vis;
+    double dt;
+};
+
+__global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const float dX = (float)g.dx, dY = (float)g.dy, dZ = (float)g.dz;
+    const int o = qix(g, i, j, k), h = hix(g, i, j, k);
+    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+    if (a.polymer) {
+        const int cs = a.cs;
+        const float *C = a.C, *fp = a.fpet;
+        auto c0 = [&](int m, int hh) {
+            const float e = (m == 1 || m == 4 || m == 6) ? 1.0f : 0.0f;
+            return fp[hh] * C[(size_t)(m - 1) * cs + hh] - e;
+        };
+        const float ix = 1.0f / dX, iy = 1.0f / dY, iz = 1.0f / dZ;
+        const float sx = (c0(1, h + ox) - c0(1, h)) * ix
+                       + (-c0(2, h - oy) - c0(2, h + ox - oy) + c0(2, h + oy) + c0(2, h + ox + oy)) * (0.25f * iy)
+                       + (-c0(3, h - oz) - c0(3, h + ox - oz) + c0(3, h + oz) + c0(3, h + ox + oz)) * (0.25f * iz);
+        const float sy = (-c0(2, h - ox) + c0(2, h + ox) - c0(2, h - ox + oy) + c0(2, h + ox + oy)) * (0.25f * ix)
+                       + (c0(4, h + oy) - c0(4, h)) * iy
+                       + (-c0(5, h - oz) - c0(5, h + oy - oz) + c0(5, h + oz) + c0(5, h + oy + oz)) * (0.25f * iz);
+        const float sz = (-c0(3, h - ox) + c0(3, h + ox) - c0(3, h - ox + oz) + c0(3, h + ox + oz)) * (0.25f * ix)
+                       + (-c0(5, h - oy) + c0(5, h + oy) - c0(5, h - oy + oz) + c0(5, h + oy + oz)) * (0.25f * iy)
+                       + (c0(6, h + oz) - c0(6, h)) * iz;
+        tx = a.coef_t * sx; ty = a.coef_t * sy; tz = a.coef_t * sz;
+    }
+    const double *U = a.U, *V = a.V, *W = a.W;
+    auto u = [&](int hh) { return (float)U[hh]; };
+    auto v = [&](int hh) { return (float)V[hh]; };
+    auto w = [&](int hh) { return (float)W[hh]; };
+    const float ix = 1.0f / dX, iy = 1.0f / dY, iz = 1.0f / dZ;
+    // convection (fenep.f90:694-734), divergence form
+    const float uc = u(h), vc = v(h), wc = w(h);
+    float t1 = 0.5f * (u(h - ox) + uc), t2 = 0.5f * (uc + u(h + ox));
+    float ax = (t2 * t2 - t1 * t1) * ix
+             + (0.25f * (v(h) + v(h + ox)) * (uc + u(h + oy)) - 0.25f * (v(h - oy) + v(h + ox - oy)) * (u(h - oy) + uc)) * iy
+             + (0.25f * (w(h) + w(h + ox)) * (uc + u(h + oz)) - 0.25f * (w(h - oz) + w(h + ox - oz)) * (u(h - oz) + uc)) * iz;
+    float t3 = 0.5f * (v(h - oy) + vc), t4 = 0.5f * (vc + v(h + oy));
+    float ay = (0.25f * (uc + u(h + oy)) * (vc + v(h + ox)) - 0.25f * (u(h - ox) + u(h - ox + oy)) * (v(h - ox) + vc)) * ix
+             + (t4 * t4 - t3 * t3) * iy
+             + (0.25f * (w(h) + w(h + oy)) * (vc + v(h + oz)) - 0.25f * (w(h - oz) + w(h + oy - oz)) * (v(h - oz) + vc)) * iz;
+    float t5 = 0.5f * (w(h - oz) + wc), t6 = 0.5f * (wc + w(h + oz));
+    float az = (0.25f * (uc + u(h + oz)) * (wc + w(h + ox)) - 0.25f * (u(h - ox) + u(h - ox + oz)) * (w(h - ox) + wc)) * ix
+             + (0.25f * (vc + v(h + oz)) * (wc + w(h + oy)) - 0.25f * (v(h - oy) + v(h - oy + oz)) * (w(h - oy) + wc)) * iy
+             + (t6 * t6 - t5 * t5) * iz;
+    // viscous (fenep.f90:736-770): second differences in FP64, then FP32
+    auto lap = [&](const double *F) {
+        const double c = F[h];
+        return (float)((F[h - ox] - 2.0 * c + F[h + ox]) * (1.0 / (g.dx * g.dx)) + (F[h - oy] - 2.0 * c + F[h + oy]) * (1.0 / (g.dy * g.dy))
+                       + (F[h - oz] - 2.0 * c + F[h + oz]) * (1.0 / (g.dz * g.dz)));
+    };
+    const float A[3] = {-ax, -ay, -az};
+    const float B[3] = {a.vis * lap(U), a.vis * lap(V), a.vis * lap(W)};
+    const float T[3] = {tx, ty, tz};
+    const int hp[3] = {h + ox, h + oy, h + oz};
+    const double dd[3] = {g.dx, g.dy, g.dz};
+    const float dt = (float)a.dt;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a0 = a.ab2_first ? A[c] : a.A0[c][o];
+        const float t0 = a.ab2_first ? T[c] : a.T0[c][o];
+        const float gp = (float)(-(a.P[hp[c]] - a.P[h]) / dd[c]);
+        const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + a.F[c][o];
+        a.Q[c][o] = dt * r;
+        a.A0[c][o] = A[c];
+        a.T0[c][o] = T[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// IBM (fenep_mpi.f90:1794-1929).  Ua = U + dt R at the stencil points with the
+// boundary values that the reference gives Ua (PBM / wall rules).
+__device__ inline double ua_at(const Geo &g, const double *Uc, const float *Qc, int comp, int i, int j, int k) {
+    const int ii = wrapx(g, i), kk = wrapz(g, k);
+    if (j >= 1 && j <= g.ny) {
+        if (g.walls && comp == 1 && j == g.ny) return 0.0;
+        return Uc[hix(g, i, j, k)] + (double)Qc[qix(g, ii, j, kk)];
+    }
+    if (!g.walls) return Uc[hix(g, i, j, k)] + (double)Qc[qix(g, ii, wrapy(g, j), kk)];
+    if (comp == 1) return 0.0;
+    const int jj = j == 0 ? 1 : g.ny;
+    const double inner = Uc[hix(g, ii, jj, kk)] + (double)Qc[qix(g, ii, jj, kk)];
+    return (comp == 0 && j != 0) ? 2 * g.uwall - inner : -inner;
+}
+
+struct IbmArgsF {
+    const double *mu, *mv;
+    const int *mcyl;
+    int nm;
+    const float *wx[3], *wy[3];      // per marker, 3 weights each
+    const int *i0[3], *j0[3];
+    float wz[3][3];                  // per component, offset k - n = -1, 0, 1
+    const double *Uc[3];
+    const float *Qc[3];
+    double *Fc[3];
+    const int *off[3], *idx[3];
+    const int *act[3];
+    int nact[3];
+    float *Q[3];
+};
+
+__global__ void k_ibm_interp_f(IbmArgsF a, Geo g) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = blockIdx.y + 1;
+    const int comp = blockIdx.z;
+    if (m >= a.nm) return;
+    const int i0 = a.i0[comp][m], j0 = a.j0[comp][m];
+    const float *wx = a.wx[comp] + 3 * m, *wy = a.wy[comp] + 3 * m;
+    double ub = 0.0;
+    for (int dk = 0; dk < 3; ++dk) {
+        const int k = n - 1 + dk;
+        for (int dj = 0; dj < 3; ++dj)
+            for (int di = 0; di < 3; ++di) {
+                const double w = (double)(wx[di] * wy[dj] * a.wz[comp][dk]);
+                ub += ua_at(g, a.Uc[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k) * w;
+            }
+    }
+    const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
+    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ub) / g.dt;
+}
+
+__device__ inline double spread_at_f(const IbmArgsF &a, const Geo &g, int comp, int ie, int je, int ke) {
+    const int col = ie + g.sx * je;
+    const int b = a.off[comp][col], e = a.off[comp][col + 1];
+    if (b == e) return 0.0;
+    double acc = 0.0;
+    const int nlo = max(ke - 1, 1), nhi = min(ke + 1, g.nz);
+    for (int n = nlo; n <= nhi; ++n) {
+        const float wz = a.wz[comp][ke - n + 1];
+        for (int q = b; q < e; ++q) {
+            const int m = a.idx[comp][q];
+            const float w = a.wx[comp][3 * m + (ie - a.i0[comp][m])] * a.wy[comp][3 * m + (je - a.j0[comp][m])] * wz;
+            acc += a.Fc[comp][m + (size_t)a.nm * (n - 1)] * (double)w;
+        }
+    }
+    return acc;
+}
+
+// spreading with the periodic fold (ibm_PBM) over the active columns only;
+// Q = dt*(R + f) for those cells
+__global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
+    const int comp = blockIdx.z;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.y + 1;
+    if (c >= a.nact[comp]) return;
+    const int col = a.act[comp][c];
+    const int i = col % g.nx + 1, j = col / g.nx + 1;
+    int xs[2] = {i, -1}, ys[2] = {j, -1}, zs[2] = {k, -1};
+    if (i == 1) xs[1] = g.nx + 1; else if (i == g.nx) xs[1] = 0;
+    if (!g.walls) { if (j == 1) ys[1] = g.ny + 1; else if (j == g.ny) ys[1] = 0; }
+    if (k == 1) zs[1] = g.nz + 1; else if (k == g.nz) zs[1] = 0;
+    double f = 0.0;
+    for (int zz = 0; zz < 2; ++zz) {
+        if (zs[zz] < 0) continue;
+        for (int yy = 0; yy < 2; ++yy) {
+            if (ys[yy] < 0) continue;
+            for (int xx = 0; xx < 2; ++xx) {
+                if (xs[xx] < 0) continue;
+                f += spread_at_f(a, g, comp, xs[xx], ys[yy], zs[zz]);
+            }
+        }
+    }
+    const int o = qix(g, i, j, k);
+    a.Q[comp][o] = (float)((double)a.Q[comp][o] + g.dt * f);
+}
+
+// ---------------------------------------------------------------------------
+// Poisson defect: r = rhs - L_h Phi (FP64), Phi with Neumann / periodic halo.
+__global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    const double c = Phi[h];
+    double lap = (Phi[h - ox] - 2.0 * c + Phi[h + ox]) / (g.dx * g.dx) + (Phi[h - oy] - 2.0 * c + Phi[h + oy]) / (g.dy * g.dy);
+    if (g.dim == 3) lap += (Phi[h - oz] - 2.0 * c + Phi[h + oz]) / (g.dz * g.dz);
+    const int o = qix(g, i, j, k);
+    r[o] = rhs[o] - lap;
+}
+
+template <typename A, typename B>
+__global__ void k_convert(const A *a, B *b, int n) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) b[q] = B(a[q]);
+}
+__global__ void k_aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    for (int m = 0; m < ncomp; ++m) soa[(size_t)m * cs + h] = (float)aos[(size_t)ncomp * h + m];
+}
+__global__ void k_soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= cs) return;
+    for (int m = 0; m < ncomp; ++m) aos[(size_t)ncomp * h + m] = (double)soa[(size_t)m * cs + h];
+}
+
+inline dim3 cell_grid_m(const Geo &g, dim3 blk) {
+    return dim3((g.nx + blk.x - 1) / blk.x, (g.ny + blk.y - 1) / blk.y, g.nz);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 spectral solves.  src (interior, FP32 or FP64) -> dst (FP64 halo
+// interior; dst = base + result when base is given).
+template <typename TS>
+cudaError_t solve_periodic_f(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
+                             cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
+    const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+    const size_t smx = (size_t)ppc * 2 * nx * sizeof(Cx<float>);
+    {
+        int npp = ny / 2, total = npp * nz;
+        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i);
+    }
+    DivideSpec none{};
+    const int txy = std::max(1, std::min(32, 4096 / ny));
+    const size_t smy = (size_t)2 * ny * txy * sizeof(Cx<float>);
+    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, -1, 0, none);
+    {
+        DivideSpec dv{d.kx2, d.ky2, d.kz2, lhs0, lhs1, (double)nx * ny * nz, 1};
+        const int txz = std::max(1, std::min(32, 4096 / nz));
+        const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<float>);
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 1, dv);
+    }
+    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, +1, 0, none);
+    {
+        int npp = ny / 2, total = npp * nz;
+        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, dst, base, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i);
+    }
+    return cudaGetLastError();
+}
+
+template <typename TS>
+cudaError_t solve_walls_f(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, n = ny + 2;
+    const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+    const size_t smx = (size_t)ppc * 2 * nx * sizeof(Cx<float>);
+    {
+        int npp = ny / 2, total = npp * nz;
+        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i);
+    }
+    DivideSpec none{};
+    const int txz = std::max(1, std::min(32, 4096 / nz));
+    const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<float>);
+    if (nz > 1)
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 0, none);
+    {
+        WallSpec w{d.kx2, d.kz2, d.ph.dt, d.ph.beta, d.ph.re, g.dy, (double)nx * nz, 0.0, sys};
+        const int tx = 32;
+        const size_t sm = (size_t)n * tx * (sizeof(Cx<float>) + sizeof(float));
+        k_wall_tdma<float><<<dim3((nxh + tx - 1) / tx, nz), 128, sm, s>>>(d.Hf, d.H2f, ny, nxh, tx, w);
+    }
+    if (nz > 1)
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, n), 256, smz, s>>>(d.H2f, nz, nxh * n, nxh, nxh, txz, d.twzf_r, d.twzf_i, +1, 0, none);
+    {
+        int npp = n / 2, total = npp * nz;
+        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.H2f, dst, base, nx, n, npp, nz, 0, g.sx, g.sy, d.twxf_r, d.twxf_i);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t init_kernels_mixed() {
+    const int big = 200 * 1024;
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_wall_tdma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    return cudaSuccess;
+}
+
+cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s) {
+    k_convert<double, float><<<(n + 255) / 256, 256, 0, s>>>(a, b, n);
+    return cudaGetLastError();
+}
+cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s) {
+    k_convert<float, double><<<(n + 255) / 256, 256, 0, s>>>(a, b, n);
+    return cudaGetLastError();
+}
+cudaError_t aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs, cudaStream_t s) {
+    k_aos_to_soa_f<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs);
+    return cudaGetLastError();
+}
+cudaError_t soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs, cudaStream_t s) {
+    k_soa_to_aos_f<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs);
+    return cudaGetLastError();
+}
+
+cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
+    F8_CUDA_RET(bc_field(d.U, d.g, BC_U, s));
+    F8_CUDA_RET(bc_field(d.V, d.g, BC_V, s));
+    F8_CUDA_RET(bc_field(d.W, d.g, BC_W, s));
+    F8_CUDA_RET(bc_field(d.P, d.g, BC_P, s));
+    long n = halo_count_m(d.g);
+    k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2);
+    k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2);
+    return cudaGetLastError();
+}
+
+cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s) {
+    const Geo &g = d.g;
+    cudaError_t e;
+    auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
+    mark(0);
+    if (o.polymer) {
+        dim3 blk(32, 4);
+        k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs);
+        mark(1);
+        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt);
+        std::swap(d.Cf, d.Cnf);
+        long n = halo_count_m(g);
+        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2);
+        if ((e = cudaGetLastError())) return e;
+    } else {
+        mark(1);
+    }
+    mark(2);
+    {
+        MomArgsF a{};
+        a.U = d.U; a.V = d.V; a.W = d.W; a.P = d.P; a.C = d.Cf; a.fpet = d.fpetf;
+        for (int c = 0; c < 3; ++c) { a.A0[c] = d.A0f[c]; a.T0[c] = d.T0f[c]; a.F[c] = d.Ff[c]; a.Q[c] = d.Qf[c]; }
+        a.cs = d.cs; a.polymer = o.polymer; a.ab2_first = o.ab2_first;
+        a.coef_t = (float)((1.0 - d.ph.beta) / (d.ph.re * d.ph.wi));
+        a.vis = (float)(d.ph.beta / d.ph.re);
+        a.dt = d.ph.dt;
+        dim3 blk(32, 8);
+        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g);
+        if ((e = cudaGetLastError())) return e;
+    }
+    mark(3);
+    if (o.ibm) {
+        IbmArgsF a{};
+        a.mu = d.mu; a.mv = d.mv; a.mcyl = d.mcyl; a.nm = d.nm;
+        const double *Us[3] = {d.U, d.V, d.W};
+        // z weights of the stencil offset k - n = -1, 0, 1 (marker plane at
+        // (n - 1/4) dZ; u, v at (k - 1/2) dZ, w at k dZ)
+        auto roma = [](double r) {
+            double ar = std::fabs(r);
+            if (ar < 1.5 && ar >= 0.5) return (5.0 - 3.0 * ar - std::sqrt(-3.0 * ((1 - ar) * (1 - ar)) + 1.0)) / 6.0;
+            if (ar < 0.5) return (1.0 + std::sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
+            return 0.0;
+        };
+        for (int c = 0; c < 3; ++c) {
+            a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
+            a.Uc[c] = Us[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c]; a.idx[c] = d.csr_idx[c];
+            a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
+            for (int dk = 0; dk < 3; ++dk) {
+                double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
+                a.wz[c][dk] = (float)roma(zg);
+            }
+        }
+        dim3 gi((d.nm + 127) / 128, g.nz, 3);
+        k_ibm_interp_f<<<gi, 128, 0, s>>>(a, g);
+        int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
+        if (maxact > 0) k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g);
+        if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
+        if ((e = cudaGetLastError())) return e;
+    }
+    mark(4);
+    // Helmholtz solves for the increments; U* = U^n + dU in FP64
+    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+    double *outs[3] = {d.Up, d.Vp, d.Wp};
+    const double *bases[3] = {d.U, d.V, d.W};
+    for (int c = 0; c < 3; ++c) {
+        if (!g.walls) e = solve_periodic_f<float>(d, d.Qf[c], outs[c], bases[c], 1.0, lhs1, s);
+        else e = solve_walls_f<float>(d, d.Qf[c], outs[c], bases[c], c == 1 ? SYS_V : SYS_U, s);
+        if (e) return e;
+    }
+    F8_CUDA_RET(bc_field(d.Up, g, BC_U, s));
+    F8_CUDA_RET(bc_field(d.Vp, g, BC_V, s));
+    F8_CUDA_RET(bc_field(d.Wp, g, BC_W, s));
+    mark(5);
+    // Poisson: FP32 solve + FP64 defect correction
+    F8_CUDA_RET(launch_poisson_rhs(d, d.Rp, s));
+    if (!g.walls) e = solve_periodic_f<double>(d, d.Rp, d.Phi, nullptr, 0.0, -1.0, s);
+    else e = solve_walls_f<double>(d, d.Rp, d.Phi, nullptr, SYS_P, s);
+    if (e) return e;
+    F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
+    for (int it = 0; it < d.defect_iters; ++it) {
+        dim3 blk(32, 8);
+        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g);
+        if (!g.walls) e = solve_periodic_f<double>(d, d.Rd, d.Phi, d.Phi, 0.0, -1.0, s);
+        else e = solve_walls_f<double>(d, d.Rd, d.Phi, d.Phi, SYS_P, s);
+        if (e) return e;
+        F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
+    }
+    mark(6);
+    F8_CUDA_RET(launch_march(d, s));
+    F8_CUDA_RET(bc_field(d.U, g, BC_U, s));
+    F8_CUDA_RET(bc_field(d.V, g, BC_V, s));
+    F8_CUDA_RET(bc_field(d.W, g, BC_W, s));
+    F8_CUDA_RET(bc_field(d.P, g, BC_P, s));
+    mark(7);
+    return cudaGetLastError();
+}
+
+}  // namespace f8

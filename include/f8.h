@@ -117,8 +117,9 @@ typedef struct f8_diag {
     double cfl;                 /* max(|u|dt/dX + |v|dt/dY + |w|dt/dZ)           */
     double trc_min, trc_max, trc_mean;
     double div_max;             /* max |div u| after the projection             */
-    long long newton_iters;     /* Newton iterations summed over cells, last step */
-    long long newton_unconverged; /* cells at newton_itrmax, last step           */
+    long long newton_iters;     /* Newton iterations summed over cells and the
+                                   steps of the last f8_step call               */
+    long long newton_unconverged; /* cell-steps that hit newton_itrmax, same span */
     int poisson_iters;          /* SOR iterations of the last step (-1: FFT)     */
     int nan_found;
 } f8_diag;

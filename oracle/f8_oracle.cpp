@@ -465,8 +465,8 @@ void lyapunov3(OCtx &c) {
             for (int i = 1; i <= NX; ++i)
                 for (int m = 0; m < 6; ++m) c.C[6 * c.hidx(i, j, k) + m] = c.C0[6 * c.hidx(i, j, k) + m];
     bc_c(c, c.C.data());
-    c.newton_iters = iters;
-    c.newton_unconv = unconv;
+    c.newton_iters += iters;
+    c.newton_unconv += unconv;
 }
 
 // fenep.f90:645-691.  C0 = f(C) C - I on every cell (interior and halo: the
@@ -658,8 +658,8 @@ void polymer2(OCtx &c) {
         for (int i = 1; i <= NX; ++i)
             for (int m = 0; m < 3; ++m) c.C[3 * c.hidx(i, j, k) + m] = Cn[3 * ((i - 1) + NX * (j - 1)) + m];
     bc_c(c, c.C.data());
-    c.newton_iters = iters;
-    c.newton_unconv = unconv;
+    c.newton_iters += iters;
+    c.newton_unconv += unconv;
 }
 
 // fenep_2d.f90:396-427
@@ -1317,7 +1317,6 @@ int do_step(OCtx &c, double *drag) {
         std::fill(c.Tx.begin(), c.Tx.end(), 0.0);
         std::fill(c.Ty.begin(), c.Ty.end(), 0.0);
         std::fill(c.Tz.begin(), c.Tz.end(), 0.0);
-        c.newton_iters = 0; c.newton_unconv = 0;
     } else if (d3) {
         c.mark(0);
         polymer_faces3(c);
@@ -1534,6 +1533,8 @@ int f8o_step(f8_ctx *ctx, int nsteps, double *drag) {
     if (!c.loaded) return F8_ERR_STATE;
     int worst = F8_OK;
     const int ncyl = (int)c.cyl.size();
+    c.newton_iters = 0;
+    c.newton_unconv = 0;
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 0; s < nsteps; ++s) {
         int st = do_step(c, drag ? drag + (size_t)s * ncyl * 3 : nullptr);

@@ -1,0 +1,75 @@
+"""FP32-mixed step vs the FP64 oracle (and the FP64 GPU step) through the C ABI.
+
+Gate (the benchmark's accuracy condition): drag within 1e-5 relative of the
+FP64 result; velocity within 1e-5 relative L2; the projected velocity is
+divergence-free to FP64 round-off thanks to the FP64 defect correction of
+the FP32 Poisson solve.
+"""
+from __future__ import annotations
+
+from dataclasses import replace
+
+import numpy as np
+import pytest
+
+from fortran8_gb300 import abi, configs
+from fortran8_gb300.solver import Solver
+
+from .conftest import interior, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+DRAG_TOL = 1e-5
+VEL_TOL = 1e-5
+
+
+def run(fns, w, steps, precision):
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=precision) as s:
+        s.load(configs.initial_state(w))
+        st, drag = s.step(steps)
+        return st, drag, s.store(), s.diagnostics()
+
+
+def drag_rel(dm, d64):
+    # relative to the largest drag magnitude of the history (the x force)
+    return float(np.max(np.abs(dm[..., 0] - d64[..., 0])) / np.max(np.abs(d64[..., 0])))
+
+
+@pytest.mark.parametrize("name,shape,steps", [("c3_channel", (32, 16, 16), 30), ("c2_3d", (16, 16, 16), 30),
+                                              ("c4_adjoint", (32, 16, 16), 20)])
+def test_mixed_matches_fp64_oracle(gpu, oracle, name, shape, steps):
+    w = configs.scaled(configs.WORKLOADS[name](), *shape)
+    sm, dm, om, diag = run(gpu, w, steps, abi.F8_MIXED)
+    so, do, oo, _ = run(oracle, w, steps, abi.F8_FP64)
+    assert sm == abi.F8_OK
+    assert drag_rel(dm, do) <= DRAG_TOL
+    for f in ("u", "v", "w"):
+        assert rel_l2(interior(om[f]), interior(oo[f])) <= VEL_TOL, f
+    assert rel_l2(interior(om["c"]), interior(oo["c"])) <= 1e-5
+    assert diag.div_max < 1e-9
+
+
+def test_mixed_matches_fp64_gpu_longer(gpu):
+    w = configs.scaled(configs.c3_channel(), 64, 32, 32)
+    _, dm, om, _ = run(gpu, w, 200, abi.F8_MIXED)
+    _, d64, o64, _ = run(gpu, w, 200, abi.F8_FP64)
+    assert drag_rel(dm, d64) <= DRAG_TOL
+    assert rel_l2(interior(om["u"]), interior(o64["u"])) <= VEL_TOL
+
+
+def test_mixed_newtonian_no_ibm(gpu, oracle):
+    w = configs.scaled(configs.c2_3d(), 16, 16, 16)
+    w = replace(w, cyls=(), phys=replace(w.phys, beta=1.0))
+    _, _, om, diag = run(gpu, w, 20, abi.F8_MIXED)
+    _, _, oo, _ = run(oracle, w, 20, abi.F8_FP64)
+    for f in ("u", "v", "w"):
+        assert rel_l2(interior(om[f]), interior(oo[f])) <= VEL_TOL, f
+
+
+def test_mixed_rejects_unbuilt_combinations(gpu):
+    w = configs.scaled(configs.c1_2d(), 32, 32, 1)
+    with pytest.raises(Exception):
+        Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED)
+    w3 = configs.scaled(configs.c3_channel(), 32, 16, 16)
+    with pytest.raises(Exception):
+        Solver(gpu, w3.grid, w3.phys, w3.cyls, precision=abi.F8_MIXED, poisson=abi.F8_POISSON_SOR)
