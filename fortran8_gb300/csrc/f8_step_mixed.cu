@@ -26,6 +26,34 @@ namespace {
 
 constexpr float TWO_PI_3F = 2.0943951023931955f;
 
+// Grid constants of the mixed kernels, computed once on the host in FP64 so
+// that no kernel divides in FP64 (FP64 division is slow on this part).
+struct MixConst {
+    float gx1, gx4, gy1, gy4, gz1, gz4;   // -dt/dX, -dt/(4dX), ... (velocity gradient)
+    float sx, sy, sz;                      // dt/(2dX) ... (upwind weights of Cstar)
+    float ix, iy, iz;                      // 1/dX ...
+    float ix2, iy2, iz2;                   // 1/dX^2 ...
+    double idx, idy, idz, idx2, idy2, idz2, idt;
+    double dtdx, dtdy, dtdz;              // dt/dX ...
+    double pc;                             // dt beta / (2 Re)
+};
+
+MixConst make_const(const Geo &g, const Phys &ph) {
+    MixConst c{};
+    c.gx1 = (float)(-ph.dt / g.dx); c.gx4 = (float)(-ph.dt / (4 * g.dx));
+    c.gy1 = (float)(-ph.dt / g.dy); c.gy4 = (float)(-ph.dt / (4 * g.dy));
+    c.gz1 = (float)(-ph.dt / g.dz); c.gz4 = (float)(-ph.dt / (4 * g.dz));
+    c.sx = (float)(ph.dt / (2 * g.dx)); c.sy = (float)(ph.dt / (2 * g.dy)); c.sz = (float)(ph.dt / (2 * g.dz));
+    c.ix = (float)(1.0 / g.dx); c.iy = (float)(1.0 / g.dy); c.iz = (float)(1.0 / g.dz);
+    c.ix2 = (float)(1.0 / (g.dx * g.dx)); c.iy2 = (float)(1.0 / (g.dy * g.dy)); c.iz2 = (float)(1.0 / (g.dz * g.dz));
+    c.idx = 1.0 / g.dx; c.idy = 1.0 / g.dy; c.idz = 1.0 / g.dz;
+    c.idx2 = 1.0 / (g.dx * g.dx); c.idy2 = 1.0 / (g.dy * g.dy); c.idz2 = 1.0 / (g.dz * g.dz);
+    c.idt = 1.0 / ph.dt;
+    c.dtdx = ph.dt / g.dx; c.dtdy = ph.dt / g.dy; c.dtdz = ph.dt / g.dz;
+    c.pc = ph.dt * ph.beta / ph.re / 2.0;
+    return c;
+}
+
 __host__ __device__ inline long halo_count_m(const Geo &g) {
     return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
 }
@@ -180,7 +208,7 @@ __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, u
 __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
                                                    float *__restrict__ fpet, const uint8_t *__restrict__ codes,
                                                    const double *__restrict__ U, const double *__restrict__ V,
-                                                   const double *__restrict__ W, Geo g, Phys ph, int cs,
+                                                   const double *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
                                                    StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -189,7 +217,6 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
     unsigned long long my_itr = 0, my_unconv = 0;
     if (active) {
         const int h = hix(g, i, j, k);
-        const float dt = (float)ph.dt, dX = (float)g.dx, dY = (float)g.dy, dZ = (float)g.dz;
         const int cself = codes[qix(g, i, j, k)];
         const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
         const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
@@ -207,7 +234,7 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
         const float u1 = (float)U[hix(g, i - 1, j, k)], u2 = (float)U[h];
         const float v1 = (float)V[hix(g, i, j - 1, k)], v2 = (float)V[h];
         const float w1 = (float)W[hix(g, i, j, k - 1)], w2 = (float)W[h];
-        const float cxs = dt / (2.0f * dX), cys = dt / (2.0f * dY), czs = dt / (2.0f * dZ);
+        const float cxs = mc.sx, cys = mc.sy, czs = mc.sz;
         const float s1 = (-u2 + fabsf(u2)) * cxs, s2 = 1.0f / 6 + (-u2 - fabsf(u2)) * cxs;
         const float s3 = 1.0f / 6 + (u1 - fabsf(u1)) * cxs, s4 = (u1 + fabsf(u1)) * cxs;
         const float s5 = (-v2 + fabsf(v2)) * cys, s6 = 1.0f / 6 + (-v2 - fabsf(v2)) * cys;
@@ -236,21 +263,22 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
         }
         const float dtwi = (float)(ph.dt / ph.wi);
         b[0] += dtwi; b[3] += dtwi; b[5] += dtwi;
-        // velocity gradient (fenep.f90:541-550), differences in FP64
-        auto U_ = [&](int a, int bb, int cc) { return U[hix(g, a, bb, cc)]; };
-        auto V_ = [&](int a, int bb, int cc) { return V[hix(g, a, bb, cc)]; };
-        auto W_ = [&](int a, int bb, int cc) { return W[hix(g, a, bb, cc)]; };
-        const double ddt = ph.dt;
+        // velocity gradient (fenep.f90:541-550) in FP32 with host-side
+        // constants -dt/dX, -dt/(4 dX), ...
+        auto U_ = [&](int a, int bb, int cc) { return (float)U[hix(g, a, bb, cc)]; };
+        auto V_ = [&](int a, int bb, int cc) { return (float)V[hix(g, a, bb, cc)]; };
+        auto W_ = [&](int a, int bb, int cc) { return (float)W[hix(g, a, bb, cc)]; };
+        const MixConst &q = mc;
         float A0[3][3];
-        A0[0][0] = (float)(-ddt * (U_(i, j, k) - U_(i - 1, j, k)) / g.dx);
-        A0[0][1] = (float)(-ddt * (-V_(i - 1, j - 1, k) + V_(i + 1, j - 1, k) - V_(i - 1, j, k) + V_(i + 1, j, k)) / (4 * g.dx));
-        A0[0][2] = (float)(-ddt * (-W_(i - 1, j, k - 1) + W_(i + 1, j, k - 1) - W_(i - 1, j, k) + W_(i + 1, j, k)) / (4 * g.dx));
-        A0[1][0] = (float)(-ddt * (-U_(i - 1, j - 1, k) - U_(i, j - 1, k) + U_(i - 1, j + 1, k) + U_(i, j + 1, k)) / (4 * g.dy));
-        A0[1][1] = (float)(-ddt * (V_(i, j, k) - V_(i, j - 1, k)) / g.dy);
-        A0[1][2] = (float)(-ddt * (-W_(i, j - 1, k - 1) + W_(i, j + 1, k - 1) - W_(i, j - 1, k) + W_(i, j + 1, k)) / (4 * g.dy));
-        A0[2][0] = (float)(-ddt * (-U_(i - 1, j, k - 1) - U_(i, j, k - 1) + U_(i - 1, j, k + 1) + U_(i, j, k + 1)) / (4 * g.dz));
-        A0[2][1] = (float)(-ddt * (-V_(i, j - 1, k - 1) - V_(i, j, k - 1) + V_(i, j - 1, k + 1) + V_(i, j, k + 1)) / (4 * g.dz));
-        A0[2][2] = (float)(-ddt * (W_(i, j, k) - W_(i, j, k - 1)) / g.dz);
+        A0[0][0] = q.gx1 * (U_(i, j, k) - U_(i - 1, j, k));
+        A0[0][1] = q.gx4 * (-V_(i - 1, j - 1, k) + V_(i + 1, j - 1, k) - V_(i - 1, j, k) + V_(i + 1, j, k));
+        A0[0][2] = q.gx4 * (-W_(i - 1, j, k - 1) + W_(i + 1, j, k - 1) - W_(i - 1, j, k) + W_(i + 1, j, k));
+        A0[1][0] = q.gy4 * (-U_(i - 1, j - 1, k) - U_(i, j - 1, k) + U_(i - 1, j + 1, k) + U_(i, j + 1, k));
+        A0[1][1] = q.gy1 * (V_(i, j, k) - V_(i, j - 1, k));
+        A0[1][2] = q.gy4 * (-W_(i, j - 1, k - 1) + W_(i, j + 1, k - 1) - W_(i, j - 1, k) + W_(i, j + 1, k));
+        A0[2][0] = q.gz4 * (-U_(i - 1, j, k - 1) - U_(i, j, k - 1) + U_(i - 1, j, k + 1) + U_(i, j, k + 1));
+        A0[2][1] = q.gz4 * (-V_(i, j - 1, k - 1) - V_(i, j, k - 1) + V_(i, j - 1, k + 1) + V_(i, j, k + 1));
+        A0[2][2] = q.gz1 * (W_(i, j, k) - W_(i, j, k - 1));
         // A = transpose(A0) (fenep.f90:550)
         const float a00 = A0[0][0], a01 = A0[1][0], a02 = A0[2][0];
         const float a10 = A0[0][1], a11 = A0[1][1], a12 = A0[2][1];
@@ -333,23 +361,23 @@ struct MomArgsF {
     double dt;
 };
 
-__global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g) {
+__global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
-    const float dX = (float)g.dx, dY = (float)g.dy, dZ = (float)g.dz;
     const int o = qix(g, i, j, k), h = hix(g, i, j, k);
     const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    const float ix = mc.ix, iy = mc.iy, iz = mc.iz;
     float tx = 0.f, ty = 0.f, tz = 0.f;
     if (a.polymer) {
+        // polymer_stress (fenep.f90:645-691) with C0 = f(C) C - I on the fly
         const int cs = a.cs;
         const float *C = a.C, *fp = a.fpet;
         auto c0 = [&](int m, int hh) {
             const float e = (m == 1 || m == 4 || m == 6) ? 1.0f : 0.0f;
             return fp[hh] * C[(size_t)(m - 1) * cs + hh] - e;
         };
-        const float ix = 1.0f / dX, iy = 1.0f / dY, iz = 1.0f / dZ;
         const float sx = (c0(1, h + ox) - c0(1, h)) * ix
                        + (-c0(2, h - oy) - c0(2, h + ox - oy) + c0(2, h + oy) + c0(2, h + ox + oy)) * (0.25f * iy)
                        + (-c0(3, h - oz) - c0(3, h + ox - oz) + c0(3, h + oz) + c0(3, h + ox + oz)) * (0.25f * iz);
@@ -365,38 +393,39 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g) {
     auto u = [&](int hh) { return (float)U[hh]; };
     auto v = [&](int hh) { return (float)V[hh]; };
     auto w = [&](int hh) { return (float)W[hh]; };
-    const float ix = 1.0f / dX, iy = 1.0f / dY, iz = 1.0f / dZ;
     // convection (fenep.f90:694-734), divergence form
     const float uc = u(h), vc = v(h), wc = w(h);
-    float t1 = 0.5f * (u(h - ox) + uc), t2 = 0.5f * (uc + u(h + ox));
+    const float uxm = u(h - ox), uxp = u(h + ox), uym = u(h - oy), uyp = u(h + oy), uzm = u(h - oz), uzp = u(h + oz);
+    const float vxm = v(h - ox), vxp = v(h + ox), vym = v(h - oy), vyp = v(h + oy), vzm = v(h - oz), vzp = v(h + oz);
+    const float wxm = w(h - ox), wxp = w(h + ox), wym = w(h - oy), wyp = w(h + oy), wzm = w(h - oz), wzp = w(h + oz);
+    float t1 = 0.5f * (uxm + uc), t2 = 0.5f * (uc + uxp);
     float ax = (t2 * t2 - t1 * t1) * ix
-             + (0.25f * (v(h) + v(h + ox)) * (uc + u(h + oy)) - 0.25f * (v(h - oy) + v(h + ox - oy)) * (u(h - oy) + uc)) * iy
-             + (0.25f * (w(h) + w(h + ox)) * (uc + u(h + oz)) - 0.25f * (w(h - oz) + w(h + ox - oz)) * (u(h - oz) + uc)) * iz;
-    float t3 = 0.5f * (v(h - oy) + vc), t4 = 0.5f * (vc + v(h + oy));
-    float ay = (0.25f * (uc + u(h + oy)) * (vc + v(h + ox)) - 0.25f * (u(h - ox) + u(h - ox + oy)) * (v(h - ox) + vc)) * ix
+             + (0.25f * (vc + v(h + ox)) * (uc + uyp) - 0.25f * (vym + v(h + ox - oy)) * (uym + uc)) * iy
+             + (0.25f * (wc + w(h + ox)) * (uc + uzp) - 0.25f * (wzm + w(h + ox - oz)) * (uzm + uc)) * iz;
+    float t3 = 0.5f * (vym + vc), t4 = 0.5f * (vc + vyp);
+    float ay = (0.25f * (uc + uyp) * (vc + vxp) - 0.25f * (uxm + u(h - ox + oy)) * (vxm + vc)) * ix
              + (t4 * t4 - t3 * t3) * iy
-             + (0.25f * (w(h) + w(h + oy)) * (vc + v(h + oz)) - 0.25f * (w(h - oz) + w(h + oy - oz)) * (v(h - oz) + vc)) * iz;
-    float t5 = 0.5f * (w(h - oz) + wc), t6 = 0.5f * (wc + w(h + oz));
-    float az = (0.25f * (uc + u(h + oz)) * (wc + w(h + ox)) - 0.25f * (u(h - ox) + u(h - ox + oz)) * (w(h - ox) + wc)) * ix
-             + (0.25f * (vc + v(h + oz)) * (wc + w(h + oy)) - 0.25f * (v(h - oy) + v(h - oy + oz)) * (w(h - oy) + wc)) * iy
+             + (0.25f * (wc + w(h + oy)) * (vc + vzp) - 0.25f * (wzm + w(h + oy - oz)) * (vzm + vc)) * iz;
+    float t5 = 0.5f * (wzm + wc), t6 = 0.5f * (wc + wzp);
+    float az = (0.25f * (uc + uzp) * (wc + wxp) - 0.25f * (uxm + u(h - ox + oz)) * (wxm + wc)) * ix
+             + (0.25f * (vc + vzp) * (wc + wyp) - 0.25f * (vym + v(h - oy + oz)) * (wym + wc)) * iy
              + (t6 * t6 - t5 * t5) * iz;
-    // viscous (fenep.f90:736-770): second differences in FP64, then FP32
-    auto lap = [&](const double *F) {
-        const double c = F[h];
-        return (float)((F[h - ox] - 2.0 * c + F[h + ox]) * (1.0 / (g.dx * g.dx)) + (F[h - oy] - 2.0 * c + F[h + oy]) * (1.0 / (g.dy * g.dy))
-                       + (F[h - oz] - 2.0 * c + F[h + oz]) * (1.0 / (g.dz * g.dz)));
-    };
+    // viscous (fenep.f90:736-770)
+    const float bx = (uxm - 2.0f * uc + uxp) * mc.ix2 + (uym - 2.0f * uc + uyp) * mc.iy2 + (uzm - 2.0f * uc + uzp) * mc.iz2;
+    const float by = (vxm - 2.0f * vc + vxp) * mc.ix2 + (vym - 2.0f * vc + vyp) * mc.iy2 + (vzm - 2.0f * vc + vzp) * mc.iz2;
+    const float bz = (wxm - 2.0f * wc + wxp) * mc.ix2 + (wym - 2.0f * wc + wyp) * mc.iy2 + (wzm - 2.0f * wc + wzp) * mc.iz2;
     const float A[3] = {-ax, -ay, -az};
-    const float B[3] = {a.vis * lap(U), a.vis * lap(V), a.vis * lap(W)};
+    const float B[3] = {a.vis * bx, a.vis * by, a.vis * bz};
     const float T[3] = {tx, ty, tz};
     const int hp[3] = {h + ox, h + oy, h + oz};
-    const double dd[3] = {g.dx, g.dy, g.dz};
+    const float id[3] = {ix, iy, iz};
+    const double pc0 = a.P[h];
     const float dt = (float)a.dt;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float a0 = a.ab2_first ? A[c] : a.A0[c][o];
         const float t0 = a.ab2_first ? T[c] : a.T0[c][o];
-        const float gp = (float)(-(a.P[hp[c]] - a.P[h]) / dd[c]);
+        const float gp = -(float)(a.P[hp[c]] - pc0) * id[c];   // pressure difference in FP64
         const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + a.F[c][o];
         a.Q[c][o] = dt * r;
         a.A0[c][o] = A[c];
@@ -502,8 +531,21 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
 }
 
 // ---------------------------------------------------------------------------
-// Poisson defect: r = rhs - L_h Phi (FP64), Phi with Neumann / periodic halo.
-__global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g) {
+// FP64 parts of the pressure solve and the projection, with reciprocal
+// multiplies instead of divisions.
+//   rhs = div(U*) / dt (fenep.f90:1547-1555)
+__global__ void k_poisson_rhs_m(const double *Up, const double *Vp, const double *Wp, double *Q, Geo g, MixConst mc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    const double s = (Up[h] - Up[h - 1]) * mc.idx + (Vp[h] - Vp[h - g.sx]) * mc.idy + (Wp[h] - Wp[h - g.sx * g.sy]) * mc.idz;
+    Q[qix(g, i, j, k)] = s * mc.idt;
+}
+
+// defect r = rhs - L_h Phi (Phi with Neumann / periodic halo)
+__global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g, MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -511,10 +553,29 @@ __global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g)
     const int h = hix(g, i, j, k);
     const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
     const double c = Phi[h];
-    double lap = (Phi[h - ox] - 2.0 * c + Phi[h + ox]) / (g.dx * g.dx) + (Phi[h - oy] - 2.0 * c + Phi[h + oy]) / (g.dy * g.dy);
-    if (g.dim == 3) lap += (Phi[h - oz] - 2.0 * c + Phi[h + oz]) / (g.dz * g.dz);
+    const double lap = (Phi[h - ox] - 2.0 * c + Phi[h + ox]) * mc.idx2 + (Phi[h - oy] - 2.0 * c + Phi[h + oy]) * mc.idy2
+                     + (Phi[h - oz] - 2.0 * c + Phi[h + oz]) * mc.idz2;
     const int o = qix(g, i, j, k);
     r[o] = rhs[o] - lap;
+}
+
+// projection and SMAC pressure update (fenep.f90:1562-1604)
+__global__ void k_march_m(double *U, double *V, double *W, double *P, const double *Up, const double *Vp,
+                          const double *Wp, const double *Phi, Geo g, MixConst mc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    const double ph = Phi[h];
+    const double px = Phi[h + ox], py = Phi[h + oy], pz = Phi[h + oz];
+    U[h] = Up[h] - mc.dtdx * (px - ph);
+    V[h] = Vp[h] - mc.dtdy * (py - ph);
+    W[h] = Wp[h] - mc.dtdz * (pz - ph);
+    const float lap = (float)(Phi[h - ox] - 2.0 * ph + px) * (float)mc.idx2 + (float)(Phi[h - oy] - 2.0 * ph + py) * (float)mc.idy2
+                    + (float)(Phi[h - oz] - 2.0 * ph + pz) * (float)mc.idz2;
+    P[h] = P[h] + ph - (double)((float)mc.pc * lap);
 }
 
 template <typename A, typename B>
@@ -642,13 +703,14 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s) {
     const Geo &g = d.g;
     cudaError_t e;
+    const MixConst mc = make_const(g, d.ph);
     auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
     mark(0);
     if (o.polymer) {
         dim3 blk(32, 4);
         k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs);
         mark(1);
-        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt);
+        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.U, d.V, d.W, g, d.ph, mc, d.cs, d.cnt);
         std::swap(d.Cf, d.Cnf);
         long n = halo_count_m(g);
         k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2);
@@ -666,7 +728,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         a.vis = (float)(d.ph.beta / d.ph.re);
         a.dt = d.ph.dt;
         dim3 blk(32, 8);
-        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g);
+        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc);
         if ((e = cudaGetLastError())) return e;
     }
     mark(3);
@@ -713,21 +775,27 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     F8_CUDA_RET(bc_field(d.Wp, g, BC_W, s));
     mark(5);
     // Poisson: FP32 solve + FP64 defect correction
-    F8_CUDA_RET(launch_poisson_rhs(d, d.Rp, s));
+    {
+        dim3 blk(32, 8);
+        k_poisson_rhs_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Rp, g, mc);
+    }
     if (!g.walls) e = solve_periodic_f<double>(d, d.Rp, d.Phi, nullptr, 0.0, -1.0, s);
     else e = solve_walls_f<double>(d, d.Rp, d.Phi, nullptr, SYS_P, s);
     if (e) return e;
     F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
     for (int it = 0; it < d.defect_iters; ++it) {
         dim3 blk(32, 8);
-        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g);
+        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g, mc);
         if (!g.walls) e = solve_periodic_f<double>(d, d.Rd, d.Phi, d.Phi, 0.0, -1.0, s);
         else e = solve_walls_f<double>(d, d.Rd, d.Phi, d.Phi, SYS_P, s);
         if (e) return e;
         F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
     }
     mark(6);
-    F8_CUDA_RET(launch_march(d, s));
+    {
+        dim3 blk(32, 8);
+        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, g, mc);
+    }
     F8_CUDA_RET(bc_field(d.U, g, BC_U, s));
     F8_CUDA_RET(bc_field(d.V, g, BC_V, s));
     F8_CUDA_RET(bc_field(d.W, g, BC_W, s));
