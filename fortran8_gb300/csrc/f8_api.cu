@@ -233,6 +233,9 @@ int setup(f8_ctx *c) {
         API_CUDA(c, c->alloc(&d.H2, nspec));
     } else {
         API_CUDA(c, c->alloc(&d.Cf, cs * d.ncomp));
+        API_CUDA(c, c->alloc(&d.Uf, cs));
+        API_CUDA(c, c->alloc(&d.Vf, cs));
+        API_CUDA(c, c->alloc(&d.Wf, cs));
         API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
         API_CUDA(c, c->alloc(&d.fpetf, cs));
         for (int q = 0; q < 3; ++q) {
@@ -276,6 +279,18 @@ int setup(f8_ctx *c) {
     if (int st = upload(c, &d.kx2, kx2)) return st;
     if (int st = upload(c, &d.ky2, ky2)) return st;
     if (int st = upload(c, &d.kz2, kz2)) return st;
+    if (mixed) {
+        if (int st = upload_f(c, &d.kx2f, kx2)) return st;
+        if (int st = upload_f(c, &d.ky2f, ky2)) return st;
+        if (int st = upload_f(c, &d.kz2f, kz2)) return st;
+        // shared memory of one (z, y) plane: walls 12 B x (NY+2 | 1) x NZ,
+        // periodic 8 B x (NY+1) x NZ; opt-in limit 227 KB
+        int dev = 0, optin = 0;
+        API_CUDA(c, cudaGetDevice(&dev));
+        API_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const size_t need = g.walls ? (size_t)12 * ((g.ny + 2) | 1) * g.nz : (size_t)8 * (g.ny + 1) * g.nz;
+        d.fused_planes = need <= (size_t)optin ? 1 : 0;
+    }
     // IBM markers and the gather lists of the spreading kernel
     d.ncyl = (int)c->cyl.size();
     if (!c->cyl.empty()) {
@@ -293,6 +308,17 @@ int setup(f8_ctx *c) {
         if (int st = upload(c, &d.mv, mv)) return st;
         API_CUDA(c, c->alloc(&d.mcyl, nm));
         API_CUDA(c, cudaMemcpyAsync(d.mcyl, mc.data(), nm * sizeof(int), cudaMemcpyHostToDevice, c->s));
+        {
+            std::vector<int> perm, off(c->cyl.size() + 1, 0);
+            for (size_t l = 0; l < c->cyl.size(); ++l) {
+                for (int m = 0; m < nm; ++m)
+                    if (mc[m] == (int)l) perm.push_back(m);
+                off[l + 1] = (int)perm.size();
+            }
+            if (int st = upload_i(c, &d.mperm, perm)) return st;
+            if (int st = upload_i(c, &d.moff, off)) return st;
+            API_CUDA(c, c->alloc(&d.dragpart, c->cyl.size() * (size_t)g.nz * 3));
+        }
         const int ncomp = g.dim == 3 ? 3 : 2;
         const int ncol = g.sx * g.sy;
         for (int comp = 0; comp < 3; ++comp) {

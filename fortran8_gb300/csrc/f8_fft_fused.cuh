@@ -1,0 +1,294 @@
+// f8_fft_fused.cuh — FP32 spectral solves of the mixed-precision path with the
+// whole (z, y) plane of one x-wavenumber resident in shared memory.
+//
+// Spectrum layout S[kx][k][j] (complex float), j contiguous, LJ values per
+// (kx, k) line: LJ = NY for periodic y, NY + 2 for walls (rows 0 and NY+1 are
+// the ghost rows of the wall systems, fenep_2d.f90:1222-1238).
+//
+//   k_xfwd_t   real rows -> S: two rows per complex FFT of length NX (the
+//              same pairing as the FP64 kernels), transposed through shared
+//              memory so that each kx receives RB consecutive rows.
+//   k_plane_*  one CTA per kx: in-place radix-2 transforms along z (and y when
+//              periodic), the spectral divide (fft_solve, fenep.f90:1400-1428)
+//              or the Thomas solve along y (tdma, fenep_2d.f90:1145-1177), and
+//              the inverse transforms.  Forward transforms are decimation in
+//              time (bit-reversed load), inverse ones decimation in frequency
+//              (bit-reversed store), so no reordering pass is needed.
+//   k_xinv_t   S -> real rows, optionally added to an FP64 base field.
+#pragma once
+#include "f8_common.cuh"
+#include "f8_fft.cuh"
+
+namespace f8 {
+
+__device__ inline int bitrev(int v, int lg) { return lg ? (int)(__brev((unsigned)v) >> (32 - lg)) : 0; }
+
+// ---------------------------------------------------------------------------
+// x forward, transposing.  Block b handles RB rows (RB/2 pairs) of plane k.
+template <typename TS>
+__global__ void k_xfwd_t(const TS *__restrict__ src, float2 *__restrict__ S, int nx, int ny, int nz, int rb, int lj,
+                         int joff, const float *__restrict__ twr, const float *__restrict__ twi) {
+    extern __shared__ unsigned char smem_raw[];
+    Cx<float> *sm = reinterpret_cast<Cx<float> *>(smem_raw);
+    const int half = nx >> 1, nxh = half + 1;
+    const int npair = rb >> 1;
+    const int p = threadIdx.x / half, t = threadIdx.x % half;
+    const int blocks_per_plane = (ny + rb - 1) / rb;
+    const int k = blockIdx.x / blocks_per_plane;
+    const int r0 = (blockIdx.x % blocks_per_plane) * rb;       // first row (0-based) of the block
+    const int nrows = min(rb, ny - r0);
+    const bool active = p < npair && 2 * p < nrows;
+    Cx<float> *x = sm + (size_t)p * 2 * nx, *y = x + nx;
+    if (active) {
+        const TS *ra = src + (size_t)nx * ((size_t)(r0 + 2 * p) + (size_t)ny * k);
+        const TS *rbp = ra + nx;
+        for (int e = t; e < nx; e += half) { x[e].r = (float)ra[e]; x[e].i = (float)rbp[e]; }
+    }
+    __syncthreads();
+    for (int ns = 1; ns < nx; ns *= 2) {
+        if (active) stockham_stage(x, y, nx, ns, t, twr, twi, -1);
+        __syncthreads();
+        Cx<float> *tmp = x; x = y; y = tmp;
+    }
+    // unpack the two real spectra of each pair into a [kx][row] tile; the
+    // result of pair p is in buffer x (the same buffer index for all pairs)
+    const bool res_in_first = ((__ffs(nx) - 1) % 2) == 0;  // log2(nx) even -> back in the first buffer
+    float2 *tile = reinterpret_cast<float2 *>(sm + (size_t)npair * 2 * nx);
+    if (active) {
+        const Cx<float> *z = sm + (size_t)p * 2 * nx + (res_in_first ? 0 : nx);
+        for (int kx = t; kx < nxh; kx += half) {
+            const int m = (nx - kx) % nx;
+            const Cx<float> zk = z[kx], zm = z[m];
+            tile[(size_t)kx * rb + 2 * p] = make_float2((zk.r + zm.r) * 0.5f, (zk.i - zm.i) * 0.5f);
+            tile[(size_t)kx * rb + 2 * p + 1] = make_float2((zk.i + zm.i) * 0.5f, (zm.r - zk.r) * 0.5f);
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nxh * rb; q += blockDim.x) {
+        const int kx = q / rb, r = q % rb;
+        if (r < nrows) S[((size_t)kx * nz + k) * lj + (r0 + r + 1 + joff)] = tile[(size_t)kx * rb + r];
+    }
+}
+
+// x inverse, transposing: rows j = jlo .. jlo+nrow-1 of S (S row index
+// j + joff2) become real rows j of the halo-layout dst (x at 1..nx), added to
+// base when given.
+template <typename TO>
+__global__ void k_xinv_t(const float2 *__restrict__ S, TO *dst, const TO *base, int nx, int nrow, int jlo, int nz,
+                         int rb, int lj, int joff2, int sx, int sy, const float *__restrict__ twr,
+                         const float *__restrict__ twi) {
+    extern __shared__ unsigned char smem_raw[];
+    Cx<float> *sm = reinterpret_cast<Cx<float> *>(smem_raw);
+    const int half = nx >> 1, nxh = half + 1;
+    const int npair = rb >> 1;
+    const int blocks_per_plane = (nrow + rb - 1) / rb;
+    const int k = blockIdx.x / blocks_per_plane;
+    const int r0 = (blockIdx.x % blocks_per_plane) * rb;
+    const int nrows = min(rb, nrow - r0);
+    float2 *tile = reinterpret_cast<float2 *>(sm + (size_t)npair * 2 * nx);
+    for (int q = threadIdx.x; q < nxh * rb; q += blockDim.x) {
+        const int kx = q / rb, r = q % rb;
+        tile[q] = r < nrows ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int p = threadIdx.x / half, t = threadIdx.x % half;
+    const bool active = p < npair && 2 * p < nrows;
+    Cx<float> *x = sm + (size_t)p * 2 * nx, *y = x + nx;
+    if (active) {
+        for (int e = t; e < nx; e += half) {
+            float ar, ai, br, bi;
+            if (e <= half) {
+                const float2 A = tile[(size_t)e * rb + 2 * p], B = tile[(size_t)e * rb + 2 * p + 1];
+                ar = A.x; ai = A.y; br = B.x; bi = B.y;
+                x[e].r = ar - bi; x[e].i = ai + br;
+            } else {
+                const int m = nx - e;
+                const float2 A = tile[(size_t)m * rb + 2 * p], B = tile[(size_t)m * rb + 2 * p + 1];
+                ar = A.x; ai = A.y; br = B.x; bi = B.y;
+                x[e].r = ar + bi; x[e].i = br - ai;
+            }
+        }
+    }
+    __syncthreads();
+    for (int ns = 1; ns < nx; ns *= 2) {
+        if (active) stockham_stage(x, y, nx, ns, t, twr, twi, +1);
+        __syncthreads();
+        Cx<float> *tmp = x; x = y; y = tmp;
+    }
+    if (!active) return;
+    const size_t oa = 1 + (size_t)sx * ((size_t)(jlo + r0 + 2 * p) + (size_t)sy * (k + 1));
+    TO *ra = dst + oa, *rbp = ra + sx;
+    if (base) {
+        const TO *ba = base + oa, *bb = ba + sx;
+        for (int e = t; e < nx; e += half) { ra[e] = ba[e] + TO(x[e].r); rbp[e] = bb[e] + TO(x[e].i); }
+    } else {
+        for (int e = t; e < nx; e += half) { ra[e] = TO(x[e].r); rbp[e] = TO(x[e].i); }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// In-place radix-2 stages over nlines lines of length n held in shared memory
+// (element e of line l at P[l*lstride_l + e*estride]).
+__device__ inline void dit_lines(float2 *P, int n, int lg, int nlines, int lstride, int estride, const float *twr,
+                                 const float *twi, float sign) {
+    const int half = n >> 1;
+    for (int m = 1; m < n; m <<= 1) {
+        const int tws = n / (2 * m);
+        for (int q = threadIdx.x; q < nlines * half; q += blockDim.x) {
+            // consecutive threads take consecutive addresses: along the line
+            // when it is contiguous, across lines otherwise
+            const int l = estride == 1 ? q / half : q % nlines;
+            const int b = estride == 1 ? q % half : q / nlines;
+            const int pos = b % m, grp = b / m;
+            const int i0 = grp * 2 * m + pos;
+            float2 *base = P + (size_t)l * lstride;
+            const float wr = twr[pos * tws], wi = sign * twi[pos * tws];
+            const float2 a = base[(size_t)i0 * estride], c = base[(size_t)(i0 + m) * estride];
+            const float tr = c.x * wr - c.y * wi, ti = c.x * wi + c.y * wr;
+            base[(size_t)i0 * estride] = make_float2(a.x + tr, a.y + ti);
+            base[(size_t)(i0 + m) * estride] = make_float2(a.x - tr, a.y - ti);
+        }
+        __syncthreads();
+    }
+    (void)lg;
+}
+
+__device__ inline void dif_lines(float2 *P, int n, int nlines, int lstride, int estride, const float *twr,
+                                 const float *twi, float sign) {
+    const int half = n >> 1;
+    for (int m = half; m >= 1; m >>= 1) {
+        const int tws = n / (2 * m);
+        for (int q = threadIdx.x; q < nlines * half; q += blockDim.x) {
+            const int l = estride == 1 ? q / half : q % nlines;
+            const int b = estride == 1 ? q % half : q / nlines;
+            const int pos = b % m, grp = b / m;
+            const int i0 = grp * 2 * m + pos;
+            float2 *base = P + (size_t)l * lstride;
+            const float wr = twr[pos * tws], wi = sign * twi[pos * tws];
+            const float2 a = base[(size_t)i0 * estride], c = base[(size_t)(i0 + m) * estride];
+            const float dr = a.x - c.x, di = a.y - c.y;
+            base[(size_t)i0 * estride] = make_float2(a.x + c.x, a.y + c.y);
+            base[(size_t)(i0 + m) * estride] = make_float2(dr * wr - di * wi, dr * wi + di * wr);
+        }
+        __syncthreads();
+    }
+}
+
+// Periodic y and z: forward 2-D transform, divide by ntot * LHS (LHS = lhs0 +
+// lhs1 (kx2 + ky2 + kz2); zero where |LHS| < 1e-16), inverse transform.
+struct PlaneSpec {
+    const float *kx2, *ky2, *kz2;   // modified wavenumbers (FP32 copies)
+    float lhs0, lhs1, inv_ntot;
+    // walls: row coefficients of the y systems (see k_plane_walls)
+    float ai_base, bc;        // interior a = ai_base + kap * lam; b = c = bc
+    float kap;                // dt beta / (2 Re) (Helmholtz) or -1 (Poisson: a = -(lam + 2/dy^2))
+    int sys;                  // WallSys
+    float nxz_inv;            // 1 / (NX NZ)
+};
+
+__global__ void k_plane_periodic(float2 *S, int ny, int nz, int lgy, int lgz, const float *twyr, const float *twyi,
+                                 const float *twzr, const float *twzi, PlaneSpec ps) {
+    extern __shared__ unsigned char smem_raw[];
+    const int nys = ny + 1;                              // odd shared-memory row stride
+    float2 *P = reinterpret_cast<float2 *>(smem_raw);    // [k][j], bit-reversed in both on load
+    const int kx = blockIdx.x;
+    float2 *Sp = S + (size_t)kx * nz * ny;
+    for (int q = threadIdx.x; q < ny * nz; q += blockDim.x) {
+        const int k = q / ny, j = q % ny;
+        P[(size_t)bitrev(k, lgz) * nys + bitrev(j, lgy)] = Sp[q];
+    }
+    __syncthreads();
+    dit_lines(P, ny, lgy, nz, nys, 1, twyr, twyi, 1.0f);     // along y (lines k)
+    dit_lines(P, nz, lgz, ny, 1, nys, twzr, twzi, 1.0f);     // along z (lines j)
+    const float k2x = ps.kx2[kx];
+    for (int q = threadIdx.x; q < ny * nz; q += blockDim.x) {
+        const int k = q / ny, j = q % ny;
+        const float lhs = ps.lhs0 + ps.lhs1 * (k2x + ps.ky2[j] + ps.kz2[k]);
+        const float sc = fabsf(lhs) < 1.0e-16f ? 0.0f : ps.inv_ntot / lhs;
+        const float2 v = P[(size_t)k * nys + j];
+        P[(size_t)k * nys + j] = make_float2(v.x * sc, v.y * sc);
+    }
+    __syncthreads();
+    dif_lines(P, nz, ny, 1, nys, twzr, twzi, -1.0f);
+    dif_lines(P, ny, nz, nys, 1, twyr, twyi, -1.0f);
+    for (int q = threadIdx.x; q < ny * nz; q += blockDim.x) {
+        const int k = q / ny, j = q % ny;
+        Sp[q] = P[(size_t)bitrev(k, lgz) * nys + bitrev(j, lgy)];
+    }
+}
+
+// Walls in y: forward z transform of rows 1..NY, Thomas solve along y of each
+// kz over rows 0..NY+1 with the boundary rows of the system (homogeneous:
+// the mixed path solves for increments), inverse z transform of all rows.
+__global__ void k_plane_walls(float2 *S, int ny, int nz, int lgz, const float *twzr, const float *twzi, PlaneSpec ps) {
+    extern __shared__ unsigned char smem_raw[];
+    const int lj = ny + 2;
+    const int ljs = lj | 1;                                            // odd shared-memory row stride
+    float2 *P = reinterpret_cast<float2 *>(smem_raw);                 // [k][j], k bit-reversed on load
+    float *Pc = reinterpret_cast<float *>(P + (size_t)ljs * nz);      // Thomas P coefficients [k][j]
+    const int kx = blockIdx.x;
+    float2 *Sp = S + (size_t)kx * nz * lj;
+    for (int q = threadIdx.x; q < lj * nz; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        P[(size_t)bitrev(k, lgz) * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    dit_lines(P + 1, nz, lgz, ny, 1, ljs, twzr, twzi, 1.0f);  // lines j = 1..ny, along k
+    // Thomas along j for each kz (natural order after DIT)
+    const float lamx = ps.kx2[kx];
+    for (int kz = threadIdx.x; kz < nz; kz += blockDim.x) {
+        float2 *x = P + (size_t)kz * ljs;
+        float *pc = Pc + (size_t)kz * ljs;
+        const float lam = lamx + ps.kz2[kz];
+        float ai, bc = ps.bc;
+        if (ps.sys == SYS_P) ai = -(lam + ps.ai_base);
+        else ai = ps.ai_base + ps.kap * lam;
+        // row 0
+        float a0, b0;
+        if (ps.sys == SYS_U) { a0 = 1.f; b0 = 1.f; }
+        else if (ps.sys == SYS_V) { a0 = 1.f; b0 = 0.f; }
+        else { a0 = 1.f; b0 = -1.f; }
+        float p = -b0 / a0;
+        float2 qv = make_float2(0.f, 0.f);
+        pc[0] = p; x[0] = qv;
+        for (int j = 1; j < lj; ++j) {
+            float a, b, c;
+            float2 d;
+            const bool last = j == lj - 1;
+            if (ps.sys == SYS_U) {
+                if (last) { a = 1.f; b = 0.f; c = 1.f; d = make_float2(0.f, 0.f); }
+                else { a = ai; b = bc; c = bc; d = x[j]; d.x *= ps.nxz_inv; d.y *= ps.nxz_inv; }
+            } else if (ps.sys == SYS_V) {
+                if (j >= ny) { a = 1.f; b = 0.f; c = 0.f; d = make_float2(0.f, 0.f); }
+                else { a = ai; b = bc; c = bc; d = x[j]; d.x *= ps.nxz_inv; d.y *= ps.nxz_inv; }
+            } else {
+                if (last) { a = 1.f; b = 0.f; c = -1.f; d = make_float2(0.f, 0.f); }
+                else { a = ai; b = bc; c = bc; d = x[j]; d.x *= ps.nxz_inv; d.y *= ps.nxz_inv; }
+            }
+            const float den = a + c * p;
+            if (fabsf(den) < 1.0e-16f * fmaxf(1.0f, fabsf(a))) {
+                p = 0.f; qv = make_float2(0.f, 0.f);
+            } else {
+                const float inv = 1.0f / den;
+                p = -b * inv;
+                qv = make_float2((d.x - c * qv.x) * inv, (d.y - c * qv.y) * inv);
+            }
+            pc[j] = p; x[j] = qv;
+        }
+        float2 xv = x[lj - 1];
+        for (int j = lj - 2; j >= 0; --j) {
+            const float pj = pc[j];
+            const float2 qj = x[j];
+            xv = make_float2(pj * xv.x + qj.x, pj * xv.y + qj.y);
+            x[j] = xv;
+        }
+    }
+    __syncthreads();
+    dif_lines(P, nz, lj, 1, ljs, twzr, twzi, -1.0f);         // all rows, along k
+    for (int q = threadIdx.x; q < lj * nz; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        Sp[q] = P[(size_t)bitrev(k, lgz) * ljs + j];
+    }
+}
+
+}  // namespace f8

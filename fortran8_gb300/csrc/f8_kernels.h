@@ -34,7 +34,9 @@ struct Dev {
     int *mcyl;
     double *Fc[3];                         // nm * nz each
     int *csr_off[3], *csr_idx[3];          // per component over (SX*SY) columns
-    double *drag;                          // per step ncyl*3
+    int *mperm, *moff;                     // markers grouped by cylinder (drag reduction)
+    double *dragpart;                      // ncyl * nz * 3 partial sums
+    float *Uf, *Vf, *Wf;                   // FP32 copies of U, V, W (halo), mixed path
     // mixed-precision state and work (F8_MIXED)
     float *Cf, *Cnf, *fpetf;               // FP32 conformation tensor (SoA halo) and f(C)
     float *A0f[3], *T0f[3], *Ff[3];        // FP32 history and body force (interior)
@@ -43,6 +45,8 @@ struct Dev {
     double *Rd;                            // FP64 Poisson defect (interior)
     float *Hf, *H2f;                       // FP32 spectra
     float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
+    float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
+    int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory
     float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
     int *mi0[3], *mj0[3];                  // per-marker stencil origins
     int *act_cols[3];                      // interior (i,j) columns that receive spreading

@@ -797,18 +797,37 @@ __global__ void k_ibm_spread_q(IbmArgs a, Geo g) {
     }
 }
 
-// drag of each cylinder: -sum(Fc) * dv per component (one block per cylinder)
-__global__ void k_drag(const double *Fx, const double *Fy, const double *Fz, const int *mcyl, int nm, int nz, int ncomp,
-                       double dv, double *out) {
-    const int l = blockIdx.x;
+// drag of each cylinder: -sum(Fc) * dv per component.  Stage 1: block
+// (l, n) sums the forces of cylinder l's markers on plane n (markers listed
+// per cylinder in mperm, ranges moff); stage 2 sums the planes.  Fixed tree
+// orders make the result deterministic.
+__global__ void k_drag_part(const double *Fx, const double *Fy, const double *Fz, const int *mperm, const int *moff,
+                            int nm, int ncomp, double *part) {
+    const int l = blockIdx.x, n = blockIdx.y, nz = gridDim.y;
     __shared__ double sh[3][256];
     double s[3] = {0.0, 0.0, 0.0};
     const double *F[3] = {Fx, Fy, Fz};
-    for (long q = threadIdx.x; q < (long)nm * nz; q += blockDim.x) {
-        int m = (int)(q % nm);
-        if (mcyl[m] != l) continue;
-        for (int c = 0; c < ncomp; ++c) s[c] += F[c][q];
+    for (int q = moff[l] + threadIdx.x; q < moff[l + 1]; q += blockDim.x) {
+        const size_t o = (size_t)mperm[q] + (size_t)nm * n;
+        for (int c = 0; c < ncomp; ++c) s[c] += F[c][o];
     }
+    for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = s[c];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) part[((size_t)l * nz + n) * 3 + c] = sh[c][0];
+}
+
+__global__ void k_drag_final(const double *part, int nz, int ncomp, double dv, double *out) {
+    const int l = blockIdx.x;
+    __shared__ double sh[3][256];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int n = threadIdx.x; n < nz; n += blockDim.x)
+        for (int c = 0; c < 3; ++c) s[c] += part[((size_t)l * nz + n) * 3 + c];
     for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = s[c];
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -1137,8 +1156,8 @@ cudaError_t launch_march(Dev &d, cudaStream_t s) {
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s) {
     const Geo &g = d.g;
     const bool d3 = g.dim == 3;
-    k_drag<<<d.ncyl, 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mcyl, d.nm, g.nz, d3 ? 3 : 2,
-                                  d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out);
+    k_drag_part<<<dim3(d.ncyl, g.nz), 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mperm, d.moff, d.nm, d3 ? 3 : 2, d.dragpart);
+    k_drag_final<<<d.ncyl, 256, 0, s>>>(d.dragpart, g.nz, d3 ? 3 : 2, d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out);
     return cudaGetLastError();
 }
 
@@ -1217,7 +1236,7 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
         k_ibm_interp<<<gi, 128, 0, s>>>(ia, g);
         dim3 blk(32, 8);
         k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g);
-        if (drag_out_dev) k_drag<<<d.ncyl, 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mcyl, d.nm, g.nz, ia.ncomp, ia.dvol, drag_out_dev);
+        if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
         if ((e = cudaGetLastError())) return e;
     }
     mark(4);

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include "f8_common.cuh"
 #include "f8_fft.cuh"
+#include "f8_fft_fused.cuh"
 #include "f8_kernels.h"
 
 namespace f8 {
@@ -116,6 +117,45 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
+// halo values of U, V, W, P (PBM / wall rules, fenep_2d.f90:1098-1129) for
+// the FP64 fields and their FP32 copies in one pass
+__device__ inline double halo_val_m(const Geo &g, const double *A, int kind, int i, int j, int k) {
+    const int ii = wrapx(g, i), kk = wrapz(g, k);
+    if (j >= 1 && j <= g.ny) {
+        if (g.walls && kind == BC_V && j == g.ny) return 0.0;
+        return A[hix(g, ii, j, kk)];
+    }
+    if (!g.walls) return A[hix(g, ii, wrapy(g, j), kk)];
+    const bool lo = j == 0;
+    switch (kind) {
+    case BC_U: return lo ? -A[hix(g, ii, 1, kk)] : 2 * g.uwall - A[hix(g, ii, g.ny, kk)];
+    case BC_W: return lo ? -A[hix(g, ii, 1, kk)] : -A[hix(g, ii, g.ny, kk)];
+    case BC_V: return 0.0;
+    default:   return lo ? A[hix(g, ii, 1, kk)] : A[hix(g, ii, g.ny, kk)];
+    }
+}
+
+__global__ void k_bc_vel_m(double *U, double *V, double *W, double *P, float *Uf, float *Vf, float *Wf, Geo g) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (halo_cell_m(g, t, i, j, k)) {
+        const int h = hix(g, i, j, k);
+        const double u = halo_val_m(g, U, BC_U, i, j, k), v = halo_val_m(g, V, BC_V, i, j, k);
+        const double w = halo_val_m(g, W, BC_W, i, j, k), p = halo_val_m(g, P, BC_P, i, j, k);
+        U[h] = u; V[h] = v; W[h] = w; P[h] = p;
+        Uf[h] = (float)u; Vf[h] = (float)v; Wf[h] = (float)w;
+        return;
+    }
+    if (g.walls) {  // V on the upper wall face
+        t -= halo_count_m(g);
+        if (t >= 0 && t < (long)g.nx * g.nz) {
+            i = 1 + (int)(t % g.nx); k = 1 + (int)(t / g.nx);
+            const int h = hix(g, i, g.ny, k);
+            V[h] = 0.0; Vf[h] = 0.0f;
+        }
+    }
+}
+
 __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= cs) return;
@@ -203,12 +243,71 @@ __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, u
 // Cstar + implicit Newton solve of A C + C A^T = Cx + dt/Wi I with
 // A = A0 + (1 + f(C) dt/Wi)/2 I (fenep.f90:518-605) in FP32.  The Jacobian is
 // analytic: J = M(A0) + a I + (dt/Wi) f'(tr C) C e^T, with a = 1 + f dt/Wi,
-// e = (1,0,0,1,0,1) and f' = (L^2-3)/(L^2-tr C)^2; the stopping rule is the
-// reference's relative step test.
+// e = (1,0,0,1,0,1) and f' = (L^2-3)/(L^2-tr C)^2.  J is dominated by its
+// diagonal a >= 1 (|M| = O(dt |grad u|)), so the 6x6 elimination runs without
+// pivoting, fully unrolled in registers.  Stopping rule: the reference's
+// relative step test (fenep.f90:575).
+__device__ inline void newton_solve_f(float (&x)[6], const float (&b)[6], float a00, float a01, float a02, float a10,
+                                      float a11, float a12, float a20, float a21, float a22, float dtwi, float lp2f,
+                                      double lp2, float epsf, int itrmax, int &itr_out) {
+    int itr;
+    for (itr = 1; itr <= itrmax; ++itr) {
+        const float f = peterlin_f(x[0], x[3], x[5], lp2f, lp2);
+        const float a = 1.0f + f * dtwi;
+        const float den = lp2f - (x[0] + x[3] + x[5]);
+        const float cc = dtwi * (lp2f - 3.0f) / (den * den);
+        // residual L(x) = M x + a x - b (rows of Lyapunov_func, fenep.f90:598-603)
+        float J[6][7];
+        J[0][6] = 2 * a00 * x[0] + 2 * a01 * x[1] + 2 * a02 * x[2] + a * x[0] - b[0];
+        J[1][6] = a10 * x[0] + (a11 + a00) * x[1] + a12 * x[2] + a01 * x[3] + a02 * x[4] + a * x[1] - b[1];
+        J[2][6] = a20 * x[0] + a21 * x[1] + (a22 + a00) * x[2] + a01 * x[4] + a02 * x[5] + a * x[2] - b[2];
+        J[3][6] = 2 * a10 * x[1] + 2 * a11 * x[3] + 2 * a12 * x[4] + a * x[3] - b[3];
+        J[4][6] = a10 * x[2] + a20 * x[1] + a21 * x[3] + (a22 + a11) * x[4] + a12 * x[5] + a * x[4] - b[4];
+        J[5][6] = 2 * a20 * x[2] + 2 * a21 * x[4] + 2 * a22 * x[5] + a * x[5] - b[5];
+        const float Mx[6][6] = {
+            {2 * a00, 2 * a01, 2 * a02, 0, 0, 0},
+            {a10, a11 + a00, a12, a01, a02, 0},
+            {a20, a21, a22 + a00, 0, a01, a02},
+            {0, 2 * a10, 0, 2 * a11, 2 * a12, 0},
+            {0, a20, a10, a21, a22 + a11, a12},
+            {0, 0, 2 * a20, 0, 2 * a21, 2 * a22}};
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const float cr = cc * x[r];
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+                J[r][q] = Mx[r][q] + ((q == 0 || q == 3 || q == 5) ? cr : 0.0f) + (q == r ? a : 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float inv = 1.0f / J[k][k];
+#pragma unroll
+            for (int q = k + 1; q < 7; ++q) J[k][q] *= inv;
+#pragma unroll
+            for (int r = 0; r < 6; ++r) {
+                if (r == k) continue;
+                const float fr = J[r][k];
+#pragma unroll
+                for (int q = k + 1; q < 7; ++q) J[r][q] -= fr * J[k][q];
+            }
+        }
+        float sr = 0.0f, sx = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            x[m] -= J[m][6];
+            sr += J[m][6] * J[m][6];
+        }
+#pragma unroll
+        for (int m = 0; m < 6; ++m) sx += x[m] * x[m];
+        if (!(sqrtf(sr / sx) >= epsf)) break;   // also leaves on NaN
+    }
+    itr_out = itr;
+}
+
 __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
                                                    float *__restrict__ fpet, const uint8_t *__restrict__ codes,
-                                                   const double *__restrict__ U, const double *__restrict__ V,
-                                                   const double *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
+                                                   const float *__restrict__ U, const float *__restrict__ V,
+                                                   const float *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
                                                    StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -217,6 +316,7 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
     unsigned long long my_itr = 0, my_unconv = 0;
     if (active) {
         const int h = hix(g, i, j, k);
+        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
         const int cself = codes[qix(g, i, j, k)];
         const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
         const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
@@ -230,10 +330,9 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
         const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
         const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
         const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
-        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-        const float u1 = (float)U[hix(g, i - 1, j, k)], u2 = (float)U[h];
-        const float v1 = (float)V[hix(g, i, j - 1, k)], v2 = (float)V[h];
-        const float w1 = (float)W[hix(g, i, j, k - 1)], w2 = (float)W[h];
+        const float u1 = U[h - ox], u2 = U[h];
+        const float v1 = V[h - oy], v2 = V[h];
+        const float w1 = W[h - oz], w2 = W[h];
         const float cxs = mc.sx, cys = mc.sy, czs = mc.sz;
         const float s1 = (-u2 + fabsf(u2)) * cxs, s2 = 1.0f / 6 + (-u2 - fabsf(u2)) * cxs;
         const float s3 = 1.0f / 6 + (u1 - fabsf(u1)) * cxs, s4 = (u1 + fabsf(u1)) * cxs;
@@ -242,99 +341,46 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
         const float s9 = (-w2 + fabsf(w2)) * czs, s10 = 1.0f / 6 + (-w2 - fabsf(w2)) * czs;
         const float s11 = 1.0f / 6 + (w1 - fabsf(w1)) * czs, s12 = (w1 + fabsf(w1)) * czs;
         float b[6], x[6];
+#pragma unroll
         for (int m = 0; m < 6; ++m) {
             const float *Cm = C + (size_t)m * cs;
             const float c0 = Cm[h];
             const float xm1 = Cm[h - ox], xp1 = Cm[h + ox];
             const float ym1 = Cm[h - oy], yp1 = Cm[h + oy];
             const float zm1 = Cm[h - oz], zp1 = Cm[h + oz];
-            float pxm = face_pf(isx, xm1, c0, xp1), nxp = face_nf(isx, xm1, c0, xp1);
-            float pxp = face_pf(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
-            float nxm = face_nf(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
-            float pym = face_pf(isy, ym1, c0, yp1), nyp = face_nf(isy, ym1, c0, yp1);
-            float pyp = yp_ghost ? Cm[hyp] : face_pf(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-            float nym = ym_ghost ? Cm[hym] : face_nf(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
-            float pzm = face_pf(isz, zm1, c0, zp1), nzp = face_nf(isz, zm1, c0, zp1);
-            float pzp = face_pf(czp + 1, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
-            float nzm = face_nf(czm + 1, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
+            const float pxm = face_pf(isx, xm1, c0, xp1), nxp = face_nf(isx, xm1, c0, xp1);
+            const float pxp = face_pf(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+            const float nxm = face_nf(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            const float pym = face_pf(isy, ym1, c0, yp1), nyp = face_nf(isy, ym1, c0, yp1);
+            const float pyp = yp_ghost ? Cm[hyp] : face_pf(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+            const float nym = ym_ghost ? Cm[hym] : face_nf(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            const float pzm = face_pf(isz, zm1, c0, zp1), nzp = face_nf(isz, zm1, c0, zp1);
+            const float pzp = face_pf(czp + 1, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
+            const float nzm = face_nf(czm + 1, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
             b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp
                    + s11 * pzm + s9 * pzp + s12 * nzm + s10 * nzp;
             x[m] = c0;
         }
         const float dtwi = (float)(ph.dt / ph.wi);
         b[0] += dtwi; b[3] += dtwi; b[5] += dtwi;
-        // velocity gradient (fenep.f90:541-550) in FP32 with host-side
-        // constants -dt/dX, -dt/(4 dX), ...
-        auto U_ = [&](int a, int bb, int cc) { return (float)U[hix(g, a, bb, cc)]; };
-        auto V_ = [&](int a, int bb, int cc) { return (float)V[hix(g, a, bb, cc)]; };
-        auto W_ = [&](int a, int bb, int cc) { return (float)W[hix(g, a, bb, cc)]; };
-        const MixConst &q = mc;
-        float A0[3][3];
-        A0[0][0] = q.gx1 * (U_(i, j, k) - U_(i - 1, j, k));
-        A0[0][1] = q.gx4 * (-V_(i - 1, j - 1, k) + V_(i + 1, j - 1, k) - V_(i - 1, j, k) + V_(i + 1, j, k));
-        A0[0][2] = q.gx4 * (-W_(i - 1, j, k - 1) + W_(i + 1, j, k - 1) - W_(i - 1, j, k) + W_(i + 1, j, k));
-        A0[1][0] = q.gy4 * (-U_(i - 1, j - 1, k) - U_(i, j - 1, k) + U_(i - 1, j + 1, k) + U_(i, j + 1, k));
-        A0[1][1] = q.gy1 * (V_(i, j, k) - V_(i, j - 1, k));
-        A0[1][2] = q.gy4 * (-W_(i, j - 1, k - 1) + W_(i, j + 1, k - 1) - W_(i, j - 1, k) + W_(i, j + 1, k));
-        A0[2][0] = q.gz4 * (-U_(i - 1, j, k - 1) - U_(i, j, k - 1) + U_(i - 1, j, k + 1) + U_(i, j, k + 1));
-        A0[2][1] = q.gz4 * (-V_(i, j - 1, k - 1) - V_(i, j, k - 1) + V_(i, j - 1, k + 1) + V_(i, j, k + 1));
-        A0[2][2] = q.gz1 * (W_(i, j, k) - W_(i, j, k - 1));
-        // A = transpose(A0) (fenep.f90:550)
-        const float a00 = A0[0][0], a01 = A0[1][0], a02 = A0[2][0];
-        const float a10 = A0[0][1], a11 = A0[1][1], a12 = A0[2][1];
-        const float a20 = A0[0][2], a21 = A0[1][2], a22 = A0[2][2];
-        // linear Lyapunov part M (rows of Lyapunov_func with A = A0^T)
-        float M[6][6] = {
-            {2 * a00, 2 * a01, 2 * a02, 0, 0, 0},
-            {a10, a11 + a00, a12, a01, a02, 0},
-            {a20, a21, a22 + a00, 0, a01, a02},
-            {0, 2 * a10, 0, 2 * a11, 2 * a12, 0},
-            {0, a20, a10, a21, a22 + a11, a12},
-            {0, 0, 2 * a20, 0, 2 * a21, 2 * a22}};
-        const float lp2f = (float)ph.lp2;
-        const float epsf = (float)ph.newton_eps;
+        // velocity gradient (fenep.f90:541-550), A = transpose(A0) (fenep.f90:550)
+        const float g00 = mc.gx1 * (u2 - u1);
+        const float g01 = mc.gx4 * (-V[h - ox - oy] + V[h + ox - oy] - V[h - ox] + V[h + ox]);
+        const float g02 = mc.gx4 * (-W[h - ox - oz] + W[h + ox - oz] - W[h - ox] + W[h + ox]);
+        const float g10 = mc.gy4 * (-U[h - ox - oy] - U[h - oy] + U[h - ox + oy] + U[h + oy]);
+        const float g11 = mc.gy1 * (v2 - v1);
+        const float g12 = mc.gy4 * (-W[h - oy - oz] + W[h + oy - oz] - W[h - oy] + W[h + oy]);
+        const float g20 = mc.gz4 * (-U[h - ox - oz] - U[h - oz] + U[h - ox + oz] + U[h + oz]);
+        const float g21 = mc.gz4 * (-V[h - oy - oz] - V[h - oz] + V[h - oy + oz] + V[h + oz]);
+        const float g22 = mc.gz1 * (w2 - w1);
         int itr;
-        for (itr = 1; itr <= ph.newton_itrmax; ++itr) {
-            const float f = peterlin_f(x[0], x[3], x[5], lp2f, ph.lp2);
-            const float a = 1.0f + f * dtwi;
-            const float den = lp2f - (x[0] + x[3] + x[5]);
-            const float fp = (lp2f - 3.0f) / (den * den);
-            const float cc = dtwi * fp;
-            float Ah[6][7];
-            for (int r = 0; r < 6; ++r) {
-                float l = -b[r] + a * x[r];
-                for (int q = 0; q < 6; ++q) l += M[r][q] * x[q];
-                for (int q = 0; q < 6; ++q) Ah[r][q] = M[r][q] + cc * x[r] * ((q == 0 || q == 3 || q == 5) ? 1.0f : 0.0f);
-                Ah[r][r] += a;
-                Ah[r][6] = l;
-            }
-            // Gauss-Jordan with partial pivoting
-            for (int kk = 0; kk < 6; ++kk) {
-                int piv = kk; float best = fabsf(Ah[kk][kk]);
-                for (int r = kk + 1; r < 6; ++r) if (fabsf(Ah[r][kk]) > best) { best = fabsf(Ah[r][kk]); piv = r; }
-                if (best == 0.0f) { for (int r = 0; r < 6; ++r) Ah[r][6] = 0.0f; break; }
-                if (piv != kk)
-                    for (int q = kk; q < 7; ++q) { float t = Ah[kk][q]; Ah[kk][q] = Ah[piv][q]; Ah[piv][q] = t; }
-                const float inv = 1.0f / Ah[kk][kk];
-                for (int q = kk + 1; q < 7; ++q) Ah[kk][q] *= inv;
-                for (int r = 0; r < 6; ++r) {
-                    if (r == kk) continue;
-                    const float fr = Ah[r][kk];
-                    for (int q = kk + 1; q < 7; ++q) Ah[r][q] -= fr * Ah[kk][q];
-                }
-            }
-            float sr = 0.0f, sx = 0.0f;
-            for (int m = 0; m < 6; ++m) {
-                x[m] -= Ah[m][6];
-                sr += Ah[m][6] * Ah[m][6];
-            }
-            for (int m = 0; m < 6; ++m) sx += x[m] * x[m];
-            if (sqrtf(sr / sx) < epsf) break;
-        }
+        newton_solve_f(x, b, g00, g10, g20, g01, g11, g21, g02, g12, g22, dtwi, (float)ph.lp2, ph.lp2,
+                       (float)ph.newton_eps, ph.newton_itrmax, itr);
         my_itr = (unsigned long long)itr;
         my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+#pragma unroll
         for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
-        fpet[h] = peterlin_f(x[0], x[3], x[5], lp2f, ph.lp2);
+        fpet[h] = peterlin_f(x[0], x[3], x[5], (float)ph.lp2, ph.lp2);
     }
     unsigned long long a = my_itr, b2 = my_unconv;
     for (int o = 16; o > 0; o >>= 1) {
@@ -350,7 +396,8 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
 // ---------------------------------------------------------------------------
 // Momentum right-hand side in increment form: Q_c = dt * R_c (FP32).
 struct MomArgsF {
-    const double *U, *V, *W, *P;
+    const float *U, *V, *W;   // FP32 copies of the velocity
+    const double *P;
     const float *C, *fpet;
     float *A0[3], *T0[3];
     const float *F[3];
@@ -389,10 +436,10 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst
                        + (c0(6, h + oz) - c0(6, h)) * iz;
         tx = a.coef_t * sx; ty = a.coef_t * sy; tz = a.coef_t * sz;
     }
-    const double *U = a.U, *V = a.V, *W = a.W;
-    auto u = [&](int hh) { return (float)U[hh]; };
-    auto v = [&](int hh) { return (float)V[hh]; };
-    auto w = [&](int hh) { return (float)W[hh]; };
+    const float *U = a.U, *V = a.V, *W = a.W;
+    auto u = [&](int hh) { return U[hh]; };
+    auto v = [&](int hh) { return V[hh]; };
+    auto w = [&](int hh) { return W[hh]; };
     // convection (fenep.f90:694-734), divergence form
     const float uc = u(h), vc = v(h), wc = w(h);
     const float uxm = u(h - ox), uxp = u(h + ox), uym = u(h - oy), uyp = u(h + oy), uzm = u(h - oz), uzp = u(h + oz);
@@ -561,7 +608,7 @@ __global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g,
 
 // projection and SMAC pressure update (fenep.f90:1562-1604)
 __global__ void k_march_m(double *U, double *V, double *W, double *P, const double *Up, const double *Vp,
-                          const double *Wp, const double *Phi, Geo g, MixConst mc) {
+                          const double *Wp, const double *Phi, float *Uf, float *Vf, float *Wf, Geo g, MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -570,9 +617,11 @@ __global__ void k_march_m(double *U, double *V, double *W, double *P, const doub
     const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
     const double ph = Phi[h];
     const double px = Phi[h + ox], py = Phi[h + oy], pz = Phi[h + oz];
-    U[h] = Up[h] - mc.dtdx * (px - ph);
-    V[h] = Vp[h] - mc.dtdy * (py - ph);
-    W[h] = Wp[h] - mc.dtdz * (pz - ph);
+    const double un = Up[h] - mc.dtdx * (px - ph);
+    const double vn = Vp[h] - mc.dtdy * (py - ph);
+    const double wn = Wp[h] - mc.dtdz * (pz - ph);
+    U[h] = un; V[h] = vn; W[h] = wn;
+    Uf[h] = (float)un; Vf[h] = (float)vn; Wf[h] = (float)wn;
     const float lap = (float)(Phi[h - ox] - 2.0 * ph + px) * (float)mc.idx2 + (float)(Phi[h - oy] - 2.0 * ph + py) * (float)mc.idy2
                     + (float)(Phi[h - oz] - 2.0 * ph + pz) * (float)mc.idz2;
     P[h] = P[h] + ph - (double)((float)mc.pc * lap);
@@ -602,7 +651,7 @@ inline dim3 cell_grid_m(const Geo &g, dim3 blk) {
 // FP32 spectral solves.  src (interior, FP32 or FP64) -> dst (FP64 halo
 // interior; dst = base + result when base is given).
 template <typename TS>
-cudaError_t solve_periodic_f(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
+cudaError_t solve_periodic_mp(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
                              cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
@@ -631,7 +680,7 @@ cudaError_t solve_periodic_f(Dev &d, const TS *src, double *dst, const double *b
 }
 
 template <typename TS>
-cudaError_t solve_walls_f(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+cudaError_t solve_walls_mp(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, n = ny + 2;
     const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
@@ -660,6 +709,69 @@ cudaError_t solve_walls_f(Dev &d, const TS *src, double *dst, const double *base
     return cudaGetLastError();
 }
 
+
+// Fused path: transposing x pass, one CTA per kx for the (z, y) plane,
+// transposing inverse x pass.
+inline int x_rows_per_block(int nx) { return 2 * std::max(1, std::min(8, 1024 / std::max(nx / 2, 1))); }
+inline size_t x_smem(int nx, int rb) { return (size_t)(rb / 2) * 2 * nx * sizeof(float2) + (size_t)(nx / 2 + 1) * rb * sizeof(float2); }
+inline int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
+
+template <typename TS>
+cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const double *base, float lhs0, float lhs1,
+                                 cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
+    float2 *S = reinterpret_cast<float2 *>(d.Hf);
+    const int rb = x_rows_per_block(nx);
+    const int thr = (rb / 2) * (nx / 2);
+    const size_t smx = x_smem(nx, rb);
+    const int bpp = (ny + rb - 1) / rb;
+    k_xfwd_t<TS><<<bpp * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, ny, -1, d.twxf_r, d.twxf_i);
+    PlaneSpec ps{};
+    ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
+    ps.lhs0 = lhs0; ps.lhs1 = lhs1; ps.inv_ntot = (float)(1.0 / ((double)nx * ny * nz));
+    k_plane_periodic<<<nxh, 1024, (size_t)8 * (ny + 1) * nz, s>>>(S, ny, nz, ilog2(ny), ilog2(nz), d.twyf_r, d.twyf_i,
+                                                                 d.twzf_r, d.twzf_i, ps);
+    k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i);
+    return cudaGetLastError();
+}
+
+template <typename TS>
+cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, lj = ny + 2;
+    float2 *S = reinterpret_cast<float2 *>(d.Hf);
+    const int rb = x_rows_per_block(nx);
+    const int thr = (rb / 2) * (nx / 2);
+    const size_t smx = x_smem(nx, rb);
+    k_xfwd_t<TS><<<((ny + rb - 1) / rb) * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, lj, 0, d.twxf_r, d.twxf_i);
+    PlaneSpec ps{};
+    ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
+    const double kap = d.ph.dt * d.ph.beta / d.ph.re / 2.0, idy2 = 1.0 / (g.dy * g.dy);
+    ps.sys = sys;
+    ps.nxz_inv = (float)(1.0 / ((double)nx * nz));
+    if (sys == SYS_P) { ps.ai_base = (float)(2.0 * idy2); ps.bc = (float)idy2; ps.kap = -1.0f; }
+    else { ps.ai_base = (float)(1.0 + kap * 2.0 * idy2); ps.bc = (float)(-kap * idy2); ps.kap = (float)kap; }
+    const size_t smp = (size_t)12 * (lj | 1) * nz;
+    k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps);
+    k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
+                                                               d.twxf_r, d.twxf_i);
+    return cudaGetLastError();
+}
+
+template <typename TS>
+cudaError_t solve_periodic_f(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
+                             cudaStream_t s) {
+    if (d.fused_planes) return solve_periodic_fused<TS>(d, src, dst, base, (float)lhs0, (float)lhs1, s);
+    return solve_periodic_mp<TS>(d, src, dst, base, lhs0, lhs1, s);
+}
+
+template <typename TS>
+cudaError_t solve_walls_f(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+    if (d.fused_planes) return solve_walls_fused<TS>(d, src, dst, base, sys, s);
+    return solve_walls_mp<TS>(d, src, dst, base, sys, s);
+}
+
 }  // namespace
 
 cudaError_t init_kernels_mixed() {
@@ -669,6 +781,14 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    int dev = 0, optin = 0;
+    F8_CUDA_RET(cudaGetDevice(&dev));
+    F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_periodic, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return cudaSuccess;
 }
 
@@ -697,6 +817,9 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     long n = halo_count_m(d.g);
     k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2);
     k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2);
+    F8_CUDA_RET(d2f(d.U, d.Uf, d.cs, s));
+    F8_CUDA_RET(d2f(d.V, d.Vf, d.cs, s));
+    F8_CUDA_RET(d2f(d.W, d.Wf, d.cs, s));
     return cudaGetLastError();
 }
 
@@ -710,7 +833,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         dim3 blk(32, 4);
         k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs);
         mark(1);
-        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.U, d.V, d.W, g, d.ph, mc, d.cs, d.cnt);
+        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.cnt);
         std::swap(d.Cf, d.Cnf);
         long n = halo_count_m(g);
         k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2);
@@ -721,7 +844,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(2);
     {
         MomArgsF a{};
-        a.U = d.U; a.V = d.V; a.W = d.W; a.P = d.P; a.C = d.Cf; a.fpet = d.fpetf;
+        a.U = d.Uf; a.V = d.Vf; a.W = d.Wf; a.P = d.P; a.C = d.Cf; a.fpet = d.fpetf;
         for (int c = 0; c < 3; ++c) { a.A0[c] = d.A0f[c]; a.T0[c] = d.T0f[c]; a.F[c] = d.Ff[c]; a.Q[c] = d.Qf[c]; }
         a.cs = d.cs; a.polymer = o.polymer; a.ab2_first = o.ab2_first;
         a.coef_t = (float)((1.0 - d.ph.beta) / (d.ph.re * d.ph.wi));
@@ -794,12 +917,12 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(6);
     {
         dim3 blk(32, 8);
-        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, g, mc);
+        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.Uf, d.Vf, d.Wf, g, mc);
     }
-    F8_CUDA_RET(bc_field(d.U, g, BC_U, s));
-    F8_CUDA_RET(bc_field(d.V, g, BC_V, s));
-    F8_CUDA_RET(bc_field(d.W, g, BC_W, s));
-    F8_CUDA_RET(bc_field(d.P, g, BC_P, s));
+    {
+        long n = halo_count_m(g) + (g.walls ? (long)g.nx * g.nz : 0);
+        k_bc_vel_m<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.U, d.V, d.W, d.P, d.Uf, d.Vf, d.Wf, g);
+    }
     mark(7);
     return cudaGetLastError();
 }

@@ -30,8 +30,15 @@ def run(fns, w, steps, precision):
         return st, drag, s.store(), s.diagnostics()
 
 
-def drag_rel(dm, d64):
-    # relative to the largest drag magnitude of the history (the x force)
+def drag_rel(dm, d64, all_components=False):
+    """Max deviation of the drag (x force) relative to its largest magnitude in the history.
+
+    With all_components the scale is the largest force component: in the
+    Taylor-Green box the cylinder sits at a stagnation point and its drag is
+    noise-level, so a relative drag error is ill-posed there.
+    """
+    if all_components:
+        return float(np.max(np.abs(dm - d64)) / np.max(np.abs(d64)))
     return float(np.max(np.abs(dm[..., 0] - d64[..., 0])) / np.max(np.abs(d64[..., 0])))
 
 
@@ -42,7 +49,7 @@ def test_mixed_matches_fp64_oracle(gpu, oracle, name, shape, steps):
     sm, dm, om, diag = run(gpu, w, steps, abi.F8_MIXED)
     so, do, oo, _ = run(oracle, w, steps, abi.F8_FP64)
     assert sm == abi.F8_OK
-    assert drag_rel(dm, do) <= DRAG_TOL
+    assert drag_rel(dm, do, all_components=(name == "c2_3d")) <= DRAG_TOL
     for f in ("u", "v", "w"):
         assert rel_l2(interior(om[f]), interior(oo[f])) <= VEL_TOL, f
     assert rel_l2(interior(om["c"]), interior(oo["c"])) <= 1e-5

@@ -54,7 +54,7 @@ def drag_err(dg, do):
     return float(np.max(np.abs(dg - do)) / max(np.max(np.abs(do)), 1e-300))
 
 
-@pytest.mark.parametrize("name,steps", [("c2_3d", 12), ("c3_channel", 12), ("c1_2d", 20), ("c4_adjoint", 8)])
+@pytest.mark.parametrize("name,steps", [("c2_3d", 30), ("c3_channel", 30), ("c1_2d", 20), ("c4_adjoint", 8)])
 def test_fp64_step_matches_oracle(gpu, oracle, name, steps):
     w = small(name)
     fields = ("u", "v", "w", "p") if w.grid.dim == 3 else ("u", "v", "p")
