@@ -265,13 +265,15 @@ __global__ void k_plane_walls(float2 *S, int ny, int nz, int lgz, const float *t
                 if (last) { a = 1.f; b = 0.f; c = -1.f; d = make_float2(0.f, 0.f); }
                 else { a = ai; b = bc; c = bc; d = x[j]; d.x *= ps.nxz_inv; d.y *= ps.nxz_inv; }
             }
+            // true divisions, as tdma does: on the singular Neumann mode of the
+            // pressure system p stays exactly 1 and the last pivot is exactly
+            // zero, so the reference's guard pins that mode
             const float den = a + c * p;
-            if (fabsf(den) < 1.0e-16f * fmaxf(1.0f, fabsf(a))) {
+            if (fabsf(den) < 1.0e-16f) {
                 p = 0.f; qv = make_float2(0.f, 0.f);
             } else {
-                const float inv = 1.0f / den;
-                p = -b * inv;
-                qv = make_float2((d.x - c * qv.x) * inv, (d.y - c * qv.y) * inv);
+                p = -b / den;
+                qv = make_float2((d.x - c * qv.x) / den, (d.y - c * qv.y) / den);
             }
             pc[j] = p; x[j] = qv;
         }

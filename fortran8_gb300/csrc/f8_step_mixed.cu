@@ -180,21 +180,16 @@ __device__ inline float eigmin_f(const float *a) {
     return m + 2.0f * sp * cosf(acosf(r) * (1.0f / 3.0f) + TWO_PI_3F);
 }
 
+// candidate faces (fenep.f90:179-184) as weights of (C_{m-1}, C_m, C_{m+1});
+// index 4 is the cell value
+__constant__ float c_fp_w[5][3] = {{0, 1, 0}, {0, 1.5f, -0.5f}, {0.5f, 0.5f, 0}, {0.25f, 1, -0.25f}, {0, 1, 0}};
+__constant__ float c_fn_w[5][3] = {{0, 1, 0}, {0, 0.5f, 0.5f}, {-0.5f, 1.5f, 0}, {-0.25f, 1, 0.25f}, {0, 1, 0}};
+
 __device__ inline float face_pf(int idx, float cm, float c0, float cp) {
-    switch (idx) {
-    case 1: return c0 * 1.5f - cp * 0.5f;
-    case 2: return cm * 0.5f + c0 * 0.5f;
-    case 3: return cm * 0.25f + c0 - cp * 0.25f;
-    default: return c0;
-    }
+    return c_fp_w[idx][0] * cm + c_fp_w[idx][1] * c0 + c_fp_w[idx][2] * cp;
 }
 __device__ inline float face_nf(int idx, float cm, float c0, float cp) {
-    switch (idx) {
-    case 1: return c0 * 0.5f + cp * 0.5f;
-    case 2: return -cm * 0.5f + c0 * 1.5f;
-    case 3: return -cm * 0.25f + c0 + cp * 0.25f;
-    default: return c0;
-    }
+    return c_fn_w[idx][0] * cm + c_fn_w[idx][1] * c0 + c_fn_w[idx][2] * cp;
 }
 
 __device__ inline int select3f(const float *cm, const float *c0, const float *cp) {
