@@ -290,6 +290,57 @@ int setup(f8_ctx *c) {
         API_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
         const size_t need = g.walls ? (size_t)12 * ((g.ny + 2) | 1) * g.nz : (size_t)8 * (g.ny + 1) * g.nz;
         d.fused_planes = need <= (size_t)optin ? 1 : 0;
+        {
+            std::vector<float2> t2(std::max(1, g.nz / 2));
+            for (int t = 0; t < g.nz / 2; ++t) {
+                double a = 2.0 * PI * t / g.nz;
+                t2[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
+            }
+            API_CUDA(c, c->alloc(&d.twz2, t2.size()));
+            API_CUDA(c, cudaMemcpyAsync(d.twz2, t2.data(), t2.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, cudaStreamSynchronize(c->s));
+        }
+        if (g.walls && d.fused_planes && (g.nz == 32 || g.nz == 64 || g.nz == 128)) {
+            // Thomas pivots of the increment Helmholtz systems (U, V) and of the
+            // pressure system (fenep_2d.f90:1222-1238, 1262-1277, 1318-1332;
+            // tdma's guard, 1157-1160), for every (kx, kz)
+            const int lj = g.ny + 2;
+            const size_t nt = nxh * (size_t)g.nz * lj;
+            const double kap = c->phys.dt * c->phys.beta / c->phys.re / 2.0, idy2 = 1.0 / (g.dy * g.dy);
+            std::vector<float> tp(nt), tr(nt);
+            for (int sys = 0; sys < 3; ++sys) {
+                for (size_t kx = 0; kx < nxh; ++kx)
+                    for (int kz = 0; kz < g.nz; ++kz) {
+                        const double lam = kx2[kx] + kz2[kz];
+                        double p = 0.0;
+                        for (int j = 0; j < lj; ++j) {
+                            double a, b, cc;
+                            if (sys == 2) {  // pressure, Neumann rows
+                                if (j == 0) { a = 1; b = -1; cc = 0; }
+                                else if (j == lj - 1) { a = 1; b = 0; cc = -1; }
+                                else { a = -(lam + 2.0 * idy2); b = idy2; cc = idy2; }
+                            } else if (sys == 0) {  // U, W
+                                if (j == 0) { a = 1; b = 1; cc = 0; }
+                                else if (j == lj - 1) { a = 1; b = 0; cc = 1; }
+                                else { a = 1.0 + kap * (lam + 2.0 * idy2); b = -kap * idy2; cc = b; }
+                            } else {  // V
+                                if (j == 0 || j >= g.ny) { a = 1; b = 0; cc = 0; }
+                                else { a = 1.0 + kap * (lam + 2.0 * idy2); b = -kap * idy2; cc = b; }
+                            }
+                            const double den = j == 0 ? a : a + cc * p;
+                            double rd;
+                            if (std::fabs(den) < 1.0e-16) { p = 0.0; rd = 0.0; }
+                            else { p = -b / den; rd = 1.0 / den; }
+                            const size_t o = (kx * g.nz + kz) * (size_t)lj + j;
+                            tp[o] = (float)p;
+                            tr[o] = (float)rd;
+                        }
+                    }
+                std::vector<double> tpd(tp.begin(), tp.end()), trd(tr.begin(), tr.end());
+                if (int st = upload_f(c, &d.wtP[sys], tpd)) return st;
+                if (int st = upload_f(c, &d.wtR[sys], trd)) return st;
+            }
+        }
     }
     // IBM markers and the gather lists of the spreading kernel
     d.ncyl = (int)c->cyl.size();

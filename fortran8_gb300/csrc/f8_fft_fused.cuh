@@ -25,6 +25,7 @@ __device__ inline int bitrev(int v, int lg) { return lg ? (int)(__brev((unsigned
 
 // ---------------------------------------------------------------------------
 // x forward, transposing.  Block b handles RB rows (RB/2 pairs) of plane k.
+// The [kx][row] tile has an odd row stride (RB + 1) against bank conflicts.
 template <typename TS>
 __global__ void k_xfwd_t(const TS *__restrict__ src, float2 *__restrict__ S, int nx, int ny, int nz, int rb, int lj,
                          int joff, const float *__restrict__ twr, const float *__restrict__ twi) {
@@ -59,14 +60,14 @@ __global__ void k_xfwd_t(const TS *__restrict__ src, float2 *__restrict__ S, int
         for (int kx = t; kx < nxh; kx += half) {
             const int m = (nx - kx) % nx;
             const Cx<float> zk = z[kx], zm = z[m];
-            tile[(size_t)kx * rb + 2 * p] = make_float2((zk.r + zm.r) * 0.5f, (zk.i - zm.i) * 0.5f);
-            tile[(size_t)kx * rb + 2 * p + 1] = make_float2((zk.i + zm.i) * 0.5f, (zm.r - zk.r) * 0.5f);
+            tile[(size_t)kx * (rb + 1) + 2 * p] = make_float2((zk.r + zm.r) * 0.5f, (zk.i - zm.i) * 0.5f);
+            tile[(size_t)kx * (rb + 1) + 2 * p + 1] = make_float2((zk.i + zm.i) * 0.5f, (zm.r - zk.r) * 0.5f);
         }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < nxh * rb; q += blockDim.x) {
         const int kx = q / rb, r = q % rb;
-        if (r < nrows) S[((size_t)kx * nz + k) * lj + (r0 + r + 1 + joff)] = tile[(size_t)kx * rb + r];
+        if (r < nrows) S[((size_t)kx * nz + k) * lj + (r0 + r + 1 + joff)] = tile[(size_t)kx * (rb + 1) + r];
     }
 }
 
@@ -88,7 +89,7 @@ __global__ void k_xinv_t(const float2 *__restrict__ S, TO *dst, const TO *base, 
     float2 *tile = reinterpret_cast<float2 *>(sm + (size_t)npair * 2 * nx);
     for (int q = threadIdx.x; q < nxh * rb; q += blockDim.x) {
         const int kx = q / rb, r = q % rb;
-        tile[q] = r < nrows ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)] : make_float2(0.f, 0.f);
+        tile[(size_t)kx * (rb + 1) + r] = r < nrows ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int p = threadIdx.x / half, t = threadIdx.x % half;
@@ -98,12 +99,12 @@ __global__ void k_xinv_t(const float2 *__restrict__ S, TO *dst, const TO *base, 
         for (int e = t; e < nx; e += half) {
             float ar, ai, br, bi;
             if (e <= half) {
-                const float2 A = tile[(size_t)e * rb + 2 * p], B = tile[(size_t)e * rb + 2 * p + 1];
+                const float2 A = tile[(size_t)e * (rb + 1) + 2 * p], B = tile[(size_t)e * (rb + 1) + 2 * p + 1];
                 ar = A.x; ai = A.y; br = B.x; bi = B.y;
                 x[e].r = ar - bi; x[e].i = ai + br;
             } else {
                 const int m = nx - e;
-                const float2 A = tile[(size_t)m * rb + 2 * p], B = tile[(size_t)m * rb + 2 * p + 1];
+                const float2 A = tile[(size_t)m * (rb + 1) + 2 * p], B = tile[(size_t)m * (rb + 1) + 2 * p + 1];
                 ar = A.x; ai = A.y; br = B.x; bi = B.y;
                 x[e].r = ar + bi; x[e].i = br - ai;
             }
@@ -290,6 +291,179 @@ __global__ void k_plane_walls(float2 *S, int ny, int nz, int lgz, const float *t
     for (int q = threadIdx.x; q < lj * nz; q += blockDim.x) {
         const int k = q / lj, j = q % lj;
         Sp[q] = P[(size_t)bitrev(k, lgz) * ljs + j];
+    }
+}
+
+}  // namespace f8
+
+namespace f8 {
+
+// ---------------------------------------------------------------------------
+// Warp-level radix-2 transform of one line of N = 32*V points: lane t holds
+// elements t + 32 s (s < V).  Spans >= 32 are butterflies inside the lane,
+// spans < 32 exchange with lane t ^ span.  tw: forward twiddles
+// (cos, -sin)(2 pi p / N), p < N/2, in shared memory.
+template <int V>
+__device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) {
+    constexpr int N = 32 * V;
+    for (int m = N / 2; m >= 1; m >>= 1) {
+        const int ts = N / (2 * m);
+        if (m >= 32) {
+            const int sm = m / 32;
+#pragma unroll
+            for (int s = 0; s < V; ++s) {
+                if ((s / sm) % 2) continue;          // upper element of the pair
+                const int pos = (lane + 32 * s) % (2 * m);
+                const float2 w = tw[pos * ts];
+                const float2 a = v[s], b = v[s + sm];
+                const float dr = a.x - b.x, di = a.y - b.y;
+                v[s] = make_float2(a.x + b.x, a.y + b.y);
+                v[s + sm] = make_float2(dr * w.x - di * w.y, dr * w.y + di * w.x);
+            }
+        } else {
+            const bool lower = lane & m;
+            const int pos = (lane % (2 * m)) - (lower ? m : 0);
+            const float2 w = tw[pos * ts];
+#pragma unroll
+            for (int s = 0; s < V; ++s) {
+                float2 o;
+                o.x = __shfl_xor_sync(0xffffffffu, v[s].x, m);
+                o.y = __shfl_xor_sync(0xffffffffu, v[s].y, m);
+                if (!lower) {
+                    v[s] = make_float2(v[s].x + o.x, v[s].y + o.y);
+                } else {
+                    const float dr = o.x - v[s].x, di = o.y - v[s].y;
+                    v[s] = make_float2(dr * w.x - di * w.y, dr * w.y + di * w.x);
+                }
+            }
+        }
+    }
+}
+
+// inverse (conjugate twiddles), decimation in time: bit-reversed in, natural out
+template <int V>
+__device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) {
+    constexpr int N = 32 * V;
+    for (int m = 1; m < N; m <<= 1) {
+        const int ts = N / (2 * m);
+        if (m >= 32) {
+            const int sm = m / 32;
+#pragma unroll
+            for (int s = 0; s < V; ++s) {
+                if ((s / sm) % 2) continue;
+                const int pos = (lane + 32 * s) % (2 * m);
+                const float2 w = make_float2(tw[pos * ts].x, -tw[pos * ts].y);
+                const float2 a = v[s], b = v[s + sm];
+                const float tr = b.x * w.x - b.y * w.y, ti = b.x * w.y + b.y * w.x;
+                v[s] = make_float2(a.x + tr, a.y + ti);
+                v[s + sm] = make_float2(a.x - tr, a.y - ti);
+            }
+        } else {
+            const bool lower = lane & m;
+            const int pos = (lane % (2 * m)) - (lower ? m : 0);
+            const float2 w = make_float2(tw[pos * ts].x, -tw[pos * ts].y);
+#pragma unroll
+            for (int s = 0; s < V; ++s) {
+                float2 o;
+                o.x = __shfl_xor_sync(0xffffffffu, v[s].x, m);
+                o.y = __shfl_xor_sync(0xffffffffu, v[s].y, m);
+                if (!lower) {
+                    const float tr = o.x * w.x - o.y * w.y, ti = o.x * w.y + o.y * w.x;
+                    v[s] = make_float2(v[s].x + tr, v[s].y + ti);
+                } else {
+                    const float tr = v[s].x * w.x - v[s].y * w.y, ti = v[s].x * w.y + v[s].y * w.x;
+                    v[s] = make_float2(o.x - tr, o.y - ti);
+                }
+            }
+        }
+    }
+}
+
+// Pivot tables of the y systems of one solve type: for each (kx, kz) the
+// Thomas coefficients P_j and 1/den_j (0 where the pivot vanishes, the
+// reference's guard), computed on the host in FP64.
+struct WallTables {
+    const float *P;      // [kx][kz][j]
+    const float *rden;   // [kx][kz][j]
+    float bc;            // interior off-diagonal b = c
+    float c_last;        // c of the last row (1 U, -1 P); V: rows >= ny are identities
+    float nxz_inv;
+    int sys;
+};
+
+template <int V>
+__global__ void __launch_bounds__(1024, 1) k_plane_walls_w(float2 *S, int ny, const float2 *twz, WallTables wt) {
+    constexpr int NZ = 32 * V;
+    extern __shared__ unsigned char smem_raw[];
+    const int lj = ny + 2;
+    const int ljs = lj | 1;
+    float2 *P = reinterpret_cast<float2 *>(smem_raw);                // [k][j]
+    float *Pc = reinterpret_cast<float *>(P + (size_t)ljs * NZ);     // [kz][j]
+    float2 *tws = reinterpret_cast<float2 *>(Pc + (size_t)ljs * NZ); // NZ/2 twiddles
+    const int kx = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2 *Sp = S + (size_t)kx * NZ * lj;
+    for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
+    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    // forward z transform of rows 1..ny (output in bit-reversed kz order)
+    for (int j = 1 + warp; j <= ny; j += nwarp) {
+        float2 v[V];
+#pragma unroll
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        warp_dif_fwd<V>(v, tws, lane);
+#pragma unroll
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+    }
+    __syncthreads();
+    // Thomas sweeps, one thread per kz (its data sits at row bitrev(kz))
+    constexpr int LG = V == 1 ? 5 : (V == 2 ? 6 : (V == 4 ? 7 : 8));
+    for (int kz = threadIdx.x; kz < NZ; kz += blockDim.x) {
+        const int row = (int)(__brev((unsigned)kz) >> (32 - LG));
+        float2 *x = P + (size_t)row * ljs;
+        float *pc = Pc + (size_t)kz * ljs;
+        const float *Pt = wt.P + ((size_t)kx * NZ + kz) * lj;
+        const float *Rt = wt.rden + ((size_t)kx * NZ + kz) * lj;
+        float2 q = make_float2(0.f, 0.f);   // d_0 = 0 for every system
+        pc[0] = Pt[0];
+        x[0] = q;
+#pragma unroll 4
+        for (int j = 1; j < lj; ++j) {
+            float c;
+            float2 d;
+            const bool ident = (wt.sys == SYS_V) ? (j >= ny) : (j == lj - 1);
+            if (ident) { c = wt.sys == SYS_V ? 0.f : wt.c_last; d = make_float2(0.f, 0.f); }
+            else { c = wt.bc; d = x[j]; d.x *= wt.nxz_inv; d.y *= wt.nxz_inv; }
+            const float rd = Rt[j];
+            q = make_float2((d.x - c * q.x) * rd, (d.y - c * q.y) * rd);
+            pc[j] = Pt[j];
+            x[j] = q;
+        }
+        float2 xv = q;
+        for (int j = lj - 2; j >= 0; --j) {
+            const float pj = pc[j];
+            const float2 qj = x[j];
+            xv = make_float2(pj * xv.x + qj.x, pj * xv.y + qj.y);
+            x[j] = xv;
+        }
+    }
+    __syncthreads();
+    // inverse z transform of all rows (bit-reversed in, natural out)
+    for (int j = warp; j < lj; j += nwarp) {
+        float2 v[V];
+#pragma unroll
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        warp_dit_inv<V>(v, tws, lane);
+#pragma unroll
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        Sp[q] = P[(size_t)k * ljs + j];
     }
 }
 

@@ -37,6 +37,7 @@ struct MixConst {
     double idx, idy, idz, idx2, idy2, idz2, idt;
     double dtdx, dtdy, dtdz;              // dt/dX ...
     double pc;                             // dt beta / (2 Re)
+    float dtwi, lp2f, epsf;                // dt/Wi, L^2, Newton tolerance (FP32)
 };
 
 MixConst make_const(const Geo &g, const Phys &ph) {
@@ -52,6 +53,9 @@ MixConst make_const(const Geo &g, const Phys &ph) {
     c.idt = 1.0 / ph.dt;
     c.dtdx = ph.dt / g.dx; c.dtdy = ph.dt / g.dy; c.dtdz = ph.dt / g.dz;
     c.pc = ph.dt * ph.beta / ph.re / 2.0;
+    c.dtwi = (float)(ph.dt / ph.wi);
+    c.lp2f = (float)ph.lp2;
+    c.epsf = (float)ph.newton_eps;
     return c;
 }
 
@@ -168,6 +172,22 @@ __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
 // root as the reference's Vieta formula (fenep.f90:425-444) but free of the
 // cancellation in p = a1 - a2^2/3 that FP32 would suffer near C = I.  Equal
 // roots (discriminant q^2 - p^3 >= 0) return the reference's -100 sentinel.
+// arccos by Abramowitz & Stegun 4.4.46: acos(x) = sqrt(1-x) * P7(x) on [0, 1]
+// with |error| <= 2e-8, and acos(-x) = pi - acos(x).
+__device__ inline float acos_as(float x) {
+    const float ax = fabsf(x);
+    float p = -0.0012624911f;
+    p = fmaf(p, ax, 0.0066700901f);
+    p = fmaf(p, ax, -0.0170881256f);
+    p = fmaf(p, ax, 0.0308918810f);
+    p = fmaf(p, ax, -0.0501743046f);
+    p = fmaf(p, ax, 0.0889789874f);
+    p = fmaf(p, ax, -0.2145988016f);
+    p = fmaf(p, ax, 1.5707963050f);
+    const float r = sqrtf(1.0f - ax) * p;
+    return x < 0.0f ? 3.14159265358979f - r : r;
+}
+
 __device__ inline float eigmin_f(const float *a) {
     const float m = (a[0] + a[3] + a[5]) * (1.0f / 3.0f);
     const float b0 = a[0] - m, b1 = a[3] - m, b2 = a[5] - m;
@@ -176,8 +196,9 @@ __device__ inline float eigmin_f(const float *a) {
     const float p3 = p2 * p2 * p2;
     if (q * q >= p3) return -100.0f;
     const float sp = sqrtf(p2);
-    const float r = fminf(1.0f, fmaxf(-1.0f, q / (p2 * sp)));
-    return m + 2.0f * sp * cosf(acosf(r) * (1.0f / 3.0f) + TWO_PI_3F);
+    const float r = fminf(1.0f, fmaxf(-1.0f, q * __frcp_rn(p2 * sp)));
+    // the angle lies in [2 pi/3, pi], where the hardware cosine is accurate
+    return m + 2.0f * sp * __cosf(acos_as(r) * (1.0f / 3.0f) + TWO_PI_3F);
 }
 
 // candidate faces (fenep.f90:179-184) as weights of (C_{m-1}, C_m, C_{m+1});
@@ -299,7 +320,7 @@ __device__ inline void newton_solve_f(float (&x)[6], const float (&b)[6], float 
     itr_out = itr;
 }
 
-__global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
+__global__ void __launch_bounds__(128, 4) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
                                                    float *__restrict__ fpet, const uint8_t *__restrict__ codes,
                                                    const float *__restrict__ U, const float *__restrict__ V,
                                                    const float *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
@@ -356,7 +377,7 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
                    + s11 * pzm + s9 * pzp + s12 * nzm + s10 * nzp;
             x[m] = c0;
         }
-        const float dtwi = (float)(ph.dt / ph.wi);
+        const float dtwi = mc.dtwi;
         b[0] += dtwi; b[3] += dtwi; b[5] += dtwi;
         // velocity gradient (fenep.f90:541-550), A = transpose(A0) (fenep.f90:550)
         const float g00 = mc.gx1 * (u2 - u1);
@@ -369,13 +390,13 @@ __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, 
         const float g21 = mc.gz4 * (-V[h - oy - oz] - V[h - oz] + V[h - oy + oz] + V[h + oz]);
         const float g22 = mc.gz1 * (w2 - w1);
         int itr;
-        newton_solve_f(x, b, g00, g10, g20, g01, g11, g21, g02, g12, g22, dtwi, (float)ph.lp2, ph.lp2,
-                       (float)ph.newton_eps, ph.newton_itrmax, itr);
+        newton_solve_f(x, b, g00, g10, g20, g01, g11, g21, g02, g12, g22, dtwi, mc.lp2f, ph.lp2, mc.epsf,
+                       ph.newton_itrmax, itr);
         my_itr = (unsigned long long)itr;
         my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
 #pragma unroll
         for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
-        fpet[h] = peterlin_f(x[0], x[3], x[5], (float)ph.lp2, ph.lp2);
+        fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
     }
     unsigned long long a = my_itr, b2 = my_unconv;
     for (int o = 16; o > 0; o >>= 1) {
@@ -708,7 +729,7 @@ cudaError_t solve_walls_mp(Dev &d, const TS *src, double *dst, const double *bas
 // Fused path: transposing x pass, one CTA per kx for the (z, y) plane,
 // transposing inverse x pass.
 inline int x_rows_per_block(int nx) { return 2 * std::max(1, std::min(8, 1024 / std::max(nx / 2, 1))); }
-inline size_t x_smem(int nx, int rb) { return (size_t)(rb / 2) * 2 * nx * sizeof(float2) + (size_t)(nx / 2 + 1) * rb * sizeof(float2); }
+inline size_t x_smem(int nx, int rb) { return (size_t)(rb / 2) * 2 * nx * sizeof(float2) + (size_t)(nx / 2 + 1) * (rb + 1) * sizeof(float2); }
 inline int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
 
 template <typename TS>
@@ -748,7 +769,16 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
     if (sys == SYS_P) { ps.ai_base = (float)(2.0 * idy2); ps.bc = (float)idy2; ps.kap = -1.0f; }
     else { ps.ai_base = (float)(1.0 + kap * 2.0 * idy2); ps.bc = (float)(-kap * idy2); ps.kap = (float)kap; }
     const size_t smp = (size_t)12 * (lj | 1) * nz;
-    k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps);
+    if (d.wtP[0] && (nz == 32 || nz == 64 || nz == 128)) {
+        const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
+        WallTables wt{d.wtP[t], d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, ps.nxz_inv, sys};
+        const size_t smw = smp + (size_t)(nz / 2) * sizeof(float2);
+        if (nz == 32) k_plane_walls_w<1><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
+        else if (nz == 64) k_plane_walls_w<2><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
+        else k_plane_walls_w<4><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
+    } else {
+        k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps);
+    }
     k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
                                                                d.twxf_r, d.twxf_i);
     return cudaGetLastError();
@@ -781,6 +811,9 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_periodic, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
