@@ -79,6 +79,8 @@ ABI_FUNCTIONS = {
     "set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_longlong)]),
     "timing_reset": (C.c_int, [C.c_void_p]),
+    "fft_solve": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                            C.c_void_p, C.c_void_p, C.c_double, C.c_double]),
 }
 
 NSTAGE = 7

@@ -25,6 +25,7 @@ UNITS = {
     "f8_step_fp64.cu": ["--fmad=false"],
     "f8_api.cu": ["--fmad=false"],
     "f8_step_mixed.cu": [],
+    "f8_fftsolve.cu": ["--fmad=false"],
 }
 
 

@@ -90,7 +90,8 @@ __global__ void k_fft_x_fwd(const TS *__restrict__ src, T *__restrict__ H, int n
 // FP64 predicted velocity from the FP32 increment here).
 template <typename T, typename TO>
 __global__ void k_fft_x_inv(const T *__restrict__ H, TO *dst, const TO *base, int n, int nrow_h, int npairs_per_plane,
-                            int nplanes, int jdst0, int sx, int sy, const T *__restrict__ twr, const T *__restrict__ twi) {
+                            int nplanes, int jdst0, int sx, int sy, const T *__restrict__ twr, const T *__restrict__ twi,
+                            int plain = 0) {
     extern __shared__ unsigned char smem_raw[];
     Cx<T> *sm = reinterpret_cast<Cx<T> *>(smem_raw);
     const int half = n >> 1;
@@ -125,9 +126,12 @@ __global__ void k_fft_x_inv(const T *__restrict__ H, TO *dst, const TO *base, in
         Cx<T> *tmp = x; x = y; y = tmp;
     }
     if (!active) return;
-    const size_t oa = 1 + (size_t)sx * ((size_t)(jdst0 + jj) + (size_t)sy * (k + 1));
+    // halo layout (x at 1..n) or, with plain, a dense [k][j][x] array of
+    // row length n and sy rows per plane
+    const size_t oa = plain ? (size_t)n * ((size_t)(jdst0 + jj) + (size_t)sy * k)
+                            : 1 + (size_t)sx * ((size_t)(jdst0 + jj) + (size_t)sy * (k + 1));
     TO *ra = dst + oa;
-    TO *rb = ra + sx;
+    TO *rb = ra + (plain ? n : sx);
     if (base) {
         const TO *ba = base + oa, *bb = ba + sx;
         for (int e = t; e < n; e += tpp) { ra[e] = ba[e] + TO(x[e].r); rb[e] = bb[e] + TO(x[e].i); }

@@ -179,6 +179,19 @@ int f8_timing(f8_ctx *ctx, double *total_ms, double *stage_ms /* F8_NSTAGE or NU
               long long *steps_timed);
 int f8_timing_reset(f8_ctx *ctx);
 
+/* Stand-alone periodic spectral solve, the reference's fft_solve
+ * (fenep.f90:1400-1428): phi = IFFT( FFT(q) / (nx ny nz) / LHS ) with
+ * LHS = lhs0 + lhs1 * (k~x^2 + k~y^2 + k~z^2), k~^2 = 2(1 - cos(2 pi m/N))/d^2,
+ * and modes with |LHS| < 1e-16 set to zero.  lhs0 = 1, lhs1 = dt beta/(2 Re)
+ * is the CN Helmholtz solve of fft_navier (fenep.f90:1458-1479); lhs0 = 0,
+ * lhs1 = -1 the Poisson solve of fft_poisson (fenep.f90:1539-1557).
+ * q and phi are DEVICE pointers to dense nx*ny*nz arrays (x fastest, no halo;
+ * nz = 1 for a 2D field).  Sizes are powers of two.  FP64.  Allocates its
+ * workspace on the device for the duration of the call; runs on the default
+ * stream and returns when the result is complete. */
+int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz,
+                 const double *q, double *phi, double lhs0, double lhs1);
+
 const char *f8_strerror(int status);
 void f8_destroy(f8_ctx *ctx);
 

@@ -1704,8 +1704,9 @@ int f8o_fft_line(int n, double *re, double *im, int sign) {
 }
 
 // Periodic Helmholtz/Poisson solve on an interior-ordered field q (nx*ny*nz),
-// LHS = lhs0 + lhs1 * k~^2; result (interior order) in out.
-int f8o_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz, const double *q, double lhs0, double lhs1, double *out) {
+// LHS = lhs0 + lhs1 * k~^2; result (interior order) in phi.  Same argument
+// order as the library's f8_fft_solve (host pointers here).
+int f8o_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz, const double *q, double *out, double lhs0, double lhs1) {
     f8_grid g{}; g.dim = nz == 1 ? 2 : 3; g.nx = nx; g.ny = ny; g.nz = nz; g.lx = lx; g.ly = ly; g.lz = lz;
     f8_phys ph; f8o_default_phys(&ph);
     f8_ctx *cx = nullptr;

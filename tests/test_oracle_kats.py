@@ -38,7 +38,7 @@ def olib(oracle_lib):
     L.f8o_gauss.argtypes = [C.c_int, dp, dp, dp]
     L.f8o_tdma.argtypes = [C.c_int, dp, dp, dp, dp, dp]
     L.f8o_fft_line.argtypes = [C.c_int, dp, dp, C.c_int]
-    L.f8o_fft_solve.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [dp, C.c_double, C.c_double, dp]
+    L.f8o_fft_solve.argtypes = [C.c_int] * 3 + [C.c_double] * 3 + [dp, dp, C.c_double, C.c_double]
     L.f8o_roma.restype = C.c_double
     L.f8o_roma.argtypes = [C.c_double]
     return L
@@ -114,7 +114,7 @@ def test_fft_solve_vs_numpy(olib, shape, lx, kind):
     out = np.zeros_like(q)
     dt_b_re_2 = 1e-3 * 0.9 / 100 / 2
     lhs0, lhs1 = (0.0, -1.0) if kind == "poisson" else (1.0, dt_b_re_2)
-    olib.f8o_fft_solve(nx, ny, nz, lx, L, L, ptr(q), lhs0, lhs1, ptr(out))
+    olib.f8o_fft_solve(nx, ny, nz, lx, L, L, ptr(q), ptr(out), lhs0, lhs1)
     dx, dy, dz = lx / nx, L / ny, L / nz
     k2 = lambda n, d: 2 * (1 - np.cos(np.arange(n) * 2 * np.pi / n)) / d ** 2
     kk = k2(nx, dx)[None, None, :] + k2(ny, dy)[None, :, None] + (k2(nz, dz)[:, None, None] if nz > 1 else 0)
