@@ -1,0 +1,176 @@
+! f8_gpu.f90 -- iso_c_binding interface to the GB300 step library (libf8.so).
+!
+! A drop-in for the body of the reference's step loop (fenep.f90:2477-2527):
+! the main program keeps its own arrays, parameters and output code and calls
+!
+!   f8_create  once (replaces fft_init + ibm_init, fenep.f90:2459-2462)
+!   f8_load    after init / input (fenep.f90:2460-2461)
+!   f8_step    for Lstep/Gstep-sized chunks of steps
+!   f8_store   before log_progress / get_data_binary / output
+!   f8_destroy at the end (fft_finalize)
+!
+! Array arguments are the reference's own arrays, passed with c_loc():
+!   U, V, W, P, Phi : real(8) (0:NX+1, 0:NY+1, 0:NZ+1)
+!   C               : real(8) (6, 0:NX+1, 0:NY+1, 0:NZ+1)  (3 components in 2D)
+!   Ax0 .. Tz0, Fx..: real(8) (1:NX, 1:NY, 1:NZ)
+! so they must be declared with the TARGET attribute.  The layouts are the
+! C side's (include/f8.h): column-major, x fastest, component fastest for C.
+module f8_gpu
+    use, intrinsic :: iso_c_binding
+    implicit none
+
+    integer(c_int), parameter :: F8_OK = 0, F8_ERR_ARG = 1, F8_ERR_STATE = 2, F8_ERR_NOMEM = 3, &
+                                 F8_ERR_CUDA = 4, F8_ERR_NAN = 5, F8_ERR_UNSUPPORTED = 6, &
+                                 F8_ERR_NO_DEVICE = 7, F8_WARN_NEWTON = 16, F8_WARN_SOR = 17
+    integer(c_int), parameter :: F8_FP64 = 0, F8_MIXED = 1
+    integer(c_int), parameter :: F8_POISSON_FFT = 0, F8_POISSON_SOR = 1
+    integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1
+
+    type, bind(C) :: f8_grid
+        integer(c_int) :: dim, nx, ny, nz
+        real(c_double) :: lx, ly, lz
+        integer(c_int) :: bc_y
+        real(c_double) :: uwall
+    end type f8_grid
+
+    type, bind(C) :: f8_phys
+        real(c_double) :: re, wi, beta, lp2, dt
+        real(c_double) :: newton_dc, newton_eps
+        integer(c_int) :: newton_itrmax
+        real(c_double) :: sor_omega, sor_eps
+        integer(c_int) :: sor_itrmax
+        integer(c_int) :: ab2_start
+    end type f8_phys
+
+    type, bind(C) :: f8_cyl
+        real(c_double) :: xc, yc, r, spin
+        integer(c_int) :: filled
+    end type f8_cyl
+
+    type, bind(C) :: f8_fields
+        type(c_ptr) :: u = c_null_ptr, v = c_null_ptr, w = c_null_ptr, p = c_null_ptr, phi = c_null_ptr
+        type(c_ptr) :: c = c_null_ptr
+        type(c_ptr) :: ax0 = c_null_ptr, ay0 = c_null_ptr, az0 = c_null_ptr
+        type(c_ptr) :: tx0 = c_null_ptr, ty0 = c_null_ptr, tz0 = c_null_ptr
+        type(c_ptr) :: fx = c_null_ptr, fy = c_null_ptr, fz = c_null_ptr
+    end type f8_fields
+
+    type, bind(C) :: f8_diag
+        integer(c_int) :: step
+        real(c_double) :: ke, cfl, trc_min, trc_max, trc_mean, div_max
+        integer(c_long_long) :: newton_iters, newton_unconverged
+        integer(c_int) :: poisson_iters, nan_found
+    end type f8_diag
+
+    interface
+        subroutine f8_default_phys(phys) bind(C, name="f8_default_phys")
+            import :: f8_phys
+            type(f8_phys), intent(out) :: phys
+        end subroutine f8_default_phys
+
+        integer(c_int) function f8_create(ctx, grid, phys, cyls, ncyl, precision, poisson) bind(C, name="f8_create")
+            import :: c_ptr, c_int, f8_grid, f8_phys, f8_cyl
+            type(c_ptr), intent(out) :: ctx
+            type(f8_grid), intent(in) :: grid
+            type(f8_phys), intent(in) :: phys
+            type(f8_cyl), intent(in) :: cyls(*)
+            integer(c_int), value :: ncyl, precision, poisson
+        end function f8_create
+
+        integer(c_int) function f8_load(ctx, fields, step0) bind(C, name="f8_load")
+            import :: c_ptr, c_int, f8_fields
+            type(c_ptr), value :: ctx
+            type(f8_fields), intent(in) :: fields
+            integer(c_int), value :: step0
+        end function f8_load
+
+        ! drag: real(8) (3, ncyl, nsteps), or c_null_ptr
+        integer(c_int) function f8_step(ctx, nsteps, drag) bind(C, name="f8_step")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nsteps
+            type(c_ptr), value :: drag
+        end function f8_step
+
+        integer(c_int) function f8_store(ctx, fields) bind(C, name="f8_store")
+            import :: c_ptr, c_int, f8_fields
+            type(c_ptr), value :: ctx
+            type(f8_fields), intent(in) :: fields
+        end function f8_store
+
+        integer(c_int) function f8_diagnostics(ctx, diag) bind(C, name="f8_diagnostics")
+            import :: c_ptr, c_int, f8_diag
+            type(c_ptr), value :: ctx
+            type(f8_diag), intent(out) :: diag
+        end function f8_diagnostics
+
+        integer(c_int) function f8_markers(ctx, n, xy) bind(C, name="f8_markers")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            integer(c_int), intent(out) :: n
+            type(c_ptr), value :: xy
+        end function f8_markers
+
+        integer(c_int) function f8_set_timing(ctx, enable) bind(C, name="f8_set_timing")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: enable
+        end function f8_set_timing
+
+        ! stage_ms: real(8) (7): C+-, Newton, momentum, IBM, Helmholtz, Poisson, projection
+        integer(c_int) function f8_timing(ctx, total_ms, stage_ms, steps_timed) bind(C, name="f8_timing")
+            import :: c_ptr, c_int, c_double, c_long_long
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: total_ms
+            real(c_double), intent(out) :: stage_ms(*)
+            integer(c_long_long), intent(out) :: steps_timed
+        end function f8_timing
+
+        integer(c_int) function f8_timing_reset(ctx) bind(C, name="f8_timing_reset")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+        end function f8_timing_reset
+
+        ! q and phi are device pointers (e.g. from a CUDA Fortran or OpenACC code)
+        integer(c_int) function f8_fft_solve(nx, ny, nz, lx, ly, lz, q, phi, lhs0, lhs1) bind(C, name="f8_fft_solve")
+            import :: c_int, c_double, c_ptr
+            integer(c_int), value :: nx, ny, nz
+            real(c_double), value :: lx, ly, lz
+            type(c_ptr), value :: q, phi
+            real(c_double), value :: lhs0, lhs1
+        end function f8_fft_solve
+
+        type(c_ptr) function f8_strerror_c(status) bind(C, name="f8_strerror")
+            import :: c_ptr, c_int
+            integer(c_int), value :: status
+        end function f8_strerror_c
+
+        subroutine f8_destroy(ctx) bind(C, name="f8_destroy")
+            import :: c_ptr
+            type(c_ptr), value :: ctx
+        end subroutine f8_destroy
+    end interface
+
+contains
+
+    ! Fortran string of a status code
+    function f8_strerror(status) result(msg)
+        integer(c_int), intent(in) :: status
+        character(len=:), allocatable :: msg
+        character(kind=c_char), pointer :: chars(:)
+        type(c_ptr) :: p
+        integer :: n
+        interface
+            integer(c_size_t) function c_strlen(s) bind(C, name="strlen")
+                import :: c_ptr, c_size_t
+                type(c_ptr), value :: s
+            end function c_strlen
+        end interface
+        p = f8_strerror_c(status)
+        n = int(c_strlen(p))
+        call c_f_pointer(p, chars, [n])
+        allocate(character(len=n) :: msg)
+        msg = transfer(chars(1:n), msg)
+    end function f8_strerror
+
+end module f8_gpu
