@@ -21,7 +21,8 @@ module f8_gpu
 
     integer(c_int), parameter :: F8_OK = 0, F8_ERR_ARG = 1, F8_ERR_STATE = 2, F8_ERR_NOMEM = 3, &
                                  F8_ERR_CUDA = 4, F8_ERR_NAN = 5, F8_ERR_UNSUPPORTED = 6, &
-                                 F8_ERR_NO_DEVICE = 7, F8_WARN_NEWTON = 16, F8_WARN_SOR = 17
+                                 F8_ERR_NO_DEVICE = 7, F8_ERR_TOO_LARGE = 8, F8_WARN_NEWTON = 16, &
+                                 F8_WARN_SOR = 17
     integer(c_int), parameter :: F8_FP64 = 0, F8_MIXED = 1
     integer(c_int), parameter :: F8_POISSON_FFT = 0, F8_POISSON_SOR = 1
     integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1
@@ -139,6 +140,17 @@ module f8_gpu
             type(c_ptr), value :: q, phi
             real(c_double), value :: lhs0, lhs1
         end function f8_fft_solve
+
+        ! the same solve on a fixed device workspace, for callers that must not
+        ! let the library allocate; (nx/2+1)*ny*nz <= 135168, no concurrent calls
+        integer(c_int) function f8_fft_solve_noalloc(nx, ny, nz, lx, ly, lz, q, phi, lhs0, lhs1) &
+                bind(C, name="f8_fft_solve_noalloc")
+            import :: c_int, c_double, c_ptr
+            integer(c_int), value :: nx, ny, nz
+            real(c_double), value :: lx, ly, lz
+            type(c_ptr), value :: q, phi
+            real(c_double), value :: lhs0, lhs1
+        end function f8_fft_solve_noalloc
 
         type(c_ptr) function f8_strerror_c(status) bind(C, name="f8_strerror")
             import :: c_ptr, c_int

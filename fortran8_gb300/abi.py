@@ -16,6 +16,7 @@ F8_ERR_CUDA = 4
 F8_ERR_NAN = 5
 F8_ERR_UNSUPPORTED = 6
 F8_ERR_NO_DEVICE = 7
+F8_ERR_TOO_LARGE = 8
 F8_WARN_NEWTON = 16
 F8_WARN_SOR = 17
 

@@ -718,6 +718,7 @@ const char *f8_strerror(int st) {
     case F8_ERR_NAN: return "NaN in the velocity field";
     case F8_ERR_UNSUPPORTED: return "unsupported option";
     case F8_ERR_NO_DEVICE: return "no CUDA device";
+    case F8_ERR_TOO_LARGE: return "grid exceeds the fixed workspace of the allocation-free solve";
     case F8_WARN_NEWTON: return "Newton iteration limit reached in some cells";
     case F8_WARN_SOR: return "SOR iteration limit reached";
     default: return "unknown status";

@@ -121,3 +121,98 @@ extern "C" int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double
     cudaGetLastError();
     return st;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some host programs cannot let a library call cudaMalloc: for example a
+// solver driver that reserves all the device memory it may use at start-up
+// (its own pool, or a budget shared with other jobs on the same GPU), so an
+// allocation inside the time loop would fail or fragment that budget.  For
+// them f8_fft_solve_noalloc runs the same periodic solve as f8_fft_solve with
+// its workspace in fixed arrays of device memory that exist from the moment
+// the library is loaded on a device, and calls no allocating routine.
+//
+// Limits and rules (also stated in include/f8.h):
+//  * the spectrum of the grid must fit in F8_NOALLOC_MAX_SPECTRUM complex
+//    values, (nx/2+1)*ny*nz <= 135168 (for example 64^3, 128 x 64 x 32 or a
+//    2D 512 x 256 field); larger grids get F8_ERR_TOO_LARGE;
+//  * the arrays are shared by every call in the process on a device and keep
+//    the last call's contents; each call overwrites all it reads (the forward
+//    transform fills the whole spectrum and the tables are rewritten), so
+//    nothing has to start at zero, but calls that overlap on the GPU (from
+//    several host threads, or other streams) race on the arrays;
+//  * the first call on a device looks up the device addresses of the arrays
+//    (cudaGetSymbolAddress, with that device current); make that first call
+//    before any stream capture on that device.
+
+#include <mutex>
+
+#define F8_NOALLOC_MAX_SPECTRUM 135168   /* complex values: 65 * 64 * 32 = 33 * 64 * 64 */
+#define F8_NOALLOC_MAX_TABLE 8192        /* doubles: twiddles and wavenumbers, N <= 1024 */
+
+static __device__ __align__(256) double g_noalloc_spectrum[2 * F8_NOALLOC_MAX_SPECTRUM];
+static __device__ __align__(256) double g_noalloc_table[F8_NOALLOC_MAX_TABLE];
+
+namespace {
+
+struct NoallocPtrs {
+    double *spec = nullptr;
+    double *tab = nullptr;
+};
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoallocPtrs g_noalloc_ptrs[kMaxDevices];
+
+// Device addresses of the fixed arrays on the current device (looked up once
+// per device; the symbol names are host-side stand-ins, not device addresses).
+int noalloc_setup(NoallocPtrs &out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return F8_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    NoallocPtrs &p = g_noalloc_ptrs[dev];
+    if (!p.spec) {
+        void *a = nullptr, *b = nullptr;
+        if (cudaGetSymbolAddress(&a, g_noalloc_spectrum) != cudaSuccess ||
+            cudaGetSymbolAddress(&b, g_noalloc_table) != cudaSuccess) {
+            cudaGetLastError();
+            return F8_ERR_CUDA;
+        }
+        if (set_smem_attrs() != cudaSuccess) {
+            cudaGetLastError();
+            return F8_ERR_CUDA;
+        }
+        p.spec = static_cast<double *>(a);
+        p.tab = static_cast<double *>(b);
+    }
+    out = p;
+    return F8_OK;
+}
+
+}  // namespace
+
+extern "C" int f8_fft_solve_noalloc(int nx, int ny, int nz, double lx, double ly, double lz, const double *q,
+                                    double *phi, double lhs0, double lhs1) {
+    if (int st = check_args(nx, ny, nz, lx, ly, lz, q, phi)) return st;
+    if ((size_t)(nx / 2 + 1) * ny * nz > (size_t)F8_NOALLOC_MAX_SPECTRUM) return F8_ERR_TOO_LARGE;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return F8_ERR_NO_DEVICE;
+    }
+    NoallocPtrs p;
+    if (int st = noalloc_setup(p)) return st;
+    const SolveTables t = make_tables(nx, ny, nz, lx, ly, lz);
+    if (t.buf.size() > (size_t)F8_NOALLOC_MAX_TABLE) return F8_ERR_TOO_LARGE;
+    if (cudaMemcpyAsync(p.tab, t.buf.data(), t.buf.size() * sizeof(double), cudaMemcpyHostToDevice, 0) != cudaSuccess ||
+        run_solve(q, phi, p.spec, p.tab, t, nx, ny, nz, lhs0, lhs1, 0) != cudaSuccess ||
+        cudaStreamSynchronize(0) != cudaSuccess) {
+        cudaGetLastError();
+        return F8_ERR_CUDA;
+    }
+    return F8_OK;
+}

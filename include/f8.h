@@ -44,6 +44,8 @@ enum f8_status {
                                (reference: stop 'NaN value', fenep_2d.f90:1974)   */
     F8_ERR_UNSUPPORTED = 6, /* option combination not built                        */
     F8_ERR_NO_DEVICE = 7,   /* no CUDA device / extension not usable               */
+    F8_ERR_TOO_LARGE = 8,   /* grid exceeds the fixed workspace of
+                               f8_fft_solve_noalloc                                */
     F8_WARN_NEWTON = 16,    /* some cells reached newton_itrmax without meeting
                                newton_eps (reference continues silently,
                                fenep.f90:556-577)                                  */
@@ -191,6 +193,24 @@ int f8_timing_reset(f8_ctx *ctx);
  * stream and returns when the result is complete. */
 int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz,
                  const double *q, double *phi, double lhs0, double lhs1);
+
+/* The same solve as f8_fft_solve for callers that cannot let a library
+ * allocate device memory (for example a driver that reserves all its device
+ * memory at start-up, so an allocation during the run would fail or break its
+ * budget).  No counterpart in the reference.  It calls no cudaMalloc, cudaFree
+ * or other allocating routine: its workspace is a fixed device array of
+ * 2.2 MB (plus 64 KB of tables) that every GPU which loads the library holds
+ * until the process exits.  Limits and rules:
+ *   - (nx/2+1)*ny*nz <= 135168 complex values (e.g. 64^3); larger grids return
+ *     F8_ERR_TOO_LARGE;
+ *   - every call shares that workspace and leaves its contents behind; each
+ *     call overwrites what it reads, but calls that overlap on the GPU (from
+ *     several threads or streams) race;
+ *   - the first call on a device looks up the workspace address on that
+ *     device (the device must be current); make it before any stream capture.
+ * q and phi are caller-owned DEVICE buffers as for f8_fft_solve. */
+int f8_fft_solve_noalloc(int nx, int ny, int nz, double lx, double ly, double lz,
+                         const double *q, double *phi, double lhs0, double lhs1);
 
 const char *f8_strerror(int status);
 void f8_destroy(f8_ctx *ctx);

@@ -1613,6 +1613,7 @@ const char *f8o_strerror(int st) {
     case F8_ERR_NOMEM: return "out of memory";
     case F8_ERR_NAN: return "NaN in the velocity field";
     case F8_ERR_UNSUPPORTED: return "unsupported option";
+    case F8_ERR_TOO_LARGE: return "grid exceeds the fixed workspace of the allocation-free solve";
     case F8_WARN_NEWTON: return "Newton iteration limit reached in some cells";
     case F8_WARN_SOR: return "SOR iteration limit reached";
     default: return "unknown status";
@@ -1720,6 +1721,13 @@ int f8o_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz, const
             for (int i = 1; i <= nx; ++i) out[c.iidx(i, j, k)] = H[c.hidx(i, j, k)];
     f8o_destroy(cx);
     return 0;
+}
+
+// The oracle allocates freely; it exports the allocation-free name so that
+// one harness can bind both libraries.
+int f8o_fft_solve_noalloc(int nx, int ny, int nz, double lx, double ly, double lz, const double *q, double *out,
+                          double lhs0, double lhs1) {
+    return f8o_fft_solve(nx, ny, nz, lx, ly, lz, q, out, lhs0, lhs1);
 }
 
 }  // extern "C"
