@@ -38,8 +38,9 @@ from fortran8_gb300.solver import Solver  # noqa: E402
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 
-# Algorithmic bytes per cell of each stage of the FP64 step (words of 8 B):
-# every field a stage must read once and write once.
+# Algorithmic bytes per cell of each stage: every field a stage must read once
+# and write once (FFT-internal passes and marker traffic excluded).
+# FP64 step, in words of 8 B:
 FP64_STAGE_WORDS = {
     "eigen": 6.125,      # C (6) read, 1-byte selection code written
     "newton": 16.125,    # C, U, V, W read (9) + code; C (6) and f(C) (1) written
@@ -49,6 +50,25 @@ FP64_STAGE_WORDS = {
     "poisson": 5.0,      # U* (3) read, RHS, Phi written (FFT-internal passes excluded)
     "project": 9.0,      # U*, Phi, P read (5); U, V, W, P written (4)
 }
+# FP32-mixed step, in bytes (FP32: C, f, A0, T0, F, velocity copies, RHS;
+# FP64: U, V, W, P, Phi, U*):
+MIXED_STAGE_BYTES = {
+    "eigen": 25.0,       # C 24 read, code 1 written
+    "newton": 65.0,      # C 24, velocity copies 12, code 1 read; C 24, f 4 written
+    "momentum": 120.0,   # velocity copies 12, P 8, C 24, f 4, A0 12, T0 12, F 12 read; Q 12, A0 12, T0 12 written
+    "ibm": 0.0,          # marker stencils only (not a per-cell stage)
+    "helmholtz": 60.0,   # 3 x (RHS 4 + U^n 8 read, U* 8 written)
+    "poisson": 96.0,     # div: U* 24 read, rhs 8 written; solve, defect (Phi 8 + rhs 8 read, r 8 written), correction
+    "project": 84.0,     # U* 24, Phi 8, P 8 read; U, V, W 24, FP32 copies 12, P 8 written
+}
+
+
+def load_traffic(precision):
+    """ncu DRAM bytes per launch of the stage kernels (profiles/traffic_<precision>_c3_channel.json)."""
+    p = ROOT / "profiles" / f"traffic_{precision}_c3_channel.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
 
 
 def load_peaks():
@@ -75,7 +95,7 @@ class ClockSampler:
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -182,7 +202,10 @@ def cpu_baseline(w, steps_cap=2, budget_s=30.0):
                       f"FP64, {threads} OpenMP threads, {el:.1f} s"}
 
 
-def run_reference(args, w):
+def run_reference(args, w, budget_s=90.0):
+    """The CPU oracle on all host cores.  Each step is a full step of the workload;
+    the timed sample stops after K steps or once the time budget is spent, so
+    the run ends within a few minutes (the sample is stated in the output)."""
     ws, rank, _ = dist_init()
     if rank != 0:
         return 0
@@ -190,18 +213,24 @@ def run_reference(args, w):
     threads = int(lib.f8o_max_threads())
     with Solver(fns, w.grid, w.phys, w.cyls) as s:
         s.load(configs.initial_state(w))
-        s.step(args.warmup)
+        s.step(min(args.warmup, 1))
         t0 = time.perf_counter()
-        s.step(args.steps)
+        n = 0
+        while n < args.steps:
+            s.step(1)
+            n += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
         el = time.perf_counter() - t0
-    v = w.cells * args.steps / el / 1e6
+    v = w.cells * n / el / 1e6
+    sample = (f"{n} full FP64 steps of {w.grid.nx}x{w.grid.ny}x{w.grid.nz} (of {args.steps} requested, "
+              f"{budget_s:.0f} s budget) after {min(args.warmup, 1)} warm-up step, {threads} OpenMP threads")
     line = {"impl": "reference", "metric": "Mcell-steps/s", "value": v, "unit": "Mcell-steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+            "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1), "ms_per_step": el * 1e3 / n,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
                        "poisson": "fft+tridiagonal"},
-            "cpu_baseline": {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} full steps after {args.warmup} warm-up, FP64, {threads} threads"},
+            "cpu_baseline": {"value": v, "unit": "Mcell-steps/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -234,6 +263,7 @@ def run_ours(args, w):
         tot_ms, stage_ms, nst = s.timing()
         clocks = clk.summary()
         diag = s.diagnostics()
+        launches = int(diag.kernel_launches)
     ms = max_over_ranks(ws, tot_ms)
     value = cells * args.steps * ws / (ms / 1e3) / 1e6
     # e2e: host arrays in, K single-step calls reading the drag every step, host arrays out
@@ -253,25 +283,26 @@ def run_ours(args, w):
     # the FP64 path on the same workload and the drag difference (accuracy gate)
     cmp = None
     if prec == abi.F8_MIXED and not args.no_fp64_compare:
+        k64 = min(args.steps, 200)   # the FP64 path runs at ~80 ms/step here
         with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s64:
             s64.load(st0)
             _, d64w = s64.step(args.warmup)
             s64.set_timing(True)
             s64.timing_reset()
-            _, d64 = s64.step(args.steps)
+            _, d64 = s64.step(k64)
             t64, st64, n64 = s64.timing()
         with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as sm:
             sm.load(st0)
             _, dmw = sm.step(args.warmup)
-            _, dm = sm.step(args.steps)
+            _, dm = sm.step(k64)
         dall64 = np.concatenate([d64w, d64]) if d64w is not None else d64
         dallm = np.concatenate([dmw, dm]) if dmw is not None else dm
         rel = None
         if dall64 is not None:
             rel = float(np.max(np.abs(dallm[..., 0] - dall64[..., 0])) / np.max(np.abs(dall64[..., 0])))
-        v64 = cells * args.steps / (t64 / 1e3) / 1e6
-        cmp = {"fp64_value": v64, "fp64_ms_per_step": t64 / args.steps, "mixed_over_fp64": value / v64,
-               "drag_rel_err_vs_fp64": rel, "steps_compared": args.warmup + args.steps,
+        v64 = cells * k64 / (t64 / 1e3) / 1e6
+        cmp = {"fp64_value": v64, "fp64_ms_per_step": t64 / k64, "mixed_over_fp64": value / v64,
+               "drag_rel_err_vs_fp64": rel, "steps_compared": args.warmup + k64,
                "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
@@ -284,11 +315,21 @@ def run_ours(args, w):
     per_step = stage_ms / max(nst, 1)
     names = abi.STAGE_NAMES
     top = int(np.argmax(per_step))
-    words = FP64_STAGE_WORDS[names[top]]
-    achieved = words * 8 * cells / (per_step[top] / 1e3) / 1e9
+    if prec == abi.F8_FP64:
+        stage_bytes = {k: v * 8 for k, v in FP64_STAGE_WORDS.items()}
+    else:
+        stage_bytes = MIXED_STAGE_BYTES
+    byts = stage_bytes[names[top]] * cells
+    achieved = byts / (per_step[top] / 1e3) / 1e9
+    traffic = load_traffic(args.precision).get(names[top])
     roof = {"bound": "hbm", "kernel_stage": names[top], "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
-            "traffic": None, "stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)}}
+            "traffic": traffic, "algorithmic_bytes": byts,
+            "stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)},
+            "stage_hbm_frac": {n: (stage_bytes[n] * cells / (float(v) / 1e3) / 1e9 / peaks["hbm_gbs"]) if v > 0 else None
+                               for n, v in zip(names, per_step)},
+            "step_bytes": sum(stage_bytes.values()) * cells,
+            "step_hbm_frac": sum(stage_bytes.values()) * cells / (ms / args.steps / 1e3) / 1e9 / peaks["hbm_gbs"]}
     line = {"metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == abi.F8_FP64 else "f32+f64",
@@ -298,7 +339,7 @@ def run_ours(args, w):
                        "l2": "inputs larger than L2 (state %.2f GB)" % (sb / 1e9), "parallelism": f"replicas{ws}"},
             "status": int(status), "div_max": diag.div_max, "newton_iters_per_cell": diag.newton_iters / cells,
             "drag_last": drag[-1].tolist() if drag is not None else None,
-            "gpu_launches": None, "clocks": clocks, "roofline": roof, "e2e": e2e, "fp64_compare": cmp}
+            "gpu_launches": launches, "clocks": clocks, "roofline": roof, "e2e": e2e, "fp64_compare": cmp}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
     print(json.dumps(line))
@@ -308,8 +349,8 @@ def run_ours(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))

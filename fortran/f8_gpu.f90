@@ -61,6 +61,7 @@ module f8_gpu
         real(c_double) :: ke, cfl, trc_min, trc_max, trc_mean, div_max
         integer(c_long_long) :: newton_iters, newton_unconverged
         integer(c_int) :: poisson_iters, nan_found
+        integer(c_long_long) :: kernel_launches
     end type f8_diag
 
     interface

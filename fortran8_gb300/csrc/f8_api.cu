@@ -101,6 +101,7 @@ struct f8_ctx {
     cudaEvent_t tot0 = nullptr, tot1 = nullptr;
     double total_ms = 0.0, stage_ms[NSTAGE] = {};
     long long timed_steps = 0;
+    long long step_launches = 0;   // kernels launched by f8_step since load / timing reset
 
     template <typename T>
     cudaError_t alloc(T **p, size_t n) {
@@ -526,6 +527,7 @@ int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
     c->step = step0;
     c->step0 = step0;
     c->loaded = true;
+    c->step_launches = 0;
     return F8_OK;
 }
 
@@ -545,6 +547,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         for (size_t q = have; q < c->evpool.size(); ++q) API_CUDA(c, cudaEventCreate(&c->evpool[q]));
     }
     API_CUDA(c, cudaEventRecord(c->tot0, c->s));
+    const long long launches0 = g_kernel_launches.load();
     int worst = F8_OK;
     for (int s = 0; s < nsteps; ++s) {
         StepOpts o{};
@@ -570,6 +573,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     }
     API_CUDA(c, cudaEventRecord(c->tot1, c->s));
     API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
+    c->step_launches += g_kernel_launches.load() - launches0;
     StepCounters cnt{};
     unsigned long long nan = 0;
     API_CUDA(c, cudaMemcpyAsync(&cnt, d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c->s));
@@ -674,6 +678,7 @@ int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
     dg->newton_iters = c->last_newton_iters;
     dg->newton_unconverged = c->last_newton_unconv;
     dg->poisson_iters = c->last_poisson_iters;
+    dg->kernel_launches = c->step_launches;
     return F8_OK;
 }
 
@@ -705,6 +710,7 @@ int f8_timing_reset(f8_ctx *c) {
     c->total_ms = 0.0;
     for (int q = 0; q < NSTAGE; ++q) c->stage_ms[q] = 0.0;
     c->timed_steps = 0;
+    c->step_launches = 0;
     return F8_OK;
 }
 

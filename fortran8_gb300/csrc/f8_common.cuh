@@ -10,6 +10,7 @@
 //     (i-1) + NX*((j-1) + NY*(k-1)).
 //   spectra: complex (re, im interleaved) [k][j][kx], kx in 0..NX/2.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -40,6 +41,11 @@ struct Phys {
 
 // Boundary-condition kinds of the halo fill kernel.
 enum BcKind { BC_U = 0, BC_V = 1, BC_W = 2, BC_P = 3, BC_C = 4, BC_CODE = 5 };
+
+// Kernel launches issued by this library in the process (reported through
+// f8_diagnostics so that a caller can count the launches of a timed region).
+inline std::atomic<long long> g_kernel_launches{0};
+inline void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // Per-step device counters (status words read by the host after a step).
 struct StepCounters {

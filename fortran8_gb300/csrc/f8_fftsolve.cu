@@ -61,18 +61,18 @@ cudaError_t run_solve(const double *q, double *phi, double *H, const double *dta
     const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
     const int npp = ny / 2, total = npp * nz;
     const size_t smx = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-    k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(q, H, nx, ny, 1, ny, npp, nz, twx_r, twx_i);
+    k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(q, H, nx, ny, 1, ny, npp, nz, twx_r, twx_i); count_launch();
     DivideSpec none{};
     const int txy = std::max(1, std::min(32, 2048 / ny));
     const size_t smy = (size_t)2 * ny * txy * sizeof(Cx<double>);
-    k_fft_lines<double><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(H, ny, nxh, nxh, nxh * ny, txy, twy_r, twy_i, -1, 0, none);
+    k_fft_lines<double><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(H, ny, nxh, nxh, nxh * ny, txy, twy_r, twy_i, -1, 0, none); count_launch();
     DivideSpec dv{dtab + t.kx2, dtab + t.ky2, dtab + t.kz2, lhs0, lhs1, (double)nx * ny * nz, 1};
     const int txz = std::max(1, std::min(32, 2048 / nz));
     const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<double>);
-    k_fft_lines<double><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(H, nz, nxh * ny, nxh, nxh, txz, twz_r, twz_i, -1, 1, dv);
-    k_fft_lines<double><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(H, ny, nxh, nxh, nxh * ny, txy, twy_r, twy_i, +1, 0, none);
+    k_fft_lines<double><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(H, nz, nxh * ny, nxh, nxh, txz, twz_r, twz_i, -1, 1, dv); count_launch();
+    k_fft_lines<double><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(H, ny, nxh, nxh, nxh * ny, txy, twy_r, twy_i, +1, 0, none); count_launch();
     k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(H, phi, nullptr, nx, ny, npp, nz, 0, nx, ny,
-                                                                            twx_r, twx_i, 1);
+                                                                            twx_r, twx_i, 1); count_launch();
     return cudaGetLastError();
 }
 

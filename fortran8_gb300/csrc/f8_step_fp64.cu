@@ -985,7 +985,7 @@ inline dim3 cell_grid(const Geo &g, dim3 blk) {
 
 cudaError_t bc(double *A, const Geo &g, int kind, cudaStream_t s) {
     long n = halo_count(g) + ((kind == BC_V && g.walls) ? (long)g.nx * g.nz : 0);
-    k_bc_scalar<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, g, kind);
+    k_bc_scalar<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, g, kind); count_launch();
     return cudaGetLastError();
 }
 
@@ -998,7 +998,7 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i); count_launch();
     }
     DivideSpec none{};
     // y forward (line along y: stride nxh, sets = k planes)
@@ -1006,7 +1006,7 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tx = std::max(1, std::min(32, 2048 / ny));
         size_t smem = (size_t)2 * ny * tx * sizeof(Cx<double>);
         dim3 grid((nxh + tx - 1) / tx, nz);
-        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, -1, 0, none);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, -1, 0, none); count_launch();
     }
     // z forward + divide + z inverse (line along z: stride nxh*ny, sets = j)
     {
@@ -1014,21 +1014,21 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tx = std::max(1, std::min(32, 2048 / nz));
         size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
         dim3 grid((nxh + tx - 1) / tx, ny);
-        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 1, dv);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 1, dv); count_launch();
     }
     // y inverse
     {
         int tx = std::max(1, std::min(32, 2048 / ny));
         size_t smem = (size_t)2 * ny * tx * sizeof(Cx<double>);
         dim3 grid((nxh + tx - 1) / tx, nz);
-        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, +1, 0, none);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, ny, nxh, nxh, nxh * ny, tx, d.twy_r, d.twy_i, +1, 0, none); count_launch();
     }
     // x inverse
     {
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nullptr, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i);
+        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nullptr, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -1043,32 +1043,32 @@ cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double u
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i);
+        k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(src, d.H, nx, ny, 1, ny, npp, nz, d.twx_r, d.twx_i); count_launch();
     }
     if (nz > 1) {
         int tx = std::max(1, std::min(32, 2048 / nz));
         size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
         dim3 grid((nxh + tx - 1) / tx, ny);
-        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 0, none);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H, nz, nxh * ny, nxh, nxh, tx, d.twz_r, d.twz_i, -1, 0, none); count_launch();
     }
     {
         WallSpec w{d.kx2, d.kz2, d.ph.dt, d.ph.beta, d.ph.re, g.dy, (double)nx * nz, uwall, sys};
         int tx = 16;
         size_t smem = (size_t)n * tx * (sizeof(Cx<double>) + sizeof(double));
         dim3 grid((nxh + tx - 1) / tx, nz);
-        k_wall_tdma<double><<<grid, 128, smem, s>>>(d.H, d.H2, ny, nxh, tx, w);
+        k_wall_tdma<double><<<grid, 128, smem, s>>>(d.H, d.H2, ny, nxh, tx, w); count_launch();
     }
     if (nz > 1) {
         int tx = std::max(1, std::min(32, 2048 / nz));
         size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
         dim3 grid((nxh + tx - 1) / tx, n);
-        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H2, nz, nxh * n, nxh, nxh, tx, d.twz_r, d.twz_i, +1, 0, none);
+        k_fft_lines<double><<<grid, 256, smem, s>>>(d.H2, nz, nxh * n, nxh, nxh, tx, d.twz_r, d.twz_i, +1, 0, none); count_launch();
     }
     {
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = n / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nullptr, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i);
+        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nullptr, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -1076,8 +1076,8 @@ cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double u
 cudaError_t reduce_sumsq(const double *A, int n, double *part, double *scal, int slot, int mode, int *flag, double eps,
                          int itr, const Geo &g, cudaStream_t s) {
     int nb = std::min(1024, (n + 255) / 256);
-    k_reduce_part<0><<<nb, 256, 0, s>>>(A, n, part, g, mode == 1 ? flag : nullptr);
-    k_reduce_final<<<1, 256, 0, s>>>(part, nb, scal, slot, mode, flag, eps, itr);
+    k_reduce_part<0><<<nb, 256, 0, s>>>(A, n, part, g, mode == 1 ? flag : nullptr); count_launch();
+    k_reduce_final<<<1, 256, 0, s>>>(part, nb, scal, slot, mode, flag, eps, itr); count_launch();
     return cudaGetLastError();
 }
 
@@ -1096,10 +1096,10 @@ cudaError_t sor_solve(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
         int last = std::min(o.sor_itrmax, it0 + chunk - 1);
         for (int it = it0; it <= last; ++it) {
             for (int color = 0; color < 2; ++color) {
-                k_sor_color<<<grd, blk, 0, s>>>(d.Phi, d.E, d.Q[0], g, color, o.sor_omega, d.flag);
-                k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag);
+                k_sor_color<<<grd, blk, 0, s>>>(d.Phi, d.E, d.Q[0], g, color, o.sor_omega, d.flag); count_launch();
+                k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag); count_launch();
             }
-            k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag);
+            k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag); count_launch();
             F8_CUDA_RET(reduce_sumsq(d.E, d.ni, d.red, d.scal, 1, 1, d.flag, o.sor_eps, it, g, s));
         }
         F8_CUDA_RET(cudaMemcpyAsync(it_host, d.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1109,9 +1109,9 @@ cudaError_t sor_solve(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
     *iters = done ? it_host[1] : o.sor_itrmax + 1;
     // zero-mean shift (fenep_2d.f90:577-579)
     int nb = std::min(1024, (d.ni + 255) / 256);
-    k_reduce_part<1><<<nb, 256, 0, s>>>(d.Phi, d.ni, d.red, g, nullptr);
-    k_reduce_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 2, 0, d.flag, 0.0, 0);
-    k_shift<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Phi, d.cs, d.scal, 2, 1.0 / ((double)g.nx * g.ny * g.nz));
+    k_reduce_part<1><<<nb, 256, 0, s>>>(d.Phi, d.ni, d.red, g, nullptr); count_launch();
+    k_reduce_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 2, 0, d.flag, 0.0, 0); count_launch();
+    k_shift<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Phi, d.cs, d.scal, 2, 1.0 / ((double)g.nx * g.ny * g.nz)); count_launch();
     return cudaGetLastError();
 }
 
@@ -1133,8 +1133,8 @@ cudaError_t bc_all_state_fp64(Dev &d, cudaStream_t s) {
     if (d.g.dim == 3 && (e = bc(d.W, d.g, BC_W, s))) return e;
     if ((e = bc(d.P, d.g, BC_P, s))) return e;
     long n = halo_count(d.g);
-    k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, d.g, d.ncomp, d.cs, d.ph.lp2);
-    k_pet_all<<<(d.cs + 255) / 256, 256, 0, s>>>(d.C, d.fpet, d.ncomp, d.cs, d.ph.lp2);
+    k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, d.g, d.ncomp, d.cs, d.ph.lp2); count_launch();
+    k_pet_all<<<(d.cs + 255) / 256, 256, 0, s>>>(d.C, d.fpet, d.ncomp, d.cs, d.ph.lp2); count_launch();
     return cudaGetLastError();
 }
 
@@ -1142,35 +1142,35 @@ cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s) { return
 
 cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s) {
     dim3 blk(32, 8);
-    k_poisson_rhs<<<cell_grid(d.g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, out, d.g);
+    k_poisson_rhs<<<cell_grid(d.g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, out, d.g); count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_march(Dev &d, cudaStream_t s) {
     dim3 blk(32, 8);
     k_march<<<cell_grid(d.g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.g,
-                                                d.ph.dt * d.ph.beta / d.ph.re / 2.0);
+                                                d.ph.dt * d.ph.beta / d.ph.re / 2.0); count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s) {
     const Geo &g = d.g;
     const bool d3 = g.dim == 3;
-    k_drag_part<<<dim3(d.ncyl, g.nz), 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mperm, d.moff, d.nm, d3 ? 3 : 2, d.dragpart);
-    k_drag_final<<<d.ncyl, 256, 0, s>>>(d.dragpart, g.nz, d3 ? 3 : 2, d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out);
+    k_drag_part<<<dim3(d.ncyl, g.nz), 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mperm, d.moff, d.nm, d3 ? 3 : 2, d.dragpart); count_launch();
+    k_drag_final<<<d.ncyl, 256, 0, s>>>(d.dragpart, g.nz, d3 ? 3 : 2, d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out); count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t aos_to_soa(const double *aos, double *soa, int ncomp, int cs, cudaStream_t s) {
-    k_aos_to_soa<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs);
+    k_aos_to_soa<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs); count_launch();
     return cudaGetLastError();
 }
 cudaError_t soa_to_aos(const double *soa, double *aos, int ncomp, int cs, cudaStream_t s) {
-    k_soa_to_aos<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs);
+    k_soa_to_aos<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs); count_launch();
     return cudaGetLastError();
 }
 cudaError_t count_nonfinite(const double *a, int n, unsigned long long *out, cudaStream_t s) {
-    k_count_nonfinite<<<(n + 255) / 256, 256, 0, s>>>(a, n, out);
+    k_count_nonfinite<<<(n + 255) / 256, 256, 0, s>>>(a, n, out); count_launch();
     return cudaGetLastError();
 }
 
@@ -1184,14 +1184,14 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     if (o.polymer) {
         dim3 blk(32, 4);
         dim3 grd = cell_grid(g, blk);
-        if (d3) k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs);
-        else k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs);
+        if (d3) { k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs); count_launch(); }
+        else { k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs); count_launch(); }
         mark(1);
-        if (d3) k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt);
-        else k_polymer_update2<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, g, d.ph, d.cs, d.cnt);
+        if (d3) { k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt); count_launch(); }
+        else { k_polymer_update2<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, g, d.ph, d.cs, d.cnt); count_launch(); }
         std::swap(d.C, d.Cn);
         long n = halo_count(g);
-        k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2);
+        k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2); count_launch();
         if ((e = cudaGetLastError())) return e;
     } else {
         mark(1);
@@ -1211,8 +1211,8 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     {
         dim3 blk(32, 8);
         dim3 grd = cell_grid(g, blk);
-        if (d3) k_momentum<3><<<grd, blk, 0, s>>>(ma, g);
-        else k_momentum<2><<<grd, blk, 0, s>>>(ma, g);
+        if (d3) { k_momentum<3><<<grd, blk, 0, s>>>(ma, g); count_launch(); }
+        else { k_momentum<2><<<grd, blk, 0, s>>>(ma, g); count_launch(); }
         if ((e = cudaGetLastError())) return e;
     }
     mark(3);
@@ -1233,9 +1233,9 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
         }
         ia.Ua[0] = d.Ua; ia.Ua[1] = d.Va; ia.Ua[2] = d.Wa;
         dim3 gi((d.nm + 127) / 128, g.nz, ia.ncomp);
-        k_ibm_interp<<<gi, 128, 0, s>>>(ia, g);
+        k_ibm_interp<<<gi, 128, 0, s>>>(ia, g); count_launch();
         dim3 blk(32, 8);
-        k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g);
+        k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g); count_launch();
         if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
         if ((e = cudaGetLastError())) return e;
     }
@@ -1255,7 +1255,7 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     // 5. Poisson
     {
         dim3 blk(32, 8);
-        k_poisson_rhs<<<cell_grid(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Q[0], g);
+        k_poisson_rhs<<<cell_grid(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Q[0], g); count_launch();
     }
     if (o.poisson == 0) {
         if (!g.walls) e = fft_solve_periodic(d, d.Q[0], d.Phi, 0.0, -1.0, s);
@@ -1271,7 +1271,7 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     {
         dim3 blk(32, 8);
         k_march<<<cell_grid(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, g,
-                                                  d.ph.dt * d.ph.beta / d.ph.re / 2.0);
+                                                  d.ph.dt * d.ph.beta / d.ph.re / 2.0); count_launch();
         if ((e = cudaGetLastError())) return e;
     }
     if ((e = bc(d.U, g, BC_U, s))) return e;

@@ -675,22 +675,22 @@ cudaError_t solve_periodic_mp(Dev &d, const TS *src, double *dst, const double *
     const size_t smx = (size_t)ppc * 2 * nx * sizeof(Cx<float>);
     {
         int npp = ny / 2, total = npp * nz;
-        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i);
+        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i); count_launch();
     }
     DivideSpec none{};
     const int txy = std::max(1, std::min(32, 4096 / ny));
     const size_t smy = (size_t)2 * ny * txy * sizeof(Cx<float>);
-    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, -1, 0, none);
+    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, -1, 0, none); count_launch();
     {
         DivideSpec dv{d.kx2, d.ky2, d.kz2, lhs0, lhs1, (double)nx * ny * nz, 1};
         const int txz = std::max(1, std::min(32, 4096 / nz));
         const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<float>);
-        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 1, dv);
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 1, dv); count_launch();
     }
-    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, +1, 0, none);
+    k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, +1, 0, none); count_launch();
     {
         int npp = ny / 2, total = npp * nz;
-        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, dst, base, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i);
+        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, dst, base, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -703,24 +703,26 @@ cudaError_t solve_walls_mp(Dev &d, const TS *src, double *dst, const double *bas
     const size_t smx = (size_t)ppc * 2 * nx * sizeof(Cx<float>);
     {
         int npp = ny / 2, total = npp * nz;
-        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i);
+        k_fft_x_fwd<float, TS><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(src, d.Hf, nx, ny, 1, ny, npp, nz, d.twxf_r, d.twxf_i); count_launch();
     }
     DivideSpec none{};
     const int txz = std::max(1, std::min(32, 4096 / nz));
     const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<float>);
-    if (nz > 1)
-        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 0, none);
+    if (nz > 1) {
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(d.Hf, nz, nxh * ny, nxh, nxh, txz, d.twzf_r, d.twzf_i, -1, 0, none); count_launch();
+    }
     {
         WallSpec w{d.kx2, d.kz2, d.ph.dt, d.ph.beta, d.ph.re, g.dy, (double)nx * nz, 0.0, sys};
         const int tx = 32;
         const size_t sm = (size_t)n * tx * (sizeof(Cx<float>) + sizeof(float));
-        k_wall_tdma<float><<<dim3((nxh + tx - 1) / tx, nz), 128, sm, s>>>(d.Hf, d.H2f, ny, nxh, tx, w);
+        k_wall_tdma<float><<<dim3((nxh + tx - 1) / tx, nz), 128, sm, s>>>(d.Hf, d.H2f, ny, nxh, tx, w); count_launch();
     }
-    if (nz > 1)
-        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, n), 256, smz, s>>>(d.H2f, nz, nxh * n, nxh, nxh, txz, d.twzf_r, d.twzf_i, +1, 0, none);
+    if (nz > 1) {
+        k_fft_lines<float><<<dim3((nxh + txz - 1) / txz, n), 256, smz, s>>>(d.H2f, nz, nxh * n, nxh, nxh, txz, d.twzf_r, d.twzf_i, +1, 0, none); count_launch();
+    }
     {
         int npp = n / 2, total = npp * nz;
-        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.H2f, dst, base, nx, n, npp, nz, 0, g.sx, g.sy, d.twxf_r, d.twxf_i);
+        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.H2f, dst, base, nx, n, npp, nz, 0, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -742,13 +744,13 @@ cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const doubl
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
     const int bpp = (ny + rb - 1) / rb;
-    k_xfwd_t<TS><<<bpp * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, ny, -1, d.twxf_r, d.twxf_i);
+    k_xfwd_t<TS><<<bpp * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, ny, -1, d.twxf_r, d.twxf_i); count_launch();
     PlaneSpec ps{};
     ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
     ps.lhs0 = lhs0; ps.lhs1 = lhs1; ps.inv_ntot = (float)(1.0 / ((double)nx * ny * nz));
     k_plane_periodic<<<nxh, 1024, (size_t)8 * (ny + 1) * nz, s>>>(S, ny, nz, ilog2(ny), ilog2(nz), d.twyf_r, d.twyf_i,
-                                                                 d.twzf_r, d.twzf_i, ps);
-    k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i);
+                                                                 d.twzf_r, d.twzf_i, ps); count_launch();
+    k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     return cudaGetLastError();
 }
 
@@ -760,7 +762,7 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
     const int rb = x_rows_per_block(nx);
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
-    k_xfwd_t<TS><<<((ny + rb - 1) / rb) * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, lj, 0, d.twxf_r, d.twxf_i);
+    k_xfwd_t<TS><<<((ny + rb - 1) / rb) * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, lj, 0, d.twxf_r, d.twxf_i); count_launch();
     PlaneSpec ps{};
     ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
     const double kap = d.ph.dt * d.ph.beta / d.ph.re / 2.0, idy2 = 1.0 / (g.dy * g.dy);
@@ -773,14 +775,14 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
         const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
         WallTables wt{d.wtP[t], d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, ps.nxz_inv, sys};
         const size_t smw = smp + (size_t)(nz / 2) * sizeof(float2);
-        if (nz == 32) k_plane_walls_w<1><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
-        else if (nz == 64) k_plane_walls_w<2><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
-        else k_plane_walls_w<4><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt);
+        if (nz == 32) { k_plane_walls_w<1><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        else if (nz == 64) { k_plane_walls_w<2><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        else { k_plane_walls_w<4><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
     } else {
-        k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps);
+        k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps); count_launch();
     }
     k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
-                                                               d.twxf_r, d.twxf_i);
+                                                               d.twxf_r, d.twxf_i); count_launch();
     return cudaGetLastError();
 }
 
@@ -821,19 +823,19 @@ cudaError_t init_kernels_mixed() {
 }
 
 cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s) {
-    k_convert<double, float><<<(n + 255) / 256, 256, 0, s>>>(a, b, n);
+    k_convert<double, float><<<(n + 255) / 256, 256, 0, s>>>(a, b, n); count_launch();
     return cudaGetLastError();
 }
 cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s) {
-    k_convert<float, double><<<(n + 255) / 256, 256, 0, s>>>(a, b, n);
+    k_convert<float, double><<<(n + 255) / 256, 256, 0, s>>>(a, b, n); count_launch();
     return cudaGetLastError();
 }
 cudaError_t aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs, cudaStream_t s) {
-    k_aos_to_soa_f<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs);
+    k_aos_to_soa_f<<<(cs + 255) / 256, 256, 0, s>>>(aos, soa, ncomp, cs); count_launch();
     return cudaGetLastError();
 }
 cudaError_t soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs, cudaStream_t s) {
-    k_soa_to_aos_f<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs);
+    k_soa_to_aos_f<<<(cs + 255) / 256, 256, 0, s>>>(soa, aos, ncomp, cs); count_launch();
     return cudaGetLastError();
 }
 
@@ -843,8 +845,8 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     F8_CUDA_RET(bc_field(d.W, d.g, BC_W, s));
     F8_CUDA_RET(bc_field(d.P, d.g, BC_P, s));
     long n = halo_count_m(d.g);
-    k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2);
-    k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2);
+    k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
+    k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
     F8_CUDA_RET(d2f(d.U, d.Uf, d.cs, s));
     F8_CUDA_RET(d2f(d.V, d.Vf, d.cs, s));
     F8_CUDA_RET(d2f(d.W, d.Wf, d.cs, s));
@@ -859,12 +861,12 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(0);
     if (o.polymer) {
         dim3 blk(32, 4);
-        k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs);
+        k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs); count_launch();
         mark(1);
-        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.cnt);
+        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.cnt); count_launch();
         std::swap(d.Cf, d.Cnf);
         long n = halo_count_m(g);
-        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2);
+        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
         if ((e = cudaGetLastError())) return e;
     } else {
         mark(1);
@@ -879,7 +881,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         a.vis = (float)(d.ph.beta / d.ph.re);
         a.dt = d.ph.dt;
         dim3 blk(32, 8);
-        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc);
+        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch();
         if ((e = cudaGetLastError())) return e;
     }
     mark(3);
@@ -905,9 +907,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
             }
         }
         dim3 gi((d.nm + 127) / 128, g.nz, 3);
-        k_ibm_interp_f<<<gi, 128, 0, s>>>(a, g);
+        k_ibm_interp_f<<<gi, 128, 0, s>>>(a, g); count_launch();
         int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
-        if (maxact > 0) k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g);
+        if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
         if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
         if ((e = cudaGetLastError())) return e;
     }
@@ -928,7 +930,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     // Poisson: FP32 solve + FP64 defect correction
     {
         dim3 blk(32, 8);
-        k_poisson_rhs_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Rp, g, mc);
+        k_poisson_rhs_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Rp, g, mc); count_launch();
     }
     if (!g.walls) e = solve_periodic_f<double>(d, d.Rp, d.Phi, nullptr, 0.0, -1.0, s);
     else e = solve_walls_f<double>(d, d.Rp, d.Phi, nullptr, SYS_P, s);
@@ -936,7 +938,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
     for (int it = 0; it < d.defect_iters; ++it) {
         dim3 blk(32, 8);
-        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g, mc);
+        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g, mc); count_launch();
         if (!g.walls) e = solve_periodic_f<double>(d, d.Rd, d.Phi, d.Phi, 0.0, -1.0, s);
         else e = solve_walls_f<double>(d, d.Rd, d.Phi, d.Phi, SYS_P, s);
         if (e) return e;
@@ -945,11 +947,11 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(6);
     {
         dim3 blk(32, 8);
-        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.Uf, d.Vf, d.Wf, g, mc);
+        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.Uf, d.Vf, d.Wf, g, mc); count_launch();
     }
     {
         long n = halo_count_m(g) + (g.walls ? (long)g.nx * g.nz : 0);
-        k_bc_vel_m<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.U, d.V, d.W, d.P, d.Uf, d.Vf, d.Wf, g);
+        k_bc_vel_m<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.U, d.V, d.W, d.P, d.Uf, d.Vf, d.Wf, g); count_launch();
     }
     mark(7);
     return cudaGetLastError();

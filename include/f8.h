@@ -124,6 +124,9 @@ typedef struct f8_diag {
     long long newton_unconverged; /* cell-steps that hit newton_itrmax, same span */
     int poisson_iters;          /* SOR iterations of the last step (-1: FFT)     */
     int nan_found;
+    long long kernel_launches;  /* CUDA kernels launched by this context's f8_step
+                                   calls since f8_load or f8_timing_reset (0 for
+                                   the CPU oracle)                                */
 } f8_diag;
 
 typedef struct f8_ctx f8_ctx;
