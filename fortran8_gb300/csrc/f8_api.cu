@@ -239,6 +239,8 @@ int setup(f8_ctx *c) {
         API_CUDA(c, c->alloc(&d.Wf, cs));
         API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
         API_CUDA(c, c->alloc(&d.fpetf, cs));
+        API_CUDA(c, c->alloc(&d.fixlist, ni));
+        API_CUDA(c, c->alloc(&d.fixcnt, 1));
         for (int q = 0; q < 3; ++q) {
             API_CUDA(c, c->alloc(&d.A0f[q], ni));
             API_CUDA(c, c->alloc(&d.T0f[q], ni));

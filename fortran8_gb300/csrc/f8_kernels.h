@@ -39,6 +39,7 @@ struct Dev {
     float *Uf, *Vf, *Wf;                   // FP32 copies of U, V, W (halo), mixed path
     // mixed-precision state and work (F8_MIXED)
     float *Cf, *Cnf, *fpetf;               // FP32 conformation tensor (SoA halo) and f(C)
+    int *fixlist, *fixcnt;                 // cells queued for the exact Newton re-solve
     float *A0f[3], *T0f[3], *Ff[3];        // FP32 history and body force (interior)
     float *Qf[3];                          // FP32 right-hand sides dt*(R + f)
     double *Rp;                            // FP64 Poisson right-hand side (interior)

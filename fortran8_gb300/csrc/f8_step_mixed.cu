@@ -236,7 +236,9 @@ __device__ inline int select3f(const float *cm, const float *c0, const float *cp
     return idx;
 }
 
-__global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+__global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs,
+                                                  int *__restrict__ fixcnt) {
+    if ((blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y) == 0) *fixcnt = 0;   // queue of k_update3_f
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -258,41 +260,100 @@ __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, u
 
 // Cstar + implicit Newton solve of A C + C A^T = Cx + dt/Wi I with
 // A = A0 + (1 + f(C) dt/Wi)/2 I (fenep.f90:518-605) in FP32.  The Jacobian is
-// analytic: J = M(A0) + a I + (dt/Wi) f'(tr C) C e^T, with a = 1 + f dt/Wi,
-// e = (1,0,0,1,0,1) and f' = (L^2-3)/(L^2-tr C)^2.  J is dominated by its
-// diagonal a >= 1 (|M| = O(dt |grad u|)), so the 6x6 elimination runs without
-// pivoting, fully unrolled in registers.  Stopping rule: the reference's
-// relative step test (fenep.f90:575).
-__device__ inline void newton_solve_f(float (&x)[6], const float (&b)[6], float a00, float a01, float a02, float a10,
-                                      float a11, float a12, float a20, float a21, float a22, float dtwi, float lp2f,
-                                      double lp2, float epsf, int itrmax, int &itr_out) {
+// J = B + c x e^T with B = a I + M(A0), a = 1 + f dt/Wi, c = (dt/Wi) f'(tr C),
+// e = (1,0,0,1,0,1) and M the linear Lyapunov part (rows of Lyapunov_func,
+// fenep.f90:598-603).  |M|/a = O(dt |grad u|) is small, so the fast solve
+// replaces B^{-1} by its three-term Neumann series (1/a)(I - M/a + (M/a)^2)
+// and the rank-one term by Sherman-Morrison with B^{-1} x ~ x/a.  This is a
+// Newton iteration with an approximate Jacobian: it converges to the same root
+// as the reference (stopping rule: the relative step test, fenep.f90:575) at
+// the rate ~(|M|/a)^3 per iteration.  Cells that have not converged after
+// NEWTON_FAST_MAX iterations are queued and re-solved from the start by the
+// exact elimination in k_newton_fix_f.
+constexpr int NEWTON_FAST_MAX = 12;
+
+struct Lyap9 { float a00, a01, a02, a10, a11, a12, a20, a21, a22; };
+
+__device__ inline void lyap_M(const Lyap9 &A, const float (&v)[6], float (&o)[6]) {
+    o[0] = 2.0f * (A.a00 * v[0] + A.a01 * v[1] + A.a02 * v[2]);
+    o[1] = A.a10 * v[0] + (A.a11 + A.a00) * v[1] + A.a12 * v[2] + A.a01 * v[3] + A.a02 * v[4];
+    o[2] = A.a20 * v[0] + A.a21 * v[1] + (A.a22 + A.a00) * v[2] + A.a01 * v[4] + A.a02 * v[5];
+    o[3] = 2.0f * (A.a10 * v[1] + A.a11 * v[3] + A.a12 * v[4]);
+    o[4] = A.a10 * v[2] + A.a20 * v[1] + A.a21 * v[3] + (A.a22 + A.a11) * v[4] + A.a12 * v[5];
+    o[5] = 2.0f * (A.a20 * v[2] + A.a21 * v[4] + A.a22 * v[5]);
+}
+
+// relative step test of fenep.f90:575; false on NaN so that the loop ends
+__device__ inline bool step_small(const float (&x)[6], float sr, float epsf) {
+    float sx = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) sx += x[m] * x[m];
+    return !(sqrtf(sr / sx) >= epsf);
+}
+
+// returns the iterations taken; > maxit when not converged
+__device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Lyap9 &A, float dtwi, float lp2f,
+                                    double lp2, float epsf, int maxit) {
     int itr;
+#pragma unroll 1
+    for (itr = 1; itr <= maxit; ++itr) {
+        const float f = peterlin_f(x[0], x[3], x[5], lp2f, lp2);
+        const float a = 1.0f + f * dtwi;
+        const float ia = 1.0f / a;
+        const float tr = x[0] + x[3] + x[5];
+        const float den = lp2f - tr;
+        const float cc = dtwi * (lp2f - 3.0f) / (den * den);
+        float r[6], y[6], t[6];
+        lyap_M(A, x, r);
+#pragma unroll
+        for (int m = 0; m < 6; ++m) { r[m] = (r[m] + a * x[m] - b[m]) * ia; y[m] = r[m]; }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {        // y = (1/a)(I - M/a + (M/a)^2) residual
+            lyap_M(A, y, t);
+#pragma unroll
+            for (int m = 0; m < 6; ++m) y[m] = fmaf(-ia, t[m], r[m]);
+        }
+        const float g = cc * (y[0] + y[3] + y[5]) / (1.0f + cc * tr * ia) * ia;
+        float sr = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            const float d = fmaf(-g, x[m], y[m]);
+            x[m] -= d;
+            sr = fmaf(d, d, sr);
+        }
+        if (step_small(x, sr, epsf)) break;
+    }
+    return itr;
+}
+
+// The exact Newton step: J assembled analytically and eliminated without
+// pivoting (J is dominated by its diagonal a >= 1), fully unrolled.
+__device__ inline int newton_exact_f(float (&x)[6], const float (&b)[6], const Lyap9 &A, float dtwi, float lp2f,
+                                     double lp2, float epsf, int itrmax) {
+    int itr;
+#pragma unroll 1
     for (itr = 1; itr <= itrmax; ++itr) {
         const float f = peterlin_f(x[0], x[3], x[5], lp2f, lp2);
         const float a = 1.0f + f * dtwi;
         const float den = lp2f - (x[0] + x[3] + x[5]);
         const float cc = dtwi * (lp2f - 3.0f) / (den * den);
-        // residual L(x) = M x + a x - b (rows of Lyapunov_func, fenep.f90:598-603)
         float J[6][7];
-        J[0][6] = 2 * a00 * x[0] + 2 * a01 * x[1] + 2 * a02 * x[2] + a * x[0] - b[0];
-        J[1][6] = a10 * x[0] + (a11 + a00) * x[1] + a12 * x[2] + a01 * x[3] + a02 * x[4] + a * x[1] - b[1];
-        J[2][6] = a20 * x[0] + a21 * x[1] + (a22 + a00) * x[2] + a01 * x[4] + a02 * x[5] + a * x[2] - b[2];
-        J[3][6] = 2 * a10 * x[1] + 2 * a11 * x[3] + 2 * a12 * x[4] + a * x[3] - b[3];
-        J[4][6] = a10 * x[2] + a20 * x[1] + a21 * x[3] + (a22 + a11) * x[4] + a12 * x[5] + a * x[4] - b[4];
-        J[5][6] = 2 * a20 * x[2] + 2 * a21 * x[4] + 2 * a22 * x[5] + a * x[5] - b[5];
+        float r[6];
+        lyap_M(A, x, r);
         const float Mx[6][6] = {
-            {2 * a00, 2 * a01, 2 * a02, 0, 0, 0},
-            {a10, a11 + a00, a12, a01, a02, 0},
-            {a20, a21, a22 + a00, 0, a01, a02},
-            {0, 2 * a10, 0, 2 * a11, 2 * a12, 0},
-            {0, a20, a10, a21, a22 + a11, a12},
-            {0, 0, 2 * a20, 0, 2 * a21, 2 * a22}};
+            {2 * A.a00, 2 * A.a01, 2 * A.a02, 0, 0, 0},
+            {A.a10, A.a11 + A.a00, A.a12, A.a01, A.a02, 0},
+            {A.a20, A.a21, A.a22 + A.a00, 0, A.a01, A.a02},
+            {0, 2 * A.a10, 0, 2 * A.a11, 2 * A.a12, 0},
+            {0, A.a20, A.a10, A.a21, A.a22 + A.a11, A.a12},
+            {0, 0, 2 * A.a20, 0, 2 * A.a21, 2 * A.a22}};
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-            const float cr = cc * x[r];
+        for (int q = 0; q < 6; ++q) {
+            J[q][6] = r[q] + a * x[q] - b[q];
+            const float cr = cc * x[q];
 #pragma unroll
-            for (int q = 0; q < 6; ++q)
-                J[r][q] = Mx[r][q] + ((q == 0 || q == 3 || q == 5) ? cr : 0.0f) + (q == r ? a : 0.0f);
+            for (int w = 0; w < 6; ++w)
+                J[q][w] = Mx[q][w] + ((w == 0 || w == 3 || w == 5) ? cr : 0.0f) + (w == q ? a : 0.0f);
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
@@ -300,30 +361,60 @@ __device__ inline void newton_solve_f(float (&x)[6], const float (&b)[6], float 
 #pragma unroll
             for (int q = k + 1; q < 7; ++q) J[k][q] *= inv;
 #pragma unroll
-            for (int r = 0; r < 6; ++r) {
-                if (r == k) continue;
-                const float fr = J[r][k];
+            for (int q = 0; q < 6; ++q) {
+                if (q == k) continue;
+                const float fr = J[q][k];
 #pragma unroll
-                for (int q = k + 1; q < 7; ++q) J[r][q] -= fr * J[k][q];
+                for (int w = k + 1; w < 7; ++w) J[q][w] -= fr * J[k][w];
             }
         }
-        float sr = 0.0f, sx = 0.0f;
+        float sr = 0.0f;
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
             x[m] -= J[m][6];
             sr += J[m][6] * J[m][6];
         }
-#pragma unroll
-        for (int m = 0; m < 6; ++m) sx += x[m] * x[m];
-        if (!(sqrtf(sr / sx) >= epsf)) break;   // also leaves on NaN
+        if (step_small(x, sr, epsf)) break;
     }
-    itr_out = itr;
+    return itr;
 }
 
-__global__ void __launch_bounds__(128, 4) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
+// A = transpose of the velocity gradient (fenep.f90:541-550) at cell h
+__device__ inline Lyap9 vel_grad_f(const float *__restrict__ U, const float *__restrict__ V,
+                                   const float *__restrict__ W, int h, int ox, int oy, int oz, const MixConst &mc) {
+    Lyap9 A;
+    A.a00 = mc.gx1 * (U[h] - U[h - ox]);
+    A.a10 = mc.gx4 * (-V[h - ox - oy] + V[h + ox - oy] - V[h - ox] + V[h + ox]);
+    A.a20 = mc.gx4 * (-W[h - ox - oz] + W[h + ox - oz] - W[h - ox] + W[h + ox]);
+    A.a01 = mc.gy4 * (-U[h - ox - oy] - U[h - oy] + U[h - ox + oy] + U[h + oy]);
+    A.a11 = mc.gy1 * (V[h] - V[h - oy]);
+    A.a21 = mc.gy4 * (-W[h - oy - oz] + W[h + oy - oz] - W[h - oy] + W[h + oy]);
+    A.a02 = mc.gz4 * (-U[h - ox - oz] - U[h - oz] + U[h - ox + oz] + U[h + oz]);
+    A.a12 = mc.gz4 * (-V[h - oy - oz] - V[h - oz] + V[h - oy + oz] + V[h + oz]);
+    A.a22 = mc.gz1 * (W[h] - W[h - oz]);
+    return A;
+}
+
+// Upwind Cstar coefficients of one direction on the points p-2 .. p+2
+// (fenep.f90:155-196): the minus face takes s_pm * (candidate is of this cell)
+// + s_nm * (candidate cm of the minus neighbour), the plus face s_np * (is) +
+// s_pp * (candidate cp of the plus neighbour).  A wall ghost neighbour
+// contributes its cell value (gm / gp).
+__device__ inline void dir_coef(float s_pm, float s_pp, float s_nm, float s_np, int is, int cm, int cp, bool gm,
+                                bool gp, float &km2, float &km1, float &k0, float &kp1, float &kp2) {
+    km2 = gm ? 0.0f : s_nm * c_fn_w[cm][0];
+    km1 = s_pm * c_fp_w[is][0] + s_np * c_fn_w[is][0] + (gm ? s_nm : s_nm * c_fn_w[cm][1]);
+    k0 += s_pm * c_fp_w[is][1] + s_np * c_fn_w[is][1] + (gm ? 0.0f : s_nm * c_fn_w[cm][2])
+          + (gp ? 0.0f : s_pp * c_fp_w[cp][0]);
+    kp1 = s_pm * c_fp_w[is][2] + s_np * c_fn_w[is][2] + (gp ? s_pp : s_pp * c_fp_w[cp][1]);
+    kp2 = gp ? 0.0f : s_pp * c_fp_w[cp][2];
+}
+
+__global__ void __launch_bounds__(128, 6) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
                                                    float *__restrict__ fpet, const uint8_t *__restrict__ codes,
                                                    const float *__restrict__ U, const float *__restrict__ V,
                                                    const float *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
+                                                   int *__restrict__ fixlist, int *__restrict__ fixcnt,
                                                    StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -334,69 +425,71 @@ __global__ void __launch_bounds__(128, 4) k_update3_f(const float *__restrict__ 
         const int h = hix(g, i, j, k);
         const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
         const int cself = codes[qix(g, i, j, k)];
-        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
-        const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
+        const int im = wrapx(g, i - 1), ip = wrapx(g, i + 1), km = wrapz(g, k - 1), kp = wrapz(g, k + 1);
         int jm = j - 1, jp = j + 1;
-        bool ym_ghost = false, yp_ghost = false;
+        bool gym = false, gyp = false;
         if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
-        const int cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
-        const int cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
-        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
-        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
-        const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
-        const float u1 = U[h - ox], u2 = U[h];
-        const float v1 = V[h - oy], v2 = V[h];
-        const float w1 = W[h - oz], w2 = W[h];
-        const float cxs = mc.sx, cys = mc.sy, czs = mc.sz;
-        const float s1 = (-u2 + fabsf(u2)) * cxs, s2 = 1.0f / 6 + (-u2 - fabsf(u2)) * cxs;
-        const float s3 = 1.0f / 6 + (u1 - fabsf(u1)) * cxs, s4 = (u1 + fabsf(u1)) * cxs;
-        const float s5 = (-v2 + fabsf(v2)) * cys, s6 = 1.0f / 6 + (-v2 - fabsf(v2)) * cys;
-        const float s7 = 1.0f / 6 + (v1 - fabsf(v1)) * cys, s8 = (v1 + fabsf(v1)) * cys;
-        const float s9 = (-w2 + fabsf(w2)) * czs, s10 = 1.0f / 6 + (-w2 - fabsf(w2)) * czs;
-        const float s11 = 1.0f / 6 + (w1 - fabsf(w1)) * czs, s12 = (w1 + fabsf(w1)) * czs;
+        else { gym = jm == 0; gyp = jp == g.ny + 1; }
+        // stencil points p-2 and p+2 through the periodic neighbours (their
+        // p+1 / p-1 are halo copies of this cell); at a wall ghost the point
+        // is unused (coefficient 0) and is aliased to p -/+ 1
+        const int hxm2 = hix(g, im, j, k) - ox, hxp2 = hix(g, ip, j, k) + ox;
+        const int hym2 = gym ? h - oy : hix(g, i, jm, k) - oy, hyp2 = gyp ? h + oy : hix(g, i, jp, k) + oy;
+        const int hzm2 = hix(g, i, j, km) - oz, hzp2 = hix(g, i, j, kp) + oz;
+        float kx[5], ky[5], kz[5];
+        {
+            const float u1 = U[h - ox], u2 = U[h];
+            const float v1 = V[h - oy], v2 = V[h];
+            const float w1 = W[h - oz], w2 = W[h];
+            const int cxm = codes[qix(g, im, j, k)] & 3, cxp = codes[qix(g, ip, j, k)] & 3;
+            const int czm = (codes[qix(g, i, j, km)] >> 4) & 3, czp = (codes[qix(g, i, j, kp)] >> 4) & 3;
+            const int cym = gym ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
+            const int cyp = gyp ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+            float k0 = 0.0f;
+            // s3 s1 s4 s2 of fenep.f90:166-177 per direction
+            dir_coef(1.0f / 6 + (u1 - fabsf(u1)) * mc.sx, (-u2 + fabsf(u2)) * mc.sx, (u1 + fabsf(u1)) * mc.sx,
+                     1.0f / 6 + (-u2 - fabsf(u2)) * mc.sx, (cself & 3) + 1, cxm + 1, cxp + 1, false, false,
+                     kx[0], kx[1], k0, kx[3], kx[4]);
+            dir_coef(1.0f / 6 + (v1 - fabsf(v1)) * mc.sy, (-v2 + fabsf(v2)) * mc.sy, (v1 + fabsf(v1)) * mc.sy,
+                     1.0f / 6 + (-v2 - fabsf(v2)) * mc.sy, ((cself >> 2) & 3) + 1, cym + 1, cyp + 1, gym, gyp,
+                     ky[0], ky[1], k0, ky[3], ky[4]);
+            dir_coef(1.0f / 6 + (w1 - fabsf(w1)) * mc.sz, (-w2 + fabsf(w2)) * mc.sz, (w1 + fabsf(w1)) * mc.sz,
+                     1.0f / 6 + (-w2 - fabsf(w2)) * mc.sz, ((cself >> 4) & 3) + 1, czm + 1, czp + 1, false, false,
+                     kz[0], kz[1], k0, kz[3], kz[4]);
+            kx[2] = k0;
+        }
+        const float dtwi = mc.dtwi;
         float b[6], x[6];
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
             const float *Cm = C + (size_t)m * cs;
             const float c0 = Cm[h];
-            const float xm1 = Cm[h - ox], xp1 = Cm[h + ox];
-            const float ym1 = Cm[h - oy], yp1 = Cm[h + oy];
-            const float zm1 = Cm[h - oz], zp1 = Cm[h + oz];
-            const float pxm = face_pf(isx, xm1, c0, xp1), nxp = face_nf(isx, xm1, c0, xp1);
-            const float pxp = face_pf(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
-            const float nxm = face_nf(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
-            const float pym = face_pf(isy, ym1, c0, yp1), nyp = face_nf(isy, ym1, c0, yp1);
-            const float pyp = yp_ghost ? Cm[hyp] : face_pf(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-            const float nym = ym_ghost ? Cm[hym] : face_nf(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
-            const float pzm = face_pf(isz, zm1, c0, zp1), nzp = face_nf(isz, zm1, c0, zp1);
-            const float pzp = face_pf(czp + 1, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
-            const float nzm = face_nf(czm + 1, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
-            b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp
-                   + s11 * pzm + s9 * pzp + s12 * nzm + s10 * nzp;
+            float acc = kx[2] * c0;
+            acc = fmaf(kx[0], Cm[hxm2], acc); acc = fmaf(kx[1], Cm[h - ox], acc);
+            acc = fmaf(kx[3], Cm[h + ox], acc); acc = fmaf(kx[4], Cm[hxp2], acc);
+            acc = fmaf(ky[0], Cm[hym2], acc); acc = fmaf(ky[1], Cm[h - oy], acc);
+            acc = fmaf(ky[3], Cm[h + oy], acc); acc = fmaf(ky[4], Cm[hyp2], acc);
+            acc = fmaf(kz[0], Cm[hzm2], acc); acc = fmaf(kz[1], Cm[h - oz], acc);
+            acc = fmaf(kz[3], Cm[h + oz], acc); acc = fmaf(kz[4], Cm[hzp2], acc);
+            b[m] = acc + ((m == 0 || m == 3 || m == 5) ? dtwi : 0.0f);
             x[m] = c0;
         }
-        const float dtwi = mc.dtwi;
-        b[0] += dtwi; b[3] += dtwi; b[5] += dtwi;
-        // velocity gradient (fenep.f90:541-550), A = transpose(A0) (fenep.f90:550)
-        const float g00 = mc.gx1 * (u2 - u1);
-        const float g01 = mc.gx4 * (-V[h - ox - oy] + V[h + ox - oy] - V[h - ox] + V[h + ox]);
-        const float g02 = mc.gx4 * (-W[h - ox - oz] + W[h + ox - oz] - W[h - ox] + W[h + ox]);
-        const float g10 = mc.gy4 * (-U[h - ox - oy] - U[h - oy] + U[h - ox + oy] + U[h + oy]);
-        const float g11 = mc.gy1 * (v2 - v1);
-        const float g12 = mc.gy4 * (-W[h - oy - oz] + W[h + oy - oz] - W[h - oy] + W[h + oy]);
-        const float g20 = mc.gz4 * (-U[h - ox - oz] - U[h - oz] + U[h - ox + oz] + U[h + oz]);
-        const float g21 = mc.gz4 * (-V[h - oy - oz] - V[h - oz] + V[h - oy + oz] + V[h + oz]);
-        const float g22 = mc.gz1 * (w2 - w1);
-        int itr;
-        newton_solve_f(x, b, g00, g10, g20, g01, g11, g21, g02, g12, g22, dtwi, mc.lp2f, ph.lp2, mc.epsf,
-                       ph.newton_itrmax, itr);
-        my_itr = (unsigned long long)itr;
-        my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+        const Lyap9 A = vel_grad_f(U, V, W, h, ox, oy, oz, mc);
+        const int fast_max = min(NEWTON_FAST_MAX, ph.newton_itrmax);
+        const int itr = newton_fast_f(x, b, A, dtwi, mc.lp2f, ph.lp2, mc.epsf, fast_max);
+        if (itr <= fast_max || fast_max == ph.newton_itrmax) {
+            my_itr = (unsigned long long)itr;
+            my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
 #pragma unroll
-        for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
-        fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
+            for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
+            fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
+        } else {
+            // keep Cstar for the exact solve
+            my_itr = (unsigned long long)fast_max;
+#pragma unroll
+            for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = b[m];
+            fixlist[atomicAdd(fixcnt, 1)] = h;
+        }
     }
     unsigned long long a = my_itr, b2 = my_unconv;
     for (int o = 16; o > 0; o >>= 1) {
@@ -406,6 +499,29 @@ __global__ void __launch_bounds__(128, 4) k_update3_f(const float *__restrict__ 
     if (((threadIdx.x + blockDim.x * threadIdx.y) & 31) == 0) {
         if (a) atomicAdd(&cnt->newton_iters, a);
         if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
+}
+
+// Exact Newton re-solve of the cells queued by k_update3_f (Cstar in Cn)
+__global__ void __launch_bounds__(128) k_newton_fix_f(const float *__restrict__ C, float *__restrict__ Cn,
+                                                      float *__restrict__ fpet, const float *__restrict__ U,
+                                                      const float *__restrict__ V, const float *__restrict__ W,
+                                                      Geo g, Phys ph, MixConst mc, int cs,
+                                                      const int *__restrict__ fixlist,
+                                                      const int *__restrict__ fixcnt, StepCounters *cnt) {
+    const int n = *fixcnt;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int h = fixlist[t];
+        float b[6], x[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) { b[m] = Cn[(size_t)m * cs + h]; x[m] = C[(size_t)m * cs + h]; }
+        const Lyap9 A = vel_grad_f(U, V, W, h, 1, g.sx, g.sx * g.sy, mc);
+        const int itr = newton_exact_f(x, b, A, mc.dtwi, mc.lp2f, ph.lp2, mc.epsf, ph.newton_itrmax);
+        atomicAdd(&cnt->newton_iters, (unsigned long long)itr);
+        if (itr > ph.newton_itrmax) atomicAdd(&cnt->newton_unconverged, 1ull);
+#pragma unroll
+        for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
+        fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
     }
 }
 
@@ -861,9 +977,12 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(0);
     if (o.polymer) {
         dim3 blk(32, 4);
-        k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs); count_launch();
+        k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs, d.fixcnt); count_launch();
         mark(1);
-        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.cnt); count_launch();
+        k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc,
+                                                        d.cs, d.fixlist, d.fixcnt, d.cnt); count_launch();
+        k_newton_fix_f<<<2 * 152, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
+                                               d.fixcnt, d.cnt); count_launch();
         std::swap(d.Cf, d.Cnf);
         long n = halo_count_m(g);
         k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
