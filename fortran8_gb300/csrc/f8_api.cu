@@ -301,6 +301,13 @@ int setup(f8_ctx *c) {
             }
             API_CUDA(c, c->alloc(&d.twz2, t2.size()));
             API_CUDA(c, cudaMemcpyAsync(d.twz2, t2.data(), t2.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
+            std::vector<float2> tx(std::max(1, g.nx / 2));
+            for (int t = 0; t < g.nx / 2; ++t) {
+                double a = 2.0 * PI * t / g.nx;
+                tx[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
+            }
+            API_CUDA(c, c->alloc(&d.twx2, tx.size()));
+            API_CUDA(c, cudaMemcpyAsync(d.twx2, tx.data(), tx.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
             API_CUDA(c, cudaStreamSynchronize(c->s));
         }
         if (g.walls && d.fused_planes && (g.nz == 32 || g.nz == 64 || g.nz == 128)) {

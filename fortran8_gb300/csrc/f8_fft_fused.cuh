@@ -306,6 +306,7 @@ namespace f8 {
 template <int V>
 __device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) {
     constexpr int N = 32 * V;
+#pragma unroll
     for (int m = N / 2; m >= 1; m >>= 1) {
         const int ts = N / (2 * m);
         if (m >= 32) {
@@ -344,6 +345,7 @@ __device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) 
 template <int V>
 __device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) {
     constexpr int N = 32 * V;
+#pragma unroll
     for (int m = 1; m < N; m <<= 1) {
         const int ts = N / (2 * m);
         if (m >= 32) {
@@ -452,6 +454,249 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_w(float2 *S, int ny, co
     }
     __syncthreads();
     // inverse z transform of all rows (bit-reversed in, natural out)
+    for (int j = warp; j < lj; j += nwarp) {
+        float2 v[V];
+#pragma unroll
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        warp_dit_inv<V>(v, tws, lane);
+#pragma unroll
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        Sp[q] = P[(size_t)k * ljs + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-per-row-pair x passes (NX = 32 E).  Each warp transforms two real rows
+// packed as one complex line with warp_dif_fwd / warp_dit_inv (lane t holds
+// x = t + 32 s), unpacks / packs the two half spectra through a per-warp
+// buffer, and the block exchanges RB rows with the [kx][row] tile as the
+// radix-2 passes above do.  Per-warp buffer index of X[k]: k + (k >> lg E),
+// which makes both the bit-reversed (lane stride E + 1) and the natural
+// accesses free of bank conflicts.
+template <int E> struct LgE { static constexpr int v = E == 1 ? 0 : E == 2 ? 1 : E == 4 ? 2 : E == 8 ? 3 : 4; };
+
+__device__ __forceinline__ int zb_ix(int k, int lge) { return k + (k >> lge); }
+
+// natural index of element s of lane t after a DIF transform (bit-reversed)
+template <int E>
+__device__ __forceinline__ int brev_elem(int lane, int s) {
+    constexpr int LG = LgE<E>::v;
+    const int bl = (int)(__brev((unsigned)lane) >> 27);
+    const int bs = LG ? (int)(__brev((unsigned)s) >> (32 - LG)) : 0;
+    return (bl << LG) | bs;
+}
+
+constexpr int XW_WARPS = 8;   // warps per block of the x passes
+
+inline size_t xw_smem(int nx, int rb) {
+    const int nh = nx / 2;
+    return ((size_t)nh + (size_t)(nh + 1) * (rb + 1) + (size_t)XW_WARPS * (nx + 32)) * sizeof(float2);
+}
+
+template <int E, typename TS>
+__global__ void __launch_bounds__(32 * XW_WARPS) k_xfwd_w(const TS *__restrict__ src, float2 *__restrict__ S, int ny,
+                                                         int nz, int rb, int lj, int joff,
+                                                         const float2 *__restrict__ twx) {
+    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v;
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *tws = reinterpret_cast<float2 *>(smem_raw);
+    float2 *tile = tws + NH;
+    float2 *zb = tile + (size_t)(NH + 1) * (rb + 1) + (size_t)warp * (N + 32);
+    for (int q = threadIdx.x; q < NH; q += blockDim.x) tws[q] = twx[q];
+    const int bpp = (ny + rb - 1) / rb;
+    const int k = blockIdx.x / bpp;
+    const int r0 = (blockIdx.x % bpp) * rb;
+    const int nrows = min(rb, ny - r0);
+    __syncthreads();
+    for (int p = warp; 2 * p < nrows; p += XW_WARPS) {
+        const bool has_b = 2 * p + 1 < nrows;
+        const TS *ra = src + (size_t)N * ((size_t)(r0 + 2 * p) + (size_t)ny * k);
+        float2 v[E];
+#pragma unroll
+        for (int s = 0; s < E; ++s)
+            v[s] = make_float2((float)ra[lane + 32 * s], has_b ? (float)ra[N + lane + 32 * s] : 0.0f);
+        warp_dif_fwd<E>(v, tws, lane);
+#pragma unroll
+        for (int s = 0; s < E; ++s) zb[zb_ix(brev_elem<E>(lane, s), LG)] = v[s];
+        __syncwarp();
+        for (int kx = lane; kx <= NH; kx += 32) {
+            const float2 zk = zb[zb_ix(kx, LG)], zm = zb[zb_ix((N - kx) & (N - 1), LG)];
+            tile[(size_t)kx * (rb + 1) + 2 * p] = make_float2((zk.x + zm.x) * 0.5f, (zk.y - zm.y) * 0.5f);
+            tile[(size_t)kx * (rb + 1) + 2 * p + 1] = make_float2((zk.y + zm.y) * 0.5f, (zm.x - zk.x) * 0.5f);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < (NH + 1) * rb; q += blockDim.x) {
+        const int kx = q / rb, r = q % rb;
+        if (r < nrows) S[((size_t)kx * nz + k) * lj + (r0 + r + 1 + joff)] = tile[(size_t)kx * (rb + 1) + r];
+    }
+}
+
+template <int E, typename TO>
+__global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restrict__ S, TO *dst, const TO *base,
+                                                         int nrow, int jlo, int nz, int rb, int lj, int joff2, int sx,
+                                                         int sy, const float2 *__restrict__ twx) {
+    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v;
+    extern __shared__ unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float2 *tws = reinterpret_cast<float2 *>(smem_raw);
+    float2 *tile = tws + NH;
+    float2 *zb = tile + (size_t)(NH + 1) * (rb + 1) + (size_t)warp * (N + 32);
+    for (int q = threadIdx.x; q < NH; q += blockDim.x) tws[q] = twx[q];
+    const int bpp = (nrow + rb - 1) / rb;
+    const int k = blockIdx.x / bpp;
+    const int r0 = (blockIdx.x % bpp) * rb;
+    const int nrows = min(rb, nrow - r0);
+    for (int q = threadIdx.x; q < (NH + 1) * rb; q += blockDim.x) {
+        const int kx = q / rb, r = q % rb;
+        tile[(size_t)kx * (rb + 1) + r] =
+            r < nrows ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int p = warp; 2 * p < nrows; p += XW_WARPS) {
+        const bool has_b = 2 * p + 1 < nrows;
+        // Z = A + i B over the full line from the two half spectra
+        for (int e = lane; e < N; e += 32) {
+            const int m = e <= NH ? e : N - e;
+            const float2 A = tile[(size_t)m * (rb + 1) + 2 * p], B = tile[(size_t)m * (rb + 1) + 2 * p + 1];
+            zb[zb_ix(e, LG)] = e <= NH ? make_float2(A.x - B.y, A.y + B.x) : make_float2(A.x + B.y, B.x - A.y);
+        }
+        __syncwarp();
+        float2 v[E];
+#pragma unroll
+        for (int s = 0; s < E; ++s) v[s] = zb[zb_ix(brev_elem<E>(lane, s), LG)];
+        __syncwarp();
+        warp_dit_inv<E>(v, tws, lane);
+        const size_t oa = 1 + (size_t)sx * ((size_t)(jlo + r0 + 2 * p) + (size_t)sy * (k + 1));
+        TO *ra = dst + oa;
+        if (base) {
+            const TO *ba = base + oa;
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                const int e = lane + 32 * s;
+                ra[e] = ba[e] + TO(v[s].x);
+                if (has_b) ra[sx + e] = ba[sx + e] + TO(v[s].y);
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                const int e = lane + 32 * s;
+                ra[e] = TO(v[s].x);
+                if (has_b) ra[sx + e] = TO(v[s].y);
+            }
+        }
+    }
+}
+
+// Wall plane with the Thomas solves split over T = 1024 / NZ threads per
+// (kx, kz) system.  Both sweeps are first-order affine recurrences,
+//   forward   q_j = alpha_j q_{j-1} + beta_j,  alpha_j = -c_j / den_j,
+//                                              beta_j  = d_j / den_j,
+//   backward  x_j = P_j x_{j+1} + q_j,
+// so each thread composes the maps of its chunk of rows, the T threads scan
+// the composed maps with shuffles, and each thread then replays its chunk
+// from its incoming value.  Same coefficients as k_plane_walls_w.
+template <int V>
+__global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, const float2 *twz, WallTables wt) {
+    constexpr int NZ = 32 * V;
+    constexpr int LG = V == 1 ? 5 : (V == 2 ? 6 : 7);
+    constexpr int T = 1024 / NZ;
+    extern __shared__ unsigned char smem_raw[];
+    const int lj = ny + 2;
+    const int ljs = lj | 1;
+    float2 *P = reinterpret_cast<float2 *>(smem_raw);                // [k][j]
+    float2 *tws = P + (size_t)ljs * NZ;                              // NZ/2 twiddles
+    const int kx = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2 *Sp = S + (size_t)kx * NZ * lj;
+    for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
+    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
+        const int k = q / lj, j = q % lj;
+        P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int j = 1 + warp; j <= ny; j += nwarp) {
+        float2 v[V];
+#pragma unroll
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        warp_dif_fwd<V>(v, tws, lane);
+#pragma unroll
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+    }
+    __syncthreads();
+    {
+        const int kz = threadIdx.x / T, t = threadIdx.x % T;
+        const int row = (int)(__brev((unsigned)kz) >> (32 - LG));
+        float2 *x = P + (size_t)row * ljs;
+        const float *Pt = wt.P + ((size_t)kx * NZ + kz) * lj;
+        const float *Rt = wt.rden + ((size_t)kx * NZ + kz) * lj;
+        const int L = (lj + T - 1) / T;
+        const int j0 = min(lj, t * L), j1 = min(lj, j0 + L);
+        const bool sysv = wt.sys == SYS_V;
+        // forward: compose the chunk's maps (row 0: q_0 = 0)
+        float A = 1.0f;
+        float2 B = make_float2(0.f, 0.f);
+        for (int j = j0; j < j1; ++j) {
+            const bool ident = sysv ? (j >= ny) : (j == lj - 1);
+            const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
+            const float rd = j == 0 ? 0.0f : Rt[j];
+            float2 d = ident ? make_float2(0.f, 0.f) : x[j];
+            const float al = -c * rd, dr = wt.nxz_inv * rd;
+            B = make_float2(fmaf(al, B.x, d.x * dr), fmaf(al, B.y, d.y * dr));
+            A *= al;
+        }
+#pragma unroll
+        for (int o = 1; o < T; o <<= 1) {
+            const float Ap = __shfl_up_sync(0xffffffffu, A, o, T);
+            const float Bx = __shfl_up_sync(0xffffffffu, B.x, o, T), By = __shfl_up_sync(0xffffffffu, B.y, o, T);
+            if (t >= o) { B = make_float2(fmaf(A, Bx, B.x), fmaf(A, By, B.y)); A *= Ap; }
+        }
+        float2 q;
+        q.x = __shfl_up_sync(0xffffffffu, B.x, 1, T);
+        q.y = __shfl_up_sync(0xffffffffu, B.y, 1, T);
+        if (t == 0) q = make_float2(0.f, 0.f);
+        for (int j = j0; j < j1; ++j) {
+            const bool ident = sysv ? (j >= ny) : (j == lj - 1);
+            const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
+            const float rd = j == 0 ? 0.0f : Rt[j];
+            float2 d = ident ? make_float2(0.f, 0.f) : x[j];
+            const float al = -c * rd, dr = wt.nxz_inv * rd;
+            q = make_float2(fmaf(al, q.x, d.x * dr), fmaf(al, q.y, d.y * dr));
+            x[j] = q;
+        }
+        // backward: x_j = P_j x_{j+1} + q_j (P of the last row is 0)
+        A = 1.0f;
+        B = make_float2(0.f, 0.f);
+        for (int j = j1 - 1; j >= j0; --j) {
+            const float pj = Pt[j];
+            const float2 qj = x[j];
+            B = make_float2(fmaf(pj, B.x, qj.x), fmaf(pj, B.y, qj.y));
+            A *= pj;
+        }
+#pragma unroll
+        for (int o = 1; o < T; o <<= 1) {
+            const float An = __shfl_down_sync(0xffffffffu, A, o, T);
+            const float Bx = __shfl_down_sync(0xffffffffu, B.x, o, T), By = __shfl_down_sync(0xffffffffu, B.y, o, T);
+            if (t + o < T) { B = make_float2(fmaf(A, Bx, B.x), fmaf(A, By, B.y)); A *= An; }
+        }
+        float2 xv;
+        xv.x = __shfl_down_sync(0xffffffffu, B.x, 1, T);
+        xv.y = __shfl_down_sync(0xffffffffu, B.y, 1, T);
+        if (t == T - 1) xv = make_float2(0.f, 0.f);
+        for (int j = j1 - 1; j >= j0; --j) {
+            const float pj = Pt[j];
+            const float2 qj = x[j];
+            xv = make_float2(fmaf(pj, xv.x, qj.x), fmaf(pj, xv.y, qj.y));
+            x[j] = xv;
+        }
+    }
+    __syncthreads();
     for (int j = warp; j < lj; j += nwarp) {
         float2 v[V];
 #pragma unroll

@@ -850,6 +850,46 @@ inline int x_rows_per_block(int nx) { return 2 * std::max(1, std::min(8, 1024 / 
 inline size_t x_smem(int nx, int rb) { return (size_t)(rb / 2) * 2 * nx * sizeof(float2) + (size_t)(nx / 2 + 1) * (rb + 1) * sizeof(float2); }
 inline int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
 
+// warp-per-row-pair x passes for NX = 32 .. 512; false when NX has no instance
+constexpr int XW_RB = 16;
+
+template <typename TS>
+bool xfwd_warp(const Dev &d, const TS *src, float2 *S, int ny, int lj, int joff, cudaStream_t s) {
+    const Geo &g = d.g;
+    const unsigned grid = (unsigned)(((ny + XW_RB - 1) / XW_RB) * g.nz);
+    const size_t sm = xw_smem(g.nx, XW_RB);
+    const int thr = 32 * XW_WARPS;
+    switch (g.nx) {
+    case 32: k_xfwd_w<1, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    case 64: k_xfwd_w<2, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    case 128: k_xfwd_w<4, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    case 256: k_xfwd_w<8, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    case 512: k_xfwd_w<16, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    default: return false;
+    }
+    count_launch();
+    return true;
+}
+
+template <typename TO>
+bool xinv_warp(const Dev &d, const float2 *S, TO *dst, const TO *base, int nrow, int jlo, int lj, int joff2,
+               cudaStream_t s) {
+    const Geo &g = d.g;
+    const unsigned grid = (unsigned)(((nrow + XW_RB - 1) / XW_RB) * g.nz);
+    const size_t sm = xw_smem(g.nx, XW_RB);
+    const int thr = 32 * XW_WARPS;
+    switch (g.nx) {
+    case 32: k_xinv_w<1, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 64: k_xinv_w<2, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 128: k_xinv_w<4, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 256: k_xinv_w<8, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 512: k_xinv_w<16, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    default: return false;
+    }
+    count_launch();
+    return true;
+}
+
 template <typename TS>
 cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const double *base, float lhs0, float lhs1,
                                  cudaStream_t s) {
@@ -860,13 +900,17 @@ cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const doubl
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
     const int bpp = (ny + rb - 1) / rb;
-    k_xfwd_t<TS><<<bpp * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, ny, -1, d.twxf_r, d.twxf_i); count_launch();
+    if (!xfwd_warp<TS>(d, src, S, ny, ny, -1, s)) {
+        k_xfwd_t<TS><<<bpp * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, ny, -1, d.twxf_r, d.twxf_i); count_launch();
+    }
     PlaneSpec ps{};
     ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
     ps.lhs0 = lhs0; ps.lhs1 = lhs1; ps.inv_ntot = (float)(1.0 / ((double)nx * ny * nz));
     k_plane_periodic<<<nxh, 1024, (size_t)8 * (ny + 1) * nz, s>>>(S, ny, nz, ilog2(ny), ilog2(nz), d.twyf_r, d.twyf_i,
                                                                  d.twzf_r, d.twzf_i, ps); count_launch();
-    k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+    if (!xinv_warp<double>(d, S, dst, base, ny, 1, ny, -1, s)) {
+        k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -878,7 +922,9 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
     const int rb = x_rows_per_block(nx);
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
-    k_xfwd_t<TS><<<((ny + rb - 1) / rb) * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, lj, 0, d.twxf_r, d.twxf_i); count_launch();
+    if (!xfwd_warp<TS>(d, src, S, ny, lj, 0, s)) {
+        k_xfwd_t<TS><<<((ny + rb - 1) / rb) * nz, thr, smx, s>>>(src, S, nx, ny, nz, rb, lj, 0, d.twxf_r, d.twxf_i); count_launch();
+    }
     PlaneSpec ps{};
     ps.kx2 = d.kx2f; ps.ky2 = d.ky2f; ps.kz2 = d.kz2f;
     const double kap = d.ph.dt * d.ph.beta / d.ph.re / 2.0, idy2 = 1.0 / (g.dy * g.dy);
@@ -890,15 +936,17 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
     if (d.wtP[0] && (nz == 32 || nz == 64 || nz == 128)) {
         const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
         WallTables wt{d.wtP[t], d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, ps.nxz_inv, sys};
-        const size_t smw = smp + (size_t)(nz / 2) * sizeof(float2);
-        if (nz == 32) { k_plane_walls_w<1><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
-        else if (nz == 64) { k_plane_walls_w<2><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
-        else { k_plane_walls_w<4><<<nxh, 1024, smw, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        const size_t sms = (size_t)8 * (lj | 1) * nz + (size_t)(nz / 2) * sizeof(float2);
+        if (nz == 32) { k_plane_walls_s<1><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        else if (nz == 64) { k_plane_walls_s<2><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        else { k_plane_walls_s<4><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
     } else {
         k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps); count_launch();
     }
-    k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
-                                                               d.twxf_r, d.twxf_i); count_launch();
+    if (!xinv_warp<double>(d, S, dst, base, lj, 0, lj, 0, s)) {
+        k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
+                                                                   d.twxf_r, d.twxf_i); count_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -929,6 +977,15 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_periodic, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+#define F8_XW_ATTR(E)                                                                                           \
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_w<E, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));   \
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_w<E, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));  \
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_w<E, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_XW_ATTR(1) F8_XW_ATTR(2) F8_XW_ATTR(4) F8_XW_ATTR(8) F8_XW_ATTR(16)
+#undef F8_XW_ATTR
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
