@@ -234,9 +234,9 @@ int setup(f8_ctx *c) {
         API_CUDA(c, c->alloc(&d.H2, nspec));
     } else {
         API_CUDA(c, c->alloc(&d.Cf, cs * d.ncomp));
-        API_CUDA(c, c->alloc(&d.Uf, cs));
-        API_CUDA(c, c->alloc(&d.Vf, cs));
-        API_CUDA(c, c->alloc(&d.Wf, cs));
+        for (float **p : {&d.Uf, &d.Vf, &d.Wf, &d.Ul, &d.Vl, &d.Wl, &d.Pf, &d.Pl, &d.Phif, &d.Phil,
+                          &d.dUf[0], &d.dUf[1], &d.dUf[2]})
+            API_CUDA(c, c->alloc(p, cs));
         API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
         API_CUDA(c, c->alloc(&d.fpetf, cs));
         API_CUDA(c, c->alloc(&d.fixlist, ni));
@@ -247,8 +247,9 @@ int setup(f8_ctx *c) {
             API_CUDA(c, c->alloc(&d.Ff[q], ni));
             API_CUDA(c, c->alloc(&d.Qf[q], ni));
         }
-        API_CUDA(c, c->alloc(&d.Rp, ni));
-        API_CUDA(c, c->alloc(&d.Rd, ni));
+        API_CUDA(c, c->alloc(&d.Rhf, ni));
+        API_CUDA(c, c->alloc(&d.Rlf, ni));
+        API_CUDA(c, c->alloc(&d.Rdf, ni));
         API_CUDA(c, c->alloc(&d.Hf, nspec));
         API_CUDA(c, c->alloc(&d.H2f, nspec));
         d.defect_iters = 1;
@@ -581,7 +582,8 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         c->step += 1;
     }
     API_CUDA(c, cudaEventRecord(c->tot1, c->s));
-    API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
+    if (c->precision == F8_MIXED) API_CUDA(c, count_nonfinite_f(d.Uf, d.cs, c->nan_dev, c->s));
+    else API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
     c->step_launches += g_kernel_launches.load() - launches0;
     StepCounters cnt{};
     unsigned long long nan = 0;
@@ -617,6 +619,7 @@ int f8_store(f8_ctx *c, f8_fields *out) {
         if (!dst) return cudaSuccess;
         return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->s);
     };
+    if (c->precision == F8_MIXED && c->loaded) API_CUDA(c, mixed_state_to_fp64(d, c->s));
     API_CUDA(c, get(out->u, d.U, cs));
     API_CUDA(c, get(out->v, d.V, cs));
     if (c->grid.dim == 3) API_CUDA(c, get(out->w, d.W, cs));

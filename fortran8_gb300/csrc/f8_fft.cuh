@@ -10,6 +10,7 @@
 // kx = 0..NX/2 (NXH = NX/2+1 values per row).
 #pragma once
 #include "f8_common.cuh"
+#include "f8_df64.cuh"
 
 namespace f8 {
 
@@ -84,12 +85,39 @@ __global__ void k_fft_x_fwd(const TS *__restrict__ src, T *__restrict__ H, int n
     }
 }
 
+// Destinations of an inverse x pass.  XOutD: an FP64 field, optionally the
+// sum base + value (FP64 path and stand-alone solve).  XOutF: the FP32 /
+// double-float fields of the mixed path: mode 0 stores the value in hi,
+// mode 1 stores the df64 value (value, 0), mode 2 adds the value to the df64
+// field (hi, lo).
+struct XOutD {
+    double *dst;
+    const double *base;
+    __device__ __forceinline__ void put(size_t o, double v) const { dst[o] = base ? base[o] + v : v; }
+};
+
+struct XOutF {
+    float *hi, *lo;
+    int mode;
+    __device__ __forceinline__ void put(size_t o, float v) const {
+        if (mode == 0) {
+            hi[o] = v;
+        } else if (mode == 1) {
+            hi[o] = v;
+            lo[o] = 0.0f;
+        } else {
+            const df r = df_add_f(df{hi[o], lo[o]}, v);
+            hi[o] = r.hi;
+            lo[o] = r.lo;
+        }
+    }
+};
+
 // Inverse: spectral rows jj, jj+1 (nrow_h per plane) -> real rows jdst0 + jj,
-// jdst0 + jj + 1 of a halo-layout field (x written at 1..n).  With a base
-// field the result is dst = base + value (the mixed-precision path forms the
-// FP64 predicted velocity from the FP32 increment here).
-template <typename T, typename TO>
-__global__ void k_fft_x_inv(const T *__restrict__ H, TO *dst, const TO *base, int n, int nrow_h, int npairs_per_plane,
+// jdst0 + jj + 1 of a halo-layout field (x written at 1..n) through the
+// destination functor.
+template <typename T, typename Out>
+__global__ void k_fft_x_inv(const T *__restrict__ H, Out out, int n, int nrow_h, int npairs_per_plane,
                             int nplanes, int jdst0, int sx, int sy, const T *__restrict__ twr, const T *__restrict__ twi,
                             int plain = 0) {
     extern __shared__ unsigned char smem_raw[];
@@ -130,14 +158,8 @@ __global__ void k_fft_x_inv(const T *__restrict__ H, TO *dst, const TO *base, in
     // row length n and sy rows per plane
     const size_t oa = plain ? (size_t)n * ((size_t)(jdst0 + jj) + (size_t)sy * k)
                             : 1 + (size_t)sx * ((size_t)(jdst0 + jj) + (size_t)sy * (k + 1));
-    TO *ra = dst + oa;
-    TO *rb = ra + (plain ? n : sx);
-    if (base) {
-        const TO *ba = base + oa, *bb = ba + sx;
-        for (int e = t; e < n; e += tpp) { ra[e] = ba[e] + TO(x[e].r); rb[e] = bb[e] + TO(x[e].i); }
-    } else {
-        for (int e = t; e < n; e += tpp) { ra[e] = TO(x[e].r); rb[e] = TO(x[e].i); }
-    }
+    const size_t ob = oa + (plain ? n : sx);
+    for (int e = t; e < n; e += tpp) { out.put(oa + e, x[e].r); out.put(ob + e, x[e].i); }
 }
 
 // ---------------------------------------------------------------------------

@@ -14,7 +14,7 @@
 //              the inverse transforms.  Forward transforms are decimation in
 //              time (bit-reversed load), inverse ones decimation in frequency
 //              (bit-reversed store), so no reordering pass is needed.
-//   k_xinv_t   S -> real rows, optionally added to an FP64 base field.
+//   k_xinv_t   S -> real rows through a destination functor (XOutF).
 #pragma once
 #include "f8_common.cuh"
 #include "f8_fft.cuh"
@@ -72,10 +72,10 @@ __global__ void k_xfwd_t(const TS *__restrict__ src, float2 *__restrict__ S, int
 }
 
 // x inverse, transposing: rows j = jlo .. jlo+nrow-1 of S (S row index
-// j + joff2) become real rows j of the halo-layout dst (x at 1..nx), added to
-// base when given.
-template <typename TO>
-__global__ void k_xinv_t(const float2 *__restrict__ S, TO *dst, const TO *base, int nx, int nrow, int jlo, int nz,
+// j + joff2) become real rows j of a halo-layout field (x at 1..nx), written
+// through the destination functor (XOutF).
+template <typename Out>
+__global__ void k_xinv_t(const float2 *__restrict__ S, Out out, int nx, int nrow, int jlo, int nz,
                          int rb, int lj, int joff2, int sx, int sy, const float *__restrict__ twr,
                          const float *__restrict__ twi) {
     extern __shared__ unsigned char smem_raw[];
@@ -118,12 +118,10 @@ __global__ void k_xinv_t(const float2 *__restrict__ S, TO *dst, const TO *base, 
     }
     if (!active) return;
     const size_t oa = 1 + (size_t)sx * ((size_t)(jlo + r0 + 2 * p) + (size_t)sy * (k + 1));
-    TO *ra = dst + oa, *rbp = ra + sx;
-    if (base) {
-        const TO *ba = base + oa, *bb = ba + sx;
-        for (int e = t; e < nx; e += half) { ra[e] = ba[e] + TO(x[e].r); rbp[e] = bb[e] + TO(x[e].i); }
-    } else {
-        for (int e = t; e < nx; e += half) { ra[e] = TO(x[e].r); rbp[e] = TO(x[e].i); }
+    const bool has_b = 2 * p + 1 < nrows;
+    for (int e = t; e < nx; e += half) {
+        out.put(oa + e, x[e].r);
+        if (has_b) out.put(oa + sx + e, x[e].i);
     }
 }
 
@@ -393,82 +391,6 @@ struct WallTables {
     int sys;
 };
 
-template <int V>
-__global__ void __launch_bounds__(1024, 1) k_plane_walls_w(float2 *S, int ny, const float2 *twz, WallTables wt) {
-    constexpr int NZ = 32 * V;
-    extern __shared__ unsigned char smem_raw[];
-    const int lj = ny + 2;
-    const int ljs = lj | 1;
-    float2 *P = reinterpret_cast<float2 *>(smem_raw);                // [k][j]
-    float *Pc = reinterpret_cast<float *>(P + (size_t)ljs * NZ);     // [kz][j]
-    float2 *tws = reinterpret_cast<float2 *>(Pc + (size_t)ljs * NZ); // NZ/2 twiddles
-    const int kx = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    float2 *Sp = S + (size_t)kx * NZ * lj;
-    for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
-    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
-        const int k = q / lj, j = q % lj;
-        P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    // forward z transform of rows 1..ny (output in bit-reversed kz order)
-    for (int j = 1 + warp; j <= ny; j += nwarp) {
-        float2 v[V];
-#pragma unroll
-        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
-        warp_dif_fwd<V>(v, tws, lane);
-#pragma unroll
-        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
-    }
-    __syncthreads();
-    // Thomas sweeps, one thread per kz (its data sits at row bitrev(kz))
-    constexpr int LG = V == 1 ? 5 : (V == 2 ? 6 : (V == 4 ? 7 : 8));
-    for (int kz = threadIdx.x; kz < NZ; kz += blockDim.x) {
-        const int row = (int)(__brev((unsigned)kz) >> (32 - LG));
-        float2 *x = P + (size_t)row * ljs;
-        float *pc = Pc + (size_t)kz * ljs;
-        const float *Pt = wt.P + ((size_t)kx * NZ + kz) * lj;
-        const float *Rt = wt.rden + ((size_t)kx * NZ + kz) * lj;
-        float2 q = make_float2(0.f, 0.f);   // d_0 = 0 for every system
-        pc[0] = Pt[0];
-        x[0] = q;
-#pragma unroll 4
-        for (int j = 1; j < lj; ++j) {
-            float c;
-            float2 d;
-            const bool ident = (wt.sys == SYS_V) ? (j >= ny) : (j == lj - 1);
-            if (ident) { c = wt.sys == SYS_V ? 0.f : wt.c_last; d = make_float2(0.f, 0.f); }
-            else { c = wt.bc; d = x[j]; d.x *= wt.nxz_inv; d.y *= wt.nxz_inv; }
-            const float rd = Rt[j];
-            q = make_float2((d.x - c * q.x) * rd, (d.y - c * q.y) * rd);
-            pc[j] = Pt[j];
-            x[j] = q;
-        }
-        float2 xv = q;
-        for (int j = lj - 2; j >= 0; --j) {
-            const float pj = pc[j];
-            const float2 qj = x[j];
-            xv = make_float2(pj * xv.x + qj.x, pj * xv.y + qj.y);
-            x[j] = xv;
-        }
-    }
-    __syncthreads();
-    // inverse z transform of all rows (bit-reversed in, natural out)
-    for (int j = warp; j < lj; j += nwarp) {
-        float2 v[V];
-#pragma unroll
-        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
-        warp_dit_inv<V>(v, tws, lane);
-#pragma unroll
-        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
-        const int k = q / lj, j = q % lj;
-        Sp[q] = P[(size_t)k * ljs + j];
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Warp-per-row-pair x passes (NX = 32 E).  Each warp transforms two real rows
 // packed as one complex line with warp_dif_fwd / warp_dit_inv (lane t holds
@@ -538,8 +460,8 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xfwd_w(const TS *__restrict__
     }
 }
 
-template <int E, typename TO>
-__global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restrict__ S, TO *dst, const TO *base,
+template <int E, typename Out>
+__global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restrict__ S, Out out,
                                                          int nrow, int jlo, int nz, int rb, int lj, int joff2, int sx,
                                                          int sy, const float2 *__restrict__ twx) {
     constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v;
@@ -574,22 +496,11 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
         __syncwarp();
         warp_dit_inv<E>(v, tws, lane);
         const size_t oa = 1 + (size_t)sx * ((size_t)(jlo + r0 + 2 * p) + (size_t)sy * (k + 1));
-        TO *ra = dst + oa;
-        if (base) {
-            const TO *ba = base + oa;
 #pragma unroll
-            for (int s = 0; s < E; ++s) {
-                const int e = lane + 32 * s;
-                ra[e] = ba[e] + TO(v[s].x);
-                if (has_b) ra[sx + e] = ba[sx + e] + TO(v[s].y);
-            }
-        } else {
-#pragma unroll
-            for (int s = 0; s < E; ++s) {
-                const int e = lane + 32 * s;
-                ra[e] = TO(v[s].x);
-                if (has_b) ra[sx + e] = TO(v[s].y);
-            }
+        for (int s = 0; s < E; ++s) {
+            const int e = lane + 32 * s;
+            out.put(oa + e, v[s].x);
+            if (has_b) out.put(oa + sx + e, v[s].y);
         }
     }
 }
@@ -601,7 +512,8 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
 //   backward  x_j = P_j x_{j+1} + q_j,
 // so each thread composes the maps of its chunk of rows, the T threads scan
 // the composed maps with shuffles, and each thread then replays its chunk
-// from its incoming value.  Same coefficients as k_plane_walls_w.
+// from its incoming value.  The coefficients are those of the sequential
+// Thomas solve of k_plane_walls (tdma, fenep_2d.f90:1145-1177), tabulated.
 template <int V>
 __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, const float2 *twz, WallTables wt) {
     constexpr int NZ = 32 * V;

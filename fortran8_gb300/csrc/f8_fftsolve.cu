@@ -71,7 +71,7 @@ cudaError_t run_solve(const double *q, double *phi, double *H, const double *dta
     const size_t smz = (size_t)2 * nz * txz * sizeof(Cx<double>);
     k_fft_lines<double><<<dim3((nxh + txz - 1) / txz, ny), 256, smz, s>>>(H, nz, nxh * ny, nxh, nxh, txz, twz_r, twz_i, -1, 1, dv); count_launch();
     k_fft_lines<double><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(H, ny, nxh, nxh, nxh * ny, txy, twy_r, twy_i, +1, 0, none); count_launch();
-    k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(H, phi, nullptr, nx, ny, npp, nz, 0, nx, ny,
+    k_fft_x_inv<double, XOutD><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(H, XOutD{phi, nullptr}, nx, ny, npp, nz, 0, nx, ny,
                                                                             twx_r, twx_i, 1); count_launch();
     return cudaGetLastError();
 }
@@ -89,7 +89,7 @@ cudaError_t set_smem_attrs() {
     const int big = 200 * 1024;
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double, XOutD>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return cudaSuccess;
 }
 

@@ -36,14 +36,18 @@ struct Dev {
     int *csr_off[3], *csr_idx[3];          // per component over (SX*SY) columns
     int *mperm, *moff;                     // markers grouped by cylinder (drag reduction)
     double *dragpart;                      // ncyl * nz * 3 partial sums
-    float *Uf, *Vf, *Wf;                   // FP32 copies of U, V, W (halo), mixed path
-    // mixed-precision state and work (F8_MIXED)
+    // mixed-precision state and work (F8_MIXED): the state as df64 pairs
+    // (hi, lo) of FP32 halo fields
+    float *Uf, *Vf, *Wf, *Ul, *Vl, *Wl;    // velocity hi / lo
+    float *Pf, *Pl;                        // pressure hi / lo
+    float *Phif, *Phil;                    // pressure correction hi / lo
+    float *dUf[3];                         // Helmholtz increments dU, dV, dW (halo)
     float *Cf, *Cnf, *fpetf;               // FP32 conformation tensor (SoA halo) and f(C)
     int *fixlist, *fixcnt;                 // cells queued for the exact Newton re-solve
     float *A0f[3], *T0f[3], *Ff[3];        // FP32 history and body force (interior)
     float *Qf[3];                          // FP32 right-hand sides dt*(R + f)
-    double *Rp;                            // FP64 Poisson right-hand side (interior)
-    double *Rd;                            // FP64 Poisson defect (interior)
+    float *Rhf, *Rlf;                      // df64 Poisson right-hand side (interior)
+    float *Rdf;                            // Poisson defect (interior)
     float *Hf, *H2f;                       // FP32 spectra
     float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
     float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
@@ -91,6 +95,8 @@ cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s);
 cudaError_t init_kernels_mixed();
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s);
 cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s);
+cudaError_t mixed_state_to_fp64(Dev &d, cudaStream_t s);
+cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cudaStream_t s);
 cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s);
 cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s);
 cudaError_t aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs, cudaStream_t s);

@@ -251,11 +251,6 @@ __device__ inline void gauss(double (&Ah)[N][N + 1], double *x) {
     for (int r = 0; r < N; ++r) x[r] = Ah[r][N];
 }
 
-__device__ inline void warp_count(unsigned long long v, unsigned long long *dst) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
-}
-
 // Cstar (fenep.f90:464-507) + Lyapunov Newton (fenep.f90:518-585) for one
 // cell.  The face states Cp/Cn of the three cells along each direction are
 // rebuilt from their selection codes, so no face arrays are stored.
@@ -1028,7 +1023,7 @@ cudaError_t fft_solve_periodic(Dev &d, const double *src, double *dst, double lh
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = ny / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, dst, nullptr, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
+        k_fft_x_inv<double, XOutD><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H, XOutD{dst, nullptr}, nx, ny, npp, nz, 1, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -1068,7 +1063,7 @@ cudaError_t wall_solve(Dev &d, const double *src, double *dst, int sys, double u
         int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
         int npp = n / 2, total = npp * nz;
         size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
-        k_fft_x_inv<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, dst, nullptr, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
+        k_fft_x_inv<double, XOutD><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(d.H2, XOutD{dst, nullptr}, nx, n, npp, nz, 0, g.sx, g.sy, d.twx_r, d.twx_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -1122,7 +1117,7 @@ cudaError_t init_kernels_fp64() {
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_wall_tdma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<double, XOutD>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return cudaSuccess;
 }
 

@@ -1,23 +1,28 @@
-// f8_step_mixed.cu — FP32-bulk / FP64-state step (F8_MIXED).
+// f8_step_mixed.cu — FP32-bulk step with a double-float state (F8_MIXED).
 //
 // Same discretisation as the FP64 step (fenep.f90 numerics; cited per kernel
 // in f8_step_fp64.cu), with the precision split:
-//   FP64: U, V, W, P, Phi state; the pressure gradient; the formation of the
-//         predicted velocity U* = U^n + dU; the Poisson right-hand side and its
-//         defect; the projection; marker forces and drag; the Peterlin factor
-//         when L^2 - tr C < 1% of L^2.
+//   df64 (hi + lo FP32 pairs, 48-bit significand, FP32 pipes only): the state
+//         U, V, W, P and the pressure correction Phi; the Poisson right-hand
+//         side div(U^n + dU)/dt and its defect; the projection and the
+//         pressure update.
+//   FP64: marker velocities, marker forces and drag; the Peterlin factor when
+//         L^2 - tr C < 1% of L^2.
 //   FP32: C, f(C), the AB2/trapezoid history, stress / convection / viscous
-//         stencils, the eigen test and Newton solve of the polymer update, and
-//         every spectral transform and tridiagonal solve.
+//         stencils (on the hi parts), the pressure gradient, the eigen test
+//         and Newton solve of the polymer update, and every spectral
+//         transform and tridiagonal solve.
 // The predictor is solved in increment form: (1 - dt beta/(2Re) L) dU =
 // dt (R + f), with R = -grad P + (3A - A0)/2 + B + (T + T0)/2 + F.  This is
 // algebraically the reference's (1 - dt beta/(2Re) L) U* = Q (fenep.f90:
-// 1469-1479, 2229-2233) with U* = U^n + dU, but FP32 rounding now touches only
-// the O(dt) increment.  The Poisson equation is solved in FP32 and corrected
-// with FP64 residuals (iterative refinement).
+// 1469-1479, 2229-2233) with U* = U^n + dU, but FP32 rounding touches only the
+// O(dt) increment.  The Poisson equation is solved in FP32 and corrected once
+// with a df64 residual (iterative refinement), so that the projected velocity
+// is divergence-free to the df64 rounding level.
 #include <algorithm>
 #include <cstdio>
 #include "f8_common.cuh"
+#include "f8_df64.cuh"
 #include "f8_fft.cuh"
 #include "f8_fft_fused.cuh"
 #include "f8_kernels.h"
@@ -34,9 +39,10 @@ struct MixConst {
     float sx, sy, sz;                      // dt/(2dX) ... (upwind weights of Cstar)
     float ix, iy, iz;                      // 1/dX ...
     float ix2, iy2, iz2;                   // 1/dX^2 ...
-    double idx, idy, idz, idx2, idy2, idz2, idt;
-    double dtdx, dtdy, dtdz;              // dt/dX ...
-    double pc;                             // dt beta / (2 Re)
+    df di[3], di2[3];                      // 1/dX, 1/dX^2 ... as df64 constants
+    df dtd[3];                             // dt/dX ...
+    df idt;                                // 1/dt
+    float pcf;                             // dt beta / (2 Re)
     float dtwi, lp2f, epsf;                // dt/Wi, L^2, Newton tolerance (FP32)
 };
 
@@ -48,11 +54,14 @@ MixConst make_const(const Geo &g, const Phys &ph) {
     c.sx = (float)(ph.dt / (2 * g.dx)); c.sy = (float)(ph.dt / (2 * g.dy)); c.sz = (float)(ph.dt / (2 * g.dz));
     c.ix = (float)(1.0 / g.dx); c.iy = (float)(1.0 / g.dy); c.iz = (float)(1.0 / g.dz);
     c.ix2 = (float)(1.0 / (g.dx * g.dx)); c.iy2 = (float)(1.0 / (g.dy * g.dy)); c.iz2 = (float)(1.0 / (g.dz * g.dz));
-    c.idx = 1.0 / g.dx; c.idy = 1.0 / g.dy; c.idz = 1.0 / g.dz;
-    c.idx2 = 1.0 / (g.dx * g.dx); c.idy2 = 1.0 / (g.dy * g.dy); c.idz2 = 1.0 / (g.dz * g.dz);
-    c.idt = 1.0 / ph.dt;
-    c.dtdx = ph.dt / g.dx; c.dtdy = ph.dt / g.dy; c.dtdz = ph.dt / g.dz;
-    c.pc = ph.dt * ph.beta / ph.re / 2.0;
+    const double dd[3] = {g.dx, g.dy, g.dz};
+    for (int q = 0; q < 3; ++q) {
+        c.di[q] = df_from_d(1.0 / dd[q]);
+        c.di2[q] = df_from_d(1.0 / (dd[q] * dd[q]));
+        c.dtd[q] = df_from_d(ph.dt / dd[q]);
+    }
+    c.idt = df_from_d(1.0 / ph.dt);
+    c.pcf = (float)(ph.dt * ph.beta / ph.re / 2.0);
     c.dtwi = (float)(ph.dt / ph.wi);
     c.lp2f = (float)ph.lp2;
     c.epsf = (float)ph.newton_eps;
@@ -121,33 +130,47 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
-// halo values of U, V, W, P (PBM / wall rules, fenep_2d.f90:1098-1129) for
-// the FP64 fields and their FP32 copies in one pass
-__device__ inline double halo_val_m(const Geo &g, const double *A, int kind, int i, int j, int k) {
+// halo values (PBM / wall rules, fenep_2d.f90:1098-1129) of a df64 field;
+// uw2 = 2 * upper wall speed (0 for the increments)
+__device__ inline df halo_df(const Geo &g, const float *H, const float *L, int kind, int i, int j, int k, df uw2) {
     const int ii = wrapx(g, i), kk = wrapz(g, k);
+    auto at = [&](int a, int b, int c) {
+        const int q = hix(g, a, b, c);
+        return df{H[q], L ? L[q] : 0.0f};
+    };
     if (j >= 1 && j <= g.ny) {
-        if (g.walls && kind == BC_V && j == g.ny) return 0.0;
-        return A[hix(g, ii, j, kk)];
+        if (g.walls && kind == BC_V && j == g.ny) return df{0.0f, 0.0f};
+        return at(ii, j, kk);
     }
-    if (!g.walls) return A[hix(g, ii, wrapy(g, j), kk)];
+    if (!g.walls) return at(ii, wrapy(g, j), kk);
     const bool lo = j == 0;
     switch (kind) {
-    case BC_U: return lo ? -A[hix(g, ii, 1, kk)] : 2 * g.uwall - A[hix(g, ii, g.ny, kk)];
-    case BC_W: return lo ? -A[hix(g, ii, 1, kk)] : -A[hix(g, ii, g.ny, kk)];
-    case BC_V: return 0.0;
-    default:   return lo ? A[hix(g, ii, 1, kk)] : A[hix(g, ii, g.ny, kk)];
+    case BC_U: return lo ? df_neg(at(ii, 1, kk)) : df_sub(uw2, at(ii, g.ny, kk));
+    case BC_W: return df_neg(at(ii, lo ? 1 : g.ny, kk));
+    case BC_V: return df{0.0f, 0.0f};
+    default:   return at(ii, lo ? 1 : g.ny, kk);
     }
 }
 
-__global__ void k_bc_vel_m(double *U, double *V, double *W, double *P, float *Uf, float *Vf, float *Wf, Geo g) {
+// Boundary values of up to four df64 (lo != null) or FP32 (lo == null)
+// fields, and V = 0 on the upper wall face when a field of kind BC_V is given.
+struct BcSet {
+    float *hi[4], *lo[4];
+    int kind[4];
+    int n;
+    df uw2;
+};
+
+__global__ void k_bc_set(BcSet b, Geo g) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
     if (halo_cell_m(g, t, i, j, k)) {
         const int h = hix(g, i, j, k);
-        const double u = halo_val_m(g, U, BC_U, i, j, k), v = halo_val_m(g, V, BC_V, i, j, k);
-        const double w = halo_val_m(g, W, BC_W, i, j, k), p = halo_val_m(g, P, BC_P, i, j, k);
-        U[h] = u; V[h] = v; W[h] = w; P[h] = p;
-        Uf[h] = (float)u; Vf[h] = (float)v; Wf[h] = (float)w;
+        for (int f = 0; f < b.n; ++f) {
+            const df v = halo_df(g, b.hi[f], b.lo[f], b.kind[f], i, j, k, b.uw2);
+            b.hi[f][h] = v.hi;
+            if (b.lo[f]) b.lo[f][h] = v.lo;
+        }
         return;
     }
     if (g.walls) {  // V on the upper wall face
@@ -155,9 +178,28 @@ __global__ void k_bc_vel_m(double *U, double *V, double *W, double *P, float *Uf
         if (t >= 0 && t < (long)g.nx * g.nz) {
             i = 1 + (int)(t % g.nx); k = 1 + (int)(t / g.nx);
             const int h = hix(g, i, g.ny, k);
-            V[h] = 0.0; Vf[h] = 0.0f;
+            for (int f = 0; f < b.n; ++f)
+                if (b.kind[f] == BC_V) {
+                    b.hi[f][h] = 0.0f;
+                    if (b.lo[f]) b.lo[f][h] = 0.0f;
+                }
         }
     }
+}
+
+// FP64 <-> df64 pairs (load / store)
+__global__ void k_split_df(const double *src, float *hi, float *lo, int n) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const df v = df_from_d(src[q]);
+    hi[q] = v.hi;
+    lo[q] = v.lo;
+}
+
+__global__ void k_join_df(const float *hi, const float *lo, double *dst, int n) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    dst[q] = (double)hi[q] + (double)lo[q];
 }
 
 __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
@@ -528,8 +570,8 @@ __global__ void __launch_bounds__(128) k_newton_fix_f(const float *__restrict__ 
 // ---------------------------------------------------------------------------
 // Momentum right-hand side in increment form: Q_c = dt * R_c (FP32).
 struct MomArgsF {
-    const float *U, *V, *W;   // FP32 copies of the velocity
-    const double *P;
+    const float *U, *V, *W;   // hi parts of the velocity
+    const float *Ph, *Pl;     // pressure (df64)
     const float *C, *fpet;
     float *A0[3], *T0[3];
     const float *F[3];
@@ -598,13 +640,15 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst
     const float T[3] = {tx, ty, tz};
     const int hp[3] = {h + ox, h + oy, h + oz};
     const float id[3] = {ix, iy, iz};
-    const double pc0 = a.P[h];
+    const float ph0 = a.Ph[h], pl0 = a.Pl[h];
     const float dt = (float)a.dt;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float a0 = a.ab2_first ? A[c] : a.A0[c][o];
         const float t0 = a.ab2_first ? T[c] : a.T0[c][o];
-        const float gp = -(float)(a.P[hp[c]] - pc0) * id[c];   // pressure difference in FP64
+        // pressure difference from the df64 pair: the hi difference is
+        // correctly rounded, the lo difference carries the rest
+        const float gp = -((a.Ph[hp[c]] - ph0) + (a.Pl[hp[c]] - pl0)) * id[c];
         const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + a.F[c][o];
         a.Q[c][o] = dt * r;
         a.A0[c][o] = A[c];
@@ -615,16 +659,18 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst
 // ---------------------------------------------------------------------------
 // IBM (fenep_mpi.f90:1794-1929).  Ua = U + dt R at the stencil points with the
 // boundary values that the reference gives Ua (PBM / wall rules).
-__device__ inline double ua_at(const Geo &g, const double *Uc, const float *Qc, int comp, int i, int j, int k) {
+__device__ inline double ua_at(const Geo &g, const float *Uh, const float *Ul, const float *Qc, int comp, int i, int j,
+                               int k) {
     const int ii = wrapx(g, i), kk = wrapz(g, k);
+    auto u = [&](int q) { return (double)Uh[q] + (double)Ul[q]; };
     if (j >= 1 && j <= g.ny) {
         if (g.walls && comp == 1 && j == g.ny) return 0.0;
-        return Uc[hix(g, i, j, k)] + (double)Qc[qix(g, ii, j, kk)];
+        return u(hix(g, i, j, k)) + (double)Qc[qix(g, ii, j, kk)];
     }
-    if (!g.walls) return Uc[hix(g, i, j, k)] + (double)Qc[qix(g, ii, wrapy(g, j), kk)];
+    if (!g.walls) return u(hix(g, i, j, k)) + (double)Qc[qix(g, ii, wrapy(g, j), kk)];
     if (comp == 1) return 0.0;
     const int jj = j == 0 ? 1 : g.ny;
-    const double inner = Uc[hix(g, ii, jj, kk)] + (double)Qc[qix(g, ii, jj, kk)];
+    const double inner = u(hix(g, ii, jj, kk)) + (double)Qc[qix(g, ii, jj, kk)];
     return (comp == 0 && j != 0) ? 2 * g.uwall - inner : -inner;
 }
 
@@ -635,7 +681,7 @@ struct IbmArgsF {
     const float *wx[3], *wy[3];      // per marker, 3 weights each
     const int *i0[3], *j0[3];
     float wz[3][3];                  // per component, offset k - n = -1, 0, 1
-    const double *Uc[3];
+    const float *Uh[3], *Ul[3];      // velocity (df64)
     const float *Qc[3];
     double *Fc[3];
     const int *off[3], *idx[3];
@@ -657,7 +703,7 @@ __global__ void k_ibm_interp_f(IbmArgsF a, Geo g) {
         for (int dj = 0; dj < 3; ++dj)
             for (int di = 0; di < 3; ++di) {
                 const double w = (double)(wx[di] * wy[dj] * a.wz[comp][dk]);
-                ub += ua_at(g, a.Uc[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k) * w;
+                ub += ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k) * w;
             }
     }
     const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
@@ -713,50 +759,89 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
 // FP64 parts of the pressure solve and the projection, with reciprocal
 // multiplies instead of divisions.
 //   rhs = div(U*) / dt (fenep.f90:1547-1555)
-__global__ void k_poisson_rhs_m(const double *Up, const double *Vp, const double *Wp, double *Q, Geo g, MixConst mc) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.nx || j > g.ny) return;
-    const int h = hix(g, i, j, k);
-    const double s = (Up[h] - Up[h - 1]) * mc.idx + (Vp[h] - Vp[h - g.sx]) * mc.idy + (Wp[h] - Wp[h - g.sx * g.sy]) * mc.idz;
-    Q[qix(g, i, j, k)] = s * mc.idt;
-}
+// The df64 state of one field
+struct DfF {
+    float *hi, *lo;
+    __device__ __forceinline__ df at(int q) const { return df{hi[q], lo[q]}; }
+    __device__ __forceinline__ void set(int q, df v) const { hi[q] = v.hi; lo[q] = v.lo; }
+};
 
-// defect r = rhs - L_h Phi (Phi with Neumann / periodic halo)
-__global__ void k_defect(const double *Phi, const double *rhs, double *r, Geo g, MixConst mc) {
+// Poisson right-hand side div(U^n + dU)/dt (fenep.f90:1494-1510) in df64:
+// each face difference of the state and of the FP32 increment is formed
+// exactly, scaled by the df64 1/dX, and summed.
+__global__ void k_poisson_rhs_df(DfF U, DfF V, DfF W, const float *__restrict__ dU, const float *__restrict__ dV,
+                                 const float *__restrict__ dW, float *__restrict__ Rh, float *__restrict__ Rl, Geo g,
+                                 MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
     const int h = hix(g, i, j, k);
-    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-    const double c = Phi[h];
-    const double lap = (Phi[h - ox] - 2.0 * c + Phi[h + ox]) * mc.idx2 + (Phi[h - oy] - 2.0 * c + Phi[h + oy]) * mc.idy2
-                     + (Phi[h - oz] - 2.0 * c + Phi[h + oz]) * mc.idz2;
+    const int off[3] = {1, g.sx, g.sx * g.sy};
+    const DfF F[3] = {U, V, W};
+    const float *D[3] = {dU, dV, dW};
+    df sum{0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int hm = h - off[c];
+        df a = df_sub(F[c].at(h), F[c].at(hm));
+        a = df_add(a, df_diff_ff(D[c][h], D[c][hm]));
+        sum = df_add(sum, df_mul(a, mc.di[c]));
+    }
+    sum = df_mul(sum, mc.idt);
     const int o = qix(g, i, j, k);
-    r[o] = rhs[o] - lap;
+    Rh[o] = sum.hi;
+    Rl[o] = sum.lo;
 }
 
-// projection and SMAC pressure update (fenep.f90:1562-1604)
-__global__ void k_march_m(double *U, double *V, double *W, double *P, const double *Up, const double *Vp,
-                          const double *Wp, const double *Phi, float *Uf, float *Vf, float *Wf, Geo g, MixConst mc) {
+// defect r = rhs - L_h Phi in df64 (Phi with its Neumann / periodic halo);
+// the FP32 value of r drives the correction solve
+__global__ void k_defect_df(DfF Phi, const float *__restrict__ Rh, const float *__restrict__ Rl,
+                            float *__restrict__ r, Geo g, MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
     const int h = hix(g, i, j, k);
-    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-    const double ph = Phi[h];
-    const double px = Phi[h + ox], py = Phi[h + oy], pz = Phi[h + oz];
-    const double un = Up[h] - mc.dtdx * (px - ph);
-    const double vn = Vp[h] - mc.dtdy * (py - ph);
-    const double wn = Wp[h] - mc.dtdz * (pz - ph);
-    U[h] = un; V[h] = vn; W[h] = wn;
-    Uf[h] = (float)un; Vf[h] = (float)vn; Wf[h] = (float)wn;
-    const float lap = (float)(Phi[h - ox] - 2.0 * ph + px) * (float)mc.idx2 + (float)(Phi[h - oy] - 2.0 * ph + py) * (float)mc.idy2
-                    + (float)(Phi[h - oz] - 2.0 * ph + pz) * (float)mc.idz2;
-    P[h] = P[h] + ph - (double)((float)mc.pc * lap);
+    const int off[3] = {1, g.sx, g.sx * g.sy};
+    const df c0 = Phi.at(h);
+    const int o = qix(g, i, j, k);
+    df res{Rh[o], Rl[o]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const df dp = df_sub(Phi.at(h + off[c]), c0), dm = df_sub(c0, Phi.at(h - off[c]));
+        res = df_sub(res, df_mul(df_sub(dp, dm), mc.di2[c]));
+    }
+    r[o] = df_to_f(res);
+}
+
+// projection and SMAC pressure update (fenep.f90:1562-1604):
+// U^{n+1} = U^n + (dU - dt/dX (Phi_{+1} - Phi)) in df64, and
+// P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
+// in FP32
+__global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
+                           const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const int h = hix(g, i, j, k);
+    const int off[3] = {1, g.sx, g.sx * g.sy};
+    const DfF F[3] = {U, V, W};
+    const float *D[3] = {dU, dV, dW};
+    const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
+    const df c0 = Phi.at(h);
+    float lap = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const df pp = Phi.at(h + off[c]), pm = Phi.at(h - off[c]);
+        const df dp = df_sub(pp, c0);
+        const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
+        F[c].set(h, df_add(F[c].at(h), inc));
+        const float dpf = (pp.hi - c0.hi) + (pp.lo - c0.lo), dmf = (c0.hi - pm.hi) + (c0.lo - pm.lo);
+        lap += (dpf - dmf) * i2[c];
+    }
+    P.set(h, df_add_f(df_add(P.at(h), c0), -mc.pcf * lap));
 }
 
 template <typename A, typename B>
@@ -783,8 +868,7 @@ inline dim3 cell_grid_m(const Geo &g, dim3 blk) {
 // FP32 spectral solves.  src (interior, FP32 or FP64) -> dst (FP64 halo
 // interior; dst = base + result when base is given).
 template <typename TS>
-cudaError_t solve_periodic_mp(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
-                             cudaStream_t s) {
+cudaError_t solve_periodic_mp(Dev &d, const TS *src, XOutF out, double lhs0, double lhs1, cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
     const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
@@ -806,13 +890,13 @@ cudaError_t solve_periodic_mp(Dev &d, const TS *src, double *dst, const double *
     k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, +1, 0, none); count_launch();
     {
         int npp = ny / 2, total = npp * nz;
-        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, dst, base, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+        k_fft_x_inv<float, XOutF><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, out, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
 
 template <typename TS>
-cudaError_t solve_walls_mp(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+cudaError_t solve_walls_mp(Dev &d, const TS *src, XOutF out, int sys, cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, n = ny + 2;
     const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
@@ -838,7 +922,7 @@ cudaError_t solve_walls_mp(Dev &d, const TS *src, double *dst, const double *bas
     }
     {
         int npp = n / 2, total = npp * nz;
-        k_fft_x_inv<float, double><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.H2f, dst, base, nx, n, npp, nz, 0, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+        k_fft_x_inv<float, XOutF><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.H2f, out, nx, n, npp, nz, 0, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
@@ -871,19 +955,17 @@ bool xfwd_warp(const Dev &d, const TS *src, float2 *S, int ny, int lj, int joff,
     return true;
 }
 
-template <typename TO>
-bool xinv_warp(const Dev &d, const float2 *S, TO *dst, const TO *base, int nrow, int jlo, int lj, int joff2,
-               cudaStream_t s) {
+bool xinv_warp(const Dev &d, const float2 *S, XOutF out, int nrow, int jlo, int lj, int joff2, cudaStream_t s) {
     const Geo &g = d.g;
     const unsigned grid = (unsigned)(((nrow + XW_RB - 1) / XW_RB) * g.nz);
     const size_t sm = xw_smem(g.nx, XW_RB);
     const int thr = 32 * XW_WARPS;
     switch (g.nx) {
-    case 32: k_xinv_w<1, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 64: k_xinv_w<2, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 128: k_xinv_w<4, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 256: k_xinv_w<8, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 512: k_xinv_w<16, TO><<<grid, thr, sm, s>>>(S, dst, base, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 32: k_xinv_w<1, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 64: k_xinv_w<2, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 128: k_xinv_w<4, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 256: k_xinv_w<8, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 512: k_xinv_w<16, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
     default: return false;
     }
     count_launch();
@@ -891,8 +973,7 @@ bool xinv_warp(const Dev &d, const float2 *S, TO *dst, const TO *base, int nrow,
 }
 
 template <typename TS>
-cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const double *base, float lhs0, float lhs1,
-                                 cudaStream_t s) {
+cudaError_t solve_periodic_fused(Dev &d, const TS *src, XOutF out, float lhs0, float lhs1, cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
     float2 *S = reinterpret_cast<float2 *>(d.Hf);
@@ -908,14 +989,14 @@ cudaError_t solve_periodic_fused(Dev &d, const TS *src, double *dst, const doubl
     ps.lhs0 = lhs0; ps.lhs1 = lhs1; ps.inv_ntot = (float)(1.0 / ((double)nx * ny * nz));
     k_plane_periodic<<<nxh, 1024, (size_t)8 * (ny + 1) * nz, s>>>(S, ny, nz, ilog2(ny), ilog2(nz), d.twyf_r, d.twyf_i,
                                                                  d.twzf_r, d.twzf_i, ps); count_launch();
-    if (!xinv_warp<double>(d, S, dst, base, ny, 1, ny, -1, s)) {
-        k_xinv_t<double><<<bpp * nz, thr, smx, s>>>(S, dst, base, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+    if (!xinv_warp(d, S, out, ny, 1, ny, -1, s)) {
+        k_xinv_t<XOutF><<<bpp * nz, thr, smx, s>>>(S, out, nx, ny, 1, nz, rb, ny, -1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
 
 template <typename TS>
-cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
+cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStream_t s) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, lj = ny + 2;
     float2 *S = reinterpret_cast<float2 *>(d.Hf);
@@ -943,24 +1024,21 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, double *dst, const double *
     } else {
         k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps); count_launch();
     }
-    if (!xinv_warp<double>(d, S, dst, base, lj, 0, lj, 0, s)) {
-        k_xinv_t<double><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, dst, base, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
-                                                                   d.twxf_r, d.twxf_i); count_launch();
+    if (!xinv_warp(d, S, out, lj, 0, lj, 0, s)) {
+        k_xinv_t<XOutF><<<((lj + rb - 1) / rb) * nz, thr, smx, s>>>(S, out, nx, lj, 0, nz, rb, lj, 0, g.sx, g.sy,
+                                                                  d.twxf_r, d.twxf_i); count_launch();
     }
     return cudaGetLastError();
 }
 
-template <typename TS>
-cudaError_t solve_periodic_f(Dev &d, const TS *src, double *dst, const double *base, double lhs0, double lhs1,
-                             cudaStream_t s) {
-    if (d.fused_planes) return solve_periodic_fused<TS>(d, src, dst, base, (float)lhs0, (float)lhs1, s);
-    return solve_periodic_mp<TS>(d, src, dst, base, lhs0, lhs1, s);
+cudaError_t solve_periodic_f(Dev &d, const float *src, XOutF out, double lhs0, double lhs1, cudaStream_t s) {
+    if (d.fused_planes) return solve_periodic_fused<float>(d, src, out, (float)lhs0, (float)lhs1, s);
+    return solve_periodic_mp<float>(d, src, out, lhs0, lhs1, s);
 }
 
-template <typename TS>
-cudaError_t solve_walls_f(Dev &d, const TS *src, double *dst, const double *base, int sys, cudaStream_t s) {
-    if (d.fused_planes) return solve_walls_fused<TS>(d, src, dst, base, sys, s);
-    return solve_walls_mp<TS>(d, src, dst, base, sys, s);
+cudaError_t solve_walls_f(Dev &d, const float *src, XOutF out, int sys, cudaStream_t s) {
+    if (d.fused_planes) return solve_walls_fused<float>(d, src, out, sys, s);
+    return solve_walls_mp<float>(d, src, out, sys, s);
 }
 
 }  // namespace
@@ -970,8 +1048,7 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_wall_tdma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_inv<float, XOutF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     int dev = 0, optin = 0;
     F8_CUDA_RET(cudaGetDevice(&dev));
     F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -982,16 +1059,11 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
 #define F8_XW_ATTR(E)                                                                                           \
     F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_w<E, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));   \
-    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_w<E, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));  \
-    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_w<E, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_w<E, XOutF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     F8_XW_ATTR(1) F8_XW_ATTR(2) F8_XW_ATTR(4) F8_XW_ATTR(8) F8_XW_ATTR(16)
 #undef F8_XW_ATTR
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_w<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_t<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_t<XOutF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     return cudaSuccess;
 }
 
@@ -1012,6 +1084,35 @@ cudaError_t soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs, cudaS
     return cudaGetLastError();
 }
 
+namespace {
+
+BcSet state_bc_set(const Dev &d) {
+    BcSet b{};
+    b.hi[0] = d.Uf; b.lo[0] = d.Ul; b.kind[0] = BC_U;
+    b.hi[1] = d.Vf; b.lo[1] = d.Vl; b.kind[1] = BC_V;
+    b.hi[2] = d.Wf; b.lo[2] = d.Wl; b.kind[2] = BC_W;
+    b.hi[3] = d.Pf; b.lo[3] = d.Pl; b.kind[3] = BC_P;
+    b.n = 4;
+    b.uw2 = df_from_d(2.0 * d.g.uwall);
+    return b;
+}
+
+cudaError_t launch_bc_set(const BcSet &b, const Geo &g, cudaStream_t s) {
+    const long n = halo_count_m(g) + (g.walls ? (long)g.nx * g.nz : 0);
+    k_bc_set<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, g); count_launch();
+    return cudaGetLastError();
+}
+
+__global__ void k_count_nonfinite_f(const float *a, int n, unsigned long long *out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool bad = q < n && !isfinite(a[q]);
+    const unsigned m = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(out, (unsigned long long)__popc(m));
+}
+
+}  // namespace
+
+// the loaded FP64 state (halo values applied) -> df64 pairs, f(C)
 cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     F8_CUDA_RET(bc_field(d.U, d.g, BC_U, s));
     F8_CUDA_RET(bc_field(d.V, d.g, BC_V, s));
@@ -1020,9 +1121,26 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     long n = halo_count_m(d.g);
     k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
     k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
-    F8_CUDA_RET(d2f(d.U, d.Uf, d.cs, s));
-    F8_CUDA_RET(d2f(d.V, d.Vf, d.cs, s));
-    F8_CUDA_RET(d2f(d.W, d.Wf, d.cs, s));
+    const double *src[5] = {d.U, d.V, d.W, d.P, d.Phi};
+    float *hi[5] = {d.Uf, d.Vf, d.Wf, d.Pf, d.Phif}, *lo[5] = {d.Ul, d.Vl, d.Wl, d.Pl, d.Phil};
+    for (int q = 0; q < 5; ++q) {
+        k_split_df<<<(d.cs + 255) / 256, 256, 0, s>>>(src[q], hi[q], lo[q], d.cs); count_launch();
+    }
+    return cudaGetLastError();
+}
+
+// df64 state -> the FP64 fields U, V, W, P, Phi (for store and diagnostics)
+cudaError_t mixed_state_to_fp64(Dev &d, cudaStream_t s) {
+    double *dst[5] = {d.U, d.V, d.W, d.P, d.Phi};
+    const float *hi[5] = {d.Uf, d.Vf, d.Wf, d.Pf, d.Phif}, *lo[5] = {d.Ul, d.Vl, d.Wl, d.Pl, d.Phil};
+    for (int q = 0; q < 5; ++q) {
+        k_join_df<<<(d.cs + 255) / 256, 256, 0, s>>>(hi[q], lo[q], dst[q], d.cs); count_launch();
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cudaStream_t s) {
+    k_count_nonfinite_f<<<(n + 255) / 256, 256, 0, s>>>(a, n, out); count_launch();
     return cudaGetLastError();
 }
 
@@ -1031,6 +1149,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     cudaError_t e;
     const MixConst mc = make_const(g, d.ph);
     auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
+    const DfF U{d.Uf, d.Ul}, V{d.Vf, d.Vl}, W{d.Wf, d.Wl}, P{d.Pf, d.Pl}, Phi{d.Phif, d.Phil};
     mark(0);
     if (o.polymer) {
         dim3 blk(32, 4);
@@ -1050,7 +1169,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(2);
     {
         MomArgsF a{};
-        a.U = d.Uf; a.V = d.Vf; a.W = d.Wf; a.P = d.P; a.C = d.Cf; a.fpet = d.fpetf;
+        a.U = d.Uf; a.V = d.Vf; a.W = d.Wf; a.Ph = d.Pf; a.Pl = d.Pl; a.C = d.Cf; a.fpet = d.fpetf;
         for (int c = 0; c < 3; ++c) { a.A0[c] = d.A0f[c]; a.T0[c] = d.T0f[c]; a.F[c] = d.Ff[c]; a.Q[c] = d.Qf[c]; }
         a.cs = d.cs; a.polymer = o.polymer; a.ab2_first = o.ab2_first;
         a.coef_t = (float)((1.0 - d.ph.beta) / (d.ph.re * d.ph.wi));
@@ -1064,7 +1183,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     if (o.ibm) {
         IbmArgsF a{};
         a.mu = d.mu; a.mv = d.mv; a.mcyl = d.mcyl; a.nm = d.nm;
-        const double *Us[3] = {d.U, d.V, d.W};
+        const float *Uh[3] = {d.Uf, d.Vf, d.Wf}, *Ul[3] = {d.Ul, d.Vl, d.Wl};
         // z weights of the stencil offset k - n = -1, 0, 1 (marker plane at
         // (n - 1/4) dZ; u, v at (k - 1/2) dZ, w at k dZ)
         auto roma = [](double r) {
@@ -1075,8 +1194,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         };
         for (int c = 0; c < 3; ++c) {
             a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
-            a.Uc[c] = Us[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c]; a.idx[c] = d.csr_idx[c];
-            a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
+            a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
+            a.idx[c] = d.csr_idx[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
             for (int dk = 0; dk < 3; ++dk) {
                 double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
                 a.wz[c][dk] = (float)roma(zg);
@@ -1090,45 +1209,52 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         if ((e = cudaGetLastError())) return e;
     }
     mark(4);
-    // Helmholtz solves for the increments; U* = U^n + dU in FP64
+    // Helmholtz solves for the FP32 increments dU (U* = U^n + dU)
     const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
-    double *outs[3] = {d.Up, d.Vp, d.Wp};
-    const double *bases[3] = {d.U, d.V, d.W};
     for (int c = 0; c < 3; ++c) {
-        if (!g.walls) e = solve_periodic_f<float>(d, d.Qf[c], outs[c], bases[c], 1.0, lhs1, s);
-        else e = solve_walls_f<float>(d, d.Qf[c], outs[c], bases[c], c == 1 ? SYS_V : SYS_U, s);
+        const XOutF out{d.dUf[c], nullptr, 0};
+        if (!g.walls) e = solve_periodic_f(d, d.Qf[c], out, 1.0, lhs1, s);
+        else e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
         if (e) return e;
     }
-    F8_CUDA_RET(bc_field(d.Up, g, BC_U, s));
-    F8_CUDA_RET(bc_field(d.Vp, g, BC_V, s));
-    F8_CUDA_RET(bc_field(d.Wp, g, BC_W, s));
+    {
+        BcSet b{};   // homogeneous boundary values of the increments
+        for (int c = 0; c < 3; ++c) { b.hi[c] = d.dUf[c]; b.lo[c] = nullptr; b.kind[c] = BC_U + c; }
+        b.n = 3;
+        F8_CUDA_RET(launch_bc_set(b, g, s));
+    }
     mark(5);
-    // Poisson: FP32 solve + FP64 defect correction
+    // Poisson: FP32 solve + one df64 defect correction
+    BcSet bphi{};
+    bphi.hi[0] = d.Phif; bphi.lo[0] = d.Phil; bphi.kind[0] = BC_P; bphi.n = 1;
     {
         dim3 blk(32, 8);
-        k_poisson_rhs_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, d.Rp, g, mc); count_launch();
+        k_poisson_rhs_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
+        count_launch();
     }
-    if (!g.walls) e = solve_periodic_f<double>(d, d.Rp, d.Phi, nullptr, 0.0, -1.0, s);
-    else e = solve_walls_f<double>(d, d.Rp, d.Phi, nullptr, SYS_P, s);
-    if (e) return e;
-    F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
+    {
+        const XOutF out{d.Phif, d.Phil, 1};
+        if (!g.walls) e = solve_periodic_f(d, d.Rhf, out, 0.0, -1.0, s);
+        else e = solve_walls_f(d, d.Rhf, out, SYS_P, s);
+        if (e) return e;
+    }
+    F8_CUDA_RET(launch_bc_set(bphi, g, s));
     for (int it = 0; it < d.defect_iters; ++it) {
         dim3 blk(32, 8);
-        k_defect<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Phi, d.Rp, d.Rd, g, mc); count_launch();
-        if (!g.walls) e = solve_periodic_f<double>(d, d.Rd, d.Phi, d.Phi, 0.0, -1.0, s);
-        else e = solve_walls_f<double>(d, d.Rd, d.Phi, d.Phi, SYS_P, s);
+        k_defect_df<<<cell_grid_m(g, blk), blk, 0, s>>>(Phi, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
+        const XOutF out{d.Phif, d.Phil, 2};
+        if (!g.walls) e = solve_periodic_f(d, d.Rdf, out, 0.0, -1.0, s);
+        else e = solve_walls_f(d, d.Rdf, out, SYS_P, s);
         if (e) return e;
-        F8_CUDA_RET(bc_field(d.Phi, g, BC_P, s));
+        F8_CUDA_RET(launch_bc_set(bphi, g, s));
     }
     mark(6);
     {
         dim3 blk(32, 8);
-        k_march_m<<<cell_grid_m(g, blk), blk, 0, s>>>(d.U, d.V, d.W, d.P, d.Up, d.Vp, d.Wp, d.Phi, d.Uf, d.Vf, d.Wf, g, mc); count_launch();
+        k_march_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc);
+        count_launch();
     }
-    {
-        long n = halo_count_m(g) + (g.walls ? (long)g.nx * g.nz : 0);
-        k_bc_vel_m<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.U, d.V, d.W, d.P, d.Uf, d.Vf, d.Wf, g); count_launch();
-    }
+    F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
     mark(7);
     return cudaGetLastError();
 }
