@@ -659,19 +659,20 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst
 // ---------------------------------------------------------------------------
 // IBM (fenep_mpi.f90:1794-1929).  Ua = U + dt R at the stencil points with the
 // boundary values that the reference gives Ua (PBM / wall rules).
-__device__ inline double ua_at(const Geo &g, const float *Uh, const float *Ul, const float *Qc, int comp, int i, int j,
-                               int k) {
+// Ua in df64 (the velocity pair plus the FP32 increment)
+__device__ inline df ua_at(const Geo &g, const float *Uh, const float *Ul, const float *Qc, int comp, int i, int j,
+                           int k, df uw2) {
     const int ii = wrapx(g, i), kk = wrapz(g, k);
-    auto u = [&](int q) { return (double)Uh[q] + (double)Ul[q]; };
+    auto u = [&](int q) { return df{Uh[q], Ul[q]}; };
     if (j >= 1 && j <= g.ny) {
-        if (g.walls && comp == 1 && j == g.ny) return 0.0;
-        return u(hix(g, i, j, k)) + (double)Qc[qix(g, ii, j, kk)];
+        if (g.walls && comp == 1 && j == g.ny) return df{0.0f, 0.0f};
+        return df_add_f(u(hix(g, i, j, k)), Qc[qix(g, ii, j, kk)]);
     }
-    if (!g.walls) return u(hix(g, i, j, k)) + (double)Qc[qix(g, ii, wrapy(g, j), kk)];
-    if (comp == 1) return 0.0;
+    if (!g.walls) return df_add_f(u(hix(g, i, j, k)), Qc[qix(g, ii, wrapy(g, j), kk)]);
+    if (comp == 1) return df{0.0f, 0.0f};
     const int jj = j == 0 ? 1 : g.ny;
-    const double inner = u(hix(g, ii, jj, kk)) + (double)Qc[qix(g, ii, jj, kk)];
-    return (comp == 0 && j != 0) ? 2 * g.uwall - inner : -inner;
+    const df inner = df_add_f(u(hix(g, ii, jj, kk)), Qc[qix(g, ii, jj, kk)]);
+    return (comp == 0 && j != 0) ? df_sub(uw2, inner) : df_neg(inner);
 }
 
 struct IbmArgsF {
@@ -688,6 +689,9 @@ struct IbmArgsF {
     const int *act[3];
     int nact[3];
     float *Q[3];
+    df uw2;                          // 2 * upper wall speed
+    double idt;                      // 1 / dt
+    float dtf;                       // dt
 };
 
 __global__ void k_ibm_interp_f(IbmArgsF a, Geo g) {
@@ -697,31 +701,32 @@ __global__ void k_ibm_interp_f(IbmArgsF a, Geo g) {
     if (m >= a.nm) return;
     const int i0 = a.i0[comp][m], j0 = a.j0[comp][m];
     const float *wx = a.wx[comp] + 3 * m, *wy = a.wy[comp] + 3 * m;
-    double ub = 0.0;
+    df ub{0.0f, 0.0f};
     for (int dk = 0; dk < 3; ++dk) {
         const int k = n - 1 + dk;
         for (int dj = 0; dj < 3; ++dj)
             for (int di = 0; di < 3; ++di) {
-                const double w = (double)(wx[di] * wy[dj] * a.wz[comp][dk]);
-                ub += ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k) * w;
+                const float w = wx[di] * wy[dj] * a.wz[comp][dk];
+                ub = df_add(ub, df_mul_f(ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2), w));
             }
     }
     const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
-    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ub) / g.dt;
+    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ((double)ub.hi + (double)ub.lo)) * a.idt;
 }
 
-__device__ inline double spread_at_f(const IbmArgsF &a, const Geo &g, int comp, int ie, int je, int ke) {
+// the spread force enters Q = dt (R + f), an FP32 field, so it is summed in FP32
+__device__ inline float spread_at_f(const IbmArgsF &a, const Geo &g, int comp, int ie, int je, int ke) {
     const int col = ie + g.sx * je;
     const int b = a.off[comp][col], e = a.off[comp][col + 1];
-    if (b == e) return 0.0;
-    double acc = 0.0;
+    if (b == e) return 0.0f;
+    float acc = 0.0f;
     const int nlo = max(ke - 1, 1), nhi = min(ke + 1, g.nz);
     for (int n = nlo; n <= nhi; ++n) {
         const float wz = a.wz[comp][ke - n + 1];
         for (int q = b; q < e; ++q) {
             const int m = a.idx[comp][q];
             const float w = a.wx[comp][3 * m + (ie - a.i0[comp][m])] * a.wy[comp][3 * m + (je - a.j0[comp][m])] * wz;
-            acc += a.Fc[comp][m + (size_t)a.nm * (n - 1)] * (double)w;
+            acc = fmaf((float)a.Fc[comp][m + (size_t)a.nm * (n - 1)], w, acc);
         }
     }
     return acc;
@@ -740,7 +745,7 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
     if (i == 1) xs[1] = g.nx + 1; else if (i == g.nx) xs[1] = 0;
     if (!g.walls) { if (j == 1) ys[1] = g.ny + 1; else if (j == g.ny) ys[1] = 0; }
     if (k == 1) zs[1] = g.nz + 1; else if (k == g.nz) zs[1] = 0;
-    double f = 0.0;
+    float f = 0.0f;
     for (int zz = 0; zz < 2; ++zz) {
         if (zs[zz] < 0) continue;
         for (int yy = 0; yy < 2; ++yy) {
@@ -752,13 +757,11 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
         }
     }
     const int o = qix(g, i, j, k);
-    a.Q[comp][o] = (float)((double)a.Q[comp][o] + g.dt * f);
+    a.Q[comp][o] = fmaf(a.dtf, f, a.Q[comp][o]);
 }
 
 // ---------------------------------------------------------------------------
-// FP64 parts of the pressure solve and the projection, with reciprocal
-// multiplies instead of divisions.
-//   rhs = div(U*) / dt (fenep.f90:1547-1555)
+// Pressure solve and projection on the df64 state.
 // The df64 state of one field
 struct DfF {
     float *hi, *lo;
@@ -1201,6 +1204,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
                 a.wz[c][dk] = (float)roma(zg);
             }
         }
+        a.uw2 = df_from_d(2.0 * g.uwall);
+        a.idt = 1.0 / g.dt;
+        a.dtf = (float)g.dt;
         dim3 gi((d.nm + 127) / 128, g.nz, 3);
         k_ibm_interp_f<<<gi, 128, 0, s>>>(a, g); count_launch();
         int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
