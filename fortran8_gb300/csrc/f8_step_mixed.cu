@@ -209,74 +209,73 @@ __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
 }
 
 // ---------------------------------------------------------------------------
-// Polymer (3D).  Eigen test: the smallest eigenvalue of the symmetric 3x3
-// candidate in the shifted (traceless) trigonometric form, which is the same
-// root as the reference's Vieta formula (fenep.f90:425-444) but free of the
-// cancellation in p = a1 - a2^2/3 that FP32 would suffer near C = I.  Equal
-// roots (discriminant q^2 - p^3 >= 0) return the reference's -100 sentinel.
+// Polymer (3D).  Eigen test: the smallest eigenvalue of each symmetric 3x3
+// candidate face in the shifted (traceless) trigonometric form, which is the
+// same root as the reference's Vieta formula (fenep.f90:425-444) but free of
+// the cancellation in p = a1 - a2^2/3 that FP32 would suffer near C = I.
+// Equal roots (discriminant q^2 - p^3 >= 0) give the reference's -100
+// sentinel.  The two faces of candidate l (fenep.f90:179-184) are c0 - v and
+// c0 + v with v = dp/2, dm/2, (dm + dp)/4 for l = 1, 2, 3 (dm = c0 - c_{-1},
+// dp = c_{+1} - c0), so they share the mean and deviatoric part of c0 and are
+// evaluated as one packed FP32x2 pair.
 // arccos by Abramowitz & Stegun 4.4.46: acos(x) = sqrt(1-x) * P7(x) on [0, 1]
 // with |error| <= 2e-8, and acos(-x) = pi - acos(x).
-__device__ inline float acos_as(float x) {
-    const float ax = fabsf(x);
-    float p = -0.0012624911f;
-    p = fmaf(p, ax, 0.0066700901f);
-    p = fmaf(p, ax, -0.0170881256f);
-    p = fmaf(p, ax, 0.0308918810f);
-    p = fmaf(p, ax, -0.0501743046f);
-    p = fmaf(p, ax, 0.0889789874f);
-    p = fmaf(p, ax, -0.2145988016f);
-    p = fmaf(p, ax, 1.5707963050f);
-    const float r = sqrtf(1.0f - ax) * p;
-    return x < 0.0f ? 3.14159265358979f - r : r;
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fms2(float2 a, float2 b, float2 c) {   // a * b - c
+    return __ffma2_rn(a, b, make_float2(-c.x, -c.y));
 }
 
-__device__ inline float eigmin_f(const float *a) {
-    const float m = (a[0] + a[3] + a[5]) * (1.0f / 3.0f);
-    const float b0 = a[0] - m, b1 = a[3] - m, b2 = a[5] - m;
-    const float p2 = (b0 * b0 + b1 * b1 + b2 * b2 + 2.0f * (a[1] * a[1] + a[2] * a[2] + a[4] * a[4])) * (1.0f / 6.0f);
-    const float q = 0.5f * (b0 * (b1 * b2 - a[4] * a[4]) - a[1] * (a[1] * b2 - a[4] * a[2]) + a[2] * (a[1] * a[4] - b1 * a[2]));
-    const float p3 = p2 * p2 * p2;
-    if (q * q >= p3) return -100.0f;
-    const float sp = sqrtf(p2);
-    const float r = fminf(1.0f, fmaxf(-1.0f, q * __frcp_rn(p2 * sp)));
-    // the angle lies in [2 pi/3, pi], where the hardware cosine is accurate
-    return m + 2.0f * sp * __cosf(acos_as(r) * (1.0f / 3.0f) + TWO_PI_3F);
+__device__ __forceinline__ float2 acos_as2(float2 x) {
+    const float2 ax = make_float2(fabsf(x.x), fabsf(x.y));
+    float2 p = f2(-0.0012624911f);
+    p = fma2(p, ax, f2(0.0066700901f));
+    p = fma2(p, ax, f2(-0.0170881256f));
+    p = fma2(p, ax, f2(0.0308918810f));
+    p = fma2(p, ax, f2(-0.0501743046f));
+    p = fma2(p, ax, f2(0.0889789874f));
+    p = fma2(p, ax, f2(-0.2145988016f));
+    p = fma2(p, ax, f2(1.5707963050f));
+    const float2 t = add2(f2(1.0f), make_float2(-ax.x, -ax.y));
+    // sqrt(1 - |x|) as t * rsqrt(t), 0 at |x| = 1
+    const float2 st = make_float2(t.x > 0.0f ? t.x * rsqrtf(t.x) : 0.0f, t.y > 0.0f ? t.y * rsqrtf(t.y) : 0.0f);
+    const float2 r = mul2(st, p);
+    return make_float2(x.x < 0.0f ? 3.14159265358979f - r.x : r.x, x.y < 0.0f ? 3.14159265358979f - r.y : r.y);
+}
+
+// smallest eigenvalues of the pair of symmetric matrices m + B (B traceless,
+// components b00 b11 b22 b01 b02 b12 as FP32x2 pairs)
+__device__ __forceinline__ float2 lam_min2(float2 m, float2 b00, float2 b11, float2 b22, float2 b01, float2 b02,
+                                           float2 b12) {
+    float2 sd = mul2(b00, b00);
+    sd = fma2(b11, b11, sd);
+    sd = fma2(b22, b22, sd);
+    float2 so = mul2(b01, b01);
+    so = fma2(b02, b02, so);
+    so = fma2(b12, b12, so);
+    const float2 p2 = mul2(fma2(so, f2(2.0f), sd), f2(1.0f / 6.0f));
+    // q = det(B) / 2 by cofactors of the first row
+    const float2 a00 = fms2(b11, b22, mul2(b12, b12));
+    const float2 a01 = fms2(b01, b22, mul2(b12, b02));
+    const float2 a02 = fms2(b01, b12, mul2(b11, b02));
+    const float2 q = mul2(fma2(b02, a02, fms2(b00, a00, mul2(b01, a01))), f2(0.5f));
+    const float2 p3 = mul2(mul2(p2, p2), p2);
+    const float2 qq = mul2(q, q);
+    const float2 rs = make_float2(rsqrtf(p2.x), rsqrtf(p2.y));
+    float2 r = mul2(mul2(q, rs), mul2(rs, rs));
+    r = make_float2(fminf(1.0f, fmaxf(-1.0f, r.x)), fminf(1.0f, fmaxf(-1.0f, r.y)));
+    const float2 ang = fma2(acos_as2(r), f2(1.0f / 3.0f), f2(TWO_PI_3F));
+    const float2 cs = make_float2(__cosf(ang.x), __cosf(ang.y));
+    const float2 lam = fma2(mul2(f2(2.0f), mul2(p2, rs)), cs, m);
+    return make_float2(qq.x >= p3.x ? -100.0f : lam.x, qq.y >= p3.y ? -100.0f : lam.y);
 }
 
 // candidate faces (fenep.f90:179-184) as weights of (C_{m-1}, C_m, C_{m+1});
-// index 4 is the cell value
+// index 4 is the cell value (the Cstar stencil coefficients below)
 __constant__ float c_fp_w[5][3] = {{0, 1, 0}, {0, 1.5f, -0.5f}, {0.5f, 0.5f, 0}, {0.25f, 1, -0.25f}, {0, 1, 0}};
 __constant__ float c_fn_w[5][3] = {{0, 1, 0}, {0, 0.5f, 0.5f}, {-0.5f, 1.5f, 0}, {-0.25f, 1, 0.25f}, {0, 1, 0}};
-
-__device__ inline float face_pf(int idx, float cm, float c0, float cp) {
-    return c_fp_w[idx][0] * cm + c_fp_w[idx][1] * c0 + c_fp_w[idx][2] * cp;
-}
-__device__ inline float face_nf(int idx, float cm, float c0, float cp) {
-    return c_fn_w[idx][0] * cm + c_fn_w[idx][1] * c0 + c_fn_w[idx][2] * cp;
-}
-
-__device__ inline int select3f(const float *cm, const float *c0, const float *cp) {
-    float best = 0.0f;
-    int idx = 4;
-    bool found = false;
-    float ml[3];
-    for (int l = 1; l <= 3; ++l) {
-        float pt[6], nt[6];
-        for (int m = 0; m < 6; ++m) {
-            pt[m] = face_pf(l, cm[m], c0[m], cp[m]);
-            nt[m] = face_nf(l, cm[m], c0[m], cp[m]);
-        }
-        float a = eigmin_f(pt), b = eigmin_f(nt);
-        ml[l - 1] = isnan(a) ? b : (isnan(b) ? a : fminf(a, b));
-    }
-    // maxloc over (ml1, ml2, ml3, 0): first maximum, NaN ignored
-    for (int l = 0; l < 3; ++l) {
-        if (isnan(ml[l])) continue;
-        if (!found || ml[l] > best) { best = ml[l]; idx = l + 1; found = true; }
-    }
-    if (!found || 0.0f > best) idx = 4;
-    return idx;
-}
 
 __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs,
                                                   int *__restrict__ fixcnt) {
@@ -286,16 +285,47 @@ __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, u
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
     const int h = hix(g, i, j, k);
-    float c0[6], cm[6], cp[6];
+    float c0[6];
+#pragma unroll
     for (int m = 0; m < 6; ++m) c0[m] = C[(size_t)m * cs + h];
-    const int off[3] = {1, g.sx, g.sx * g.sy};
+    const float m0 = (c0[0] + c0[3] + c0[5]) * (1.0f / 3.0f);
+    const float e00 = c0[0] - m0, e11 = c0[3] - m0, e22 = c0[5] - m0;
     int code = 0;
+#pragma unroll 1
     for (int d = 0; d < 3; ++d) {
+        const int od = d == 0 ? 1 : (d == 1 ? g.sx : g.sx * g.sy);
+        float dm[6], dp[6];
+#pragma unroll
         for (int m = 0; m < 6; ++m) {
-            cm[m] = C[(size_t)m * cs + h - off[d]];
-            cp[m] = C[(size_t)m * cs + h + off[d]];
+            dm[m] = c0[m] - C[(size_t)m * cs + h - od];
+            dp[m] = C[(size_t)m * cs + h + od] - c0[m];
         }
-        code |= (select3f(cm, c0, cp) - 1) << (2 * d);
+        float ml[3];
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            float v[6];
+#pragma unroll
+            for (int m = 0; m < 6; ++m) v[m] = l == 0 ? 0.5f * dp[m] : (l == 1 ? 0.5f * dm[m] : 0.25f * (dm[m] + dp[m]));
+            const float mv = (v[0] + v[3] + v[5]) * (1.0f / 3.0f);
+            // lane x: c0 - v (the face on the minus side), lane y: c0 + v
+            const float2 pm = make_float2(-1.0f, 1.0f);
+            const float2 lam = lam_min2(fma2(f2(mv), pm, f2(m0)), fma2(f2(v[0] - mv), pm, f2(e00)),
+                                        fma2(f2(v[3] - mv), pm, f2(e11)), fma2(f2(v[5] - mv), pm, f2(e22)),
+                                        fma2(f2(v[1]), pm, f2(c0[1])), fma2(f2(v[2]), pm, f2(c0[2])),
+                                        fma2(f2(v[4]), pm, f2(c0[4])));
+            ml[l] = fminf(lam.x, lam.y);   // NaN-ignoring minimum
+        }
+        // maxloc over (ml1, ml2, ml3, 0): first maximum, NaN ignored
+        float best = 0.0f;
+        int idx = 4;
+        bool found = false;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            if (isnan(ml[l])) continue;
+            if (!found || ml[l] > best) { best = ml[l]; idx = l + 1; found = true; }
+        }
+        if (!found || 0.0f > best) idx = 4;
+        code |= (idx - 1) << (2 * d);
     }
     codes[qix(g, i, j, k)] = (uint8_t)code;
 }
