@@ -292,7 +292,8 @@ int setup(f8_ctx *c) {
         int dev = 0, optin = 0;
         API_CUDA(c, cudaGetDevice(&dev));
         API_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        const size_t need = g.walls ? (size_t)12 * ((g.ny + 2) | 1) * g.nz : (size_t)8 * (g.ny + 1) * g.nz;
+        const size_t need = g.walls ? std::max((size_t)12 * ((g.ny + 2) | 1) * g.nz, wall_plane_smem(g.ny, g.nz))
+                                    : (size_t)8 * (g.ny + 1) * g.nz;
         d.fused_planes = need <= (size_t)optin ? 1 : 0;
         {
             std::vector<float2> t2(std::max(1, g.nz / 2));
@@ -318,7 +319,7 @@ int setup(f8_ctx *c) {
             const int lj = g.ny + 2;
             const size_t nt = nxh * (size_t)g.nz * lj;
             const double kap = c->phys.dt * c->phys.beta / c->phys.re / 2.0, idy2 = 1.0 / (g.dy * g.dy);
-            std::vector<float> tp(nt), tr(nt);
+            std::vector<float> tr(nt);
             for (int sys = 0; sys < 3; ++sys) {
                 for (size_t kx = 0; kx < nxh; ++kx)
                     for (int kz = 0; kz < g.nz; ++kz) {
@@ -342,13 +343,10 @@ int setup(f8_ctx *c) {
                             double rd;
                             if (std::fabs(den) < 1.0e-16) { p = 0.0; rd = 0.0; }
                             else { p = -b / den; rd = 1.0 / den; }
-                            const size_t o = (kx * g.nz + kz) * (size_t)lj + j;
-                            tp[o] = (float)p;
-                            tr[o] = (float)rd;
+                            tr[(kx * g.nz + kz) * (size_t)lj + j] = (float)rd;
                         }
                     }
-                std::vector<double> tpd(tp.begin(), tp.end()), trd(tr.begin(), tr.end());
-                if (int st = upload_f(c, &d.wtP[sys], tpd)) return st;
+                std::vector<double> trd(tr.begin(), tr.end());
                 if (int st = upload_f(c, &d.wtR[sys], trd)) return st;
             }
         }

@@ -48,6 +48,17 @@ inline std::atomic<long long> g_kernel_launches{0};
 inline void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // Per-step device counters (status words read by the host after a step).
+// Shared memory of the scan-Thomas wall plane kernel: the (z, y) plane of one
+// kx (complex, odd row stride), the 1/den table of its systems with a row
+// stride >= lj and = 8 (mod 32) (the 4 systems x 8 chunks of a warp then read
+// 32 distinct banks), and the z twiddles.
+__host__ __device__ inline int wall_rd_stride(int lj) { return lj + (((8 - lj) % 32) + 32) % 32; }
+
+__host__ __device__ inline size_t wall_plane_smem(int ny, int nz) {
+    const int lj = ny + 2;
+    return (size_t)8 * (lj | 1) * nz + (size_t)4 * wall_rd_stride(lj) * nz + (size_t)(nz / 2) * 8;
+}
+
 struct StepCounters {
     unsigned long long newton_iters;
     unsigned long long newton_unconverged;

@@ -379,14 +379,15 @@ __device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) 
     }
 }
 
-// Pivot tables of the y systems of one solve type: for each (kx, kz) the
-// Thomas coefficients P_j and 1/den_j (0 where the pivot vanishes, the
-// reference's guard), computed on the host in FP64.
+// Pivot table of the y systems of one solve type: for each (kx, kz) the
+// Thomas factors 1/den_j (0 where the pivot vanishes, the reference's guard),
+// computed on the host in FP64.  The back-substitution multipliers are
+// P_j = -b_j / den_j with b_j the super-diagonal of row j.
 struct WallTables {
-    const float *P;      // [kx][kz][j]
     const float *rden;   // [kx][kz][j]
     float bc;            // interior off-diagonal b = c
     float c_last;        // c of the last row (1 U, -1 P); V: rows >= ny are identities
+    float b_first;       // b of row 0 (1 U, -1 P, 0 V)
     float nxz_inv;
     int sys;
 };
@@ -509,11 +510,13 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
 // (kx, kz) system.  Both sweeps are first-order affine recurrences,
 //   forward   q_j = alpha_j q_{j-1} + beta_j,  alpha_j = -c_j / den_j,
 //                                              beta_j  = d_j / den_j,
-//   backward  x_j = P_j x_{j+1} + q_j,
+//   backward  x_j = P_j x_{j+1} + q_j,          P_j = -b_j / den_j,
 // so each thread composes the maps of its chunk of rows, the T threads scan
 // the composed maps with shuffles, and each thread then replays its chunk
 // from its incoming value.  The coefficients are those of the sequential
-// Thomas solve of k_plane_walls (tdma, fenep_2d.f90:1145-1177), tabulated.
+// Thomas solve of k_plane_walls (tdma, fenep_2d.f90:1145-1177); the 1/den
+// table of this kx is staged in shared memory, its rows in the bit-reversed
+// kz order of the spectrum rows.
 template <int V>
 __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, const float2 *twz, WallTables wt) {
     constexpr int NZ = 32 * V;
@@ -522,15 +525,19 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
     extern __shared__ unsigned char smem_raw[];
     const int lj = ny + 2;
     const int ljs = lj | 1;
+    const int rs = wall_rd_stride(lj);
     float2 *P = reinterpret_cast<float2 *>(smem_raw);                // [k][j]
-    float2 *tws = P + (size_t)ljs * NZ;                              // NZ/2 twiddles
+    float *Rs = reinterpret_cast<float *>(P + (size_t)ljs * NZ);     // [row][j], row = bitrev(kz)
+    float2 *tws = reinterpret_cast<float2 *>(Rs + (size_t)rs * NZ);  // NZ/2 twiddles
     const int kx = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     float2 *Sp = S + (size_t)kx * NZ * lj;
+    const float *Rg = wt.rden + (size_t)kx * NZ * lj;
     for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
     for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
         const int k = q / lj, j = q % lj;
         P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+        Rs[(size_t)(__brev((unsigned)k) >> (32 - LG)) * rs + j] = Rg[q];
     }
     __syncthreads();
     for (int j = 1 + warp; j <= ny; j += nwarp) {
@@ -543,11 +550,9 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
     }
     __syncthreads();
     {
-        const int kz = threadIdx.x / T, t = threadIdx.x % T;
-        const int row = (int)(__brev((unsigned)kz) >> (32 - LG));
+        const int row = threadIdx.x / T, t = threadIdx.x % T;
         float2 *x = P + (size_t)row * ljs;
-        const float *Pt = wt.P + ((size_t)kx * NZ + kz) * lj;
-        const float *Rt = wt.rden + ((size_t)kx * NZ + kz) * lj;
+        const float *rd = Rs + (size_t)row * rs;
         const int L = (lj + T - 1) / T;
         const int j0 = min(lj, t * L), j1 = min(lj, j0 + L);
         const bool sysv = wt.sys == SYS_V;
@@ -557,9 +562,9 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
         for (int j = j0; j < j1; ++j) {
             const bool ident = sysv ? (j >= ny) : (j == lj - 1);
             const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
-            const float rd = j == 0 ? 0.0f : Rt[j];
-            float2 d = ident ? make_float2(0.f, 0.f) : x[j];
-            const float al = -c * rd, dr = wt.nxz_inv * rd;
+            const float r = j == 0 ? 0.0f : rd[j];
+            const float2 d = ident ? make_float2(0.f, 0.f) : x[j];
+            const float al = -c * r, dr = wt.nxz_inv * r;
             B = make_float2(fmaf(al, B.x, d.x * dr), fmaf(al, B.y, d.y * dr));
             A *= al;
         }
@@ -576,17 +581,22 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
         for (int j = j0; j < j1; ++j) {
             const bool ident = sysv ? (j >= ny) : (j == lj - 1);
             const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
-            const float rd = j == 0 ? 0.0f : Rt[j];
-            float2 d = ident ? make_float2(0.f, 0.f) : x[j];
-            const float al = -c * rd, dr = wt.nxz_inv * rd;
+            const float r = j == 0 ? 0.0f : rd[j];
+            const float2 d = ident ? make_float2(0.f, 0.f) : x[j];
+            const float al = -c * r, dr = wt.nxz_inv * r;
             q = make_float2(fmaf(al, q.x, d.x * dr), fmaf(al, q.y, d.y * dr));
             x[j] = q;
         }
-        // backward: x_j = P_j x_{j+1} + q_j (P of the last row is 0)
+        // backward: x_j = P_j x_{j+1} + q_j (b and so P of the last row are 0)
+        auto pmul = [&](int j) {
+            const bool zero_b = (j == lj - 1) || (sysv && j >= ny);
+            const float b = j == 0 ? wt.b_first : (zero_b ? 0.0f : wt.bc);
+            return -b * rd[j];
+        };
         A = 1.0f;
         B = make_float2(0.f, 0.f);
         for (int j = j1 - 1; j >= j0; --j) {
-            const float pj = Pt[j];
+            const float pj = pmul(j);
             const float2 qj = x[j];
             B = make_float2(fmaf(pj, B.x, qj.x), fmaf(pj, B.y, qj.y));
             A *= pj;
@@ -602,7 +612,7 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
         xv.y = __shfl_down_sync(0xffffffffu, B.y, 1, T);
         if (t == T - 1) xv = make_float2(0.f, 0.f);
         for (int j = j1 - 1; j >= j0; --j) {
-            const float pj = Pt[j];
+            const float pj = pmul(j);
             const float2 qj = x[j];
             xv = make_float2(fmaf(pj, xv.x, qj.x), fmaf(pj, xv.y, qj.y));
             x[j] = xv;

@@ -54,7 +54,7 @@ struct Dev {
     int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory
     float2 *twz2;                          // (cos, -sin)(2 pi p/NZ), p < NZ/2
     float2 *twx2;                          // (cos, -sin)(2 pi p/NX), p < NX/2
-    float *wtP[3], *wtR[3];                // Thomas pivot tables of the U, V, P wall systems
+    float *wtR[3];                         // Thomas 1/den tables of the U, V, P wall systems
     float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
     int *mi0[3], *mj0[3];                  // per-marker stencil origins
     int *act_cols[3];                      // interior (i,j) columns that receive spreading

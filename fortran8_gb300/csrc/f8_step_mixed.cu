@@ -44,6 +44,8 @@ struct MixConst {
     df idt;                                // 1/dt
     float pcf;                             // dt beta / (2 Re)
     float dtwi, lp2f, epsf;                // dt/Wi, L^2, Newton tolerance (FP32)
+    float eps2f;                           // Newton tolerance squared
+    float cpet;                            // (dt/Wi) (L^2 - 3), the scale of f'(tr C)
 };
 
 MixConst make_const(const Geo &g, const Phys &ph) {
@@ -65,6 +67,8 @@ MixConst make_const(const Geo &g, const Phys &ph) {
     c.dtwi = (float)(ph.dt / ph.wi);
     c.lp2f = (float)ph.lp2;
     c.epsf = (float)ph.newton_eps;
+    c.eps2f = (float)(ph.newton_eps * ph.newton_eps);
+    c.cpet = (float)(ph.dt / ph.wi * (ph.lp2 - 3.0));
     return c;
 }
 
@@ -363,18 +367,30 @@ __device__ inline bool step_small(const float (&x)[6], float sr, float epsf) {
     return !(sqrtf(sr / sx) >= epsf);
 }
 
-// returns the iterations taken; > maxit when not converged
-__device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Lyap9 &A, float dtwi, float lp2f,
-                                    double lp2, float epsf, int maxit) {
+// The relative step test of fenep.f90:575, |dx| / |x| < eps, without the
+// square root: leaves when |dx|^2 <= eps^2 |x|^2 or on NaN
+__device__ inline bool step_small_sq(const float (&x)[6], float sr, float eps2) {
+    float sx = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) sx = fmaf(x[m], x[m], sx);
+    return !(sr > eps2 * sx);
+}
+
+// returns the iterations taken; > maxit when not converged.  The reciprocals
+// are hardware approximations (2 ulp): the iteration corrects them, and the
+// converged root satisfies the residual built with them.
+__device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Lyap9 &A, const MixConst &mc,
+                                    double lp2, int maxit) {
+    const float dtwi = mc.dtwi, lp2f = mc.lp2f;
     int itr;
 #pragma unroll 1
     for (itr = 1; itr <= maxit; ++itr) {
-        const float f = peterlin_f(x[0], x[3], x[5], lp2f, lp2);
-        const float a = 1.0f + f * dtwi;
-        const float ia = 1.0f / a;
         const float tr = x[0] + x[3] + x[5];
         const float den = lp2f - tr;
-        const float cc = dtwi * (lp2f - 3.0f) / (den * den);
+        const float f = den > 0.01f * lp2f ? __fdividef(lp2f - 3.0f, den) : peterlin_f(x[0], x[3], x[5], lp2f, lp2);
+        const float a = fmaf(f, dtwi, 1.0f);
+        const float ia = __fdividef(1.0f, a);
+        const float cc = __fdividef(mc.cpet, den * den);
         float r[6], y[6], t[6];
         lyap_M(A, x, r);
 #pragma unroll
@@ -385,7 +401,7 @@ __device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Ly
 #pragma unroll
             for (int m = 0; m < 6; ++m) y[m] = fmaf(-ia, t[m], r[m]);
         }
-        const float g = cc * (y[0] + y[3] + y[5]) / (1.0f + cc * tr * ia) * ia;
+        const float g = __fdividef(cc * (y[0] + y[3] + y[5]), fmaf(cc * tr, ia, 1.0f)) * ia;
         float sr = 0.0f;
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
@@ -393,7 +409,7 @@ __device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Ly
             x[m] -= d;
             sr = fmaf(d, d, sr);
         }
-        if (step_small(x, sr, epsf)) break;
+        if (step_small_sq(x, sr, mc.eps2f)) break;
     }
     return itr;
 }
@@ -482,7 +498,7 @@ __device__ inline void dir_coef(float s_pm, float s_pp, float s_nm, float s_np, 
     kp2 = gp ? 0.0f : s_pp * c_fp_w[cp][2];
 }
 
-__global__ void __launch_bounds__(128, 6) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
+__global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
                                                    float *__restrict__ fpet, const uint8_t *__restrict__ codes,
                                                    const float *__restrict__ U, const float *__restrict__ V,
                                                    const float *__restrict__ W, Geo g, Phys ph, MixConst mc, int cs,
@@ -548,7 +564,7 @@ __global__ void __launch_bounds__(128, 6) k_update3_f(const float *__restrict__ 
         }
         const Lyap9 A = vel_grad_f(U, V, W, h, ox, oy, oz, mc);
         const int fast_max = min(NEWTON_FAST_MAX, ph.newton_itrmax);
-        const int itr = newton_fast_f(x, b, A, dtwi, mc.lp2f, ph.lp2, mc.epsf, fast_max);
+        const int itr = newton_fast_f(x, b, A, mc, ph.lp2, fast_max);
         if (itr <= fast_max || fast_max == ph.newton_itrmax) {
             my_itr = (unsigned long long)itr;
             my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
@@ -1047,10 +1063,11 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStr
     if (sys == SYS_P) { ps.ai_base = (float)(2.0 * idy2); ps.bc = (float)idy2; ps.kap = -1.0f; }
     else { ps.ai_base = (float)(1.0 + kap * 2.0 * idy2); ps.bc = (float)(-kap * idy2); ps.kap = (float)kap; }
     const size_t smp = (size_t)12 * (lj | 1) * nz;
-    if (d.wtP[0] && (nz == 32 || nz == 64 || nz == 128)) {
+    if (d.wtR[0] && (nz == 32 || nz == 64 || nz == 128)) {
         const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
-        WallTables wt{d.wtP[t], d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, ps.nxz_inv, sys};
-        const size_t sms = (size_t)8 * (lj | 1) * nz + (size_t)(nz / 2) * sizeof(float2);
+        const float b_first = sys == SYS_P ? -1.0f : (sys == SYS_V ? 0.0f : 1.0f);
+        WallTables wt{d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, b_first, ps.nxz_inv, sys};
+        const size_t sms = wall_plane_smem(ny, nz);
         if (nz == 32) { k_plane_walls_s<1><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
         else if (nz == 64) { k_plane_walls_s<2><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
         else { k_plane_walls_s<4><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
