@@ -529,6 +529,17 @@ int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
                 API_CUDA(c, cudaMemsetAsync(dst[q], 0, ni * sizeof(float), c->s));
             }
         }
+        // a spatially uniform body force component (the channel's driving
+        // force) is passed to the momentum kernel as a constant
+        for (int q = 0; q < 3; ++q) {
+            const double *f = src[6 + q];
+            bool uni = true;
+            const double f0 = f ? f[0] : 0.0;
+            if (f)
+                for (size_t n = 1; n < ni && uni; ++n) uni = f[n] == f0;
+            d.Funi[q] = uni ? 1 : 0;
+            d.Fval[q] = (float)f0;
+        }
         API_CUDA(c, bc_all_state_mixed(d, c->s));
     }
     API_CUDA(c, cudaStreamSynchronize(c->s));

@@ -47,14 +47,12 @@ __device__ __forceinline__ df df_add_f(df a, float b) {
     return r;
 }
 
-// a + b
+// a + b with absolute error ~2^-48 (|a| + |b|): the accuracy FP64 gives the
+// stencil differences and sums of this path (the "sloppy" double-double add)
 __device__ __forceinline__ df df_add(df a, df b) {
-    float s, e, t, f;
+    float s, e;
     two_sum(a.hi, b.hi, s, e);
-    two_sum(a.lo, b.lo, t, f);
-    e = __fadd_rn(e, t);
-    fast_two_sum(s, e, s, e);
-    e = __fadd_rn(e, f);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
     df r;
     fast_two_sum(s, e, r.hi, r.lo);
     return r;

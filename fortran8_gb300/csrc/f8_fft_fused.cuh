@@ -534,10 +534,13 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
     float2 *Sp = S + (size_t)kx * NZ * lj;
     const float *Rg = wt.rden + (size_t)kx * NZ * lj;
     for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
-    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
-        const int k = q / lj, j = q % lj;
-        P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
-        Rs[(size_t)(__brev((unsigned)k) >> (32 - LG)) * rs + j] = Rg[q];
+    for (int k = warp; k < NZ; k += nwarp) {
+        float *rrow = Rs + (size_t)(__brev((unsigned)k) >> (32 - LG)) * rs;
+        for (int j = lane; j < lj; j += 32) {
+            const size_t q = (size_t)k * lj + j;
+            P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+            rrow[j] = Rg[q];
+        }
     }
     __syncthreads();
     for (int j = 1 + warp; j <= ny; j += nwarp) {
@@ -628,10 +631,8 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
         for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < lj * NZ; q += blockDim.x) {
-        const int k = q / lj, j = q % lj;
-        Sp[q] = P[(size_t)k * ljs + j];
-    }
+    for (int k = warp; k < NZ; k += nwarp)
+        for (int j = lane; j < lj; j += 32) Sp[(size_t)k * lj + j] = P[(size_t)k * ljs + j];
 }
 
 }  // namespace f8

@@ -45,6 +45,8 @@ struct Dev {
     float *Cf, *Cnf, *fpetf;               // FP32 conformation tensor (SoA halo) and f(C)
     int *fixlist, *fixcnt;                 // cells queued for the exact Newton re-solve
     float *A0f[3], *T0f[3], *Ff[3];        // FP32 history and body force (interior)
+    int Funi[3];                           // body force component uniform (value Fval)
+    float Fval[3];
     float *Qf[3];                          // FP32 right-hand sides dt*(R + f)
     float *Rhf, *Rlf;                      // df64 Poisson right-hand side (interior)
     float *Rdf;                            // Poisson defect (interior)

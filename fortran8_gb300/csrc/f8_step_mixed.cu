@@ -620,7 +620,8 @@ struct MomArgsF {
     const float *Ph, *Pl;     // pressure (df64)
     const float *C, *fpet;
     float *A0[3], *T0[3];
-    const float *F[3];
+    const float *F[3];        // body force, or null when uniform (value in Fu)
+    float Fu[3];
     float *Q[3];
     int cs;
     int polymer, ab2_first;
@@ -695,7 +696,8 @@ __global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst
         // pressure difference from the df64 pair: the hi difference is
         // correctly rounded, the lo difference carries the rest
         const float gp = -((a.Ph[hp[c]] - ph0) + (a.Pl[hp[c]] - pl0)) * id[c];
-        const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + a.F[c][o];
+        const float fb = a.F[c] ? a.F[c][o] : a.Fu[c];
+        const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + fb;
         a.Q[c][o] = dt * r;
         a.A0[c][o] = A[c];
         a.T0[c][o] = T[c];
@@ -808,6 +810,16 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
 
 // ---------------------------------------------------------------------------
 // Pressure solve and projection on the df64 state.
+// Index of the neighbour (d = -1 / +1 along axis c) of interior cell
+// (i, j, k) for a field whose halo has not been filled: periodic wrap, and
+// the Neumann copy (P-kind boundary value) at the walls.
+__device__ __forceinline__ int nbr_p(const Geo &g, int i, int j, int k, int c, int d) {
+    if (c == 0) return hix(g, wrapx(g, i + d), j, k);
+    if (c == 2) return hix(g, i, j, wrapz(g, k + d));
+    const int jj = g.walls ? max(1, min(g.ny, j + d)) : wrapy(g, j + d);
+    return hix(g, i, jj, k);
+}
+
 // The df64 state of one field
 struct DfF {
     float *hi, *lo;
@@ -829,12 +841,15 @@ __global__ void k_poisson_rhs_df(DfF U, DfF V, DfF W, const float *__restrict__ 
     const int off[3] = {1, g.sx, g.sx * g.sy};
     const DfF F[3] = {U, V, W};
     const float *D[3] = {dU, dV, dW};
+    // the increments have no halo pass: periodic neighbours by wrapping; at
+    // the lower wall dV(j = 0) = 0 is the ghost row the wall solve wrote
+    const int dm[3] = {hix(g, wrapx(g, i - 1), j, k), g.walls ? h - off[1] : hix(g, i, wrapy(g, j - 1), k),
+                       hix(g, i, j, wrapz(g, k - 1))};
     df sum{0.0f, 0.0f};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const int hm = h - off[c];
-        df a = df_sub(F[c].at(h), F[c].at(hm));
-        a = df_add(a, df_diff_ff(D[c][h], D[c][hm]));
+        df a = df_sub(F[c].at(h), F[c].at(h - off[c]));
+        a = df_add(a, df_diff_ff(D[c][h], D[c][dm[c]]));
         sum = df_add(sum, df_mul(a, mc.di[c]));
     }
     sum = df_mul(sum, mc.idt);
@@ -852,13 +867,12 @@ __global__ void k_defect_df(DfF Phi, const float *__restrict__ Rh, const float *
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
     const int h = hix(g, i, j, k);
-    const int off[3] = {1, g.sx, g.sx * g.sy};
     const df c0 = Phi.at(h);
     const int o = qix(g, i, j, k);
     df res{Rh[o], Rl[o]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const df dp = df_sub(Phi.at(h + off[c]), c0), dm = df_sub(c0, Phi.at(h - off[c]));
+        const df dp = df_sub(Phi.at(nbr_p(g, i, j, k, c, 1)), c0), dm = df_sub(c0, Phi.at(nbr_p(g, i, j, k, c, -1)));
         res = df_sub(res, df_mul(df_sub(dp, dm), mc.di2[c]));
     }
     r[o] = df_to_f(res);
@@ -875,7 +889,6 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
     const int k = blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
     const int h = hix(g, i, j, k);
-    const int off[3] = {1, g.sx, g.sx * g.sy};
     const DfF F[3] = {U, V, W};
     const float *D[3] = {dU, dV, dW};
     const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
@@ -883,7 +896,7 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
     float lap = 0.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const df pp = Phi.at(h + off[c]), pm = Phi.at(h - off[c]);
+        const df pp = Phi.at(nbr_p(g, i, j, k, c, 1)), pm = Phi.at(nbr_p(g, i, j, k, c, -1));
         const df dp = df_sub(pp, c0);
         const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
         F[c].set(h, df_add(F[c].at(h), inc));
@@ -1181,6 +1194,9 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
 
 // df64 state -> the FP64 fields U, V, W, P, Phi (for store and diagnostics)
 cudaError_t mixed_state_to_fp64(Dev &d, cudaStream_t s) {
+    BcSet bphi{};   // Phi carries no halo during the step
+    bphi.hi[0] = d.Phif; bphi.lo[0] = d.Phil; bphi.kind[0] = BC_P; bphi.n = 1;
+    F8_CUDA_RET(launch_bc_set(bphi, d.g, s));
     double *dst[5] = {d.U, d.V, d.W, d.P, d.Phi};
     const float *hi[5] = {d.Uf, d.Vf, d.Wf, d.Pf, d.Phif}, *lo[5] = {d.Ul, d.Vl, d.Wl, d.Pl, d.Phil};
     for (int q = 0; q < 5; ++q) {
@@ -1220,7 +1236,11 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     {
         MomArgsF a{};
         a.U = d.Uf; a.V = d.Vf; a.W = d.Wf; a.Ph = d.Pf; a.Pl = d.Pl; a.C = d.Cf; a.fpet = d.fpetf;
-        for (int c = 0; c < 3; ++c) { a.A0[c] = d.A0f[c]; a.T0[c] = d.T0f[c]; a.F[c] = d.Ff[c]; a.Q[c] = d.Qf[c]; }
+        for (int c = 0; c < 3; ++c) {
+            a.A0[c] = d.A0f[c]; a.T0[c] = d.T0f[c]; a.Q[c] = d.Qf[c];
+            a.F[c] = d.Funi[c] ? nullptr : d.Ff[c];
+            a.Fu[c] = d.Fval[c];
+        }
         a.cs = d.cs; a.polymer = o.polymer; a.ab2_first = o.ab2_first;
         a.coef_t = (float)((1.0 - d.ph.beta) / (d.ph.re * d.ph.wi));
         a.vis = (float)(d.ph.beta / d.ph.re);
@@ -1270,16 +1290,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         else e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
         if (e) return e;
     }
-    {
-        BcSet b{};   // homogeneous boundary values of the increments
-        for (int c = 0; c < 3; ++c) { b.hi[c] = d.dUf[c]; b.lo[c] = nullptr; b.kind[c] = BC_U + c; }
-        b.n = 3;
-        F8_CUDA_RET(launch_bc_set(b, g, s));
-    }
     mark(5);
-    // Poisson: FP32 solve + one df64 defect correction
-    BcSet bphi{};
-    bphi.hi[0] = d.Phif; bphi.lo[0] = d.Phil; bphi.kind[0] = BC_P; bphi.n = 1;
+    // Poisson: FP32 solve + one df64 defect correction.  The increments and
+    // Phi get no halo pass: their readers wrap / apply the Neumann rule.
     {
         dim3 blk(32, 8);
         k_poisson_rhs_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
@@ -1291,7 +1304,6 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         else e = solve_walls_f(d, d.Rhf, out, SYS_P, s);
         if (e) return e;
     }
-    F8_CUDA_RET(launch_bc_set(bphi, g, s));
     for (int it = 0; it < d.defect_iters; ++it) {
         dim3 blk(32, 8);
         k_defect_df<<<cell_grid_m(g, blk), blk, 0, s>>>(Phi, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
@@ -1299,7 +1311,6 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         if (!g.walls) e = solve_periodic_f(d, d.Rdf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rdf, out, SYS_P, s);
         if (e) return e;
-        F8_CUDA_RET(launch_bc_set(bphi, g, s));
     }
     mark(6);
     {
