@@ -300,7 +300,13 @@ namespace f8 {
 // Warp-level radix-2 transform of one line of N = 32*V points: lane t holds
 // elements t + 32 s (s < V).  Spans >= 32 are butterflies inside the lane,
 // spans < 32 exchange with lane t ^ span.  tw: forward twiddles
-// (cos, -sin)(2 pi p / N), p < N/2, in shared memory.
+// (cos, -sin)(2 pi p / N), p < N/2, in shared memory.  The complex arithmetic
+// uses packed FP32x2 operations; the cross-lane butterflies are branch-free
+// (the lanes holding the first element of a pair multiply by 1).
+__device__ __forceinline__ float2 cmul_p(float2 a, float2 w) {
+    return __ffma2_rn(make_float2(a.x, a.x), w, __fmul2_rn(make_float2(a.y, a.y), make_float2(-w.y, w.x)));
+}
+
 template <int V>
 __device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) {
     constexpr int N = 32 * V;
@@ -315,25 +321,20 @@ __device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) 
                 const int pos = (lane + 32 * s) % (2 * m);
                 const float2 w = tw[pos * ts];
                 const float2 a = v[s], b = v[s + sm];
-                const float dr = a.x - b.x, di = a.y - b.y;
-                v[s] = make_float2(a.x + b.x, a.y + b.y);
-                v[s + sm] = make_float2(dr * w.x - di * w.y, dr * w.y + di * w.x);
+                v[s] = __fadd2_rn(a, b);
+                v[s + sm] = cmul_p(__ffma2_rn(b, make_float2(-1.0f, -1.0f), a), w);
             }
         } else {
-            const bool lower = lane & m;
-            const int pos = (lane % (2 * m)) - (lower ? m : 0);
-            const float2 w = tw[pos * ts];
+            const bool second = lane & m;            // this lane holds the second element
+            const float2 w = second ? tw[((lane % (2 * m)) - m) * ts] : make_float2(1.0f, 0.0f);
+            const float sg = second ? -1.0f : 1.0f;
 #pragma unroll
             for (int s = 0; s < V; ++s) {
                 float2 o;
                 o.x = __shfl_xor_sync(0xffffffffu, v[s].x, m);
                 o.y = __shfl_xor_sync(0xffffffffu, v[s].y, m);
-                if (!lower) {
-                    v[s] = make_float2(v[s].x + o.x, v[s].y + o.y);
-                } else {
-                    const float dr = o.x - v[s].x, di = o.y - v[s].y;
-                    v[s] = make_float2(dr * w.x - di * w.y, dr * w.y + di * w.x);
-                }
+                // first: a + b; second: (a - b) w, with a the first element
+                v[s] = cmul_p(__ffma2_rn(make_float2(sg, sg), v[s], o), w);
             }
         }
     }
@@ -352,28 +353,29 @@ __device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) 
             for (int s = 0; s < V; ++s) {
                 if ((s / sm) % 2) continue;
                 const int pos = (lane + 32 * s) % (2 * m);
-                const float2 w = make_float2(tw[pos * ts].x, -tw[pos * ts].y);
-                const float2 a = v[s], b = v[s + sm];
-                const float tr = b.x * w.x - b.y * w.y, ti = b.x * w.y + b.y * w.x;
-                v[s] = make_float2(a.x + tr, a.y + ti);
-                v[s + sm] = make_float2(a.x - tr, a.y - ti);
+                const float2 w = tw[pos * ts];
+                const float2 t = cmul_p(v[s + sm], make_float2(w.x, -w.y));
+                const float2 a = v[s];
+                v[s] = __fadd2_rn(a, t);
+                v[s + sm] = __ffma2_rn(t, make_float2(-1.0f, -1.0f), a);
             }
         } else {
-            const bool lower = lane & m;
-            const int pos = (lane % (2 * m)) - (lower ? m : 0);
-            const float2 w = make_float2(tw[pos * ts].x, -tw[pos * ts].y);
+            const bool second = lane & m;
+            float2 w = make_float2(1.0f, 0.0f);
+            if (second) {
+                const float2 tv = tw[((lane % (2 * m)) - m) * ts];
+                w = make_float2(tv.x, -tv.y);
+            }
+            const float sg = second ? -1.0f : 1.0f;
 #pragma unroll
             for (int s = 0; s < V; ++s) {
+                // the second element is multiplied by the twiddle before the
+                // exchange: first: a + b w; second: a - b w
+                const float2 p = cmul_p(v[s], w);
                 float2 o;
-                o.x = __shfl_xor_sync(0xffffffffu, v[s].x, m);
-                o.y = __shfl_xor_sync(0xffffffffu, v[s].y, m);
-                if (!lower) {
-                    const float tr = o.x * w.x - o.y * w.y, ti = o.x * w.y + o.y * w.x;
-                    v[s] = make_float2(v[s].x + tr, v[s].y + ti);
-                } else {
-                    const float tr = v[s].x * w.x - v[s].y * w.y, ti = v[s].x * w.y + v[s].y * w.x;
-                    v[s] = make_float2(o.x - tr, o.y - ti);
-                }
+                o.x = __shfl_xor_sync(0xffffffffu, p.x, m);
+                o.y = __shfl_xor_sync(0xffffffffu, p.y, m);
+                v[s] = __ffma2_rn(make_float2(sg, sg), p, o);
             }
         }
     }
