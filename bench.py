@@ -50,16 +50,28 @@ FP64_STAGE_WORDS = {
     "poisson": 5.0,      # U* (3) read, RHS, Phi written (FFT-internal passes excluded)
     "project": 9.0,      # U*, Phi, P read (5); U, V, W, P written (4)
 }
-# FP32-mixed step, in bytes (FP32: C, f, A0, T0, F, velocity copies, RHS;
-# FP64: U, V, W, P, Phi, U*):
+# FP32-mixed step, in bytes.  FP32: C, f, A0, T0, F, the Helmholtz increments
+# dU and the defect; double-float (hi + lo FP32, 8 B): U, V, W, P, Phi and the
+# Poisson right-hand side.  F is not read when uniform (the channel's force).
 MIXED_STAGE_BYTES = {
     "eigen": 25.0,       # C 24 read, code 1 written
-    "newton": 65.0,      # C 24, velocity copies 12, code 1 read; C 24, f 4 written
-    "momentum": 120.0,   # velocity copies 12, P 8, C 24, f 4, A0 12, T0 12, F 12 read; Q 12, A0 12, T0 12 written
+    "newton": 65.0,      # C 24, velocity hi 12, code 1 read; C 24, f 4 written
+    "momentum": 108.0,   # velocity hi 12, P 8, C 24, f 4, A0 12, T0 12 read; Q 12, A0 12, T0 12 written
     "ibm": 0.0,          # marker stencils only (not a per-cell stage)
-    "helmholtz": 60.0,   # 3 x (RHS 4 + U^n 8 read, U* 8 written)
-    "poisson": 96.0,     # div: U* 24 read, rhs 8 written; solve, defect (Phi 8 + rhs 8 read, r 8 written), correction
-    "project": 84.0,     # U* 24, Phi 8, P 8 read; U, V, W 24, FP32 copies 12, P 8 written
+    "helmholtz": 24.0,   # 3 x (Q 4 read, dU 4 written)
+    "poisson": 96.0,     # rhs: U, V, W 24 + dU 12 read, R 8 written; solve: R hi 4 read, Phi 8 written;
+                         # defect: Phi 8 + R 8 read, r 4 written; correction: r 4 read, Phi 8 read + 8 written
+    "project": 84.0,     # U, V, W, P 32 + dU 12 + Phi 8 read; U, V, W, P 32 written
+}
+# kernels of each stage of the mixed step (for the ncu traffic of a stage)
+MIXED_STAGE_KERNELS = {
+    "eigen": ["k_codes3_f"],
+    "newton": ["k_update3_f", "k_newton_fix_f", "k_bc_c_pet_f"],
+    "momentum": ["k_momentum3_f"],
+    "ibm": ["k_ibm_interp_f", "k_ibm_spread_f", "k_drag_part", "k_drag_final"],
+    "helmholtz": ["3 x (k_xfwd_w, k_plane_walls_s, k_xinv_w)"],
+    "poisson": ["k_poisson_rhs_df", "2 x (k_xfwd_w, k_plane_walls_s, k_xinv_w)", "k_defect_df"],
+    "project": ["k_march_df", "k_bc_set"],
 }
 
 
@@ -328,6 +340,7 @@ def run_ours(args, w):
     roof = {"bound": "hbm", "kernel_stage": names[top], "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
             "traffic": traffic, "algorithmic_bytes": byts,
+            "stage_kernels": (MIXED_STAGE_KERNELS.get(names[top]) if prec == abi.F8_MIXED else None),
             "stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)},
             "stage_hbm_frac": {n: (stage_bytes[n] * cells / (float(v) / 1e3) / 1e9 / peaks["hbm_gbs"]) if v > 0 else None
                                for n, v in zip(names, per_step)},
@@ -349,6 +362,62 @@ def run_ours(args, w):
     return 0
 
 
+# launches per step of each stage kernel of the mixed step (wall channel)
+MIXED_STAGE_LAUNCHES = {
+    "eigen": {"k_codes3_f": 1},
+    "newton": {"k_update3_f": 1, "k_newton_fix_f": 1, "k_bc_c_pet_f": 1},
+    "momentum": {"k_momentum3_f": 1},
+    "ibm": {"k_ibm_interp_f": 1, "k_ibm_spread_f": 1, "k_drag_part": 1, "k_drag_final": 1},
+    "helmholtz": {"k_xfwd_w": 3, "k_plane_walls_s": 3, "k_xinv_w": 3},
+    "poisson": {"k_poisson_rhs_df": 1, "k_xfwd_w": 2, "k_plane_walls_s": 2, "k_xinv_w": 2, "k_defect_df": 1},
+    "project": {"k_march_df": 1, "k_bc_set": 1},
+}
+
+
+def summarize_ncu(csv_path, traffic_out=None):
+    """Launch list of an ncu --csv log (per kernel: launches, total time, share)
+    and, when the log holds dram__bytes_{read,write}.sum, the DRAM bytes per
+    step of each stage of the mixed step (written to traffic_out as JSON)."""
+    import collections
+    import csv
+    import io
+    import re
+    txt = Path(csv_path).read_text()
+    rows = list(csv.DictReader(io.StringIO(txt[txt.index('"ID"'):])))
+    launches = collections.defaultdict(dict)
+    for r in rows:
+        launches[r["ID"]]["name"] = r["Kernel Name"]
+        launches[r["ID"]]["grid"] = r["Grid Size"]
+        launches[r["ID"]]["block"] = r["Block Size"]
+        launches[r["ID"]][r["Metric Name"]] = float(r["Metric Value"].replace(",", ""))
+
+    def base(n):
+        n = re.sub(r"\(.*", "", n).replace("unnamed>::", "").replace("f8::", "").replace("void ", "")
+        return re.sub(r"<.*", "", n).strip()
+
+    agg = collections.defaultdict(lambda: [0, 0.0, 0.0])
+    for L in launches.values():
+        a = agg[base(L["name"])]
+        a[0] += 1
+        a[1] += L.get("gpu__time_duration.sum", 0.0) / 1e3
+        a[2] += L.get("dram__bytes_read.sum", 0.0) + L.get("dram__bytes_write.sum", 0.0)
+    tot = sum(v[1] for v in agg.values())
+    print("| kernel | launches | total us | share | avg us | DRAM MB / launch |")
+    print("|---|---|---|---|---|---|")
+    for k, v in sorted(agg.items(), key=lambda kv: -kv[1][1]):
+        print(f"| {k} | {v[0]} | {v[1]:.1f} | {100 * v[1] / max(tot, 1e-9):.1f}% | {v[1] / v[0]:.1f} | "
+              f"{v[2] / v[0] / 1e6:.1f} |")
+    print(f"total {tot:.1f} us over {sum(v[0] for v in agg.values())} launches")
+    if traffic_out:
+        per = {k: v[2] / v[0] for k, v in agg.items() if v[0]}
+        out = {st: sum(per.get(k, 0.0) * n for k, n in ks.items()) for st, ks in MIXED_STAGE_LAUNCHES.items()}
+        out["source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, mean per launch x launches per step "
+                         f"({Path(csv_path).name})")
+        Path(traffic_out).write_text(json.dumps(out, indent=1) + "\n")
+        print("wrote", traffic_out)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,10 +428,18 @@ def main():
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
+                    help="scale the workload to this grid (small cases for profiling)")
+    ap.add_argument("--summarize-ncu", metavar="CSV", help="summarise an ncu --csv log instead of running")
+    ap.add_argument("--traffic-out", metavar="JSON", help="with --summarize-ncu: write per-stage DRAM bytes")
     args = ap.parse_args()
+    if args.summarize_ncu:
+        return summarize_ncu(args.summarize_ncu, args.traffic_out)
     if args.precision == "auto":
         args.precision = "mixed"
     w = configs.WORKLOADS[args.workload]()
+    if args.grid:
+        w = configs.scaled(w, *args.grid)
     if args.impl == "reference":
         return run_reference(args, w)
     return run_ours(args, w)

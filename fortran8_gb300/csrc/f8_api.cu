@@ -591,8 +591,8 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         c->step += 1;
     }
     API_CUDA(c, cudaEventRecord(c->tot1, c->s));
-    if (c->precision == F8_MIXED) API_CUDA(c, count_nonfinite_f(d.Uf, d.cs, c->nan_dev, c->s));
-    else API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
+    // the mixed step counts non-finite velocities inside its projection kernel
+    if (c->precision != F8_MIXED) API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
     c->step_launches += g_kernel_launches.load() - launches0;
     StepCounters cnt{};
     unsigned long long nan = 0;
@@ -615,7 +615,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     }
     c->last_newton_iters = (long long)cnt.newton_iters;
     c->last_newton_unconv = (long long)cnt.newton_unconverged;
-    if (nan) return F8_ERR_NAN;
+    if (nan || cnt.nan_cells) return F8_ERR_NAN;
     if (cnt.newton_unconverged) worst = std::max(worst, (int)F8_WARN_NEWTON);
     return worst;
 }

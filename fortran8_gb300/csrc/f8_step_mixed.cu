@@ -883,7 +883,7 @@ __global__ void k_defect_df(DfF Phi, const float *__restrict__ Rh, const float *
 // P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
 // in FP32
 __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
-                           const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc) {
+                           const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc, StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -893,17 +893,24 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
     const float *D[3] = {dU, dV, dW};
     const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
     const df c0 = Phi.at(h);
-    float lap = 0.0f;
+    float lap = 0.0f, unew = 0.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const df pp = Phi.at(nbr_p(g, i, j, k, c, 1)), pm = Phi.at(nbr_p(g, i, j, k, c, -1));
         const df dp = df_sub(pp, c0);
         const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
-        F[c].set(h, df_add(F[c].at(h), inc));
+        const df nu = df_add(F[c].at(h), inc);
+        F[c].set(h, nu);
+        if (c == 0) unew = nu.hi;
         const float dpf = (pp.hi - c0.hi) + (pp.lo - c0.lo), dmf = (c0.hi - pm.hi) + (c0.lo - pm.lo);
         lap += (dpf - dmf) * i2[c];
     }
     P.set(h, df_add_f(df_add(P.at(h), c0), -mc.pcf * lap));
+    // NaN watch on the new U (the reference stops on a NaN velocity,
+    // fenep_2d.f90:1974), counted here instead of in a separate pass
+    const unsigned act = __activemask();
+    const unsigned nb = __ballot_sync(act, !isfinite(unew));
+    if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
 }
 
 template <typename A, typename B>
@@ -1315,7 +1322,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
     mark(6);
     {
         dim3 blk(32, 8);
-        k_march_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc);
+        k_march_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
         count_launch();
     }
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from fortran8_gb300 import abi, configs
-from fortran8_gb300.solver import Solver
+from fortran8_gb300.solver import F8Error, Solver
 
 from .conftest import interior, rel_l2
 
@@ -87,3 +87,17 @@ def test_mixed_rejects_unbuilt_combinations(gpu):
     w3 = configs.scaled(configs.c3_channel(), 32, 16, 16)
     with pytest.raises(Exception):
         Solver(gpu, w3.grid, w3.phys, w3.cyls, precision=abi.F8_MIXED, poisson=abi.F8_POISSON_SOR)
+
+
+@pytest.mark.parametrize("precision", [abi.F8_MIXED, abi.F8_FP64])
+def test_nan_velocity_reported(gpu, precision):
+    """A NaN in the loaded velocity ends the call with F8_ERR_NAN (the
+    reference's 'NaN value' stop, fenep_2d.f90:1974) instead of running on."""
+    w = configs.scaled(configs.c3_channel(), 32, 16, 16)
+    st0 = configs.initial_state(w)
+    st0.arrays["u"][5, 6, 7] = np.nan
+    with Solver(gpu, w.grid, w.phys, w.cyls, precision=precision) as s:
+        s.load(st0)
+        with pytest.raises(F8Error) as exc:
+            s.step(2)
+        assert exc.value.status == abi.F8_ERR_NAN
