@@ -292,9 +292,9 @@ int setup(f8_ctx *c) {
         int dev = 0, optin = 0;
         API_CUDA(c, cudaGetDevice(&dev));
         API_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        const size_t need = g.walls ? std::max((size_t)12 * ((g.ny + 2) | 1) * g.nz, wall_plane_smem(g.ny, g.nz))
-                                    : (size_t)8 * (g.ny + 1) * g.nz;
-        d.fused_planes = need <= (size_t)optin ? 1 : 0;
+        d.plane_cl = g.walls ? wall_plane_cluster(g.ny, g.nz, (size_t)optin) : 0;
+        if (g.walls) d.fused_planes = (d.plane_cl > 0 || (size_t)12 * ((g.ny + 2) | 1) * g.nz <= (size_t)optin) ? 1 : 0;
+        else d.fused_planes = (size_t)8 * (g.ny + 1) * g.nz <= (size_t)optin ? 1 : 0;
         {
             std::vector<float2> t2(std::max(1, g.nz / 2));
             for (int t = 0; t < g.nz / 2; ++t) {
@@ -312,7 +312,7 @@ int setup(f8_ctx *c) {
             API_CUDA(c, cudaMemcpyAsync(d.twx2, tx.data(), tx.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
             API_CUDA(c, cudaStreamSynchronize(c->s));
         }
-        if (g.walls && d.fused_planes && (g.nz == 32 || g.nz == 64 || g.nz == 128)) {
+        if (g.walls && d.plane_cl > 0) {
             // Thomas pivots of the increment Helmholtz systems (U, V) and of the
             // pressure system (fenep_2d.f90:1222-1238, 1262-1277, 1318-1332;
             // tdma's guard, 1157-1160), for every (kx, kz)

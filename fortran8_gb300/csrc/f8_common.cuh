@@ -48,15 +48,28 @@ inline std::atomic<long long> g_kernel_launches{0};
 inline void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // Per-step device counters (status words read by the host after a step).
-// Shared memory of the scan-Thomas wall plane kernel: the (z, y) plane of one
-// kx (complex, odd row stride), the 1/den table of its systems with a row
-// stride >= lj and = 8 (mod 32) (the 4 systems x 8 chunks of a warp then read
-// 32 distinct banks), and the z twiddles.
-__host__ __device__ inline int wall_rd_stride(int lj) { return lj + (((8 - lj) % 32) + 32) % 32; }
+// Shared memory of the scan-Thomas wall plane kernel, whose (z, y) plane of
+// one kx is split over a cluster of cl CTAs, each holding R = ceil(lj / cl)
+// y rows: the rows (complex, odd row stride), the 1/den table of its systems
+// (row stride >= R and = T (mod 32), T = 1024 / nz threads per system, so
+// that the systems x chunks of a warp read distinct banks), the z twiddles,
+// and the composed forward / backward maps of its systems (3 floats each).
+__host__ __device__ inline int wall_rows_per_cta(int lj, int cl) { return (lj + cl - 1) / cl; }
+__host__ __device__ inline int wall_rd_stride(int r, int t) { return r + (((t - r) % 32) + 32) % 32; }
 
-__host__ __device__ inline size_t wall_plane_smem(int ny, int nz) {
-    const int lj = ny + 2;
-    return (size_t)8 * (lj | 1) * nz + (size_t)4 * wall_rd_stride(lj) * nz + (size_t)(nz / 2) * 8;
+__host__ __device__ inline size_t wall_plane_smem(int ny, int nz, int cl) {
+    const int r = wall_rows_per_cta(ny + 2, cl);
+    return (size_t)8 * (r | 1) * nz + (size_t)4 * wall_rd_stride(r, 1024 / nz) * nz + (size_t)(nz / 2) * 8
+           + (size_t)24 * nz;
+}
+
+// smallest cluster (<= 8 CTAs) whose per-CTA share of the plane fits in
+// `limit` bytes of shared memory, or 0
+inline int wall_plane_cluster(int ny, int nz, size_t limit) {
+    if (nz != 32 && nz != 64 && nz != 128 && nz != 256) return 0;
+    for (int cl = 1; cl <= 8; ++cl)
+        if (wall_plane_smem(ny, nz, cl) <= limit) return cl;
+    return 0;
 }
 
 struct StepCounters {

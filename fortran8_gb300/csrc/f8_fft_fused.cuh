@@ -16,6 +16,7 @@
 //              (bit-reversed store), so no reordering pass is needed.
 //   k_xinv_t   S -> real rows through a destination functor (XOutF).
 #pragma once
+#include <cooperative_groups.h>
 #include "f8_common.cuh"
 #include "f8_fft.cuh"
 
@@ -509,68 +510,97 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
 }
 
 // Wall plane with the Thomas solves split over T = 1024 / NZ threads per
-// (kx, kz) system.  Both sweeps are first-order affine recurrences,
+// (kx, kz) system and, for planes larger than one CTA's shared memory, over a
+// thread-block cluster of cl CTAs holding consecutive bands of y rows.  Both
+// sweeps are first-order affine recurrences,
 //   forward   q_j = alpha_j q_{j-1} + beta_j,  alpha_j = -c_j / den_j,
 //                                              beta_j  = d_j / den_j,
 //   backward  x_j = P_j x_{j+1} + q_j,          P_j = -b_j / den_j,
-// so each thread composes the maps of its chunk of rows, the T threads scan
-// the composed maps with shuffles, and each thread then replays its chunk
-// from its incoming value.  The coefficients are those of the sequential
-// Thomas solve of k_plane_walls (tdma, fenep_2d.f90:1145-1177); the 1/den
-// table of this kx is staged in shared memory, its rows in the bit-reversed
-// kz order of the spectrum rows.
+// so each thread composes the maps of its chunk of rows, the T threads of a
+// system scan the composed maps with shuffles, the CTAs of the cluster
+// exchange their composed maps through distributed shared memory, and each
+// thread then replays its chunk from its incoming value.  The coefficients
+// are those of the sequential Thomas solve of k_plane_walls (tdma,
+// fenep_2d.f90:1145-1177); the 1/den table of the CTA's rows is staged in
+// shared memory, its rows in the bit-reversed kz order of the spectrum rows.
+// The cluster barriers are hardware barriers; no thread waits on a flag.
 template <int V>
-__global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, const float2 *twz, WallTables wt) {
+__global__ void __launch_bounds__(1024, 1) k_plane_walls_c(float2 *S, int ny, int cl, const float2 *twz,
+                                                           WallTables wt) {
     constexpr int NZ = 32 * V;
-    constexpr int LG = V == 1 ? 5 : (V == 2 ? 6 : 7);
+    constexpr int LG = V == 1 ? 5 : (V == 2 ? 6 : (V == 4 ? 7 : 8));
     constexpr int T = 1024 / NZ;
+    namespace cg = cooperative_groups;
     extern __shared__ unsigned char smem_raw[];
     const int lj = ny + 2;
-    const int ljs = lj | 1;
-    const int rs = wall_rd_stride(lj);
-    float2 *P = reinterpret_cast<float2 *>(smem_raw);                // [k][j]
-    float *Rs = reinterpret_cast<float *>(P + (size_t)ljs * NZ);     // [row][j], row = bitrev(kz)
-    float2 *tws = reinterpret_cast<float2 *>(Rs + (size_t)rs * NZ);  // NZ/2 twiddles
-    const int kx = blockIdx.x;
+    const int R = wall_rows_per_cta(lj, cl);
+    const int rank = cl > 1 ? (int)cg::this_cluster().block_rank() : 0;
+    const int kx = blockIdx.x / cl;
+    const int jlo = rank * R;
+    const int nr = max(0, min(R, lj - jlo));   // rows held by this CTA
+    const int ps = R | 1;
+    const int rs = wall_rd_stride(R, T);
+    float2 *P = reinterpret_cast<float2 *>(smem_raw);                 // [k][jl]
+    float *Rs = reinterpret_cast<float *>(P + (size_t)ps * NZ);       // [row][jl], row = bitrev(kz)
+    float2 *tws = reinterpret_cast<float2 *>(Rs + (size_t)rs * NZ);   // NZ/2 twiddles
+    float *mapF = reinterpret_cast<float *>(tws + NZ / 2);            // [3][NZ]: A, Bx, By
+    float *mapB = mapF + 3 * NZ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     float2 *Sp = S + (size_t)kx * NZ * lj;
     const float *Rg = wt.rden + (size_t)kx * NZ * lj;
     for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
     for (int k = warp; k < NZ; k += nwarp) {
         float *rrow = Rs + (size_t)(__brev((unsigned)k) >> (32 - LG)) * rs;
-        for (int j = lane; j < lj; j += 32) {
+        for (int jl = lane; jl < nr; jl += 32) {
+            const int j = jlo + jl;
             const size_t q = (size_t)k * lj + j;
-            P[(size_t)k * ljs + j] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
-            rrow[j] = Rg[q];
+            P[(size_t)k * ps + jl] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+            rrow[jl] = Rg[q];
         }
     }
     __syncthreads();
-    for (int j = 1 + warp; j <= ny; j += nwarp) {
+    for (int jl = warp; jl < nr; jl += nwarp) {
+        const int j = jlo + jl;
+        if (j < 1 || j > ny) continue;   // ghost rows are zero
         float2 v[V];
 #pragma unroll
-        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ps + jl];
         warp_dif_fwd<V>(v, tws, lane);
 #pragma unroll
-        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ps + jl] = v[s];
     }
     __syncthreads();
     {
         const int row = threadIdx.x / T, t = threadIdx.x % T;
-        float2 *x = P + (size_t)row * ljs;
+        float2 *x = P + (size_t)row * ps;
         const float *rd = Rs + (size_t)row * rs;
-        const int L = (lj + T - 1) / T;
-        const int j0 = min(lj, t * L), j1 = min(lj, j0 + L);
+        const int L = (nr + T - 1) / T;
+        const int c0 = min(nr, t * L), c1 = min(nr, c0 + L);
         const bool sysv = wt.sys == SYS_V;
+        auto fwd_coef = [&](int jl, float &al, float2 &be) {
+            const int j = jlo + jl;
+            const bool ident = sysv ? (j >= ny) : (j == lj - 1);
+            const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
+            const float r = j == 0 ? 0.0f : rd[jl];
+            const float2 d = ident ? make_float2(0.f, 0.f) : x[jl];
+            al = -c * r;
+            const float dr = wt.nxz_inv * r;
+            be = make_float2(d.x * dr, d.y * dr);
+        };
+        auto pmul = [&](int jl) {
+            const int j = jlo + jl;
+            const bool zero_b = (j == lj - 1) || (sysv && j >= ny);
+            const float b = j == 0 ? wt.b_first : (zero_b ? 0.0f : wt.bc);
+            return -b * rd[jl];
+        };
         // forward: compose the chunk's maps (row 0: q_0 = 0)
         float A = 1.0f;
         float2 B = make_float2(0.f, 0.f);
-        for (int j = j0; j < j1; ++j) {
-            const bool ident = sysv ? (j >= ny) : (j == lj - 1);
-            const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
-            const float r = j == 0 ? 0.0f : rd[j];
-            const float2 d = ident ? make_float2(0.f, 0.f) : x[j];
-            const float al = -c * r, dr = wt.nxz_inv * r;
-            B = make_float2(fmaf(al, B.x, d.x * dr), fmaf(al, B.y, d.y * dr));
+        for (int jl = c0; jl < c1; ++jl) {
+            float al;
+            float2 be;
+            fwd_coef(jl, al, be);
+            B = make_float2(fmaf(al, B.x, be.x), fmaf(al, B.y, be.y));
             A *= al;
         }
 #pragma unroll
@@ -579,30 +609,35 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
             const float Bx = __shfl_up_sync(0xffffffffu, B.x, o, T), By = __shfl_up_sync(0xffffffffu, B.y, o, T);
             if (t >= o) { B = make_float2(fmaf(A, Bx, B.x), fmaf(A, By, B.y)); A *= Ap; }
         }
-        float2 q;
-        q.x = __shfl_up_sync(0xffffffffu, B.x, 1, T);
-        q.y = __shfl_up_sync(0xffffffffu, B.y, 1, T);
-        if (t == 0) q = make_float2(0.f, 0.f);
-        for (int j = j0; j < j1; ++j) {
-            const bool ident = sysv ? (j >= ny) : (j == lj - 1);
-            const float c = ident ? (sysv ? 0.f : wt.c_last) : wt.bc;
-            const float r = j == 0 ? 0.0f : rd[j];
-            const float2 d = ident ? make_float2(0.f, 0.f) : x[j];
-            const float al = -c * r, dr = wt.nxz_inv * r;
-            q = make_float2(fmaf(al, q.x, d.x * dr), fmaf(al, q.y, d.y * dr));
-            x[j] = q;
+        if (t == T - 1) { mapF[row] = A; mapF[NZ + row] = B.x; mapF[2 * NZ + row] = B.y; }
+        float Ae = __shfl_up_sync(0xffffffffu, A, 1, T);
+        float2 Be;
+        Be.x = __shfl_up_sync(0xffffffffu, B.x, 1, T);
+        Be.y = __shfl_up_sync(0xffffffffu, B.y, 1, T);
+        if (t == 0) { Ae = 1.0f; Be = make_float2(0.f, 0.f); }
+        float2 qin = make_float2(0.f, 0.f);
+        if (cl > 1) {
+            cg::this_cluster().sync();
+            for (int rr = 0; rr < rank; ++rr) {
+                const float *m = cg::this_cluster().map_shared_rank(mapF, rr);
+                const float a = m[row];
+                qin = make_float2(fmaf(a, qin.x, m[NZ + row]), fmaf(a, qin.y, m[2 * NZ + row]));
+            }
+        }
+        float2 q = make_float2(fmaf(Ae, qin.x, Be.x), fmaf(Ae, qin.y, Be.y));
+        for (int jl = c0; jl < c1; ++jl) {
+            float al;
+            float2 be;
+            fwd_coef(jl, al, be);
+            q = make_float2(fmaf(al, q.x, be.x), fmaf(al, q.y, be.y));
+            x[jl] = q;
         }
         // backward: x_j = P_j x_{j+1} + q_j (b and so P of the last row are 0)
-        auto pmul = [&](int j) {
-            const bool zero_b = (j == lj - 1) || (sysv && j >= ny);
-            const float b = j == 0 ? wt.b_first : (zero_b ? 0.0f : wt.bc);
-            return -b * rd[j];
-        };
         A = 1.0f;
         B = make_float2(0.f, 0.f);
-        for (int j = j1 - 1; j >= j0; --j) {
-            const float pj = pmul(j);
-            const float2 qj = x[j];
+        for (int jl = c1 - 1; jl >= c0; --jl) {
+            const float pj = pmul(jl);
+            const float2 qj = x[jl];
             B = make_float2(fmaf(pj, B.x, qj.x), fmaf(pj, B.y, qj.y));
             A *= pj;
         }
@@ -612,29 +647,42 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_s(float2 *S, int ny, co
             const float Bx = __shfl_down_sync(0xffffffffu, B.x, o, T), By = __shfl_down_sync(0xffffffffu, B.y, o, T);
             if (t + o < T) { B = make_float2(fmaf(A, Bx, B.x), fmaf(A, By, B.y)); A *= An; }
         }
-        float2 xv;
-        xv.x = __shfl_down_sync(0xffffffffu, B.x, 1, T);
-        xv.y = __shfl_down_sync(0xffffffffu, B.y, 1, T);
-        if (t == T - 1) xv = make_float2(0.f, 0.f);
-        for (int j = j1 - 1; j >= j0; --j) {
-            const float pj = pmul(j);
-            const float2 qj = x[j];
+        if (t == 0) { mapB[row] = A; mapB[NZ + row] = B.x; mapB[2 * NZ + row] = B.y; }
+        Ae = __shfl_down_sync(0xffffffffu, A, 1, T);
+        Be.x = __shfl_down_sync(0xffffffffu, B.x, 1, T);
+        Be.y = __shfl_down_sync(0xffffffffu, B.y, 1, T);
+        if (t == T - 1) { Ae = 1.0f; Be = make_float2(0.f, 0.f); }
+        float2 xin = make_float2(0.f, 0.f);
+        if (cl > 1) {
+            cg::this_cluster().sync();
+            for (int rr = cl - 1; rr > rank; --rr) {
+                const float *m = cg::this_cluster().map_shared_rank(mapB, rr);
+                const float a = m[row];
+                xin = make_float2(fmaf(a, xin.x, m[NZ + row]), fmaf(a, xin.y, m[2 * NZ + row]));
+            }
+        }
+        float2 xv = make_float2(fmaf(Ae, xin.x, Be.x), fmaf(Ae, xin.y, Be.y));
+        for (int jl = c1 - 1; jl >= c0; --jl) {
+            const float pj = pmul(jl);
+            const float2 qj = x[jl];
             xv = make_float2(fmaf(pj, xv.x, qj.x), fmaf(pj, xv.y, qj.y));
-            x[j] = xv;
+            x[jl] = xv;
         }
     }
-    __syncthreads();
-    for (int j = warp; j < lj; j += nwarp) {
+    // the other CTAs' reads of this CTA's maps are complete past this barrier
+    if (cl > 1) cg::this_cluster().sync();
+    else __syncthreads();
+    for (int jl = warp; jl < nr; jl += nwarp) {
         float2 v[V];
 #pragma unroll
-        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ljs + j];
+        for (int s = 0; s < V; ++s) v[s] = P[(size_t)(lane + 32 * s) * ps + jl];
         warp_dit_inv<V>(v, tws, lane);
 #pragma unroll
-        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ljs + j] = v[s];
+        for (int s = 0; s < V; ++s) P[(size_t)(lane + 32 * s) * ps + jl] = v[s];
     }
     __syncthreads();
     for (int k = warp; k < NZ; k += nwarp)
-        for (int j = lane; j < lj; j += 32) Sp[(size_t)k * lj + j] = P[(size_t)k * ljs + j];
+        for (int jl = lane; jl < nr; jl += 32) Sp[(size_t)k * lj + jlo + jl] = P[(size_t)k * ps + jl];
 }
 
 }  // namespace f8

@@ -54,6 +54,7 @@ struct Dev {
     float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
     float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
     int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory
+    int plane_cl;                          // walls: CTAs per cluster holding one (z, y) plane (0: none)
     float2 *twz2;                          // (cos, -sin)(2 pi p/NZ), p < NZ/2
     float2 *twx2;                          // (cos, -sin)(2 pi p/NX), p < NX/2
     float *wtR[3];                         // Thomas 1/den tables of the U, V, P wall systems

@@ -1083,14 +1083,30 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStr
     if (sys == SYS_P) { ps.ai_base = (float)(2.0 * idy2); ps.bc = (float)idy2; ps.kap = -1.0f; }
     else { ps.ai_base = (float)(1.0 + kap * 2.0 * idy2); ps.bc = (float)(-kap * idy2); ps.kap = (float)kap; }
     const size_t smp = (size_t)12 * (lj | 1) * nz;
-    if (d.wtR[0] && (nz == 32 || nz == 64 || nz == 128)) {
+    if (d.plane_cl > 0 && d.wtR[0]) {
         const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
         const float b_first = sys == SYS_P ? -1.0f : (sys == SYS_V ? 0.0f : 1.0f);
         WallTables wt{d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, b_first, ps.nxz_inv, sys};
-        const size_t sms = wall_plane_smem(ny, nz);
-        if (nz == 32) { k_plane_walls_s<1><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
-        else if (nz == 64) { k_plane_walls_s<2><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
-        else { k_plane_walls_s<4><<<nxh, 1024, sms, s>>>(S, ny, d.twz2, wt); count_launch(); }
+        const int cl = d.plane_cl;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)(nxh * cl));
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = wall_plane_smem(ny, nz, cl);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaError_t e;
+        if (nz == 32) e = cudaLaunchKernelEx(&cfg, k_plane_walls_c<1>, S, ny, cl, (const float2 *)d.twz2, wt);
+        else if (nz == 64) e = cudaLaunchKernelEx(&cfg, k_plane_walls_c<2>, S, ny, cl, (const float2 *)d.twz2, wt);
+        else if (nz == 128) e = cudaLaunchKernelEx(&cfg, k_plane_walls_c<4>, S, ny, cl, (const float2 *)d.twz2, wt);
+        else e = cudaLaunchKernelEx(&cfg, k_plane_walls_c<8>, S, ny, cl, (const float2 *)d.twz2, wt);
+        count_launch();
+        if (e) return e;
     } else {
         k_plane_walls<<<nxh, 1024, smp, s>>>(S, ny, nz, ilog2(nz), d.twzf_r, d.twzf_i, ps); count_launch();
     }
@@ -1124,9 +1140,10 @@ cudaError_t init_kernels_mixed() {
     F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     F8_CUDA_RET(cudaFuncSetAttribute(k_plane_periodic, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_s<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_c<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_c<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_c<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_plane_walls_c<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
 #define F8_XW_ATTR(E)                                                                                           \
     F8_CUDA_RET(cudaFuncSetAttribute(k_xfwd_w<E, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));   \
     F8_CUDA_RET(cudaFuncSetAttribute(k_xinv_w<E, XOutF>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));

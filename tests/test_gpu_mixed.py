@@ -101,3 +101,19 @@ def test_nan_velocity_reported(gpu, precision):
         with pytest.raises(F8Error) as exc:
             s.step(2)
         assert exc.value.status == abi.F8_ERR_NAN
+
+
+@pytest.mark.parametrize("shape", [(32, 512, 64), (16, 256, 256)])
+def test_mixed_cluster_plane_matches_fp64(gpu, shape):
+    """Channels whose (z, y) plane is split over a thread-block cluster (2 CTAs
+    for 512 x 64, 4 CTAs for 256 x 256, the 512x256x256 configuration's
+    plane) against the FP64 step: fields after 10 steps (no cylinders, the
+    IBM needs dX = dY)."""
+    w = replace(configs.scaled(configs.c3_channel(), *shape), cyls=())
+    sm, _, om, _ = run(gpu, w, 10, abi.F8_MIXED)
+    s6, _, o6, _ = run(gpu, w, 10, abi.F8_FP64)
+    assert sm == abi.F8_OK and s6 == abi.F8_OK
+    for f in ("u", "v", "w"):
+        assert rel_l2(interior(om[f]), interior(o6[f])) <= VEL_TOL, f
+    pm, p6 = interior(om["p"]), interior(o6["p"])
+    assert rel_l2(pm - pm.mean(), p6 - p6.mean()) <= 1e-4
