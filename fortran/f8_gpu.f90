@@ -62,6 +62,7 @@ module f8_gpu
         integer(c_long_long) :: newton_iters, newton_unconverged
         integer(c_int) :: poisson_iters, nan_found
         integer(c_long_long) :: kernel_launches
+        real(c_double) :: trc_std
     end type f8_diag
 
     interface

@@ -62,7 +62,7 @@ class Diag(C.Structure):
                 ("trc_min", C.c_double), ("trc_max", C.c_double), ("trc_mean", C.c_double),
                 ("div_max", C.c_double), ("newton_iters", C.c_longlong),
                 ("newton_unconverged", C.c_longlong), ("poisson_iters", C.c_int),
-                ("nan_found", C.c_int), ("kernel_launches", C.c_longlong)]
+                ("nan_found", C.c_int), ("kernel_launches", C.c_longlong), ("trc_std", C.c_double)]
 
 
 # Entry points declared in include/f8.h (without prefix).

@@ -26,6 +26,7 @@ UNITS = {
     "f8_api.cu": ["--fmad=false"],
     "f8_step_mixed.cu": [],
     "f8_fftsolve.cu": ["--fmad=false"],
+    "f8_diag.cu": ["--fmad=false"],
 }
 
 

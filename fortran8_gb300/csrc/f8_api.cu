@@ -92,6 +92,7 @@ struct f8_ctx {
     int drag_cap = 0;
     double *scratch_aos = nullptr;   // ncomp * cs doubles (C transposes)
     unsigned long long *nan_dev = nullptr;
+    double *diag_part = nullptr;      // block partials of the on-device diagnostics
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -259,6 +260,7 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.flag, 4));
     API_CUDA(c, c->alloc(&d.cnt, 1));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
+    API_CUDA(c, c->alloc(&c->diag_part, diag_partials()));
     std::vector<double> tr, ti;
     double **twd[3][2] = {{&d.twx_r, &d.twx_i}, {&d.twy_r, &d.twy_i}, {&d.twz_r, &d.twz_i}};
     float **twf[3][2] = {{&d.twxf_r, &d.twxf_i}, {&d.twyf_r, &d.twyf_i}, {&d.twzf_r, &d.twzf_i}};
@@ -662,40 +664,16 @@ int f8_store(f8_ctx *c, f8_fields *out) {
 
 int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
     if (!c || !dg) return F8_ERR_ARG;
-    const Geo &g = c->d.g;
-    const size_t cs = c->d.cs;
-    const int nc = c->d.ncomp;
-    std::vector<double> U(cs), V(cs), W(cs, 0.0), C(cs * nc);
-    f8_fields f{};
-    f.u = U.data(); f.v = V.data(); f.w = W.data(); f.c = C.data();
-    if (int st = f8_store(c, &f)) return st;
+    if (!c->loaded) return F8_ERR_STATE;
     std::memset(dg, 0, sizeof(*dg));
+    DiagValues v{};
+    API_CUDA(c, device_diagnostics(c->d, c->precision == F8_MIXED, c->diag_part, c->d.scal, &v, c->s));
     dg->step = c->step;
-    const bool d3 = g.dim == 3;
-    auto h = [&](int i, int j, int k) { return (size_t)i + (size_t)g.sx * ((size_t)j + (size_t)g.sy * k); };
-    double ke = 0, tmin = 1e300, tmax = -1e300, tsum = 0, dmax = 0, umax = -1e300, vmax = -1e300, wmax = -1e300;
-    for (int k = 1; k <= g.nz; ++k)
-        for (int j = 1; j <= g.ny; ++j)
-            for (int i = 1; i <= g.nx; ++i) {
-                double ur = (U[h(i, j, k)] + U[h(i - 1, j, k)]) / 2.0, vr = (V[h(i, j, k)] + V[h(i, j - 1, k)]) / 2.0;
-                double wr = d3 ? (W[h(i, j, k)] + W[h(i, j, k - 1)]) / 2.0 : 0.0;
-                ke += ur * ur + vr * vr + wr * wr;
-                const double *cc = &C[nc * h(i, j, k)];
-                double tr = d3 ? cc[0] + cc[3] + cc[5] : cc[0] + cc[2];
-                tmin = std::min(tmin, tr); tmax = std::max(tmax, tr); tsum += tr;
-                double dv = (U[h(i, j, k)] - U[h(i - 1, j, k)]) / g.dx + (V[h(i, j, k)] - V[h(i, j - 1, k)]) / g.dy;
-                if (d3) dv += (W[h(i, j, k)] - W[h(i, j, k - 1)]) / g.dz;
-                dmax = std::max(dmax, std::fabs(dv));
-                if (std::isnan(ur) || std::isnan(vr) || std::isnan(wr)) dg->nan_found = 1;
-            }
-    for (size_t n = 0; n < cs; ++n) { umax = std::max(umax, U[n]); vmax = std::max(vmax, V[n]); if (d3) wmax = std::max(wmax, W[n]); }
-    const double N = (double)c->d.ni;
-    dg->ke = ke / 2.0 / N;
-    double cfl = std::max(umax * g.dt / g.dx, vmax * g.dt / g.dy);
-    if (d3) cfl = std::max(cfl, wmax * g.dt / g.dz);
-    dg->cfl = cfl * 6.0;
-    dg->trc_min = tmin; dg->trc_max = tmax; dg->trc_mean = tsum / N;
-    dg->div_max = dmax;
+    dg->ke = v.ke;
+    dg->cfl = v.cfl;
+    dg->trc_min = v.trc_min; dg->trc_max = v.trc_max; dg->trc_mean = v.trc_mean; dg->trc_std = v.trc_std;
+    dg->div_max = v.div_max;
+    dg->nan_found = v.nan_found;
     dg->newton_iters = c->last_newton_iters;
     dg->newton_unconverged = c->last_newton_unconv;
     dg->poisson_iters = c->last_poisson_iters;

@@ -94,6 +94,13 @@ cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s);
 cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s);
 cudaError_t launch_march(Dev &d, cudaStream_t s);
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s);
+// On-device diagnostics (f8_diag.cu)
+struct DiagValues {
+    double ke, cfl, trc_min, trc_max, trc_mean, trc_std, div_max;
+    int nan_found;
+};
+size_t diag_partials();   // doubles of the partials buffer
+cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)
 cudaError_t init_kernels_mixed();
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s);

@@ -127,6 +127,8 @@ typedef struct f8_diag {
     long long kernel_launches;  /* CUDA kernels launched by this context's f8_step
                                    calls since f8_load or f8_timing_reset (0 for
                                    the CPU oracle)                                */
+    double trc_std;             /* standard deviation of trC over the cells,
+                                   mean first (fenep.f90:2316-2317)              */
 } f8_diag;
 
 typedef struct f8_ctx f8_ctx;
@@ -156,7 +158,9 @@ int f8_step(f8_ctx *ctx, int nsteps, double *drag);
  * pointers are skipped.  Replaces: output (fenep.f90:1186-1233). */
 int f8_store(f8_ctx *ctx, f8_fields *out);
 
-/* Diagnostics of the current state (log_progress, fenep.f90:2266-2342). */
+/* Diagnostics of the current state (log_progress, fenep.f90:2266-2342),
+ * reduced on the device: kinetic energy, CFL, trC min / max / mean / std,
+ * max |div u|, NaN flag, and the iteration counters of the last f8_step. */
 int f8_diagnostics(f8_ctx *ctx, f8_diag *out);
 
 /* Number of Lagrangian markers per z-plane and their host-side positions

@@ -1590,6 +1590,19 @@ int f8o_diagnostics(f8_ctx *ctx, f8_diag *d) {
     if (d3) cfl = std::max(cfl, wmax * c.ph.dt / c.dZ);
     d->cfl = cfl * 6.0;
     d->trc_min = tmin; d->trc_max = tmax; d->trc_mean = tsum / N;
+    // std = sqrt(sum((trC - mean)^2) / N), mean first (fenep.f90:2316-2317)
+    {
+        const double mean = tsum / N;
+        double s2 = 0.0;
+        for (int k = 1; k <= c.NZ; ++k)
+            for (int j = 1; j <= c.NY; ++j)
+                for (int i = 1; i <= c.NX; ++i) {
+                    const double *cc = &c.C[c.NC * c.hidx(i, j, k)];
+                    const double tr = d3 ? cc[0] + cc[3] + cc[5] : cc[0] + cc[2];
+                    s2 += (tr - mean) * (tr - mean);
+                }
+        d->trc_std = std::sqrt(s2 / N);
+    }
     d->div_max = dmax;
     d->newton_iters = c.newton_iters; d->newton_unconverged = c.newton_unconv;
     d->poisson_iters = c.poisson_iters;

@@ -47,13 +47,17 @@ def drag_rel(dm, d64, all_components=False):
 def test_mixed_matches_fp64_oracle(gpu, oracle, name, shape, steps):
     w = configs.scaled(configs.WORKLOADS[name](), *shape)
     sm, dm, om, diag = run(gpu, w, steps, abi.F8_MIXED)
-    so, do, oo, _ = run(oracle, w, steps, abi.F8_FP64)
+    so, do, oo, diag_o = run(oracle, w, steps, abi.F8_FP64)
     assert sm == abi.F8_OK
     if name != "c2_3d":
         # the drag gate applies to the channel workloads; in the Taylor-Green
         # box the cylinder sits at a stagnation point and its force is
         # noise-level, so only the fields are compared there
         assert drag_rel(dm, do) <= DRAG_TOL
+    # the on-device diagnostics of the double-float state against the oracle
+    for f in ("ke", "trc_mean", "trc_max"):
+        a, b = getattr(diag, f), getattr(diag_o, f)
+        assert abs(a - b) <= 1e-5 * abs(b), (f, a, b)
     # the pressure is compared up to its additive constant
     pm, po = interior(om["p"]), interior(oo["p"])
     assert rel_l2(pm - pm.mean(), po - po.mean()) <= 1e-4

@@ -66,6 +66,11 @@ def test_fp64_step_matches_oracle(gpu, oracle, name, steps):
     assert drag_err(dg, do) <= DRAG_TOL
     assert diag_g.newton_iters == diag_o.newton_iters
     assert diag_g.div_max < 1e-10
+    # on-device reductions of log_progress against the oracle's sequential sums
+    for f in ("ke", "cfl", "trc_min", "trc_max", "trc_mean", "trc_std"):
+        a, b = getattr(diag_g, f), getattr(diag_o, f)
+        assert abs(a - b) <= 1e-10 * max(abs(b), 1e-300), (f, a, b)
+    assert diag_g.nan_found == diag_o.nan_found == 0
 
 
 def test_fp64_newtonian_no_ibm(gpu, oracle):
