@@ -114,6 +114,15 @@ module f8_gpu
             type(c_ptr), value :: xy
         end function f8_markers
 
+        ! out: real(8) (18, points) of the mid-plane slice (axis 2: x-y, 1: x-z, 0: y-z);
+        ! variant 0: column 7 = KE (fenep.f90), 1: Q (fenep_mpi.f90)
+        integer(c_int) function f8_slice(ctx, axis, variant, out) bind(C, name="f8_slice")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: axis, variant
+            type(c_ptr), value :: out
+        end function f8_slice
+
         integer(c_int) function f8_set_timing(ctx, enable) bind(C, name="f8_set_timing")
             import :: c_ptr, c_int
             type(c_ptr), value :: ctx

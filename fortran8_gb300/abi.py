@@ -74,6 +74,7 @@ ABI_FUNCTIONS = {
     "store": (C.c_int, [C.c_void_p, C.POINTER(Fields)]),
     "diagnostics": (C.c_int, [C.c_void_p, C.POINTER(Diag)]),
     "markers": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _dp]),
+    "slice": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "strerror": (C.c_char_p, [C.c_int]),
     "destroy": (None, [C.c_void_p]),
     "default_phys": (None, [C.POINTER(Phys)]),

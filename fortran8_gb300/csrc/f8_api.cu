@@ -93,6 +93,7 @@ struct f8_ctx {
     double *scratch_aos = nullptr;   // ncomp * cs doubles (C transposes)
     unsigned long long *nan_dev = nullptr;
     double *diag_part = nullptr;      // block partials of the on-device diagnostics
+    double *slice_dev = nullptr;      // 18 doubles per point of the largest slice
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -261,6 +262,10 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.cnt, 1));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
     API_CUDA(c, c->alloc(&c->diag_part, diag_partials()));
+    if (g.dim == 3) {
+        const size_t np = std::max({(size_t)g.nx * g.ny, (size_t)g.nx * g.nz, (size_t)g.ny * g.nz});
+        API_CUDA(c, c->alloc(&c->slice_dev, 18 * np));
+    }
     std::vector<double> tr, ti;
     double **twd[3][2] = {{&d.twx_r, &d.twx_i}, {&d.twy_r, &d.twy_i}, {&d.twz_r, &d.twz_i}};
     float **twf[3][2] = {{&d.twxf_r, &d.twxf_i}, {&d.twyf_r, &d.twyf_i}, {&d.twzf_r, &d.twzf_i}};
@@ -678,6 +683,17 @@ int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
     dg->newton_unconverged = c->last_newton_unconv;
     dg->poisson_iters = c->last_poisson_iters;
     dg->kernel_launches = c->step_launches;
+    return F8_OK;
+}
+
+int f8_slice(f8_ctx *c, int axis, int variant, double *out) {
+    if (!c || !out || axis < 0 || axis > 2 || variant < 0 || variant > 1) return F8_ERR_ARG;
+    if (!c->loaded) return F8_ERR_STATE;
+    if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
+    const int n = slice_points(c->d.g, axis);
+    API_CUDA(c, device_slice(c->d, c->precision == F8_MIXED, axis, variant, c->slice_dev, c->s));
+    API_CUDA(c, cudaMemcpyAsync(out, c->slice_dev, (size_t)n * 18 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
     return F8_OK;
 }
 

@@ -27,6 +27,23 @@ struct DiagIn {
     double idx, idy, idz;
 };
 
+}  // namespace
+
+static __device__ double slice_vel(const DiagSliceIn &in, int c, int q) {
+    if (in.mixed) {
+        const float *h = c == 0 ? in.Uh : (c == 1 ? in.Vh : in.Wh);
+        const float *l = c == 0 ? in.Ul : (c == 1 ? in.Vl : in.Wl);
+        return (double)h[q] + (double)l[q];
+    }
+    return (c == 0 ? in.U : (c == 1 ? in.V : in.W))[q];
+}
+
+static __device__ double slice_c(const DiagSliceIn &in, int m, int q) {
+    return in.mixed ? (double)in.Cf[(size_t)m * in.cs + q] : in.C[(size_t)m * in.cs + q];
+}
+
+namespace {
+
 __device__ inline double vel(const DiagIn &in, int c, int q) {
     if (in.mixed) {
         const float *h = c == 0 ? in.Uh : (c == 1 ? in.Vh : in.Wh);
@@ -174,5 +191,80 @@ cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, Di
 }
 
 size_t diag_partials() { return (size_t)DIAG_BLOCKS * P_N; }
+
+}  // namespace f8
+
+// ---------------------------------------------------------------------------
+// Slice output of get_data_binary (fenep.f90:1108-1183, fenep_mpi.f90:811-937):
+// per point of the mid-plane slice, 18 doubles x, y, z, E (3), KE or Q,
+// Omega (3), |Omega|^2/2, trC, C (6), with the velocity gradient D of the
+// reference's staggered differences.  The reference's nondimensional scales
+// U_C = L_C = 1 (fenep.f90:28-29) are used, so dX_C = dX.
+namespace f8 {
+namespace {
+
+__global__ void k_slice(DiagSliceIn in, Geo g, int axis, int variant, double *out) {
+    const int n1 = axis == 0 ? g.ny : g.nx;          // inner loop length
+    const int n2 = axis == 2 ? g.ny : g.nz;          // outer loop length
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2) return;
+    const int a = t % n1, b = t / n1;
+    int i, j, k;
+    if (axis == 2) { k = g.nz / 2; j = 1 + b; i = 1 + a; }
+    else if (axis == 1) { j = g.ny / 2; k = 1 + b; i = 1 + a; }
+    else { i = g.nx / 2; k = 1 + b; j = 1 + a; }
+    auto U = [&](int ii, int jj, int kk) { return slice_vel(in, 0, hix(g, ii, jj, kk)); };
+    auto V = [&](int ii, int jj, int kk) { return slice_vel(in, 1, hix(g, ii, jj, kk)); };
+    auto W = [&](int ii, int jj, int kk) { return slice_vel(in, 2, hix(g, ii, jj, kk)); };
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    double D[3][3];
+    D[0][0] = (U(i, j, k) - U(i - 1, j, k)) / dX;
+    D[0][1] = (U(i, j + 1, k) - U(i, j - 1, k) + U(i - 1, j + 1, k) - U(i - 1, j - 1, k)) / (4 * dY);
+    D[0][2] = (U(i, j, k + 1) - U(i, j, k - 1) + U(i - 1, j, k + 1) - U(i - 1, j, k - 1)) / (4 * dZ);
+    D[1][0] = (V(i + 1, j, k) - V(i - 1, j, k) + V(i + 1, j - 1, k) - V(i - 1, j - 1, k)) / (4 * dX);
+    D[1][1] = (V(i, j, k) - V(i, j - 1, k)) / dY;
+    D[1][2] = (V(i, j, k + 1) - V(i, j, k - 1) + V(i, j - 1, k + 1) - V(i, j - 1, k - 1)) / (4 * dZ);
+    D[2][0] = (W(i + 1, j, k) - W(i - 1, j, k) + W(i + 1, j, k - 1) - W(i - 1, j, k - 1)) / (4 * dX);
+    D[2][1] = (W(i, j + 1, k) - W(i, j - 1, k) + W(i, j + 1, k - 1) - W(i, j - 1, k - 1)) / (4 * dY);
+    D[2][2] = (W(i, j, k) - W(i, j, k - 1)) / dZ;
+    const double E0 = (U(i - 1, j, k) + U(i, j, k)) / 2, E1 = (V(i, j - 1, k) + V(i, j, k)) / 2,
+                 E2 = (W(i, j, k - 1) + W(i, j, k)) / 2;
+    const double O0 = D[2][1] - D[1][2], O1 = D[0][2] - D[2][0], O2 = D[1][0] - D[0][1];
+    const double Q = D[1][1] * D[2][2] - D[2][1] * D[1][2] + D[0][0] * D[1][1] - D[1][0] * D[0][1]
+                   + D[0][0] * D[2][2] - D[2][0] * D[0][2];
+    const int h = hix(g, i, j, k);
+    double c[6];
+    for (int m = 0; m < 6; ++m) c[m] = slice_c(in, m, h);
+    double *o = out + (size_t)t * 18;
+    o[0] = (i - 0.5) * dX; o[1] = (j - 0.5) * dY; o[2] = (k - 0.5) * dZ;
+    o[3] = E0; o[4] = E1; o[5] = E2;
+    o[6] = variant == 1 ? Q : (E0 * E0 + E1 * E1 + E2 * E2) / 2;
+    o[7] = O0; o[8] = O1; o[9] = O2;
+    o[10] = (O0 * O0 + O1 * O1 + O2 * O2) / 2;
+    o[11] = c[0] + c[3] + c[5];
+    for (int m = 0; m < 6; ++m) o[12 + m] = c[m];
+}
+
+}  // namespace
+
+int slice_points(const Geo &g, int axis) {
+    return axis == 2 ? g.nx * g.ny : (axis == 1 ? g.nx * g.nz : g.ny * g.nz);
+}
+
+cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_out, cudaStream_t s) {
+    DiagSliceIn in{};
+    in.cs = d.cs;
+    in.mixed = mixed ? 1 : 0;
+    if (mixed) {
+        in.Uh = d.Uf; in.Ul = d.Ul; in.Vh = d.Vf; in.Vl = d.Vl; in.Wh = d.Wf; in.Wl = d.Wl;
+        in.Cf = d.Cf;
+    } else {
+        in.U = d.U; in.V = d.V; in.W = d.W;
+        in.C = d.C;
+    }
+    const int n = slice_points(d.g, axis);
+    k_slice<<<(n + 127) / 128, 128, 0, s>>>(in, d.g, axis, variant, dev_out); count_launch();
+    return cudaGetLastError();
+}
 
 }  // namespace f8

@@ -100,6 +100,16 @@ struct DiagValues {
     int nan_found;
 };
 size_t diag_partials();   // doubles of the partials buffer
+// slice output (f8_diag.cu): the state of either precision, read as FP64
+struct DiagSliceIn {
+    const double *U, *V, *W;
+    const float *Uh, *Ul, *Vh, *Vl, *Wh, *Wl;
+    const double *C;
+    const float *Cf;
+    int cs, mixed;
+};
+int slice_points(const Geo &g, int axis);
+cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_out, cudaStream_t s);
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)
 cudaError_t init_kernels_mixed();

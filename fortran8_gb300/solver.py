@@ -176,6 +176,14 @@ class Solver:
         self._check(self._fns["diagnostics"](self._h, C.byref(d)))
         return d
 
+    def slice(self, axis: int = 2, variant: int = 0) -> np.ndarray:
+        """Mid-plane slice records of get_data_binary, shape (points, 18) (see f8_slice)."""
+        g = self.grid
+        n = {2: g.nx * g.ny, 1: g.nx * g.nz, 0: g.ny * g.nz}[axis]
+        out = np.zeros((n, 18))
+        self._check(self._fns["slice"](self._h, axis, variant, _ptr(out)))
+        return out
+
     def markers(self) -> np.ndarray:
         n = C.c_int()
         self._check(self._fns["markers"](self._h, C.byref(n), None))

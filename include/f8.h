@@ -163,6 +163,15 @@ int f8_store(f8_ctx *ctx, f8_fields *out);
  * max |div u|, NaN flag, and the iteration counters of the last f8_step. */
 int f8_diagnostics(f8_ctx *ctx, f8_diag *out);
 
+/* Mid-plane slice of get_data_binary (fenep.f90:1108-1183; fenep_mpi.f90:
+ * 811-937), computed on the device from the resident state: axis 2 is the
+ * x-y plane k = NZ/2 (j outer, i inner), axis 1 the x-z plane j = NY/2 and
+ * axis 0 the y-z plane i = NX/2 (k outer).  Per point 18 doubles: x, y, z,
+ * E(3), KE (variant 0, fenep.f90) or Q (variant 1, fenep_mpi.f90), Omega(3),
+ * |Omega|^2/2, trC, C(6); scales U_C = L_C = 1.  out holds 18 * points
+ * doubles (host).  3D only (F8_ERR_UNSUPPORTED in 2D). */
+int f8_slice(f8_ctx *ctx, int axis, int variant, double *out);
+
 /* Number of Lagrangian markers per z-plane and their host-side positions
  * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */
 int f8_markers(f8_ctx *ctx, int *n_per_plane, double *xy);

@@ -1609,6 +1609,51 @@ int f8o_diagnostics(f8_ctx *ctx, f8_diag *d) {
     return F8_OK;
 }
 
+// get_data_binary's slice records (fenep.f90:1108-1183; fenep_mpi.f90:811-937)
+// with U_C = L_C = 1: x, y, z, E(3), KE or Q, Omega(3), |Omega|^2/2, trC, C(6)
+int f8o_slice(f8_ctx *ctx, int axis, int variant, double *out) {
+    if (!ctx || !out || axis < 0 || axis > 2 || variant < 0 || variant > 1) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (c.dim != 3) return F8_ERR_UNSUPPORTED;
+    const double dX = c.dX, dY = c.dY, dZ = c.dZ;
+    auto U = [&](int i, int j, int k) { return c.U[c.hidx(i, j, k)]; };
+    auto V = [&](int i, int j, int k) { return c.V[c.hidx(i, j, k)]; };
+    auto W = [&](int i, int j, int k) { return c.W[c.hidx(i, j, k)]; };
+    const int n1 = axis == 0 ? c.NY : c.NX, n2 = axis == 2 ? c.NY : c.NZ;
+    for (int b = 0; b < n2; ++b)
+        for (int a = 0; a < n1; ++a) {
+            int i, j, k;
+            if (axis == 2) { k = c.NZ / 2; j = 1 + b; i = 1 + a; }
+            else if (axis == 1) { j = c.NY / 2; k = 1 + b; i = 1 + a; }
+            else { i = c.NX / 2; k = 1 + b; j = 1 + a; }
+            double D[3][3];
+            D[0][0] = (U(i, j, k) - U(i - 1, j, k)) / dX;
+            D[0][1] = (U(i, j + 1, k) - U(i, j - 1, k) + U(i - 1, j + 1, k) - U(i - 1, j - 1, k)) / (4 * dY);
+            D[0][2] = (U(i, j, k + 1) - U(i, j, k - 1) + U(i - 1, j, k + 1) - U(i - 1, j, k - 1)) / (4 * dZ);
+            D[1][0] = (V(i + 1, j, k) - V(i - 1, j, k) + V(i + 1, j - 1, k) - V(i - 1, j - 1, k)) / (4 * dX);
+            D[1][1] = (V(i, j, k) - V(i, j - 1, k)) / dY;
+            D[1][2] = (V(i, j, k + 1) - V(i, j, k - 1) + V(i, j - 1, k + 1) - V(i, j - 1, k - 1)) / (4 * dZ);
+            D[2][0] = (W(i + 1, j, k) - W(i - 1, j, k) + W(i + 1, j, k - 1) - W(i - 1, j, k - 1)) / (4 * dX);
+            D[2][1] = (W(i, j + 1, k) - W(i, j - 1, k) + W(i, j + 1, k - 1) - W(i, j - 1, k - 1)) / (4 * dY);
+            D[2][2] = (W(i, j, k) - W(i, j, k - 1)) / dZ;
+            const double E0 = (U(i - 1, j, k) + U(i, j, k)) / 2, E1 = (V(i, j - 1, k) + V(i, j, k)) / 2,
+                         E2 = (W(i, j, k - 1) + W(i, j, k)) / 2;
+            const double O0 = D[2][1] - D[1][2], O1 = D[0][2] - D[2][0], O2 = D[1][0] - D[0][1];
+            const double Q = D[1][1] * D[2][2] - D[2][1] * D[1][2] + D[0][0] * D[1][1] - D[1][0] * D[0][1]
+                           + D[0][0] * D[2][2] - D[2][0] * D[0][2];
+            const double *cc = &c.C[6 * c.hidx(i, j, k)];
+            double *o = out + 18 * ((size_t)b * n1 + a);
+            o[0] = (i - 0.5) * dX; o[1] = (j - 0.5) * dY; o[2] = (k - 0.5) * dZ;
+            o[3] = E0; o[4] = E1; o[5] = E2;
+            o[6] = variant == 1 ? Q : (E0 * E0 + E1 * E1 + E2 * E2) / 2;
+            o[7] = O0; o[8] = O1; o[9] = O2;
+            o[10] = (O0 * O0 + O1 * O1 + O2 * O2) / 2;
+            o[11] = cc[0] + cc[3] + cc[5];
+            for (int m = 0; m < 6; ++m) o[12 + m] = cc[m];
+        }
+    return F8_OK;
+}
+
 int f8o_markers(f8_ctx *ctx, int *n, double *xy) {
     if (!ctx) return F8_ERR_ARG;
     OCtx &c = *reinterpret_cast<OCtx *>(ctx);

@@ -147,3 +147,18 @@ def test_fft_solve_entry_matches_oracle(gpu, oracle, shape, lx, lhs):
     out = pd.cpu().numpy()
     # same transform order and tables as the oracle: identical to round-off
     assert np.max(np.abs(out - ref)) <= 1e-14 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("precision,tol", [(abi.F8_FP64, 1e-10), (abi.F8_MIXED, 1e-5)])
+def test_slice_matches_oracle(gpu, oracle, precision, tol):
+    """f8_slice (device) against the oracle's slice after 5 steps of the channel."""
+    w = small("c3_channel")
+    out = {}
+    for name, fns, prec in (("gpu", gpu, precision), ("oracle", oracle, abi.F8_FP64)):
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+            s.load(configs.initial_state(w))
+            s.step(5)
+            out[name] = [s.slice(a, v) for a in (0, 1, 2) for v in (0, 1)]
+    for g, o in zip(out["gpu"], out["oracle"]):
+        scale = np.max(np.abs(o), axis=0) + 1e-30
+        assert np.max(np.abs(g - o) / scale) <= tol
