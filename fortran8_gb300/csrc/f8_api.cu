@@ -481,7 +481,7 @@ int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *c
     *out = nullptr;
     int st = validate(g, ph, ncyl, cy, prec, poisson);
     if (st) return st;
-    if (prec == F8_MIXED && (g->dim != 3 || poisson != F8_POISSON_FFT)) return F8_ERR_UNSUPPORTED;
+    if (prec == F8_MIXED && g->dim != 3) return F8_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -591,7 +591,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         }
         int sor_iters = -1;
         double *dg = (ncyl && drag) ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
-        cudaError_t e = mixed ? step_mixed(d, o, dg, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
+        cudaError_t e = mixed ? step_mixed(d, o, dg, &sor_iters, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
         if (e != cudaSuccess) return fail(c, e, "step");
         c->last_poisson_iters = sor_iters;
         if (c->poisson == F8_POISSON_SOR && sor_iters > c->phys.sor_itrmax) worst = std::max(worst, (int)F8_WARN_SOR);

@@ -113,7 +113,7 @@ cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)
 cudaError_t init_kernels_mixed();
-cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s);
+cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s);
 cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s);
 cudaError_t mixed_state_to_fp64(Dev &d, cudaStream_t s);
 cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cudaStream_t s);

@@ -21,6 +21,7 @@
 // is divergence-free to the df64 rounding level.
 #include <algorithm>
 #include <cstdio>
+#include "../../include/f8.h"
 #include "f8_common.cuh"
 #include "f8_df64.cuh"
 #include "f8_fft.cuh"
@@ -913,6 +914,90 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
     if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
 }
 
+// ---------------------------------------------------------------------------
+// Red-black SOR variant of the pressure solve (the reference's poisson,
+// fenep.f90:848-905; the GPU colours by (i+j+k) parity as the FP64 step does)
+// on the FP32 pressure correction: Phi (hi part) warm-started from the
+// previous step, sweeps until sqrt(sum E^2 / sum R^2) < eps with the sums in
+// FP64, then the zero-mean shift (fenep_2d.f90:577-579).  The reference's
+// tolerance (1e-5) is far above FP32 rounding.  Halo-free: periodic wrap and
+// the Neumann copy at the walls, which is what the halo pass between the
+// colour sweeps of the FP64 step provides.
+__global__ void k_sor_color_f(float *Phi, float *E, const float *R, Geo g, int color, float om, float bx, float by,
+                              float bz, const int *flag) {
+    if (flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    if (((i + j + k) & 1) != color) return;
+    const int h = hix(g, i, j, k);
+    const float b0 = 2.0f * (bx + by + bz);
+    const int q = qix(g, i, j, k);
+    const float e = bz * Phi[nbr_p(g, i, j, k, 2, -1)] + by * Phi[nbr_p(g, i, j, k, 1, -1)]
+                  + bx * Phi[nbr_p(g, i, j, k, 0, -1)] - b0 * Phi[h] + bx * Phi[nbr_p(g, i, j, k, 0, 1)]
+                  + by * Phi[nbr_p(g, i, j, k, 1, 1)] + bz * Phi[nbr_p(g, i, j, k, 2, 1)] - R[q];
+    E[q] = e;
+    Phi[h] = Phi[h] + om * e / b0;
+}
+
+// block partials of sum(a^2) (mode 0) or of the interior sum of a halo field
+// (mode 1), in FP64, fixed order
+__global__ void k_sum_part_f(const float *a, int n, int mode, double *part, Geo g, const int *flag) {
+    if (flag && flag[0]) return;
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        if (mode == 0) {
+            const double v = a[q];
+            s += v * v;
+        } else {
+            const int i = 1 + (int)(q % g.nx), j = 1 + (int)((q / g.nx) % g.ny), k = 1 + (int)(q / ((long)g.nx * g.ny));
+            s += a[hix(g, i, j, k)];
+        }
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// mode 0: scal[slot] = sum (er0, the reference's zero guard); mode 1: the
+// convergence test against scal[0] (flag[0] = 1, flag[1] = iteration);
+// mode 2: scal[slot] = sum
+__global__ void k_sum_final(const double *part, int nparts, double *scal, int slot, int mode, int *flag, double eps,
+                            int itr) {
+    if (mode == 1 && flag[0]) return;
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        scal[slot] = (mode == 0 && sh[0] == 0.0) ? 1.0e-16 : sh[0];
+        if (mode == 1) {
+            flag[1] = itr;
+            if (sqrt(sh[0] / scal[0]) < eps) flag[0] = 1;
+        }
+    }
+}
+
+__global__ void k_shift_f(float *a, Geo g, const double *scal, int slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return;
+    const float mean = (float)(scal[slot] / ((double)g.nx * g.ny * g.nz));
+    a[hix(g, i, j, k)] -= mean;
+}
+
 template <typename A, typename B>
 __global__ void k_convert(const A *a, B *b, int n) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1127,6 +1212,38 @@ cudaError_t solve_walls_f(Dev &d, const float *src, XOutF out, int sys, cudaStre
     return solve_walls_mp<float>(d, src, out, sys, s);
 }
 
+cudaError_t sor_solve_m(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
+    const Geo &g = d.g;
+    const dim3 blk(32, 8), grd = cell_grid_m(g, blk);
+    const int nb = std::min(1024, (d.ni + 255) / 256);
+    F8_CUDA_RET(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), s));
+    F8_CUDA_RET(cudaMemsetAsync(d.Phil, 0, (size_t)d.cs * sizeof(float), s));
+    k_sum_part_f<<<nb, 256, 0, s>>>(d.Rhf, d.ni, 0, d.red, g, nullptr); count_launch();
+    k_sum_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 0, 0, d.flag, 0.0, 0); count_launch();
+    const float bx = (float)(1.0 / (g.dx * g.dx)), by = (float)(1.0 / (g.dy * g.dy)), bz = (float)(1.0 / (g.dz * g.dz));
+    int done = 0, it_host[2] = {0, 0};
+    const int chunk = 25;
+    for (int it0 = 1; it0 <= o.sor_itrmax && !done; it0 += chunk) {
+        const int last = std::min(o.sor_itrmax, it0 + chunk - 1);
+        for (int it = it0; it <= last; ++it) {
+            for (int color = 0; color < 2; ++color) {
+                k_sor_color_f<<<grd, blk, 0, s>>>(d.Phif, d.Rdf, d.Rhf, g, color, (float)o.sor_omega, bx, by, bz,
+                                                  d.flag); count_launch();
+            }
+            k_sum_part_f<<<nb, 256, 0, s>>>(d.Rdf, d.ni, 0, d.red, g, d.flag); count_launch();
+            k_sum_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 1, 1, d.flag, o.sor_eps, it); count_launch();
+        }
+        F8_CUDA_RET(cudaMemcpyAsync(it_host, d.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        F8_CUDA_RET(cudaStreamSynchronize(s));
+        done = it_host[0];
+    }
+    *iters = done ? it_host[1] : o.sor_itrmax + 1;
+    k_sum_part_f<<<nb, 256, 0, s>>>(d.Phif, d.ni, 1, d.red, g, nullptr); count_launch();
+    k_sum_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 2, 2, d.flag, 0.0, 0); count_launch();
+    k_shift_f<<<grd, blk, 0, s>>>(d.Phif, g, d.scal, 2); count_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t init_kernels_mixed() {
@@ -1234,7 +1351,7 @@ cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cu
     return cudaGetLastError();
 }
 
-cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStream_t s) {
+cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s) {
     const Geo &g = d.g;
     cudaError_t e;
     const MixConst mc = make_const(g, d.ph);
@@ -1322,13 +1439,16 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, cudaStre
         k_poisson_rhs_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
         count_launch();
     }
-    {
+    if (o.poisson == F8_POISSON_SOR) {
+        if ((e = sor_solve_m(d, o, sor_iters, s))) return e;
+    } else {
+        *sor_iters = -1;
         const XOutF out{d.Phif, d.Phil, 1};
         if (!g.walls) e = solve_periodic_f(d, d.Rhf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rhf, out, SYS_P, s);
         if (e) return e;
     }
-    for (int it = 0; it < d.defect_iters; ++it) {
+    for (int it = 0; o.poisson != F8_POISSON_SOR && it < d.defect_iters; ++it) {
         dim3 blk(32, 8);
         k_defect_df<<<cell_grid_m(g, blk), blk, 0, s>>>(Phi, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
         const XOutF out{d.Phif, d.Phil, 2};

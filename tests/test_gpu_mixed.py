@@ -84,13 +84,10 @@ def test_mixed_newtonian_no_ibm(gpu, oracle):
         assert rel_l2(interior(om[f]), interior(oo[f])) <= VEL_TOL, f
 
 
-def test_mixed_rejects_unbuilt_combinations(gpu):
+def test_mixed_rejects_2d(gpu):
     w = configs.scaled(configs.c1_2d(), 32, 32, 1)
     with pytest.raises(Exception):
         Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED)
-    w3 = configs.scaled(configs.c3_channel(), 32, 16, 16)
-    with pytest.raises(Exception):
-        Solver(gpu, w3.grid, w3.phys, w3.cyls, precision=abi.F8_MIXED, poisson=abi.F8_POISSON_SOR)
 
 
 @pytest.mark.parametrize("precision", [abi.F8_MIXED, abi.F8_FP64])
@@ -121,3 +118,24 @@ def test_mixed_cluster_plane_matches_fp64(gpu, shape):
         assert rel_l2(interior(om[f]), interior(o6[f])) <= VEL_TOL, f
     pm, p6 = interior(om["p"]), interior(o6["p"])
     assert rel_l2(pm - pm.mean(), p6 - p6.mean()) <= 1e-4
+
+
+def test_mixed_sor_variant_matches_fp64_sor(gpu):
+    """The red-black SOR pressure variant (omega 1.8) of the mixed step against
+    the FP64 step's SOR at a common tolerance: both stop at
+    sqrt(sum E^2 / sum R^2) < 1e-6, so they agree to that level."""
+    w = configs.scaled(configs.c3_channel(), 32, 16, 16)
+    w = replace(w, phys=replace(w.phys, sor_eps=1e-6, sor_itrmax=20000))
+    out = {}
+    for prec in (abi.F8_MIXED, abi.F8_FP64):
+        with Solver(gpu, w.grid, w.phys, w.cyls, precision=prec, poisson=abi.F8_POISSON_SOR) as s:
+            s.load(configs.initial_state(w))
+            st, drag = s.step(3)
+            dg = s.diagnostics()
+            out[prec] = (st, drag, s.store(), dg)
+    (sm, dm, om, gm), (s6, d6, o6, g6) = out[abi.F8_MIXED], out[abi.F8_FP64]
+    assert sm == abi.F8_OK and s6 == abi.F8_OK
+    assert 0 < gm.poisson_iters <= 20000 and 0 < g6.poisson_iters <= 20000
+    for f in ("u", "v", "w"):
+        assert rel_l2(interior(om[f]), interior(o6[f])) <= 1e-5, f
+    assert drag_rel(dm, d6) <= 1e-4
