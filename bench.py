@@ -69,8 +69,8 @@ MIXED_STAGE_KERNELS = {
     "newton": ["k_update3_f", "k_newton_fix_f", "k_bc_c_pet_f"],
     "momentum": ["k_momentum3_f"],
     "ibm": ["k_ibm_interp_f", "k_ibm_spread_f", "k_drag_part", "k_drag_final"],
-    "helmholtz": ["3 x (k_xfwd_w, k_plane_walls_s, k_xinv_w)"],
-    "poisson": ["k_poisson_rhs_df", "2 x (k_xfwd_w, k_plane_walls_s, k_xinv_w)", "k_defect_df"],
+    "helmholtz": ["3 x (k_xfwd_w, k_plane_walls_c, k_xinv_w)"],
+    "poisson": ["k_poisson_rhs_df", "2 x (k_xfwd_w, k_plane_walls_c, k_xinv_w)", "k_defect_df"],
     "project": ["k_march_df", "k_bc_set"],
 }
 
@@ -261,10 +261,12 @@ def run_ours(args, w):
     torch.cuda.set_device(local)
     fns = flib.functions()
     prec = {"fp64": abi.F8_FP64, "mixed": abi.F8_MIXED}[args.precision]
+    pois = {"fft": abi.F8_POISSON_FFT, "sor": abi.F8_POISSON_SOR}[args.poisson]
+    pois_name = "fft+tridiagonal" if args.poisson == "fft" else "red-black SOR (omega %.2f)" % w.phys.sor_omega
     st0 = configs.initial_state(w)
     cells = w.cells
     peaks, peak_kind = load_peaks()
-    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as s:
         s.load(st0)
         s.step(args.warmup)
         s.set_timing(True)
@@ -283,7 +285,7 @@ def run_ours(args, w):
     value = cells * args.steps * ws / (ms / 1e3) / 1e6
     # e2e: host arrays in, K single-step calls reading the drag every step, host arrays out
     pst, _keep = pinned_state(st0)
-    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as s:
         s.load(pst)
         s.step(args.warmup)
         torch.cuda.synchronize()
@@ -299,14 +301,14 @@ def run_ours(args, w):
     cmp = None
     if prec == abi.F8_MIXED and not args.no_fp64_compare:
         k64 = min(args.steps, 200)   # the FP64 path runs at ~80 ms/step here
-        with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s64:
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64, poisson=pois) as s64:
             s64.load(st0)
             _, d64w = s64.step(args.warmup)
             s64.set_timing(True)
             s64.timing_reset()
             _, d64 = s64.step(k64)
             t64, st64, n64 = s64.timing()
-        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as sm:
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as sm:
             sm.load(st0)
             _, dmw = sm.step(args.warmup)
             _, dm = sm.step(k64)
@@ -351,7 +353,7 @@ def run_ours(args, w):
             "vs_baseline": None, "dtype": "f64" if prec == abi.F8_FP64 else "f32+f64",
             "data": "synthetic (seeded Poiseuille + noise, C = I)",
             "config": {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": ncyl,
-                       "precision": args.precision, "poisson": "fft+tridiagonal",
+                       "precision": args.precision, "poisson": pois_name,
                        "l2": "inputs larger than L2 (state %.2f GB)" % (sb / 1e9), "parallelism": f"replicas{ws}"},
             "status": int(status), "div_max": diag.div_max, "newton_iters_per_cell_step": diag.newton_iters / (cells * args.steps),
             "drag_last": drag[-1].tolist() if drag is not None else None,
@@ -368,8 +370,8 @@ MIXED_STAGE_LAUNCHES = {
     "newton": {"k_update3_f": 1, "k_newton_fix_f": 1, "k_bc_c_pet_f": 1},
     "momentum": {"k_momentum3_f": 1},
     "ibm": {"k_ibm_interp_f": 1, "k_ibm_spread_f": 1, "k_drag_part": 1, "k_drag_final": 1},
-    "helmholtz": {"k_xfwd_w": 3, "k_plane_walls_s": 3, "k_xinv_w": 3},
-    "poisson": {"k_poisson_rhs_df": 1, "k_xfwd_w": 2, "k_plane_walls_s": 2, "k_xinv_w": 2, "k_defect_df": 1},
+    "helmholtz": {"k_xfwd_w": 3, "k_plane_walls_c": 3, "k_xinv_w": 3},
+    "poisson": {"k_poisson_rhs_df": 1, "k_xfwd_w": 2, "k_plane_walls_c": 2, "k_xinv_w": 2, "k_defect_df": 1},
     "project": {"k_march_df": 1, "k_bc_set": 1},
 }
 
@@ -428,6 +430,8 @@ def main():
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--poisson", default="fft", choices=["fft", "sor"],
+                    help="pressure solver: FFT + tridiagonal (default) or red-black SOR")
     ap.add_argument("--grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
                     help="scale the workload to this grid (small cases for profiling)")
     ap.add_argument("--summarize-ncu", metavar="CSV", help="summarise an ncu --csv log instead of running")
