@@ -65,6 +65,11 @@ module f8_gpu
         real(c_double) :: trc_std
     end type f8_diag
 
+    type, bind(C) :: f8_turb
+        real(c_double) :: k_energy, k_staggered, lambda, re_lambda, epsilon
+        real(c_double) :: l_kolmogorov, t_kolmogorov, u_kolmogorov, ep_energy, trc_mean, trc_std
+    end type f8_turb
+
     interface
         subroutine f8_default_phys(phys) bind(C, name="f8_default_phys")
             import :: f8_phys
@@ -122,6 +127,19 @@ module f8_gpu
             integer(c_int), value :: axis, variant
             type(c_ptr), value :: out
         end function f8_slice
+
+        ! mean_u/v/w: real(8) (1:NX,1:NY,1:NZ) with the TARGET attribute, or c_null_ptr
+        integer(c_int) function f8_turbulence(ctx, mean_u, mean_v, mean_w, out) bind(C, name="f8_turbulence")
+            import :: c_ptr, c_int, f8_turb
+            type(c_ptr), value :: ctx, mean_u, mean_v, mean_w
+            type(f8_turb), intent(out) :: out
+        end function f8_turbulence
+
+        ! energy: real(8) (0:NX)
+        integer(c_int) function f8_spectrum(ctx, mean_u, mean_v, mean_w, energy) bind(C, name="f8_spectrum")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx, mean_u, mean_v, mean_w, energy
+        end function f8_spectrum
 
         integer(c_int) function f8_set_timing(ctx, enable) bind(C, name="f8_set_timing")
             import :: c_ptr, c_int

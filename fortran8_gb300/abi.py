@@ -57,6 +57,12 @@ class Fields(C.Structure):
     _fields_ = [(n, _dp) for n in FIELD_NAMES]
 
 
+class Turb(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("k_energy", "k_staggered", "lambda_", "re_lambda", "epsilon",
+                                          "l_kolmogorov", "t_kolmogorov", "u_kolmogorov", "ep_energy",
+                                          "trc_mean", "trc_std")]
+
+
 class Diag(C.Structure):
     _fields_ = [("step", C.c_int), ("ke", C.c_double), ("cfl", C.c_double),
                 ("trc_min", C.c_double), ("trc_max", C.c_double), ("trc_mean", C.c_double),
@@ -75,6 +81,8 @@ ABI_FUNCTIONS = {
     "diagnostics": (C.c_int, [C.c_void_p, C.POINTER(Diag)]),
     "markers": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _dp]),
     "slice": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    "turbulence": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_void_p]),
+    "spectrum": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
     "strerror": (C.c_char_p, [C.c_int]),
     "destroy": (None, [C.c_void_p]),
     "default_phys": (None, [C.POINTER(Phys)]),

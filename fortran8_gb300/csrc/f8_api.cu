@@ -94,6 +94,9 @@ struct f8_ctx {
     unsigned long long *nan_dev = nullptr;
     double *diag_part = nullptr;      // block partials of the on-device diagnostics
     double *slice_dev = nullptr;      // 18 doubles per point of the largest slice
+    SpecWork spec{};                  // spectrum workspace (first f8_spectrum call)
+    double *mean_dev = nullptr;       // mean velocity fields of f8_turbulence / f8_spectrum
+    double *energy_dev = nullptr;
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -261,7 +264,7 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.flag, 4));
     API_CUDA(c, c->alloc(&d.cnt, 1));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
-    API_CUDA(c, c->alloc(&c->diag_part, diag_partials()));
+    API_CUDA(c, c->alloc(&c->diag_part, std::max(diag_partials(), turb_partials(0))));
     if (g.dim == 3) {
         const size_t np = std::max({(size_t)g.nx * g.ny, (size_t)g.nx * g.nz, (size_t)g.ny * g.nz});
         API_CUDA(c, c->alloc(&c->slice_dev, 18 * np));
@@ -693,6 +696,70 @@ int f8_slice(f8_ctx *c, int axis, int variant, double *out) {
     const int n = slice_points(c->d.g, axis);
     API_CUDA(c, device_slice(c->d, c->precision == F8_MIXED, axis, variant, c->slice_dev, c->s));
     API_CUDA(c, cudaMemcpyAsync(out, c->slice_dev, (size_t)n * 18 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+namespace {
+// upload the optional mean fields; mean[] gets device pointers or nulls
+int upload_means(f8_ctx *c, const double *mu, const double *mv, const double *mw, const double *mean[3]) {
+    const size_t ni = c->d.ni;
+    const double *src[3] = {mu, mv, mw};
+    for (int q = 0; q < 3; ++q) mean[q] = nullptr;
+    if (!mu && !mv && !mw) return F8_OK;
+    if (!c->mean_dev) API_CUDA(c, c->alloc(&c->mean_dev, 3 * ni));
+    for (int q = 0; q < 3; ++q) {
+        if (!src[q]) continue;
+        API_CUDA(c, cudaMemcpyAsync(c->mean_dev + q * ni, src[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        mean[q] = c->mean_dev + q * ni;
+    }
+    return F8_OK;
+}
+}  // namespace
+
+int f8_turbulence(f8_ctx *c, const double *mu, const double *mv, const double *mw, f8_turb *out) {
+    if (!c || !out) return F8_ERR_ARG;
+    if (!c->loaded) return F8_ERR_STATE;
+    if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
+    const double *mean[3];
+    if (int st = upload_means(c, mu, mv, mw, mean)) return st;
+    const bool mixed = c->precision == F8_MIXED;
+    TurbValues t{};
+    API_CUDA(c, device_turbulence(c->d, mixed, mean, c->diag_part, c->d.scal, &t, c->s));
+    DiagValues v{};
+    API_CUDA(c, device_diagnostics(c->d, mixed, c->diag_part, c->d.scal, &v, c->s));
+    std::memset(out, 0, sizeof(*out));
+    out->k_energy = t.k_energy; out->k_staggered = t.k_staggered;
+    out->lambda = t.lambda; out->re_lambda = t.re_lambda; out->epsilon = t.epsilon;
+    out->l_kolmogorov = t.l_kolmogorov; out->t_kolmogorov = t.t_kolmogorov; out->u_kolmogorov = t.u_kolmogorov;
+    out->ep_energy = t.ep_energy; out->trc_mean = v.trc_mean; out->trc_std = v.trc_std;
+    return F8_OK;
+}
+
+int f8_spectrum(f8_ctx *c, const double *mu, const double *mv, const double *mw, double *energy) {
+    if (!c || !energy) return F8_ERR_ARG;
+    if (!c->loaded) return F8_ERR_STATE;
+    if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
+    const Geo &g = c->d.g;
+    const double *mean[3];
+    if (int st = upload_means(c, mu, mv, mw, mean)) return st;
+    SpecWork &w = c->spec;
+    if (!w.pack) {
+        API_CUDA(c, spectrum_kernel_attrs());
+        API_CUDA(c, c->alloc(&w.pack, (size_t)c->d.ni));
+        API_CUDA(c, c->alloc(&w.H, 2 * (size_t)(g.nx / 2 + 1) * g.ny * g.nz));
+        API_CUDA(c, c->alloc(&w.hist, turb_partials(g.nx)));
+        API_CUDA(c, c->alloc(&c->energy_dev, (size_t)g.nx + 1));
+        std::vector<double> tr, ti;
+        const int nn[3] = {g.nx, g.ny, g.nz};
+        for (int a = 0; a < 3; ++a) {
+            make_tw(nn[a], tr, ti);
+            if (int st = upload(c, &w.twr[a], tr)) return st;
+            if (int st = upload(c, &w.twi[a], ti)) return st;
+        }
+    }
+    API_CUDA(c, device_spectrum(c->d, c->precision == F8_MIXED, mean, w, c->energy_dev, c->s));
+    API_CUDA(c, cudaMemcpyAsync(energy, c->energy_dev, ((size_t)g.nx + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
     return F8_OK;
 }

@@ -268,3 +268,226 @@ cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_
 }
 
 }  // namespace f8
+
+// ---------------------------------------------------------------------------
+// Turbulence statistics of all_time_dif (fenep_mpi.f90:2200-2348) and the
+// energy spectrum of energy_single / fft_energy_dif (fenep.f90:1606-1672,
+// fenep_mpi.f90:2567-2667), with U_C = L_C = 1 and nu = 1/Re.  The velocity
+// fluctuation U - <U> (the mean is optional) has the periodic boundary values
+// the reference gives it (PBM), i.e. neighbours wrap in every direction.
+#include "f8_fft.cuh"
+
+namespace f8 {
+namespace {
+
+struct TurbIn {
+    DiagSliceIn st;
+    const double *mean[3];   // interior mean fields, or null
+    int d3;
+};
+
+__device__ inline double fluct(const TurbIn &in, const Geo &g, int c, int i, int j, int k) {
+    i = wrapx(g, i); j = wrapy(g, j); k = wrapz(g, k);
+    double v = slice_vel(in.st, c, hix(g, i, j, k));
+    if (in.mean[c]) v -= in.mean[c][qix(g, i, j, k)];
+    return v;
+}
+
+enum { T_U2, T_V2, T_W2, T_GU, T_GV, T_GW, T_S2, T_KS, T_EP, T_N };
+
+__global__ void __launch_bounds__(DIAG_THREADS) k_turb_pass(TurbIn in, Geo g, double dep, double lp2, double *part) {
+    __shared__ double sh[DIAG_THREADS];
+    const long ni = (long)g.nx * g.ny * g.nz;
+    double a[T_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)DIAG_BLOCKS * DIAG_THREADS) {
+        const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
+        auto U = [&](int ii, int jj, int kk) { return fluct(in, g, 0, ii, jj, kk); };
+        auto V = [&](int ii, int jj, int kk) { return fluct(in, g, 1, ii, jj, kk); };
+        auto W = [&](int ii, int jj, int kk) { return fluct(in, g, 2, ii, jj, kk); };
+        const double ur = (U(i, j, k) + U(i - 1, j, k)) / 2.0, vr = (V(i, j, k) + V(i, j - 1, k)) / 2.0,
+                     wr = (W(i, j, k) + W(i, j, k - 1)) / 2.0;
+        a[T_U2] += ur * ur; a[T_V2] += vr * vr; a[T_W2] += wr * wr;
+        const double gu = (U(i, j, k) - U(i - 1, j, k)) / dX, gv = (V(i, j, k) - V(i, j - 1, k)) / dY,
+                     gw = (W(i, j, k) - W(i, j, k - 1)) / dZ;
+        a[T_GU] += gu * gu; a[T_GV] += gv * gv; a[T_GW] += gw * gw;
+        double D[3][3];
+        D[0][0] = gu;
+        D[0][1] = (U(i, j + 1, k) - U(i, j - 1, k) + U(i - 1, j + 1, k) - U(i - 1, j - 1, k)) / (4 * dY);
+        D[0][2] = (U(i, j, k + 1) - U(i, j, k - 1) + U(i - 1, j, k + 1) - U(i - 1, j, k - 1)) / (4 * dZ);
+        D[1][0] = (V(i + 1, j, k) - V(i - 1, j, k) + V(i + 1, j - 1, k) - V(i - 1, j - 1, k)) / (4 * dX);
+        D[1][1] = gv;
+        D[1][2] = (V(i, j, k + 1) - V(i, j, k - 1) + V(i, j - 1, k + 1) - V(i, j - 1, k - 1)) / (4 * dZ);
+        D[2][0] = (W(i + 1, j, k) - W(i - 1, j, k) + W(i + 1, j, k - 1) - W(i - 1, j, k - 1)) / (4 * dX);
+        D[2][1] = (W(i, j + 1, k) - W(i, j - 1, k) + W(i, j + 1, k - 1) - W(i, j - 1, k - 1)) / (4 * dY);
+        D[2][2] = gw;
+        double s2 = 0.0;
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) {
+                const double sv = D[p][q] + D[q][p];
+                s2 += sv * sv;
+            }
+        a[T_S2] += s2;
+        const int h = hix(g, i, j, k);
+        const double us = slice_vel(in.st, 0, h), vs = slice_vel(in.st, 1, h), ws = slice_vel(in.st, 2, h);
+        a[T_KS] += us * us + vs * vs + ws * ws;
+        // elastic energy 0.5 (1-beta)/(Re Wi) (L^2-3) log f(C)
+        const double tr = slice_c(in.st, 0, h) + slice_c(in.st, 3, h) + slice_c(in.st, 5, h);
+        a[T_EP] += dep * log((lp2 - 3.0) / (lp2 - tr));
+    }
+    double r[T_N];
+    for (int m = 0; m < T_N; ++m) r[m] = block_reduce(a[m], sh, Add());
+    if (threadIdx.x == 0)
+        for (int m = 0; m < T_N; ++m) part[(size_t)blockIdx.x * T_N + m] = r[m];
+}
+
+__global__ void k_sum_parts(const double *part, int np, int nv, double *out) {
+    __shared__ double sh[DIAG_THREADS];
+    for (int m = 0; m < nv; ++m) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < DIAG_BLOCKS; b += DIAG_THREADS) v += part[(size_t)b * np + m];
+        const double r = block_reduce(v, sh, Add());
+        if (threadIdx.x == 0) out[m] = r;
+    }
+}
+
+// interior fluctuation of component c, packed (x fastest) for the transform
+__global__ void k_pack_fluct(TurbIn in, Geo g, int c, double *dst) {
+    const long ni = (long)g.nx * g.ny * g.nz;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni) return;
+    const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
+    dst[t] = fluct(in, g, c, i, j, k);
+}
+
+// shell binning of |u_hat|^2 / N^2 (spectrum [k][j][kx] complex): nint(|k|)
+// with the half-spectrum weights of energy_single (1/2 at kx = 0 and NX/2,
+// 1 elsewhere); per-block histograms accumulated over the components
+__global__ void __launch_bounds__(DIAG_THREADS) k_spec_bin(const double *H, Geo g, int nbins, double inv_n2,
+                                                           double *hist, int accumulate) {
+    extern __shared__ double hs[];
+    for (int b = threadIdx.x; b < nbins; b += DIAG_THREADS) hs[b] = 0.0;
+    __syncthreads();
+    const int nxh = g.nx / 2 + 1;
+    const long nm = (long)nxh * g.ny * g.nz;
+    // each block owns a contiguous range of modes and bins them in order
+    const long per = (nm + DIAG_BLOCKS - 1) / DIAG_BLOCKS;
+    const long m0 = (long)blockIdx.x * per, m1 = min(nm, m0 + per);
+    if (threadIdx.x == 0) {
+        for (long m = m0; m < m1; ++m) {
+            const int ii = (int)(m % nxh), jj = (int)((m / nxh) % g.ny), kk = (int)(m / ((long)nxh * g.ny));
+            const double kx = ii, ky = jj <= g.ny / 2 ? jj : jj - g.ny, kz = kk <= g.nz / 2 ? kk : kk - g.nz;
+            const int idx = min(nbins - 1, (int)lround(sqrt(kx * kx + ky * ky + kz * kz)));
+            const double re = H[2 * m], im = H[2 * m + 1];
+            const double e = (re * re + im * im) * inv_n2;
+            hs[idx] += (ii == 0 || ii == g.nx / 2) ? e / 2.0 : e / 2.0 * 2.0;
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbins; b += DIAG_THREADS)
+        hist[(size_t)blockIdx.x * nbins + b] = (accumulate ? hist[(size_t)blockIdx.x * nbins + b] : 0.0) + hs[b];
+}
+
+__global__ void k_hist_final(const double *hist, int nbins, double *out) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
+        double v = 0.0;
+        for (int q = 0; q < DIAG_BLOCKS; ++q) v += hist[(size_t)q * nbins + b];
+        out[b] = v;
+    }
+}
+
+}  // namespace
+
+size_t turb_partials(int nx) { return (size_t)DIAG_BLOCKS * std::max<int>(T_N, nx + 1); }
+
+cudaError_t device_turbulence(Dev &d, bool mixed, const double *const mean[3], double *part, double *out,
+                              TurbValues *res, cudaStream_t s) {
+    const Geo &g = d.g;
+    TurbIn in{};
+    in.st.cs = d.cs;
+    in.st.mixed = mixed ? 1 : 0;
+    if (mixed) {
+        in.st.Uh = d.Uf; in.st.Ul = d.Ul; in.st.Vh = d.Vf; in.st.Vl = d.Vl; in.st.Wh = d.Wf; in.st.Wl = d.Wl;
+        in.st.Cf = d.Cf;
+    } else {
+        in.st.U = d.U; in.st.V = d.V; in.st.W = d.W;
+        in.st.C = d.C;
+    }
+    for (int c = 0; c < 3; ++c) in.mean[c] = mean ? mean[c] : nullptr;
+    in.d3 = 1;
+    const double dep = 0.5 * (1.0 - d.ph.beta) / d.ph.re / d.ph.wi * (d.ph.lp2 - 3.0);
+    k_turb_pass<<<DIAG_BLOCKS, DIAG_THREADS, 0, s>>>(in, g, dep, d.ph.lp2, part); count_launch();
+    k_sum_parts<<<1, DIAG_THREADS, 0, s>>>(part, T_N, T_N, out); count_launch();
+    double h[T_N];
+    F8_CUDA_RET(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
+    F8_CUDA_RET(cudaStreamSynchronize(s));
+    const double N = (double)g.nx * g.ny * g.nz, nu = 1.0 / d.ph.re;
+    const double urms = h[T_U2] / N, vrms = h[T_V2] / N, wrms = h[T_W2] / N;
+    const double ugrad = h[T_GU] / N, vgrad = h[T_GV] / N, wgrad = h[T_GW] / N;
+    const double all_rms = (urms + vrms + wrms) / 3.0, all_grad = (ugrad + vgrad + wgrad) / 3.0;
+    res->epsilon = nu / 2.0 * h[T_S2] / N;
+    res->l_kolmogorov = std::pow(nu * nu * nu / res->epsilon, 0.25);
+    res->t_kolmogorov = std::pow(nu / res->epsilon, 0.5);
+    res->u_kolmogorov = std::pow(nu * res->epsilon, 0.25);
+    res->lambda = std::sqrt(all_rms / all_grad);
+    res->re_lambda = std::sqrt(all_rms) * res->lambda / nu;
+    res->k_energy = (urms + vrms + wrms) / 2.0;
+    res->k_staggered = h[T_KS] / (2.0 * N);
+    res->ep_energy = h[T_EP] / N;
+    return cudaGetLastError();
+}
+
+cudaError_t device_spectrum(Dev &d, bool mixed, const double *const mean[3], SpecWork &w, double *energy_dev,
+                            cudaStream_t s) {
+    const Geo &g = d.g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
+    TurbIn in{};
+    in.st.cs = d.cs;
+    in.st.mixed = mixed ? 1 : 0;
+    if (mixed) {
+        in.st.Uh = d.Uf; in.st.Ul = d.Ul; in.st.Vh = d.Vf; in.st.Vl = d.Vl; in.st.Wh = d.Wf; in.st.Wl = d.Wl;
+    } else {
+        in.st.U = d.U; in.st.V = d.V; in.st.W = d.W;
+    }
+    for (int c = 0; c < 3; ++c) in.mean[c] = mean ? mean[c] : nullptr;
+    const long ni = (long)nx * ny * nz;
+    const int nbins = nx + 1;
+    const double inv_n2 = 1.0 / ((double)ni * (double)ni);
+    for (int c = 0; c < 3; ++c) {
+        k_pack_fluct<<<(unsigned)((ni + 255) / 256), 256, 0, s>>>(in, g, c, w.pack); count_launch();
+        {
+            const int tpp = std::max(nx / 2, 1), ppc = std::max(1, 256 / tpp);
+            const int npp = ny / 2, total = npp * nz;
+            const size_t smem = (size_t)ppc * 2 * nx * sizeof(Cx<double>);
+            k_fft_x_fwd<double, double><<<(total + ppc - 1) / ppc, ppc * tpp, smem, s>>>(w.pack, w.H, nx, ny, 1, ny, npp, nz,
+                                                                                         w.twr[0], w.twi[0]); count_launch();
+        }
+        DivideSpec none{};
+        {
+            const int tx = std::max(1, std::min(32, 2048 / ny));
+            const size_t smem = (size_t)2 * ny * tx * sizeof(Cx<double>);
+            k_fft_lines<double><<<dim3((nxh + tx - 1) / tx, nz), 256, smem, s>>>(w.H, ny, nxh, nxh, nxh * ny, tx, w.twr[1],
+                                                                                  w.twi[1], -1, 0, none); count_launch();
+        }
+        {
+            const int tx = std::max(1, std::min(32, 2048 / nz));
+            const size_t smem = (size_t)2 * nz * tx * sizeof(Cx<double>);
+            k_fft_lines<double><<<dim3((nxh + tx - 1) / tx, ny), 256, smem, s>>>(w.H, nz, nxh * ny, nxh, nxh, tx, w.twr[2],
+                                                                                  w.twi[2], -1, 0, none); count_launch();
+        }
+        k_spec_bin<<<DIAG_BLOCKS, DIAG_THREADS, (size_t)nbins * sizeof(double), s>>>(w.H, g, nbins, inv_n2, w.hist,
+                                                                                    c > 0 ? 1 : 0); count_launch();
+    }
+    k_hist_final<<<(nbins + 255) / 256, 256, 0, s>>>(w.hist, nbins, energy_dev); count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t spectrum_kernel_attrs() {
+    const int big = 200 * 1024;
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_x_fwd<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    F8_CUDA_RET(cudaFuncSetAttribute(k_spec_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    return cudaSuccess;
+}
+
+}  // namespace f8

@@ -109,6 +109,22 @@ struct DiagSliceIn {
     int cs, mixed;
 };
 int slice_points(const Geo &g, int axis);
+// turbulence statistics and energy spectrum (f8_diag.cu)
+struct TurbValues {
+    double k_energy, k_staggered, lambda, re_lambda, epsilon, l_kolmogorov, t_kolmogorov, u_kolmogorov, ep_energy;
+};
+struct SpecWork {       // FP64 transform workspace of the spectrum (allocated on first use)
+    double *pack;       // one interior field, packed
+    double *H;          // half spectrum [k][j][kx] complex
+    double *twr[3], *twi[3];
+    double *hist;       // per-block histograms
+};
+size_t turb_partials(int nx);
+cudaError_t device_turbulence(Dev &d, bool mixed, const double *const mean[3], double *part, double *out,
+                              TurbValues *res, cudaStream_t s);
+cudaError_t device_spectrum(Dev &d, bool mixed, const double *const mean[3], SpecWork &w, double *energy_dev,
+                            cudaStream_t s);
+cudaError_t spectrum_kernel_attrs();
 cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_out, cudaStream_t s);
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)

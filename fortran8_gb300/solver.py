@@ -184,6 +184,28 @@ class Solver:
         self._check(self._fns["slice"](self._h, axis, variant, _ptr(out)))
         return out
 
+    def _means(self, mean):
+        if mean is None:
+            return (None, None, None), None
+        arrs = [np.ascontiguousarray(m, dtype=np.float64) for m in mean]
+        return tuple(_ptr(a) for a in arrs), arrs
+
+    def turbulence(self, mean=None) -> abi.Turb:
+        """all_time_dif statistics; mean = (U, V, W) interior mean fields or None."""
+        ptrs, keep = self._means(mean)
+        t = abi.Turb()
+        self._check(self._fns["turbulence"](self._h, *ptrs, C.byref(t)))
+        del keep
+        return t
+
+    def spectrum(self, mean=None) -> np.ndarray:
+        """Shell-binned energy spectrum E[0..NX] of energy_single."""
+        ptrs, keep = self._means(mean)
+        e = np.zeros(self.grid.nx + 1)
+        self._check(self._fns["spectrum"](self._h, *ptrs, _ptr(e)))
+        del keep
+        return e
+
     def markers(self) -> np.ndarray:
         n = C.c_int()
         self._check(self._fns["markers"](self._h, C.byref(n), None))

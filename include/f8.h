@@ -131,6 +131,18 @@ typedef struct f8_diag {
                                    mean first (fenep.f90:2316-2317)              */
 } f8_diag;
 
+/* Turbulence statistics of all_time_dif (fenep_mpi.f90:2200-2348), scales
+ * U_C = L_C = 1, nu = 1/Re.  "rms" in the reference is a mean square. */
+typedef struct f8_turb {
+    double k_energy;            /* (<u'^2> + <v'^2> + <w'^2>)/2 on cell centres     */
+    double k_staggered;         /* sum(U^2 + V^2 + W^2) / (2 N) of the state        */
+    double lambda, re_lambda;   /* Taylor length sqrt(<u'^2>/<(du'/dx)^2>), Re_lambda */
+    double epsilon;             /* nu/2 <S_ij S_ij>, S = D + D^T                     */
+    double l_kolmogorov, t_kolmogorov, u_kolmogorov;
+    double ep_energy;           /* <0.5 (1-beta)/(Re Wi) (L^2-3) log f(C)>           */
+    double trc_mean, trc_std;
+} f8_turb;
+
 typedef struct f8_ctx f8_ctx;
 
 /* Create a solver context.  cyls may be NULL when ncyl == 0 (no IBM; the
@@ -171,6 +183,19 @@ int f8_diagnostics(f8_ctx *ctx, f8_diag *out);
  * |Omega|^2/2, trC, C(6); scales U_C = L_C = 1.  out holds 18 * points
  * doubles (host).  3D only (F8_ERR_UNSUPPORTED in 2D). */
 int f8_slice(f8_ctx *ctx, int axis, int variant, double *out);
+
+/* Turbulence statistics of the current state (all_time_dif).  mean_u/v/w are
+ * host interior fields (1:NX,1:NY,1:NZ) subtracted from the velocity, or NULL
+ * (the reference's 'same' key).  3D only. */
+int f8_turbulence(f8_ctx *ctx, const double *mean_u, const double *mean_v, const double *mean_w,
+                  f8_turb *out);
+
+/* Shell-binned energy spectrum of energy_single (fenep.f90:1606-1672) /
+ * fft_energy_dif (fenep_mpi.f90:2567-2667): energy[0..NX] (host, NX+1
+ * doubles) from the FP64 3D transform of the (optionally mean-subtracted)
+ * velocity on the device; the bins sum to the staggered kinetic energy
+ * (Parseval).  3D only. */
+int f8_spectrum(f8_ctx *ctx, const double *mean_u, const double *mean_v, const double *mean_w, double *energy);
 
 /* Number of Lagrangian markers per z-plane and their host-side positions
  * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */

@@ -1654,6 +1654,117 @@ int f8o_slice(f8_ctx *ctx, int axis, int variant, double *out) {
     return F8_OK;
 }
 
+// all_time_dif (fenep_mpi.f90:2200-2348) with U_C = L_C = 1, nu = 1/Re; the
+// fluctuation gets the periodic boundary values of PBM
+int f8o_turbulence(f8_ctx *ctx, const double *mu, const double *mv, const double *mw, f8_turb *out) {
+    if (!ctx || !out) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (c.dim != 3) return F8_ERR_UNSUPPORTED;
+    const int NX = c.NX, NY = c.NY, NZ = c.NZ;
+    const double *mean[3] = {mu, mv, mw};
+    const std::vector<double> *F[3] = {&c.U, &c.V, &c.W};
+    auto wrap = [](int a, int n) { return a < 1 ? a + n : (a > n ? a - n : a); };
+    auto fl = [&](int q, int i, int j, int k) {
+        i = wrap(i, NX); j = wrap(j, NY); k = wrap(k, NZ);
+        double v = (*F[q])[c.hidx(i, j, k)];
+        if (mean[q]) v -= mean[q][(size_t)(i - 1) + NX * ((size_t)(j - 1) + (size_t)NY * (k - 1))];
+        return v;
+    };
+    const double dX = c.dX, dY = c.dY, dZ = c.dZ, N = (double)NX * NY * NZ, nu = 1.0 / c.ph.re;
+    double u2 = 0, v2 = 0, w2 = 0, gu2 = 0, gv2 = 0, gw2 = 0, s2 = 0, ks = 0, ep = 0, tsum = 0;
+    const double dep = 0.5 * (1.0 - c.ph.beta) / c.ph.re / c.ph.wi * (c.ph.lp2 - 3.0);
+    for (int k = 1; k <= NZ; ++k)
+        for (int j = 1; j <= NY; ++j)
+            for (int i = 1; i <= NX; ++i) {
+                auto U = [&](int a, int b, int cc) { return fl(0, a, b, cc); };
+                auto V = [&](int a, int b, int cc) { return fl(1, a, b, cc); };
+                auto W = [&](int a, int b, int cc) { return fl(2, a, b, cc); };
+                const double ur = (U(i, j, k) + U(i - 1, j, k)) / 2.0, vr = (V(i, j, k) + V(i, j - 1, k)) / 2.0,
+                             wr = (W(i, j, k) + W(i, j, k - 1)) / 2.0;
+                u2 += ur * ur; v2 += vr * vr; w2 += wr * wr;
+                const double gu = (U(i, j, k) - U(i - 1, j, k)) / dX, gv = (V(i, j, k) - V(i, j - 1, k)) / dY,
+                             gw = (W(i, j, k) - W(i, j, k - 1)) / dZ;
+                gu2 += gu * gu; gv2 += gv * gv; gw2 += gw * gw;
+                double D[3][3];
+                D[0][0] = gu;
+                D[0][1] = (U(i, j + 1, k) - U(i, j - 1, k) + U(i - 1, j + 1, k) - U(i - 1, j - 1, k)) / (4 * dY);
+                D[0][2] = (U(i, j, k + 1) - U(i, j, k - 1) + U(i - 1, j, k + 1) - U(i - 1, j, k - 1)) / (4 * dZ);
+                D[1][0] = (V(i + 1, j, k) - V(i - 1, j, k) + V(i + 1, j - 1, k) - V(i - 1, j - 1, k)) / (4 * dX);
+                D[1][1] = gv;
+                D[1][2] = (V(i, j, k + 1) - V(i, j, k - 1) + V(i, j - 1, k + 1) - V(i, j - 1, k - 1)) / (4 * dZ);
+                D[2][0] = (W(i + 1, j, k) - W(i - 1, j, k) + W(i + 1, j, k - 1) - W(i - 1, j, k - 1)) / (4 * dX);
+                D[2][1] = (W(i, j + 1, k) - W(i, j - 1, k) + W(i, j + 1, k - 1) - W(i, j - 1, k - 1)) / (4 * dY);
+                D[2][2] = gw;
+                for (int p = 0; p < 3; ++p)
+                    for (int q = 0; q < 3; ++q) s2 += (D[p][q] + D[q][p]) * (D[p][q] + D[q][p]);
+                const size_t h = c.hidx(i, j, k);
+                ks += c.U[h] * c.U[h] + c.V[h] * c.V[h] + c.W[h] * c.W[h];
+                const double *cc = &c.C[6 * h];
+                const double tr = cc[0] + cc[3] + cc[5];
+                ep += dep * std::log((c.ph.lp2 - 3.0) / (c.ph.lp2 - tr));
+                tsum += tr;
+            }
+    const double urms = u2 / N, vrms = v2 / N, wrms = w2 / N;
+    const double all_rms = (urms + vrms + wrms) / 3.0, all_grad = (gu2 / N + gv2 / N + gw2 / N) / 3.0;
+    std::memset(out, 0, sizeof(*out));
+    out->epsilon = nu / 2.0 * s2 / N;
+    out->l_kolmogorov = std::pow(nu * nu * nu / out->epsilon, 0.25);
+    out->t_kolmogorov = std::pow(nu / out->epsilon, 0.5);
+    out->u_kolmogorov = std::pow(nu * out->epsilon, 0.25);
+    out->lambda = std::sqrt(all_rms / all_grad);
+    out->re_lambda = std::sqrt(all_rms) * out->lambda / nu;
+    out->k_energy = (urms + vrms + wrms) / 2.0;
+    out->k_staggered = ks / (2.0 * N);
+    out->ep_energy = ep / N;
+    out->trc_mean = tsum / N;
+    double sd = 0;
+    for (int k = 1; k <= NZ; ++k)
+        for (int j = 1; j <= NY; ++j)
+            for (int i = 1; i <= NX; ++i) {
+                const double *cc = &c.C[6 * c.hidx(i, j, k)];
+                const double d = cc[0] + cc[3] + cc[5] - out->trc_mean;
+                sd += d * d;
+            }
+    out->trc_std = std::sqrt(sd / N);
+    return F8_OK;
+}
+
+// energy_single (fenep.f90:1606-1672): shell-binned |u_hat|^2 / N^2 of the
+// (optionally mean-subtracted) velocity, half-spectrum weights 1/2 at kx = 0
+// and NX/2
+int f8o_spectrum(f8_ctx *ctx, const double *mu, const double *mv, const double *mw, double *energy) {
+    if (!ctx || !energy) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (c.dim != 3) return F8_ERR_UNSUPPORTED;
+    const int NX = c.NX, NY = c.NY, NZ = c.NZ, NXH = NX / 2 + 1;
+    const double *mean[3] = {mu, mv, mw};
+    const std::vector<double> *F[3] = {&c.U, &c.V, &c.W};
+    std::fill(energy, energy + NX + 1, 0.0);
+    const double N = (double)NX * NY * NZ;
+    for (int q = 0; q < 3; ++q) {
+        std::vector<double> src((size_t)NX * NY * NZ), H(2 * (size_t)NXH * NY * NZ);
+        for (int k = 1; k <= NZ; ++k)
+            for (int j = 1; j <= NY; ++j)
+                for (int i = 1; i <= NX; ++i) {
+                    const size_t o = (size_t)(i - 1) + NX * ((size_t)(j - 1) + (size_t)NY * (k - 1));
+                    src[o] = (*F[q])[c.hidx(i, j, k)] - (mean[q] ? mean[q][o] : 0.0);
+                }
+        fft_x_forward(c, src, 1, NY, H);
+        fft_y(c, H, NY, -1);
+        fft_z(c, H, NY, -1);
+        for (int k = 0; k < NZ; ++k)
+            for (int j = 0; j < NY; ++j)
+                for (int i = 0; i < NXH; ++i) {
+                    const double kx = i, ky = j <= NY / 2 ? j : j - NY, kz = k <= NZ / 2 ? k : k - NZ;
+                    const int idx = std::min(NX, (int)std::lround(std::sqrt(kx * kx + ky * ky + kz * kz)));
+                    const size_t o = 2 * ((size_t)i + NXH * ((size_t)j + (size_t)NY * k));
+                    const double e = (H[o] * H[o] + H[o + 1] * H[o + 1]) / (N * N);
+                    energy[idx] += (i == 0 || i == NX / 2) ? e / 2.0 : e / 2.0 * 2.0;
+                }
+    }
+    return F8_OK;
+}
+
 int f8o_markers(f8_ctx *ctx, int *n, double *xy) {
     if (!ctx) return F8_ERR_ARG;
     OCtx &c = *reinterpret_cast<OCtx *>(ctx);

@@ -170,3 +170,23 @@ def test_slice_matches_oracle(gpu, oracle, precision, tol):
             cols = list(cols)
             scale = np.max(np.abs(o[:, cols])) + 1e-30
             assert np.max(np.abs(g[:, cols] - o[:, cols])) / scale <= tol, cols
+
+
+@pytest.mark.parametrize("precision,tol", [(abi.F8_FP64, 1e-10), (abi.F8_MIXED, 1e-5)])
+@pytest.mark.parametrize("with_mean", [False, True])
+def test_turbulence_and_spectrum_match_oracle(gpu, oracle, precision, tol, with_mean):
+    """f8_turbulence / f8_spectrum on the device against the oracle's sums."""
+    w = small("c3_channel")
+    rng = np.random.default_rng(11)
+    mean = tuple(0.05 * rng.random(w.grid.interior_shape) for _ in range(3)) if with_mean else None
+    res = {}
+    for name, fns, prec in (("gpu", gpu, precision), ("oracle", oracle, abi.F8_FP64)):
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+            s.load(configs.initial_state(w))
+            s.step(5)
+            res[name] = (s.turbulence(mean), s.spectrum(mean))
+    (tg, eg), (to, eo) = res["gpu"], res["oracle"]
+    for f, _ in abi.Turb._fields_:
+        a, b = getattr(tg, f), getattr(to, f)
+        assert abs(a - b) <= tol * max(abs(b), 1e-300), (f, a, b)
+    assert np.max(np.abs(eg - eo)) <= tol * np.max(np.abs(eo))
