@@ -188,5 +188,16 @@ def test_turbulence_and_spectrum_match_oracle(gpu, oracle, precision, tol, with_
     (tg, eg), (to, eo) = res["gpu"], res["oracle"]
     for f, _ in abi.Turb._fields_:
         a, b = getattr(tg, f), getattr(to, f)
+        if f == "ep_energy" and precision == abi.F8_MIXED:
+            # near C = I, log f(C) ~ (trC - 3)/(L^2 - 3) resolves trC - 3 only to
+            # the FP32 rounding of C: compare with an absolute trC error of 1e-6
+            ph = w.phys
+            assert abs(a - b) <= 0.5 * (1 - ph.beta) / (ph.re * ph.wi) * 1e-6, (f, a, b)
+            continue
+        if f in ("trc_mean", "trc_std") and precision == abi.F8_MIXED:
+            # FP32 C: trC carries an absolute rounding of ~1e-7 (its spread after
+            # 5 steps from C = I is itself only ~4e-6)
+            assert abs(a - b) <= 1e-6, (f, a, b)
+            continue
         assert abs(a - b) <= tol * max(abs(b), 1e-300), (f, a, b)
     assert np.max(np.abs(eg - eo)) <= tol * np.max(np.abs(eo))
