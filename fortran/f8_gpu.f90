@@ -141,6 +141,21 @@ module f8_gpu
             type(c_ptr), value :: ctx, mean_u, mean_v, mean_w, energy
         end function f8_spectrum
 
+        ! mode 1: sums of U, V, W and centre-line probes; mode 2: squared fluctuations
+        integer(c_int) function f8_stats_begin(ctx, mode, mean_u, mean_v, mean_w, max_steps) &
+                bind(C, name="f8_stats_begin")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx, mean_u, mean_v, mean_w
+            integer(c_int), value :: mode, max_steps
+        end function f8_stats_begin
+
+        ! probes: real(8) (NZ, steps, 3)
+        integer(c_int) function f8_stats_read(ctx, sum_u, sum_v, sum_w, probes, nsteps) bind(C, name="f8_stats_read")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx, sum_u, sum_v, sum_w, probes
+            integer(c_int), intent(out) :: nsteps
+        end function f8_stats_read
+
         integer(c_int) function f8_set_timing(ctx, enable) bind(C, name="f8_set_timing")
             import :: c_ptr, c_int
             type(c_ptr), value :: ctx

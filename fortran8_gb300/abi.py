@@ -83,6 +83,8 @@ ABI_FUNCTIONS = {
     "slice": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "turbulence": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_void_p]),
     "spectrum": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+    "stats_begin": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_int]),
+    "stats_read": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, C.POINTER(C.c_int)]),
     "strerror": (C.c_char_p, [C.c_int]),
     "destroy": (None, [C.c_void_p]),
     "default_phys": (None, [C.POINTER(Phys)]),

@@ -97,6 +97,8 @@ struct f8_ctx {
     SpecWork spec{};                  // spectrum workspace (first f8_spectrum call)
     double *mean_dev = nullptr;       // mean velocity fields of f8_turbulence / f8_spectrum
     double *energy_dev = nullptr;
+    int stats_mode = 0, stats_n = 0, stats_max = 0;   // running statistics (f8_stats_begin)
+    double *stats_sum = nullptr, *stats_probe = nullptr;
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -125,6 +127,8 @@ struct f8_ctx {
         tot0 = tot1 = nullptr;
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
+        if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
+        stats_probe = nullptr;
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
@@ -596,6 +600,11 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         double *dg = (ncyl && drag) ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
         cudaError_t e = mixed ? step_mixed(d, o, dg, &sor_iters, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
         if (e != cudaSuccess) return fail(c, e, "step");
+        if (c->stats_mode) {
+            API_CUDA(c, device_stats_accum(d, mixed, c->stats_mode, c->mean_dev, c->stats_sum, c->stats_probe,
+                                           c->stats_n, c->stats_max, c->s));
+            c->stats_n += 1;
+        }
         c->last_poisson_iters = sor_iters;
         if (c->poisson == F8_POISSON_SOR && sor_iters > c->phys.sor_itrmax) worst = std::max(worst, (int)F8_WARN_SOR);
         c->step += 1;
@@ -761,6 +770,51 @@ int f8_spectrum(f8_ctx *c, const double *mu, const double *mv, const double *mw,
     API_CUDA(c, device_spectrum(c->d, c->precision == F8_MIXED, mean, w, c->energy_dev, c->s));
     API_CUDA(c, cudaMemcpyAsync(energy, c->energy_dev, ((size_t)g.nx + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+int f8_stats_begin(f8_ctx *c, int mode, const double *mu, const double *mv, const double *mw, int max_steps) {
+    if (!c || mode < 0 || mode > 2 || max_steps < 0) return F8_ERR_ARG;
+    if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
+    if (mode == 2 && (!mu || !mv || !mw)) return F8_ERR_ARG;
+    const size_t ni = c->d.ni;
+    c->stats_mode = 0;
+    c->stats_n = 0;
+    if (mode == 0) return F8_OK;
+    if (!c->stats_sum) API_CUDA(c, c->alloc(&c->stats_sum, 3 * ni));
+    API_CUDA(c, cudaMemsetAsync(c->stats_sum, 0, 3 * ni * sizeof(double), c->s));
+    if (mode == 1 && max_steps > c->stats_max) {
+        if (c->stats_probe) cudaFree(c->stats_probe);
+        c->stats_probe = nullptr;
+        c->stats_max = 0;
+        API_CUDA(c, cudaMalloc(&c->stats_probe, (size_t)3 * max_steps * c->d.g.nz * sizeof(double)));
+        c->stats_max = max_steps;
+    }
+    if (mode == 2) {
+        const double *mean[3];
+        if (int st = upload_means(c, mu, mv, mw, mean)) return st;
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    c->stats_mode = mode;
+    return F8_OK;
+}
+
+int f8_stats_read(f8_ctx *c, double *su, double *sv, double *sw, double *probes, int *nsteps) {
+    if (!c) return F8_ERR_ARG;
+    const size_t ni = c->d.ni;
+    double *dst[3] = {su, sv, sw};
+    for (int q = 0; q < 3; ++q)
+        if (dst[q] && c->stats_sum)
+            API_CUDA(c, cudaMemcpyAsync(dst[q], c->stats_sum + q * ni, ni * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    const int n = std::min(c->stats_n, c->stats_max);
+    if (probes && c->stats_probe) {
+        const size_t per = (size_t)c->stats_max * c->d.g.nz;
+        for (int q = 0; q < 3; ++q)
+            API_CUDA(c, cudaMemcpyAsync(probes + (size_t)q * n * c->d.g.nz, c->stats_probe + q * per,
+                                        (size_t)n * c->d.g.nz * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    if (nsteps) *nsteps = c->stats_n;
     return F8_OK;
 }
 

@@ -491,3 +491,55 @@ cudaError_t spectrum_kernel_attrs() {
 }
 
 }  // namespace f8
+
+// ---------------------------------------------------------------------------
+// Running statistics after each step (fenep_mpi.f90:2934-2941, 3054-3056):
+// mode 1 sums U, V, W and records the centre-line probes U_step(k, n) =
+// (U(NX/2, NY/2, k) + U(NX/2-1, NY/2, k))/2 (V over j, W over k alike);
+// mode 2 sums the squared fluctuations about given mean fields.
+namespace f8 {
+namespace {
+
+__global__ void k_stats_accum(DiagSliceIn st, Geo g, int mode, const double *mean, double *sums, double *probes,
+                              int n, int max_steps) {
+    const long ni = (long)g.nx * g.ny * g.nz;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni) return;
+    const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
+    const int h = hix(g, i, j, k);
+    for (int c = 0; c < 3; ++c) {
+        const double v = slice_vel(st, c, h);
+        if (mode == 1) {
+            sums[(size_t)c * ni + t] += v;
+        } else {
+            const double d = v - mean[(size_t)c * ni + t];
+            sums[(size_t)c * ni + t] += d * d;
+        }
+    }
+    if (mode == 1 && i == g.nx / 2 && j == g.ny / 2 && n < max_steps) {
+        const int off[3] = {1, g.sx, g.sx * g.sy};
+        for (int c = 0; c < 3; ++c)
+            probes[((size_t)c * max_steps + n) * g.nz + (k - 1)] =
+                (slice_vel(st, c, h) + slice_vel(st, c, h - off[c])) / 2.0;
+    }
+}
+
+}  // namespace
+
+cudaError_t device_stats_accum(Dev &d, bool mixed, int mode, const double *mean, double *sums, double *probes, int n,
+                               int max_steps, cudaStream_t s) {
+    DiagSliceIn st{};
+    st.cs = d.cs;
+    st.mixed = mixed ? 1 : 0;
+    if (mixed) {
+        st.Uh = d.Uf; st.Ul = d.Ul; st.Vh = d.Vf; st.Vl = d.Vl; st.Wh = d.Wf; st.Wl = d.Wl;
+    } else {
+        st.U = d.U; st.V = d.V; st.W = d.W;
+    }
+    const long ni = (long)d.ni;
+    k_stats_accum<<<(unsigned)((ni + 255) / 256), 256, 0, s>>>(st, d.g, mode, mean, sums, probes, n, max_steps);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace f8

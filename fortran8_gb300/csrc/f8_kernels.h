@@ -125,6 +125,8 @@ cudaError_t device_turbulence(Dev &d, bool mixed, const double *const mean[3], d
 cudaError_t device_spectrum(Dev &d, bool mixed, const double *const mean[3], SpecWork &w, double *energy_dev,
                             cudaStream_t s);
 cudaError_t spectrum_kernel_attrs();
+cudaError_t device_stats_accum(Dev &d, bool mixed, int mode, const double *mean, double *sums, double *probes, int n,
+                               int max_steps, cudaStream_t s);
 cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_out, cudaStream_t s);
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)

@@ -206,6 +206,26 @@ class Solver:
         del keep
         return e
 
+    def stats_begin(self, mode: int, mean=None, max_steps: int = 0) -> None:
+        """Start the running statistics of f8_stats_begin (mode 1: sums and probes,
+        mode 2: squared fluctuations about mean = (U, V, W), 0: stop)."""
+        ptrs, keep = self._means(mean)
+        self._check(self._fns["stats_begin"](self._h, mode, *ptrs, max_steps))
+        del keep
+
+    def stats_read(self, max_steps: int = 0):
+        """(sums: three interior fields, probes: (3, steps, NZ) or None, steps)."""
+        g = self.grid
+        sums = [np.zeros(g.interior_shape) for _ in range(3)]
+        n = C.c_int()
+        self._check(self._fns["stats_read"](self._h, *(_ptr(a) for a in sums), None, C.byref(n)))
+        probes = None
+        if max_steps:
+            m = min(n.value, max_steps)
+            probes = np.zeros((3, m, g.nz))
+            self._check(self._fns["stats_read"](self._h, None, None, None, _ptr(probes), C.byref(n)))
+        return sums, probes, n.value
+
     def markers(self) -> np.ndarray:
         n = C.c_int()
         self._check(self._fns["markers"](self._h, C.byref(n), None))

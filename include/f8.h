@@ -197,6 +197,21 @@ int f8_turbulence(f8_ctx *ctx, const double *mean_u, const double *mean_v, const
  * (Parseval).  3D only. */
 int f8_spectrum(f8_ctx *ctx, const double *mean_u, const double *mean_v, const double *mean_w, double *energy);
 
+/* Running statistics accumulated by f8_step after every step of the current
+ * context (fenep_mpi.f90:2934-2941 first pass, 3054-3056 second pass).
+ *   mode 1: sums of U, V, W over the steps, and the centre-line probes
+ *           U_step(k, n) = (U(NX/2,NY/2,k) + U(NX/2-1,NY/2,k))/2, V alike in j,
+ *           W alike in k, for k = 1..NZ and the first max_steps steps;
+ *   mode 2: sums of (U - mean_u)^2 ... with the interior mean fields given;
+ *   mode 0: stop.  Starting a mode clears the sums and the step count.  3D only. */
+int f8_stats_begin(f8_ctx *ctx, int mode, const double *mean_u, const double *mean_v, const double *mean_w,
+                   int max_steps);
+
+/* Read the running statistics: three interior fields of sums (host, each may
+ * be NULL), the probes as (component, step, k) doubles for the steps recorded
+ * (NULL to skip), and the number of steps accumulated. */
+int f8_stats_read(f8_ctx *ctx, double *sum_u, double *sum_v, double *sum_w, double *probes, int *nsteps);
+
 /* Number of Lagrangian markers per z-plane and their host-side positions
  * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */
 int f8_markers(f8_ctx *ctx, int *n_per_plane, double *xy);

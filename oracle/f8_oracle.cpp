@@ -72,6 +72,10 @@ struct OCtx {
     std::vector<double> kx2, ky2, kz2;  // modified wavenumbers 2(1-cos(m d))/d^2
     // diagnostics of the last step
     long long newton_iters = 0, newton_unconv = 0;
+    // running statistics (f8o_stats_begin): sums of U, V, W or of squared
+    // fluctuations, centre-line probes (component, step, k)
+    int stats_mode = 0, stats_n = 0, stats_max = 0;
+    std::vector<double> stats_sum, stats_mean, stats_probe;
     int poisson_iters = -1;
     int sor_order = 0;  // 0: reference sweep order, 1: red-black
     bool timing = false;
@@ -1438,6 +1442,32 @@ void copy_in_int(OCtx &c, std::vector<double> &dst, const double *src) {
 
 }  // namespace
 
+// fenep_mpi.f90:2934-2941 (mode 1) and 3054-3056 (mode 2), after each step
+void stats_accumulate(OCtx &c) {
+    const int NX = c.NX, NY = c.NY, NZ = c.NZ;
+    const size_t ni = (size_t)NX * NY * NZ;
+    const std::vector<double> *F[3] = {&c.U, &c.V, &c.W};
+    for (int q = 0; q < 3; ++q)
+        for (int k = 1; k <= NZ; ++k)
+            for (int j = 1; j <= NY; ++j)
+                for (int i = 1; i <= NX; ++i) {
+                    const size_t o = (size_t)(i - 1) + NX * ((size_t)(j - 1) + (size_t)NY * (k - 1));
+                    const double v = (*F[q])[c.hidx(i, j, k)];
+                    if (c.stats_mode == 1) c.stats_sum[q * ni + o] += v;
+                    else c.stats_sum[q * ni + o] += (v - c.stats_mean[q * ni + o]) * (v - c.stats_mean[q * ni + o]);
+                }
+    if (c.stats_mode == 1 && c.stats_n < c.stats_max) {
+        const int i = NX / 2, j = NY / 2;
+        for (int k = 1; k <= NZ; ++k) {
+            const size_t base = (size_t)c.stats_n * NZ + (k - 1);
+            c.stats_probe[0 * (size_t)c.stats_max * NZ + base] = (c.U[c.hidx(i, j, k)] + c.U[c.hidx(i - 1, j, k)]) / 2.0;
+            c.stats_probe[1 * (size_t)c.stats_max * NZ + base] = (c.V[c.hidx(i, j, k)] + c.V[c.hidx(i, j - 1, k)]) / 2.0;
+            c.stats_probe[2 * (size_t)c.stats_max * NZ + base] = (c.W[c.hidx(i, j, k)] + c.W[c.hidx(i, j, k - 1)]) / 2.0;
+        }
+    }
+    c.stats_n += 1;
+}
+
 extern "C" {
 
 void f8o_default_phys(f8_phys *ph) {
@@ -1538,6 +1568,7 @@ int f8o_step(f8_ctx *ctx, int nsteps, double *drag) {
     auto t0 = std::chrono::steady_clock::now();
     for (int s = 0; s < nsteps; ++s) {
         int st = do_step(c, drag ? drag + (size_t)s * ncyl * 3 : nullptr);
+        if (c.stats_mode) stats_accumulate(c);
         c.total_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         t0 = std::chrono::steady_clock::now();
         c.timed_steps += 1;
@@ -1762,6 +1793,45 @@ int f8o_spectrum(f8_ctx *ctx, const double *mu, const double *mv, const double *
                     energy[idx] += (i == 0 || i == NX / 2) ? e / 2.0 : e / 2.0 * 2.0;
                 }
     }
+    return F8_OK;
+}
+
+int f8o_stats_begin(f8_ctx *ctx, int mode, const double *mu, const double *mv, const double *mw, int max_steps) {
+    if (!ctx || mode < 0 || mode > 2 || max_steps < 0) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (c.dim != 3) return F8_ERR_UNSUPPORTED;
+    if (mode == 2 && (!mu || !mv || !mw)) return F8_ERR_ARG;
+    const size_t ni = (size_t)c.NX * c.NY * c.NZ;
+    c.stats_mode = mode;
+    c.stats_n = 0;
+    c.stats_sum.assign(3 * ni, 0.0);
+    if (mode == 1) {
+        c.stats_max = max_steps;
+        c.stats_probe.assign((size_t)3 * max_steps * c.NZ, 0.0);
+    }
+    if (mode == 2) {
+        c.stats_mean.resize(3 * ni);
+        std::copy(mu, mu + ni, c.stats_mean.begin());
+        std::copy(mv, mv + ni, c.stats_mean.begin() + ni);
+        std::copy(mw, mw + ni, c.stats_mean.begin() + 2 * ni);
+    }
+    return F8_OK;
+}
+
+int f8o_stats_read(f8_ctx *ctx, double *su, double *sv, double *sw, double *probes, int *nsteps) {
+    if (!ctx) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    const size_t ni = (size_t)c.NX * c.NY * c.NZ;
+    double *dst[3] = {su, sv, sw};
+    for (int q = 0; q < 3; ++q)
+        if (dst[q] && c.stats_sum.size() == 3 * ni) std::copy(c.stats_sum.begin() + q * ni, c.stats_sum.begin() + (q + 1) * ni, dst[q]);
+    const int n = std::min(c.stats_n, c.stats_max);
+    if (probes && !c.stats_probe.empty())
+        for (int q = 0; q < 3; ++q)
+            std::copy(c.stats_probe.begin() + (size_t)q * c.stats_max * c.NZ,
+                      c.stats_probe.begin() + (size_t)q * c.stats_max * c.NZ + (size_t)n * c.NZ,
+                      probes + (size_t)q * n * c.NZ);
+    if (nsteps) *nsteps = c.stats_n;
     return F8_OK;
 }
 

@@ -201,3 +201,20 @@ def test_turbulence_and_spectrum_match_oracle(gpu, oracle, precision, tol, with_
             continue
         assert abs(a - b) <= tol * max(abs(b), 1e-300), (f, a, b)
     assert np.max(np.abs(eg - eo)) <= tol * np.max(np.abs(eo))
+
+
+@pytest.mark.parametrize("precision,tol", [(abi.F8_FP64, 1e-12), (abi.F8_MIXED, 1e-6)])
+def test_running_stats_match_oracle(gpu, oracle, precision, tol):
+    w = small("c3_channel")
+    res = {}
+    for name, fns, prec in (("gpu", gpu, precision), ("oracle", oracle, abi.F8_FP64)):
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
+            s.load(configs.initial_state(w))
+            s.stats_begin(1, max_steps=8)
+            s.step(6)
+            res[name] = s.stats_read(max_steps=8)
+    (sg, pg, ng), (so, po, no) = res["gpu"], res["oracle"]
+    assert ng == no == 6
+    for a, b in zip(sg, so):
+        assert np.max(np.abs(a - b)) <= tol * np.max(np.abs(b))
+    assert np.max(np.abs(pg - po)) <= tol * np.max(np.abs(po))
