@@ -97,6 +97,13 @@ struct f8_ctx {
     SpecWork spec{};                  // spectrum workspace (first f8_spectrum call)
     double *mean_dev = nullptr;       // mean velocity fields of f8_turbulence / f8_spectrum
     double *energy_dev = nullptr;
+    // CUDA graphs of the mixed FFT step, one per parity of the C / C-new
+    // buffer pair (the step swaps them), replayed when no stage timing,
+    // AB2 start or SOR is requested
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    float *cf_base = nullptr;
+    double *drag_slot = nullptr;
+    long long graph_launches = 0;
     int stats_mode = 0, stats_n = 0, stats_max = 0;   // running statistics (f8_stats_begin)
     double *stats_sum = nullptr, *stats_probe = nullptr;
     long long last_newton_iters = 0, last_newton_unconv = 0;
@@ -125,6 +132,8 @@ struct f8_ctx {
         if (tot0) cudaEventDestroy(tot0);
         if (tot1) cudaEventDestroy(tot1);
         tot0 = tot1 = nullptr;
+        for (cudaGraphExec_t &ge : gexec)
+            if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
         if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
@@ -247,6 +256,7 @@ int setup(f8_ctx *c) {
                           &d.dUf[0], &d.dUf[1], &d.dUf[2]})
             API_CUDA(c, c->alloc(p, cs));
         API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
+        c->cf_base = d.Cf;
         API_CUDA(c, c->alloc(&d.fpetf, cs));
         API_CUDA(c, c->alloc(&d.fixlist, ni));
         API_CUDA(c, c->alloc(&d.fixcnt, 1));
@@ -267,6 +277,7 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.scal, 64));
     API_CUDA(c, c->alloc(&d.flag, 4));
     API_CUDA(c, c->alloc(&d.cnt, 1));
+    if (c->cyl.size()) API_CUDA(c, c->alloc(&c->drag_slot, c->cyl.size() * 3));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
     API_CUDA(c, c->alloc(&c->diag_part, std::max(diag_partials(), turb_partials(0))));
     if (g.dim == 3) {
@@ -598,7 +609,36 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         }
         int sor_iters = -1;
         double *dg = (ncyl && drag) ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
-        cudaError_t e = mixed ? step_mixed(d, o, dg, &sor_iters, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
+        const bool graph = mixed && !o.ev && !o.ab2_first && c->poisson == F8_POISSON_FFT;
+        cudaError_t e = cudaSuccess;
+        if (graph) {
+            const int p = d.Cf == c->cf_base ? 0 : 1;
+            if (!c->gexec[p]) {
+                // capture one step; the capture runs no work, so the host-side
+                // buffer swap the step makes is undone afterwards
+                float *cf0 = d.Cf, *cn0 = d.Cnf;
+                const long long l0 = g_kernel_launches.load();
+                cudaGraph_t gr = nullptr;
+                API_CUDA(c, cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+                e = step_mixed(d, o, ncyl ? c->drag_slot : nullptr, &sor_iters, c->s);
+                const cudaError_t e2 = cudaStreamEndCapture(c->s, &gr);
+                d.Cf = cf0;
+                d.Cnf = cn0;
+                c->graph_launches = g_kernel_launches.load() - l0;
+                g_kernel_launches -= c->graph_launches;
+                if (e == cudaSuccess) e = e2;
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&c->gexec[p], gr, 0);
+                if (gr) cudaGraphDestroy(gr);
+                if (e != cudaSuccess) return fail(c, e, "graph capture");
+            }
+            e = cudaGraphLaunch(c->gexec[p], c->s);
+            if (o.polymer) std::swap(d.Cf, d.Cnf);
+            g_kernel_launches += c->graph_launches;
+            if (e == cudaSuccess && dg)
+                e = cudaMemcpyAsync(dg, c->drag_slot, (size_t)ncyl * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->s);
+        } else {
+            e = mixed ? step_mixed(d, o, dg, &sor_iters, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
+        }
         if (e != cudaSuccess) return fail(c, e, "step");
         if (c->stats_mode) {
             API_CUDA(c, device_stats_accum(d, mixed, c->stats_mode, c->mean_dev, c->stats_sum, c->stats_probe,

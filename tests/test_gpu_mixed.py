@@ -139,3 +139,23 @@ def test_mixed_sor_variant_matches_fp64_sor(gpu):
     for f in ("u", "v", "w"):
         assert rel_l2(interior(om[f]), interior(o6[f])) <= 1e-5, f
     assert drag_rel(dm, d6) <= 1e-4
+
+
+def test_graph_replay_is_bit_identical(gpu):
+    """The mixed step replays CUDA graphs when no stage timing is requested;
+    the state and drag equal the directly launched step bit for bit."""
+    w = configs.scaled(configs.c3_channel(), 32, 16, 16)
+    res = []
+    for timing in (True, False):
+        with Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED) as s:
+            s.set_timing(timing)
+            s.load(configs.initial_state(w))
+            _, d1 = s.step(3)        # the first step (AB2 start) is never replayed
+            _, d2 = s.step(4)        # odd and even buffer parities
+            st = s.store()
+            res.append((np.concatenate([d1, d2]), st, s.diagnostics().kernel_launches))
+    (da, sa, la), (db, sb, lb) = res
+    np.testing.assert_array_equal(da, db)
+    for f in ("u", "v", "w", "p", "c"):
+        np.testing.assert_array_equal(sa[f], sb[f])
+    assert la == lb   # replayed kernels are counted as launches
