@@ -630,7 +630,7 @@ struct MomArgsF {
     double dt;
 };
 
-__global__ void __launch_bounds__(256) k_momentum3_f(MomArgsF a, Geo g, MixConst mc) {
+__global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixConst mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -883,34 +883,56 @@ __global__ void k_defect_df(DfF Phi, const float *__restrict__ Rh, const float *
 // U^{n+1} = U^n + (dU - dt/dX (Phi_{+1} - Phi)) in df64, and
 // P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
 // in FP32
+// Two cells per thread, k and k + 1: the z neighbours of Phi are shared and
+// every load of both cells is issued before the first store.
+__device__ __forceinline__ void march_cell(DfF (&F)[3], DfF P, const float *const (&D)[3], int h, df c0,
+                                           const df (&pp)[3], const df (&pm)[3], const MixConst &mc, float &unew) {
+    const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
+    df nu[3];
+    float lap = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const df dp = df_sub(pp[c], c0);
+        const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
+        nu[c] = df_add(F[c].at(h), inc);
+        const float dpf = (pp[c].hi - c0.hi) + (pp[c].lo - c0.lo), dmf = (c0.hi - pm[c].hi) + (c0.lo - pm[c].lo);
+        lap += (dpf - dmf) * i2[c];
+    }
+    const df pn = df_add_f(df_add(P.at(h), c0), -mc.pcf * lap);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) F[c].set(h, nu[c]);
+    P.set(h, pn);
+    unew = nu[0].hi;
+}
+
 __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
                            const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc, StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
+    const int k = 2 * blockIdx.z + 1;
     if (i > g.nx || j > g.ny) return;
-    const int h = hix(g, i, j, k);
-    const DfF F[3] = {U, V, W};
-    const float *D[3] = {dU, dV, dW};
-    const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
-    const df c0 = Phi.at(h);
-    float lap = 0.0f, unew = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const df pp = Phi.at(nbr_p(g, i, j, k, c, 1)), pm = Phi.at(nbr_p(g, i, j, k, c, -1));
-        const df dp = df_sub(pp, c0);
-        const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
-        const df nu = df_add(F[c].at(h), inc);
-        F[c].set(h, nu);
-        if (c == 0) unew = nu.hi;
-        const float dpf = (pp.hi - c0.hi) + (pp.lo - c0.lo), dmf = (c0.hi - pm.hi) + (c0.lo - pm.lo);
-        lap += (dpf - dmf) * i2[c];
+    const bool two = k + 1 <= g.nz;
+    DfF F[3] = {U, V, W};
+    const float *const D[3] = {dU, dV, dW};
+    const int h = hix(g, i, j, k), oz = g.sx * g.sy;
+    // Phi at z = k-1 .. k+2 and the x / y neighbours of both cells
+    const df z0 = Phi.at(nbr_p(g, i, j, k, 2, -1)), z1 = Phi.at(h);
+    const df z2 = Phi.at(two ? h + oz : nbr_p(g, i, j, k, 2, 1));
+    const df z3 = two ? Phi.at(nbr_p(g, i, j, k + 1, 2, 1)) : z2;
+    df ppa[3] = {Phi.at(nbr_p(g, i, j, k, 0, 1)), Phi.at(nbr_p(g, i, j, k, 1, 1)), z2};
+    df pma[3] = {Phi.at(nbr_p(g, i, j, k, 0, -1)), Phi.at(nbr_p(g, i, j, k, 1, -1)), z0};
+    df ppb[3] = {z3, z3, z3}, pmb[3] = {z1, z1, z1};
+    if (two) {
+        ppb[0] = Phi.at(nbr_p(g, i, j, k + 1, 0, 1)); ppb[1] = Phi.at(nbr_p(g, i, j, k + 1, 1, 1));
+        pmb[0] = Phi.at(nbr_p(g, i, j, k + 1, 0, -1)); pmb[1] = Phi.at(nbr_p(g, i, j, k + 1, 1, -1));
     }
-    P.set(h, df_add_f(df_add(P.at(h), c0), -mc.pcf * lap));
+    float ua = 0.0f, ub = 0.0f;
+    march_cell(F, P, D, h, z1, ppa, pma, mc, ua);
+    if (two) march_cell(F, P, D, h + oz, z2, ppb, pmb, mc, ub);
     // NaN watch on the new U (the reference stops on a NaN velocity,
     // fenep_2d.f90:1974), counted here instead of in a separate pass
     const unsigned act = __activemask();
-    const unsigned nb = __ballot_sync(act, !isfinite(unew));
+    const unsigned nb = __ballot_sync(act, !isfinite(ua) || !isfinite(ub));
     if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
 }
 
@@ -1459,7 +1481,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     mark(6);
     {
         dim3 blk(32, 8);
-        k_march_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
+        const dim3 gm((g.nx + blk.x - 1) / blk.x, (g.ny + blk.y - 1) / blk.y, (g.nz + 1) / 2);
+        k_march_df<<<gm, blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
         count_launch();
     }
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
