@@ -479,10 +479,21 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
     const int k = blockIdx.x / bpp;
     const int r0 = (blockIdx.x % bpp) * rb;
     const int nrows = min(rb, nrow - r0);
-    for (int q = threadIdx.x; q < (NH + 1) * rb; q += blockDim.x) {
-        const int kx = q / rb, r = q % rb;
-        tile[(size_t)kx * (rb + 1) + r] =
-            r < nrows ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)] : make_float2(0.f, 0.f);
+    // gather the tile: four loads in flight per thread before their stores
+    for (int q0 = threadIdx.x; q0 < (NH + 1) * rb; q0 += 4 * blockDim.x) {
+        float2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * blockDim.x;
+            const int kx = q / rb, r = q % rb;
+            v[u] = (q < (NH + 1) * rb && r < nrows) ? S[((size_t)kx * nz + k) * lj + (jlo + r0 + r + joff2)]
+                                                   : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * blockDim.x;
+            if (q < (NH + 1) * rb) tile[(size_t)(q / rb) * (rb + 1) + q % rb] = v[u];
+        }
     }
     __syncthreads();
     for (int p = warp; 2 * p < nrows; p += XW_WARPS) {
@@ -551,11 +562,21 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_c(float2 *S, int ny, in
     for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
     for (int k = warp; k < NZ; k += nwarp) {
         float *rrow = Rs + (size_t)(__brev((unsigned)k) >> (32 - LG)) * rs;
-        for (int jl = lane; jl < nr; jl += 32) {
-            const int j = jlo + jl;
-            const size_t q = (size_t)k * lj + j;
-            P[(size_t)k * ps + jl] = (j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
-            rrow[jl] = Rg[q];
+        for (int jl0 = lane; jl0 < nr; jl0 += 128) {   // four loads of each array in flight per lane
+            float2 pv[4];
+            float rv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int jl = jl0 + 32 * u, j = jlo + jl;
+                const size_t q = (size_t)k * lj + j;
+                pv[u] = (jl < nr && j >= 1 && j <= ny) ? Sp[q] : make_float2(0.f, 0.f);
+                rv[u] = jl < nr ? Rg[q] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int jl = jl0 + 32 * u;
+                if (jl < nr) { P[(size_t)k * ps + jl] = pv[u]; rrow[jl] = rv[u]; }
+            }
         }
     }
     __syncthreads();
