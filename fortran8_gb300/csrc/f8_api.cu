@@ -103,6 +103,12 @@ struct f8_ctx {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     float *cf_base = nullptr;
     double *drag_slot = nullptr;
+    // pinned host staging of the per-call results (counters, NaN count, drag),
+    // so that their copies are asynchronous and end with one synchronisation
+    StepCounters *cnt_host = nullptr;
+    unsigned long long *nan_host = nullptr;
+    double *drag_host = nullptr;
+    size_t drag_host_n = 0;
     long long graph_launches = 0;
     int stats_mode = 0, stats_n = 0, stats_max = 0;   // running statistics (f8_stats_begin)
     double *stats_sum = nullptr, *stats_probe = nullptr;
@@ -136,6 +142,10 @@ struct f8_ctx {
             if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
+        if (cnt_host) cudaFreeHost(cnt_host);
+        if (nan_host) cudaFreeHost(nan_host);
+        if (drag_host) cudaFreeHost(drag_host);
+        cnt_host = nullptr; nan_host = nullptr; drag_host = nullptr; drag_host_n = 0;
         if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
         stats_probe = nullptr;
         if (s) cudaStreamDestroy(s);
@@ -279,6 +289,8 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.cnt, 1));
     if (c->cyl.size()) API_CUDA(c, c->alloc(&c->drag_slot, c->cyl.size() * 3));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
+    API_CUDA(c, cudaHostAlloc((void **)&c->cnt_host, sizeof(StepCounters), cudaHostAllocDefault));
+    API_CUDA(c, cudaHostAlloc((void **)&c->nan_host, sizeof(unsigned long long), cudaHostAllocDefault));
     API_CUDA(c, c->alloc(&c->diag_part, std::max(diag_partials(), turb_partials(0))));
     if (g.dim == 3) {
         const size_t np = std::max({(size_t)g.nx * g.ny, (size_t)g.nx * g.nz, (size_t)g.ny * g.nz});
@@ -479,6 +491,12 @@ int ensure_drag(f8_ctx *c, int nsteps) {
     API_CUDA(c, c->alloc(&p, (size_t)cap * c->cyl.size() * 3));
     c->drag_dev = p;
     c->drag_cap = cap;
+    if (c->drag_host) cudaFreeHost(c->drag_host);
+    c->drag_host = nullptr;
+    c->drag_host_n = 0;
+    API_CUDA(c, cudaHostAlloc((void **)&c->drag_host, (size_t)cap * c->cyl.size() * 3 * sizeof(double),
+                              cudaHostAllocDefault));
+    c->drag_host_n = (size_t)cap * c->cyl.size() * 3;
     return F8_OK;
 }
 
@@ -583,7 +601,8 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     Dev &d = c->d;
     const int ncyl = (int)c->cyl.size();
     API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
-    API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
+    // the mixed step counts non-finite velocities in its counters instead
+    if (c->precision != F8_MIXED) API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
     const size_t per = NSTAGE + 1;
     if (c->timing && c->evpool.size() < per * nsteps) {
         size_t have = c->evpool.size();
@@ -653,13 +672,17 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     // the mixed step counts non-finite velocities inside its projection kernel
     if (c->precision != F8_MIXED) API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
     c->step_launches += g_kernel_launches.load() - launches0;
-    StepCounters cnt{};
-    unsigned long long nan = 0;
-    API_CUDA(c, cudaMemcpyAsync(&cnt, d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c->s));
-    API_CUDA(c, cudaMemcpyAsync(&nan, c->nan_dev, sizeof(nan), cudaMemcpyDeviceToHost, c->s));
+    const size_t ndrag = (size_t)nsteps * ncyl * 3;
+    *c->nan_host = 0;
+    API_CUDA(c, cudaMemcpyAsync(c->cnt_host, d.cnt, sizeof(StepCounters), cudaMemcpyDeviceToHost, c->s));
+    if (c->precision != F8_MIXED)
+        API_CUDA(c, cudaMemcpyAsync(c->nan_host, c->nan_dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
     if (drag && ncyl)
-        API_CUDA(c, cudaMemcpyAsync(drag, c->drag_dev, (size_t)nsteps * ncyl * 3 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+        API_CUDA(c, cudaMemcpyAsync(c->drag_host, c->drag_dev, ndrag * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
+    const StepCounters cnt = *c->cnt_host;
+    const unsigned long long nan = *c->nan_host;
+    if (drag && ncyl) std::memcpy(drag, c->drag_host, ndrag * sizeof(double));
     {
         float ms = 0.f;
         API_CUDA(c, cudaEventElapsedTime(&ms, c->tot0, c->tot1));
