@@ -95,6 +95,12 @@ ABI_FUNCTIONS = {
                             C.c_void_p, C.c_void_p, C.c_double, C.c_double]),
 }
 
+# Entry points of the CUDA library only (the oracle has no adjoint).
+GPU_FUNCTIONS = {
+    "grad": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.POINTER(Fields), _dp, _dp,
+                       C.POINTER(Fields), _dp]),
+}
+
 NSTAGE = 7
 STAGE_NAMES = ("eigen", "newton", "momentum", "ibm", "helmholtz", "poisson", "project")
 
@@ -104,6 +110,13 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
     out = {}
     for name, (res, args) in ABI_FUNCTIONS.items():
         fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+        out[name] = fn
+    for name, (res, args) in GPU_FUNCTIONS.items():
+        fn = getattr(lib, prefix + name, None)
+        if fn is None:
+            continue
         fn.restype = res
         fn.argtypes = args
         out[name] = fn

@@ -27,6 +27,7 @@ UNITS = {
     "f8_step_mixed.cu": [],
     "f8_fftsolve.cu": ["--fmad=false"],
     "f8_diag.cu": ["--fmad=false"],
+    "f8_adjoint.cu": ["--fmad=false"],
 }
 
 

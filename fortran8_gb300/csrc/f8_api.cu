@@ -74,6 +74,34 @@ void stencil_origin_h(int comp, double xc, double yc, double dX, double dY, int 
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// Device memory of f8_grad: the adjoint fields, the tape of one checkpoint
+// segment (the fields the reverse of each step reads) and the checkpoints of
+// the state.  Kept between calls; regrown when a call needs more.
+struct GradMem {
+    std::vector<void *> mem;
+    AdjState A{};
+    int K = 0, nck = 0, nsteps = 0;
+    size_t ck_slot = 0;                     // doubles per checkpoint
+    double *tU = nullptr, *tV = nullptr, *tW = nullptr, *tC = nullptr;
+    double *tUa = nullptr, *tUp = nullptr, *tPhi = nullptr, *tFc = nullptr;
+    uint8_t *tcodes = nullptr;
+    double *ck = nullptr, *dw = nullptr;
+    template <typename T>
+    cudaError_t get(T **p, size_t n) {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        mem.push_back(q);
+        *p = static_cast<T *>(q);
+        return cudaSuccess;
+    }
+    void free_all() {
+        for (void *p : mem) cudaFree(p);
+        mem.clear();
+        *this = GradMem{};
+    }
+};
+
 }  // namespace
 
 struct f8_ctx {
@@ -112,6 +140,7 @@ struct f8_ctx {
     long long graph_launches = 0;
     int stats_mode = 0, stats_n = 0, stats_max = 0;   // running statistics (f8_stats_begin)
     double *stats_sum = nullptr, *stats_probe = nullptr;
+    GradMem gm;                        // f8_grad buffers
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -146,6 +175,7 @@ struct f8_ctx {
         if (nan_host) cudaFreeHost(nan_host);
         if (drag_host) cudaFreeHost(drag_host);
         cnt_host = nullptr; nan_host = nullptr; drag_host = nullptr; drag_host_n = 0;
+        gm.free_all();
         if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
         stats_probe = nullptr;
         if (s) cudaStreamDestroy(s);
@@ -739,6 +769,249 @@ int f8_store(f8_ctx *c, f8_fields *out) {
         }
     }
     API_CUDA(c, cudaStreamSynchronize(c->s));
+    return F8_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
+    GradMem &G = c->gm;
+    if (G.A.grad && G.K >= K && G.nck >= nck && G.nsteps >= nsteps) return F8_OK;
+    K = std::max(K, G.K);
+    nck = std::max(nck, G.nck);
+    nsteps = std::max(nsteps, G.nsteps);
+    G.free_all();
+    Dev &d = c->d;
+    const size_t cs = d.cs, ni = d.ni, ncyl = c->cyl.size(), nfc = (size_t)d.nm * d.g.nz;
+    AdjState &A = G.A;
+    for (double **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(p, cs));
+    for (double **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(p, 6 * cs));
+    for (int q = 0; q < 3; ++q) {
+        API_CUDA(c, G.get(&A.lA0[q], ni));
+        API_CUDA(c, G.get(&A.lT0[q], ni));
+        API_CUDA(c, G.get(&A.lUa[q], cs));
+        API_CUDA(c, G.get(&A.lUp[q], cs));
+        API_CUDA(c, G.get(&A.lQ[q], cs));
+    }
+    API_CUDA(c, G.get(&A.pack, ni));
+    API_CUDA(c, G.get(&A.grad, 3 + 2 * ncyl));
+    API_CUDA(c, G.get(&G.tU, K * cs));
+    API_CUDA(c, G.get(&G.tV, K * cs));
+    API_CUDA(c, G.get(&G.tW, K * cs));
+    API_CUDA(c, G.get(&G.tC, (K + 1) * 6 * cs));
+    API_CUDA(c, G.get(&G.tcodes, K * ni));
+    API_CUDA(c, G.get(&G.tUa, 3 * K * cs));
+    API_CUDA(c, G.get(&G.tUp, 3 * K * cs));
+    API_CUDA(c, G.get(&G.tPhi, K * cs));
+    API_CUDA(c, G.get(&G.tFc, 3 * K * nfc));
+    G.ck_slot = 10 * cs + 6 * ni;
+    API_CUDA(c, G.get(&G.ck, nck * G.ck_slot));
+    API_CUDA(c, G.get(&G.dw, (size_t)nsteps * std::max<size_t>(ncyl, 1) * 3));
+    G.K = K;
+    G.nck = nck;
+    G.nsteps = nsteps;
+    return F8_OK;
+}
+
+// state <-> checkpoint slot: U, V, W, P, C (halo) and the AB2 histories
+cudaError_t ck_copy(f8_ctx *c, int slot, bool save) {
+    Dev &d = c->d;
+    GradMem &G = c->gm;
+    const size_t cs = d.cs, ni = d.ni;
+    double *base = G.ck + (size_t)slot * G.ck_slot;
+    double *f[11] = {d.U, d.V, d.W, d.P, d.C, d.Ax0, d.Ay0, d.Az0, d.Tx0, d.Ty0, d.Tz0};
+    const size_t n[11] = {cs, cs, cs, cs, 6 * cs, ni, ni, ni, ni, ni, ni};
+    size_t off = 0;
+    for (int q = 0; q < 11; ++q) {
+        const size_t b = n[q] * sizeof(double);
+        cudaError_t e = save ? cudaMemcpyAsync(base + off, f[q], b, cudaMemcpyDeviceToDevice, c->s)
+                             : cudaMemcpyAsync(f[q], base + off, b, cudaMemcpyDeviceToDevice, c->s);
+        if (e != cudaSuccess) return e;
+        off += n[q];
+    }
+    return cudaSuccess;
+}
+
+// one forward step of f8_grad (absolute step index s of the call); rec >= 0
+// stores the tape of the step in segment slot rec
+cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
+    Dev &d = c->d;
+    GradMem &G = c->gm;
+    const size_t cs = d.cs, ni = d.ni, nfc = (size_t)d.nm * d.g.nz, hb = cs * sizeof(double);
+    const int ncyl = (int)c->cyl.size();
+    StepOpts o{};
+    o.polymer = c->phys.beta != 1.0;
+    o.ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
+    o.ibm = ncyl > 0;
+    o.poisson = F8_POISSON_FFT;
+    if (!o.polymer) F8_CUDA_RET(cudaMemsetAsync(d.C, 0, 6 * hb, c->s));
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->s);
+    };
+    if (rec >= 0) {
+        F8_CUDA_RET(cp(G.tU + rec * cs, d.U, hb));
+        F8_CUDA_RET(cp(G.tV + rec * cs, d.V, hb));
+        F8_CUDA_RET(cp(G.tW + rec * cs, d.W, hb));
+        if (rec == 0) F8_CUDA_RET(cp(G.tC, d.C, 6 * hb));
+    }
+    int sor = -1;
+    F8_CUDA_RET(step_fp64(d, o, ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr, &sor, c->s));
+    if (rec >= 0) {
+        F8_CUDA_RET(cp(G.tC + (size_t)(rec + 1) * 6 * cs, d.C, 6 * hb));
+        F8_CUDA_RET(cp(G.tcodes + rec * ni, d.codes, ni));
+        const double *ua[3] = {d.Ua, d.Va, d.Wa}, *up[3] = {d.Up, d.Vp, d.Wp};
+        for (int q = 0; q < 3; ++q) {
+            F8_CUDA_RET(cp(G.tUa + (3 * rec + q) * cs, ua[q], hb));
+            F8_CUDA_RET(cp(G.tUp + (3 * rec + q) * cs, up[q], hb));
+            if (nfc) F8_CUDA_RET(cp(G.tFc + (3 * rec + q) * nfc, d.Fc[q], nfc * sizeof(double)));
+        }
+        F8_CUDA_RET(cp(G.tPhi + rec * cs, d.Phi, hb));
+    }
+    return cudaSuccess;
+}
+
+TapeStep tape_step(f8_ctx *c, int rec) {
+    GradMem &G = c->gm;
+    const size_t cs = c->d.cs, ni = c->d.ni, nfc = (size_t)c->d.nm * c->d.g.nz;
+    TapeStep t{};
+    t.U = G.tU + rec * cs; t.V = G.tV + rec * cs; t.W = G.tW + rec * cs;
+    t.C = G.tC + (size_t)rec * 6 * cs; t.Cn = G.tC + (size_t)(rec + 1) * 6 * cs;
+    t.codes = G.tcodes + rec * ni;
+    for (int q = 0; q < 3; ++q) {
+        t.Ua[q] = G.tUa + (3 * rec + q) * cs;
+        t.Up[q] = G.tUp + (3 * rec + q) * cs;
+        t.Fc[q] = G.tFc + (3 * rec + q) * nfc;
+    }
+    t.Phi = G.tPhi + rec * cs;
+    return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed, double *J,
+            double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
+    if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
+    if (!c->loaded) return F8_ERR_STATE;
+    if (c->precision != F8_FP64 || c->grid.dim != 3 || c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
+    Dev &d = c->d;
+    const int ncyl = (int)c->cyl.size();
+    const size_t cs = d.cs, ni = d.ni;
+    const int K = checkpoint_every == 0 ? nsteps : std::min(checkpoint_every, nsteps);
+    const int nseg = (nsteps + K - 1) / K;
+    if (int st = grad_alloc(c, K, nseg, nsteps)) return st;
+    if (int st = ensure_drag(c, nsteps)) return st;
+    GradMem &G = c->gm;
+    AdjState &A = G.A;
+    const size_t nw = (size_t)nsteps * ncyl * 3;
+    std::vector<double> w(nw, 0.0);
+    if (drag_w) std::copy(drag_w, drag_w + nw, w.begin());
+    else
+        for (int n = 0; n < nsteps; ++n)
+            for (int l = 0; l < ncyl; ++l) w[((size_t)n * ncyl + l) * 3] = 1.0 / nsteps;
+    if (nw) API_CUDA(c, cudaMemcpyAsync(G.dw, w.data(), nw * sizeof(double), cudaMemcpyHostToDevice, c->s));
+    API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
+    API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
+    const int step0 = c->step;
+    // forward: checkpoints at the segment starts, the tape of the last segment
+    for (int seg = 0; seg < nseg; ++seg) {
+        const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
+        const bool last = seg == nseg - 1;
+        if (!last) API_CUDA(c, ck_copy(c, seg, true));
+        for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step(c, step0, s, last ? s - s0 : -1));
+    }
+    API_CUDA(c, count_nonfinite(d.U, d.cs, c->nan_dev, c->s));
+    if (nseg > 1) API_CUDA(c, ck_copy(c, nseg - 1, true));   // final state
+    // adjoint of the final state
+    for (double *p : {A.lU, A.lV, A.lW, A.lP}) API_CUDA(c, cudaMemsetAsync(p, 0, cs * sizeof(double), c->s));
+    API_CUDA(c, cudaMemsetAsync(A.lC, 0, 6 * cs * sizeof(double), c->s));
+    for (int q = 0; q < 3; ++q) {
+        API_CUDA(c, cudaMemsetAsync(A.lA0[q], 0, ni * sizeof(double), c->s));
+        API_CUDA(c, cudaMemsetAsync(A.lT0[q], 0, ni * sizeof(double), c->s));
+    }
+    API_CUDA(c, cudaMemsetAsync(A.grad, 0, (3 + 2 * ncyl) * sizeof(double), c->s));
+    if (seed) {
+        double *tmp = c->scratch_aos;   // 6 * cs doubles
+        const double *hs[4] = {seed->u, seed->v, seed->w, seed->p};
+        double *hd[4] = {A.lU, A.lV, A.lW, A.lP};
+        for (int q = 0; q < 4; ++q) {
+            if (!hs[q]) continue;
+            API_CUDA(c, cudaMemcpyAsync(tmp, hs[q], cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, take_interior(tmp, hd[q], d.g, (int)cs, c->s));
+        }
+        if (seed->c) {
+            API_CUDA(c, cudaMemcpyAsync(tmp, seed->c, 6 * cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, aos_to_soa(tmp, A.lC2, 6, (int)cs, c->s));
+            API_CUDA(c, take_interior(A.lC2, A.lC, d.g, (int)(6 * cs), c->s));
+        }
+        const double *is[6] = {seed->ax0, seed->ay0, seed->az0, seed->tx0, seed->ty0, seed->tz0};
+        double *id[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};
+        for (int q = 0; q < 6; ++q)
+            if (is[q]) API_CUDA(c, cudaMemcpyAsync(id[q], is[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        API_CUDA(c, cudaStreamSynchronize(c->s));
+    }
+    // reverse sweep over the segments
+    const bool polymer = c->phys.beta != 1.0;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
+        if (seg != nseg - 1) {
+            API_CUDA(c, ck_copy(c, seg, false));
+            for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step(c, step0, s, s - s0));
+        }
+        for (int s = s1 - 1; s >= s0; --s) {
+            const TapeStep t = tape_step(c, s - s0);
+            const bool ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
+            API_CUDA(c, step_fp64_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
+        }
+    }
+    if (nseg > 1) API_CUDA(c, ck_copy(c, nseg - 1, false));
+    c->step = step0 + nsteps;
+    // results
+    std::vector<double> hd((size_t)std::max<size_t>(nw, 1));
+    if (nw) API_CUDA(c, cudaMemcpyAsync(hd.data(), c->drag_dev, nw * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    std::vector<double> gr(3 + 2 * ncyl);
+    API_CUDA(c, cudaMemcpyAsync(gr.data(), A.grad, gr.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    StepCounters cnt{};
+    unsigned long long nan = 0;
+    API_CUDA(c, cudaMemcpyAsync(&cnt, d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaMemcpyAsync(&nan, c->nan_dev, sizeof(nan), cudaMemcpyDeviceToHost, c->s));
+    if (dJ_dstate) {
+        auto get = [&](double *dst, const double *src, size_t n) -> cudaError_t {
+            if (!dst) return cudaSuccess;
+            return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+        };
+        API_CUDA(c, get(dJ_dstate->u, A.lU, cs));
+        API_CUDA(c, get(dJ_dstate->v, A.lV, cs));
+        API_CUDA(c, get(dJ_dstate->w, A.lW, cs));
+        API_CUDA(c, get(dJ_dstate->p, A.lP, cs));
+        if (dJ_dstate->c) {
+            API_CUDA(c, soa_to_aos(A.lC, c->scratch_aos, 6, (int)cs, c->s));
+            API_CUDA(c, get(dJ_dstate->c, c->scratch_aos, 6 * cs));
+        }
+        double *od[6] = {dJ_dstate->ax0, dJ_dstate->ay0, dJ_dstate->az0, dJ_dstate->tx0, dJ_dstate->ty0, dJ_dstate->tz0};
+        const double *os[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};
+        for (int q = 0; q < 6; ++q) API_CUDA(c, get(od[q], os[q], ni));
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    if (dJ_dstate) {
+        if (dJ_dstate->phi) std::fill(dJ_dstate->phi, dJ_dstate->phi + cs, 0.0);
+        for (double *p : {dJ_dstate->fx, dJ_dstate->fy, dJ_dstate->fz})
+            if (p) std::fill(p, p + ni, 0.0);
+    }
+    if (J) {
+        double sum = 0.0;
+        for (size_t q = 0; q < nw; ++q) sum += w[q] * hd[q];
+        *J = sum;
+    }
+    if (drag && nw) std::copy(hd.begin(), hd.begin() + nw, drag);
+    if (dJ_dparams) std::copy(gr.begin(), gr.end(), dJ_dparams);
+    c->last_newton_iters = (long long)cnt.newton_iters;
+    c->last_newton_unconv = (long long)cnt.newton_unconverged;
+    if (nan) return F8_ERR_NAN;
+    if (cnt.newton_unconverged) return F8_WARN_NEWTON;
     return F8_OK;
 }
 

@@ -94,6 +94,11 @@ cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s);
 cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s);
 cudaError_t launch_march(Dev &d, cudaStream_t s);
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s);
+// the linear solves of the step without their inhomogeneous boundary terms:
+// Helmholtz (I - dt beta/(2 Re) L) x = q of velocity component comp, and the
+// pressure Poisson L x = q; src interior, dst halo layout (interior written)
+cudaError_t helmholtz_solve_fp64(Dev &d, int comp, const double *src, double *dst, cudaStream_t s);
+cudaError_t poisson_solve_fp64(Dev &d, const double *src, double *dst, cudaStream_t s);
 // On-device diagnostics (f8_diag.cu)
 struct DiagValues {
     double ke, cfl, trc_min, trc_max, trc_mean, trc_std, div_max;
@@ -129,6 +134,29 @@ cudaError_t device_stats_accum(Dev &d, bool mixed, int mode, const double *mean,
                                int max_steps, cudaStream_t s);
 cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_out, cudaStream_t s);
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
+// Discrete adjoint of the FP64 3D step (f8_adjoint.cu).  Adjoint fields are
+// full halo arrays whose halo cells are zero between stages.
+struct AdjState {
+    double *lU, *lV, *lW, *lP, *lPhi;      // state U, V, W, P and the pressure correction
+    double *lC, *lC2, *lC0;                // C, a second C buffer, C0 = f C - I (6 fields each)
+    double *lA0[3], *lT0[3];               // AB2 histories (interior)
+    double *lUa[3], *lUp[3], *lQ[3];       // explicit velocity, Helmholtz solution, right-hand side
+    double *pack;                          // one packed interior field
+    double *grad;                          // dJ/d(Wi, beta, L^2, (xc, yc) per cylinder), accumulated
+};
+// what the reverse of one step reads from its forward step
+struct TapeStep {
+    const double *U, *V, *W;               // velocity at the start of the step (halo)
+    const double *C, *Cn;                  // C before and after the polymer update (halo)
+    const uint8_t *codes;                  // face selection codes
+    const double *Ua[3], *Up[3], *Phi;     // explicit velocity, Helmholtz solutions, Phi (halo)
+    const double *Fc[3];                   // marker forces
+};
+cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const double *drag_w, bool ab2_first,
+                              bool polymer, cudaStream_t s);
+cudaError_t adjoint_fold_state(AdjState &A, const Dev &d, cudaStream_t s);
+// dst[q] = src[q] on interior cells of n / cs stacked halo fields, 0 on halo cells
+cudaError_t take_interior(const double *src, double *dst, const Geo &g, int n, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)
 cudaError_t init_kernels_mixed();
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s);

@@ -1135,6 +1135,16 @@ cudaError_t bc_all_state_fp64(Dev &d, cudaStream_t s) {
 
 cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s) { return bc(A, g, kind, s); }
 
+cudaError_t helmholtz_solve_fp64(Dev &d, int comp, const double *src, double *dst, cudaStream_t s) {
+    if (!d.g.walls) return fft_solve_periodic(d, src, dst, 1.0, d.ph.dt * d.ph.beta / d.ph.re / 2.0, s);
+    return wall_solve(d, src, dst, comp == 1 ? SYS_V : SYS_U, 0.0, s);
+}
+
+cudaError_t poisson_solve_fp64(Dev &d, const double *src, double *dst, cudaStream_t s) {
+    if (!d.g.walls) return fft_solve_periodic(d, src, dst, 0.0, -1.0, s);
+    return wall_solve(d, src, dst, SYS_P, 0.0, s);
+}
+
 cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s) {
     dim3 blk(32, 8);
     k_poisson_rhs<<<cell_grid(d.g, blk), blk, 0, s>>>(d.Up, d.Vp, d.Wp, out, d.g); count_launch();

@@ -165,6 +165,29 @@ class Solver:
         self._check(st)
         return st, (drag[:, :n] if drag is not None else None)
 
+    def grad(self, nsteps: int, checkpoint_every: int = 0, weights=None, seed: State | None = None,
+             want_dstate: bool = False):
+        """f8_grad: advance nsteps and return the gradient of
+        J = sum(weights * drag) + <seed, final state>.
+
+        Returns (status, J (drag term), dparams [dWi, dbeta, dL2, dxc0, dyc0, ...],
+        dstate State or None, drag history (nsteps, ncyl, 3))."""
+        n = len(self.cyls)
+        w = None
+        if weights is not None:
+            w = np.ascontiguousarray(np.broadcast_to(np.asarray(weights, dtype=np.float64), (nsteps, n, 3)))
+        jv = C.c_double()
+        dp = np.zeros(3 + 2 * n)
+        drag = np.zeros((nsteps, max(n, 1), 3))
+        sf = _fields_struct(seed) if seed is not None else None
+        out = empty_state(self.grid) if want_dstate else None
+        of = _fields_struct(out) if out is not None else None
+        st = self._fns["grad"](self._h, nsteps, checkpoint_every, _ptr(w) if w is not None else None,
+                               C.byref(sf) if sf is not None else None, C.byref(jv), _ptr(dp),
+                               C.byref(of) if of is not None else None, _ptr(drag))
+        self._check(st)
+        return st, jv.value, dp, out, drag[:, :n]
+
     def store(self) -> State:
         out = empty_state(self.grid)
         f = _fields_struct(out)

@@ -170,6 +170,34 @@ int f8_step(f8_ctx *ctx, int nsteps, double *drag);
  * pointers are skipped.  Replaces: output (fenep.f90:1186-1233). */
 int f8_store(f8_ctx *ctx, f8_fields *out);
 
+/* Advance nsteps steps like f8_step and return the gradient of
+ *     J = sum_{n,l,c} drag_weights[n][l][c] * drag[n][l][c]
+ *       + <seed, state after the nsteps> (interior values)
+ * from the discrete adjoint of the FP64 3D step.  The reference has no
+ * adjoint; the forward it differentiates is the step of f8_step
+ * (fenep.f90:2477-2527 with the IBM of fenep_mpi.f90:1794-1929).
+ *   drag_weights : nsteps * ncyl * 3 doubles, or NULL for the time-averaged
+ *                  total drag J = (1/nsteps) sum_n sum_l drag_x[n][l];
+ *   seed         : adjoint of the final state (interior cells of u, v, w, p,
+ *                  c, ax0..az0, tx0..tz0; NULL members are zero), or NULL;
+ *   J            : the drag term of J (host, 1 double) or NULL;
+ *   dJ_dparams   : 3 + 2*ncyl doubles: dJ/dWi, dJ/dbeta, dJ/dL^2, then
+ *                  dJ/dxc, dJ/dyc of each cylinder (its markers move with it);
+ *   dJ_dstate    : adjoint of the initial state (interior cells of u, v, w,
+ *                  p, c, ax0..tz0; halo cells and the other members are set
+ *                  to 0; NULL members skipped), or NULL;
+ *   drag         : the drag history as f8_step returns it, or NULL.
+ * The forward runs once, keeping a checkpoint of the state every
+ * checkpoint_every steps (0: one segment); the reverse sweep recomputes each
+ * segment with its intermediate fields stored, then runs the adjoint of its
+ * steps.  The selection of the SPD face candidates is held fixed (its
+ * derivative is zero almost everywhere); the Newton solution is
+ * differentiated through the implicit-function theorem.  Requires an F8_FP64
+ * 3D context with the FFT Poisson solver (F8_ERR_UNSUPPORTED otherwise).  The
+ * context's state advances by nsteps as with f8_step. */
+int f8_grad(f8_ctx *ctx, int nsteps, int checkpoint_every, const double *drag_weights,
+            const f8_fields *seed, double *J, double *dJ_dparams, f8_fields *dJ_dstate, double *drag);
+
 /* Diagnostics of the current state (log_progress, fenep.f90:2266-2342),
  * reduced on the device: kinetic energy, CFL, trC min / max / mean / std,
  * max |div u|, NaN flag, and the iteration counters of the last f8_step. */

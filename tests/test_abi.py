@@ -39,8 +39,20 @@ def test_library_exports_every_declared_symbol(cuda_lib):
 
 
 def test_oracle_exports_the_same_abi(oracle_lib):
+    """Every entry point but the adjoint (the oracle's gradient reference is the
+    differentiable torch restatement, oracle/f8_torch.py)."""
     for name in declared_functions():
+        if name[3:] in abi.GPU_FUNCTIONS:
+            assert not hasattr(oracle_lib, "f8o_" + name[3:]), name
+            continue
         assert hasattr(oracle_lib, "f8o_" + name[3:]), name
+
+
+def test_grad_is_bound_and_rejects_bad_arguments(cuda_lib):
+    fns = abi.bind(cuda_lib, "f8_")
+    assert "grad" in fns
+    dp = (C.c_double * 3)()
+    assert fns["grad"](None, 1, 0, None, None, None, dp, None, None) == abi.F8_ERR_ARG
 
 
 def test_invalid_arguments_are_rejected_without_a_device(cuda_lib):
