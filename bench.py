@@ -328,6 +328,9 @@ def run_ours(args, w):
         cmp = {"fp64_value": v64, "fp64_ms_per_step": t64 / k64, "mixed_over_fp64": value / v64,
                "drag_rel_err_vs_fp64": rel, "steps_compared": args.warmup + k64,
                "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
+    adj = None
+    if not args.no_adjoint:
+        adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every)
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s",
@@ -364,11 +367,43 @@ def run_ours(args, w):
                        "l2": "inputs larger than L2 (state %.2f GB)" % (sb / 1e9), "parallelism": f"replicas{ws}"},
             "status": int(status), "div_max": diag.div_max, "newton_iters_per_cell_step": diag.newton_iters / (cells * args.steps),
             "drag_last": drag[-1].tolist() if drag is not None else None,
-            "gpu_launches": launches, "clocks": clocks, "roofline": roof, "e2e": e2e, "fp64_compare": cmp}
+            "gpu_launches": launches, "clocks": clocks, "roofline": roof, "e2e": e2e, "fp64_compare": cmp,
+            "adjoint": adj}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w)
     print(json.dumps(line))
     return 0
+
+
+def adjoint_cost(fns, steps, every):
+    """Cost of the gradient (f8_grad: forward with checkpoints, recomputation of
+    each segment, adjoint sweep) over that of the FP64 forward (f8_step), on the
+    adjoint workload: 128 x 64 x 64 channel, 2 cylinders, gradient of the
+    time-averaged total drag w.r.t. Wi, beta, L^2 and the centres.  Both calls
+    are synchronous; timed on the host clock after a warm-up call of each."""
+    import torch
+    w = configs.c4_adjoint()
+    st0 = configs.initial_state(w)
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s:
+        s.load(st0)
+        s.step(2)
+        s.load(st0)
+        s.grad(min(steps, 2 * every), every)
+        torch.cuda.synchronize()
+        s.load(st0)
+        t0 = time.perf_counter()
+        s.step(steps)
+        tf = time.perf_counter() - t0
+        s.load(st0)
+        t0 = time.perf_counter()
+        status, J, dp, _, _ = s.grad(steps, every)
+        tg = time.perf_counter() - t0
+    return {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
+            "steps": steps, "checkpoint_every": every, "precision": "fp64",
+            "forward_ms_per_step": tf * 1e3 / steps, "grad_ms_per_step": tg * 1e3 / steps,
+            "adjoint_over_forward": tg / tf, "J": J,
+            "dJ_dparams": {"wi": dp[0], "beta": dp[1], "lp2": dp[2], "centres": dp[3:].tolist()},
+            "status": int(status)}
 
 
 # launches per step of each stage kernel of the mixed step (wall channel)
@@ -437,6 +472,9 @@ def main():
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=400)
+    ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint run")
     ap.add_argument("--poisson", default="fft", choices=["fft", "sor"],
                     help="pressure solver: FFT + tridiagonal (default) or red-black SOR")
     ap.add_argument("--grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),

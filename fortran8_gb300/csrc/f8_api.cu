@@ -78,7 +78,9 @@ bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 // segment (the fields the reverse of each step reads) and the checkpoints of
 // the state.  Kept between calls; regrown when a call needs more.
 struct GradMem {
-    std::vector<void *> mem;
+    // four groups, each regrown on its own: the adjoint fields (grid), the
+    // tape (segment length), the checkpoints (segments) and the drag weights
+    std::vector<void *> mem[4];
     AdjState A{};
     int K = 0, nck = 0, nsteps = 0;
     size_t ck_slot = 0;                     // doubles per checkpoint
@@ -87,17 +89,20 @@ struct GradMem {
     uint8_t *tcodes = nullptr;
     double *ck = nullptr, *dw = nullptr;
     template <typename T>
-    cudaError_t get(T **p, size_t n) {
+    cudaError_t get(int grp, T **p, size_t n) {
         void *q = nullptr;
         cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
         if (e != cudaSuccess) return e;
-        mem.push_back(q);
+        mem[grp].push_back(q);
         *p = static_cast<T *>(q);
         return cudaSuccess;
     }
+    void free_group(int grp) {
+        for (void *p : mem[grp]) cudaFree(p);
+        mem[grp].clear();
+    }
     void free_all() {
-        for (void *p : mem) cudaFree(p);
-        mem.clear();
+        for (int q = 0; q < 4; ++q) free_group(q);
         *this = GradMem{};
     }
 };
@@ -778,40 +783,49 @@ namespace {
 
 int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
     GradMem &G = c->gm;
-    if (G.A.grad && G.K >= K && G.nck >= nck && G.nsteps >= nsteps) return F8_OK;
-    K = std::max(K, G.K);
-    nck = std::max(nck, G.nck);
-    nsteps = std::max(nsteps, G.nsteps);
-    G.free_all();
     Dev &d = c->d;
     const size_t cs = d.cs, ni = d.ni, ncyl = c->cyl.size(), nfc = (size_t)d.nm * d.g.nz;
-    AdjState &A = G.A;
-    for (double **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(p, cs));
-    for (double **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(p, 6 * cs));
-    for (int q = 0; q < 3; ++q) {
-        API_CUDA(c, G.get(&A.lA0[q], ni));
-        API_CUDA(c, G.get(&A.lT0[q], ni));
-        API_CUDA(c, G.get(&A.lUa[q], cs));
-        API_CUDA(c, G.get(&A.lUp[q], cs));
-        API_CUDA(c, G.get(&A.lQ[q], cs));
+    if (!G.A.grad) {
+        AdjState &A = G.A;
+        for (double **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(0, p, cs));
+        for (double **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(0, p, 6 * cs));
+        for (int q = 0; q < 3; ++q) {
+            API_CUDA(c, G.get(0, &A.lA0[q], ni));
+            API_CUDA(c, G.get(0, &A.lT0[q], ni));
+            API_CUDA(c, G.get(0, &A.lUa[q], cs));
+            API_CUDA(c, G.get(0, &A.lUp[q], cs));
+            API_CUDA(c, G.get(0, &A.lQ[q], cs));
+        }
+        API_CUDA(c, G.get(0, &A.pack, ni));
+        API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
     }
-    API_CUDA(c, G.get(&A.pack, ni));
-    API_CUDA(c, G.get(&A.grad, 3 + 2 * ncyl));
-    API_CUDA(c, G.get(&G.tU, K * cs));
-    API_CUDA(c, G.get(&G.tV, K * cs));
-    API_CUDA(c, G.get(&G.tW, K * cs));
-    API_CUDA(c, G.get(&G.tC, (K + 1) * 6 * cs));
-    API_CUDA(c, G.get(&G.tcodes, K * ni));
-    API_CUDA(c, G.get(&G.tUa, 3 * K * cs));
-    API_CUDA(c, G.get(&G.tUp, 3 * K * cs));
-    API_CUDA(c, G.get(&G.tPhi, K * cs));
-    API_CUDA(c, G.get(&G.tFc, 3 * K * nfc));
-    G.ck_slot = 10 * cs + 6 * ni;
-    API_CUDA(c, G.get(&G.ck, nck * G.ck_slot));
-    API_CUDA(c, G.get(&G.dw, (size_t)nsteps * std::max<size_t>(ncyl, 1) * 3));
-    G.K = K;
-    G.nck = nck;
-    G.nsteps = nsteps;
+    if (K > G.K) {
+        G.free_group(1);
+        G.K = 0;
+        API_CUDA(c, G.get(1, &G.tU, K * cs));
+        API_CUDA(c, G.get(1, &G.tV, K * cs));
+        API_CUDA(c, G.get(1, &G.tW, K * cs));
+        API_CUDA(c, G.get(1, &G.tC, (K + 1) * 6 * cs));
+        API_CUDA(c, G.get(1, &G.tcodes, K * ni));
+        API_CUDA(c, G.get(1, &G.tUa, 3 * K * cs));
+        API_CUDA(c, G.get(1, &G.tUp, 3 * K * cs));
+        API_CUDA(c, G.get(1, &G.tPhi, K * cs));
+        API_CUDA(c, G.get(1, &G.tFc, 3 * K * nfc));
+        G.K = K;
+    }
+    if (nck > G.nck) {
+        G.free_group(2);
+        G.nck = 0;
+        G.ck_slot = 10 * cs + 6 * ni;
+        API_CUDA(c, G.get(2, &G.ck, nck * G.ck_slot));
+        G.nck = nck;
+    }
+    if (nsteps > G.nsteps) {
+        G.free_group(3);
+        G.nsteps = 0;
+        API_CUDA(c, G.get(3, &G.dw, (size_t)nsteps * std::max<size_t>(ncyl, 1) * 3));
+        G.nsteps = nsteps;
+    }
     return F8_OK;
 }
 

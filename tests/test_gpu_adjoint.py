@@ -107,3 +107,18 @@ def test_grad_matches_gpu_central_differences(gpu, oracle):
             vals.append(drag[:, :, 0].sum() / n)
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(dp[q] - fd) <= 1e-4 * abs(fd) + 1e-8, (q, dp[q], fd)
+
+
+def test_autograd_function_returns_the_adjoint_gradient(gpu, oracle):
+    import torch
+    from fortran8_gb300.autograd import DragProblem, drag_objective
+    w, st, step0 = case("channel", oracle)
+    n = 3
+    prob = DragProblem(w.grid, w.phys, w.cyls, st, n, step0=step0, checkpoint_every=2)
+    p = prob.params().requires_grad_(True)
+    J = drag_objective(p, prob)
+    loss = (J - 1.0) ** 2
+    loss.backward()
+    Jg, dp, _, _, _ = gpu_grad(gpu, w, st, step0, n, K=2)
+    assert J.item() == Jg
+    assert np.allclose(p.grad.numpy(), 2.0 * (Jg - 1.0) * dp, rtol=1e-12, atol=0.0)
