@@ -7,6 +7,8 @@
 !   f8_load    after init / input (fenep.f90:2460-2461)
 !   f8_step    for Lstep/Gstep-sized chunks of steps
 !   f8_store   before log_progress / get_data_binary / output
+!   f8_grad    (optional) gradients of the drag w.r.t. Wi, beta, L^2 and the
+!              cylinder centres by the discrete adjoint
 !   f8_destroy at the end (fft_finalize)
 !
 ! Array arguments are the reference's own arrays, passed with c_loc():
@@ -105,6 +107,20 @@ module f8_gpu
             type(c_ptr), value :: ctx
             type(f8_fields), intent(in) :: fields
         end function f8_store
+
+        ! Gradient of J = sum(drag_weights * drag) + <seed, final state> by the
+        ! discrete adjoint (FP64 3D contexts).  drag_weights: real(8)
+        ! (3, ncyl, nsteps) or c_null_ptr (time-averaged total x drag); seed,
+        ! dJ_dstate: c_loc of an f8_fields or c_null_ptr; J: real(8) or
+        ! c_null_ptr; dJ_dparams: real(8) (3 + 2*ncyl) = dWi, dbeta, dL^2,
+        ! then (dxc, dyc) per cylinder; drag as f8_step's.
+        integer(c_int) function f8_grad(ctx, nsteps, checkpoint_every, drag_weights, seed, J, dJ_dparams, &
+                                        dJ_dstate, drag) bind(C, name="f8_grad")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nsteps, checkpoint_every
+            type(c_ptr), value :: drag_weights, seed, J, dJ_dparams, dJ_dstate, drag
+        end function f8_grad
 
         integer(c_int) function f8_diagnostics(ctx, diag) bind(C, name="f8_diagnostics")
             import :: c_ptr, c_int, f8_diag
