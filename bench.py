@@ -330,7 +330,7 @@ def run_ours(args, w):
                "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
     adj = None
     if not args.no_adjoint:
-        adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every)
+        adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, args.adjoint_grid)
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s",
@@ -375,35 +375,57 @@ def run_ours(args, w):
     return 0
 
 
-def adjoint_cost(fns, steps, every):
+def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_prefix=0):
     """Cost of the gradient (f8_grad: forward with checkpoints, recomputation of
-    each segment, adjoint sweep) over that of the FP64 forward (f8_step), on the
-    adjoint workload: 128 x 64 x 64 channel, 2 cylinders, gradient of the
-    time-averaged total drag w.r.t. Wi, beta, L^2 and the centres.  Both calls
-    are synchronous; timed on the host clock after a warm-up call of each."""
+    each segment, adjoint sweep) over that of the FP64 forward (f8_step).
+
+    Default: the adjoint workload, a 128 x 64 x 64 channel with 2 cylinders,
+    gradient of the time-averaged total drag w.r.t. Wi, beta, L^2 and the
+    centres.  With mixed_prefix > 0 the FP32-mixed step first advances the
+    seeded state that many steps (timed), and the adjoint window starts from
+    its state in an FP64 context.  Both timed calls are synchronous; they are
+    timed on the host clock after a warm-up call of each."""
     import torch
-    w = configs.c4_adjoint()
+    w = configs.WORKLOADS[workload]()
+    if grid:
+        w = configs.scaled(w, *grid)
     st0 = configs.initial_state(w)
+    step0 = 0
+    pre = None
+    if mixed_prefix > 0:
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED) as sm:
+            sm.load(st0)
+            sm.timing_reset()
+            sm.step(mixed_prefix)
+            tms, _, _ = sm.timing()
+            st0 = sm.store()
+        step0 = mixed_prefix
+        pre = {"mixed_steps": mixed_prefix, "mixed_ms_per_step": tms / mixed_prefix,
+               "mixed_value": w.cells * mixed_prefix / (tms / 1e3) / 1e6}
     with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s:
-        s.load(st0)
+        s.load(st0, step0)
         s.step(2)
-        s.load(st0)
+        s.load(st0, step0)
         s.grad(min(steps, 2 * every), every)
         torch.cuda.synchronize()
-        s.load(st0)
+        s.load(st0, step0)
         t0 = time.perf_counter()
         s.step(steps)
         tf = time.perf_counter() - t0
-        s.load(st0)
+        s.load(st0, step0)
         t0 = time.perf_counter()
         status, J, dp, _, _ = s.grad(steps, every)
         tg = time.perf_counter() - t0
-    return {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
-            "steps": steps, "checkpoint_every": every, "precision": "fp64",
-            "forward_ms_per_step": tf * 1e3 / steps, "grad_ms_per_step": tg * 1e3 / steps,
-            "adjoint_over_forward": tg / tf, "J": J,
-            "dJ_dparams": {"wi": dp[0], "beta": dp[1], "lp2": dp[2], "centres": dp[3:].tolist()},
-            "status": int(status)}
+    out = {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
+           "steps": steps, "checkpoint_every": every, "precision": "fp64", "step0": step0,
+           "forward_ms_per_step": tf * 1e3 / steps, "grad_ms_per_step": tg * 1e3 / steps,
+           "adjoint_over_forward": tg / tf, "J": J,
+           "dJ_dparams": {"wi": dp[0], "beta": dp[1], "lp2": dp[2], "centres": dp[3:].tolist()},
+           "status": int(status)}
+    if pre:
+        out["mixed_prefix"] = pre
+        out["grad_over_mixed_forward"] = (tg / steps) / (pre["mixed_ms_per_step"] / 1e3)
+    return out
 
 
 # launches per step of each stage kernel of the mixed step (wall channel)
@@ -475,6 +497,13 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint run")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="print only the adjoint/forward cost measurement (JSON)")
+    ap.add_argument("--adjoint-grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
+                    help="scale the adjoint workload (small cases for profiling)")
+    ap.add_argument("--adjoint-workload", default="c4_adjoint", choices=sorted(configs.WORKLOADS))
+    ap.add_argument("--adjoint-mixed-prefix", type=int, default=0,
+                    help="FP32-mixed steps before the adjoint window (with --adjoint-only)")
     ap.add_argument("--poisson", default="fft", choices=["fft", "sor"],
                     help="pressure solver: FFT + tridiagonal (default) or red-black SOR")
     ap.add_argument("--grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
@@ -491,6 +520,14 @@ def main():
         w = configs.scaled(w, *args.grid)
     if args.impl == "reference":
         return run_reference(args, w)
+    if args.adjoint_only:
+        import torch
+        from fortran8_gb300 import build as b, lib as flib
+        b.build()
+        torch.cuda.set_device(0)
+        print(json.dumps(adjoint_cost(flib.functions(), args.adjoint_steps, args.adjoint_every, args.adjoint_grid,
+                                      args.adjoint_workload, args.adjoint_mixed_prefix)))
+        return 0
     return run_ours(args, w)
 
 
