@@ -764,13 +764,14 @@ int f8_store(f8_ctx *c, f8_fields *out) {
             API_CUDA(c, soa_to_aos_f(d.Cf, c->scratch_aos, d.ncomp, (int)cs, c->s));
             API_CUDA(c, get(out->c, c->scratch_aos, cs * d.ncomp));
         }
+        // the FP32 histories go through the FP64 staging area; each copy is
+        // ordered on the stream before the next conversion overwrites it
         double *dsts[9] = {out->ax0, out->ay0, out->az0, out->tx0, out->ty0, out->tz0, out->fx, out->fy, out->fz};
         const float *srcs[9] = {d.A0f[0], d.A0f[1], d.A0f[2], d.T0f[0], d.T0f[1], d.T0f[2], d.Ff[0], d.Ff[1], d.Ff[2]};
         for (int q = 0; q < 9; ++q) {
             if (!dsts[q]) continue;
             API_CUDA(c, f2d(srcs[q], c->scratch_aos, (int)ni, c->s));
             API_CUDA(c, get(dsts[q], c->scratch_aos, ni));
-            API_CUDA(c, cudaStreamSynchronize(c->s));
         }
     }
     API_CUDA(c, cudaStreamSynchronize(c->s));

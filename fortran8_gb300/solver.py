@@ -188,8 +188,11 @@ class Solver:
         self._check(st)
         return st, jv.value, dp, out, drag[:, :n]
 
-    def store(self) -> State:
-        out = empty_state(self.grid)
+    def store(self, out: State | None = None) -> State:
+        """Copy the state out; into ``out``'s arrays when given (e.g. page-locked
+        buffers reused across calls), else into new arrays."""
+        if out is None:
+            out = empty_state(self.grid)
         f = _fields_struct(out)
         self._check(self._fns["store"](self._h, C.byref(f)))
         return out
