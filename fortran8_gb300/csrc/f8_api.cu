@@ -512,6 +512,16 @@ int setup(f8_ctx *c) {
                 if (int st = upload_i(c, &d.act_cols[comp], act)) return st;
             }
         }
+        if (!mixed) {
+            for (int comp = 0; comp < 3; ++comp) {
+                API_CUDA(c, c->alloc(&d.mwxd[comp], 3 * (size_t)nm));
+                API_CUDA(c, c->alloc(&d.mwyd[comp], 3 * (size_t)nm));
+                API_CUDA(c, c->alloc(&d.mwzd[comp], 3 * (size_t)g.nz));
+                API_CUDA(c, c->alloc(&d.mi0d[comp], nm));
+                API_CUDA(c, c->alloc(&d.mj0d[comp], nm));
+            }
+            API_CUDA(c, marker_weights_fp64(d, c->s));
+        }
         // the interpolation stencil reads k = n-1 .. n+1 and marker columns
         // inside the halo box; validated above through the gather lists
     }

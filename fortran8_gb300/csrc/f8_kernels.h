@@ -60,6 +60,9 @@ struct Dev {
     float *wtR[3];                         // Thomas 1/den tables of the U, V, P wall systems
     float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
     int *mi0[3], *mj0[3];                  // per-marker stencil origins
+    double *mwxd[3], *mwyd[3];             // FP64: per-marker x / y kernel weights (3 each)
+    double *mwzd[3];                       // FP64: per-plane z weights of planes n-1, n, n+1 (3 each)
+    int *mi0d[3], *mj0d[3];                // FP64: per-marker stencil origins
     int *act_cols[3];                      // interior (i,j) columns that receive spreading
     int nact[3];
     int defect_iters;                      // Poisson defect corrections (mixed)
@@ -94,6 +97,8 @@ cudaError_t bc_field(double *A, const Geo &g, int kind, cudaStream_t s);
 cudaError_t launch_poisson_rhs(Dev &d, double *out, cudaStream_t s);
 cudaError_t launch_march(Dev &d, cudaStream_t s);
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s);
+// the FP64 IBM weight tables (mwxd, mwyd, mwzd, mi0d, mj0d) from the marker positions
+cudaError_t marker_weights_fp64(Dev &d, cudaStream_t s);
 // the linear solves of the step without their inhomogeneous boundary terms:
 // Helmholtz (I - dt beta/(2 Re) L) x = q of velocity component comp, and the
 // pressure Poisson L x = q; src interior, dst halo layout (interior written)

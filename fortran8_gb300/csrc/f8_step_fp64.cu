@@ -704,7 +704,50 @@ struct IbmArgs {
     const int *off[3], *idx[3];
     const double *Ua[3], *B[3];
     double *Q[3];
+    // kernel weight tables (k_marker_weights): roma of the x, y offsets of each
+    // marker's 3 stencil columns / rows, and of the z offsets of planes n-1..n+1
+    const double *wx[3], *wy[3], *wz[3];
+    const int *i0[3], *j0[3];
 };
+
+// Tables of the Roma weights (fenep.f90:2045-2055): the same expressions as the
+// reference's delta evaluation inside its stencil loops, evaluated once per
+// marker (x, y) and per plane (z), so that each product below is the same double.
+__global__ void k_marker_weights(const double *mx, const double *my, int nm, int comp, Geo g, double *wx, double *wy,
+                                 int *i0o, int *j0o) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nm) return;
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    const double xc = mx[m], yc = my[m];
+    int i0, j0;
+    stencil_origin(comp, xc, yc, dX, dY, i0, j0);
+    i0o[m] = i0;
+    j0o[m] = j0;
+    for (int a = 0; a < 3; ++a) {
+        double x, y, z;
+        grid_pos(comp, i0 + a, j0 + a, 1, dX, dY, dZ, x, y, z);
+        wx[3 * m + a] = roma((x - xc) / dX);
+        wy[3 * m + a] = roma((y - yc) / dY);
+    }
+}
+
+__global__ void k_plane_weights(int comp, Geo g, double *wz) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    if (n > g.nz) return;
+    const double dX = g.dx, dY = g.dy, dZ = g.dz;
+    const double zc = (n - 0.25) * dZ;
+    for (int c = 0; c < 3; ++c) {
+        double x, y, z;
+        grid_pos(comp, 1, 1, n - 1 + c, dX, dY, dZ, x, y, z);
+        wz[3 * (n - 1) + c] = roma((z - zc) / dZ);
+    }
+}
+
+// delta(x_e - X_m) of stencil cell (a, b, c) of marker m on plane n
+__device__ inline double ibm_delta(const IbmArgs &a, int comp, int m, int n, int ia, int jb, int kc) {
+    return a.d3 ? a.wx[comp][3 * m + ia] * a.wy[comp][3 * m + jb] * a.wz[comp][3 * (n - 1) + kc] / a.dvol
+                : a.wx[comp][3 * m + ia] * a.wy[comp][3 * m + jb] / a.dvol;
+}
 
 // interpolation at the markers and the marker force Fc = (Uc - Ub)/dt
 __global__ void k_ibm_interp(IbmArgs a, Geo g) {
@@ -712,21 +755,14 @@ __global__ void k_ibm_interp(IbmArgs a, Geo g) {
     const int n = blockIdx.y + 1;
     const int comp = blockIdx.z;
     if (m >= a.nm) return;
-    const double dX = g.dx, dY = g.dy, dZ = g.dz;
-    const double xc = a.mx[m], yc = a.my[m];
-    const double zc = a.d3 ? (n - 0.25) * dZ : 0.0;
-    int i0, j0;
-    stencil_origin(comp, xc, yc, dX, dY, i0, j0);
+    const int i0 = a.i0[comp][m], j0 = a.j0[comp][m];
     const int klo = a.d3 ? n - 1 : 1, khi = a.d3 ? n + 1 : 1;
     double ub = 0.0;
     const double *Uf = a.Uf[comp];
     for (int k = klo; k <= khi; ++k)
         for (int j = j0; j <= j0 + 2; ++j)
             for (int i = i0; i <= i0 + 2; ++i) {
-                double x, y, z;
-                grid_pos(comp, i, j, k, dX, dY, dZ, x, y, z);
-                double del = a.d3 ? roma((x - xc) / dX) * roma((y - yc) / dY) * roma((z - zc) / dZ) / a.dvol
-                                  : roma((x - xc) / dX) * roma((y - yc) / dY) / a.dvol;
+                const double del = ibm_delta(a, comp, m, n, i - i0, j - j0, k - klo);
                 ub = ub + Uf[hix(g, i, j, k)] * del * a.dxn;
             }
     const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
@@ -738,18 +774,13 @@ __device__ inline double spread_at(const IbmArgs &a, const Geo &g, int comp, int
     const int col = ie + g.sx * je;
     const int b = a.off[comp][col], e = a.off[comp][col + 1];
     if (b == e) return 0.0;
-    const double dX = g.dx, dY = g.dy, dZ = g.dz;
-    double x, y, z;
-    grid_pos(comp, ie, je, ke, dX, dY, dZ, x, y, z);
     double acc = 0.0;
     const int nlo = a.d3 ? max(ke - 1, 1) : 1, nhi = a.d3 ? min(ke + 1, g.nz) : 1;
     for (int n = nlo; n <= nhi; ++n) {
-        const double zc = a.d3 ? (n - 0.25) * dZ : 0.0;
+        const int kc = a.d3 ? ke - n + 1 : 0;
         for (int q = b; q < e; ++q) {
             const int m = a.idx[comp][q];
-            const double xc = a.mx[m], yc = a.my[m];
-            double del = a.d3 ? roma((x - xc) / dX) * roma((y - yc) / dY) * roma((z - zc) / dZ) / a.dvol
-                              : roma((x - xc) / dX) * roma((y - yc) / dY) / a.dvol;
+            const double del = ibm_delta(a, comp, m, n, ie - a.i0[comp][m], je - a.j0[comp][m], kc);
             double fcv = a.Fc[comp][m + (size_t)a.nm * (n - 1)];
             acc = acc + fcv * del * a.dxn;
         }
@@ -1158,6 +1189,16 @@ cudaError_t launch_march(Dev &d, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t marker_weights_fp64(Dev &d, cudaStream_t s) {
+    const int ncomp = d.g.dim == 3 ? 3 : 2;
+    for (int c = 0; c < ncomp; ++c) {
+        k_marker_weights<<<(d.nm + 127) / 128, 128, 0, s>>>(d.mx, d.my, d.nm, c, d.g, d.mwxd[c], d.mwyd[c], d.mi0d[c],
+                                                            d.mj0d[c]); count_launch();
+        k_plane_weights<<<(d.g.nz + 127) / 128, 128, 0, s>>>(c, d.g, d.mwzd[c]); count_launch();
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s) {
     const Geo &g = d.g;
     const bool d3 = g.dim == 3;
@@ -1237,6 +1278,10 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
             ia.Q[c] = d.Q[c]; ia.B[c] = (c == 0 ? d.Bx : c == 1 ? d.By : d.Bz);
         }
         ia.Ua[0] = d.Ua; ia.Ua[1] = d.Va; ia.Ua[2] = d.Wa;
+        for (int c = 0; c < 3; ++c) {
+            ia.wx[c] = d.mwxd[c]; ia.wy[c] = d.mwyd[c]; ia.wz[c] = d.mwzd[c];
+            ia.i0[c] = d.mi0d[c]; ia.j0[c] = d.mj0d[c];
+        }
         dim3 gi((d.nm + 127) / 128, g.nz, ia.ncomp);
         k_ibm_interp<<<gi, 128, 0, s>>>(ia, g); count_launch();
         dim3 blk(32, 8);
