@@ -591,6 +591,10 @@ __global__ void k_c0_adj(const double *C, const double *lC0, double *lC, int cs,
 // Polymer update transposed: implicit-function adjoint of the Lyapunov Newton
 // solve and the Cstar upwind sum (fenep.f90:464-643).
 
+struct W3 {
+    double m, c, p;   // weights of C at the - neighbour, the cell, the + neighbour
+};
+
 __device__ inline void wface_p(int idx, double &wm, double &w0, double &wp) {
     switch (idx) {
     case 1: wm = 0.0; w0 = 1.5; wp = -0.5; break;
@@ -632,6 +636,7 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
         const double dt = a.dt, wi = a.wi, lp2 = a.lp2, dX = g.dx, dY = g.dy, dZ = g.dz;
         double lx[6], x[6];
         bool any = false;
+#pragma unroll
         for (int m = 0; m < 6; ++m) {
             lx[m] = a.lX[m * cs + h];
             x[m] = a.Cn[m * cs + h];
@@ -654,7 +659,9 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             A0[2][2] = -dt * (-w(i, j, k - 1) + w(i, j, k)) / dZ;
             // A = A0^T (the matrix the Newton solve uses)
             double A[3][3];
+#pragma unroll
             for (int r = 0; r < 3; ++r)
+#pragma unroll
                 for (int q = 0; q < 3; ++q) A[r][q] = A0[q][r];
             const double tr = x[0] + x[3] + x[5];
             const double den = lp2 - tr;
@@ -665,7 +672,9 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             double M[6][7];
             {
                 double J[6][6];
+#pragma unroll
                 for (int r = 0; r < 6; ++r)
+#pragma unroll
                     for (int q = 0; q < 6; ++q) J[r][q] = 0.0;
                 J[0][0] = 2 * A[0][0]; J[0][1] = 2 * A[0][1]; J[0][2] = 2 * A[0][2];
                 J[1][0] = A[1][0]; J[1][1] = A[1][1] + A[0][0]; J[1][2] = A[1][2]; J[1][3] = A[0][1]; J[1][4] = A[0][2];
@@ -673,39 +682,54 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
                 J[3][1] = 2 * A[1][0]; J[3][3] = 2 * A[1][1]; J[3][4] = 2 * A[1][2];
                 J[4][1] = A[2][0]; J[4][2] = A[1][0]; J[4][3] = A[2][1]; J[4][4] = A[2][2] + A[1][1]; J[4][5] = A[1][2];
                 J[5][2] = 2 * A[2][0]; J[5][4] = 2 * A[2][1]; J[5][5] = 2 * A[2][2];
+#pragma unroll
                 for (int r = 0; r < 6; ++r) {
                     J[r][r] += dd2;
                     J[r][0] += cf * x[r];
                     J[r][3] += cf * x[r];
                     J[r][5] += cf * x[r];
                 }
+#pragma unroll
                 for (int r = 0; r < 6; ++r) {
+#pragma unroll
                     for (int q = 0; q < 6; ++q) M[r][q] = J[q][r];
                     M[r][6] = lx[r];
                 }
             }
-            // Gaussian elimination with partial pivoting
+            // Gaussian elimination with partial pivoting.  The pivot row is found
+            // by compare-and-exchange with each lower row (a running maximum),
+            // so every index is a compile-time constant and M stays in registers.
+#pragma unroll
             for (int c = 0; c < 6; ++c) {
-                int p = c;
-                double best = fabs(M[c][c]);
-                for (int r = c + 1; r < 6; ++r)
-                    if (fabs(M[r][c]) > best) { best = fabs(M[r][c]); p = r; }
-                if (p != c)
-                    for (int q = c; q < 7; ++q) { const double tmp = M[c][q]; M[c][q] = M[p][q]; M[p][q] = tmp; }
+#pragma unroll
+                for (int r = c + 1; r < 6; ++r) {
+                    const bool sw = fabs(M[r][c]) > fabs(M[c][c]);
+#pragma unroll
+                    for (int q = c; q < 7; ++q) {
+                        const double u0 = M[c][q], u1 = M[r][q];
+                        M[c][q] = sw ? u1 : u0;
+                        M[r][q] = sw ? u0 : u1;
+                    }
+                }
                 const double inv = 1.0 / M[c][c];
+#pragma unroll
                 for (int r = c + 1; r < 6; ++r) {
                     const double fr = M[r][c] * inv;
+#pragma unroll
                     for (int q = c; q < 7; ++q) M[r][q] -= fr * M[c][q];
                 }
             }
             double mu[6];
+#pragma unroll
             for (int r = 5; r >= 0; --r) {
                 double s = M[r][6];
+#pragma unroll
                 for (int q = r + 1; q < 6; ++q) s -= M[r][q] * mu[q];
                 mu[r] = s / M[r][r];
             }
             // parameters: G = L(x) + (1 + f dt/Wi) x - b, b includes dt/Wi on the diagonal
             double mx = 0.0;
+#pragma unroll
             for (int m = 0; m < 6; ++m) mx += mu[m] * x[m];
             gwi = f * dt / (wi * wi) * mx - dt / (wi * wi) * (mu[0] + mu[3] + mu[5]);
             gl2 = -dt / wi * (3.0 - tr) / (den * den) * mx;
@@ -761,6 +785,7 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             s[11] = 1.0 / 6 + (w1 - fabs(w1)) * dt / (2 * dZ);
             s[12] = (w1 + fabs(w1)) * dt / (2 * dZ);
             double ls[13];
+#pragma unroll
             for (int q = 0; q < 13; ++q) ls[q] = 0.0;
             // selection codes (as the forward kernel reads them)
             const int cself = a.codes[qix(g, i, j, k)];
@@ -778,11 +803,14 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
             const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
             const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-            double pw[4][3], nw[4][3];    // face weights by code 1..4 (index code-1)
-            for (int c = 0; c < 4; ++c) {
-                wface_p(c + 1, pw[c][0], pw[c][1], pw[c][2]);
-                wface_n(c + 1, nw[c][0], nw[c][1], nw[c][2]);
-            }
+            // face weights of the cell's own faces and of the neighbours' faces,
+            // by selection code
+            auto wp = [](int code) { W3 w; wface_p(code, w.m, w.c, w.p); return w; };
+            auto wn = [](int code) { W3 w; wface_n(code, w.m, w.c, w.p); return w; };
+            const W3 wpx = wp(isx), wnx = wn(isx), wpy = wp(isy), wny = wn(isy), wpz = wp(isz), wnz = wn(isz);
+            const W3 qx = wp(cxp + 1), rx = wn(cxm + 1), qy = wp(cyp + 1), ry = wn(cym + 1);
+            const W3 qz = wp(czp + 1), rz = wn(czm + 1);
+#pragma unroll
             for (int m = 0; m < 6; ++m) {
                 const double *Cm = a.C + m * cs;
                 double *Lm = a.lC + m * cs;
@@ -790,16 +818,15 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
                 double lc0 = 0.0;   // accumulated weight at the cell itself
                 // one direction: own faces (code is, coefficients sp on the p face, sn on the n face),
                 // the + neighbour's p face (code cp_, coefficient sq), the - neighbour's n face (code cm_, sr)
-                auto dir = [&](int is, int off, int hp, int cp_, int hm, int cm_, double sp, double sn, double sq,
-                               double sr, bool pghost, bool mghost, double &lsp, double &lsn, double &lsq,
-                               double &lsr) {
+                auto dir = [&](W3 wp_, W3 wn_, int off, int hp, W3 wq, int hm, W3 wr, double sp, double sn,
+                               double sq, double sr, bool pghost, bool mghost, double &lsp, double &lsn,
+                               double &lsq, double &lsr) {
                     const double cmv = Cm[h - off], c0v = Cm[h], cpv = Cm[h + off];
-                    const double *wp_ = pw[is - 1], *wn_ = nw[is - 1];
-                    lsp += mum * (wp_[0] * cmv + wp_[1] * c0v + wp_[2] * cpv);
-                    lsn += mum * (wn_[0] * cmv + wn_[1] * c0v + wn_[2] * cpv);
-                    const double am = mum * (sp * wp_[0] + sn * wn_[0]);
-                    const double ap = mum * (sp * wp_[2] + sn * wn_[2]);
-                    lc0 += mum * (sp * wp_[1] + sn * wn_[1]);
+                    lsp += mum * (wp_.m * cmv + wp_.c * c0v + wp_.p * cpv);
+                    lsn += mum * (wn_.m * cmv + wn_.c * c0v + wn_.p * cpv);
+                    const double am = mum * (sp * wp_.m + sn * wn_.m);
+                    const double ap = mum * (sp * wp_.p + sn * wn_.p);
+                    lc0 += mum * (sp * wp_.c + sn * wn_.c);
                     if (am != 0.0) atomicAdd(&Lm[h - off], am);
                     if (ap != 0.0) atomicAdd(&Lm[h + off], ap);
                     // + neighbour's p face
@@ -807,13 +834,12 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
                         lsq += mum * Cm[hp];
                         if (sq != 0.0) atomicAdd(&Lm[hp], mum * sq);
                     } else {
-                        const double *wq = pw[cp_];
-                        lsq += mum * (wq[0] * Cm[hp - off] + wq[1] * Cm[hp] + wq[2] * Cm[hp + off]);
+                        lsq += mum * (wq.m * Cm[hp - off] + wq.c * Cm[hp] + wq.p * Cm[hp + off]);
                         const double b = mum * sq;
                         if (b != 0.0) {
-                            if (wq[0] != 0.0) atomicAdd(&Lm[hp - off], b * wq[0]);
-                            atomicAdd(&Lm[hp], b * wq[1]);
-                            if (wq[2] != 0.0) atomicAdd(&Lm[hp + off], b * wq[2]);
+                            if (wq.m != 0.0) atomicAdd(&Lm[hp - off], b * wq.m);
+                            atomicAdd(&Lm[hp], b * wq.c);
+                            if (wq.p != 0.0) atomicAdd(&Lm[hp + off], b * wq.p);
                         }
                     }
                     // - neighbour's n face
@@ -821,20 +847,21 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
                         lsr += mum * Cm[hm];
                         if (sr != 0.0) atomicAdd(&Lm[hm], mum * sr);
                     } else {
-                        const double *wr = nw[cm_];
-                        lsr += mum * (wr[0] * Cm[hm - off] + wr[1] * Cm[hm] + wr[2] * Cm[hm + off]);
+                        lsr += mum * (wr.m * Cm[hm - off] + wr.c * Cm[hm] + wr.p * Cm[hm + off]);
                         const double b = mum * sr;
                         if (b != 0.0) {
-                            if (wr[0] != 0.0) atomicAdd(&Lm[hm - off], b * wr[0]);
-                            atomicAdd(&Lm[hm], b * wr[1]);
-                            if (wr[2] != 0.0) atomicAdd(&Lm[hm + off], b * wr[2]);
+                            if (wr.m != 0.0) atomicAdd(&Lm[hm - off], b * wr.m);
+                            atomicAdd(&Lm[hm], b * wr.c);
+                            if (wr.p != 0.0) atomicAdd(&Lm[hm + off], b * wr.p);
                         }
                     }
                 };
                 // x: pxm (s3, own p), nxp (s2, own n), pxp (s1, neighbour i+1), nxm (s4, neighbour i-1)
-                dir(isx, ox, hxp, cxp, hxm, cxm, s[3], s[2], s[1], s[4], false, false, ls[3], ls[2], ls[1], ls[4]);
-                dir(isy, oy, hyp, cyp, hym, cym, s[7], s[6], s[5], s[8], yp_ghost, ym_ghost, ls[7], ls[6], ls[5], ls[8]);
-                dir(isz, oz, hzp, czp, hzm, czm, s[11], s[10], s[9], s[12], false, false, ls[11], ls[10], ls[9], ls[12]);
+                dir(wpx, wnx, ox, hxp, qx, hxm, rx, s[3], s[2], s[1], s[4], false, false, ls[3], ls[2], ls[1], ls[4]);
+                dir(wpy, wny, oy, hyp, qy, hym, ry, s[7], s[6], s[5], s[8], yp_ghost, ym_ghost, ls[7], ls[6], ls[5],
+                    ls[8]);
+                dir(wpz, wnz, oz, hzp, qz, hzm, rz, s[11], s[10], s[9], s[12], false, false, ls[11], ls[10], ls[9],
+                    ls[12]);
                 atomicAdd(&Lm[h], lc0);
             }
             // s coefficients -> velocities

@@ -565,9 +565,15 @@ def step(st: dict, prm: dict, g: TGrid, ph: TPhys, geom, first: bool):
     dt, re = ph.dt, ph.re
     wi, beta, lp2 = prm["wi"], prm["beta"], prm["lp2"]
     U, V, W, P, C = st["U"], st["V"], st["W"], st["P"], st["C"]
-    Cn_int, iters = polymer(C, U, V, W, g, dt, wi, lp2, ph.newton_dc, ph.newton_eps, ph.newton_itrmax)
-    Cn = bc(torch.stack([embed(c, g) for c in Cn_int], 0), "c", g)
-    T = stress(Cn, g, lp2, (1.0 - beta) / (re * wi))
+    if _num(beta) == 1.0:
+        # Newtonian: C and T vanish and the polymer stage is skipped (fenep.f90:2479-2485)
+        Cn = torch.zeros_like(C)
+        T = [torch.zeros_like(sh(U, g)) for _ in range(3)]
+        iters = None
+    else:
+        Cn_int, iters = polymer(C, U, V, W, g, dt, wi, lp2, ph.newton_dc, ph.newton_eps, ph.newton_itrmax)
+        Cn = bc(torch.stack([embed(c, g) for c in Cn_int], 0), "c", g)
+        T = stress(Cn, g, lp2, (1.0 - beta) / (re * wi))
     A, B = conv_visc(U, V, W, g, beta / re)
     A0 = A if first else st["A0"]
     T0 = T if first else st["T0"]

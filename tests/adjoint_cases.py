@@ -25,12 +25,19 @@ if str(ROOT / "oracle") not in sys.path:
 
 def case(name: str, oracle_fns, spinup: int = 10):
     """(workload, state, step0) of a gradient case: 'channel' (32x16x16, y walls,
-    two cylinders) or 'periodic' (16^3, one cylinder)."""
-    if name == "channel":
+    two filled cylinders), 'periodic' (16^3, one cylinder), 'moving' (the channel
+    with surface-ring cylinders spinning and the upper wall moving) or
+    'newtonian' (the channel with beta = 1: no polymer stage)."""
+    if name in ("channel", "moving", "newtonian"):
         w = configs.scaled(configs.c4_adjoint(), 32, 16, 16)
     else:
         w = configs.scaled(configs.c2_3d(), 16, 16, 16)
     cyls = tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls)
+    if name == "moving":
+        cyls = tuple(replace(c, filled=0, spin=0.4 * (1 - 2 * l)) for l, c in enumerate(cyls))
+        w = replace(w, grid=replace(w.grid, uwall=0.3))
+    if name == "newtonian":
+        w = replace(w, phys=replace(w.phys, beta=1.0))
     w = replace(w, cyls=cyls)
     st = configs.initial_state(w)
     g = w.grid
@@ -127,8 +134,9 @@ def torch_grad(w, st, step0, nsteps, weights=None, seed=None):
             if n in seed:
                 J = J + (cur["T0"][q] * t(seed[n])).sum()
     J.backward()
-    gp = [prm["wi"].grad.item(), prm["beta"].grad.item(), prm["lp2"].grad.item()]
-    gp += list(prm["centres"].grad.numpy().ravel())
+    val = lambda v: v.grad.numpy() if v.grad is not None else np.zeros(tuple(v.shape))
+    gp = [float(val(prm["wi"])), float(val(prm["beta"])), float(val(prm["lp2"]))]
+    gp += list(val(prm["centres"]).ravel())
     dstate = {}
     for n, v in leaves.items():
         a = v.grad.numpy() if v.grad is not None else np.zeros(tuple(v.shape))

@@ -3,7 +3,8 @@
 * Against the torch restatement (oracle/f8_torch.py, pinned to the C++ oracle
   and to its own central differences): the gradient of the time-averaged
   total drag with respect to Wi, beta, L^2 and the cylinder centres to 1e-8
-  relative, with and without the AB2 start step, channel and periodic box.
+  relative, with and without the AB2 start step, channel and periodic box,
+  spinning surface-ring cylinders under a moving wall, and beta = 1.
 * The vector-Jacobian product of the whole state: seeded adjoints of the final
   state give the adjoint of the initial state and the parameters to 1e-8.
 * Checkpointing: every checkpoint interval gives the same gradient, and the
@@ -38,7 +39,8 @@ def close(a, b, rel):
     return np.all(np.abs(a - b) <= rel * np.abs(b) + 1e-3 * rel * scale)
 
 
-@pytest.mark.parametrize("name,spinup", [("channel", 10), ("channel", 0), ("periodic", 10)])
+@pytest.mark.parametrize("name,spinup", [("channel", 10), ("channel", 0), ("periodic", 10), ("moving", 10),
+                                         ("newtonian", 10)])
 def test_grad_matches_torch(gpu, oracle, name, spinup):
     w, st, step0 = case(name, oracle, spinup=spinup)
     n = 4
