@@ -183,6 +183,14 @@ struct f8_ctx {
         gm.free_all();
         if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
         stats_probe = nullptr;
+        for (int b = 0; b < 2; ++b) {
+            if (d.aux[b]) cudaStreamDestroy(d.aux[b]);
+            if (d.ev_join[b]) cudaEventDestroy(d.ev_join[b]);
+            d.aux[b] = nullptr;
+            d.ev_join[b] = nullptr;
+        }
+        if (d.ev_fork) cudaEventDestroy(d.ev_fork);
+        d.ev_fork = nullptr;
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
@@ -367,6 +375,15 @@ int setup(f8_ctx *c) {
         d.plane_cl = g.walls ? wall_plane_cluster(g.ny, g.nz, (size_t)optin) : 0;
         if (g.walls) d.fused_planes = (d.plane_cl > 0 || (size_t)12 * ((g.ny + 2) | 1) * g.nz <= (size_t)optin) ? 1 : 0;
         else d.fused_planes = (size_t)8 * (g.ny + 1) * g.nz <= (size_t)optin ? 1 : 0;
+        if (d.fused_planes) {
+            // side streams and spectra of the V and W Helmholtz solves
+            for (int b = 0; b < 2; ++b) {
+                API_CUDA(c, c->alloc(&d.HfB[b], nspec));
+                API_CUDA(c, cudaStreamCreateWithFlags(&d.aux[b], cudaStreamNonBlocking));
+                API_CUDA(c, cudaEventCreateWithFlags(&d.ev_join[b], cudaEventDisableTiming));
+            }
+            API_CUDA(c, cudaEventCreateWithFlags(&d.ev_fork, cudaEventDisableTiming));
+        }
         {
             std::vector<float2> t2(std::max(1, g.nz / 2));
             for (int t = 0; t < g.nz / 2; ++t) {

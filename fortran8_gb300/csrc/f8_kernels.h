@@ -51,6 +51,10 @@ struct Dev {
     float *Rhf, *Rlf;                      // df64 Poisson right-hand side (interior)
     float *Rdf;                            // Poisson defect (interior)
     float *Hf, *H2f;                       // FP32 spectra
+    float *HfB[2];                         // spectra of the V and W Helmholtz solves when they run
+                                           // beside the U solve (fused spectral path)
+    cudaStream_t aux[2];                   // the side streams of those two solves (0: none)
+    cudaEvent_t ev_fork, ev_join[2];
     float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
     float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
     int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory

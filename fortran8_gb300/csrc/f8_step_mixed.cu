@@ -1149,10 +1149,11 @@ bool xinv_warp(const Dev &d, const float2 *S, XOutF out, int nrow, int jlo, int 
 }
 
 template <typename TS>
-cudaError_t solve_periodic_fused(Dev &d, const TS *src, XOutF out, float lhs0, float lhs1, cudaStream_t s) {
+cudaError_t solve_periodic_fused(Dev &d, const TS *src, XOutF out, float lhs0, float lhs1, cudaStream_t s,
+                                 float *spec = nullptr) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1;
-    float2 *S = reinterpret_cast<float2 *>(d.Hf);
+    float2 *S = reinterpret_cast<float2 *>(spec ? spec : d.Hf);
     const int rb = x_rows_per_block(nx);
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
@@ -1172,10 +1173,10 @@ cudaError_t solve_periodic_fused(Dev &d, const TS *src, XOutF out, float lhs0, f
 }
 
 template <typename TS>
-cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStream_t s) {
+cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStream_t s, float *spec = nullptr) {
     const Geo &g = d.g;
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxh = nx / 2 + 1, lj = ny + 2;
-    float2 *S = reinterpret_cast<float2 *>(d.Hf);
+    float2 *S = reinterpret_cast<float2 *>(spec ? spec : d.Hf);
     const int rb = x_rows_per_block(nx);
     const int thr = (rb / 2) * (nx / 2);
     const size_t smx = x_smem(nx, rb);
@@ -1445,13 +1446,36 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         if ((e = cudaGetLastError())) return e;
     }
     mark(4);
-    // Helmholtz solves for the FP32 increments dU (U* = U^n + dU)
+    // Helmholtz solves for the FP32 increments dU (U* = U^n + dU).  On the
+    // fused spectral path the three solves are independent branches: V and W
+    // run on side streams with their own spectra, forked from and joined to
+    // the step's stream (parallel branches of the captured graph), so their
+    // x transforms fill the SMs that one solve's kernels leave idle.
     const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+    const bool branches = d.fused_planes && d.aux[0] && d.aux[1];
+    if (branches) {
+        F8_CUDA_RET(cudaEventRecord(d.ev_fork, s));
+        for (int b = 0; b < 2; ++b) F8_CUDA_RET(cudaStreamWaitEvent(d.aux[b], d.ev_fork, 0));
+    }
     for (int c = 0; c < 3; ++c) {
         const XOutF out{d.dUf[c], nullptr, 0};
-        if (!g.walls) e = solve_periodic_f(d, d.Qf[c], out, 1.0, lhs1, s);
-        else e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
+        if (branches) {
+            cudaStream_t sc = c == 0 ? s : d.aux[c - 1];
+            float *spec = c == 0 ? d.Hf : d.HfB[c - 1];
+            if (!g.walls) e = solve_periodic_fused<float>(d, d.Qf[c], out, 1.0f, (float)lhs1, sc, spec);
+            else e = solve_walls_fused<float>(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, sc, spec);
+        } else if (!g.walls) {
+            e = solve_periodic_f(d, d.Qf[c], out, 1.0, lhs1, s);
+        } else {
+            e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
+        }
         if (e) return e;
+    }
+    if (branches) {
+        for (int b = 0; b < 2; ++b) {
+            F8_CUDA_RET(cudaEventRecord(d.ev_join[b], d.aux[b]));
+            F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_join[b], 0));
+        }
     }
     mark(5);
     // Poisson: FP32 solve + one df64 defect correction.  The increments and
