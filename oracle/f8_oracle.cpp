@@ -255,71 +255,96 @@ int reconstruct3(const double *cm, const double *c0, const double *cp, double *f
     return index;
 }
 
-// Face arrays: Cpd holds faces 0..N (N+1 of them) of each line, face f is
-// between cell f and f+1.  Cell n writes Cp(n-1) and Cn(n).
+// Rows of the polymer update.  Periodic: 1..NY.  With y walls also the ghost
+// rows 0 and NY+1: the reference's wall mode runs the polymer update on every
+// row of its box (CpxCnx .. Lyapunov, fenep_2d.f90:138-348, 1912-1929), where
+// the rows beyond the walls hold zero C and velocity (C_kabe, U_kabe, V_kabe,
+// fenep_2d.f90:1097-1143), so the ghost rows evolve with the step and the
+// stress reads them; they are re-extrapolated only at the end of the step
+// (fft_march_kabe, fenep_2d.f90:1371-1374).  The reference's published
+// wall-channel accuracy table (_theory.py:44-49) is reproduced this way.
+inline int prow_lo(const OCtx &c) { return c.walls ? 0 : 1; }
+inline int prow_hi(const OCtx &c) { return c.walls ? c.NY + 1 : c.NY; }
+
+// C of cell (i, j, k), zero beyond the ghost rows (the wall mode's outside rows)
+inline const double *cval(const OCtx &c, const double *C, int nc, int i, int j, int k) {
+    static const double zero[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    return (j < 0 || j > c.NY + 1) ? zero : C + (size_t)nc * c.hidx(i, j, k);
+}
+inline double vval(const OCtx &c, const double *A, int i, int j, int k) {
+    return (j < 0 || j > c.NY + 1) ? 0.0 : A[c.hidx(i, j, k)];
+}
+
+// Face arrays: Cpd holds the faces of each line, face f is between cell f and
+// f+1; cell n writes Cp(n-1) and Cn(n).  Lines along y cover faces jlo-1 .. jhi.
+struct FaceIdx {
+    int NX, NY, NZ, jlo, nr;
+    size_t x(int f, int j, int k) const { return (size_t)6 * ((size_t)f + (size_t)(NX + 1) * ((size_t)(j - jlo) + (size_t)nr * (k - 1))); }
+    size_t y(int i, int f, int k) const { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)(f - jlo + 1) + (size_t)(nr + 1) * (k - 1))); }
+    size_t z(int i, int j, int f) const { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)(j - jlo) + (size_t)nr * f)); }
+    size_t cell(int i, int j, int k) const { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)(j - jlo) + (size_t)nr * (k - 1))); }
+};
+inline FaceIdx face_idx(const OCtx &c) {
+    return FaceIdx{c.NX, c.NY, c.NZ, prow_lo(c), prow_hi(c) - prow_lo(c) + 1};
+}
+
 void polymer_faces3(OCtx &c) {
-    const int NX = c.NX, NY = c.NY, NZ = c.NZ;
+    const int NX = c.NX, NY = c.NY, NZ = c.NZ, jlo = prow_lo(c), jhi = prow_hi(c);
+    const FaceIdx F = face_idx(c);
     const double *C = c.C.data();
-    // x faces: (6, 0:NX, NY, NZ)
-    auto fx = [&](int f, int j, int k) { return (size_t)6 * ((size_t)f + (size_t)(NX + 1) * ((size_t)(j - 1) + (size_t)NY * (k - 1))); };
-    auto fy = [&](int i, int f, int k) { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)f + (size_t)(NY + 1) * (k - 1))); };
-    auto fz = [&](int i, int j, int f) { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)(j - 1) + (size_t)NY * f)); };
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= NZ; ++k)
-        for (int j = 1; j <= NY; ++j)
+        for (int j = jlo; j <= jhi; ++j)
             for (int i = 1; i <= NX; ++i) {
-                const double *c0 = C + 6 * c.hidx(i, j, k);
-                reconstruct3(C + 6 * c.hidx(i - 1, j, k), c0, C + 6 * c.hidx(i + 1, j, k),
-                             &c.Cpx[fx(i - 1, j, k)], &c.Cnx[fx(i, j, k)]);
-                reconstruct3(C + 6 * c.hidx(i, j - 1, k), c0, C + 6 * c.hidx(i, j + 1, k),
-                             &c.Cpy[fy(i, j - 1, k)], &c.Cny[fy(i, j, k)]);
-                reconstruct3(C + 6 * c.hidx(i, j, k - 1), c0, C + 6 * c.hidx(i, j, k + 1),
-                             &c.Cpz[fz(i, j, k - 1)], &c.Cnz[fz(i, j, k)]);
+                const double *c0 = cval(c, C, 6, i, j, k);
+                reconstruct3(cval(c, C, 6, i - 1, j, k), c0, cval(c, C, 6, i + 1, j, k),
+                             &c.Cpx[F.x(i - 1, j, k)], &c.Cnx[F.x(i, j, k)]);
+                reconstruct3(cval(c, C, 6, i, j - 1, k), c0, cval(c, C, 6, i, j + 1, k),
+                             &c.Cpy[F.y(i, j - 1, k)], &c.Cny[F.y(i, j, k)]);
+                reconstruct3(cval(c, C, 6, i, j, k - 1), c0, cval(c, C, 6, i, j, k + 1),
+                             &c.Cpz[F.z(i, j, k - 1)], &c.Cnz[F.z(i, j, k)]);
             }
-    // Periodic face copies (fenep.f90:240-241, 310-311, 380-381).  At y-walls the
-    // faces Cpy(NY) and Cny(0) belong to the ghost rows; Cstar multiplies them
-    // by exactly zero there (the wall-normal velocity vanishes on the wall), so
-    // they are set to the ghost value, which is finite.
+    // Periodic face copies (fenep.f90:240-241, 310-311, 380-381).  With walls
+    // the faces beyond the ghost rows belong to the outside cells; Cstar
+    // multiplies them by exactly zero (the wall-normal velocity vanishes there).
     for (int k = 1; k <= NZ; ++k)
-        for (int j = 1; j <= NY; ++j)
+        for (int j = jlo; j <= jhi; ++j)
             for (int m = 0; m < 6; ++m) {
-                c.Cpx[fx(NX, j, k) + m] = c.Cpx[fx(0, j, k) + m];
-                c.Cnx[fx(0, j, k) + m] = c.Cnx[fx(NX, j, k) + m];
+                c.Cpx[F.x(NX, j, k) + m] = c.Cpx[F.x(0, j, k) + m];
+                c.Cnx[F.x(0, j, k) + m] = c.Cnx[F.x(NX, j, k) + m];
             }
     for (int k = 1; k <= NZ; ++k)
         for (int i = 1; i <= NX; ++i)
             for (int m = 0; m < 6; ++m) {
                 if (!c.walls) {
-                    c.Cpy[fy(i, NY, k) + m] = c.Cpy[fy(i, 0, k) + m];
-                    c.Cny[fy(i, 0, k) + m] = c.Cny[fy(i, NY, k) + m];
+                    c.Cpy[F.y(i, NY, k) + m] = c.Cpy[F.y(i, 0, k) + m];
+                    c.Cny[F.y(i, 0, k) + m] = c.Cny[F.y(i, NY, k) + m];
                 } else {
-                    c.Cpy[fy(i, NY, k) + m] = C[6 * c.hidx(i, NY + 1, k) + m];
-                    c.Cny[fy(i, 0, k) + m] = C[6 * c.hidx(i, 0, k) + m];
+                    c.Cpy[F.y(i, jhi, k) + m] = 0.0;
+                    c.Cny[F.y(i, jlo - 1, k) + m] = 0.0;
                 }
             }
-    for (int j = 1; j <= NY; ++j)
+    for (int j = jlo; j <= jhi; ++j)
         for (int i = 1; i <= NX; ++i)
             for (int m = 0; m < 6; ++m) {
-                c.Cpz[fz(i, j, NZ) + m] = c.Cpz[fz(i, j, 0) + m];
-                c.Cnz[fz(i, j, 0) + m] = c.Cnz[fz(i, j, NZ) + m];
+                c.Cpz[F.z(i, j, NZ) + m] = c.Cpz[F.z(i, j, 0) + m];
+                c.Cnz[F.z(i, j, 0) + m] = c.Cnz[F.z(i, j, NZ) + m];
             }
 }
 
 // fenep.f90:464-507
 void cstar3(OCtx &c) {
-    const int NX = c.NX, NY = c.NY, NZ = c.NZ;
+    const int NX = c.NX, NZ = c.NZ, jlo = prow_lo(c), jhi = prow_hi(c);
+    const FaceIdx F = face_idx(c);
     const double dt = c.ph.dt, dX = c.dX, dY = c.dY, dZ = c.dZ;
-    auto fx = [&](int f, int j, int k) { return (size_t)6 * ((size_t)f + (size_t)(NX + 1) * ((size_t)(j - 1) + (size_t)NY * (k - 1))); };
-    auto fy = [&](int i, int f, int k) { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)f + (size_t)(NY + 1) * (k - 1))); };
-    auto fz = [&](int i, int j, int f) { return (size_t)6 * ((size_t)(i - 1) + (size_t)NX * ((size_t)(j - 1) + (size_t)NY * f)); };
     const double *U = c.U.data(), *V = c.V.data(), *W = c.W.data();
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= NZ; ++k)
-        for (int j = 1; j <= NY; ++j)
+        for (int j = jlo; j <= jhi; ++j)
             for (int i = 1; i <= NX; ++i) {
-                double u1 = U[c.hidx(i - 1, j, k)], u2 = U[c.hidx(i, j, k)];
-                double v1 = V[c.hidx(i, j - 1, k)], v2 = V[c.hidx(i, j, k)];
-                double w1 = W[c.hidx(i, j, k - 1)], w2 = W[c.hidx(i, j, k)];
+                double u1 = vval(c, U, i - 1, j, k), u2 = vval(c, U, i, j, k);
+                double v1 = vval(c, V, i, j - 1, k), v2 = vval(c, V, i, j, k);
+                double w1 = vval(c, W, i, j, k - 1), w2 = vval(c, W, i, j, k);
                 double s1 = (-u2 + std::fabs(u2)) * dt / (2 * dX);
                 double s2 = 1.0 / 6 + (-u2 - std::fabs(u2)) * dt / (2 * dX);
                 double s3 = 1.0 / 6 + (u1 - std::fabs(u1)) * dt / (2 * dX);
@@ -332,13 +357,13 @@ void cstar3(OCtx &c) {
                 double s10 = 1.0 / 6 + (-w2 - std::fabs(w2)) * dt / (2 * dZ);
                 double s11 = 1.0 / 6 + (w1 - std::fabs(w1)) * dt / (2 * dZ);
                 double s12 = (w1 + std::fabs(w1)) * dt / (2 * dZ);
-                const double *pxm = &c.Cpx[fx(i - 1, j, k)], *pxp = &c.Cpx[fx(i, j, k)];
-                const double *nxm = &c.Cnx[fx(i - 1, j, k)], *nxp = &c.Cnx[fx(i, j, k)];
-                const double *pym = &c.Cpy[fy(i, j - 1, k)], *pyp = &c.Cpy[fy(i, j, k)];
-                const double *nym = &c.Cny[fy(i, j - 1, k)], *nyp = &c.Cny[fy(i, j, k)];
-                const double *pzm = &c.Cpz[fz(i, j, k - 1)], *pzp = &c.Cpz[fz(i, j, k)];
-                const double *nzm = &c.Cnz[fz(i, j, k - 1)], *nzp = &c.Cnz[fz(i, j, k)];
-                double *out = &c.Cx[6 * c.iidx(i, j, k)];
+                const double *pxm = &c.Cpx[F.x(i - 1, j, k)], *pxp = &c.Cpx[F.x(i, j, k)];
+                const double *nxm = &c.Cnx[F.x(i - 1, j, k)], *nxp = &c.Cnx[F.x(i, j, k)];
+                const double *pym = &c.Cpy[F.y(i, j - 1, k)], *pyp = &c.Cpy[F.y(i, j, k)];
+                const double *nym = &c.Cny[F.y(i, j - 1, k)], *nyp = &c.Cny[F.y(i, j, k)];
+                const double *pzm = &c.Cpz[F.z(i, j, k - 1)], *pzp = &c.Cpz[F.z(i, j, k)];
+                const double *nzm = &c.Cnz[F.z(i, j, k - 1)], *nzp = &c.Cnz[F.z(i, j, k)];
+                double *out = &c.Cx[F.cell(i, j, k)];
                 for (int m = 0; m < 6; ++m)
                     out[m] = s3 * pxm[m] + s1 * pxp[m] + s4 * nxm[m] + s2 * nxp[m]
                              + s7 * pym[m] + s5 * pyp[m] + s8 * nym[m] + s6 * nyp[m]
@@ -424,23 +449,24 @@ int newton_cell3(const double A0T[3][3], const double *b, double *x, const f8_ph
 
 // fenep.f90:518-585
 void lyapunov3(OCtx &c) {
-    const int NX = c.NX, NY = c.NY, NZ = c.NZ;
+    const int NX = c.NX, NZ = c.NZ, jlo = prow_lo(c), jhi = prow_hi(c);
+    const FaceIdx F = face_idx(c);
     const double dt = c.ph.dt, wi = c.ph.wi, dX = c.dX, dY = c.dY, dZ = c.dZ;
     const double *U = c.U.data(), *V = c.V.data(), *W = c.W.data();
     long long iters = 0, unconv = 0;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : iters, unconv)
     for (int k = 1; k <= NZ; ++k)
-        for (int j = 1; j <= NY; ++j)
+        for (int j = jlo; j <= jhi; ++j)
             for (int i = 1; i <= NX; ++i) {
                 double b[6];
-                const double *cx = &c.Cx[6 * c.iidx(i, j, k)];
+                const double *cx = &c.Cx[F.cell(i, j, k)];
                 for (int m = 0; m < 6; ++m) b[m] = cx[m];
                 b[0] = b[0] + dt / wi;
                 b[3] = b[3] + dt / wi;
                 b[5] = b[5] + dt / wi;
-                auto u = [&](int a, int bb, int cc) { return U[c.hidx(a, bb, cc)]; };
-                auto v = [&](int a, int bb, int cc) { return V[c.hidx(a, bb, cc)]; };
-                auto w = [&](int a, int bb, int cc) { return W[c.hidx(a, bb, cc)]; };
+                auto u = [&](int a, int bb, int cc) { return vval(c, U, a, bb, cc); };
+                auto v = [&](int a, int bb, int cc) { return vval(c, V, a, bb, cc); };
+                auto w = [&](int a, int bb, int cc) { return vval(c, W, a, bb, cc); };
                 double A0[3][3];
                 A0[0][0] = -dt * (-u(i - 1, j, k) + u(i, j, k)) / dX;
                 A0[0][1] = -dt * (-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) / (4 * dX);
@@ -462,13 +488,20 @@ void lyapunov3(OCtx &c) {
                 double *outp = &c.C0[6 * c.hidx(i, j, k)];  // new C goes to a side buffer
                 for (int m = 0; m < 6; ++m) outp[m] = x[m];
             }
-    // copy the new interior values back (the reference overwrites C in place;
-    // each cell reads only its own old value, so the result is the same)
+    // copy the new values back (the reference overwrites C in place; each cell
+    // reads only its own old value, so the result is the same)
     for (int k = 1; k <= NZ; ++k)
-        for (int j = 1; j <= NY; ++j)
+        for (int j = jlo; j <= jhi; ++j)
             for (int i = 1; i <= NX; ++i)
                 for (int m = 0; m < 6; ++m) c.C[6 * c.hidx(i, j, k) + m] = c.C0[6 * c.hidx(i, j, k) + m];
-    bc_c(c, c.C.data());
+    // C_PBM after Lyapunov (fenep_2d.f90:348): with walls only the periodic
+    // x and z copies (the ghost rows keep their updated values)
+    if (c.walls) {
+        bc_periodic_xz(c, c.C.data(), 6);
+        bc_periodic_z(c, c.C.data(), 6);
+    } else {
+        bc_c(c, c.C.data());
+    }
     c.newton_iters += iters;
     c.newton_unconv += unconv;
 }
@@ -596,17 +629,21 @@ int newton_cell2(const double A0T[2][2], const double *b, double *x, const f8_ph
 void polymer2(OCtx &c) {
     const int NX = c.NX, NY = c.NY;
     const int k = 1;
+    const bool ext = c.walls;   // ghost rows updated too (see prow_lo)
+    const int jlo = prow_lo(c), jhi = prow_hi(c);
     const double *C = c.C.data();
-    std::vector<double> Cpx(3 * (NX + 1) * NY), Cnx(3 * (NX + 1) * NY), Cpy(3 * NX * (NY + 1)), Cny(3 * NX * (NY + 1));
-    auto fx = [&](int f, int j) { return (size_t)3 * ((size_t)f + (size_t)(NX + 1) * (j - 1)); };
-    auto fy = [&](int i, int f) { return (size_t)3 * ((size_t)(i - 1) + (size_t)NX * f); };
-    for (int j = 1; j <= NY; ++j)
+    auto cp_ = [&](int i, int j) { return cval(c, C, 3, i, j, k); };
+    const int nr = jhi - jlo + 1;
+    std::vector<double> Cpx(3 * (NX + 1) * nr), Cnx(3 * (NX + 1) * nr), Cpy(3 * NX * (nr + 1), 0.0), Cny(3 * NX * (nr + 1), 0.0);
+    auto fx = [&](int f, int j) { return (size_t)3 * ((size_t)f + (size_t)(NX + 1) * (j - jlo)); };
+    auto fy = [&](int i, int f) { return (size_t)3 * ((size_t)(i - 1) + (size_t)NX * (f - (jlo - 1))); };
+    for (int j = jlo; j <= jhi; ++j)
         for (int i = 1; i <= NX; ++i) {
-            const double *c0 = C + 3 * c.hidx(i, j, k);
-            reconstruct2(C + 3 * c.hidx(i - 1, j, k), c0, C + 3 * c.hidx(i + 1, j, k), &Cpx[fx(i - 1, j)], &Cnx[fx(i, j)]);
-            reconstruct2(C + 3 * c.hidx(i, j - 1, k), c0, C + 3 * c.hidx(i, j + 1, k), &Cpy[fy(i, j - 1)], &Cny[fy(i, j)]);
+            const double *c0 = cp_(i, j);
+            reconstruct2(cp_(i - 1, j), c0, cp_(i + 1, j), &Cpx[fx(i - 1, j)], &Cnx[fx(i, j)]);
+            reconstruct2(cp_(i, j - 1), c0, cp_(i, j + 1), &Cpy[fy(i, j - 1)], &Cny[fy(i, j)]);
         }
-    for (int j = 1; j <= NY; ++j)
+    for (int j = jlo; j <= jhi; ++j)
         for (int m = 0; m < 3; ++m) {
             Cpx[fx(NX, j) + m] = Cpx[fx(0, j) + m];
             Cnx[fx(0, j) + m] = Cnx[fx(NX, j) + m];
@@ -617,18 +654,20 @@ void polymer2(OCtx &c) {
                 Cpy[fy(i, NY) + m] = Cpy[fy(i, 0) + m];
                 Cny[fy(i, 0) + m] = Cny[fy(i, NY) + m];
             } else {
-                Cpy[fy(i, NY) + m] = C[3 * c.hidx(i, NY + 1, k) + m];
-                Cny[fy(i, 0) + m] = C[3 * c.hidx(i, 0, k) + m];
+                Cpy[fy(i, jhi) + m] = 0.0;
+                Cny[fy(i, jlo - 1) + m] = 0.0;
             }
         }
     const double dt = c.ph.dt, wi = c.ph.wi, dX = c.dX, dY = c.dY;
     const double *U = c.U.data(), *V = c.V.data();
     long long iters = 0, unconv = 0;
-    std::vector<double> Cn(3 * NX * NY);
-    for (int j = 1; j <= NY; ++j)
+    std::vector<double> Cn(3 * NX * nr);
+    for (int j = jlo; j <= jhi; ++j)
         for (int i = 1; i <= NX; ++i) {
-            double u1 = U[c.hidx(i - 1, j, k)], u2 = U[c.hidx(i, j, k)];
-            double v1 = V[c.hidx(i, j - 1, k)], v2 = V[c.hidx(i, j, k)];
+            auto u = [&](int a, int bb) { return vval(c, U, a, bb, k); };
+            auto v = [&](int a, int bb) { return vval(c, V, a, bb, k); };
+            double u1 = u(i - 1, j), u2 = u(i, j);
+            double v1 = v(i, j - 1), v2 = v(i, j);
             double s1 = (-u2 + std::fabs(u2)) * dt / (2 * dX);
             double s2 = 1.0 / 4 + (-u2 - std::fabs(u2)) * dt / (2 * dX);
             double s3 = 1.0 / 4 + (u1 - std::fabs(u1)) * dt / (2 * dX);
@@ -643,8 +682,6 @@ void polymer2(OCtx &c) {
                        + s7 * Cpy[fy(i, j - 1) + m] + s5 * Cpy[fy(i, j) + m] + s8 * Cny[fy(i, j - 1) + m] + s6 * Cny[fy(i, j) + m];
             b[0] = b[0] + dt / wi;
             b[2] = b[2] + dt / wi;
-            auto u = [&](int a, int bb) { return U[c.hidx(a, bb, k)]; };
-            auto v = [&](int a, int bb) { return V[c.hidx(a, bb, k)]; };
             double A0[2][2];
             A0[0][0] = -dt * (-u(i - 1, j) + u(i, j)) / dX;
             A0[0][1] = -dt * (-v(i - 1, j - 1) + v(i + 1, j - 1) - v(i - 1, j) + v(i + 1, j)) / (4 * dX);
@@ -656,12 +693,13 @@ void polymer2(OCtx &c) {
             int itr = newton_cell2(AT, b, x, c.ph);
             iters += itr;
             if (itr > c.ph.newton_itrmax) unconv += 1;
-            for (int m = 0; m < 3; ++m) Cn[3 * ((i - 1) + NX * (j - 1)) + m] = x[m];
+            for (int m = 0; m < 3; ++m) Cn[3 * ((i - 1) + NX * (j - jlo)) + m] = x[m];
         }
-    for (int j = 1; j <= NY; ++j)
+    for (int j = jlo; j <= jhi; ++j)
         for (int i = 1; i <= NX; ++i)
-            for (int m = 0; m < 3; ++m) c.C[3 * c.hidx(i, j, k) + m] = Cn[3 * ((i - 1) + NX * (j - 1)) + m];
-    bc_c(c, c.C.data());
+            for (int m = 0; m < 3; ++m) c.C[3 * c.hidx(i, j, k) + m] = Cn[3 * ((i - 1) + NX * (j - jlo)) + m];
+    if (ext) bc_periodic_xz(c, c.C.data(), 3);
+    else bc_c(c, c.C.data());
     c.newton_iters += iters;
     c.newton_unconv += unconv;
 }
@@ -1397,6 +1435,8 @@ int do_step(OCtx &c, double *drag) {
     }
     c.mark(6);
     march(c);
+    // C_kabe at the end of the step (fft_march_kabe, fenep_2d.f90:1374)
+    if (c.walls && c.ph.beta != 1.0) bc_c(c, c.C.data());
     c.mark(7);
     c.step += 1;
     // NaN guard (fenep_2d.f90:1974)
@@ -1501,10 +1541,11 @@ int f8o_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *
                         &c->Bx, &c->By, &c->Bz, &c->Tx, &c->Ty, &c->Tz, &c->fint[0], &c->fint[1], &c->fint[2]})
             v->assign(ni, 0.0);
         if (c->dim == 3) {
-            c->Cx.assign(6 * ni, 0.0);
-            c->Cpx.assign((size_t)6 * (c->NX + 1) * c->NY * c->NZ, 0.0); c->Cnx = c->Cpx;
-            c->Cpy.assign((size_t)6 * c->NX * (c->NY + 1) * c->NZ, 0.0); c->Cny = c->Cpy;
-            c->Cpz.assign((size_t)6 * c->NX * c->NY * (c->NZ + 1), 0.0); c->Cnz = c->Cpz;
+            const size_t nr = (size_t)(prow_hi(*c) - prow_lo(*c) + 1);   // rows of the polymer update
+            c->Cx.assign((size_t)6 * c->NX * nr * c->NZ, 0.0);
+            c->Cpx.assign((size_t)6 * (c->NX + 1) * nr * c->NZ, 0.0); c->Cnx = c->Cpx;
+            c->Cpy.assign((size_t)6 * c->NX * (nr + 1) * c->NZ, 0.0); c->Cny = c->Cpy;
+            c->Cpz.assign((size_t)6 * c->NX * nr * (c->NZ + 1), 0.0); c->Cnz = c->Cpz;
         }
     } catch (...) { delete c; return F8_ERR_NOMEM; }
     make_tw(c->NX, c->twx_r, c->twx_i);

@@ -10,7 +10,10 @@ the reference's known-answer programs) to round-off.
 The step follows machapin/fortran8 as the oracle restates it:
 
 * halo fill: PBM (fenep.f90:147-166) and the wall rules of
-  fenep_2d.f90:1098-1143 (x, then y, then z);
+  fenep_2d.f90:1098-1143 (x, then y, then z); with walls the polymer update
+  also covers the ghost rows (zero C and velocity beyond them), which keep
+  their updated values through the stress and are extrapolated at the end of
+  the step, as the reference's wall mode does;
 * polymer: candidate faces and the Vieta eigen test (fenep.f90:169-242,
   425-444), Cstar (464-507), the Lyapunov Newton solve with its central
   difference Jacobian (518-643), stress divergence (645-691);
@@ -92,6 +95,13 @@ def bc(A: torch.Tensor, kind: str, g: TGrid) -> torch.Tensor:
         A = torch.cat([lo, mid, hi], dim=-2)
     A = torch.cat([A[..., NZ:NZ + 1, :, :], A[..., 1:NZ + 1, :, :], A[..., 1:2, :, :]], dim=-3)
     return A
+
+
+def bc_xz(A: torch.Tensor, g: TGrid) -> torch.Tensor:
+    """Periodic x and z halo copies only (every y row, ghost rows included)."""
+    NX, NZ = g.nx, g.nz
+    A = torch.cat([A[..., NX:NX + 1], A[..., 1:NX + 1], A[..., 1:2]], dim=-1)
+    return torch.cat([A[..., NZ:NZ + 1, :, :], A[..., 1:NZ + 1, :, :], A[..., 1:2, :, :]], dim=-3)
 
 
 def sh(A: torch.Tensor, g: TGrid, di=0, dj=0, dk=0) -> torch.Tensor:
@@ -209,7 +219,15 @@ def _num(x) -> float:
 
 
 def polymer(C, U, V, W, g: TGrid, dt, wi, lp2, dc, eps, itrmax):
-    """C^{n+1} (interior, list of 6) from C^n (halo, (6, ...)) and the velocity."""
+    """C^{n+1} of the updated cells (list of 6) from C^n (halo, (6, ...)) and the
+    velocity.  Periodic: the interior cells.  With walls also the ghost rows
+    (rows 0..NY+1, shape (NZ, NY+2, NX)): the reference's wall mode updates C on
+    every row of its box, the rows beyond the walls holding zero C and velocity
+    (fenep_2d.f90:138-348, 1097-1143, 1912-1929)."""
+    if g.walls:
+        pad = lambda A: torch.nn.functional.pad(A, (0, 0, 1, 1, 0, 0))
+        C, U, V, W = pad(C), pad(U), pad(V), pad(W)
+        g = TGrid(g.nx, g.ny + 2, g.nz, g.dx, g.dy, g.dz, True, g.uwall)
     dX, dY, dZ = g.dx, g.dy, g.dz
     c0 = [sh(C[m], g) for m in range(6)]
     faces = []
@@ -232,9 +250,11 @@ def polymer(C, U, V, W, g: TGrid, dt, wi, lp2, dc, eps, itrmax):
         pyp = [torch.roll(f, -1, -2) for f in fpy]
         nym = [torch.roll(f, 1, -2) for f in fny]
     else:
-        NX, NY, NZ = g.nx, g.ny, g.nz
-        pyp = [torch.cat([fpy[m][:, 1:, :], C[m][1:NZ + 1, NY + 1:NY + 2, 1:NX + 1]], dim=-2) for m in range(6)]
-        nym = [torch.cat([C[m][1:NZ + 1, 0:1, 1:NX + 1], fny[m][:, :-1, :]], dim=-2) for m in range(6)]
+        # faces of the cells beyond the ghost rows: multiplied by exactly zero
+        # (the wall-normal velocity vanishes there)
+        zrow = torch.zeros_like(fpy[0][:, :1, :])
+        pyp = [torch.cat([fpy[m][:, 1:, :], zrow], dim=-2) for m in range(6)]
+        nym = [torch.cat([zrow, fny[m][:, :-1, :]], dim=-2) for m in range(6)]
     u1, u2 = sh(U, g, -1), sh(U, g)
     v1, v2 = sh(V, g, 0, -1), sh(V, g)
     w1, w2 = sh(W, g, 0, 0, -1), sh(W, g)
@@ -571,8 +591,13 @@ def step(st: dict, prm: dict, g: TGrid, ph: TPhys, geom, first: bool):
         T = [torch.zeros_like(sh(U, g)) for _ in range(3)]
         iters = None
     else:
-        Cn_int, iters = polymer(C, U, V, W, g, dt, wi, lp2, ph.newton_dc, ph.newton_eps, ph.newton_itrmax)
-        Cn = bc(torch.stack([embed(c, g) for c in Cn_int], 0), "c", g)
+        Cn_cells, iters = polymer(C, U, V, W, g, dt, wi, lp2, ph.newton_dc, ph.newton_eps, ph.newton_itrmax)
+        if g.walls:
+            # updated ghost rows kept through the stress (C_PBM in x, z only);
+            # extrapolated at the end of the step (fenep_2d.f90:1371-1374)
+            Cn = bc_xz(torch.stack([torch.nn.functional.pad(c, (1, 1, 0, 0, 1, 1)) for c in Cn_cells], 0), g)
+        else:
+            Cn = bc(torch.stack([embed(c, g) for c in Cn_cells], 0), "c", g)
         T = stress(Cn, g, lp2, (1.0 - beta) / (re * wi))
     A, B = conv_visc(U, V, W, g, beta / re)
     A0 = A if first else st["A0"]
@@ -618,7 +643,7 @@ def step(st: dict, prm: dict, g: TGrid, ph: TPhys, geom, first: bool):
            + (sh(Phi, g, 0, 0, -1) - 2 * ph0 + sh(Phi, g, 0, 0, 1)) / (dZ * dZ))
     Pn = sh(P, g) + ph0 - kap * lap
     new = {"U": bc(embed(Un, g), "u", g), "V": bc(embed(Vn, g), "v", g), "W": bc(embed(Wn, g), "w", g),
-           "P": bc(embed(Pn, g), "p", g), "C": Cn, "A0": A, "T0": T, "F": st["F"],
+           "P": bc(embed(Pn, g), "p", g), "C": bc(Cn, "c", g) if g.walls else Cn, "A0": A, "T0": T, "F": st["F"],
            "Phi": Phi}
     return new, drag, iters
 
