@@ -292,6 +292,7 @@ int setup(f8_ctx *c) {
         API_CUDA(c, c->alloc(p, cs));
     API_CUDA(c, c->alloc(&c->scratch_aos, cs * d.ncomp));
     API_CUDA(c, c->alloc(&d.codes, ni));
+    API_CUDA(c, c->alloc(&d.codes_g, 2 * (size_t)g.nx * g.nz));
     const size_t nxh = g.nx / 2 + 1;
     const size_t nspec = 2 * nxh * (size_t)(g.ny + 2) * g.nz;
     if (!mixed) {

@@ -32,6 +32,18 @@ __host__ __device__ inline int wrapx(const Geo &g, int i) { return i < 1 ? i + g
 __host__ __device__ inline int wrapy(const Geo &g, int j) { return j < 1 ? j + g.ny : (j > g.ny ? j - g.ny : j); }
 __host__ __device__ inline int wrapz(const Geo &g, int k) { return k < 1 ? k + g.nz : (k > g.nz ? k - g.nz : k); }
 
+// Rows of the polymer update.  Periodic in y: 1..NY.  With y walls also the
+// ghost rows 0 and NY+1: the reference's wall mode updates C on every row of
+// its box, the rows beyond the walls holding zero C and velocity, keeps the
+// updated ghost rows through the stress and extrapolates them only at the end
+// of the step (fenep_2d.f90:1097-1143, 1371-1374, 1912-1966).
+__host__ __device__ inline int prow0(const Geo &g) { return g.walls ? 0 : 1; }
+__host__ __device__ inline int prows(const Geo &g) { return g.walls ? g.ny + 2 : g.ny; }
+// selection codes of the ghost rows (walls): [k][side][i], side 0: j = 0, 1: j = NY+1
+__host__ __device__ inline int gcix(const Geo &g, int i, int j, int k) {
+    return (i - 1) + g.nx * ((j == 0 ? 0 : 1) + 2 * (k - 1));
+}
+
 // Physical parameters the kernels need (copied from f8_phys).
 struct Phys {
     double re, wi, beta, lp2, dt;

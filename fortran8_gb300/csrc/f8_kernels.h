@@ -18,6 +18,7 @@ struct Dev {
     double *C, *Cn;      // ncomp SoA halo fields each
     double *fpet;        // Peterlin factor f(C) on every halo cell
     uint8_t *codes;      // interior: 2 bits per direction, chosen candidate - 1
+    uint8_t *codes_g;    // the same for the ghost rows of a wall channel (gcix)
     double *Ax0, *Ay0, *Az0, *Tx0, *Ty0, *Tz0, *Fx, *Fy, *Fz;
     // work
     double *Up, *Vp, *Wp, *Ua, *Va, *Wa;   // halo

@@ -109,6 +109,25 @@ __global__ void k_bc_c_pet(double *C, double *fpet, Geo g, int ncomp, int cs, do
     fpet[h] = peterlin(x, ncomp, lp2);
 }
 
+// After the polymer update of a wall channel: the x and z halo cells of every
+// row (ghost rows included) as periodic copies and their Peterlin factor; the
+// ghost rows keep their updated values (C_PBM after Lyapunov,
+// fenep_2d.f90:348; the wall extrapolation comes at the end of the step).
+__global__ void k_bc_c_pet_xz(double *C, double *fpet, Geo g, int ncomp, int cs, double lp2) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (!halo_cell(g, t, i, j, k)) return;
+    if ((j == 0 || j == g.sy - 1) && i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) return;   // updated ghost cell
+    const int src = hix(g, wrapx(g, i), j, wrapz(g, k));
+    const int h = hix(g, i, j, k);
+    double x[6];
+    for (int m = 0; m < ncomp; ++m) {
+        x[m] = C[(size_t)m * cs + src];
+        C[(size_t)m * cs + h] = x[m];
+    }
+    fpet[h] = peterlin(x, ncomp, lp2);
+}
+
 // f on every cell (after a load, or when the polymer stage is skipped)
 __global__ void k_pet_all(const double *C, double *fpet, int ncomp, int cs, double lp2) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -184,11 +203,23 @@ __device__ inline int select3(const double *cm, const double *c0, const double *
     return maxloc4(minlist);
 }
 
-__global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+// C of component array Cm at row jj of column (i, k): zero beyond the ghost
+// rows of a wall channel (the wall mode's outside rows)
+__device__ inline double crow(const double *Cm, const Geo &g, int i, int jj, int k) {
+    return (jj < 0 || jj > g.ny + 1) ? 0.0 : Cm[hix(g, i, jj, k)];
+}
+
+// code of cell (i, j, k), interior or ghost row
+__device__ inline int code_at(const uint8_t *codes, const uint8_t *codes_g, const Geo &g, int i, int j, int k) {
+    return (j >= 1 && j <= g.ny) ? codes[qix(g, i, j, k)] : codes_g[gcix(g, i, j, k)];
+}
+
+__global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict__ C, uint8_t *__restrict__ codes,
+                                                        uint8_t *__restrict__ codes_g, Geo g, int cs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
-    if (i > g.nx || j > g.ny) return;
+    if (i > g.nx || j >= prow0(g) + prows(g)) return;
     double c0[6], cm[6], cp[6];
     const int h = hix(g, i, j, k);
     for (int m = 0; m < 6; ++m) c0[m] = C[(size_t)m * cs + h];
@@ -196,12 +227,18 @@ __global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict
     int code = 0;
     for (int d = 0; d < 3; ++d) {
         for (int m = 0; m < 6; ++m) {
-            cm[m] = C[(size_t)m * cs + h - off[d]];
-            cp[m] = C[(size_t)m * cs + h + off[d]];
+            if (d == 1 && g.walls) {
+                cm[m] = crow(C + (size_t)m * cs, g, i, j - 1, k);
+                cp[m] = crow(C + (size_t)m * cs, g, i, j + 1, k);
+            } else {
+                cm[m] = C[(size_t)m * cs + h - off[d]];
+                cp[m] = C[(size_t)m * cs + h + off[d]];
+            }
         }
         code |= (select3(cm, c0, cp) - 1) << (2 * d);
     }
-    codes[qix(g, i, j, k)] = (uint8_t)code;
+    if (j >= 1 && j <= g.ny) codes[qix(g, i, j, k)] = (uint8_t)code;
+    else codes_g[gcix(g, i, j, k)] = (uint8_t)code;
 }
 
 // fenep.f90:588-605
@@ -256,40 +293,41 @@ __device__ inline void gauss(double (&Ah)[N][N + 1], double *x) {
 // rebuilt from their selection codes, so no face arrays are stored.
 __global__ void __launch_bounds__(128) k_polymer_update3(const double *__restrict__ C, double *__restrict__ Cn,
                                                          double *__restrict__ fpet, const uint8_t *__restrict__ codes,
+                                                         const uint8_t *__restrict__ codes_g,
                                                          const double *__restrict__ U, const double *__restrict__ V,
                                                          const double *__restrict__ W, Geo g, Phys ph, int cs,
                                                          StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
-    const bool active = i <= g.nx && j <= g.ny;
+    const bool active = i <= g.nx && j < prow0(g) + prows(g);
     unsigned long long my_itr = 0, my_unconv = 0;
     if (active) {
         const int h = hix(g, i, j, k);
         const double dt = ph.dt, dX = g.dx, dY = g.dy, dZ = g.dz;
-        // selection codes of the cell and its neighbours; wall ghost rows use
-        // the cell value (their faces are multiplied by zero in Cstar)
-        const int cself = codes[qix(g, i, j, k)];
-        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
-        const int czm = (codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3, czp = (codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
+        // selection codes of the cell and its neighbours (with walls the rows
+        // beyond the ghost rows are outside: their faces are multiplied by
+        // exactly zero in Cstar, the code there is the cell value's)
+        const int cself = code_at(codes, codes_g, g, i, j, k);
+        const int cxm = code_at(codes, codes_g, g, wrapx(g, i - 1), j, k) & 3;
+        const int cxp = code_at(codes, codes_g, g, wrapx(g, i + 1), j, k) & 3;
+        const int czm = (code_at(codes, codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
+        const int czp = (code_at(codes, codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
         int cym, cyp;
         int jm = j - 1, jp = j + 1;
-        bool ym_ghost = false, yp_ghost = false;
         if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
-        cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
-        cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+        cym = (jm < 0) ? 3 : (code_at(codes, codes_g, g, i, jm, k) >> 2) & 3;
+        cyp = (jp > g.ny + 1) ? 3 : (code_at(codes, codes_g, g, i, jp, k) >> 2) & 3;
         const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
         // centres of the neighbour cells along each direction (wrapped)
         const int xm = wrapx(g, i - 1), xp = wrapx(g, i + 1);
         const int zm = wrapz(g, k - 1), zp = wrapz(g, k + 1);
         const int hxm = hix(g, xm, j, k), hxp = hix(g, xp, j, k);
-        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
         const int hzm = hix(g, i, j, zm), hzp = hix(g, i, j, zp);
-        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+        const int ox = 1, oz = g.sx * g.sy;
 
         double u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
-        double v1 = V[hix(g, i, j - 1, k)], v2 = V[h];
+        double v1 = crow(V, g, i, j - 1, k), v2 = V[h];
         double w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
         double s1 = (-u2 + fabs(u2)) * dt / (2 * dX);
         double s2 = 1.0 / 6 + (-u2 - fabs(u2)) * dt / (2 * dX);
@@ -314,10 +352,21 @@ __global__ void __launch_bounds__(128) k_polymer_update3(const double *__restric
             double pxp = face_p(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
             double nxm = face_n(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
             // y
-            double pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
-            double nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
-            double pyp = yp_ghost ? Cm[hyp] : face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-            double nym = ym_ghost ? Cm[hym] : face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            double pym, nyp, pyp, nym;
+            if (!g.walls) {   // jm, jp wrapped; rows read around them through the halo
+                const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k), oy = g.sx;
+                pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
+                nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
+                pyp = face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+                nym = face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            } else {          // zero beyond the ghost rows
+                const double ym2 = crow(Cm, g, i, j - 2, k), ym1 = crow(Cm, g, i, j - 1, k);
+                const double yp1 = crow(Cm, g, i, j + 1, k), yp2 = crow(Cm, g, i, j + 2, k);
+                pym = face_p(isy, ym1, c0, yp1);
+                nyp = face_n(isy, ym1, c0, yp1);
+                pyp = face_p(cyp + 1, c0, yp1, yp2);   // the p face of cell j+1
+                nym = face_n(cym + 1, ym2, ym1, c0);   // the n face of cell j-1
+            }
             // z
             double pzm = face_p(isz, Cm[h - oz], c0, Cm[h + oz]);
             double nzp = face_n(isz, Cm[h - oz], c0, Cm[h + oz]);
@@ -331,9 +380,9 @@ __global__ void __launch_bounds__(128) k_polymer_update3(const double *__restric
         b[0] = b[0] + dt / wi;
         b[3] = b[3] + dt / wi;
         b[5] = b[5] + dt / wi;
-        auto u = [&](int a, int bb, int cc) { return U[hix(g, a, bb, cc)]; };
-        auto v = [&](int a, int bb, int cc) { return V[hix(g, a, bb, cc)]; };
-        auto w = [&](int a, int bb, int cc) { return W[hix(g, a, bb, cc)]; };
+        auto u = [&](int a, int bb, int cc) { return crow(U, g, a, bb, cc); };
+        auto v = [&](int a, int bb, int cc) { return crow(V, g, a, bb, cc); };
+        auto w = [&](int a, int bb, int cc) { return crow(W, g, a, bb, cc); };
         double A0[3][3];
         A0[0][0] = -dt * (-u(i - 1, j, k) + u(i, j, k)) / dX;
         A0[0][1] = -dt * (-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) / (4 * dX);
@@ -419,10 +468,11 @@ __device__ inline int select2(const double *cm, const double *c0, const double *
     return index;
 }
 
-__global__ void k_polymer_codes2(const double *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs) {
+__global__ void k_polymer_codes2(const double *__restrict__ C, uint8_t *__restrict__ codes,
+                                 uint8_t *__restrict__ codes_g, Geo g, int cs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > g.nx || j > g.ny) return;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
+    if (i > g.nx || j >= prow0(g) + prows(g)) return;
     const int k = 1;
     double c0[3], cm[3], cp[3];
     const int h = hix(g, i, j, k);
@@ -431,13 +481,19 @@ __global__ void k_polymer_codes2(const double *__restrict__ C, uint8_t *__restri
     int code = 0;
     for (int d = 0; d < 2; ++d) {
         for (int m = 0; m < 3; ++m) {
-            cm[m] = C[(size_t)m * cs + h - off[d]];
-            cp[m] = C[(size_t)m * cs + h + off[d]];
+            if (d == 1 && g.walls) {
+                cm[m] = crow(C + (size_t)m * cs, g, i, j - 1, k);
+                cp[m] = crow(C + (size_t)m * cs, g, i, j + 1, k);
+            } else {
+                cm[m] = C[(size_t)m * cs + h - off[d]];
+                cp[m] = C[(size_t)m * cs + h + off[d]];
+            }
         }
         int idx = select2(cm, c0, cp);   // 0..3; 0 -> cell value (stored as 3 = "4")
         code |= (idx == 0 ? 3 : idx - 1) << (2 * d);
     }
-    codes[qix(g, i, j, k)] = (uint8_t)code;
+    if (j >= 1 && j <= g.ny) codes[qix(g, i, j, k)] = (uint8_t)code;
+    else codes_g[gcix(g, i, j, k)] = (uint8_t)code;
 }
 
 __device__ inline void lyap_func2(const double A0[2][2], const double *b, const double *x, double *l, double lp2,
@@ -453,30 +509,29 @@ __device__ inline void lyap_func2(const double A0[2][2], const double *b, const 
 }
 
 __global__ void k_polymer_update2(const double *__restrict__ C, double *__restrict__ Cn, double *__restrict__ fpet,
-                                  const uint8_t *__restrict__ codes, const double *__restrict__ U,
-                                  const double *__restrict__ V, Geo g, Phys ph, int cs, StepCounters *cnt) {
+                                  const uint8_t *__restrict__ codes, const uint8_t *__restrict__ codes_g,
+                                  const double *__restrict__ U, const double *__restrict__ V, Geo g, Phys ph, int cs,
+                                  StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = 1;
-    const bool active = i <= g.nx && j <= g.ny;
+    const bool active = i <= g.nx && j < prow0(g) + prows(g);
     unsigned long long my_itr = 0, my_unconv = 0;
     if (active) {
         const int h = hix(g, i, j, k);
         const double dt = ph.dt, dX = g.dx, dY = g.dy;
-        const int cself = codes[qix(g, i, j, k)];
-        const int cxm = codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
+        const int cself = code_at(codes, codes_g, g, i, j, k);
+        const int cxm = code_at(codes, codes_g, g, wrapx(g, i - 1), j, k) & 3;
+        const int cxp = code_at(codes, codes_g, g, wrapx(g, i + 1), j, k) & 3;
         int jm = j - 1, jp = j + 1;
-        bool ym_ghost = false, yp_ghost = false;
         if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-        else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
-        const int cym = ym_ghost ? 3 : (codes[qix(g, i, jm, k)] >> 2) & 3;
-        const int cyp = yp_ghost ? 3 : (codes[qix(g, i, jp, k)] >> 2) & 3;
+        const int cym = (jm < 0) ? 3 : (code_at(codes, codes_g, g, i, jm, k) >> 2) & 3;
+        const int cyp = (jp > g.ny + 1) ? 3 : (code_at(codes, codes_g, g, i, jp, k) >> 2) & 3;
         const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1;
         const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
-        const int ox = 1, oy = g.sx;
+        const int ox = 1;
         double u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
-        double v1 = V[hix(g, i, j - 1, k)], v2 = V[h];
+        double v1 = crow(V, g, i, j - 1, k), v2 = V[h];
         double s1 = (-u2 + fabs(u2)) * dt / (2 * dX);
         double s2 = 1.0 / 4 + (-u2 - fabs(u2)) * dt / (2 * dX);
         double s3 = 1.0 / 4 + (u1 - fabs(u1)) * dt / (2 * dX);
@@ -493,18 +548,29 @@ __global__ void k_polymer_update2(const double *__restrict__ C, double *__restri
             double nxp = face_n(isx, Cm[h - ox], c0, Cm[h + ox]);
             double pxp = face_p(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
             double nxm = face_n(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
-            double pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
-            double nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
-            double pyp = yp_ghost ? Cm[hyp] : face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-            double nym = ym_ghost ? Cm[hym] : face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            double pym, nyp, pyp, nym;
+            if (!g.walls) {   // jm, jp wrapped; rows read around them through the halo
+                const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k), oy = g.sx;
+                pym = face_p(isy, Cm[h - oy], c0, Cm[h + oy]);
+                nyp = face_n(isy, Cm[h - oy], c0, Cm[h + oy]);
+                pyp = face_p(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+                nym = face_n(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            } else {          // zero beyond the ghost rows
+                const double ym2 = crow(Cm, g, i, j - 2, k), ym1 = crow(Cm, g, i, j - 1, k);
+                const double yp1 = crow(Cm, g, i, j + 1, k), yp2 = crow(Cm, g, i, j + 2, k);
+                pym = face_p(isy, ym1, c0, yp1);
+                nyp = face_n(isy, ym1, c0, yp1);
+                pyp = face_p(cyp + 1, c0, yp1, yp2);
+                nym = face_n(cym + 1, ym2, ym1, c0);
+            }
             b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp;
             x[m] = c0;
         }
         const double wi = ph.wi;
         b[0] = b[0] + dt / wi;
         b[2] = b[2] + dt / wi;
-        auto u = [&](int a, int bb) { return U[hix(g, a, bb, k)]; };
-        auto v = [&](int a, int bb) { return V[hix(g, a, bb, k)]; };
+        auto u = [&](int a, int bb) { return crow(U, g, a, bb, k); };
+        auto v = [&](int a, int bb) { return crow(V, g, a, bb, k); };
         double A0[2][2];
         A0[0][0] = -dt * (-u(i - 1, j) + u(i, j)) / dX;
         A0[0][1] = -dt * (-v(i - 1, j - 1) + v(i + 1, j - 1) - v(i - 1, j) + v(i + 1, j)) / (4 * dX);
@@ -1229,15 +1295,17 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     // 1. polymer
     if (o.polymer) {
         dim3 blk(32, 4);
-        dim3 grd = cell_grid(g, blk);
-        if (d3) { k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs); count_launch(); }
-        else { k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, g, d.cs); count_launch(); }
+        // the rows of the polymer update (with walls the ghost rows too)
+        dim3 grd((g.nx + blk.x - 1) / blk.x, (prows(g) + blk.y - 1) / blk.y, g.nz);
+        if (d3) { k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, d.codes_g, g, d.cs); count_launch(); }
+        else { k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, d.codes_g, g, d.cs); count_launch(); }
         mark(1);
-        if (d3) { k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt); count_launch(); }
-        else { k_polymer_update2<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.U, d.V, g, d.ph, d.cs, d.cnt); count_launch(); }
+        if (d3) { k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.codes_g, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt); count_launch(); }
+        else { k_polymer_update2<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.codes_g, d.U, d.V, g, d.ph, d.cs, d.cnt); count_launch(); }
         std::swap(d.C, d.Cn);
         long n = halo_count(g);
-        k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2); count_launch();
+        if (g.walls) { k_bc_c_pet_xz<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2); count_launch(); }
+        else { k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2); count_launch(); }
         if ((e = cudaGetLastError())) return e;
     } else {
         mark(1);
@@ -1328,6 +1396,12 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     if ((e = bc(d.V, g, BC_V, s))) return e;
     if (d3 && (e = bc(d.W, g, BC_W, s))) return e;
     if ((e = bc(d.P, g, BC_P, s))) return e;
+    if (o.polymer && g.walls) {
+        // the wall extrapolation of the ghost rows (C_kabe at the end of the
+        // step, fenep_2d.f90:1374)
+        long n = halo_count(g);
+        k_bc_c_pet<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.C, d.fpet, g, d.ncomp, d.cs, d.ph.lp2); count_launch();
+    }
     mark(7);
     return cudaGetLastError();
 }
