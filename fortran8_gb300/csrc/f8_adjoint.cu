@@ -115,10 +115,13 @@ __global__ void k_fold_y(FoldSet f, Geo g) {
     }
 }
 
-__global__ void k_fold_x(FoldSet f, Geo g) {
+// rows: 1..NY, or every row 0..NY+1 (rows_all) for the periodic x/z fill of
+// the updated wall ghost rows
+__global__ void k_fold_x(FoldSet f, Geo g, int rows_all) {
+    const int ny = rows_all ? g.sy : g.ny, j0 = rows_all ? 0 : 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.ny * g.nz) return;
-    const int j = 1 + t % g.ny, k = 1 + t / g.ny;
+    if (t >= ny * g.nz) return;
+    const int j = j0 + t % ny, k = 1 + t / ny;
     const int lo = hix(g, 0, j, k), hi = hix(g, g.sx - 1, j, k);
     for (int q = 0; q < f.n; ++q) {
         double *A = f.A[q];
@@ -133,7 +136,15 @@ __global__ void k_fold_x(FoldSet f, Geo g) {
 cudaError_t fold(const FoldSet &f, const Geo &g, cudaStream_t s) {
     k_fold_z<<<(g.sx * g.sy + 255) / 256, 256, 0, s>>>(f, g); count_launch();
     k_fold_y<<<(g.sx * g.nz + 255) / 256, 256, 0, s>>>(f, g); count_launch();
-    k_fold_x<<<(g.ny * g.nz + 255) / 256, 256, 0, s>>>(f, g); count_launch();
+    k_fold_x<<<(g.ny * g.nz + 255) / 256, 256, 0, s>>>(f, g, 0); count_launch();
+    return cudaGetLastError();
+}
+
+// transpose of the periodic x and z copies of every row (k_bc_c_pet_xz): the
+// wall ghost rows stay (they are updated cells)
+cudaError_t fold_xz(const FoldSet &f, const Geo &g, cudaStream_t s) {
+    k_fold_z<<<(g.sx * g.sy + 255) / 256, 256, 0, s>>>(f, g); count_launch();
+    k_fold_x<<<(g.sy * g.nz + 255) / 256, 256, 0, s>>>(f, g, 1); count_launch();
     return cudaGetLastError();
 }
 
@@ -613,8 +624,8 @@ __device__ inline void wface_n(int idx, double &wm, double &w0, double &wp) {
 }
 
 struct PolyAdjArgs {
-    const double *C, *Cn;             // C^n, C^{n+1} (halo, 6 SoA fields)
-    const uint8_t *codes;
+    const double *C, *Cn;             // C^n (the state) and C after the update (halo, 6 SoA fields)
+    const uint8_t *codes, *codes_g;
     const double *U, *V, *W;          // U^n (halo)
     const double *lX;                 // adjoint of C^{n+1} (interior)
     double *lC;                       // out: adjoint of C^n (full halo box, scattered)
@@ -624,11 +635,23 @@ struct PolyAdjArgs {
     double *grad;
 };
 
+// value of a halo field at row jj of column (i, k); zero beyond the ghost rows
+// of a wall channel (the reference wall mode's outside rows)
+__device__ inline double rowv(const double *A, const Geo &g, int i, int jj, int k) {
+    return (jj < 0 || jj > g.ny + 1) ? 0.0 : A[hix(g, i, jj, k)];
+}
+
+__device__ inline int code_of(const uint8_t *codes, const uint8_t *codes_g, const Geo &g, int i, int j, int k) {
+    return (j >= 1 && j <= g.ny) ? codes[qix(g, i, j, k)] : codes_g[gcix(g, i, j, k)];
+}
+
+// Rows: the cells of the polymer update (with walls also the ghost rows,
+// whose faces towards the outside rows carry zero C)
 __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
-    const bool active = i <= g.nx && j <= g.ny;
+    const bool active = i <= g.nx && j < prow0(g) + prows(g);
     double gwi = 0.0, gl2 = 0.0;
     if (active) {
         const size_t cs = (size_t)a.cs;
@@ -644,9 +667,9 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
         }
         if (any) {
             const double *U = a.U, *V = a.V, *W = a.W;
-            auto u = [&](int p, int q, int r) { return U[hix(g, p, q, r)]; };
-            auto v = [&](int p, int q, int r) { return V[hix(g, p, q, r)]; };
-            auto w = [&](int p, int q, int r) { return W[hix(g, p, q, r)]; };
+            auto u = [&](int p, int q, int r) { return rowv(U, g, p, q, r); };
+            auto v = [&](int p, int q, int r) { return rowv(V, g, p, q, r); };
+            auto w = [&](int p, int q, int r) { return rowv(W, g, p, q, r); };
             double A0[3][3];
             A0[0][0] = -dt * (-u(i - 1, j, k) + u(i, j, k)) / dX;
             A0[0][1] = -dt * (-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) / (4 * dX);
@@ -744,9 +767,11 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             lAt[2][0] = -(mu[2] * x[0] + mu[4] * x[1] + 2 * mu[5] * x[2]);
             lAt[2][1] = -(mu[2] * x[1] + mu[4] * x[3] + 2 * mu[5] * x[4]);
             lAt[2][2] = -(mu[2] * x[2] + mu[4] * x[4] + 2 * mu[5] * x[5]);
-            auto addu = [&](int p, int q, int r, double val) { atomicAdd(&a.lU[hix(g, p, q, r)], val); };
-            auto addv = [&](int p, int q, int r, double val) { atomicAdd(&a.lV[hix(g, p, q, r)], val); };
-            auto addw = [&](int p, int q, int r, double val) { atomicAdd(&a.lW[hix(g, p, q, r)], val); };
+            // scatters to rows beyond the ghost rows are dropped (constant zeros)
+            auto inrow = [&](int q) { return q >= 0 && q <= g.ny + 1; };
+            auto addu = [&](int p, int q, int r, double val) { if (inrow(q)) atomicAdd(&a.lU[hix(g, p, q, r)], val); };
+            auto addv = [&](int p, int q, int r, double val) { if (inrow(q)) atomicAdd(&a.lV[hix(g, p, q, r)], val); };
+            auto addw = [&](int p, int q, int r, double val) { if (inrow(q)) atomicAdd(&a.lW[hix(g, p, q, r)], val); };
             {
                 double l = lAt[0][0] * dt / dX;   // A0[0][0]
                 addu(i - 1, j, k, l); addu(i, j, k, -l);
@@ -769,7 +794,7 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
             }
             // Cstar: b = s3 pxm + s1 pxp + s4 nxm + s2 nxp + (y: s7 s5 s8 s6) + (z: s11 s9 s12 s10)
             const double u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
-            const double v1 = V[hix(g, i, j - 1, k)], v2 = V[h];
+            const double v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
             const double w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
             double s[13];
             s[1] = (-u2 + fabs(u2)) * dt / (2 * dX);
@@ -788,19 +813,18 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
 #pragma unroll
             for (int q = 0; q < 13; ++q) ls[q] = 0.0;
             // selection codes (as the forward kernel reads them)
-            const int cself = a.codes[qix(g, i, j, k)];
-            const int cxm = a.codes[qix(g, wrapx(g, i - 1), j, k)] & 3, cxp = a.codes[qix(g, wrapx(g, i + 1), j, k)] & 3;
-            const int czm = (a.codes[qix(g, i, j, wrapz(g, k - 1))] >> 4) & 3;
-            const int czp = (a.codes[qix(g, i, j, wrapz(g, k + 1))] >> 4) & 3;
+            const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
+            const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
+            const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
+            const int czm = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
+            const int czp = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
             int jm = j - 1, jp = j + 1;
-            bool ym_ghost = false, yp_ghost = false;
             if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-            else { ym_ghost = jm == 0; yp_ghost = jp == g.ny + 1; }
-            const int cym = ym_ghost ? 3 : (a.codes[qix(g, i, jm, k)] >> 2) & 3;
-            const int cyp = yp_ghost ? 3 : (a.codes[qix(g, i, jp, k)] >> 2) & 3;
+            const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
+            const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
             const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
             const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-            const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+            const int hym = g.walls ? h : hix(g, i, jm, k), hyp = g.walls ? h : hix(g, i, jp, k);
             const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
             const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
             // face weights of the cell's own faces and of the neighbours' faces,
@@ -858,8 +882,33 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs a, Geo g) {
                 };
                 // x: pxm (s3, own p), nxp (s2, own n), pxp (s1, neighbour i+1), nxm (s4, neighbour i-1)
                 dir(wpx, wnx, ox, hxp, qx, hxm, rx, s[3], s[2], s[1], s[4], false, false, ls[3], ls[2], ls[1], ls[4]);
-                dir(wpy, wny, oy, hyp, qy, hym, ry, s[7], s[6], s[5], s[8], yp_ghost, ym_ghost, ls[7], ls[6], ls[5],
-                    ls[8]);
+                if (!g.walls) {
+                    dir(wpy, wny, oy, hyp, qy, hym, ry, s[7], s[6], s[5], s[8], false, false, ls[7], ls[6], ls[5],
+                        ls[8]);
+                } else {
+                    // rows j-2 .. j+2 of the column, zero beyond the ghost rows
+                    auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
+                    auto yadd = [&](int jj, double val) {
+                        if (val != 0.0 && jj >= 0 && jj <= g.ny + 1) atomicAdd(&Lm[hix(g, i, jj, k)], val);
+                    };
+                    const double cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
+                    ls[7] += mum * (wpy.m * cmv + wpy.c * c0v + wpy.p * cpv);
+                    ls[6] += mum * (wny.m * cmv + wny.c * c0v + wny.p * cpv);
+                    yadd(j - 1, mum * (s[7] * wpy.m + s[6] * wny.m));
+                    yadd(j + 1, mum * (s[7] * wpy.p + s[6] * wny.p));
+                    lc0 += mum * (s[7] * wpy.c + s[6] * wny.c);
+                    // the p face of cell j+1 (rows j .. j+2), the n face of cell j-1 (rows j-2 .. j)
+                    ls[5] += mum * (qy.m * c0v + qy.c * cpv + qy.p * yv(j + 2));
+                    const double bq = mum * s[5];
+                    lc0 += bq * qy.m;
+                    yadd(j + 1, bq * qy.c);
+                    yadd(j + 2, bq * qy.p);
+                    ls[8] += mum * (ry.m * yv(j - 2) + ry.c * cmv + ry.p * c0v);
+                    const double br = mum * s[8];
+                    yadd(j - 2, br * ry.m);
+                    yadd(j - 1, br * ry.c);
+                    lc0 += br * ry.p;
+                }
                 dir(wpz, wnz, oz, hzp, qz, hzm, rz, s[11], s[10], s[9], s[12], false, false, ls[11], ls[10], ls[9],
                     ls[12]);
                 atomicAdd(&Lm[h], lc0);
@@ -966,14 +1015,18 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
     // 1. polymer
     if (polymer) {
         k_c0_adj<<<nb, 256, 0, s>>>(t.Cn, A.lC0, A.lC, cs, d.ph.lp2, 1.0 / (1.0 - beta), 1.0 / wi, A.grad); count_launch();
-        F8_CUDA_RET(fold(fold_c(A.lC, cs), g, s));
+        // with walls the stress read the updated ghost rows and their x/z
+        // copies; the state's C (wall-extrapolated) adjoint is interior already
+        if (g.walls) F8_CUDA_RET(fold_xz(fold_c(A.lC, cs), g, s));
+        else F8_CUDA_RET(fold(fold_c(A.lC, cs), g, s));
         F8_CUDA_RET(cudaMemsetAsync(A.lC2, 0, 6 * hb, s));
         PolyAdjArgs pa{};
-        pa.C = t.C; pa.Cn = t.Cn; pa.codes = t.codes; pa.U = t.U; pa.V = t.V; pa.W = t.W;
+        pa.C = t.C; pa.Cn = t.Cn; pa.codes = t.codes; pa.codes_g = t.codes_g; pa.U = t.U; pa.V = t.V; pa.W = t.W;
         pa.lX = A.lC; pa.lC = A.lC2; pa.lU = A.lU; pa.lV = A.lV; pa.lW = A.lW;
         pa.cs = cs; pa.dt = dt; pa.wi = wi; pa.lp2 = d.ph.lp2; pa.grad = A.grad;
         dim3 pb(32, 4);
-        k_polymer_adj3<<<cells(g, pb), pb, 0, s>>>(pa, g); count_launch();
+        const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
+        k_polymer_adj3<<<pg, pb, 0, s>>>(pa, g); count_launch();
         std::swap(A.lC, A.lC2);
     } else {
         F8_CUDA_RET(cudaMemsetAsync(A.lC, 0, 6 * hb, s));

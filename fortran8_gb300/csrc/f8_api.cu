@@ -85,8 +85,8 @@ struct GradMem {
     int K = 0, nck = 0, nsteps = 0;
     size_t ck_slot = 0;                     // doubles per checkpoint
     double *tU = nullptr, *tV = nullptr, *tW = nullptr, *tC = nullptr;
-    double *tUa = nullptr, *tUp = nullptr, *tPhi = nullptr, *tFc = nullptr;
-    uint8_t *tcodes = nullptr;
+    double *tUa = nullptr, *tUp = nullptr, *tPhi = nullptr, *tFc = nullptr, *tCm = nullptr;
+    uint8_t *tcodes = nullptr, *tcodes_g = nullptr;
     double *ck = nullptr, *dw = nullptr;
     template <typename T>
     cudaError_t get(int grp, T **p, size_t n) {
@@ -835,7 +835,9 @@ int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
         API_CUDA(c, G.get(1, &G.tV, K * cs));
         API_CUDA(c, G.get(1, &G.tW, K * cs));
         API_CUDA(c, G.get(1, &G.tC, (K + 1) * 6 * cs));
+        API_CUDA(c, G.get(1, &G.tCm, K * 6 * cs));
         API_CUDA(c, G.get(1, &G.tcodes, K * ni));
+        API_CUDA(c, G.get(1, &G.tcodes_g, K * 2 * (size_t)d.g.nx * d.g.nz));
         API_CUDA(c, G.get(1, &G.tUa, 3 * K * cs));
         API_CUDA(c, G.get(1, &G.tUp, 3 * K * cs));
         API_CUDA(c, G.get(1, &G.tPhi, K * cs));
@@ -900,10 +902,13 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
         if (rec == 0) F8_CUDA_RET(cp(G.tC, d.C, 6 * hb));
     }
     int sor = -1;
+    if (rec >= 0) o.c_mid = G.tCm + (size_t)rec * 6 * cs;
     F8_CUDA_RET(step_fp64(d, o, ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr, &sor, c->s));
     if (rec >= 0) {
+        const size_t ng = 2 * (size_t)d.g.nx * d.g.nz;
         F8_CUDA_RET(cp(G.tC + (size_t)(rec + 1) * 6 * cs, d.C, 6 * hb));
         F8_CUDA_RET(cp(G.tcodes + rec * ni, d.codes, ni));
+        F8_CUDA_RET(cp(G.tcodes_g + rec * ng, d.codes_g, ng));
         const double *ua[3] = {d.Ua, d.Va, d.Wa}, *up[3] = {d.Up, d.Vp, d.Wp};
         for (int q = 0; q < 3; ++q) {
             F8_CUDA_RET(cp(G.tUa + (3 * rec + q) * cs, ua[q], hb));
@@ -920,8 +925,9 @@ TapeStep tape_step(f8_ctx *c, int rec) {
     const size_t cs = c->d.cs, ni = c->d.ni, nfc = (size_t)c->d.nm * c->d.g.nz;
     TapeStep t{};
     t.U = G.tU + rec * cs; t.V = G.tV + rec * cs; t.W = G.tW + rec * cs;
-    t.C = G.tC + (size_t)rec * 6 * cs; t.Cn = G.tC + (size_t)(rec + 1) * 6 * cs;
+    t.C = G.tC + (size_t)rec * 6 * cs; t.Cn = G.tCm + (size_t)rec * 6 * cs;
     t.codes = G.tcodes + rec * ni;
+    t.codes_g = G.tcodes_g + rec * 2 * (size_t)c->d.g.nx * c->d.g.nz;
     for (int q = 0; q < 3; ++q) {
         t.Ua[q] = G.tUa + (3 * rec + q) * cs;
         t.Up[q] = G.tUp + (3 * rec + q) * cs;

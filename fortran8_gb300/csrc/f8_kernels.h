@@ -86,6 +86,7 @@ struct StepOpts {
     double sor_omega, sor_eps;
     int sor_itrmax;
     cudaEvent_t *ev;   // NSTAGE+1 events recorded at the stage boundaries, or null
+    double *c_mid;     // FP64: receives C as the momentum stage read it (6 halo fields), or null
 };
 constexpr int NSTAGE = 7;
 
@@ -157,8 +158,9 @@ struct AdjState {
 // what the reverse of one step reads from its forward step
 struct TapeStep {
     const double *U, *V, *W;               // velocity at the start of the step (halo)
-    const double *C, *Cn;                  // C before and after the polymer update (halo)
-    const uint8_t *codes;                  // face selection codes
+    const double *C, *Cn;                  // C before the polymer update (the state) and after it as
+                                           // the stress read it (with walls: updated ghost rows)
+    const uint8_t *codes, *codes_g;        // face selection codes (interior, wall ghost rows)
     const double *Ua[3], *Up[3], *Phi;     // explicit velocity, Helmholtz solutions, Phi (halo)
     const double *Fc[3];                   // marker forces
 };

@@ -1396,6 +1396,8 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
     if ((e = bc(d.V, g, BC_V, s))) return e;
     if (d3 && (e = bc(d.W, g, BC_W, s))) return e;
     if ((e = bc(d.P, g, BC_P, s))) return e;
+    if (o.c_mid) F8_CUDA_RET(cudaMemcpyAsync(o.c_mid, d.C, (size_t)d.ncomp * d.cs * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, s));
     if (o.polymer && g.walls) {
         // the wall extrapolation of the ghost rows (C_kabe at the end of the
         // step, fenep_2d.f90:1374)

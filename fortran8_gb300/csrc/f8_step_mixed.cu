@@ -135,6 +135,23 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
+// After the polymer update of a wall channel: the x and z halo cells of every
+// row (ghost rows included) as periodic copies, with their Peterlin factor;
+// the updated ghost rows are kept (extrapolated at the end of the step).
+__global__ void k_bc_c_pet_xz_f(float *C, float *fpet, Geo g, int cs, double lp2) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (!halo_cell_m(g, t, i, j, k)) return;
+    if ((j == 0 || j == g.sy - 1) && i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) return;   // updated ghost cell
+    const int h = hix(g, i, j, k), src = hix(g, wrapx(g, i), j, wrapz(g, k));
+    float x[6];
+    for (int m = 0; m < 6; ++m) {
+        x[m] = C[(size_t)m * cs + src];
+        C[(size_t)m * cs + h] = x[m];
+    }
+    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+}
+
 // halo values (PBM / wall rules, fenep_2d.f90:1098-1129) of a df64 field;
 // uw2 = 2 * upper wall speed (0 for the increments)
 __device__ inline df halo_df(const Geo &g, const float *H, const float *L, int kind, int i, int j, int k, df uw2) {
@@ -282,6 +299,73 @@ __device__ __forceinline__ float2 lam_min2(float2 m, float2 b00, float2 b11, flo
 __constant__ float c_fp_w[5][3] = {{0, 1, 0}, {0, 1.5f, -0.5f}, {0.5f, 0.5f, 0}, {0.25f, 1, -0.25f}, {0, 1, 0}};
 __constant__ float c_fn_w[5][3] = {{0, 1, 0}, {0, 0.5f, 0.5f}, {-0.5f, 1.5f, 0}, {-0.25f, 1, 0.25f}, {0, 1, 0}};
 
+// candidate choice of one direction (maxloc over the three candidates' least
+// eigenvalues and 0, first maximum, NaN ignored), returns the code 0..3
+__device__ __forceinline__ int select_dir_f(const float (&c0)[6], float m0, float e00, float e11, float e22,
+                                            const float (&dm)[6], const float (&dp)[6]) {
+    float ml[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+        float v[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) v[m] = l == 0 ? 0.5f * dp[m] : (l == 1 ? 0.5f * dm[m] : 0.25f * (dm[m] + dp[m]));
+        const float mv = (v[0] + v[3] + v[5]) * (1.0f / 3.0f);
+        const float2 pm = make_float2(-1.0f, 1.0f);
+        const float2 lam = lam_min2(fma2(f2(mv), pm, f2(m0)), fma2(f2(v[0] - mv), pm, f2(e00)),
+                                    fma2(f2(v[3] - mv), pm, f2(e11)), fma2(f2(v[5] - mv), pm, f2(e22)),
+                                    fma2(f2(v[1]), pm, f2(c0[1])), fma2(f2(v[2]), pm, f2(c0[2])),
+                                    fma2(f2(v[4]), pm, f2(c0[4])));
+        ml[l] = fminf(lam.x, lam.y);   // NaN-ignoring minimum
+    }
+    float best = 0.0f;
+    int idx = 4;
+    bool found = false;
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+        if (isnan(ml[l])) continue;
+        if (!found || ml[l] > best) { best = ml[l]; idx = l + 1; found = true; }
+    }
+    if (!found || 0.0f > best) idx = 4;
+    return idx - 1;
+}
+
+// selection codes of the ghost rows of a wall channel (the rows beyond them
+// hold zero C): the reference's wall mode updates C there too
+// (fenep_2d.f90:138-226, 1131-1143)
+__global__ void k_codes_ghost3_f(const float *__restrict__ C, uint8_t *__restrict__ codes_g, Geo g, int cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int side = blockIdx.y, k = blockIdx.z + 1;
+    if (i > g.nx) return;
+    const int j = side ? g.ny + 1 : 0;
+    const int h = hix(g, i, j, k);
+    float c0[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) c0[m] = C[(size_t)m * cs + h];
+    const float m0 = (c0[0] + c0[3] + c0[5]) * (1.0f / 3.0f);
+    const float e00 = c0[0] - m0, e11 = c0[3] - m0, e22 = c0[5] - m0;
+    int code = 0;
+    for (int d = 0; d < 3; ++d) {
+        float dm[6], dp[6];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            const float *Cm = C + (size_t)m * cs;
+            float cmv, cpv;
+            if (d == 1) {
+                cmv = j - 1 < 0 ? 0.0f : Cm[hix(g, i, j - 1, k)];
+                cpv = j + 1 > g.ny + 1 ? 0.0f : Cm[hix(g, i, j + 1, k)];
+            } else {
+                const int od = d == 0 ? 1 : g.sx * g.sy;
+                cmv = Cm[h - od];
+                cpv = Cm[h + od];
+            }
+            dm[m] = c0[m] - cmv;
+            dp[m] = cpv - c0[m];
+        }
+        code |= select_dir_f(c0, m0, e00, e11, e22, dm, dp) << (2 * d);
+    }
+    codes_g[gcix(g, i, j, k)] = (uint8_t)code;
+}
+
 __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, uint8_t *__restrict__ codes, Geo g, int cs,
                                                   int *__restrict__ fixcnt) {
     if ((blockIdx.x | blockIdx.y | blockIdx.z | threadIdx.x | threadIdx.y) == 0) *fixcnt = 0;   // queue of k_update3_f
@@ -305,32 +389,8 @@ __global__ void __launch_bounds__(256) k_codes3_f(const float *__restrict__ C, u
             dm[m] = c0[m] - C[(size_t)m * cs + h - od];
             dp[m] = C[(size_t)m * cs + h + od] - c0[m];
         }
-        float ml[3];
-#pragma unroll
-        for (int l = 0; l < 3; ++l) {
-            float v[6];
-#pragma unroll
-            for (int m = 0; m < 6; ++m) v[m] = l == 0 ? 0.5f * dp[m] : (l == 1 ? 0.5f * dm[m] : 0.25f * (dm[m] + dp[m]));
-            const float mv = (v[0] + v[3] + v[5]) * (1.0f / 3.0f);
-            // lane x: c0 - v (the face on the minus side), lane y: c0 + v
-            const float2 pm = make_float2(-1.0f, 1.0f);
-            const float2 lam = lam_min2(fma2(f2(mv), pm, f2(m0)), fma2(f2(v[0] - mv), pm, f2(e00)),
-                                        fma2(f2(v[3] - mv), pm, f2(e11)), fma2(f2(v[5] - mv), pm, f2(e22)),
-                                        fma2(f2(v[1]), pm, f2(c0[1])), fma2(f2(v[2]), pm, f2(c0[2])),
-                                        fma2(f2(v[4]), pm, f2(c0[4])));
-            ml[l] = fminf(lam.x, lam.y);   // NaN-ignoring minimum
-        }
-        // maxloc over (ml1, ml2, ml3, 0): first maximum, NaN ignored
-        float best = 0.0f;
-        int idx = 4;
-        bool found = false;
-#pragma unroll
-        for (int l = 0; l < 3; ++l) {
-            if (isnan(ml[l])) continue;
-            if (!found || ml[l] > best) { best = ml[l]; idx = l + 1; found = true; }
-        }
-        if (!found || 0.0f > best) idx = 4;
-        code |= (idx - 1) << (2 * d);
+        // lane x of each pair: c0 - v (the face on the minus side), lane y: c0 + v
+        code |= select_dir_f(c0, m0, e00, e11, e22, dm, dp) << (2 * d);
     }
     codes[qix(g, i, j, k)] = (uint8_t)code;
 }
@@ -612,6 +672,86 @@ __global__ void __launch_bounds__(128) k_newton_fix_f(const float *__restrict__ 
         for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
         fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
     }
+}
+
+// Polymer update of the ghost rows of a wall channel (the reference's wall
+// mode, fenep_2d.f90:1912-1929): Cstar with the rows beyond the ghost rows
+// holding zero C and velocity, then the exact FP32 Newton of k_newton_fix_f.
+__global__ void __launch_bounds__(128) k_update_ghost3_f(const float *__restrict__ C, float *__restrict__ Cn,
+                                                         float *__restrict__ fpet, const uint8_t *__restrict__ codes,
+                                                         const uint8_t *__restrict__ codes_g,
+                                                         const float *__restrict__ U, const float *__restrict__ V,
+                                                         const float *__restrict__ W, Geo g, Phys ph, MixConst mc,
+                                                         int cs, StepCounters *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int side = blockIdx.y, k = blockIdx.z + 1;
+    if (i > g.nx) return;
+    const int j = side ? g.ny + 1 : 0;
+    const int h = hix(g, i, j, k);
+    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    auto vrow = [&](const float *A, int ii, int jj, int kk) {
+        return (jj < 0 || jj > g.ny + 1) ? 0.0f : A[hix(g, ii, jj, kk)];
+    };
+    const int im = wrapx(g, i - 1), ip = wrapx(g, i + 1), km = wrapz(g, k - 1), kp = wrapz(g, k + 1);
+    const int cself = codes_g[gcix(g, i, j, k)];
+    const int cxm = codes_g[gcix(g, im, j, k)] & 3, cxp = codes_g[gcix(g, ip, j, k)] & 3;
+    const int czm = (codes_g[gcix(g, i, j, km)] >> 4) & 3, czp = (codes_g[gcix(g, i, j, kp)] >> 4) & 3;
+    // the interior neighbour's y code (its face towards this row); the cell
+    // beyond is outside (coefficient zero)
+    const int cyin = (codes[qix(g, i, side ? g.ny : 1, k)] >> 2) & 3;
+    const bool lower = side == 0;
+    float kx[5], ky[5], kz[5];
+    {
+        const float u1 = U[h - ox], u2 = U[h];
+        const float v1 = vrow(V, i, j - 1, k), v2 = V[h];
+        const float w1 = W[h - oz], w2 = W[h];
+        float k0 = 0.0f;
+        dir_coef(1.0f / 6 + (u1 - fabsf(u1)) * mc.sx, (-u2 + fabsf(u2)) * mc.sx, (u1 + fabsf(u1)) * mc.sx,
+                 1.0f / 6 + (-u2 - fabsf(u2)) * mc.sx, (cself & 3) + 1, cxm + 1, cxp + 1, false, false,
+                 kx[0], kx[1], k0, kx[3], kx[4]);
+        dir_coef(1.0f / 6 + (v1 - fabsf(v1)) * mc.sy, (-v2 + fabsf(v2)) * mc.sy, (v1 + fabsf(v1)) * mc.sy,
+                 1.0f / 6 + (-v2 - fabsf(v2)) * mc.sy, ((cself >> 2) & 3) + 1, lower ? 4 : cyin + 1,
+                 lower ? cyin + 1 : 4, lower, !lower, ky[0], ky[1], k0, ky[3], ky[4]);
+        dir_coef(1.0f / 6 + (w1 - fabsf(w1)) * mc.sz, (-w2 + fabsf(w2)) * mc.sz, (w1 + fabsf(w1)) * mc.sz,
+                 1.0f / 6 + (-w2 - fabsf(w2)) * mc.sz, ((cself >> 4) & 3) + 1, czm + 1, czp + 1, false, false,
+                 kz[0], kz[1], k0, kz[3], kz[4]);
+        kx[2] = k0;
+    }
+    const int hxm2 = hix(g, im, j, k) - ox, hxp2 = hix(g, ip, j, k) + ox;
+    const int hzm2 = hix(g, i, j, km) - oz, hzp2 = hix(g, i, j, kp) + oz;
+    float b[6], x[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        const float *Cm = C + (size_t)m * cs;
+        const float c0 = Cm[h];
+        float acc = kx[2] * c0;
+        acc = fmaf(kx[0], Cm[hxm2], acc); acc = fmaf(kx[1], Cm[h - ox], acc);
+        acc = fmaf(kx[3], Cm[h + ox], acc); acc = fmaf(kx[4], Cm[hxp2], acc);
+        acc = fmaf(ky[0], vrow(Cm, i, j - 2, k), acc); acc = fmaf(ky[1], vrow(Cm, i, j - 1, k), acc);
+        acc = fmaf(ky[3], vrow(Cm, i, j + 1, k), acc); acc = fmaf(ky[4], vrow(Cm, i, j + 2, k), acc);
+        acc = fmaf(kz[0], Cm[hzm2], acc); acc = fmaf(kz[1], Cm[h - oz], acc);
+        acc = fmaf(kz[3], Cm[h + oz], acc); acc = fmaf(kz[4], Cm[hzp2], acc);
+        b[m] = acc + ((m == 0 || m == 3 || m == 5) ? mc.dtwi : 0.0f);
+        x[m] = c0;
+    }
+    // velocity gradient with zero velocity beyond the ghost row
+    Lyap9 A;
+    A.a00 = mc.gx1 * (U[h] - U[h - ox]);
+    A.a10 = mc.gx4 * (-vrow(V, i - 1, j - 1, k) + vrow(V, i + 1, j - 1, k) - V[h - ox] + V[h + ox]);
+    A.a20 = mc.gx4 * (-W[h - ox - oz] + W[h + ox - oz] - W[h - ox] + W[h + ox]);
+    A.a01 = mc.gy4 * (-vrow(U, i - 1, j - 1, k) - vrow(U, i, j - 1, k) + vrow(U, i - 1, j + 1, k) + vrow(U, i, j + 1, k));
+    A.a11 = mc.gy1 * (V[h] - vrow(V, i, j - 1, k));
+    A.a21 = mc.gy4 * (-vrow(W, i, j - 1, k - 1) + vrow(W, i, j + 1, k - 1) - vrow(W, i, j - 1, k) + vrow(W, i, j + 1, k));
+    A.a02 = mc.gz4 * (-U[h - ox - oz] - U[h - oz] + U[h - ox + oz] + U[h + oz]);
+    A.a12 = mc.gz4 * (-vrow(V, i, j - 1, k - 1) - V[h - oz] + vrow(V, i, j - 1, k + 1) + V[h + oz]);
+    A.a22 = mc.gz1 * (W[h] - W[h - oz]);
+    (void)oy;
+    const int itr = newton_exact_f(x, b, A, mc.dtwi, mc.lp2f, ph.lp2, mc.epsf, ph.newton_itrmax);
+    atomicAdd(&cnt->newton_iters, (unsigned long long)itr);
+    if (itr > ph.newton_itrmax) atomicAdd(&cnt->newton_unconverged, 1ull);
+#pragma unroll
+    for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
+    fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
 }
 
 // ---------------------------------------------------------------------------
@@ -1389,9 +1529,20 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
                                                         d.cs, d.fixlist, d.fixcnt, d.cnt); count_launch();
         k_newton_fix_f<<<2 * 152, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
                                                d.fixcnt, d.cnt); count_launch();
-        std::swap(d.Cf, d.Cnf);
         long n = halo_count_m(g);
-        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+        if (g.walls) {
+            // ghost rows of the wall channel: updated like the interior
+            // (their codes read the state before the update)
+            const dim3 gg((g.nx + 127) / 128, 2, g.nz);
+            k_codes_ghost3_f<<<gg, 128, 0, s>>>(d.Cf, d.codes_g, g, d.cs); count_launch();
+            k_update_ghost3_f<<<gg, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.codes_g, d.Uf, d.Vf, d.Wf, g, d.ph,
+                                                 mc, d.cs, d.cnt); count_launch();
+            std::swap(d.Cf, d.Cnf);
+            k_bc_c_pet_xz_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+        } else {
+            std::swap(d.Cf, d.Cnf);
+            k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+        }
         if ((e = cudaGetLastError())) return e;
     } else {
         mark(1);
@@ -1510,6 +1661,12 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         count_launch();
     }
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
+    if (o.polymer && g.walls) {
+        // the wall extrapolation of the C ghost rows (C_kabe at the end of the
+        // step, fenep_2d.f90:1374)
+        long n = halo_count_m(g);
+        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+    }
     mark(7);
     return cudaGetLastError();
 }
