@@ -191,6 +191,10 @@ struct f8_ctx {
         }
         if (d.ev_fork) cudaEventDestroy(d.ev_fork);
         d.ev_fork = nullptr;
+        for (cudaEvent_t &ev : d.ev_g) {
+            if (ev) cudaEventDestroy(ev);
+            ev = nullptr;
+        }
         if (s) cudaStreamDestroy(s);
         s = nullptr;
     }
@@ -384,6 +388,7 @@ int setup(f8_ctx *c) {
                 API_CUDA(c, cudaEventCreateWithFlags(&d.ev_join[b], cudaEventDisableTiming));
             }
             API_CUDA(c, cudaEventCreateWithFlags(&d.ev_fork, cudaEventDisableTiming));
+            for (int q = 0; q < 4; ++q) API_CUDA(c, cudaEventCreateWithFlags(&d.ev_g[q], cudaEventDisableTiming));
         }
         {
             std::vector<float2> t2(std::max(1, g.nz / 2));

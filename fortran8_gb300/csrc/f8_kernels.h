@@ -56,6 +56,7 @@ struct Dev {
                                            // beside the U solve (fused spectral path)
     cudaStream_t aux[2];                   // the side streams of those two solves (0: none)
     cudaEvent_t ev_fork, ev_join[2];
+    cudaEvent_t ev_g[4];                   // wall ghost-row branch: start, codes ready, update done, momentum done
     float *twxf_r, *twxf_i, *twyf_r, *twyf_i, *twzf_r, *twzf_i;
     float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
     int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory

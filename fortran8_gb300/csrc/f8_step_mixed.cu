@@ -152,6 +152,26 @@ __global__ void k_bc_c_pet_xz_f(float *C, float *fpet, Geo g, int cs, double lp2
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
+// The wall extrapolation of the C ghost rows (C_kabe, fenep_2d.f90:1131-1143)
+// and their Peterlin factor, every x and z (the x/z halo copies of rows 1, 2,
+// NY-1, NY are already in place).
+__global__ void k_extrap_ghost_f(float *C, float *fpet, Geo g, int cs, double lp2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * g.sx * g.sz) return;
+    const int side = t / (g.sx * g.sz), r = t % (g.sx * g.sz);
+    const int i = r % g.sx, k = r / g.sx;
+    const int j = side ? g.ny + 1 : 0, j1 = side ? g.ny : 1, j2 = side ? g.ny - 1 : 2;
+    const int h = hix(g, i, j, k), h1 = hix(g, i, j1, k), h2 = hix(g, i, j2, k);
+    float x[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        float *A = C + (size_t)m * cs;
+        x[m] = 2.0f * A[h1] - A[h2];
+        A[h] = x[m];
+    }
+    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+}
+
 // halo values (PBM / wall rules, fenep_2d.f90:1098-1129) of a df64 field;
 // uw2 = 2 * upper wall speed (0 for the increments)
 __device__ inline df halo_df(const Geo &g, const float *H, const float *L, int kind, int i, int j, int k, df uw2) {
@@ -685,7 +705,8 @@ __global__ void __launch_bounds__(128) k_update_ghost3_f(const float *__restrict
                                                          int cs, StepCounters *cnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int side = blockIdx.y, k = blockIdx.z + 1;
-    if (i > g.nx) return;
+    unsigned long long my_itr = 0, my_unconv = 0;
+    if (i <= g.nx) {
     const int j = side ? g.ny + 1 : 0;
     const int h = hix(g, i, j, k);
     const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
@@ -746,12 +767,30 @@ __global__ void __launch_bounds__(128) k_update_ghost3_f(const float *__restrict
     A.a12 = mc.gz4 * (-vrow(V, i, j - 1, k - 1) - V[h - oz] + vrow(V, i, j - 1, k + 1) + V[h + oz]);
     A.a22 = mc.gz1 * (W[h] - W[h - oz]);
     (void)oy;
-    const int itr = newton_exact_f(x, b, A, mc.dtwi, mc.lp2f, ph.lp2, mc.epsf, ph.newton_itrmax);
-    atomicAdd(&cnt->newton_iters, (unsigned long long)itr);
-    if (itr > ph.newton_itrmax) atomicAdd(&cnt->newton_unconverged, 1ull);
+    // the fast Newton of k_update3_f, then (rarely) the exact one from the start
+    const float x0[6] = {x[0], x[1], x[2], x[3], x[4], x[5]};
+    const int fast_max = min(NEWTON_FAST_MAX, ph.newton_itrmax);
+    int itr = newton_fast_f(x, b, A, mc, ph.lp2, fast_max);
+    if (itr > fast_max && fast_max < ph.newton_itrmax) {
+#pragma unroll
+        for (int m = 0; m < 6; ++m) x[m] = x0[m];
+        itr = fast_max + newton_exact_f(x, b, A, mc.dtwi, mc.lp2f, ph.lp2, mc.epsf, ph.newton_itrmax);
+    }
+    my_itr = (unsigned long long)itr;
+    my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
 #pragma unroll
     for (int m = 0; m < 6; ++m) Cn[(size_t)m * cs + h] = x[m];
     fpet[h] = peterlin_f(x[0], x[3], x[5], mc.lp2f, ph.lp2);
+    }
+    unsigned long long a = my_itr, b2 = my_unconv;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b2 += __shfl_down_sync(0xffffffffu, b2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicAdd(&cnt->newton_iters, a);
+        if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1521,22 +1560,39 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
     const DfF U{d.Uf, d.Ul}, V{d.Vf, d.Vl}, W{d.Wf, d.Wl}, P{d.Pf, d.Pl}, Phi{d.Phif, d.Phil};
     mark(0);
+    // wall channel: the ghost rows' codes and update run on a side stream
+    // beside the interior kernels (they read the state and the interior codes
+    // of rows 1 and NY, and write only ghost-row cells)
+    const bool gbranch = o.polymer && g.walls && d.aux[0];
+    const dim3 gg((g.nx + 127) / 128, 2, g.nz);
+    cudaStream_t sg = gbranch ? d.aux[0] : s;
     if (o.polymer) {
         dim3 blk(32, 4);
+        if (g.walls) {
+            if (gbranch) {
+                F8_CUDA_RET(cudaEventRecord(d.ev_g[0], s));
+                F8_CUDA_RET(cudaStreamWaitEvent(sg, d.ev_g[0], 0));
+            }
+            k_codes_ghost3_f<<<gg, 128, 0, sg>>>(d.Cf, d.codes_g, g, d.cs); count_launch();
+        }
         k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs, d.fixcnt); count_launch();
         mark(1);
+        if (g.walls) {
+            if (gbranch) {
+                F8_CUDA_RET(cudaEventRecord(d.ev_g[1], s));
+                F8_CUDA_RET(cudaStreamWaitEvent(sg, d.ev_g[1], 0));
+            }
+            k_update_ghost3_f<<<gg, 128, 0, sg>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.codes_g, d.Uf, d.Vf, d.Wf, g, d.ph,
+                                                  mc, d.cs, d.cnt); count_launch();
+            if (gbranch) F8_CUDA_RET(cudaEventRecord(d.ev_g[2], sg));
+        }
         k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc,
                                                         d.cs, d.fixlist, d.fixcnt, d.cnt); count_launch();
         k_newton_fix_f<<<2 * 152, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
                                                d.fixcnt, d.cnt); count_launch();
         long n = halo_count_m(g);
         if (g.walls) {
-            // ghost rows of the wall channel: updated like the interior
-            // (their codes read the state before the update)
-            const dim3 gg((g.nx + 127) / 128, 2, g.nz);
-            k_codes_ghost3_f<<<gg, 128, 0, s>>>(d.Cf, d.codes_g, g, d.cs); count_launch();
-            k_update_ghost3_f<<<gg, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.codes_g, d.Uf, d.Vf, d.Wf, g, d.ph,
-                                                 mc, d.cs, d.cnt); count_launch();
+            if (gbranch) F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_g[2], 0));
             std::swap(d.Cf, d.Cnf);
             k_bc_c_pet_xz_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
         } else {
@@ -1563,6 +1619,17 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         dim3 blk(32, 8);
         k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch();
         if ((e = cudaGetLastError())) return e;
+    }
+    if (o.polymer && g.walls) {
+        // the momentum stage was the last reader of the updated ghost rows:
+        // extrapolate them (C_kabe at the end of the reference's step,
+        // fenep_2d.f90:1374), beside the IBM stage when a side stream exists
+        const int ng = 2 * g.sx * g.sz;
+        if (gbranch) {
+            F8_CUDA_RET(cudaEventRecord(d.ev_g[3], s));
+            F8_CUDA_RET(cudaStreamWaitEvent(sg, d.ev_g[3], 0));
+        }
+        k_extrap_ghost_f<<<(ng + 255) / 256, 256, 0, sg>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
     }
     mark(3);
     if (o.ibm) {
@@ -1661,11 +1728,10 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         count_launch();
     }
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
-    if (o.polymer && g.walls) {
-        // the wall extrapolation of the C ghost rows (C_kabe at the end of the
-        // step, fenep_2d.f90:1374)
-        long n = halo_count_m(g);
-        k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+    if (gbranch) {
+        // join the ghost-row branch (when the Helmholtz branches did not)
+        F8_CUDA_RET(cudaEventRecord(d.ev_g[2], sg));
+        F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_g[2], 0));
     }
     mark(7);
     return cudaGetLastError();
