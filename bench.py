@@ -438,9 +438,9 @@ def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_pref
 
 # launches per step of each stage kernel of the mixed step (wall channel)
 MIXED_STAGE_LAUNCHES = {
-    "eigen": {"k_codes3_f": 1},
-    "newton": {"k_update3_f": 1, "k_newton_fix_f": 1, "k_bc_c_pet_f": 1},
-    "momentum": {"k_momentum3_f": 1},
+    "eigen": {"k_codes3_f": 1, "k_codes_ghost3_f": 1},
+    "newton": {"k_update3_f": 1, "k_newton_fix_f": 1, "k_update_ghost3_f": 1, "k_bc_c_pet_xz_f": 1},
+    "momentum": {"k_momentum3_f": 1, "k_extrap_ghost_f": 1},
     "ibm": {"k_ibm_interp_f": 1, "k_ibm_spread_f": 1, "k_drag_part": 1, "k_drag_final": 1},
     "helmholtz": {"k_xfwd_w": 3, "k_plane_walls_c": 3, "k_xinv_w": 3},
     "poisson": {"k_poisson_rhs_df": 1, "k_xfwd_w": 2, "k_plane_walls_c": 2, "k_xinv_w": 2, "k_defect_df": 1},
