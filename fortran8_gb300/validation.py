@@ -46,25 +46,36 @@ def koide_profile(nx: int, beta: float, wi: float, lp: float, re: float = 1.0, f
     return out
 
 
-def koide_case(nx: int, beta: float, wi: float, lp: float = 55.0, re: float = 1.0, dt: float = 0.005):
+def koide_case(nx: int, beta: float, wi: float, lp: float = 55.0, re: float = 1.0, dt: float = 0.005,
+               nz: int = 0):
     """(grid, phys, initial state) of the validation channel: U = V = 0, C = I,
-    Fx = 1 (flow_type 2, fenep_2d.f90:86-90); 2D Newton parameters of
-    fenep_2d.f90:291-293."""
-    g = GridSpec(2, nx, nx // 2, 1, 2 * PI, PI, 2 * PI / nx, abi.F8_BC_WALLS, 0.0)
-    ph = PhysSpec(re=re, wi=wi, beta=beta, lp2=lp * lp, dt=dt, newton_dc=1.0e-10, newton_eps=1.0e-10)
+    Fx = 1 (flow_type 2, fenep_2d.f90:86-90).  nz = 0: the 2D channel with the
+    2D Newton parameters of fenep_2d.f90:291-293; nz > 0: the same channel
+    extruded over nz cells in z (periodic), a 3D grid whose steady Newtonian
+    flow is the 2D one."""
+    if nz:
+        g = GridSpec(3, nx, nx // 2, nz, 2 * PI, PI, nz * 2 * PI / nx, abi.F8_BC_WALLS, 0.0)
+        ph = PhysSpec(re=re, wi=wi, beta=beta, lp2=lp * lp, dt=dt)
+    else:
+        g = GridSpec(2, nx, nx // 2, 1, 2 * PI, PI, 2 * PI / nx, abi.F8_BC_WALLS, 0.0)
+        ph = PhysSpec(re=re, wi=wi, beta=beta, lp2=lp * lp, dt=dt, newton_dc=1.0e-10, newton_eps=1.0e-10)
     st = empty_state(g)
-    st.arrays["c"][..., 0] = 1.0
-    st.arrays["c"][..., 2] = 1.0
+    c = st.arrays["c"]
+    c[..., 0] = 1.0
+    c[..., 3 if nz else 2] = 1.0
+    if nz:
+        c[..., 5] = 1.0
     st.arrays["fx"][:] = 1.0
     return g, ph, st
 
 
 def koide_rmse(state: State, nx: int, beta: float, wi: float, lp: float = 55.0, re: float = 1.0) -> float:
     """RMSE of U against the analytic profile over the channel cells, as
-    koide_theory sums it (fenep_2d.f90:1426-1432)."""
-    u = state["u"][1, 1:-1, 1:-1]
+    koide_theory sums it (fenep_2d.f90:1426-1432); for a 3D grid over every
+    z plane."""
+    u = state["u"][1:-1, 1:-1, 1:-1]
     ut = koide_profile(nx, beta, wi, lp, re)
-    return math.sqrt(float(((u - ut[:, None]) ** 2).sum()) / (nx * (nx // 2)))
+    return math.sqrt(float(((u - ut[None, :, None]) ** 2).sum()) / u.size)
 
 
 def run_to_steady(solver, nx: int, beta: float, wi: float, lp: float = 55.0, chunk: int = 2000,
