@@ -329,7 +329,6 @@ int setup(f8_ctx *c) {
         API_CUDA(c, c->alloc(&d.Rdf, ni));
         API_CUDA(c, c->alloc(&d.Hf, nspec));
         API_CUDA(c, c->alloc(&d.H2f, nspec));
-        d.defect_iters = 1;
     }
     API_CUDA(c, c->alloc(&d.red, 4096));
     API_CUDA(c, c->alloc(&d.scal, 64));

@@ -92,6 +92,75 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
 
 __device__ __forceinline__ float df_to_f(df a) { return __fadd_rn(a.hi, a.lo); }
 
+// Two independent df64 values in the lanes of FP32x2 registers, for the
+// packed FP32 instructions of sm_100 and later.  Each lane performs the
+// operations of the scalar routine of the same name in the same order with
+// the same rounding (a - b is a + (-b) exactly), so a lane's result is
+// bit-identical to the scalar one.
+struct df2 {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
+    s = add2_rn(a, b);
+    const float2 bb = sub2_rn(s, a);
+    e = add2_rn(sub2_rn(a, sub2_rn(s, bb)), sub2_rn(b, bb));
+}
+
+__device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
+    s = add2_rn(a, b);
+    e = sub2_rn(b, sub2_rn(s, a));
+}
+
+__device__ __forceinline__ df2 df2_pack(df a, df b) {
+    return df2{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
+}
+__device__ __forceinline__ df df2_x(df2 a) { return df{a.hi.x, a.lo.x}; }
+__device__ __forceinline__ df df2_y(df2 a) { return df{a.hi.y, a.lo.y}; }
+
+__device__ __forceinline__ df2 df2_add(df2 a, df2 b) {
+    float2 s, e;
+    two_sum2(a.hi, b.hi, s, e);
+    e = add2_rn(e, add2_rn(a.lo, b.lo));
+    df2 r;
+    fast_two_sum2(s, e, r.hi, r.lo);
+    return r;
+}
+
+__device__ __forceinline__ df2 df2_neg(df2 a) { return df2{neg2(a.hi), neg2(a.lo)}; }
+__device__ __forceinline__ df2 df2_sub(df2 a, df2 b) { return df2_add(a, df2_neg(b)); }
+
+// a + b, b a float pair
+__device__ __forceinline__ df2 df2_add_f(df2 a, float2 b) {
+    float2 s, e;
+    two_sum2(a.hi, b, s, e);
+    e = add2_rn(e, a.lo);
+    df2 r;
+    fast_two_sum2(s, e, r.hi, r.lo);
+    return r;
+}
+
+// a - b for float pairs, exact
+__device__ __forceinline__ df2 df2_diff_ff(float2 a, float2 b) {
+    df2 r;
+    two_sum2(a, neg2(b), r.hi, r.lo);
+    return r;
+}
+
+__device__ __forceinline__ df2 df2_mul(df2 a, df2 b) {
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, neg2(p));
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    df2 r;
+    fast_two_sum2(p, e, r.hi, r.lo);
+    return r;
+}
+
 // split of a double into a df64 pair (host and device)
 __host__ __device__ inline df df_from_d(double x) {
     const float hi = (float)x;

@@ -87,9 +87,7 @@ __global__ void k_fft_x_fwd(const TS *__restrict__ src, T *__restrict__ H, int n
 
 // Destinations of an inverse x pass.  XOutD: an FP64 field, optionally the
 // sum base + value (FP64 path and stand-alone solve).  XOutF: the FP32 /
-// double-float fields of the mixed path: mode 0 stores the value in hi,
-// mode 1 stores the df64 value (value, 0), mode 2 adds the value to the df64
-// field (hi, lo).
+// double-float fields of the mixed path (modes below).
 struct XOutD {
     double *dst;
     const double *base;
@@ -99,16 +97,16 @@ struct XOutD {
 struct XOutF {
     float *hi, *lo;
     int mode;
+    // mode 0: hi = v.  mode 2: (hi, lo) = hi + v exactly (two-sum), the
+    // correction of an FP32 field to a df64 pair
     __device__ __forceinline__ void put(size_t o, float v) const {
         if (mode == 0) {
             hi[o] = v;
-        } else if (mode == 1) {
-            hi[o] = v;
-            lo[o] = 0.0f;
         } else {
-            const df r = df_add_f(df{hi[o], lo[o]}, v);
-            hi[o] = r.hi;
-            lo[o] = r.lo;
+            float s, e;
+            two_sum(hi[o], v, s, e);
+            hi[o] = s;
+            lo[o] = e;
         }
     }
 };

@@ -71,7 +71,6 @@ struct Dev {
     int *mi0d[3], *mj0d[3];                // FP64: per-marker stencil origins
     int *act_cols[3];                      // interior (i,j) columns that receive spreading
     int nact[3];
-    int defect_iters;                      // Poisson defect corrections (mixed)
     // reductions
     double *red;                           // scratch partial sums (>= 4096)
     double *scal;                          // small scalar results

@@ -31,7 +31,6 @@
 namespace f8 {
 namespace {
 
-constexpr float TWO_PI_3F = 2.0943951023931955f;
 
 // Grid constants of the mixed kernels, computed once on the host in FP64 so
 // that no kernel divides in FP64 (FP64 division is slow on this part).
@@ -255,13 +254,21 @@ __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
 // candidate face in the shifted (traceless) trigonometric form, which is the
 // same root as the reference's Vieta formula (fenep.f90:425-444) but free of
 // the cancellation in p = a1 - a2^2/3 that FP32 would suffer near C = I.
-// Equal roots (discriminant q^2 - p^3 >= 0) give the reference's -100
-// sentinel.  The two faces of candidate l (fenep.f90:179-184) are c0 - v and
-// c0 + v with v = dp/2, dm/2, (dm + dp)/4 for l = 1, 2, 3 (dm = c0 - c_{-1},
-// dp = c_{+1} - c0), so they share the mean and deviatoric part of c0 and are
-// evaluated as one packed FP32x2 pair.
-// arccos by Abramowitz & Stegun 4.4.46: acos(x) = sqrt(1-x) * P7(x) on [0, 1]
-// with |error| <= 2e-8, and acos(-x) = pi - acos(x).
+// Equal roots (discriminant q^2 - p^3 >= 0, i.e. |r| >= 1 below) give the
+// reference's -100 sentinel.  The two faces of candidate l (fenep.f90:179-184)
+// are c0 - v and c0 + v with v = dp/2, dm/2, (dm + dp)/4 for l = 1, 2, 3
+// (dm = c0 - c_{-1}, dp = c_{+1} - c0), so they share the mean and deviatoric
+// part of c0 and are evaluated as one packed FP32x2 pair.
+//
+// With B the deviatoric part, p = |B|^2 / 6, q = det(B) / 2 and
+// r = q / p^(3/2), the smallest eigenvalue is m + 2 sqrt(p) t(r),
+// t(r) = cos(acos(r)/3 + 2 pi/3), the smallest root of 4t^3 - 3t = r.  t has a
+// square-root branch point at r = 1 (two equal smallest roots) and is
+// analytic at r = -1, so as a function of u = sqrt(1 - r) on [0, sqrt 2] it is
+// analytic: 2t(u) is evaluated as the degree-7 polynomial interpolating it at
+// the Chebyshev points of [0, sqrt 2] (fitted offline in double precision;
+// |error| <= 2.6e-8 before FP32 rounding, 2.2e-7 in FP32 Horner form).  This
+// replaces the arccos and cosine of the trigonometric formula.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -270,21 +277,16 @@ __device__ __forceinline__ float2 fms2(float2 a, float2 b, float2 c) {   // a * 
     return __ffma2_rn(a, b, make_float2(-c.x, -c.y));
 }
 
-__device__ __forceinline__ float2 acos_as2(float2 x) {
-    const float2 ax = make_float2(fabsf(x.x), fabsf(x.y));
-    float2 p = f2(-0.0012624911f);
-    p = fma2(p, ax, f2(0.0066700901f));
-    p = fma2(p, ax, f2(-0.0170881256f));
-    p = fma2(p, ax, f2(0.0308918810f));
-    p = fma2(p, ax, f2(-0.0501743046f));
-    p = fma2(p, ax, f2(0.0889789874f));
-    p = fma2(p, ax, f2(-0.2145988016f));
-    p = fma2(p, ax, f2(1.5707963050f));
-    const float2 t = add2(f2(1.0f), make_float2(-ax.x, -ax.y));
-    // sqrt(1 - |x|) as t * rsqrt(t), 0 at |x| = 1
-    const float2 st = make_float2(t.x > 0.0f ? t.x * rsqrtf(t.x) : 0.0f, t.y > 0.0f ? t.y * rsqrtf(t.y) : 0.0f);
-    const float2 r = mul2(st, p);
-    return make_float2(x.x < 0.0f ? 3.14159265358979f - r.x : r.x, x.y < 0.0f ? 3.14159265358979f - r.y : r.y);
+// 2 t(u), u = sqrt(1 - r)
+__device__ __forceinline__ float2 two_t2(float2 u) {
+    float2 p = f2(-1.993398037e-04f);
+    p = fma2(p, u, f2(1.522336388e-03f));
+    p = fma2(p, u, f2(-5.673570558e-03f));
+    p = fma2(p, u, f2(1.511769835e-02f));
+    p = fma2(p, u, f2(-3.736452013e-02f));
+    p = fma2(p, u, f2(1.110385135e-01f));
+    p = fma2(p, u, f2(-8.164918423e-01f));
+    return fma2(p, u, f2(-1.0f));
 }
 
 // smallest eigenvalues of the pair of symmetric matrices m + B (B traceless,
@@ -303,15 +305,15 @@ __device__ __forceinline__ float2 lam_min2(float2 m, float2 b00, float2 b11, flo
     const float2 a01 = fms2(b01, b22, mul2(b12, b02));
     const float2 a02 = fms2(b01, b12, mul2(b11, b02));
     const float2 q = mul2(fma2(b02, a02, fms2(b00, a00, mul2(b01, a01))), f2(0.5f));
-    const float2 p3 = mul2(mul2(p2, p2), p2);
-    const float2 qq = mul2(q, q);
     const float2 rs = make_float2(rsqrtf(p2.x), rsqrtf(p2.y));
-    float2 r = mul2(mul2(q, rs), mul2(rs, rs));
-    r = make_float2(fminf(1.0f, fmaxf(-1.0f, r.x)), fminf(1.0f, fmaxf(-1.0f, r.y)));
-    const float2 ang = fma2(acos_as2(r), f2(1.0f / 3.0f), f2(TWO_PI_3F));
-    const float2 cs = make_float2(__cosf(ang.x), __cosf(ang.y));
-    const float2 lam = fma2(mul2(f2(2.0f), mul2(p2, rs)), cs, m);
-    return make_float2(qq.x >= p3.x ? -100.0f : lam.x, qq.y >= p3.y ? -100.0f : lam.y);
+    const float2 r = mul2(mul2(q, rs), mul2(rs, rs));
+    // w = 1 - r; 0 < w < 2 is |r| < 1.  p = 0 (an isotropic face) gives
+    // r = NaN, which fails the test: equal roots, the sentinel.
+    const float2 w = add2(f2(1.0f), make_float2(-r.x, -r.y));
+    const bool okx = w.x > 0.0f && w.x < 2.0f, oky = w.y > 0.0f && w.y < 2.0f;
+    const float2 u = make_float2(okx ? w.x * rsqrtf(w.x) : 0.0f, oky ? w.y * rsqrtf(w.y) : 0.0f);
+    const float2 lam = fma2(mul2(p2, rs), two_t2(u), m);
+    return make_float2(okx ? lam.x : -100.0f, oky ? lam.y : -100.0f);
 }
 
 // candidate faces (fenep.f90:179-184) as weights of (C_{m-1}, C_m, C_{m+1});
@@ -1007,111 +1009,165 @@ struct DfF {
     __device__ __forceinline__ void set(int q, df v) const { hi[q] = v.hi; lo[q] = v.lo; }
 };
 
+// The three df64 kernels of the pressure stage take two cells per thread,
+// (i, j, k) and (i, j, k + 1) with k odd, in the two lanes of FP32x2 pairs:
+// every df64 operation runs once on the pair (the packed routines of
+// f8_df64.cuh, lane-wise identical to the scalar ones), the z neighbours
+// shared by the two cells are loaded once, and every load is issued before
+// the first store.  For odd NZ the last thread's second lane repeats the
+// first cell and is not stored.
+struct Pair {
+    int h, hb;    // the two cells (hb = h when there is no second cell)
+    bool two;
+};
+
+__device__ __forceinline__ bool pair_of(const Geo &g, int &i, int &j, int &k, Pair &p) {
+    i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    k = 2 * blockIdx.z + 1;
+    if (i > g.nx || j > g.ny) return false;
+    p.two = k + 1 <= g.nz;
+    p.h = hix(g, i, j, k);
+    p.hb = p.two ? p.h + g.sx * g.sy : p.h;
+    return true;
+}
+
+__device__ __forceinline__ df2 at2(const DfF &F, int a, int b) { return df2_pack(F.at(a), F.at(b)); }
+__device__ __forceinline__ float2 at2f(const float *F, int a, int b) { return make_float2(F[a], F[b]); }
+__device__ __forceinline__ df2 bcast(df a) { return df2_pack(a, a); }
+
 // Poisson right-hand side div(U^n + dU)/dt (fenep.f90:1494-1510) in df64:
 // each face difference of the state and of the FP32 increment is formed
-// exactly, scaled by the df64 1/dX, and summed.
+// exactly, scaled by the df64 1/dX, and summed (x, y, z in that order).
 __global__ void k_poisson_rhs_df(DfF U, DfF V, DfF W, const float *__restrict__ dU, const float *__restrict__ dV,
                                  const float *__restrict__ dW, float *__restrict__ Rh, float *__restrict__ Rl, Geo g,
                                  MixConst mc) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.nx || j > g.ny) return;
-    const int h = hix(g, i, j, k);
-    const int off[3] = {1, g.sx, g.sx * g.sy};
-    const DfF F[3] = {U, V, W};
-    const float *D[3] = {dU, dV, dW};
+    int i, j, k;
+    Pair p;
+    if (!pair_of(g, i, j, k, p)) return;
+    const int h = p.h, hb = p.hb, oy = g.sx;
     // the increments have no halo pass: periodic neighbours by wrapping; at
     // the lower wall dV(j = 0) = 0 is the ghost row the wall solve wrote
-    const int dm[3] = {hix(g, wrapx(g, i - 1), j, k), g.walls ? h - off[1] : hix(g, i, wrapy(g, j - 1), k),
-                       hix(g, i, j, wrapz(g, k - 1))};
-    df sum{0.0f, 0.0f};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        df a = df_sub(F[c].at(h), F[c].at(h - off[c]));
-        a = df_add(a, df_diff_ff(D[c][h], D[c][dm[c]]));
-        sum = df_add(sum, df_mul(a, mc.di[c]));
+    const int kb = p.two ? k + 1 : k;
+    const int xa = hix(g, wrapx(g, i - 1), j, k), xb = hix(g, wrapx(g, i - 1), j, kb);
+    const int ya = g.walls ? h - oy : hix(g, i, wrapy(g, j - 1), k);
+    const int yb = g.walls ? hb - oy : hix(g, i, wrapy(g, j - 1), kb);
+    const int za = hix(g, i, j, wrapz(g, k - 1));
+    // loads: W and dW at k - 1 .. k + 1, the cells' own values and their
+    // x / y neighbours
+    const df2 Uc = at2(U, h, hb), Um = at2(U, h - 1, hb - 1);
+    const df2 Vc = at2(V, h, hb), Vm = at2(V, h - oy, hb - oy);
+    const df W0 = W.at(hix(g, i, j, k - 1)), W1 = W.at(h), W2 = W.at(hb);
+    const float2 dUc = at2f(dU, h, hb), dUm = at2f(dU, xa, xb);
+    const float2 dVc = at2f(dV, h, hb), dVm = at2f(dV, ya, yb);
+    const float dW0 = dW[za], dW1 = dW[h], dW2 = dW[hb];
+    df2 a = df2_add(df2_sub(Uc, Um), df2_diff_ff(dUc, dUm));
+    df2 sum = df2_mul(a, bcast(mc.di[0]));
+    a = df2_add(df2_sub(Vc, Vm), df2_diff_ff(dVc, dVm));
+    sum = df2_add(sum, df2_mul(a, bcast(mc.di[1])));
+    a = df2_add(df2_sub(df2_pack(W1, W2), df2_pack(W0, W1)),
+                df2_diff_ff(make_float2(dW1, dW2), make_float2(dW0, dW1)));
+    sum = df2_add(sum, df2_mul(a, bcast(mc.di[2])));
+    sum = df2_mul(sum, bcast(mc.idt));
+    const int oa = qix(g, i, j, k);
+    Rh[oa] = sum.hi.x;
+    Rl[oa] = sum.lo.x;
+    if (p.two) {
+        const int ob = oa + g.nx * g.ny;
+        Rh[ob] = sum.hi.y;
+        Rl[ob] = sum.lo.y;
     }
-    sum = df_mul(sum, mc.idt);
-    const int o = qix(g, i, j, k);
-    Rh[o] = sum.hi;
-    Rl[o] = sum.lo;
 }
 
-// defect r = rhs - L_h Phi in df64 (Phi with its Neumann / periodic halo);
-// the FP32 value of r drives the correction solve
-__global__ void k_defect_df(DfF Phi, const float *__restrict__ Rh, const float *__restrict__ Rl,
+// defect r = rhs - L_h Phi in df64.  Phi is the first FP32 solve's result
+// (no low part), so each one-sided difference is the exact difference of two
+// floats; the FP32 value of r drives the correction solve.
+__global__ void k_defect_df(const float *__restrict__ Phi, const float *__restrict__ Rh, const float *__restrict__ Rl,
                             float *__restrict__ r, Geo g, MixConst mc) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > g.nx || j > g.ny) return;
-    const int h = hix(g, i, j, k);
-    const df c0 = Phi.at(h);
-    const int o = qix(g, i, j, k);
-    df res{Rh[o], Rl[o]};
+    int i, j, k;
+    Pair p;
+    if (!pair_of(g, i, j, k, p)) return;
+    const int h = p.h, hb = p.hb, kb = p.two ? k + 1 : k;
+    const int oa = qix(g, i, j, k), ob = p.two ? oa + g.nx * g.ny : oa;
+    const float z0 = Phi[nbr_p(g, i, j, k, 2, -1)], z1 = Phi[h], z2 = Phi[p.two ? hb : nbr_p(g, i, j, k, 2, 1)];
+    const float z3 = p.two ? Phi[nbr_p(g, i, j, kb, 2, 1)] : z2;
+    const float2 c0 = make_float2(z1, p.two ? z2 : z1);
+    const float2 pp[3] = {make_float2(Phi[nbr_p(g, i, j, k, 0, 1)], Phi[nbr_p(g, i, j, kb, 0, 1)]),
+                          make_float2(Phi[nbr_p(g, i, j, k, 1, 1)], Phi[nbr_p(g, i, j, kb, 1, 1)]),
+                          make_float2(z2, p.two ? z3 : z2)};
+    const float2 pm[3] = {make_float2(Phi[nbr_p(g, i, j, k, 0, -1)], Phi[nbr_p(g, i, j, kb, 0, -1)]),
+                          make_float2(Phi[nbr_p(g, i, j, k, 1, -1)], Phi[nbr_p(g, i, j, kb, 1, -1)]),
+                          make_float2(z0, p.two ? z1 : z0)};
+    df2 res{make_float2(Rh[oa], Rh[ob]), make_float2(Rl[oa], Rl[ob])};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const df dp = df_sub(Phi.at(nbr_p(g, i, j, k, c, 1)), c0), dm = df_sub(c0, Phi.at(nbr_p(g, i, j, k, c, -1)));
-        res = df_sub(res, df_mul(df_sub(dp, dm), mc.di2[c]));
+        const df2 dp = df2_diff_ff(pp[c], c0), dm = df2_diff_ff(c0, pm[c]);
+        res = df2_sub(res, df2_mul(df2_sub(dp, dm), bcast(mc.di2[c])));
     }
-    r[o] = df_to_f(res);
+    r[oa] = __fadd_rn(res.hi.x, res.lo.x);
+    if (p.two) r[ob] = __fadd_rn(res.hi.y, res.lo.y);
 }
 
 // projection and SMAC pressure update (fenep.f90:1562-1604):
 // U^{n+1} = U^n + (dU - dt/dX (Phi_{+1} - Phi)) in df64, and
 // P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
-// in FP32
-// Two cells per thread, k and k + 1: the z neighbours of Phi are shared and
-// every load of both cells is issued before the first store.
-__device__ __forceinline__ void march_cell(DfF (&F)[3], DfF P, const float *const (&D)[3], int h, df c0,
-                                           const df (&pp)[3], const df (&pm)[3], const MixConst &mc, float &unew) {
-    const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
-    df nu[3];
-    float lap = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const df dp = df_sub(pp[c], c0);
-        const df inc = df_add_f(df_mul(dp, df_neg(mc.dtd[c])), D[c][h]);
-        nu[c] = df_add(F[c].at(h), inc);
-        const float dpf = (pp[c].hi - c0.hi) + (pp[c].lo - c0.lo), dmf = (c0.hi - pm[c].hi) + (c0.lo - pm[c].lo);
-        lap += (dpf - dmf) * i2[c];
-    }
-    const df pn = df_add_f(df_add(P.at(h), c0), -mc.pcf * lap);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) F[c].set(h, nu[c]);
-    P.set(h, pn);
-    unew = nu[0].hi;
-}
-
+// in FP32; NaN watch on the new U.
 __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
                            const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc, StepCounters *cnt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = 2 * blockIdx.z + 1;
-    if (i > g.nx || j > g.ny) return;
-    const bool two = k + 1 <= g.nz;
-    DfF F[3] = {U, V, W};
-    const float *const D[3] = {dU, dV, dW};
-    const int h = hix(g, i, j, k), oz = g.sx * g.sy;
-    // Phi at z = k-1 .. k+2 and the x / y neighbours of both cells
-    const df z0 = Phi.at(nbr_p(g, i, j, k, 2, -1)), z1 = Phi.at(h);
-    const df z2 = Phi.at(two ? h + oz : nbr_p(g, i, j, k, 2, 1));
-    const df z3 = two ? Phi.at(nbr_p(g, i, j, k + 1, 2, 1)) : z2;
-    df ppa[3] = {Phi.at(nbr_p(g, i, j, k, 0, 1)), Phi.at(nbr_p(g, i, j, k, 1, 1)), z2};
-    df pma[3] = {Phi.at(nbr_p(g, i, j, k, 0, -1)), Phi.at(nbr_p(g, i, j, k, 1, -1)), z0};
-    df ppb[3] = {z3, z3, z3}, pmb[3] = {z1, z1, z1};
-    if (two) {
-        ppb[0] = Phi.at(nbr_p(g, i, j, k + 1, 0, 1)); ppb[1] = Phi.at(nbr_p(g, i, j, k + 1, 1, 1));
-        pmb[0] = Phi.at(nbr_p(g, i, j, k + 1, 0, -1)); pmb[1] = Phi.at(nbr_p(g, i, j, k + 1, 1, -1));
+    int i, j, k;
+    Pair p;
+    const bool in = pair_of(g, i, j, k, p);
+    float2 unew = make_float2(0.0f, 0.0f);
+    if (in) {
+        const int h = p.h, hb = p.hb, kb = p.two ? k + 1 : k;
+        const DfF F[3] = {U, V, W};
+        const float *const D[3] = {dU, dV, dW};
+        // Phi at z = k-1 .. k+2 and the x / y neighbours of both cells
+        const df z0 = Phi.at(nbr_p(g, i, j, k, 2, -1)), z1 = Phi.at(h);
+        const df z2 = Phi.at(p.two ? hb : nbr_p(g, i, j, k, 2, 1));
+        const df z3 = p.two ? Phi.at(nbr_p(g, i, j, kb, 2, 1)) : z2;
+        const df2 c0 = df2_pack(z1, p.two ? z2 : z1);
+        const df2 pp[3] = {df2_pack(Phi.at(nbr_p(g, i, j, k, 0, 1)), Phi.at(nbr_p(g, i, j, kb, 0, 1))),
+                           df2_pack(Phi.at(nbr_p(g, i, j, k, 1, 1)), Phi.at(nbr_p(g, i, j, kb, 1, 1))),
+                           df2_pack(z2, p.two ? z3 : z2)};
+        const df2 pm[3] = {df2_pack(Phi.at(nbr_p(g, i, j, k, 0, -1)), Phi.at(nbr_p(g, i, j, kb, 0, -1))),
+                           df2_pack(Phi.at(nbr_p(g, i, j, k, 1, -1)), Phi.at(nbr_p(g, i, j, kb, 1, -1))),
+                           df2_pack(z0, p.two ? z1 : z0)};
+        df2 Fv[3];
+        float2 Dv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            Fv[c] = at2(F[c], h, hb);
+            Dv[c] = at2f(D[c], h, hb);
+        }
+        const df2 Pv = at2(P, h, hb);
+        const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
+        df2 nu[3];
+        float2 lap = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const df2 dp = df2_sub(pp[c], c0);
+            const df2 inc = df2_add_f(df2_mul(dp, bcast(df_neg(mc.dtd[c]))), Dv[c]);
+            nu[c] = df2_add(Fv[c], inc);
+            const float2 dpf = add2_rn(sub2_rn(pp[c].hi, c0.hi), sub2_rn(pp[c].lo, c0.lo));
+            const float2 dmf = add2_rn(sub2_rn(c0.hi, pm[c].hi), sub2_rn(c0.lo, pm[c].lo));
+            lap = __ffma2_rn(sub2_rn(dpf, dmf), make_float2(i2[c], i2[c]), lap);
+        }
+        const df2 pn = df2_add_f(df2_add(Pv, c0), __fmul2_rn(make_float2(-mc.pcf, -mc.pcf), lap));
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[c].set(h, df2_x(nu[c]));
+        P.set(h, df2_x(pn));
+        if (p.two) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) F[c].set(hb, df2_y(nu[c]));
+            P.set(hb, df2_y(pn));
+        }
+        unew = make_float2(nu[0].hi.x, p.two ? nu[0].hi.y : 0.0f);
     }
-    float ua = 0.0f, ub = 0.0f;
-    march_cell(F, P, D, h, z1, ppa, pma, mc, ua);
-    if (two) march_cell(F, P, D, h + oz, z2, ppb, pmb, mc, ub);
     // NaN watch on the new U (the reference stops on a NaN velocity,
     // fenep_2d.f90:1974), counted here instead of in a separate pass
     const unsigned act = __activemask();
-    const unsigned nb = __ballot_sync(act, !isfinite(ua) || !isfinite(ub));
+    const unsigned nb = __ballot_sync(act, !isfinite(unew.x) || !isfinite(unew.y));
     if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
 }
 
@@ -1698,35 +1754,29 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     mark(5);
     // Poisson: FP32 solve + one df64 defect correction.  The increments and
     // Phi get no halo pass: their readers wrap / apply the Neumann rule.
-    {
-        dim3 blk(32, 8);
-        k_poisson_rhs_df<<<cell_grid_m(g, blk), blk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
-        count_launch();
-    }
+    const dim3 pblk(32, 8), pgrid((g.nx + pblk.x - 1) / pblk.x, (g.ny + pblk.y - 1) / pblk.y, (g.nz + 1) / 2);
+    k_poisson_rhs_df<<<pgrid, pblk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
+    count_launch();
     if (o.poisson == F8_POISSON_SOR) {
         if ((e = sor_solve_m(d, o, sor_iters, s))) return e;
     } else {
         *sor_iters = -1;
-        const XOutF out{d.Phif, d.Phil, 1};
+        // the first solve writes the FP32 Phi (high parts only); the
+        // correction of the defect solve then sets Phi = Phi + dPhi exactly
+        // as a df64 pair
+        XOutF out{d.Phif, d.Phil, 0};
         if (!g.walls) e = solve_periodic_f(d, d.Rhf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rhf, out, SYS_P, s);
         if (e) return e;
-    }
-    for (int it = 0; o.poisson != F8_POISSON_SOR && it < d.defect_iters; ++it) {
-        dim3 blk(32, 8);
-        k_defect_df<<<cell_grid_m(g, blk), blk, 0, s>>>(Phi, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
-        const XOutF out{d.Phif, d.Phil, 2};
+        k_defect_df<<<pgrid, pblk, 0, s>>>(d.Phif, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
+        out.mode = 2;
         if (!g.walls) e = solve_periodic_f(d, d.Rdf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rdf, out, SYS_P, s);
         if (e) return e;
     }
     mark(6);
-    {
-        dim3 blk(32, 8);
-        const dim3 gm((g.nx + blk.x - 1) / blk.x, (g.ny + blk.y - 1) / blk.y, (g.nz + 1) / 2);
-        k_march_df<<<gm, blk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
-        count_launch();
-    }
+    k_march_df<<<pgrid, pblk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
+    count_launch();
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
     if (gbranch) {
         // join the ghost-row branch (when the Helmholtz branches did not)
