@@ -1143,7 +1143,8 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
         const df2 Pv = at2(P, h, hb);
         const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
         df2 nu[3];
-        float2 lap = make_float2(0.0f, 0.0f);
+        // the FP32 Laplacian of Phi, per lane as the scalar expression
+        float lapx = 0.0f, lapy = 0.0f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const df2 dp = df2_sub(pp[c], c0);
@@ -1151,9 +1152,10 @@ __global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__
             nu[c] = df2_add(Fv[c], inc);
             const float2 dpf = add2_rn(sub2_rn(pp[c].hi, c0.hi), sub2_rn(pp[c].lo, c0.lo));
             const float2 dmf = add2_rn(sub2_rn(c0.hi, pm[c].hi), sub2_rn(c0.lo, pm[c].lo));
-            lap = __ffma2_rn(sub2_rn(dpf, dmf), make_float2(i2[c], i2[c]), lap);
+            lapx += (dpf.x - dmf.x) * i2[c];
+            lapy += (dpf.y - dmf.y) * i2[c];
         }
-        const df2 pn = df2_add_f(df2_add(Pv, c0), __fmul2_rn(make_float2(-mc.pcf, -mc.pcf), lap));
+        const df2 pn = df2_add_f(df2_add(Pv, c0), make_float2(-mc.pcf * lapx, -mc.pcf * lapy));
 #pragma unroll
         for (int c = 0; c < 3; ++c) F[c].set(h, df2_x(nu[c]));
         P.set(h, df2_x(pn));
