@@ -135,10 +135,18 @@ struct f8_ctx {
     // AB2 start or SOR is requested
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     float *cf_base = nullptr;
+    // one device block holds the step counters (cumulative since the load;
+    // a call reports the difference from cnt_prev) followed by the drag slot
+    // that the replayed step writes, so that a one-step call reads both back
+    // with one copy into the same layout on the host (res_host)
+    unsigned char *res_dev = nullptr;
+    unsigned char *res_host = nullptr;
+    size_t res_bytes = 0;
     double *drag_slot = nullptr;
+    StepCounters cnt_prev{};
+    int *load_flags = nullptr;        // device: non-uniform body force components (f8_load)
     // pinned host staging of the per-call results (counters, NaN count, drag),
     // so that their copies are asynchronous and end with one synchronisation
-    StepCounters *cnt_host = nullptr;
     unsigned long long *nan_host = nullptr;
     double *drag_host = nullptr;
     size_t drag_host_n = 0;
@@ -166,20 +174,24 @@ struct f8_ctx {
         *p = static_cast<T *>(q);
         return cudaMemsetAsync(q, 0, std::max<size_t>(n, 1) * sizeof(T), s);
     }
+    void drop_graphs() {
+        for (cudaGraphExec_t &ge : gexec)
+            if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+    }
     void release() {
         for (cudaEvent_t e : evpool) cudaEventDestroy(e);
         evpool.clear();
         if (tot0) cudaEventDestroy(tot0);
         if (tot1) cudaEventDestroy(tot1);
         tot0 = tot1 = nullptr;
-        for (cudaGraphExec_t &ge : gexec)
-            if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+        drop_graphs();
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
-        if (cnt_host) cudaFreeHost(cnt_host);
+        if (res_host) cudaFreeHost(res_host);
+        res_host = nullptr;
         if (nan_host) cudaFreeHost(nan_host);
         if (drag_host) cudaFreeHost(drag_host);
-        cnt_host = nullptr; nan_host = nullptr; drag_host = nullptr; drag_host_n = 0;
+        nan_host = nullptr; drag_host = nullptr; drag_host_n = 0;
         gm.free_all();
         if (stats_probe) cudaFree(stats_probe);   // resized outside the allocation list
         stats_probe = nullptr;
@@ -333,10 +345,14 @@ int setup(f8_ctx *c) {
     API_CUDA(c, c->alloc(&d.red, 4096));
     API_CUDA(c, c->alloc(&d.scal, 64));
     API_CUDA(c, c->alloc(&d.flag, 4));
-    API_CUDA(c, c->alloc(&d.cnt, 1));
-    if (c->cyl.size()) API_CUDA(c, c->alloc(&c->drag_slot, c->cyl.size() * 3));
+    c->res_bytes = sizeof(StepCounters) + c->cyl.size() * 3 * sizeof(double);
+    static_assert(sizeof(StepCounters) % sizeof(double) == 0, "drag slot alignment");
+    API_CUDA(c, c->alloc(&c->res_dev, c->res_bytes));
+    API_CUDA(c, cudaHostAlloc((void **)&c->res_host, c->res_bytes, cudaHostAllocDefault));
+    d.cnt = reinterpret_cast<StepCounters *>(c->res_dev);
+    if (c->cyl.size()) c->drag_slot = reinterpret_cast<double *>(c->res_dev + sizeof(StepCounters));
+    API_CUDA(c, c->alloc(&c->load_flags, 3));
     API_CUDA(c, c->alloc(&c->nan_dev, 1));
-    API_CUDA(c, cudaHostAlloc((void **)&c->cnt_host, sizeof(StepCounters), cudaHostAllocDefault));
     API_CUDA(c, cudaHostAlloc((void **)&c->nan_host, sizeof(unsigned long long), cudaHostAllocDefault));
     API_CUDA(c, c->alloc(&c->diag_part, std::max(diag_partials(), turb_partials(0))));
     if (g.dim == 3) {
@@ -631,28 +647,40 @@ int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
         const double *src[9] = {in->ax0, in->ay0, in->az0, in->tx0, in->ty0, in->tz0, in->fx, in->fy, in->fz};
         float *dst[9] = {d.A0f[0], d.A0f[1], d.A0f[2], d.T0f[0], d.T0f[1], d.T0f[2], d.Ff[0], d.Ff[1], d.Ff[2]};
         double *tmp = c->scratch_aos;  // ncomp*cs >= ni doubles
+        // the force conversions also flag a component that is not uniform
+        API_CUDA(c, cudaMemsetAsync(c->load_flags, 0, 3 * sizeof(int), c->s));
         for (int q = 0; q < 9; ++q) {
             if (src[q]) {
                 API_CUDA(c, cudaMemcpyAsync(tmp, src[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
-                API_CUDA(c, d2f(tmp, dst[q], (int)ni, c->s));
+                API_CUDA(c, d2f(tmp, dst[q], (int)ni, c->s, q >= 6 ? c->load_flags + (q - 6) : nullptr));
             } else {
                 API_CUDA(c, cudaMemsetAsync(dst[q], 0, ni * sizeof(float), c->s));
             }
         }
-        // a spatially uniform body force component (the channel's driving
-        // force) is passed to the momentum kernel as a constant
-        for (int q = 0; q < 3; ++q) {
-            const double *f = src[6 + q];
-            bool uni = true;
-            const double f0 = f ? f[0] : 0.0;
-            if (f)
-                for (size_t n = 1; n < ni && uni; ++n) uni = f[n] == f0;
-            d.Funi[q] = uni ? 1 : 0;
-            d.Fval[q] = (float)f0;
-        }
         API_CUDA(c, bc_all_state_mixed(d, c->s));
     }
+    API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
+    int varies[3] = {0, 0, 0};
+    if (c->precision == F8_MIXED)
+        API_CUDA(c, cudaMemcpyAsync(varies, c->load_flags, sizeof(varies), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
+    c->cnt_prev = StepCounters{};
+    if (c->precision == F8_MIXED) {
+        // a spatially uniform body force component (the channel's driving
+        // force) is passed to the momentum kernel as a constant.  The
+        // replayed step graphs hold those kernel arguments, so a load that
+        // changes them drops the graphs (recaptured at the next step).
+        const double *f[3] = {in->fx, in->fy, in->fz};
+        bool force_changed = false;
+        for (int q = 0; q < 3; ++q) {
+            const int u = f[q] && varies[q] ? 0 : 1;
+            const float v = f[q] ? (float)f[q][0] : 0.0f;
+            if (u != d.Funi[q] || v != d.Fval[q]) force_changed = true;
+            d.Funi[q] = u;
+            d.Fval[q] = v;
+        }
+        if (force_changed) c->drop_graphs();
+    }
     c->step = step0;
     c->step0 = step0;
     c->loaded = true;
@@ -667,7 +695,9 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     if (int st = ensure_drag(c, nsteps)) return st;
     Dev &d = c->d;
     const int ncyl = (int)c->cyl.size();
-    API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
+    // a one-step call of the replayed step reads its drag from the result
+    // block together with the counters (one copy)
+    bool drag_in_slot = false;
     // the mixed step counts non-finite velocities in its counters instead
     if (c->precision != F8_MIXED) API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
     const size_t per = NSTAGE + 1;
@@ -720,8 +750,11 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
             e = cudaGraphLaunch(c->gexec[p], c->s);
             if (o.polymer) std::swap(d.Cf, d.Cnf);
             g_kernel_launches += c->graph_launches;
-            if (e == cudaSuccess && dg)
-                e = cudaMemcpyAsync(dg, c->drag_slot, (size_t)ncyl * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->s);
+            if (e == cudaSuccess && dg) {
+                if (nsteps == 1) drag_in_slot = true;
+                else e = cudaMemcpyAsync(dg, c->drag_slot, (size_t)ncyl * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                         c->s);
+            }
         } else {
             e = mixed ? step_mixed(d, o, dg, &sor_iters, c->s) : step_fp64(d, o, dg, &sor_iters, c->s);
         }
@@ -741,15 +774,23 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     c->step_launches += g_kernel_launches.load() - launches0;
     const size_t ndrag = (size_t)nsteps * ncyl * 3;
     *c->nan_host = 0;
-    API_CUDA(c, cudaMemcpyAsync(c->cnt_host, d.cnt, sizeof(StepCounters), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaMemcpyAsync(c->res_host, c->res_dev, drag_in_slot ? c->res_bytes : sizeof(StepCounters),
+                                cudaMemcpyDeviceToHost, c->s));
     if (c->precision != F8_MIXED)
         API_CUDA(c, cudaMemcpyAsync(c->nan_host, c->nan_dev, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
-    if (drag && ncyl)
+    if (drag && ncyl && !drag_in_slot)
         API_CUDA(c, cudaMemcpyAsync(c->drag_host, c->drag_dev, ndrag * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
-    const StepCounters cnt = *c->cnt_host;
+    StepCounters now;
+    std::memcpy(&now, c->res_host, sizeof(now));
+    const StepCounters cnt{now.newton_iters - c->cnt_prev.newton_iters,
+                           now.newton_unconverged - c->cnt_prev.newton_unconverged,
+                           now.nan_cells - c->cnt_prev.nan_cells};
+    c->cnt_prev = now;
     const unsigned long long nan = *c->nan_host;
-    if (drag && ncyl) std::memcpy(drag, c->drag_host, ndrag * sizeof(double));
+    if (drag && ncyl)
+        std::memcpy(drag, drag_in_slot ? c->res_host + sizeof(StepCounters) : (const unsigned char *)c->drag_host,
+                    ndrag * sizeof(double));
     {
         float ms = 0.f;
         API_CUDA(c, cudaEventElapsedTime(&ms, c->tot0, c->tot1));
@@ -967,6 +1008,7 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
             for (int l = 0; l < ncyl; ++l) w[((size_t)n * ncyl + l) * 3] = 1.0 / nsteps;
     if (nw) API_CUDA(c, cudaMemcpyAsync(G.dw, w.data(), nw * sizeof(double), cudaMemcpyHostToDevice, c->s));
     API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
+    c->cnt_prev = StepCounters{};   // f8_step reports differences from this
     API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
     const int step0 = c->step;
     // forward: checkpoints at the segment starts, the tape of the last segment
@@ -1061,6 +1103,7 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
     }
     if (drag && nw) std::copy(hd.begin(), hd.begin() + nw, drag);
     if (dJ_dparams) std::copy(gr.begin(), gr.end(), dJ_dparams);
+    c->cnt_prev = cnt;
     c->last_newton_iters = (long long)cnt.newton_iters;
     c->last_newton_unconv = (long long)cnt.newton_unconverged;
     if (nan) return F8_ERR_NAN;

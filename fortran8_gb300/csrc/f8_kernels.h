@@ -175,7 +175,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
 cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s);
 cudaError_t mixed_state_to_fp64(Dev &d, cudaStream_t s);
 cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cudaStream_t s);
-cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s);
+cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s, int *varies = nullptr);
 cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s);
 cudaError_t aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs, cudaStream_t s);
 cudaError_t soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs, cudaStream_t s);

@@ -1531,8 +1531,19 @@ cudaError_t init_kernels_mixed() {
     return cudaSuccess;
 }
 
-cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s) {
-    k_convert<double, float><<<(n + 255) / 256, 256, 0, s>>>(a, b, n); count_launch();
+// FP64 -> FP32; with `varies`, also set *varies = 1 when some a[q] != a[0]
+__global__ void k_convert_check(const double *__restrict__ a, float *__restrict__ b, int n, int *varies) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const double v = a[q];
+    b[q] = (float)v;
+    if (v != a[0]) *varies = 1;
+}
+
+cudaError_t d2f(const double *a, float *b, int n, cudaStream_t s, int *varies) {
+    if (varies) k_convert_check<<<(n + 255) / 256, 256, 0, s>>>(a, b, n, varies);
+    else k_convert<double, float><<<(n + 255) / 256, 256, 0, s>>>(a, b, n);
+    count_launch();
     return cudaGetLastError();
 }
 cudaError_t f2d(const float *a, double *b, int n, cudaStream_t s) {

@@ -159,3 +159,32 @@ def test_graph_replay_is_bit_identical(gpu):
     for f in ("u", "v", "w", "p", "c"):
         np.testing.assert_array_equal(sa[f], sb[f])
     assert la == lb   # replayed kernels are counted as launches
+
+
+@pytest.mark.parametrize("second", ["uniform", "varying"])
+def test_reload_with_another_force_recaptures_the_graphs(gpu, second):
+    """A uniform body force is a kernel argument of the replayed step graphs:
+    reloading a context with another force (another uniform value, or a
+    varying field) gives the same steps as a fresh context."""
+    w = configs.scaled(configs.c3_channel(), 32, 16, 16)
+    st_a = configs.initial_state(w)
+    st_b = st_a.copy()
+    if second == "uniform":
+        st_b.arrays["fx"] = np.full_like(st_a.arrays["fx"], 2.0 * st_a.arrays["fx"].flat[0])
+    else:
+        fx = st_a.arrays["fx"].copy()
+        fx[..., : fx.shape[-1] // 2] *= 1.5
+        st_b.arrays["fx"] = fx
+    with Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED) as s:
+        s.load(st_a)
+        s.step(4)                 # graphs captured with the first force
+        s.load(st_b)
+        _, d_reload = s.step(4)
+        out_reload = s.store()
+    with Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED) as s:
+        s.load(st_b)
+        _, d_fresh = s.step(4)
+        out_fresh = s.store()
+    np.testing.assert_array_equal(d_reload, d_fresh)
+    for f in ("u", "v", "w", "p", "c"):
+        np.testing.assert_array_equal(out_reload[f], out_fresh[f])
