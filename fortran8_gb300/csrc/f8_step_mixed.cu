@@ -316,10 +316,22 @@ __device__ __forceinline__ float2 lam_min2(float2 m, float2 b00, float2 b11, flo
     return make_float2(okx ? lam.x : -100.0f, oky ? lam.y : -100.0f);
 }
 
-// candidate faces (fenep.f90:179-184) as weights of (C_{m-1}, C_m, C_{m+1});
-// index 4 is the cell value (the Cstar stencil coefficients below)
-__constant__ float c_fp_w[5][3] = {{0, 1, 0}, {0, 1.5f, -0.5f}, {0.5f, 0.5f, 0}, {0.25f, 1, -0.25f}, {0, 1, 0}};
-__constant__ float c_fn_w[5][3] = {{0, 1, 0}, {0, 0.5f, 0.5f}, {-0.5f, 1.5f, 0}, {-0.25f, 1, 0.25f}, {0, 1, 0}};
+// candidate faces (fenep.f90:179-184) as weights (w0, w1, w2) of
+// (C_{m-1}, C_m, C_{m+1}); candidate c = 1, 2, 3, and 4 for the cell value
+// (the Cstar stencil coefficients below).  The plus face of c is
+// (p0, 1 - p0 - p2, p2) with (p0, p2) = (0, -1/2), (1/2, 0), (1/4, -1/4),
+// (0, 0); the minus face is its mirror (-p0, 1 + p0 + p2, -p2).  The weights
+// are exact in FP32 and are formed with selects: the candidate differs from
+// thread to thread, and a constant-memory table read with per-thread indices
+// is serialised.
+struct FaceW {
+    float p0, p1, p2, n0, n1, n2;
+};
+__device__ __forceinline__ FaceW face_w(int c) {
+    const float p0 = c == 2 ? 0.5f : (c == 3 ? 0.25f : 0.0f);
+    const float p2 = c == 1 ? -0.5f : (c == 3 ? -0.25f : 0.0f);
+    return FaceW{p0, 1.0f - p0 - p2, p2, -p0, 1.0f + p0 + p2, -p2};
+}
 
 // candidate choice of one direction (maxloc over the three candidates' least
 // eigenvalues and 0, first maximum, NaN ignored), returns the code 0..3
@@ -573,12 +585,12 @@ __device__ inline Lyap9 vel_grad_f(const float *__restrict__ U, const float *__r
 // contributes its cell value (gm / gp).
 __device__ inline void dir_coef(float s_pm, float s_pp, float s_nm, float s_np, int is, int cm, int cp, bool gm,
                                 bool gp, float &km2, float &km1, float &k0, float &kp1, float &kp2) {
-    km2 = gm ? 0.0f : s_nm * c_fn_w[cm][0];
-    km1 = s_pm * c_fp_w[is][0] + s_np * c_fn_w[is][0] + (gm ? s_nm : s_nm * c_fn_w[cm][1]);
-    k0 += s_pm * c_fp_w[is][1] + s_np * c_fn_w[is][1] + (gm ? 0.0f : s_nm * c_fn_w[cm][2])
-          + (gp ? 0.0f : s_pp * c_fp_w[cp][0]);
-    kp1 = s_pm * c_fp_w[is][2] + s_np * c_fn_w[is][2] + (gp ? s_pp : s_pp * c_fp_w[cp][1]);
-    kp2 = gp ? 0.0f : s_pp * c_fp_w[cp][2];
+    const FaceW ws = face_w(is), wm = face_w(cm), wp = face_w(cp);
+    km2 = gm ? 0.0f : s_nm * wm.n0;
+    km1 = s_pm * ws.p0 + s_np * ws.n0 + (gm ? s_nm : s_nm * wm.n1);
+    k0 += s_pm * ws.p1 + s_np * ws.n1 + (gm ? 0.0f : s_nm * wm.n2) + (gp ? 0.0f : s_pp * wp.p0);
+    kp1 = s_pm * ws.p2 + s_np * ws.n2 + (gp ? s_pp : s_pp * wp.p1);
+    kp2 = gp ? 0.0f : s_pp * wp.p2;
 }
 
 __global__ void __launch_bounds__(128) k_update3_f(const float *__restrict__ C, float *__restrict__ Cn,
