@@ -1124,7 +1124,7 @@ __global__ void k_defect_df(const float *__restrict__ Phi, const float *__restri
 // U^{n+1} = U^n + (dU - dt/dX (Phi_{+1} - Phi)) in df64, and
 // P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
 // in FP32; NaN watch on the new U.
-__global__ void k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
+__global__ void __launch_bounds__(256, 4) k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
                            const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc, StepCounters *cnt) {
     int i, j, k;
     Pair p;
