@@ -883,15 +883,23 @@ __global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixCo
     const float id[3] = {ix, iy, iz};
     const float ph0 = a.Ph[h], pl0 = a.Pl[h];
     const float dt = (float)a.dt;
+    // every load of the three components before the first store (the
+    // history arrays are read and written in place)
+    float a0[3], t0[3], php[3], plp[3], fb[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float a0 = a.ab2_first ? A[c] : a.A0[c][o];
-        const float t0 = a.ab2_first ? T[c] : a.T0[c][o];
+        a0[c] = a.ab2_first ? A[c] : a.A0[c][o];
+        t0[c] = a.ab2_first ? T[c] : a.T0[c][o];
+        php[c] = a.Ph[hp[c]];
+        plp[c] = a.Pl[hp[c]];
+        fb[c] = a.F[c] ? a.F[c][o] : a.Fu[c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
         // pressure difference from the df64 pair: the hi difference is
         // correctly rounded, the lo difference carries the rest
-        const float gp = -((a.Ph[hp[c]] - ph0) + (a.Pl[hp[c]] - pl0)) * id[c];
-        const float fb = a.F[c] ? a.F[c][o] : a.Fu[c];
-        const float r = gp + 0.5f * (3.0f * A[c] - a0) + B[c] + 0.5f * (T[c] + t0) + fb;
+        const float gp = -((php[c] - ph0) + (plp[c] - pl0)) * id[c];
+        const float r = gp + 0.5f * (3.0f * A[c] - a0[c]) + B[c] + 0.5f * (T[c] + t0[c]) + fb[c];
         a.Q[c][o] = dt * r;
         a.A0[c][o] = A[c];
         a.T0[c][o] = T[c];
