@@ -120,17 +120,22 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     if (!halo_cell_m(g, t, i, j, k)) return;
     const int h = hix(g, i, j, k);
     const int ii = wrapx(g, i), kk = wrapz(g, k);
+    // the source cells: a periodic image, or the two rows of the wall
+    // extrapolation (weights 2 and -1)
+    int s1, s2 = -1;
+    if (j >= 1 && j <= g.ny) s1 = hix(g, ii, j, kk);
+    else if (!g.walls) s1 = hix(g, ii, wrapy(g, j), kk);
+    else if (j == 0) { s1 = hix(g, ii, 1, kk); s2 = hix(g, ii, 2, kk); }
+    else { s1 = hix(g, ii, g.ny, kk); s2 = hix(g, ii, g.ny - 1, kk); }
+    // every component's sources before the first store
     float x[6];
+#pragma unroll
     for (int m = 0; m < 6; ++m) {
         const float *A = C + (size_t)m * cs;
-        float v;
-        if (j >= 1 && j <= g.ny) v = A[hix(g, ii, j, kk)];
-        else if (!g.walls) v = A[hix(g, ii, wrapy(g, j), kk)];
-        else if (j == 0) v = 2.0f * A[hix(g, ii, 1, kk)] - A[hix(g, ii, 2, kk)];
-        else v = 2.0f * A[hix(g, ii, g.ny, kk)] - A[hix(g, ii, g.ny - 1, kk)];
-        x[m] = v;
-        C[(size_t)m * cs + h] = v;
+        x[m] = s2 < 0 ? A[s1] : 2.0f * A[s1] - A[s2];
     }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
@@ -144,10 +149,10 @@ __global__ void k_bc_c_pet_xz_f(float *C, float *fpet, Geo g, int cs, double lp2
     if ((j == 0 || j == g.sy - 1) && i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) return;   // updated ghost cell
     const int h = hix(g, i, j, k), src = hix(g, wrapx(g, i), j, wrapz(g, k));
     float x[6];
-    for (int m = 0; m < 6; ++m) {
-        x[m] = C[(size_t)m * cs + src];
-        C[(size_t)m * cs + h] = x[m];
-    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) x[m] = C[(size_t)m * cs + src];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
@@ -164,10 +169,11 @@ __global__ void k_extrap_ghost_f(float *C, float *fpet, Geo g, int cs, double lp
     float x[6];
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
-        float *A = C + (size_t)m * cs;
+        const float *A = C + (size_t)m * cs;
         x[m] = 2.0f * A[h1] - A[h2];
-        A[h] = x[m];
     }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
     fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
 }
 
@@ -207,11 +213,17 @@ __global__ void k_bc_set(BcSet b, Geo g) {
     int i, j, k;
     if (halo_cell_m(g, t, i, j, k)) {
         const int h = hix(g, i, j, k);
-        for (int f = 0; f < b.n; ++f) {
-            const df v = halo_df(g, b.hi[f], b.lo[f], b.kind[f], i, j, k, b.uw2);
-            b.hi[f][h] = v.hi;
-            if (b.lo[f]) b.lo[f][h] = v.lo;
-        }
+        // every field's source value before the first store
+        df v[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+            if (f < b.n) v[f] = halo_df(g, b.hi[f], b.lo[f], b.kind[f], i, j, k, b.uw2);
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+            if (f < b.n) {
+                b.hi[f][h] = v[f].hi;
+                if (b.lo[f]) b.lo[f][h] = v[f].lo;
+            }
         return;
     }
     if (g.walls) {  // V on the upper wall face
@@ -219,8 +231,9 @@ __global__ void k_bc_set(BcSet b, Geo g) {
         if (t >= 0 && t < (long)g.nx * g.nz) {
             i = 1 + (int)(t % g.nx); k = 1 + (int)(t / g.nx);
             const int h = hix(g, i, g.ny, k);
-            for (int f = 0; f < b.n; ++f)
-                if (b.kind[f] == BC_V) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+                if (f < b.n && b.kind[f] == BC_V) {
                     b.hi[f][h] = 0.0f;
                     if (b.lo[f]) b.lo[f][h] = 0.0f;
                 }
@@ -1282,15 +1295,29 @@ __global__ void k_convert(const A *a, B *b, int n) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) b[q] = B(a[q]);
 }
-__global__ void k_aos_to_soa_f(const double *aos, float *soa, int ncomp, int cs) {
+// C component-fastest (FP64) <-> one FP32 array per component, ncomp <= 6;
+// all loads of a cell before its stores
+__global__ void k_aos_to_soa_f(const double *__restrict__ aos, float *__restrict__ soa, int ncomp, int cs) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= cs) return;
-    for (int m = 0; m < ncomp; ++m) soa[(size_t)m * cs + h] = (float)aos[(size_t)ncomp * h + m];
+    float v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+        if (m < ncomp) v[m] = (float)aos[(size_t)ncomp * h + m];
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+        if (m < ncomp) soa[(size_t)m * cs + h] = v[m];
 }
-__global__ void k_soa_to_aos_f(const float *soa, double *aos, int ncomp, int cs) {
+__global__ void k_soa_to_aos_f(const float *__restrict__ soa, double *__restrict__ aos, int ncomp, int cs) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= cs) return;
-    for (int m = 0; m < ncomp; ++m) aos[(size_t)ncomp * h + m] = (double)soa[(size_t)m * cs + h];
+    double v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+        if (m < ncomp) v[m] = (double)soa[(size_t)m * cs + h];
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+        if (m < ncomp) aos[(size_t)ncomp * h + m] = v[m];
 }
 
 inline dim3 cell_grid_m(const Geo &g, dim3 blk) {
