@@ -417,6 +417,7 @@ __device__ __forceinline__ int brev_elem(int lane, int s) {
 }
 
 constexpr int XW_WARPS = 8;   // warps per block of the x passes
+constexpr int XW_RB = 16;     // rows per block of the x passes (a constant: the tile indexing divides by it)
 
 inline size_t xw_smem(int nx, int rb) {
     const int nh = nx / 2;
@@ -425,9 +426,8 @@ inline size_t xw_smem(int nx, int rb) {
 
 template <int E, typename TS>
 __global__ void __launch_bounds__(32 * XW_WARPS) k_xfwd_w(const TS *__restrict__ src, float2 *__restrict__ S, int ny,
-                                                         int nz, int rb, int lj, int joff,
-                                                         const float2 *__restrict__ twx) {
-    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v;
+                                                         int nz, int lj, int joff, const float2 *__restrict__ twx) {
+    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v, rb = XW_RB;
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float2 *tws = reinterpret_cast<float2 *>(smem_raw);
@@ -466,9 +466,9 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xfwd_w(const TS *__restrict__
 
 template <int E, typename Out>
 __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restrict__ S, Out out,
-                                                         int nrow, int jlo, int nz, int rb, int lj, int joff2, int sx,
+                                                         int nrow, int jlo, int nz, int lj, int joff2, int sx,
                                                          int sy, const float2 *__restrict__ twx) {
-    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v;
+    constexpr int N = 32 * E, NH = N / 2, LG = LgE<E>::v, rb = XW_RB;
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float2 *tws = reinterpret_cast<float2 *>(smem_raw);

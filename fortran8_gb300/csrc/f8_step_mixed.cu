@@ -1395,8 +1395,6 @@ inline size_t x_smem(int nx, int rb) { return (size_t)(rb / 2) * 2 * nx * sizeof
 inline int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
 
 // warp-per-row-pair x passes for NX = 32 .. 512; false when NX has no instance
-constexpr int XW_RB = 16;
-
 template <typename TS>
 bool xfwd_warp(const Dev &d, const TS *src, float2 *S, int ny, int lj, int joff, cudaStream_t s) {
     const Geo &g = d.g;
@@ -1404,11 +1402,11 @@ bool xfwd_warp(const Dev &d, const TS *src, float2 *S, int ny, int lj, int joff,
     const size_t sm = xw_smem(g.nx, XW_RB);
     const int thr = 32 * XW_WARPS;
     switch (g.nx) {
-    case 32: k_xfwd_w<1, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
-    case 64: k_xfwd_w<2, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
-    case 128: k_xfwd_w<4, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
-    case 256: k_xfwd_w<8, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
-    case 512: k_xfwd_w<16, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, XW_RB, lj, joff, d.twx2); break;
+    case 32: k_xfwd_w<1, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, lj, joff, d.twx2); break;
+    case 64: k_xfwd_w<2, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, lj, joff, d.twx2); break;
+    case 128: k_xfwd_w<4, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, lj, joff, d.twx2); break;
+    case 256: k_xfwd_w<8, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, lj, joff, d.twx2); break;
+    case 512: k_xfwd_w<16, TS><<<grid, thr, sm, s>>>(src, S, ny, g.nz, lj, joff, d.twx2); break;
     default: return false;
     }
     count_launch();
@@ -1421,11 +1419,11 @@ bool xinv_warp(const Dev &d, const float2 *S, XOutF out, int nrow, int jlo, int 
     const size_t sm = xw_smem(g.nx, XW_RB);
     const int thr = 32 * XW_WARPS;
     switch (g.nx) {
-    case 32: k_xinv_w<1, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 64: k_xinv_w<2, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 128: k_xinv_w<4, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 256: k_xinv_w<8, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
-    case 512: k_xinv_w<16, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, XW_RB, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 32: k_xinv_w<1, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 64: k_xinv_w<2, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 128: k_xinv_w<4, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 256: k_xinv_w<8, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, lj, joff2, g.sx, g.sy, d.twx2); break;
+    case 512: k_xinv_w<16, XOutF><<<grid, thr, sm, s>>>(S, out, nrow, jlo, g.nz, lj, joff2, g.sx, g.sy, d.twx2); break;
     default: return false;
     }
     count_launch();
