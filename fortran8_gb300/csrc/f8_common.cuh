@@ -69,6 +69,44 @@ inline void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_re
 __host__ __device__ inline int wall_rows_per_cta(int lj, int cl) { return (lj + cl - 1) / cl; }
 __host__ __device__ inline int wall_rd_stride(int r, int t) { return r + (((t - r) % 32) + 32) % 32; }
 
+// Halo cells of a field with one halo layer, numbered face by face.
+__host__ __device__ inline long halo_count(const Geo &g) {
+    return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
+}
+
+// halo cell number t -> (i, j, k): the two x faces (all j, k), the two y
+// faces (interior i, all k), the two z faces (interior i, j).  32-bit index
+// arithmetic (the grid has fewer than 2^31 cells), one division per cell.
+__device__ inline bool halo_cell(const Geo &g, long tl, int &i, int &j, int &k) {
+    if (tl < 0 || tl >= halo_count(g)) return false;
+    int t = (int)tl;
+    int plane = g.sy * g.sz;
+    if (t < 2 * plane) {
+        const bool hi = t >= plane;
+        const int r = hi ? t - plane : t;
+        i = hi ? g.sx - 1 : 0;
+        k = r / g.sy; j = r - k * g.sy;
+        return true;
+    }
+    t -= 2 * plane;
+    plane = g.nx * g.sz;
+    if (t < 2 * plane) {
+        const bool hi = t >= plane;
+        const int r = hi ? t - plane : t;
+        j = hi ? g.sy - 1 : 0;
+        k = r / g.nx; i = 1 + r - k * g.nx;
+        return true;
+    }
+    t -= 2 * plane;
+    plane = g.nx * g.ny;
+    const bool hi = t >= plane;
+    const int r = hi ? t - plane : t;
+    k = hi ? g.sz - 1 : 0;
+    j = r / g.nx; i = 1 + r - j * g.nx;
+    j += 1;
+    return true;
+}
+
 __host__ __device__ inline size_t wall_plane_smem(int ny, int nz, int cl) {
     const int r = wall_rows_per_cta(ny + 2, cl);
     return (size_t)8 * (r | 1) * nz + (size_t)4 * wall_rd_stride(r, 1024 / nz) * nz + (size_t)(nz / 2) * 8

@@ -23,37 +23,6 @@ constexpr double PI_D = 3.141592653589793238462643383279502884;
 // periodic directions, which is what the reference's plane-by-plane copies
 // produce.
 
-__host__ __device__ inline long halo_count(const Geo &g) {
-    return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
-}
-
-__device__ inline bool halo_cell(const Geo &g, long t, int &i, int &j, int &k) {
-    long nf = 2L * g.sy * g.sz;
-    if (t < nf) {
-        long r = t % ((long)g.sy * g.sz);
-        i = (t / ((long)g.sy * g.sz)) ? g.sx - 1 : 0;
-        j = (int)(r % g.sy); k = (int)(r / g.sy);
-        return true;
-    }
-    t -= nf;
-    nf = 2L * g.nx * g.sz;
-    if (t < nf) {
-        long r = t % ((long)g.nx * g.sz);
-        j = (t / ((long)g.nx * g.sz)) ? g.sy - 1 : 0;
-        i = 1 + (int)(r % g.nx); k = (int)(r / g.nx);
-        return true;
-    }
-    t -= nf;
-    nf = 2L * g.nx * g.ny;
-    if (t < nf) {
-        long r = t % ((long)g.nx * g.ny);
-        k = (t / ((long)g.nx * g.ny)) ? g.sz - 1 : 0;
-        i = 1 + (int)(r % g.nx); j = 1 + (int)(r / g.nx);
-        return true;
-    }
-    return false;
-}
-
 __device__ inline double halo_value(const Geo &g, const double *A, int kind, int i, int j, int k) {
     const int ii = wrapx(g, i), kk = wrapz(g, k);
     if (j >= 1 && j <= g.ny) {

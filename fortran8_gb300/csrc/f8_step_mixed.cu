@@ -72,37 +72,6 @@ MixConst make_const(const Geo &g, const Phys &ph) {
     return c;
 }
 
-__host__ __device__ inline long halo_count_m(const Geo &g) {
-    return 2L * g.sy * g.sz + 2L * g.nx * g.sz + 2L * g.nx * g.ny;
-}
-
-__device__ inline bool halo_cell_m(const Geo &g, long t, int &i, int &j, int &k) {
-    long nf = 2L * g.sy * g.sz;
-    if (t < nf) {
-        long r = t % ((long)g.sy * g.sz);
-        i = (t / ((long)g.sy * g.sz)) ? g.sx - 1 : 0;
-        j = (int)(r % g.sy); k = (int)(r / g.sy);
-        return true;
-    }
-    t -= nf;
-    nf = 2L * g.nx * g.sz;
-    if (t < nf) {
-        long r = t % ((long)g.nx * g.sz);
-        j = (t / ((long)g.nx * g.sz)) ? g.sy - 1 : 0;
-        i = 1 + (int)(r % g.nx); k = (int)(r / g.nx);
-        return true;
-    }
-    t -= nf;
-    nf = 2L * g.nx * g.ny;
-    if (t < nf) {
-        long r = t % ((long)g.nx * g.ny);
-        k = (t / ((long)g.nx * g.ny)) ? g.sz - 1 : 0;
-        i = 1 + (int)(r % g.nx); j = 1 + (int)(r / g.nx);
-        return true;
-    }
-    return false;
-}
-
 // Peterlin factor (fenep.f90:510-515) from FP32 components: FP32 normally, FP64
 // when the denominator L^2 - tr C is within 1% of L^2 of the limit.
 __device__ inline float peterlin_f(float x0, float x3, float x5, float lp2f, double lp2) {
@@ -117,7 +86,7 @@ __device__ inline float peterlin_f(float x0, float x3, float x5, float lp2f, dou
 __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
-    if (!halo_cell_m(g, t, i, j, k)) return;
+    if (!halo_cell(g, t, i, j, k)) return;
     const int h = hix(g, i, j, k);
     const int ii = wrapx(g, i), kk = wrapz(g, k);
     // the source cells: a periodic image, or the two rows of the wall
@@ -145,7 +114,7 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
 __global__ void k_bc_c_pet_xz_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
-    if (!halo_cell_m(g, t, i, j, k)) return;
+    if (!halo_cell(g, t, i, j, k)) return;
     if ((j == 0 || j == g.sy - 1) && i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) return;   // updated ghost cell
     const int h = hix(g, i, j, k), src = hix(g, wrapx(g, i), j, wrapz(g, k));
     float x[6];
@@ -211,7 +180,7 @@ struct BcSet {
 __global__ void k_bc_set(BcSet b, Geo g) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
-    if (halo_cell_m(g, t, i, j, k)) {
+    if (halo_cell(g, t, i, j, k)) {
         const int h = hix(g, i, j, k);
         // every field's source value before the first store
         df v[4];
@@ -227,7 +196,7 @@ __global__ void k_bc_set(BcSet b, Geo g) {
         return;
     }
     if (g.walls) {  // V on the upper wall face
-        t -= halo_count_m(g);
+        t -= halo_count(g);
         if (t >= 0 && t < (long)g.nx * g.nz) {
             i = 1 + (int)(t % g.nx); k = 1 + (int)(t / g.nx);
             const int h = hix(g, i, g.ny, k);
@@ -1618,7 +1587,7 @@ BcSet state_bc_set(const Dev &d) {
 }
 
 cudaError_t launch_bc_set(const BcSet &b, const Geo &g, cudaStream_t s) {
-    const long n = halo_count_m(g) + (g.walls ? (long)g.nx * g.nz : 0);
+    const long n = halo_count(g) + (g.walls ? (long)g.nx * g.nz : 0);
     k_bc_set<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, g); count_launch();
     return cudaGetLastError();
 }
@@ -1638,7 +1607,7 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     F8_CUDA_RET(bc_field(d.V, d.g, BC_V, s));
     F8_CUDA_RET(bc_field(d.W, d.g, BC_W, s));
     F8_CUDA_RET(bc_field(d.P, d.g, BC_P, s));
-    long n = halo_count_m(d.g);
+    long n = halo_count(d.g);
     k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
     k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
     const double *src[5] = {d.U, d.V, d.W, d.P, d.Phi};
@@ -1704,7 +1673,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
                                                         d.cs, d.fixlist, d.fixcnt, d.cnt); count_launch();
         k_newton_fix_f<<<2 * 152, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
                                                d.fixcnt, d.cnt); count_launch();
-        long n = halo_count_m(g);
+        long n = halo_count(g);
         if (g.walls) {
             if (gbranch) F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_g[2], 0));
             std::swap(d.Cf, d.Cnf);
