@@ -926,24 +926,36 @@ struct IbmArgsF {
     float dtf;                       // dt
 };
 
-__global__ void k_ibm_interp_f(IbmArgsF a, Geo g) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+// One marker per threadIdx.x and one z plane of its 3 x 3 x 3 stencil per
+// threadIdx.y (blocks of 32 x 3): each thread sums 9 points in df64, and the
+// three plane sums are added in plane order.
+__global__ void __launch_bounds__(96) k_ibm_interp_f(IbmArgsF a, Geo g) {
+    __shared__ df part[3][32];
+    const int m = blockIdx.x * 32 + threadIdx.x;
+    const int dk = threadIdx.y;
     const int n = blockIdx.y + 1;
     const int comp = blockIdx.z;
-    if (m >= a.nm) return;
-    const int i0 = a.i0[comp][m], j0 = a.j0[comp][m];
-    const float *wx = a.wx[comp] + 3 * m, *wy = a.wy[comp] + 3 * m;
     df ub{0.0f, 0.0f};
-    for (int dk = 0; dk < 3; ++dk) {
+    if (m < a.nm) {
+        const int i0 = a.i0[comp][m], j0 = a.j0[comp][m];
+        const float *wx = a.wx[comp] + 3 * m, *wy = a.wy[comp] + 3 * m;
         const int k = n - 1 + dk;
+        const float wz = a.wz[comp][dk];
+#pragma unroll
         for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
             for (int di = 0; di < 3; ++di) {
-                const float w = wx[di] * wy[dj] * a.wz[comp][dk];
+                const float w = wx[di] * wy[dj] * wz;
                 ub = df_add(ub, df_mul_f(ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2), w));
             }
     }
-    const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
-    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ((double)ub.hi + (double)ub.lo)) * a.idt;
+    part[dk][threadIdx.x] = ub;
+    __syncthreads();
+    if (dk == 0 && m < a.nm) {
+        const df s3 = df_add(df_add(part[0][threadIdx.x], part[1][threadIdx.x]), part[2][threadIdx.x]);
+        const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
+        a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ((double)s3.hi + (double)s3.lo)) * a.idt;
+    }
 }
 
 // the spread force enters Q = dt (R + f), an FP32 field, so it is summed in FP32
@@ -1739,8 +1751,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         a.uw2 = df_from_d(2.0 * g.uwall);
         a.idt = 1.0 / g.dt;
         a.dtf = (float)g.dt;
-        dim3 gi((d.nm + 127) / 128, g.nz, 3);
-        k_ibm_interp_f<<<gi, 128, 0, s>>>(a, g); count_launch();
+        dim3 gi((d.nm + 31) / 32, g.nz, 3);
+        k_ibm_interp_f<<<gi, dim3(32, 3), 0, s>>>(a, g); count_launch();
         int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
         if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
         if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
