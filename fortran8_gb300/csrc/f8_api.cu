@@ -532,6 +532,19 @@ int setup(f8_ctx *c) {
                 }
                 if (int st = upload_f(c, &d.mwx[comp], wx)) return st;
                 if (int st = upload_f(c, &d.mwy[comp], wy)) return st;
+                // the FP32 product wx * wy of each list entry (the spreading
+                // multiplies it by the z weight), as the kernel would form it
+                std::vector<double> cw(std::max<size_t>(idx.size(), 1), 0.0);
+                for (int q = 0; q < ncol; ++q) {
+                    const int ii = q % g.sx, jj = q / g.sx;
+                    for (int e = off[q]; e < off[q + 1]; ++e) {
+                        const int m = idx[e];
+                        const float fx = (float)wx[3 * (size_t)m + (ii - i0v[m])];
+                        const float fy = (float)wy[3 * (size_t)m + (jj - j0v[m])];
+                        cw[e] = (double)(fx * fy);
+                    }
+                }
+                if (int st = upload_f(c, &d.csr_w[comp], cw)) return st;
                 if (int st = upload_i(c, &d.mi0[comp], i0v)) return st;
                 if (int st = upload_i(c, &d.mj0[comp], j0v)) return st;
                 std::vector<int> act;

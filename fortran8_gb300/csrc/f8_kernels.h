@@ -65,6 +65,7 @@ struct Dev {
     float2 *twx2;                          // (cos, -sin)(2 pi p/NX), p < NX/2
     float *wtR[3];                         // Thomas 1/den tables of the U, V, P wall systems
     float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
+    float *csr_w[3];                       // per column-list entry: the marker's x weight times y weight there
     int *mi0[3], *mj0[3];                  // per-marker stencil origins
     double *mwxd[3], *mwyd[3];             // FP64: per-marker x / y kernel weights (3 each)
     double *mwzd[3];                       // FP64: per-plane z weights of planes n-1, n, n+1 (3 each)

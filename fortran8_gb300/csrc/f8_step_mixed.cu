@@ -918,6 +918,7 @@ struct IbmArgsF {
     const float *Qc[3];
     double *Fc[3];
     const int *off[3], *idx[3];
+    const float *cw[3];              // per list entry: x weight * y weight
     const int *act[3];
     int nact[3];
     float *Q[3];
@@ -969,7 +970,7 @@ __device__ inline float spread_at_f(const IbmArgsF &a, const Geo &g, int comp, i
         const float wz = a.wz[comp][ke - n + 1];
         for (int q = b; q < e; ++q) {
             const int m = a.idx[comp][q];
-            const float w = a.wx[comp][3 * m + (ie - a.i0[comp][m])] * a.wy[comp][3 * m + (je - a.j0[comp][m])] * wz;
+            const float w = a.cw[comp][q] * wz;
             acc = fmaf((float)a.Fc[comp][m + (size_t)a.nm * (n - 1)], w, acc);
         }
     }
@@ -990,10 +991,13 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
     if (!g.walls) { if (j == 1) ys[1] = g.ny + 1; else if (j == g.ny) ys[1] = 0; }
     if (k == 1) zs[1] = g.nz + 1; else if (k == g.nz) zs[1] = 0;
     float f = 0.0f;
+#pragma unroll
     for (int zz = 0; zz < 2; ++zz) {
         if (zs[zz] < 0) continue;
+#pragma unroll
         for (int yy = 0; yy < 2; ++yy) {
             if (ys[yy] < 0) continue;
+#pragma unroll
             for (int xx = 0; xx < 2; ++xx) {
                 if (xs[xx] < 0) continue;
                 f += spread_at_f(a, g, comp, xs[xx], ys[yy], zs[zz]);
@@ -1742,7 +1746,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         for (int c = 0; c < 3; ++c) {
             a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
             a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
-            a.idx[c] = d.csr_idx[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
+            a.idx[c] = d.csr_idx[c]; a.cw[c] = d.csr_w[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
             for (int dk = 0; dk < 3; ++dk) {
                 double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
                 a.wz[c][dk] = (float)roma(zg);
