@@ -337,7 +337,8 @@ def run_ours(args, w):
                "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
     adj = None
     if not args.no_adjoint:
-        adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, args.adjoint_grid)
+        adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, args.adjoint_grid, args.adjoint_workload,
+                           args.adjoint_mixed_prefix)
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s", "repetitions": len(reps),
