@@ -103,7 +103,9 @@ struct df2 {
 
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 add2_rn(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+// a - b as one packed FMA: b * (-1) is exact, so the result is a - b rounded
+// once, as __fsub_rn gives it (the sign of a zero result included)
+__device__ __forceinline__ float2 sub2_rn(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 
 __device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
     s = add2_rn(a, b);
@@ -132,7 +134,18 @@ __device__ __forceinline__ df2 df2_add(df2 a, df2 b) {
 }
 
 __device__ __forceinline__ df2 df2_neg(df2 a) { return df2{neg2(a.hi), neg2(a.lo)}; }
-__device__ __forceinline__ df2 df2_sub(df2 a, df2 b) { return df2_add(a, df2_neg(b)); }
+
+// a - b: df2_add(a, -b) with each addition of a negated operand written as
+// the subtraction (exactly the same roundings)
+__device__ __forceinline__ df2 df2_sub(df2 a, df2 b) {
+    const float2 s = sub2_rn(a.hi, b.hi);
+    const float2 bb = sub2_rn(s, a.hi);
+    float2 e = sub2_rn(sub2_rn(a.hi, sub2_rn(s, bb)), add2_rn(b.hi, bb));
+    e = add2_rn(e, sub2_rn(a.lo, b.lo));
+    df2 r;
+    fast_two_sum2(s, e, r.hi, r.lo);
+    return r;
+}
 
 // a + b, b a float pair
 __device__ __forceinline__ df2 df2_add_f(df2 a, float2 b) {
@@ -146,8 +159,11 @@ __device__ __forceinline__ df2 df2_add_f(df2 a, float2 b) {
 
 // a - b for float pairs, exact
 __device__ __forceinline__ df2 df2_diff_ff(float2 a, float2 b) {
+    // two_sum2(a, -b) with the additions of -b written as subtractions
     df2 r;
-    two_sum2(a, neg2(b), r.hi, r.lo);
+    r.hi = sub2_rn(a, b);
+    const float2 bb = sub2_rn(r.hi, a);
+    r.lo = sub2_rn(sub2_rn(a, sub2_rn(r.hi, bb)), add2_rn(b, bb));
     return r;
 }
 

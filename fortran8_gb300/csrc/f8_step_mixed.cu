@@ -1057,7 +1057,7 @@ __device__ __forceinline__ df2 bcast(df a) { return df2_pack(a, a); }
 // Poisson right-hand side div(U^n + dU)/dt (fenep.f90:1494-1510) in df64:
 // each face difference of the state and of the FP32 increment is formed
 // exactly, scaled by the df64 1/dX, and summed (x, y, z in that order).
-__global__ void k_poisson_rhs_df(DfF U, DfF V, DfF W, const float *__restrict__ dU, const float *__restrict__ dV,
+__global__ void __launch_bounds__(256, 8) k_poisson_rhs_df(DfF U, DfF V, DfF W, const float *__restrict__ dU, const float *__restrict__ dV,
                                  const float *__restrict__ dW, float *__restrict__ Rh, float *__restrict__ Rl, Geo g,
                                  MixConst mc) {
     int i, j, k;
