@@ -247,10 +247,11 @@ __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
 // t(r) = cos(acos(r)/3 + 2 pi/3), the smallest root of 4t^3 - 3t = r.  t has a
 // square-root branch point at r = 1 (two equal smallest roots) and is
 // analytic at r = -1, so as a function of u = sqrt(1 - r) on [0, sqrt 2] it is
-// analytic: 2t(u) is evaluated as the degree-7 polynomial interpolating it at
-// the Chebyshev points of [0, sqrt 2] (fitted offline in double precision;
-// |error| <= 2.6e-8 before FP32 rounding, 2.2e-7 in FP32 Horner form).  This
-// replaces the arccos and cosine of the trigonometric formula.
+// analytic: t(u) is interpolated at the 8 Chebyshev points of [0, sqrt 2]
+// (fitted offline in double precision, |error| <= 2.7e-8), and 2t(u) is
+// evaluated from the FP32 coefficients of twice that polynomial in FP32 Horner
+// form (|error| <= 2.2e-7).  This replaces the arccos and cosine of the
+// trigonometric formula.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
