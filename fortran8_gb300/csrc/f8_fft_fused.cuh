@@ -416,7 +416,7 @@ __device__ __forceinline__ int brev_elem(int lane, int s) {
     return (bl << LG) | bs;
 }
 
-constexpr int XW_WARPS = 8;   // warps per block of the x passes
+constexpr int XW_WARPS = 4;   // warps per block of the x passes
 constexpr int XW_RB = 16;     // rows per block of the x passes (a constant: the tile indexing divides by it)
 
 inline size_t xw_smem(int nx, int rb) {
