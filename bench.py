@@ -65,14 +65,32 @@ MIXED_STAGE_BYTES = {
 }
 # kernels of each stage of the mixed step (for the ncu traffic of a stage)
 MIXED_STAGE_KERNELS = {
-    "eigen": ["k_codes3_f"],
-    "newton": ["k_update3_f", "k_newton_fix_f", "k_bc_c_pet_f"],
+    "eigen": ["k_codes3_f", "k_codes_ghost3_f"],
+    "newton": ["k_update3_f", "k_newton_fix_f", "k_update_ghost3_f", "k_bc_c_pet_xz_f"],
     "momentum": ["k_momentum3_f"],
     "ibm": ["k_ibm_interp_f", "k_ibm_spread_f", "k_drag_part", "k_drag_final"],
     "helmholtz": ["3 x (k_xfwd_w, k_plane_walls_c, k_xinv_w)"],
     "poisson": ["k_poisson_rhs_df", "2 x (k_xfwd_w, k_plane_walls_c, k_xinv_w)", "k_defect_df"],
     "project": ["k_march_df", "k_bc_set"],
 }
+
+
+# algorithmic bytes per cell of the single-launch kernels of the mixed step
+# (the share of MIXED_STAGE_BYTES each one moves), in the order of abi.KERNEL_NAMES
+MIXED_KERNEL_BYTES = {
+    "k_codes3_f": 25.0,        # C 24 read, code 1 written
+    "k_update3_f": 65.0,       # C 24, velocity hi 12, code 1 read; C 24, f 4 written
+    "k_momentum3_f": 108.0,    # the momentum stage
+    "k_poisson_rhs_df": 44.0,  # U, V, W 24 + dU 12 read; rhs (hi, lo) 8 written
+    "k_defect_df": 20.0,       # Phi 8 + rhs 8 read; defect 4 written
+    "k_march_df": 84.0,        # U, V, W, P 32 + dU 12 + Phi 8 read; U, V, W, P 32 written
+}
+
+
+def load_kernel_profiles():
+    """Per-kernel ncu figures of the mixed step (DRAM bytes per launch, pipe use)."""
+    p = ROOT / "profiles" / "kernels_mixed_c3_channel.json"
+    return json.loads(p.read_text()) if p.exists() else {}
 
 
 def load_traffic(precision):
@@ -288,6 +306,7 @@ def run_ours(args, w):
         s.timing_reset()
         s.step(min(args.steps, 100))
         _, stage_ms, nst = s.timing()
+        kern_ms, kern_n = s.kernel_timing() if prec == abi.F8_MIXED else (None, 0)
     ms = max_over_ranks(ws, tot_ms)
     value = cells * args.steps * ws / (ms / 1e3) / 1e6
     # e2e: host arrays in, K single-step calls reading the drag every step, host
@@ -311,30 +330,11 @@ def run_ours(args, w):
             torch.cuda.synchronize()
             reps.append(max_over_ranks(ws, time.perf_counter() - t0))
     e2e_s = sorted(reps)[1]
-    # the FP64 path on the same workload and the drag difference (accuracy gate)
+    # the FP64 path on the same workload over the workload's whole horizon and
+    # the per-field and drag differences (accuracy gate)
     cmp = None
     if prec == abi.F8_MIXED and not args.no_fp64_compare:
-        k64 = min(args.steps, 200)   # the FP64 path runs at ~80 ms/step here
-        with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64, poisson=pois) as s64:
-            s64.load(st0)
-            _, d64w = s64.step(args.warmup)
-            s64.set_timing(True)
-            s64.timing_reset()
-            _, d64 = s64.step(k64)
-            t64, st64, n64 = s64.timing()
-        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as sm:
-            sm.load(st0)
-            _, dmw = sm.step(args.warmup)
-            _, dm = sm.step(k64)
-        dall64 = np.concatenate([d64w, d64]) if d64w is not None else d64
-        dallm = np.concatenate([dmw, dm]) if dmw is not None else dm
-        rel = None
-        if dall64 is not None:
-            rel = float(np.max(np.abs(dallm[..., 0] - dall64[..., 0])) / np.max(np.abs(dall64[..., 0])))
-        v64 = cells * k64 / (t64 / 1e3) / 1e6
-        cmp = {"fp64_value": v64, "fp64_ms_per_step": t64 / k64, "mixed_over_fp64": value / v64,
-               "drag_rel_err_vs_fp64": rel, "steps_compared": args.warmup + k64,
-               "fp64_stage_ms_per_step": {n: float(v) for n, v in zip(abi.STAGE_NAMES, st64 / max(n64, 1))}}
+        cmp = fp64_compare(fns, w, pois, args.compare_steps or w.steps, value)
     adj = None
     if not args.no_adjoint:
         adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, args.adjoint_grid, args.adjoint_workload,
@@ -347,26 +347,43 @@ def run_ours(args, w):
            "d2h_bytes_per_step": int(sb / args.steps + ncyl * 3 * 8 + 8)}
     if rank != 0:
         return 0
-    # roofline of the dominant stage
+    # roofline of the dominant kernel: the single-launch kernel of the mixed
+    # step with the longest event-timed duration in the stage-timing pass
     per_step = stage_ms / max(nst, 1)
     names = abi.STAGE_NAMES
-    top = int(np.argmax(per_step))
     if prec == abi.F8_FP64:
         stage_bytes = {k: v * 8 for k, v in FP64_STAGE_WORDS.items()}
     else:
         stage_bytes = MIXED_STAGE_BYTES
-    byts = stage_bytes[names[top]] * cells
-    achieved = byts / (per_step[top] / 1e3) / 1e9
-    traffic = load_traffic(args.precision).get(names[top])
-    roof = {"bound": "hbm", "kernel_stage": names[top], "achieved": achieved, "peak": peaks["hbm_gbs"],
-            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
-            "traffic": traffic, "algorithmic_bytes": byts,
-            "stage_kernels": (MIXED_STAGE_KERNELS.get(names[top]) if prec == abi.F8_MIXED else None),
-            "stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)},
-            "stage_hbm_frac": {n: (stage_bytes[n] * cells / (float(v) / 1e3) / 1e9 / peaks["hbm_gbs"]) if v > 0 else None
+    hbm = peaks["hbm_gbs"]
+    roof = {"stage_ms_per_step": {n: float(v) for n, v in zip(names, per_step)},
+            "stage_hbm_frac": {n: (stage_bytes[n] * cells / (float(v) / 1e3) / 1e9 / hbm) if v > 0 else None
                                for n, v in zip(names, per_step)},
             "step_bytes": sum(stage_bytes.values()) * cells,
-            "step_hbm_frac": sum(stage_bytes.values()) * cells / (ms / args.steps / 1e3) / 1e9 / peaks["hbm_gbs"]}
+            "step_hbm_frac": sum(stage_bytes.values()) * cells / (ms / args.steps / 1e3) / 1e9 / hbm}
+    if kern_ms is not None:
+        prof = load_kernel_profiles()
+        kms = {n: float(v) / max(kern_n, 1) for n, v in zip(abi.KERNEL_NAMES, kern_ms)}
+        top = max(kms, key=kms.get)
+        byts = MIXED_KERNEL_BYTES[top] * cells
+        achieved = byts / (kms[top] / 1e3) / 1e9
+        pk = prof.get(top, {})
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": pk.get("dram_bytes"),
+                "algorithmic_bytes": byts, "kernel_ms": kms[top], "launches_timed": int(kern_n),
+                "compute": {k: pk[k] for k in ("issue_active", "fma_pipe", "fp64_pipe", "bound") if k in pk},
+                "kernels": {n: {"ms": v, "hbm_frac": MIXED_KERNEL_BYTES[n] * cells / (v / 1e3) / 1e9 / hbm if v > 0 else None,
+                                **({"ncu_bound": prof[n]["bound"]} if n in prof and "bound" in prof[n] else {})}
+                            for n, v in kms.items()},
+                "profiles": "profiles/kernels_mixed_c3_channel.json (ncu per-kernel captures)",
+                **roof}
+    else:
+        top = int(np.argmax(per_step))
+        byts = stage_bytes[names[top]] * cells
+        achieved = byts / (per_step[top] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel_stage": names[top], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": load_traffic(args.precision).get(names[top]),
+                "algorithmic_bytes": byts, **roof}
     line = {"metric": "Mcell-steps/s", "value": value, "unit": "Mcell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == abi.F8_FP64 else "f32+f64",
@@ -382,6 +399,51 @@ def run_ours(args, w):
         line["cpu_baseline"] = cpu_baseline(w)
     print(json.dumps(line))
     return 0
+
+
+def fp64_compare(fns, w, pois, nsteps, mixed_value):
+    """Mixed and FP64 runs from the same seeded state over nsteps steps: the
+    drag histories (largest difference over all steps relative to the largest
+    FP64 drag, per component x / y) and the relative L2 differences of the
+    final u, v, w, p and trC over the interior cells.  The FP64 run is also
+    the FP64-GPU speed (CUDA events of its f8_step calls)."""
+    st0 = configs.initial_state(w)
+    res = {}
+    for name, prec in (("fp64", abi.F8_FP64), ("mixed", abi.F8_MIXED)):
+        with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as s:
+            s.load(st0)
+            s.timing_reset()
+            drags = []
+            done = 0
+            while done < nsteps:
+                n = min(500, nsteps - done)
+                _, d = s.step(n)
+                if d is not None:
+                    drags.append(d)
+                done += n
+            tms, _, _ = s.timing()
+            res[name] = (np.concatenate(drags) if drags else None, s.store(), tms)
+    (d64, o64, t64), (dm, om, _) = res["fp64"], res["mixed"]
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    inner = (slice(1, -1), slice(1, -1), slice(1, -1))
+    errs = {f: rel(om[f][inner], o64[f][inner]) for f in ("u", "v", "w", "p")}
+    tr = lambda o: o["c"][inner][..., 0] + o["c"][inner][..., 3] + o["c"][inner][..., 5]
+    errs["trC"] = rel(tr(om), tr(o64))
+    out = {"steps_compared": nsteps, "field_rel_l2": errs}
+    if d64 is not None:
+        scale = np.max(np.abs(d64[..., 0]))
+        out["drag_rel_err_vs_fp64"] = float(np.max(np.abs(dm[..., 0] - d64[..., 0])) / scale)
+        out["drag_rel_err_by_component"] = {
+            c: float(np.max(np.abs(dm[..., q] - d64[..., q])) / np.max(np.abs(d64[..., q])))
+            for q, c in ((0, "x"), (1, "y"))}
+        tail = max(1, nsteps // 10)
+        out["drag_rel_err_last_10pct"] = float(np.max(np.abs(dm[-tail:, :, 0] - d64[-tail:, :, 0])) / scale)
+    v64 = w.cells * nsteps / (t64 / 1e3) / 1e6
+    out.update({"fp64_value": v64, "fp64_ms_per_step": t64 / nsteps, "mixed_over_fp64": mixed_value / v64})
+    return out
 
 
 def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_prefix=0):
@@ -503,6 +565,8 @@ def main():
     ap.add_argument("--workload", default="c3_channel", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--compare-steps", type=int, default=0,
+                    help="steps of the mixed-vs-FP64 comparison (default: the workload's horizon, 2000)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint run")

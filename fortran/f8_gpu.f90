@@ -135,6 +135,13 @@ module f8_gpu
             type(c_ptr), value :: xy
         end function f8_markers
 
+        ! codes: integer(1) (NX, rows, NZ) of the last step's SPD candidate choices
+        integer(c_int) function f8_selection_codes(ctx, codes) bind(C, name="f8_selection_codes")
+            import :: c_ptr, c_int
+            type(c_ptr), value :: ctx
+            type(c_ptr), value :: codes
+        end function f8_selection_codes
+
         ! out: real(8) (18, points) of the mid-plane slice (axis 2: x-y, 1: x-z, 0: y-z);
         ! variant 0: column 7 = KE (fenep.f90), 1: Q (fenep_mpi.f90)
         integer(c_int) function f8_slice(ctx, axis, variant, out) bind(C, name="f8_slice")
@@ -191,6 +198,14 @@ module f8_gpu
             import :: c_ptr, c_int
             type(c_ptr), value :: ctx
         end function f8_timing_reset
+
+        ! kernel_ms: real(8) (6) of the mixed step's single-launch kernels (enum f8_kernel)
+        integer(c_int) function f8_kernel_timing(ctx, kernel_ms, steps_timed) bind(C, name="f8_kernel_timing")
+            import :: c_ptr, c_int, c_double, c_long_long
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: kernel_ms(*)
+            integer(c_long_long), intent(out) :: steps_timed
+        end function f8_kernel_timing
 
         ! q and phi are device pointers (e.g. from a CUDA Fortran or OpenACC code)
         integer(c_int) function f8_fft_solve(nx, ny, nz, lx, ly, lz, q, phi, lhs0, lhs1) bind(C, name="f8_fft_solve")

@@ -80,6 +80,7 @@ ABI_FUNCTIONS = {
     "store": (C.c_int, [C.c_void_p, C.POINTER(Fields)]),
     "diagnostics": (C.c_int, [C.c_void_p, C.POINTER(Diag)]),
     "markers": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), _dp]),
+    "selection_codes": (C.c_int, [C.c_void_p, C.c_void_p]),
     "slice": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "turbulence": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_void_p]),
     "spectrum": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
@@ -91,6 +92,7 @@ ABI_FUNCTIONS = {
     "set_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "timing": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_longlong)]),
     "timing_reset": (C.c_int, [C.c_void_p]),
+    "kernel_timing": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_longlong)]),
     "fft_solve": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                             C.c_void_p, C.c_void_p, C.c_double, C.c_double]),
 }
@@ -103,6 +105,8 @@ GPU_FUNCTIONS = {
 
 NSTAGE = 7
 STAGE_NAMES = ("eigen", "newton", "momentum", "ibm", "helmholtz", "poisson", "project")
+NKERNEL = 6
+KERNEL_NAMES = ("k_codes3_f", "k_update3_f", "k_momentum3_f", "k_poisson_rhs_df", "k_defect_df", "k_march_df")
 
 
 def bind(lib: C.CDLL, prefix: str) -> dict:

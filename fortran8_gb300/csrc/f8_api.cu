@@ -161,8 +161,9 @@ struct f8_ctx {
     bool timing = false;
     std::vector<cudaEvent_t> evpool;
     cudaEvent_t tot0 = nullptr, tot1 = nullptr;
-    double total_ms = 0.0, stage_ms[NSTAGE] = {};
+    double total_ms = 0.0, stage_ms[NSTAGE] = {}, kernel_ms[NKERNEL] = {};
     long long timed_steps = 0;
+    long long kernel_steps = 0;    // steps covered by kernel_ms
     long long step_launches = 0;   // kernels launched by f8_step since load / timing reset
 
     template <typename T>
@@ -582,7 +583,17 @@ int setup(f8_ctx *c) {
 
 int ensure_drag(f8_ctx *c, int nsteps) {
     if (c->cyl.empty() || nsteps <= c->drag_cap) return F8_OK;
-    int cap = std::max(nsteps, 64);
+    // grow geometrically and free the smaller buffer (no work on it is in
+    // flight: every f8_step call ends with a synchronisation)
+    int cap = std::max({nsteps, 64, 2 * c->drag_cap});
+    if (c->drag_dev) {
+        API_CUDA(c, cudaStreamSynchronize(c->s));
+        auto it = std::find(c->allocs.begin(), c->allocs.end(), (void *)c->drag_dev);
+        if (it != c->allocs.end()) c->allocs.erase(it);
+        cudaFree(c->drag_dev);
+        c->drag_dev = nullptr;
+        c->drag_cap = 0;
+    }
     double *p = nullptr;
     API_CUDA(c, c->alloc(&p, (size_t)cap * c->cyl.size() * 3));
     c->drag_dev = p;
@@ -713,7 +724,9 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     bool drag_in_slot = false;
     // the mixed step counts non-finite velocities in its counters instead
     if (c->precision != F8_MIXED) API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
-    const size_t per = NSTAGE + 1;
+    // per step: the stage boundaries, then the pairs around the single-launch
+    // kernels of the mixed step
+    const size_t per = NSTAGE + 1 + 2 * NKERNEL;
     if (c->timing && c->evpool.size() < per * nsteps) {
         size_t have = c->evpool.size();
         c->evpool.resize(per * nsteps, nullptr);
@@ -730,6 +743,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
         o.poisson = c->poisson;
         o.sor_omega = c->phys.sor_omega; o.sor_eps = c->phys.sor_eps; o.sor_itrmax = c->phys.sor_itrmax;
         o.ev = c->timing ? &c->evpool[per * s] : nullptr;
+        o.kev = (c->timing && c->precision == F8_MIXED) ? &c->evpool[per * s + NSTAGE + 1] : nullptr;
         const bool mixed = c->precision == F8_MIXED;
         if (!o.polymer && s == 0) {
             // beta == 1: C and T vanish (fenep.f90:2479-2485)
@@ -814,6 +828,14 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
                 for (int q = 0; q < NSTAGE; ++q) {
                     API_CUDA(c, cudaEventElapsedTime(&ms, c->evpool[per * s2 + q], c->evpool[per * s2 + q + 1]));
                     c->stage_ms[q] += ms;
+                }
+        if (c->timing && c->precision == F8_MIXED) c->kernel_steps += nsteps;
+        if (c->timing && c->precision == F8_MIXED)
+            for (int s2 = 0; s2 < nsteps; ++s2)
+                for (int q = 0; q < NKERNEL; ++q) {
+                    const size_t e0 = per * s2 + NSTAGE + 1 + 2 * q;
+                    API_CUDA(c, cudaEventElapsedTime(&ms, c->evpool[e0], c->evpool[e0 + 1]));
+                    c->kernel_ms[q] += ms;
                 }
     }
     c->last_newton_iters = (long long)cnt.newton_iters;
@@ -1263,6 +1285,28 @@ int f8_stats_read(f8_ctx *c, double *su, double *sv, double *sw, double *probes,
     return F8_OK;
 }
 
+int f8_selection_codes(f8_ctx *c, unsigned char *codes) {
+    if (!c || !codes) return F8_ERR_ARG;
+    if (!c->loaded || c->step == c->step0 || c->phys.beta == 1.0) return F8_ERR_STATE;
+    const f8::Geo &g = c->d.g;
+    const int rows = f8::prows(g), r0 = f8::prow0(g);
+    std::vector<unsigned char> in((size_t)g.nx * g.ny * g.nz), gh;
+    API_CUDA(c, cudaMemcpyAsync(in.data(), c->d.codes, in.size(), cudaMemcpyDeviceToHost, c->s));
+    if (g.walls) {
+        gh.resize((size_t)g.nx * 2 * g.nz);
+        API_CUDA(c, cudaMemcpyAsync(gh.data(), c->d.codes_g, gh.size(), cudaMemcpyDeviceToHost, c->s));
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    for (int k = 1; k <= g.nz; ++k)
+        for (int r = 0; r < rows; ++r) {
+            const int j = r0 + r;
+            for (int i = 1; i <= g.nx; ++i)
+                codes[(size_t)(i - 1) + (size_t)g.nx * ((size_t)r + (size_t)rows * (k - 1))] =
+                    (j >= 1 && j <= g.ny) ? in[f8::qix(g, i, j, k)] : gh[f8::gcix(g, i, j, k)];
+        }
+    return F8_OK;
+}
+
 int f8_markers(f8_ctx *c, int *n, double *xy) {
     if (!c) return F8_ERR_ARG;
     if (n) *n = (int)c->mk.size();
@@ -1274,6 +1318,14 @@ int f8_markers(f8_ctx *c, int *n, double *xy) {
 int f8_set_timing(f8_ctx *c, int enable) {
     if (!c) return F8_ERR_ARG;
     c->timing = enable != 0;
+    return F8_OK;
+}
+
+int f8_kernel_timing(f8_ctx *c, double *kernel_ms, long long *steps_timed) {
+    if (!c || !kernel_ms) return F8_ERR_ARG;
+    if (c->precision != F8_MIXED) return F8_ERR_UNSUPPORTED;
+    for (int q = 0; q < NKERNEL; ++q) kernel_ms[q] = c->kernel_ms[q];
+    if (steps_timed) *steps_timed = c->kernel_steps;
     return F8_OK;
 }
 
@@ -1290,7 +1342,9 @@ int f8_timing_reset(f8_ctx *c) {
     if (!c) return F8_ERR_ARG;
     c->total_ms = 0.0;
     for (int q = 0; q < NSTAGE; ++q) c->stage_ms[q] = 0.0;
+    for (int q = 0; q < NKERNEL; ++q) c->kernel_ms[q] = 0.0;
     c->timed_steps = 0;
+    c->kernel_steps = 0;
     c->step_launches = 0;
     return F8_OK;
 }

@@ -2,9 +2,9 @@
 // the divergence residual: kinetic energy on the cell centres, CFL from the
 // maxima of U, V, W over the whole halo field, trC minimum / maximum / mean /
 // standard deviation (the reference's two-pass form, mean first), max |div u|
-// and a NaN flag.  Deterministic: a fixed grid of DIAG_BLOCKS blocks
-// accumulates grid-stride partials per thread, a block tree reduces them, and
-// one block reduces the block partials in a fixed order.  Both precisions: the
+// and a NaN flag.  Deterministic: a grid of 4 blocks per SM (fixed for a
+// device) accumulates grid-stride partials per thread, a block tree reduces
+// them, and one block reduces the block partials in a fixed order.  Both precisions: the
 // FP64 state, or the double-float state and FP32 C of the mixed path.
 #include <algorithm>
 #include <cfloat>
@@ -15,7 +15,6 @@
 namespace f8 {
 namespace {
 
-constexpr int DIAG_BLOCKS = 592;   // 4 x 148-152 SMs
 constexpr int DIAG_THREADS = 256;
 
 struct DiagIn {
@@ -86,7 +85,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_pass1(DiagIn in, Geo g, d
     __shared__ double sh[DIAG_THREADS];
     const long ni = (long)g.nx * g.ny * g.nz;
     double ke = 0.0, tsum = 0.0, tmin = DBL_MAX, tmax = -DBL_MAX, dmax = 0.0, nan = 0.0;
-    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)DIAG_BLOCKS * DIAG_THREADS) {
+    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)gridDim.x * DIAG_THREADS) {
         const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
         const int h = hix(g, i, j, k);
         const double u0 = vel(in, 0, h), u1 = vel(in, 0, h - 1);
@@ -107,7 +106,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_pass1(DiagIn in, Geo g, d
         if (isnan(ur) || isnan(vr) || isnan(wr)) nan = 1.0;
     }
     double umax = -DBL_MAX, vmax = -DBL_MAX, wmax = -DBL_MAX;
-    for (long q = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; q < in.cs; q += (long)DIAG_BLOCKS * DIAG_THREADS) {
+    for (long q = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; q < in.cs; q += (long)gridDim.x * DIAG_THREADS) {
         umax = fmax(umax, vel(in, 0, (int)q));
         vmax = fmax(vmax, vel(in, 1, (int)q));
         if (in.d3) wmax = fmax(wmax, vel(in, 2, (int)q));
@@ -128,7 +127,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_pass2(DiagIn in, Geo g, c
     const long ni = (long)g.nx * g.ny * g.nz;
     const double mean = out[P_TSUM] / (double)ni;
     double s = 0.0;
-    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)DIAG_BLOCKS * DIAG_THREADS) {
+    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)gridDim.x * DIAG_THREADS) {
         const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
         const double d = trace_at(in, hix(g, i, j, k)) - mean;
         s += d * d;
@@ -138,13 +137,13 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_pass2(DiagIn in, Geo g, c
 }
 
 // final: one block reduces the block partials (stride np per block) in order
-__global__ void __launch_bounds__(DIAG_THREADS) k_diag_final(const double *part, int np, int nv, double *out) {
+__global__ void __launch_bounds__(DIAG_THREADS) k_diag_final(const double *part, int nb, int np, int nv, double *out) {
     __shared__ double sh[DIAG_THREADS];
     for (int m = 0; m < nv; ++m) {
         const bool mx = m == P_TMAX || m == P_DIV || m == P_UMAX || m == P_VMAX || m == P_WMAX || m == P_NAN;
         const bool mn = m == P_TMIN;
         double v = mn ? DBL_MAX : (mx ? -DBL_MAX : 0.0);
-        for (int b = threadIdx.x; b < DIAG_BLOCKS; b += DIAG_THREADS) {
+        for (int b = threadIdx.x; b < nb; b += DIAG_THREADS) {
             const double x = part[(size_t)b * np + m];
             v = mn ? fmin(v, x) : (mx ? fmax(v, x) : v + x);
         }
@@ -169,10 +168,11 @@ cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, Di
         in.U = d.U; in.V = d.V; in.W = d.W;
         in.C = d.C;
     }
-    k_diag_pass1<<<DIAG_BLOCKS, DIAG_THREADS, 0, s>>>(in, g, part); count_launch();
-    k_diag_final<<<1, DIAG_THREADS, 0, s>>>(part, P_N, P_N, out); count_launch();
-    k_diag_pass2<<<DIAG_BLOCKS, DIAG_THREADS, 0, s>>>(in, g, out, part); count_launch();
-    k_diag_final<<<1, DIAG_THREADS, 0, s>>>(part, 1, 1, out + P_N); count_launch();
+    const int nb = diag_blocks();
+    k_diag_pass1<<<nb, DIAG_THREADS, 0, s>>>(in, g, part); count_launch();
+    k_diag_final<<<1, DIAG_THREADS, 0, s>>>(part, nb, P_N, P_N, out); count_launch();
+    k_diag_pass2<<<nb, DIAG_THREADS, 0, s>>>(in, g, out, part); count_launch();
+    k_diag_final<<<1, DIAG_THREADS, 0, s>>>(part, nb, 1, 1, out + P_N); count_launch();
     double h[P_N + 1];
     F8_CUDA_RET(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
     F8_CUDA_RET(cudaStreamSynchronize(s));
@@ -190,7 +190,25 @@ cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, Di
     return cudaGetLastError();
 }
 
-size_t diag_partials() { return (size_t)DIAG_BLOCKS * P_N; }
+int device_sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;
+    }
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 152;
+        }
+        cache[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+size_t diag_partials() { return (size_t)diag_blocks() * P_N; }
 
 }  // namespace f8
 
@@ -300,7 +318,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_turb_pass(TurbIn in, Geo g, do
     const long ni = (long)g.nx * g.ny * g.nz;
     double a[T_N] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const double dX = g.dx, dY = g.dy, dZ = g.dz;
-    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)DIAG_BLOCKS * DIAG_THREADS) {
+    for (long t = (long)blockIdx.x * DIAG_THREADS + threadIdx.x; t < ni; t += (long)gridDim.x * DIAG_THREADS) {
         const int i = 1 + (int)(t % g.nx), j = 1 + (int)((t / g.nx) % g.ny), k = 1 + (int)(t / ((long)g.nx * g.ny));
         auto U = [&](int ii, int jj, int kk) { return fluct(in, g, 0, ii, jj, kk); };
         auto V = [&](int ii, int jj, int kk) { return fluct(in, g, 1, ii, jj, kk); };
@@ -341,11 +359,11 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_turb_pass(TurbIn in, Geo g, do
         for (int m = 0; m < T_N; ++m) part[(size_t)blockIdx.x * T_N + m] = r[m];
 }
 
-__global__ void k_sum_parts(const double *part, int np, int nv, double *out) {
+__global__ void k_sum_parts(const double *part, int nb, int np, int nv, double *out) {
     __shared__ double sh[DIAG_THREADS];
     for (int m = 0; m < nv; ++m) {
         double v = 0.0;
-        for (int b = threadIdx.x; b < DIAG_BLOCKS; b += DIAG_THREADS) v += part[(size_t)b * np + m];
+        for (int b = threadIdx.x; b < nb; b += DIAG_THREADS) v += part[(size_t)b * np + m];
         const double r = block_reduce(v, sh, Add());
         if (threadIdx.x == 0) out[m] = r;
     }
@@ -371,7 +389,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_spec_bin(const double *H, Geo 
     const int nxh = g.nx / 2 + 1;
     const long nm = (long)nxh * g.ny * g.nz;
     // each block owns a contiguous range of modes and bins them in order
-    const long per = (nm + DIAG_BLOCKS - 1) / DIAG_BLOCKS;
+    const long per = (nm + gridDim.x - 1) / gridDim.x;
     const long m0 = (long)blockIdx.x * per, m1 = min(nm, m0 + per);
     if (threadIdx.x == 0) {
         for (long m = m0; m < m1; ++m) {
@@ -388,17 +406,17 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_spec_bin(const double *H, Geo 
         hist[(size_t)blockIdx.x * nbins + b] = (accumulate ? hist[(size_t)blockIdx.x * nbins + b] : 0.0) + hs[b];
 }
 
-__global__ void k_hist_final(const double *hist, int nbins, double *out) {
+__global__ void k_hist_final(const double *hist, int nb, int nbins, double *out) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += gridDim.x * blockDim.x) {
         double v = 0.0;
-        for (int q = 0; q < DIAG_BLOCKS; ++q) v += hist[(size_t)q * nbins + b];
+        for (int q = 0; q < nb; ++q) v += hist[(size_t)q * nbins + b];
         out[b] = v;
     }
 }
 
 }  // namespace
 
-size_t turb_partials(int nx) { return (size_t)DIAG_BLOCKS * std::max<int>(T_N, nx + 1); }
+size_t turb_partials(int nx) { return (size_t)diag_blocks() * std::max<int>(T_N, nx + 1); }
 
 cudaError_t device_turbulence(Dev &d, bool mixed, const double *const mean[3], double *part, double *out,
                               TurbValues *res, cudaStream_t s) {
@@ -416,8 +434,9 @@ cudaError_t device_turbulence(Dev &d, bool mixed, const double *const mean[3], d
     for (int c = 0; c < 3; ++c) in.mean[c] = mean ? mean[c] : nullptr;
     in.d3 = 1;
     const double dep = 0.5 * (1.0 - d.ph.beta) / d.ph.re / d.ph.wi * (d.ph.lp2 - 3.0);
-    k_turb_pass<<<DIAG_BLOCKS, DIAG_THREADS, 0, s>>>(in, g, dep, d.ph.lp2, part); count_launch();
-    k_sum_parts<<<1, DIAG_THREADS, 0, s>>>(part, T_N, T_N, out); count_launch();
+    const int nb = diag_blocks();
+    k_turb_pass<<<nb, DIAG_THREADS, 0, s>>>(in, g, dep, d.ph.lp2, part); count_launch();
+    k_sum_parts<<<1, DIAG_THREADS, 0, s>>>(part, nb, T_N, T_N, out); count_launch();
     double h[T_N];
     F8_CUDA_RET(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
     F8_CUDA_RET(cudaStreamSynchronize(s));
@@ -475,10 +494,10 @@ cudaError_t device_spectrum(Dev &d, bool mixed, const double *const mean[3], Spe
             k_fft_lines<double><<<dim3((nxh + tx - 1) / tx, ny), 256, smem, s>>>(w.H, nz, nxh * ny, nxh, nxh, tx, w.twr[2],
                                                                                   w.twi[2], -1, 0, none); count_launch();
         }
-        k_spec_bin<<<DIAG_BLOCKS, DIAG_THREADS, (size_t)nbins * sizeof(double), s>>>(w.H, g, nbins, inv_n2, w.hist,
+        k_spec_bin<<<diag_blocks(), DIAG_THREADS, (size_t)nbins * sizeof(double), s>>>(w.H, g, nbins, inv_n2, w.hist,
                                                                                     c > 0 ? 1 : 0); count_launch();
     }
-    k_hist_final<<<(nbins + 255) / 256, 256, 0, s>>>(w.hist, nbins, energy_dev); count_launch();
+    k_hist_final<<<(nbins + 255) / 256, 256, 0, s>>>(w.hist, diag_blocks(), nbins, energy_dev); count_launch();
     return cudaGetLastError();
 }
 

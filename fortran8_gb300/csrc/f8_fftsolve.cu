@@ -130,8 +130,11 @@ extern "C" int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double
 // (its own pool, or a budget shared with other jobs on the same GPU), so an
 // allocation inside the time loop would fail or fragment that budget.  For
 // them f8_fft_solve_noalloc runs the same periodic solve as f8_fft_solve with
-// its workspace in fixed arrays of device memory that exist from the moment
-// the library is loaded on a device, and calls no allocating routine.
+// its workspace in fixed arrays of device memory, and calls no allocating
+// routine.  With CUDA's lazy module loading the arrays are placed in device
+// memory when this library's device code is first used on a device (which
+// may be the first call of this entry point), so a caller makes that first
+// call before it reserves the rest of the device memory for itself.
 //
 // Limits and rules (also stated in include/f8.h):
 //  * the spectrum of the grid must fit in F8_NOALLOC_MAX_SPECTRUM complex
@@ -144,7 +147,9 @@ extern "C" int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double
 //    several host threads, or other streams) race on the arrays;
 //  * the first call on a device looks up the device addresses of the arrays
 //    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture on that device.
+//    before any stream capture on that device.  The addresses are kept for
+//    the life of the process: after a cudaDeviceReset the library has to be
+//    unloaded and loaded again before this entry point is used there.
 
 #include <mutex>
 

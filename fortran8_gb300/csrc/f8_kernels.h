@@ -87,9 +87,11 @@ struct StepOpts {
     double sor_omega, sor_eps;
     int sor_itrmax;
     cudaEvent_t *ev;   // NSTAGE+1 events recorded at the stage boundaries, or null
+    cudaEvent_t *kev;  // 2*NKERNEL events bracketing the single-launch kernels (f8_kernel), or null
     double *c_mid;     // FP64: receives C as the momentum stage read it (6 halo fields), or null
 };
 constexpr int NSTAGE = 7;
+constexpr int NKERNEL = 6;   // enum f8_kernel
 
 // FP64 step (f8_step_fp64.cu).  Returns a cudaError_t of the launches; SOR
 // iteration count in *sor_iters.
@@ -116,6 +118,10 @@ struct DiagValues {
     double ke, cfl, trc_min, trc_max, trc_mean, trc_std, div_max;
     int nan_found;
 };
+// streaming multiprocessors of the current device (queried once per device)
+int device_sm_count();
+// blocks of the deterministic on-device reductions: 4 per SM of the device
+inline int diag_blocks() { return 4 * device_sm_count(); }
 size_t diag_partials();   // doubles of the partials buffer
 // slice output (f8_diag.cu): the state of either precision, read as FP64
 struct DiagSliceIn {

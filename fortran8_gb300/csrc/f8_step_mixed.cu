@@ -1658,6 +1658,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     cudaError_t e;
     const MixConst mc = make_const(g, d.ph);
     auto mark = [&](int q) { if (o.ev) cudaEventRecord(o.ev[q], s); };
+    // events bracketing one kernel launch (enum f8_kernel), on its stream
+    auto kmark = [&](int kq, int edge) { if (o.kev) cudaEventRecord(o.kev[2 * kq + edge], s); };
     const DfF U{d.Uf, d.Ul}, V{d.Vf, d.Vl}, W{d.Wf, d.Wl}, P{d.Pf, d.Pl}, Phi{d.Phif, d.Phil};
     mark(0);
     // wall channel: the ghost rows' codes and update run on a side stream
@@ -1675,7 +1677,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             }
             k_codes_ghost3_f<<<gg, 128, 0, sg>>>(d.Cf, d.codes_g, g, d.cs); count_launch();
         }
+        kmark(F8_KERNEL_CODES, 0);
         k_codes3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.codes, g, d.cs, d.fixcnt); count_launch();
+        kmark(F8_KERNEL_CODES, 1);
         mark(1);
         if (g.walls) {
             if (gbranch) {
@@ -1686,9 +1690,11 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
                                                   mc, d.cs, d.cnt); count_launch();
             if (gbranch) F8_CUDA_RET(cudaEventRecord(d.ev_g[2], sg));
         }
+        kmark(F8_KERNEL_UPDATE, 0);
         k_update3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.Uf, d.Vf, d.Wf, g, d.ph, mc,
                                                         d.cs, d.fixlist, d.fixcnt, d.cnt); count_launch();
-        k_newton_fix_f<<<2 * 152, 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
+        kmark(F8_KERNEL_UPDATE, 1);
+        k_newton_fix_f<<<2 * device_sm_count(), 128, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.Uf, d.Vf, d.Wf, g, d.ph, mc, d.cs, d.fixlist,
                                                d.fixcnt, d.cnt); count_launch();
         long n = halo_count(g);
         if (g.walls) {
@@ -1701,7 +1707,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         }
         if ((e = cudaGetLastError())) return e;
     } else {
+        kmark(F8_KERNEL_CODES, 0); kmark(F8_KERNEL_CODES, 1);
         mark(1);
+        kmark(F8_KERNEL_UPDATE, 0); kmark(F8_KERNEL_UPDATE, 1);
     }
     mark(2);
     {
@@ -1717,7 +1725,9 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         a.vis = (float)(d.ph.beta / d.ph.re);
         a.dt = d.ph.dt;
         dim3 blk(32, 8);
+        kmark(F8_KERNEL_MOMENTUM, 0);
         k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch();
+        kmark(F8_KERNEL_MOMENTUM, 1);
         if ((e = cudaGetLastError())) return e;
     }
     if (o.polymer && g.walls) {
@@ -1799,9 +1809,12 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     // Poisson: FP32 solve + one df64 defect correction.  The increments and
     // Phi get no halo pass: their readers wrap / apply the Neumann rule.
     const dim3 pblk(32, 8), pgrid((g.nx + pblk.x - 1) / pblk.x, (g.ny + pblk.y - 1) / pblk.y, (g.nz + 1) / 2);
+    kmark(F8_KERNEL_POISSON_RHS, 0);
     k_poisson_rhs_df<<<pgrid, pblk, 0, s>>>(U, V, W, d.dUf[0], d.dUf[1], d.dUf[2], d.Rhf, d.Rlf, g, mc);
     count_launch();
+    kmark(F8_KERNEL_POISSON_RHS, 1);
     if (o.poisson == F8_POISSON_SOR) {
+        kmark(F8_KERNEL_DEFECT, 0); kmark(F8_KERNEL_DEFECT, 1);
         if ((e = sor_solve_m(d, o, sor_iters, s))) return e;
     } else {
         *sor_iters = -1;
@@ -1812,15 +1825,19 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         if (!g.walls) e = solve_periodic_f(d, d.Rhf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rhf, out, SYS_P, s);
         if (e) return e;
+        kmark(F8_KERNEL_DEFECT, 0);
         k_defect_df<<<pgrid, pblk, 0, s>>>(d.Phif, d.Rhf, d.Rlf, d.Rdf, g, mc); count_launch();
+        kmark(F8_KERNEL_DEFECT, 1);
         out.mode = 2;
         if (!g.walls) e = solve_periodic_f(d, d.Rdf, out, 0.0, -1.0, s);
         else e = solve_walls_f(d, d.Rdf, out, SYS_P, s);
         if (e) return e;
     }
     mark(6);
+    kmark(F8_KERNEL_MARCH, 0);
     k_march_df<<<pgrid, pblk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
     count_launch();
+    kmark(F8_KERNEL_MARCH, 1);
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
     if (gbranch) {
         // join the ghost-row branch (when the Helmholtz branches did not)

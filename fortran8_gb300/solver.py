@@ -252,6 +252,15 @@ class Solver:
             self._check(self._fns["stats_read"](self._h, None, None, None, _ptr(probes), C.byref(n)))
         return sums, probes, n.value
 
+    def selection_codes(self) -> np.ndarray:
+        """SPD candidate choices of the last step (f8_selection_codes), shape
+        (NZ, rows, NX) uint8; rows = NY + 2 with walls, else NY."""
+        g = self.grid
+        rows = g.ny + 2 if g.bc_y == abi.F8_BC_WALLS else g.ny
+        out = np.zeros((g.nz, rows, g.nx), dtype=np.uint8)
+        self._check(self._fns["selection_codes"](self._h, out.ctypes.data))
+        return out
+
     def markers(self) -> np.ndarray:
         n = C.c_int()
         self._check(self._fns["markers"](self._h, C.byref(n), None))
@@ -269,6 +278,14 @@ class Solver:
         n = C.c_longlong()
         self._check(self._fns["timing"](self._h, C.byref(tot), _ptr(st), C.byref(n)))
         return tot.value, st, n.value
+
+    def kernel_timing(self):
+        """(per-kernel ms array over abi.KERNEL_NAMES, steps covered) of the
+        mixed step's single-launch kernels (f8_kernel_timing)."""
+        ms = np.zeros(abi.NKERNEL)
+        n = C.c_longlong()
+        self._check(self._fns["kernel_timing"](self._h, _ptr(ms), C.byref(n)))
+        return ms, n.value
 
     def timing_reset(self) -> None:
         self._check(self._fns["timing_reset"](self._h))

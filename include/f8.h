@@ -122,7 +122,10 @@ typedef struct f8_diag {
     long long newton_iters;     /* Newton iterations summed over cells and the
                                    steps of the last f8_step call               */
     long long newton_unconverged; /* cell-steps that hit newton_itrmax, same span */
-    int poisson_iters;          /* SOR iterations of the last step (-1: FFT)     */
+    int poisson_iters;          /* SOR iterations of the last step (-1: FFT);
+                                   sor_itrmax + 1 when the cap was reached, the
+                                   value of the reference's loop counter after
+                                   a DO loop that did not exit (fenep.f90:885-901) */
     int nan_found;
     long long kernel_launches;  /* CUDA kernels launched by this context's f8_step
                                    calls since f8_load or f8_timing_reset (0 for
@@ -240,6 +243,15 @@ int f8_stats_begin(f8_ctx *ctx, int mode, const double *mean_u, const double *me
  * (NULL to skip), and the number of steps accumulated. */
 int f8_stats_read(f8_ctx *ctx, double *sum_u, double *sum_v, double *sum_w, double *probes, int *nsteps);
 
+/* SPD face-candidate choices of the last step's polymer update
+ * (CpxCnx / CpyCny / CpzCnz, fenep.f90:220-230; 2D fenep_2d.f90:159-175),
+ * one byte per updated cell, layout [k][row][i] with row 0..NY+1 (walls:
+ * the ghost rows are updated too) or 1..NY (periodic): bits 2d..2d+1 hold
+ * the chosen candidate - 1 (0..2), or 3 when the cell value was used, for
+ * d = x, y, z.  For parity checks that count selection flips between two
+ * runs.  F8_ERR_STATE before the first step after a load or when beta == 1. */
+int f8_selection_codes(f8_ctx *ctx, unsigned char *codes);
+
 /* Number of Lagrangian markers per z-plane and their host-side positions
  * (x, y interleaved; xy may be NULL).  Used by tests and tooling. */
 int f8_markers(f8_ctx *ctx, int *n_per_plane, double *xy);
@@ -260,10 +272,25 @@ enum f8_stage {
     F8_STAGE_PROJECT = 6,    /* projection, pressure update, boundary values     */
     F8_NSTAGE = 7
 };
+/* Kernels of the FP32-mixed step launched once per step, each bracketed by
+ * its own pair of CUDA events on its stream while timing is enabled: */
+enum f8_kernel {
+    F8_KERNEL_CODES = 0,       /* k_codes3_f: candidate faces + eigen test       */
+    F8_KERNEL_UPDATE = 1,      /* k_update3_f: Cstar + Newton + f(C)             */
+    F8_KERNEL_MOMENTUM = 2,    /* k_momentum3_f: stress, convection, viscous, RHS */
+    F8_KERNEL_POISSON_RHS = 3, /* k_poisson_rhs_df: div(U + dU)/dt               */
+    F8_KERNEL_DEFECT = 4,      /* k_defect_df: Poisson defect                    */
+    F8_KERNEL_MARCH = 5,       /* k_march_df: projection + pressure update       */
+    F8_NKERNEL = 6
+};
 int f8_set_timing(f8_ctx *ctx, int enable);
 int f8_timing(f8_ctx *ctx, double *total_ms, double *stage_ms /* F8_NSTAGE or NULL */,
               long long *steps_timed);
 int f8_timing_reset(f8_ctx *ctx);
+/* Accumulated device milliseconds of each enum f8_kernel launch (F8_NKERNEL
+ * doubles) and the number of steps they cover, since the last timing reset.
+ * FP32-mixed 3D contexts only (F8_ERR_UNSUPPORTED otherwise). */
+int f8_kernel_timing(f8_ctx *ctx, double *kernel_ms, long long *steps_timed);
 
 /* Stand-alone periodic spectral solve, the reference's fft_solve
  * (fenep.f90:1400-1428): phi = IFFT( FFT(q) / (nx ny nz) / LHS ) with
@@ -291,7 +318,15 @@ int f8_fft_solve(int nx, int ny, int nz, double lx, double ly, double lz,
  *     call overwrites what it reads, but calls that overlap on the GPU (from
  *     several threads or streams) race;
  *   - the first call on a device looks up the workspace address on that
- *     device (the device must be current); make it before any stream capture.
+ *     device (the device must be current); make it before any stream capture;
+ *   - with CUDA's lazy module loading, the fixed arrays are placed in device
+ *     memory when the library's device code is first used on that device,
+ *     which may be that first call: make the first call (or any other f8
+ *     call on that device) before the caller reserves the rest of the
+ *     device memory for its own pool;
+ *   - the looked-up address is kept for the life of the process; after a
+ *     cudaDeviceReset the library must be unloaded and loaded again before
+ *     this entry point is used on that device.
  * q and phi are caller-owned DEVICE buffers as for f8_fft_solve. */
 int f8_fft_solve_noalloc(int nx, int ny, int nz, double lx, double ly, double lz,
                          const double *q, double *phi, double lhs0, double lhs1);

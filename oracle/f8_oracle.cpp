@@ -72,6 +72,10 @@ struct OCtx {
     std::vector<double> kx2, ky2, kz2;  // modified wavenumbers 2(1-cos(m d))/d^2
     // diagnostics of the last step
     long long newton_iters = 0, newton_unconv = 0;
+    // SPD candidate choice of the last polymer update, one byte per updated
+    // cell [k][row][i]: bits 2d..2d+1 = candidate - 1 (0..2) or 3 for the cell
+    // value, direction d = x, y, z (fenep.f90:220-230, fenep_2d.f90:159-175)
+    std::vector<unsigned char> codes;
     // running statistics (f8o_stats_begin): sums of U, V, W or of squared
     // fluctuations, centre-line probes (component, step, k)
     int stats_mode = 0, stats_n = 0, stats_max = 0;
@@ -291,18 +295,21 @@ inline FaceIdx face_idx(const OCtx &c) {
 void polymer_faces3(OCtx &c) {
     const int NX = c.NX, NY = c.NY, NZ = c.NZ, jlo = prow_lo(c), jhi = prow_hi(c);
     const FaceIdx F = face_idx(c);
+    c.codes.assign((size_t)NX * F.nr * NZ, 0);
     const double *C = c.C.data();
 #pragma omp parallel for schedule(static)
     for (int k = 1; k <= NZ; ++k)
         for (int j = jlo; j <= jhi; ++j)
             for (int i = 1; i <= NX; ++i) {
                 const double *c0 = cval(c, C, 6, i, j, k);
-                reconstruct3(cval(c, C, 6, i - 1, j, k), c0, cval(c, C, 6, i + 1, j, k),
-                             &c.Cpx[F.x(i - 1, j, k)], &c.Cnx[F.x(i, j, k)]);
-                reconstruct3(cval(c, C, 6, i, j - 1, k), c0, cval(c, C, 6, i, j + 1, k),
-                             &c.Cpy[F.y(i, j - 1, k)], &c.Cny[F.y(i, j, k)]);
-                reconstruct3(cval(c, C, 6, i, j, k - 1), c0, cval(c, C, 6, i, j, k + 1),
-                             &c.Cpz[F.z(i, j, k - 1)], &c.Cnz[F.z(i, j, k)]);
+                const int ix = reconstruct3(cval(c, C, 6, i - 1, j, k), c0, cval(c, C, 6, i + 1, j, k),
+                                            &c.Cpx[F.x(i - 1, j, k)], &c.Cnx[F.x(i, j, k)]);
+                const int iy = reconstruct3(cval(c, C, 6, i, j - 1, k), c0, cval(c, C, 6, i, j + 1, k),
+                                            &c.Cpy[F.y(i, j - 1, k)], &c.Cny[F.y(i, j, k)]);
+                const int iz = reconstruct3(cval(c, C, 6, i, j, k - 1), c0, cval(c, C, 6, i, j, k + 1),
+                                            &c.Cpz[F.z(i, j, k - 1)], &c.Cnz[F.z(i, j, k)]);
+                c.codes[(size_t)(i - 1) + (size_t)NX * ((size_t)(j - jlo) + (size_t)F.nr * (k - 1))] =
+                    (unsigned char)((ix - 1) | ((iy - 1) << 2) | ((iz - 1) << 4));
             }
     // Periodic face copies (fenep.f90:240-241, 310-311, 380-381).  With walls
     // the faces beyond the ghost rows belong to the outside cells; Cstar
@@ -637,11 +644,15 @@ void polymer2(OCtx &c) {
     std::vector<double> Cpx(3 * (NX + 1) * nr), Cnx(3 * (NX + 1) * nr), Cpy(3 * NX * (nr + 1), 0.0), Cny(3 * NX * (nr + 1), 0.0);
     auto fx = [&](int f, int j) { return (size_t)3 * ((size_t)f + (size_t)(NX + 1) * (j - jlo)); };
     auto fy = [&](int i, int f) { return (size_t)3 * ((size_t)(i - 1) + (size_t)NX * (f - (jlo - 1))); };
+    c.codes.assign((size_t)NX * nr, 0);
     for (int j = jlo; j <= jhi; ++j)
         for (int i = 1; i <= NX; ++i) {
             const double *c0 = cp_(i, j);
-            reconstruct2(cp_(i - 1, j), c0, cp_(i + 1, j), &Cpx[fx(i - 1, j)], &Cnx[fx(i, j)]);
-            reconstruct2(cp_(i, j - 1), c0, cp_(i, j + 1), &Cpy[fy(i, j - 1)], &Cny[fy(i, j)]);
+            const int ix = reconstruct2(cp_(i - 1, j), c0, cp_(i + 1, j), &Cpx[fx(i - 1, j)], &Cnx[fx(i, j)]);
+            const int iy = reconstruct2(cp_(i, j - 1), c0, cp_(i, j + 1), &Cpy[fy(i, j - 1)], &Cny[fy(i, j)]);
+            // index 0 (no candidate qualified: the cell value) is stored as 3
+            c.codes[(size_t)(i - 1) + (size_t)NX * (j - jlo)] =
+                (unsigned char)((ix == 0 ? 3 : ix - 1) | ((iy == 0 ? 3 : iy - 1) << 2));
         }
     for (int j = jlo; j <= jhi; ++j)
         for (int m = 0; m < 3; ++m) {
@@ -1873,6 +1884,19 @@ int f8o_stats_read(f8_ctx *ctx, double *su, double *sv, double *sw, double *prob
                       c.stats_probe.begin() + (size_t)q * c.stats_max * c.NZ + (size_t)n * c.NZ,
                       probes + (size_t)q * n * c.NZ);
     if (nsteps) *nsteps = c.stats_n;
+    return F8_OK;
+}
+
+int f8o_kernel_timing(f8_ctx *ctx, double *kernel_ms, long long *steps_timed) {
+    (void)kernel_ms; (void)steps_timed;
+    return ctx ? F8_ERR_UNSUPPORTED : F8_ERR_ARG;   // no device kernels
+}
+
+int f8o_selection_codes(f8_ctx *ctx, unsigned char *codes) {
+    if (!ctx || !codes) return F8_ERR_ARG;
+    OCtx &c = *reinterpret_cast<OCtx *>(ctx);
+    if (c.codes.empty()) return F8_ERR_STATE;
+    std::memcpy(codes, c.codes.data(), c.codes.size());
     return F8_OK;
 }
 

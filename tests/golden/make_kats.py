@@ -15,7 +15,7 @@ them to kats.json so the tests run without the reference present:
                       repeated root makes Vieta's discriminant vanish and the
                       reference returns its -100 sentinel (fenep.f90:438-439)
 
-Usage: python tests/golden/make_kats.py [/path/to/reference]
+Usage: python tests/golden/make_kats.py <path of the reference checkout>
 """
 from __future__ import annotations
 
@@ -66,4 +66,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <path of the reference checkout>")
+    main(Path(sys.argv[1]))

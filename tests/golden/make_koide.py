@@ -22,7 +22,7 @@ The agreement also needs the reference's wall mode, in which the ghost rows
 of C are updated with the polymer step and extrapolated only at the end of
 the step (fenep_2d.f90:1371-1374, 1912-1966).
 
-Usage: python tests/golden/make_koide.py [/path/to/reference]
+Usage: python tests/golden/make_koide.py <path of the reference checkout>
 """
 from __future__ import annotations
 
@@ -49,4 +49,6 @@ def main(ref: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {Path(__file__).name} <path of the reference checkout>")
+    main(Path(sys.argv[1]))

@@ -57,6 +57,26 @@ def test_noalloc_matches_allocating_solve_twice(lib):
         assert np.max(np.abs(out - ref)) <= TOL * max(1.0, np.abs(ref).max())
 
 
+def test_noalloc_call_leaves_free_device_memory_unchanged(lib):
+    """After a first call, a call allocates nothing: the device's free memory
+    (cudaMemGetInfo) is the same before and after it."""
+    import torch
+    shape = (32, 64, 64)
+    q = np.random.default_rng(7).random(shape)
+    q -= q.mean()
+    qd = torch.from_numpy(q).cuda()
+    pd = torch.zeros_like(qd)
+    args = (64, 64, 32, 2 * np.pi, 2 * np.pi, 2 * np.pi, qd.data_ptr(), pd.data_ptr(), 0.0, -1.0)
+    assert lib.f8_fft_solve_noalloc(*args) == abi.F8_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert lib.f8_fft_solve_noalloc(*args) == abi.F8_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
 def test_noalloc_rejects_grids_beyond_its_workspace(lib):
     import torch
     qd = torch.zeros((64, 64, 64), dtype=torch.float64, device="cuda")   # 33*64*64 fits
