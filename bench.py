@@ -310,26 +310,36 @@ def run_ours(args, w):
     ms = max_over_ranks(ws, tot_ms)
     value = cells * args.steps * ws / (ms / 1e3) / 1e6
     # e2e: host arrays in, K single-step calls reading the drag every step, host
-    # arrays out; timed on the host clock, so the median of three repetitions
-    # (the host is shared)
+    # arrays out; timed on the host clock after one untimed repetition (which
+    # touches every page-locked buffer once), median of five (the host is
+    # shared).  The store leaves out the body force, an input the caller keeps.
     pst, _keep = pinned_state(st0)
     from fortran8_gb300.solver import empty_state
     pout, _keep_out = pinned_state(empty_state(w.grid))
-    reps = []
+    for f in ("fx", "fy", "fz"):
+        del pout.arrays[f]
+    reps, parts = [], []
     with Solver(fns, w.grid, w.phys, w.cyls, precision=prec, poisson=pois) as s:
         s.load(pst)
         s.step(args.warmup)
-        for _ in range(3):
+        for rep in range(6):
             torch.cuda.synchronize()
             barrier(ws)
             t0 = time.perf_counter()
             s.load(pst, step0=0)
+            t1 = time.perf_counter()
             for _ in range(args.steps):
                 s.step(1)
-            out = s.store(pout)
+            t2 = time.perf_counter()
+            s.store(pout)
             torch.cuda.synchronize()
-            reps.append(max_over_ranks(ws, time.perf_counter() - t0))
-    e2e_s = sorted(reps)[1]
+            t3 = time.perf_counter()
+            if rep > 0:
+                reps.append(max_over_ranks(ws, t3 - t0))
+                parts.append((t1 - t0, t2 - t1, t3 - t2))
+    e2e_s = sorted(reps)[len(reps) // 2]
+    e2e_parts = parts[reps.index(e2e_s)]
+    out_bytes = int(sum(a.nbytes for a in pout.arrays.values()))
     # the FP64 path on the same workload over the workload's whole horizon and
     # the per-field and drag differences (accuracy gate)
     cmp = None
@@ -338,13 +348,18 @@ def run_ours(args, w):
     adj = None
     if not args.no_adjoint:
         adj = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, args.adjoint_grid, args.adjoint_workload,
-                           args.adjoint_mixed_prefix)
+                           args.adjoint_mixed_prefix, args.adjoint_precision)
+        if args.adjoint_precision == "mixed" and not args.adjoint_grid:
+            # the same gradient in FP64 (the parity path), for its own ratio
+            adj["fp64"] = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, None, args.adjoint_workload,
+                                       0, "fp64")
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s", "repetitions": len(reps),
            "values": [cells * args.steps * ws / r / 1e6 for r in reps],
+           "median_rep_ms": {"load": e2e_parts[0] * 1e3, "steps": e2e_parts[1] * 1e3, "store": e2e_parts[2] * 1e3},
            "h2d_bytes_per_step": int(sb / args.steps),
-           "d2h_bytes_per_step": int(sb / args.steps + ncyl * 3 * 8 + 8)}
+           "d2h_bytes_per_step": int(out_bytes / args.steps + ncyl * 3 * 8 + 8)}
     if rank != 0:
         return 0
     # roofline of the dominant kernel: the single-launch kernel of the mixed
@@ -446,20 +461,23 @@ def fp64_compare(fns, w, pois, nsteps, mixed_value):
     return out
 
 
-def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_prefix=0):
+def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_prefix=0, precision="mixed"):
     """Cost of the gradient (f8_grad: forward with checkpoints, recomputation of
-    each segment, adjoint sweep) over that of the FP64 forward (f8_step).
+    each segment, adjoint sweep) over that of the forward (f8_step) in the
+    same precision.
 
     Default: the adjoint workload, a 128 x 64 x 64 channel with 2 cylinders,
     gradient of the time-averaged total drag w.r.t. Wi, beta, L^2 and the
-    centres.  With mixed_prefix > 0 the FP32-mixed step first advances the
-    seeded state that many steps (timed), and the adjoint window starts from
-    its state in an FP64 context.  Both timed calls are synchronous; they are
-    timed on the host clock after a warm-up call of each."""
+    centres, in FP32-mixed precision.  With mixed_prefix > 0 the FP32-mixed
+    step first advances the seeded state that many steps (timed), and the
+    gradient window starts from its state.  The forward and the gradient are
+    each timed by CUDA events on the default stream around one synchronous
+    call, after a warm-up call of each."""
     import torch
     w = configs.WORKLOADS[workload]()
     if grid:
         w = configs.scaled(w, *grid)
+    prec = {"fp64": abi.F8_FP64, "mixed": abi.F8_MIXED}[precision]
     st0 = configs.initial_state(w)
     step0 = 0
     pre = None
@@ -473,29 +491,36 @@ def adjoint_cost(fns, steps, every, grid=None, workload="c4_adjoint", mixed_pref
         step0 = mixed_prefix
         pre = {"mixed_steps": mixed_prefix, "mixed_ms_per_step": tms / mixed_prefix,
                "mixed_value": w.cells * mixed_prefix / (tms / 1e3) / 1e6}
-    with Solver(fns, w.grid, w.phys, w.cyls, precision=abi.F8_FP64) as s:
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    with Solver(fns, w.grid, w.phys, w.cyls, precision=prec) as s:
         s.load(st0, step0)
         s.step(2)
         s.load(st0, step0)
         s.grad(min(steps, 2 * every), every)
-        torch.cuda.synchronize()
         s.load(st0, step0)
-        t0 = time.perf_counter()
-        s.step(steps)
-        tf = time.perf_counter() - t0
+        _, tf = timed(lambda: s.step(steps))
         s.load(st0, step0)
-        t0 = time.perf_counter()
-        status, J, dp, _, _ = s.grad(steps, every)
-        tg = time.perf_counter() - t0
+        (status, J, dp, _, _), tg = timed(lambda: s.grad(steps, every))
     out = {"workload": w.name, "grid": [w.grid.nx, w.grid.ny, w.grid.nz], "cylinders": len(w.cyls),
-           "steps": steps, "checkpoint_every": every, "precision": "fp64", "step0": step0,
-           "forward_ms_per_step": tf * 1e3 / steps, "grad_ms_per_step": tg * 1e3 / steps,
+           "steps": steps, "checkpoint_every": every, "precision": precision, "step0": step0,
+           "forward_ms_per_step": tf / steps, "grad_ms_per_step": tg / steps,
            "adjoint_over_forward": tg / tf, "J": J,
            "dJ_dparams": {"wi": dp[0], "beta": dp[1], "lp2": dp[2], "centres": dp[3:].tolist()},
            "status": int(status)}
     if pre:
         out["mixed_prefix"] = pre
-        out["grad_over_mixed_forward"] = (tg / steps) / (pre["mixed_ms_per_step"] / 1e3)
+        out["grad_over_mixed_forward"] = (tg / steps) / pre["mixed_ms_per_step"]
+    elif precision == "mixed":
+        out["grad_over_mixed_forward"] = tg / tf
     return out
 
 
@@ -577,6 +602,8 @@ def main():
     ap.add_argument("--adjoint-workload", default="c4_adjoint", choices=sorted(configs.WORKLOADS))
     ap.add_argument("--adjoint-mixed-prefix", type=int, default=0,
                     help="FP32-mixed steps before the adjoint window (with --adjoint-only)")
+    ap.add_argument("--adjoint-precision", default="mixed", choices=["mixed", "fp64"],
+                    help="precision of the gradient whose cost is measured")
     ap.add_argument("--poisson", default="fft", choices=["fft", "sor"],
                     help="pressure solver: FFT + tridiagonal (default) or red-black SOR")
     ap.add_argument("--grid", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
@@ -599,7 +626,7 @@ def main():
         b.build()
         torch.cuda.set_device(0)
         print(json.dumps(adjoint_cost(flib.functions(), args.adjoint_steps, args.adjoint_every, args.adjoint_grid,
-                                      args.adjoint_workload, args.adjoint_mixed_prefix)))
+                                      args.adjoint_workload, args.adjoint_mixed_prefix, args.adjoint_precision)))
         return 0
     return run_ours(args, w)
 

@@ -28,6 +28,7 @@ UNITS = {
     "f8_fftsolve.cu": ["--fmad=false"],
     "f8_diag.cu": ["--fmad=false"],
     "f8_adjoint.cu": ["--fmad=false"],
+    "f8_adjoint_mixed.cu": [],
 }
 
 

@@ -88,6 +88,14 @@ struct GradMem {
     double *tUa = nullptr, *tUp = nullptr, *tPhi = nullptr, *tFc = nullptr, *tCm = nullptr;
     uint8_t *tcodes = nullptr, *tcodes_g = nullptr;
     double *ck = nullptr, *dw = nullptr;
+    // FP32-mixed contexts: adjoint fields, K tape slots of MIXED_TAPE_FIELDS
+    // halo fields each (plus codes and marker forces), checkpoints of the
+    // mixed state
+    AdjStateF AF{};
+    float *ftape = nullptr, *fck = nullptr;
+    uint8_t *fcodes = nullptr, *fcodes_g = nullptr;
+    double *fFc = nullptr;
+    size_t fck_slot = 0;                    // floats per mixed checkpoint
     template <typename T>
     cudaError_t get(int grp, T **p, size_t n) {
         void *q = nullptr;
@@ -1000,6 +1008,253 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
     return cudaSuccess;
 }
 
+// ---- FP32-mixed contexts --------------------------------------------------
+
+constexpr int MIXED_TAPE_FIELDS = 22;   // U V W, C (6), Cn (6), Ua (3), Up (3), Phi
+
+int grad_alloc_mixed(f8_ctx *c, int K, int nck, int nsteps) {
+    GradMem &G = c->gm;
+    Dev &d = c->d;
+    const size_t cs = d.cs, ni = d.ni, ncyl = c->cyl.size(), nfc = (size_t)d.nm * d.g.nz;
+    if (!G.AF.grad) {
+        AdjStateF &A = G.AF;
+        for (float **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(0, p, cs));
+        for (float **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(0, p, 6 * cs));
+        for (int q = 0; q < 3; ++q) {
+            API_CUDA(c, G.get(0, &A.lA0[q], ni));
+            API_CUDA(c, G.get(0, &A.lT0[q], ni));
+            API_CUDA(c, G.get(0, &A.lUa[q], cs));
+            API_CUDA(c, G.get(0, &A.lUp[q], cs));
+            API_CUDA(c, G.get(0, &A.lQ[q], cs));
+        }
+        API_CUDA(c, G.get(0, &A.pack, ni));
+        API_CUDA(c, G.get(0, &A.qlo, cs));
+        API_CUDA(c, G.get(0, &A.zero, ni));
+        API_CUDA(c, G.get(0, &A.rdef, ni));
+        API_CUDA(c, cudaMemsetAsync(A.zero, 0, ni * sizeof(float), c->s));
+        API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
+    }
+    if (K > G.K) {
+        G.free_group(1);
+        G.K = 0;
+        API_CUDA(c, G.get(1, &G.ftape, (size_t)K * MIXED_TAPE_FIELDS * cs));
+        API_CUDA(c, G.get(1, &G.fcodes, K * ni));
+        API_CUDA(c, G.get(1, &G.fcodes_g, K * 2 * (size_t)d.g.nx * d.g.nz));
+        API_CUDA(c, G.get(1, &G.fFc, 3 * K * std::max<size_t>(nfc, 1)));
+        G.K = K;
+    }
+    if (nck > G.nck) {
+        G.free_group(2);
+        G.nck = 0;
+        G.fck_slot = 15 * cs + 6 * ni;
+        API_CUDA(c, G.get(2, &G.fck, nck * G.fck_slot));
+        G.nck = nck;
+    }
+    if (nsteps > G.nsteps) {
+        G.free_group(3);
+        G.nsteps = 0;
+        API_CUDA(c, G.get(3, &G.dw, (size_t)nsteps * std::max<size_t>(ncyl, 1) * 3));
+        G.nsteps = nsteps;
+    }
+    return F8_OK;
+}
+
+// mixed state <-> checkpoint slot: the double-float velocity and pressure,
+// C and f(C) (halo), the AB2 histories
+cudaError_t ck_copy_mixed(f8_ctx *c, int slot, bool save) {
+    Dev &d = c->d;
+    GradMem &G = c->gm;
+    const size_t cs = d.cs, ni = d.ni;
+    float *base = G.fck + (size_t)slot * G.fck_slot;
+    float *f[16] = {d.Uf, d.Ul, d.Vf, d.Vl, d.Wf, d.Wl, d.Pf, d.Pl, d.Cf, d.fpetf,
+                    d.A0f[0], d.A0f[1], d.A0f[2], d.T0f[0], d.T0f[1], d.T0f[2]};
+    const size_t n[16] = {cs, cs, cs, cs, cs, cs, cs, cs, 6 * cs, cs, ni, ni, ni, ni, ni, ni};
+    size_t off = 0;
+    for (int q = 0; q < 16; ++q) {
+        const size_t b = n[q] * sizeof(float);
+        cudaError_t e = save ? cudaMemcpyAsync(base + off, f[q], b, cudaMemcpyDeviceToDevice, c->s)
+                             : cudaMemcpyAsync(f[q], base + off, b, cudaMemcpyDeviceToDevice, c->s);
+        if (e != cudaSuccess) return e;
+        off += n[q];
+    }
+    return cudaSuccess;
+}
+
+MixTape tape_slot_mixed(f8_ctx *c, int rec) {
+    GradMem &G = c->gm;
+    const size_t cs = c->d.cs, ni = c->d.ni, nfc = std::max<size_t>((size_t)c->d.nm * c->d.g.nz, 1);
+    float *b = G.ftape + (size_t)rec * MIXED_TAPE_FIELDS * cs;
+    MixTape t{};
+    t.U = b; t.V = b + cs; t.W = b + 2 * cs;
+    t.C = b + 3 * cs; t.Cn = b + 9 * cs;
+    for (int q = 0; q < 3; ++q) {
+        t.Ua[q] = b + (15 + q) * cs;
+        t.Up[q] = b + (18 + q) * cs;
+        t.Fc[q] = G.fFc + (3 * (size_t)rec + q) * nfc;
+    }
+    t.Phi = b + 21 * cs;
+    t.codes = G.fcodes + rec * ni;
+    t.codes_g = G.fcodes_g + rec * 2 * (size_t)c->d.g.nx * c->d.g.nz;
+    return t;
+}
+
+// one forward step of f8_grad on a mixed context (absolute step index s of
+// the call); rec >= 0 writes the tape of the step into segment slot rec
+cudaError_t grad_forward_step_mixed(f8_ctx *c, int step0, int s, int rec) {
+    Dev &d = c->d;
+    const int ncyl = (int)c->cyl.size();
+    StepOpts o{};
+    o.polymer = c->phys.beta != 1.0;
+    o.ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
+    o.ibm = ncyl > 0;
+    o.poisson = F8_POISSON_FFT;
+    if (!o.polymer) F8_CUDA_RET(cudaMemsetAsync(d.Cf, 0, (size_t)d.cs * d.ncomp * sizeof(float), c->s));
+    MixTape t{};
+    if (rec >= 0) {
+        t = tape_slot_mixed(c, rec);
+        o.tape = &t;
+    }
+    int sor = -1;
+    return step_mixed(d, o, ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr, &sor, c->s);
+}
+
+// f8_grad on an FP32-mixed 3D context with the FFT solvers: the same
+// checkpointed schedule as the FP64 gradient, with the mixed forward step
+// (its tape written by the step itself) and the FP32 adjoint step.
+int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed, double *J,
+               double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
+    Dev &d = c->d;
+    const int ncyl = (int)c->cyl.size();
+    const size_t cs = d.cs, ni = d.ni;
+    const int K = checkpoint_every == 0 ? nsteps : std::min(checkpoint_every, nsteps);
+    const int nseg = (nsteps + K - 1) / K;
+    if (int st = grad_alloc_mixed(c, K, nseg, nsteps)) return st;
+    if (int st = ensure_drag(c, nsteps)) return st;
+    GradMem &G = c->gm;
+    AdjStateF &A = G.AF;
+    const size_t nw = (size_t)nsteps * ncyl * 3;
+    std::vector<double> w(nw, 0.0);
+    if (drag_w) std::copy(drag_w, drag_w + nw, w.begin());
+    else
+        for (int n = 0; n < nsteps; ++n)
+            for (int l = 0; l < ncyl; ++l) w[((size_t)n * ncyl + l) * 3] = 1.0 / nsteps;
+    if (nw) API_CUDA(c, cudaMemcpyAsync(G.dw, w.data(), nw * sizeof(double), cudaMemcpyHostToDevice, c->s));
+    // the mixed step's counters are cumulative since the load; report this
+    // call's share
+    StepCounters cnt0{};
+    API_CUDA(c, cudaMemcpyAsync(&cnt0, d.cnt, sizeof(cnt0), cudaMemcpyDeviceToHost, c->s));
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    const int step0 = c->step;
+    // forward: checkpoints at the segment starts, the tape of the last segment
+    for (int seg = 0; seg < nseg; ++seg) {
+        const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
+        const bool last = seg == nseg - 1;
+        if (!last) API_CUDA(c, ck_copy_mixed(c, seg, true));
+        for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step_mixed(c, step0, s, last ? s - s0 : -1));
+    }
+    if (nseg > 1) API_CUDA(c, ck_copy_mixed(c, nseg - 1, true));   // final state
+    // adjoint of the final state
+    for (float *p : {A.lU, A.lV, A.lW, A.lP}) API_CUDA(c, cudaMemsetAsync(p, 0, cs * sizeof(float), c->s));
+    API_CUDA(c, cudaMemsetAsync(A.lC, 0, 6 * cs * sizeof(float), c->s));
+    for (int q = 0; q < 3; ++q) {
+        API_CUDA(c, cudaMemsetAsync(A.lA0[q], 0, ni * sizeof(float), c->s));
+        API_CUDA(c, cudaMemsetAsync(A.lT0[q], 0, ni * sizeof(float), c->s));
+    }
+    API_CUDA(c, cudaMemsetAsync(A.grad, 0, (3 + 2 * ncyl) * sizeof(double), c->s));
+    if (seed) {
+        // host FP64 -> device FP64 staging (the load buffers) -> FP32 interior
+        double *tmp = c->scratch_aos;   // 6 * cs doubles
+        const double *hs[4] = {seed->u, seed->v, seed->w, seed->p};
+        float *hd[4] = {A.lU, A.lV, A.lW, A.lP};
+        for (int q = 0; q < 4; ++q) {
+            if (!hs[q]) continue;
+            API_CUDA(c, cudaMemcpyAsync(tmp, hs[q], cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, d2f(tmp, A.lC2, (int)cs, c->s));
+            API_CUDA(c, take_interior_f(A.lC2, hd[q], d.g, (int)cs, c->s));
+        }
+        if (seed->c) {
+            API_CUDA(c, cudaMemcpyAsync(tmp, seed->c, 6 * cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, aos_to_soa_f(tmp, A.lC2, 6, (int)cs, c->s));
+            API_CUDA(c, take_interior_f(A.lC2, A.lC, d.g, (int)(6 * cs), c->s));
+        }
+        const double *is[6] = {seed->ax0, seed->ay0, seed->az0, seed->tx0, seed->ty0, seed->tz0};
+        float *id[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};
+        for (int q = 0; q < 6; ++q) {
+            if (!is[q]) continue;
+            API_CUDA(c, cudaMemcpyAsync(tmp, is[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, d2f(tmp, id[q], (int)ni, c->s));
+        }
+        API_CUDA(c, cudaStreamSynchronize(c->s));
+    }
+    // reverse sweep over the segments
+    const bool polymer = c->phys.beta != 1.0;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
+        if (seg != nseg - 1) {
+            API_CUDA(c, ck_copy_mixed(c, seg, false));
+            for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step_mixed(c, step0, s, s - s0));
+        }
+        for (int s = s1 - 1; s >= s0; --s) {
+            const MixTape t = tape_slot_mixed(c, s - s0);
+            const bool ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
+            API_CUDA(c, step_mixed_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
+        }
+    }
+    if (nseg > 1) API_CUDA(c, ck_copy_mixed(c, nseg - 1, false));
+    c->step = step0 + nsteps;
+    // results
+    std::vector<double> hd((size_t)std::max<size_t>(nw, 1));
+    if (nw) API_CUDA(c, cudaMemcpyAsync(hd.data(), c->drag_dev, nw * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    std::vector<double> gr(3 + 2 * ncyl);
+    API_CUDA(c, cudaMemcpyAsync(gr.data(), A.grad, gr.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    StepCounters cnt{};
+    API_CUDA(c, cudaMemcpyAsync(&cnt, d.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, c->s));
+    if (dJ_dstate) {
+        auto get = [&](double *dst, const float *src, size_t n) -> cudaError_t {
+            if (!dst) return cudaSuccess;
+            cudaError_t e = f2d(src, c->scratch_aos, (int)n, c->s);
+            if (e != cudaSuccess) return e;
+            e = cudaMemcpyAsync(dst, c->scratch_aos, n * sizeof(double), cudaMemcpyDeviceToHost, c->s);
+            if (e != cudaSuccess) return e;
+            return cudaStreamSynchronize(c->s);   // the staging buffer is reused
+        };
+        API_CUDA(c, get(dJ_dstate->u, A.lU, cs));
+        API_CUDA(c, get(dJ_dstate->v, A.lV, cs));
+        API_CUDA(c, get(dJ_dstate->w, A.lW, cs));
+        API_CUDA(c, get(dJ_dstate->p, A.lP, cs));
+        if (dJ_dstate->c) {
+            API_CUDA(c, soa_to_aos_f(A.lC, c->scratch_aos, 6, (int)cs, c->s));
+            API_CUDA(c, cudaMemcpyAsync(dJ_dstate->c, c->scratch_aos, 6 * cs * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->s));
+            API_CUDA(c, cudaStreamSynchronize(c->s));
+        }
+        double *od[6] = {dJ_dstate->ax0, dJ_dstate->ay0, dJ_dstate->az0, dJ_dstate->tx0, dJ_dstate->ty0, dJ_dstate->tz0};
+        const float *os[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};
+        for (int q = 0; q < 6; ++q) API_CUDA(c, get(od[q], os[q], ni));
+    }
+    API_CUDA(c, cudaStreamSynchronize(c->s));
+    if (dJ_dstate) {
+        if (dJ_dstate->phi) std::fill(dJ_dstate->phi, dJ_dstate->phi + cs, 0.0);
+        for (double *p : {dJ_dstate->fx, dJ_dstate->fy, dJ_dstate->fz})
+            if (p) std::fill(p, p + ni, 0.0);
+    }
+    if (J) {
+        double sum = 0.0;
+        for (size_t q = 0; q < nw; ++q) sum += w[q] * hd[q];
+        *J = sum;
+    }
+    if (drag && nw) std::copy(hd.begin(), hd.begin() + nw, drag);
+    if (dJ_dparams) std::copy(gr.begin(), gr.end(), dJ_dparams);
+    const StepCounters dc{cnt.newton_iters - cnt0.newton_iters, cnt.newton_unconverged - cnt0.newton_unconverged,
+                          cnt.nan_cells - cnt0.nan_cells};
+    c->cnt_prev = cnt;
+    c->last_newton_iters = (long long)dc.newton_iters;
+    c->last_newton_unconv = (long long)dc.newton_unconverged;
+    if (dc.nan_cells) return F8_ERR_NAN;
+    if (dc.newton_unconverged) return F8_WARN_NEWTON;
+    return F8_OK;
+}
+
 TapeStep tape_step(f8_ctx *c, int rec) {
     GradMem &G = c->gm;
     const size_t cs = c->d.cs, ni = c->d.ni, nfc = (size_t)c->d.nm * c->d.g.nz;
@@ -1025,7 +1280,8 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
             double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
-    if (c->precision != F8_FP64 || c->grid.dim != 3 || c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
+    if (c->grid.dim != 3 || c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
+    if (c->precision == F8_MIXED) return grad_mixed(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
     Dev &d = c->d;
     const int ncyl = (int)c->cyl.size();
     const size_t cs = d.cs, ni = d.ni;

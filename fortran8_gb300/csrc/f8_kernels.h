@@ -79,6 +79,20 @@ struct Dev {
     StepCounters *cnt;
 };
 
+// Fields of one FP32-mixed step that the reverse of that step reads (the
+// tape), written by step_mixed when StepOpts::tape is set.  Halo fields
+// carry the boundary values the forward kernels read there.
+struct MixTape {
+    float *U, *V, *W;        // velocity (hi parts) at the start of the step
+    float *C;                // C at the start of the step (6 SoA halo fields)
+    float *Cn;               // C after the update as the stress read it (6 fields)
+    uint8_t *codes, *codes_g;
+    float *Ua[3];            // explicit velocity U^n + dt R (halo, boundary values)
+    float *Up[3];            // Helmholtz solutions U^n + dU (halo)
+    float *Phi;              // pressure correction (hi part, halo)
+    double *Fc[3];           // marker forces (nm * nz each)
+};
+
 struct StepOpts {
     bool polymer;      // beta != 1
     bool ab2_first;    // this step copies A->A0, T->T0 first
@@ -89,6 +103,7 @@ struct StepOpts {
     cudaEvent_t *ev;   // NSTAGE+1 events recorded at the stage boundaries, or null
     cudaEvent_t *kev;  // 2*NKERNEL events bracketing the single-launch kernels (f8_kernel), or null
     double *c_mid;     // FP64: receives C as the momentum stage read it (6 halo fields), or null
+    const MixTape *tape;   // FP32-mixed: tape of this step, or null
 };
 constexpr int NSTAGE = 7;
 constexpr int NKERNEL = 6;   // enum f8_kernel
@@ -176,6 +191,28 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
 cudaError_t adjoint_fold_state(AdjState &A, const Dev &d, cudaStream_t s);
 // dst[q] = src[q] on interior cells of n / cs stacked halo fields, 0 on halo cells
 cudaError_t take_interior(const double *src, double *dst, const Geo &g, int n, cudaStream_t s);
+// Discrete adjoint of the FP32-mixed 3D step (f8_adjoint_mixed.cu): the same
+// stage transposes as the FP64 adjoint in FP32, reading a MixTape.
+struct AdjStateF {
+    float *lU, *lV, *lW, *lP, *lPhi;
+    float *lC, *lC2, *lC0;
+    float *lA0[3], *lT0[3];
+    float *lUa[3], *lUp[3], *lQ[3];
+    float *pack;
+    float *qlo;              // low part of the refined pressure adjoint (halo, with lQ[0] its high part)
+    float *zero, *rdef;      // interior: zeros (the right-hand side's low part), the defect
+    double *grad;
+};
+// FP32 solves of the mixed step (f8_step_mixed.cu); mode 0 writes dst, mode 2
+// adds the solution to the pair (dst, lo) exactly; sys: 0 U/W, 1 V, 2 P
+cudaError_t mixed_solve_periodic(Dev &d, const float *src, float *dst, float *lo, int mode, double lhs0, double lhs1,
+                                 cudaStream_t s);
+cudaError_t mixed_solve_walls(Dev &d, const float *src, float *dst, float *lo, int mode, int sys, cudaStream_t s);
+cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float *rl, float *rd, cudaStream_t s);
+cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const double *drag_w, bool ab2_first,
+                               bool polymer, cudaStream_t s);
+cudaError_t adjoint_fold_state_f(AdjStateF &A, const Dev &d, cudaStream_t s);
+cudaError_t take_interior_f(const float *src, float *dst, const Geo &g, int n, cudaStream_t s);
 // Mixed path (f8_step_mixed.cu)
 cudaError_t init_kernels_mixed();
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s);

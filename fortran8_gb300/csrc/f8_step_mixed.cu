@@ -1537,6 +1537,29 @@ cudaError_t sor_solve_m(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
 
 }  // namespace
 
+// FP32 solves of the mixed step for the discrete adjoint (f8_adjoint_mixed.cu):
+// the periodic spectral solve with LHS = lhs0 + lhs1 k~^2, or the wall system
+// sys (0 U/W Helmholtz, 1 V Helmholtz, 2 pressure).  mode 0: dst = v at the
+// interior cells (and the wall ghost rows); mode 2: (dst, lo) = dst + v as an
+// exact two-sum (the correction of a double-float pair).
+cudaError_t mixed_solve_periodic(Dev &d, const float *src, float *dst, float *lo, int mode, double lhs0, double lhs1,
+                                 cudaStream_t s) {
+    return solve_periodic_f(d, src, XOutF{dst, lo, mode}, lhs0, lhs1, s);
+}
+
+cudaError_t mixed_solve_walls(Dev &d, const float *src, float *dst, float *lo, int mode, int sys, cudaStream_t s) {
+    return solve_walls_f(d, src, XOutF{dst, lo, mode}, sys, s);
+}
+
+// defect rd = (rh + rl) - L_h phi of an FP32 pressure-type field in df64, the
+// operator of the mixed step's Poisson solve (interior arrays rh, rl, rd)
+cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float *rl, float *rd, cudaStream_t s) {
+    const Geo &g = d.g;
+    const dim3 pblk(32, 8), pgrid((g.nx + pblk.x - 1) / pblk.x, (g.ny + pblk.y - 1) / pblk.y, (g.nz + 1) / 2);
+    k_defect_df<<<pgrid, pblk, 0, s>>>(phi, rh, rl, rd, g, make_const(g, d.ph)); count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t init_kernels_mixed() {
     const int big = 200 * 1024;
     F8_CUDA_RET(cudaFuncSetAttribute(k_fft_lines<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -1653,6 +1676,48 @@ cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cu
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Tape of the discrete adjoint (MixTape): halo fields over the whole halo box
+// with the values the forward kernels read at each position.
+
+// Ua = U^n + dt R with the boundary values of ua_at (the IBM's explicit velocity)
+__global__ void k_tape_ua(const float *__restrict__ Uh, const float *__restrict__ Ul, const float *__restrict__ Vh,
+                          const float *__restrict__ Vl, const float *__restrict__ Wh, const float *__restrict__ Wl,
+                          const float *__restrict__ Qu, const float *__restrict__ Qv, const float *__restrict__ Qw,
+                          float *__restrict__ ou, float *__restrict__ ov, float *__restrict__ ow, Geo g, df uw2) {
+    const int cs = g.sx * g.sy * g.sz;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cs) return;
+    const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
+    const df a = ua_at(g, Uh, Ul, Qu, 0, i, j, k, uw2);
+    const df b = ua_at(g, Vh, Vl, Qv, 1, i, j, k, uw2);
+    const df c = ua_at(g, Wh, Wl, Qw, 2, i, j, k, uw2);
+    ou[t] = a.hi + a.lo;
+    ov[t] = b.hi + b.lo;
+    ow[t] = c.hi + c.lo;
+}
+
+// U* = U^n + dU: the increments have no halo pass; their readers wrap x and z
+// (and y when periodic), and the wall solves write the ghost rows
+__global__ void k_tape_up(const float *__restrict__ U, const float *__restrict__ D, float *__restrict__ out, Geo g) {
+    const int cs = g.sx * g.sy * g.sz;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cs) return;
+    const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
+    const int jj = g.walls ? j : wrapy(g, j);
+    out[t] = U[t] + D[hix(g, wrapx(g, i), jj, wrapz(g, k))];
+}
+
+// Phi (hi part) with the periodic wrap and the Neumann copy at the walls
+__global__ void k_tape_phi(const float *__restrict__ Phi, float *__restrict__ out, Geo g) {
+    const int cs = g.sx * g.sy * g.sz;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cs) return;
+    const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
+    const int jj = g.walls ? max(1, min(g.ny, j)) : wrapy(g, j);
+    out[t] = Phi[hix(g, wrapx(g, i), jj, wrapz(g, k))];
+}
+
 cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_iters, cudaStream_t s) {
     const Geo &g = d.g;
     cudaError_t e;
@@ -1661,6 +1726,15 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     // events bracketing one kernel launch (enum f8_kernel), on its stream
     auto kmark = [&](int kq, int edge) { if (o.kev) cudaEventRecord(o.kev[2 * kq + edge], s); };
     const DfF U{d.Uf, d.Ul}, V{d.Vf, d.Vl}, W{d.Wf, d.Wl}, P{d.Pf, d.Pl}, Phi{d.Phif, d.Phil};
+    const MixTape *tp = o.tape;
+    const size_t hbf = (size_t)d.cs * sizeof(float);
+    const unsigned tnb = (unsigned)((d.cs + 255) / 256);
+    if (tp) {
+        F8_CUDA_RET(cudaMemcpyAsync(tp->U, d.Uf, hbf, cudaMemcpyDeviceToDevice, s));
+        F8_CUDA_RET(cudaMemcpyAsync(tp->V, d.Vf, hbf, cudaMemcpyDeviceToDevice, s));
+        F8_CUDA_RET(cudaMemcpyAsync(tp->W, d.Wf, hbf, cudaMemcpyDeviceToDevice, s));
+        if (o.polymer) F8_CUDA_RET(cudaMemcpyAsync(tp->C, d.Cf, 6 * hbf, cudaMemcpyDeviceToDevice, s));
+    }
     mark(0);
     // wall channel: the ghost rows' codes and update run on a side stream
     // beside the interior kernels (they read the state and the interior codes
@@ -1705,6 +1779,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             std::swap(d.Cf, d.Cnf);
             k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
         }
+        if (tp) F8_CUDA_RET(cudaMemcpyAsync(tp->Cn, d.Cf, 6 * hbf, cudaMemcpyDeviceToDevice, s));
         if ((e = cudaGetLastError())) return e;
     } else {
         kmark(F8_KERNEL_CODES, 0); kmark(F8_KERNEL_CODES, 1);
@@ -1741,6 +1816,10 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         }
         k_extrap_ghost_f<<<(ng + 255) / 256, 256, 0, sg>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
     }
+    if (tp) {
+        k_tape_ua<<<tnb, 256, 0, s>>>(d.Uf, d.Ul, d.Vf, d.Vl, d.Wf, d.Wl, d.Qf[0], d.Qf[1], d.Qf[2], tp->Ua[0],
+                                      tp->Ua[1], tp->Ua[2], g, df_from_d(2.0 * g.uwall)); count_launch();
+    }
     mark(3);
     if (o.ibm) {
         IbmArgsF a{};
@@ -1772,6 +1851,10 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
         if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
         if ((e = cudaGetLastError())) return e;
+        if (tp)
+            for (int c = 0; c < 3; ++c)
+                F8_CUDA_RET(cudaMemcpyAsync(tp->Fc[c], d.Fc[c], (size_t)d.nm * g.nz * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, s));
     }
     mark(4);
     // Helmholtz solves for the FP32 increments dU (U* = U^n + dU).  On the
@@ -1805,6 +1888,10 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_join[b], 0));
         }
     }
+    if (tp) {
+        const float *uh[3] = {d.Uf, d.Vf, d.Wf};
+        for (int c = 0; c < 3; ++c) { k_tape_up<<<tnb, 256, 0, s>>>(uh[c], d.dUf[c], tp->Up[c], g); count_launch(); }
+    }
     mark(5);
     // Poisson: FP32 solve + one df64 defect correction.  The increments and
     // Phi get no halo pass: their readers wrap / apply the Neumann rule.
@@ -1833,6 +1920,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         else e = solve_walls_f(d, d.Rdf, out, SYS_P, s);
         if (e) return e;
     }
+    if (tp) { k_tape_phi<<<tnb, 256, 0, s>>>(d.Phif, tp->Phi, g); count_launch(); }
     mark(6);
     kmark(F8_KERNEL_MARCH, 0);
     k_march_df<<<pgrid, pblk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
@@ -1843,6 +1931,11 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         // join the ghost-row branch (when the Helmholtz branches did not)
         F8_CUDA_RET(cudaEventRecord(d.ev_g[2], sg));
         F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_g[2], 0));
+    }
+    if (tp && o.polymer) {
+        F8_CUDA_RET(cudaMemcpyAsync(tp->codes, d.codes, (size_t)d.ni, cudaMemcpyDeviceToDevice, s));
+        if (g.walls)
+            F8_CUDA_RET(cudaMemcpyAsync(tp->codes_g, d.codes_g, (size_t)2 * g.nx * g.nz, cudaMemcpyDeviceToDevice, s));
     }
     mark(7);
     return cudaGetLastError();

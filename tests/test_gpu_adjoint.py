@@ -9,10 +9,11 @@
   state give the adjoint of the initial state and the parameters to 1e-8.
 * Checkpointing: every checkpoint interval gives the same gradient, and the
   state f8_grad leaves equals f8_step's bit for bit.
-* Central differences of the GPU forward (h = 1e-4) agree with the adjoint to
-  1e-4 relative: on a 32 x 16 x 16 channel over 3 steps, and on the adjoint
-  workload itself, the 128 x 64 x 64 channel with two cylinders from its
-  seeded initial state, over 400 steps with a checkpoint every 20 steps.
+* Central differences of the GPU forward agree with the adjoint: on a
+  32 x 16 x 16 channel over 3 steps (h = 1e-4, within 1e-4), and on the
+  adjoint workload itself, the 128 x 64 x 64 channel with two cylinders from
+  its seeded initial state, over 400 steps with a checkpoint every 20 steps
+  (relative steps; see the two workload tests for the tolerances).
 """
 from __future__ import annotations
 
@@ -124,27 +125,13 @@ def test_grad_matches_gpu_central_differences(gpu, oracle):
         assert abs(dp[q] - fd) <= 1e-4 * abs(fd) + 1e-8, (q, dp[q], fd)
 
 
-def test_grad_adjoint_workload_matches_central_differences(gpu):
-    """The 128 x 64 x 64 channel with 2 cylinders (r = 0.3), Re 300, Wi 3,
-    beta 0.85, L^2 400, dt 5e-4, from its seeded initial state (seed 3, C = I):
-    the gradient of the drag averaged over 400 steps, with a checkpoint every
-    20 steps, against FP64 central differences with h = 1e-4 on each of Wi,
-    beta, L^2 and the four centre coordinates (14 perturbed forward runs).
-    The centres are moved off the grid lines by a fraction of a cell so that no
-    marker sits on a break point of the Roma kernel, where the drag is only once
-    differentiable and central differences lose an order."""
-    from dataclasses import replace
-    from fortran8_gb300 import configs
-    w = configs.c4_adjoint()
-    assert (w.grid.nx, w.grid.ny, w.grid.nz, w.steps) == (128, 64, 64, 400)
-    w = replace(w, cyls=tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls))
-    st = configs.initial_state(w)
-    n, K = w.steps, 20
-    J, dp, _, _, _ = gpu_grad(gpu, w, st, 0, n, K=K)
+def _workload_fd(gpu, w, st, n, qs_rel):
+    """Central differences of the mean x drag over n steps from st, with the
+    relative step h_q = rel * |p_q| for each parameter index q in qs_rel."""
     base = param_vector(w)
-    h = 1e-4
-    fds = []
-    for q in range(len(base)):
+    fds = {}
+    for q, rel in qs_rel.items():
+        h = rel * max(abs(base[q]), 1.0)
         vals = []
         for sgn in (1, -1):
             b = base.copy()
@@ -154,11 +141,60 @@ def test_grad_adjoint_workload_matches_central_differences(gpu):
                 s.load(st, 0)
                 _, drag = s.step(n)
             vals.append(drag[:, :, 0].sum() / n)
-        fds.append((vals[0] - vals[1]) / (2 * h))
+        fds[q] = (vals[0] - vals[1]) / (2 * h)
+    return fds
+
+
+def _adjoint_workload(beta=None):
+    from dataclasses import replace
+    from fortran8_gb300 import configs
+    w = configs.c4_adjoint()
+    assert (w.grid.nx, w.grid.ny, w.grid.nz, w.steps) == (128, 64, 64, 400)
+    w = replace(w, cyls=tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls))
+    if beta is not None:
+        w = replace(w, phys=replace(w.phys, beta=beta))
+    return w, configs.initial_state(w)
+
+
+def test_grad_adjoint_workload_matches_central_differences(gpu):
+    """The 128 x 64 x 64 channel with 2 cylinders (r = 0.3), Re 300, Wi 3,
+    beta 0.85, L^2 400, dt 5e-4, from its seeded initial state (seed 3, C = I):
+    the gradient of the drag averaged over 400 steps, with a checkpoint every
+    20 steps, against FP64 central differences (14 perturbed forward runs).
+
+    The steps are relative, because the parameters differ in scale by 10^3
+    (beta 0.85, L^2 400): h = 1e-4 |p| for Wi, beta and L^2, within 1e-4 (plus
+    1e-10 absolute for L^2, whose sensitivity of ~6e-8 moves the differenced
+    drag by ~1e-10 of J).  The centre differences need h = 1e-5 |p|: the Roma
+    kernel is only C^1, and at h = 1e-4 their own truncation error is ~1e-3
+    (the Newtonian test below shows it vanishing as h decreases).  At that
+    step the perturbed runs of this 400-step FENE-P flow also differ in some
+    SPD face-candidate choices (a discontinuous function of C whose derivative
+    the adjoint takes as zero), which moves the differences by ~2e-4, so the
+    centres are held to 1e-3 here and to 1e-4 in the Newtonian test.
+    The centres are moved off the grid lines by a fraction of a cell so that no
+    marker sits on a break point of the Roma kernel."""
+    w, st = _adjoint_workload()
+    n, K = w.steps, 20
+    J, dp, _, _, _ = gpu_grad(gpu, w, st, 0, n, K=K)
+    fds = _workload_fd(gpu, w, st, n, {0: 1e-4, 1: 1e-4, 2: 1e-4, 3: 1e-5, 4: 1e-5, 5: 1e-5, 6: 1e-5})
     print("adjoint", list(dp), "central differences", fds)
-    for q, fd in enumerate(fds):
-        # the absolute term covers round-off of the differenced drag (~1e-13 / 2h)
-        assert abs(dp[q] - fd) <= 1e-4 * abs(fd) + 1e-8, (q, dp[q], fd)
+    for q, fd in fds.items():
+        tol = 1e-4 if q < 3 else 1e-3
+        assert abs(dp[q] - fd) <= tol * abs(fd) + 1e-10, (q, dp[q], fd)
+
+
+def test_grad_newtonian_adjoint_workload_matches_central_differences(gpu):
+    """The same workload with beta = 1 (no polymer stage, hence no candidate
+    choice): beta and the centre gradients over 400 steps within 1e-4 of
+    central differences with h = 1e-4 |beta| and 1e-5 |centre|."""
+    w, st = _adjoint_workload(beta=1.0)
+    n, K = w.steps, 20
+    J, dp, _, _, _ = gpu_grad(gpu, w, st, 0, n, K=K)
+    fds = _workload_fd(gpu, w, st, n, {1: 1e-4, 3: 1e-5, 4: 1e-5, 5: 1e-5, 6: 1e-5})
+    print("adjoint", list(dp), "central differences", fds)
+    for q, fd in fds.items():
+        assert abs(dp[q] - fd) <= 1e-4 * abs(fd), (q, dp[q], fd)
 
 
 def test_autograd_function_returns_the_adjoint_gradient(gpu, oracle):
