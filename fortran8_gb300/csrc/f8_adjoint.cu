@@ -39,9 +39,6 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
     k_pack<double><<<adj_cells(g, blk), blk, 0, s>>>(A.lPhi, A.pack, g); count_launch();
     F8_CUDA_RET(poisson_solve_fp64(d, A.pack, A.lQ[0], s));
     k_div_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lQ[0], A.lUp[0], A.lUp[1], A.lUp[2], g); count_launch();
-    F8_CUDA_RET(cudaMemsetAsync(A.lU, 0, hb, s));
-    F8_CUDA_RET(cudaMemsetAsync(A.lV, 0, hb, s));
-    F8_CUDA_RET(cudaMemsetAsync(A.lW, 0, hb, s));
     F8_CUDA_RET(fold(fold_set<double>({{A.lUp[0], BC_U}, {A.lUp[1], BC_V}, {A.lUp[2], BC_W}}), g, s));
     // 4. Helmholtz
     for (int c = 0; c < 3; ++c) {
@@ -62,8 +59,8 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
         k_ibm_adj<double><<<dim3((d.nm + 127) / 128, g.nz, 3), 128, 0, s>>>(ia, g); count_launch();
         F8_CUDA_RET(fold(fold_set<double>({{A.lUa[0], BC_U}, {A.lUa[1], BC_V}, {A.lUa[2], BC_W}}), g, s));
     }
-    // 2. momentum right-hand side
-    if (polymer) F8_CUDA_RET(cudaMemsetAsync(A.lC0, 0, 6 * hb, s));
+    // 2. momentum right-hand side: per-cell sources, then the gather of the
+    // velocity, pressure and (with the polymer) C0 / C adjoints
     {
         MomAdjArgs<double> ma{};
         ma.U = t.U; ma.V = t.V; ma.W = t.W;
@@ -71,27 +68,36 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
             ma.Up[c] = t.Up[c]; ma.lQ[c] = A.lQ[c]; ma.lUa[c] = A.lUa[c];
             ma.lA0[c] = A.lA0[c]; ma.lT0[c] = A.lT0[c];
         }
-        ma.lU = A.lU; ma.lV = A.lV; ma.lW = A.lW; ma.lP = A.lP; ma.lC0 = A.lC0;
         ma.cs = cs; ma.ab2_first = ab2_first ? 1 : 0; ma.polymer = polymer ? 1 : 0;
-        ma.vis = beta / re; ma.coef_t = (1.0 - beta) / (re * wi); ma.c_helm = dt / (2.0 * re); ma.inv_re = 1.0 / re;
+        ma.vis = beta / re; ma.coef_t = (1.0 - beta) / (re * wi);
+        ma.c_helm = dt / (2.0 * re); ma.inv_re = 1.0 / re;
         ma.grad = A.grad;
-        k_momentum_adj<double><<<adj_cells(g, blk), blk, 0, s>>>(ma, g); count_launch();
+        k_momadj_src<double><<<adj_cells(g, blk), blk, 0, s>>>(ma, A.work, g); count_launch();
+        MomGatherArgs<double> mg{};
+        mg.U = t.U; mg.V = t.V; mg.W = t.W; mg.src = A.work;
+        mg.lU = A.lU; mg.lV = A.lV; mg.lW = A.lW; mg.lP = A.lP; mg.C = t.Cn; mg.lC = A.lC;
+        mg.cs = cs; mg.polymer = polymer ? 1 : 0;
+        mg.lp2 = d.ph.lp2; mg.inv_1mb = 1.0 / (1.0 - beta); mg.inv_wi = 1.0 / wi;
+        mg.grad = A.grad;
+        k_momadj_gather<double><<<nb, 256, 0, s>>>(mg, g); count_launch();
     }
-    // 1. polymer
+    // 1. polymer: per-cell implicit-function adjoint and Cstar weights, then
+    // the gather of the adjoint of C^n and of the velocity
     if (polymer) {
-        k_c0_adj<double><<<nb, 256, 0, s>>>(t.Cn, A.lC0, A.lC, cs, d.ph.lp2, 1.0 / (1.0 - beta), 1.0 / wi, A.grad); count_launch();
         // with walls the stress read the updated ghost rows and their x/z
         // copies; the state's C (wall-extrapolated) adjoint is interior already
         if (g.walls) F8_CUDA_RET(fold_xz(fold_c(A.lC, cs), g, s));
         else F8_CUDA_RET(fold(fold_c(A.lC, cs), g, s));
-        F8_CUDA_RET(cudaMemsetAsync(A.lC2, 0, 6 * hb, s));
         PolyAdjArgs<double> pa{};
         pa.C = t.C; pa.Cn = t.Cn; pa.codes = t.codes; pa.codes_g = t.codes_g; pa.U = t.U; pa.V = t.V; pa.W = t.W;
-        pa.lX = A.lC; pa.lC = A.lC2; pa.lU = A.lU; pa.lV = A.lV; pa.lW = A.lW;
+        pa.lX = A.lC;
         pa.cs = cs; pa.dt = dt; pa.wi = wi; pa.lp2 = d.ph.lp2; pa.grad = A.grad;
         dim3 pb(32, 4);
         const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
-        k_polymer_adj3<double><<<pg, pb, 0, s>>>(pa, g); count_launch();
+        k_polyadj_src<double><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
+        PolyGatherArgs<double> pga{};
+        pga.src = A.work; pga.lC = A.lC2; pga.lU = A.lU; pga.lV = A.lV; pga.lW = A.lW; pga.cs = cs;
+        k_polyadj_gather<double><<<nb, 256, 0, s>>>(pga, g); count_launch();
         std::swap(A.lC, A.lC2);
     } else {
         F8_CUDA_RET(cudaMemsetAsync(A.lC, 0, 6 * hb, s));

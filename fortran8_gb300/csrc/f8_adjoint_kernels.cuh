@@ -15,8 +15,8 @@
 //   divergence                     k_div_adj
 //   Helmholtz solves               (1430-1527) the forward solves again
 //   IBM direct forcing             (fenep_mpi.f90:1794-1929)   k_ibm_adj
-//   momentum right-hand side       (fenep.f90:645-770, 1469)   k_momentum_adj, k_c0_adj
-//   Lyapunov Newton + Cstar        (fenep.f90:464-643)         k_polymer_adj3
+//   momentum right-hand side       (fenep.f90:645-770, 1469)   k_momadj_src, k_momadj_gather
+//   Lyapunov Newton + Cstar        (fenep.f90:464-643)         k_polyadj_src, k_polyadj_gather
 // Halo fills (fenep.f90:147-166, fenep_2d.f90:1098-1143) are linear maps of
 // the interior; their transposes (k_fold_*) move the adjoint gathered on halo
 // cells back to the interior cells they were copied from.
@@ -27,8 +27,11 @@
 // is differentiated by the implicit-function theorem with the exact 6x6
 // Jacobian at C*; d|u|/du = sign(u), 0 at 0.
 //
-// Stencil transposes scatter with atomics into full halo arrays, so the
-// adjoint fields are reproducible to round-off, not bit for bit.
+// The momentum and polymer transposes are gathers (each position sums, in a
+// fixed order, the contributions of the cells whose stencils read it); the
+// IBM transpose scatters with atomics onto the few stencil cells of the
+// markers, and the parameter gradient is a sum of per-block partials added
+// atomically, so the gradient is reproducible to round-off.
 #pragma once
 #include <initializer_list>
 #include <utility>
@@ -375,258 +378,11 @@ struct MomAdjArgs {
     const T *lQ[3];                   // adjoint of Q (interior of halo arrays)
     const T *lUa[3];                  // adjoint of Ua from the interpolation (interior)
     T *lA0[3], *lT0[3];               // in: adjoint of the new history; out: of the old
-    T *lU, *lV, *lW, *lP;             // scattered adjoint of U^n, P^n (full halo box)
-    T *lC0;                           // scattered adjoint of C0 = f C - I (6 x full halo box)
     int cs, ab2_first, polymer;
     T vis, coef_t, c_helm;            // beta/Re, (1-beta)/(Re Wi), dt/(2 Re)
     T inv_re;
     double *grad;
 };
-
-// per-thread accumulation of a stencil transpose: 9 positions per velocity
-// component (offsets listed below), added with one atomic each
-template <typename T>
-struct Acc9 {
-    T v[9];
-    __device__ void zero() {
-        for (int q = 0; q < 9; ++q) v[q] = T(0);
-    }
-};
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_momentum_adj(MomAdjArgs<T> a, Geo g) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    const bool active = i <= g.nx && j <= g.ny;
-    T gb = T(0);
-    if (active) {
-        const T dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz), dt = T(g.dt);
-        const T h2 = T(0.5), h15 = T(1.5);
-        const T *U = a.U, *V = a.V, *W = a.W;
-        auto u = [&](int x, int y, int z) { return U[hix(g, i + x, j + y, k + z)]; };
-        auto v = [&](int x, int y, int z) { return V[hix(g, i + x, j + y, k + z)]; };
-        auto w = [&](int x, int y, int z) { return W[hix(g, i + x, j + y, k + z)]; };
-        const int o = qix(g, i, j, k), h = hix(g, i, j, k);
-        T lua[3], lA[3], lT[3], lB[3];
-        for (int c = 0; c < 3; ++c) {
-            const T lq = a.lQ[c][h];
-            lua[c] = lq + a.lUa[c][h];
-            lA[c] = h15 * dt * lua[c] + a.lA0[c][o];
-            lT[c] = h2 * dt * lua[c] + a.lT0[c][o];
-            if (a.ab2_first) {
-                lA[c] += -h2 * dt * lua[c];
-                lT[c] += h2 * dt * lua[c];
-                a.lA0[c][o] = T(0);
-                a.lT0[c][o] = T(0);
-            } else {
-                a.lA0[c][o] = -h2 * dt * lua[c];
-                a.lT0[c][o] = h2 * dt * lua[c];
-            }
-            lB[c] = dt * lua[c] - h2 * dt * lq;
-            // Helmholtz coefficient dt beta/(2 Re): d/dbeta = (dt/2Re) lQ . L(Up)
-            if (lq != T(0)) {
-                const T *X = a.Up[c];
-                const T x0 = X[h];
-                const T L = (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) / (dX * dX)
-                          + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) / (dY * dY)
-                          + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) / (dZ * dZ);
-                gb += a.c_helm * lq * L;
-            }
-        }
-        // positions of the U, V, W transposes (offsets from (i, j, k))
-        //   U: 0 (0,0,0) 1 (-1,0,0) 2 (1,0,0) 3 (0,-1,0) 4 (0,1,0) 5 (0,0,-1) 6 (0,0,1) 7 (-1,1,0) 8 (-1,0,1)
-        //   V: 0 (0,0,0) 1 (-1,0,0) 2 (1,0,0) 3 (0,-1,0) 4 (0,1,0) 5 (0,0,-1) 6 (0,0,1) 7 (1,-1,0) 8 (0,-1,1)
-        //   W: 0 (0,0,0) 1 (-1,0,0) 2 (1,0,0) 3 (0,-1,0) 4 (0,1,0) 5 (0,0,-1) 6 (0,0,1) 7 (1,0,-1) 8 (0,1,-1)
-        Acc9<T> aU, aV, aW;
-        aU.zero(); aV.zero(); aW.zero();
-        aU.v[0] += lua[0];
-        aV.v[0] += lua[1];
-        aW.v[0] += lua[2];
-        // viscous terms B = vis lap(U) and d/dbeta (B/beta = lap/Re)
-        {
-            const T ib[3] = {T(1) / (dX * dX), T(1) / (dY * dY), T(1) / (dZ * dZ)};
-            Acc9<T> *acc[3] = {&aU, &aV, &aW};
-            const T *F[3] = {U, V, W};
-            for (int c = 0; c < 3; ++c) {
-                const T lb = a.vis * lB[c];
-                Acc9<T> &A = *acc[c];
-                A.v[1] += lb * ib[0]; A.v[2] += lb * ib[0];
-                A.v[3] += lb * ib[1]; A.v[4] += lb * ib[1];
-                A.v[5] += lb * ib[2]; A.v[6] += lb * ib[2];
-                A.v[0] += T(-2) * lb * (ib[0] + ib[1] + ib[2]);
-                const T *X = F[c];
-                const T x0 = X[h];
-                const T L = (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) / (dX * dX)
-                          + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) / (dY * dY)
-                          + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) / (dZ * dZ);
-                gb += a.inv_re * lB[c] * L;
-            }
-        }
-        // convection: A = -a.  a "square" term s (p1 + p2)^2/4 id and a "cross"
-        // term s (a1 + a2)/2 (b1 + b2)/2 id; ga = adjoint of a
-        {
-            const T ga = -lA[0], gbv = -lA[1], gc = -lA[2];
-            // ax
-            {
-                const T t1 = (u(-1, 0, 0) + u(0, 0, 0)) / 2, t2 = (u(0, 0, 0) + u(1, 0, 0)) / 2;
-                aU.v[1] += ga * (-t1) / dX;
-                aU.v[0] += ga * (-t1 + t2) / dX;
-                aU.v[2] += ga * t2 / dX;
-                // y: -(v(0,-1)+v(1,-1))/2 (u(0,-1)+u(0,0))/2 + (v(0,0)+v(1,0))/2 (u(0,0)+u(0,1))/2
-                const T a1 = (v(0, -1, 0) + v(1, -1, 0)) / 2, b1 = (u(0, -1, 0) + u(0, 0, 0)) / 2;
-                const T a2 = (v(0, 0, 0) + v(1, 0, 0)) / 2, b2 = (u(0, 0, 0) + u(0, 1, 0)) / 2;
-                const T s = ga / dY;
-                aV.v[3] += -s * b1 / 2; aV.v[7] += -s * b1 / 2;
-                aU.v[3] += -s * a1 / 2; aU.v[0] += -s * a1 / 2;
-                aV.v[0] += s * b2 / 2; aV.v[2] += s * b2 / 2;
-                aU.v[0] += s * a2 / 2; aU.v[4] += s * a2 / 2;
-                // z: -(w(0,0,-1)+w(1,0,-1))/2 (u(0,0,-1)+u)/2 + (w+w(1,0,0))/2 (u+u(0,0,1))/2
-                const T c1 = (w(0, 0, -1) + w(1, 0, -1)) / 2, d1 = (u(0, 0, -1) + u(0, 0, 0)) / 2;
-                const T c2 = (w(0, 0, 0) + w(1, 0, 0)) / 2, d2 = (u(0, 0, 0) + u(0, 0, 1)) / 2;
-                const T sz = ga / dZ;
-                aW.v[5] += -sz * d1 / 2; aW.v[7] += -sz * d1 / 2;
-                aU.v[5] += -sz * c1 / 2; aU.v[0] += -sz * c1 / 2;
-                aW.v[0] += sz * d2 / 2; aW.v[2] += sz * d2 / 2;
-                aU.v[0] += sz * c2 / 2; aU.v[6] += sz * c2 / 2;
-            }
-            // ay
-            {
-                // x: -(u(-1,0)+u(-1,1))/2 (v(-1,0)+v)/2 + (u+u(0,1))/2 (v+v(1,0))/2
-                const T a1 = (u(-1, 0, 0) + u(-1, 1, 0)) / 2, b1 = (v(-1, 0, 0) + v(0, 0, 0)) / 2;
-                const T a2 = (u(0, 0, 0) + u(0, 1, 0)) / 2, b2 = (v(0, 0, 0) + v(1, 0, 0)) / 2;
-                const T s = gbv / dX;
-                aU.v[1] += -s * b1 / 2; aU.v[7] += -s * b1 / 2;
-                aV.v[1] += -s * a1 / 2; aV.v[0] += -s * a1 / 2;
-                aU.v[0] += s * b2 / 2; aU.v[4] += s * b2 / 2;
-                aV.v[0] += s * a2 / 2; aV.v[2] += s * a2 / 2;
-                const T t3 = (v(0, -1, 0) + v(0, 0, 0)) / 2, t4 = (v(0, 0, 0) + v(0, 1, 0)) / 2;
-                aV.v[3] += gbv * (-t3) / dY;
-                aV.v[0] += gbv * (-t3 + t4) / dY;
-                aV.v[4] += gbv * t4 / dY;
-                // z: -(w(0,0,-1)+w(0,1,-1))/2 (v(0,0,-1)+v)/2 + (w+w(0,1,0))/2 (v+v(0,0,1))/2
-                const T c1 = (w(0, 0, -1) + w(0, 1, -1)) / 2, d1 = (v(0, 0, -1) + v(0, 0, 0)) / 2;
-                const T c2 = (w(0, 0, 0) + w(0, 1, 0)) / 2, d2 = (v(0, 0, 0) + v(0, 0, 1)) / 2;
-                const T sz = gbv / dZ;
-                aW.v[5] += -sz * d1 / 2; aW.v[8] += -sz * d1 / 2;
-                aV.v[5] += -sz * c1 / 2; aV.v[0] += -sz * c1 / 2;
-                aW.v[0] += sz * d2 / 2; aW.v[4] += sz * d2 / 2;
-                aV.v[0] += sz * c2 / 2; aV.v[6] += sz * c2 / 2;
-            }
-            // az
-            {
-                // x: -(u(-1,0,0)+u(-1,0,1))/2 (w(-1)+w)/2 + (u+u(0,0,1))/2 (w+w(1))/2
-                const T a1 = (u(-1, 0, 0) + u(-1, 0, 1)) / 2, b1 = (w(-1, 0, 0) + w(0, 0, 0)) / 2;
-                const T a2 = (u(0, 0, 0) + u(0, 0, 1)) / 2, b2 = (w(0, 0, 0) + w(1, 0, 0)) / 2;
-                const T s = gc / dX;
-                aU.v[1] += -s * b1 / 2; aU.v[8] += -s * b1 / 2;
-                aW.v[1] += -s * a1 / 2; aW.v[0] += -s * a1 / 2;
-                aU.v[0] += s * b2 / 2; aU.v[6] += s * b2 / 2;
-                aW.v[0] += s * a2 / 2; aW.v[2] += s * a2 / 2;
-                // y: -(v(0,-1,0)+v(0,-1,1))/2 (w(0,-1)+w)/2 + (v+v(0,0,1))/2 (w+w(0,1))/2
-                const T c1 = (v(0, -1, 0) + v(0, -1, 1)) / 2, d1 = (w(0, -1, 0) + w(0, 0, 0)) / 2;
-                const T c2 = (v(0, 0, 0) + v(0, 0, 1)) / 2, d2 = (w(0, 0, 0) + w(0, 1, 0)) / 2;
-                const T sy = gc / dY;
-                aV.v[3] += -sy * d1 / 2; aV.v[8] += -sy * d1 / 2;
-                aW.v[3] += -sy * c1 / 2; aW.v[0] += -sy * c1 / 2;
-                aV.v[0] += sy * d2 / 2; aV.v[6] += sy * d2 / 2;
-                aW.v[0] += sy * c2 / 2; aW.v[4] += sy * c2 / 2;
-                const T t5 = (w(0, 0, -1) + w(0, 0, 0)) / 2, t6 = (w(0, 0, 0) + w(0, 0, 1)) / 2;
-                aW.v[5] += gc * (-t5) / dZ;
-                aW.v[0] += gc * (-t5 + t6) / dZ;
-                aW.v[6] += gc * t6 / dZ;
-            }
-        }
-        {
-            const int offU[9][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}, {-1, 1, 0}, {-1, 0, 1}};
-            const int offV[9][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}, {1, -1, 0}, {0, -1, 1}};
-            const int offW[9][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}, {1, 0, -1}, {0, 1, -1}};
-            for (int q = 0; q < 9; ++q) {
-                if (aU.v[q] != T(0)) atomicAdd(&a.lU[hix(g, i + offU[q][0], j + offU[q][1], k + offU[q][2])], aU.v[q]);
-                if (aV.v[q] != T(0)) atomicAdd(&a.lV[hix(g, i + offV[q][0], j + offV[q][1], k + offV[q][2])], aV.v[q]);
-                if (aW.v[q] != T(0)) atomicAdd(&a.lW[hix(g, i + offW[q][0], j + offW[q][1], k + offW[q][2])], aW.v[q]);
-            }
-        }
-        // pressure gradient gp_c = -dt (P(o + e_c) - P(o)) / d_c
-        {
-            const T px = dt / dX * lua[0], py = dt / dY * lua[1], pz = dt / dZ * lua[2];
-            atomicAdd(&a.lP[h], px + py + pz);
-            atomicAdd(&a.lP[hix(g, i + 1, j, k)], -px);
-            atomicAdd(&a.lP[hix(g, i, j + 1, k)], -py);
-            atomicAdd(&a.lP[hix(g, i, j, k + 1)], -pz);
-        }
-        // polymer stress T = coef_t div(C0), C0 = f C - I (fenep.f90:645-691)
-        if (a.polymer) {
-            const T sx = a.coef_t * lT[0], sy = a.coef_t * lT[1], sz = a.coef_t * lT[2];
-            T *L = a.lC0;
-            const size_t cs = (size_t)a.cs;
-            auto add = [&](int m, int x, int y, int z, T val) {
-                atomicAdd(&L[(size_t)(m - 1) * cs + hix(g, i + x, j + y, k + z)], val);
-            };
-            // tx
-            add(1, 0, 0, 0, -sx / dX); add(1, 1, 0, 0, sx / dX);
-            add(2, 0, -1, 0, -sx / (4 * dY)); add(2, 1, -1, 0, -sx / (4 * dY));
-            add(2, 0, 1, 0, sx / (4 * dY)); add(2, 1, 1, 0, sx / (4 * dY));
-            add(3, 0, 0, -1, -sx / (4 * dZ)); add(3, 1, 0, -1, -sx / (4 * dZ));
-            add(3, 0, 0, 1, sx / (4 * dZ)); add(3, 1, 0, 1, sx / (4 * dZ));
-            // ty
-            add(2, -1, 0, 0, -sy / (4 * dX)); add(2, 1, 0, 0, sy / (4 * dX));
-            add(2, -1, 1, 0, -sy / (4 * dX)); add(2, 1, 1, 0, sy / (4 * dX));
-            add(4, 0, 0, 0, -sy / dY); add(4, 0, 1, 0, sy / dY);
-            add(5, 0, 0, -1, -sy / (4 * dZ)); add(5, 0, 1, -1, -sy / (4 * dZ));
-            add(5, 0, 0, 1, sy / (4 * dZ)); add(5, 0, 1, 1, sy / (4 * dZ));
-            // tz
-            add(3, -1, 0, 0, -sz / (4 * dX)); add(3, 1, 0, 0, sz / (4 * dX));
-            add(3, -1, 0, 1, -sz / (4 * dX)); add(3, 1, 0, 1, sz / (4 * dX));
-            add(5, 0, -1, 0, -sz / (4 * dY)); add(5, 0, 1, 0, sz / (4 * dY));
-            add(5, 0, -1, 1, -sz / (4 * dY)); add(5, 0, 1, 1, sz / (4 * dY));
-            add(6, 0, 0, 0, -sz / dZ); add(6, 0, 0, 1, sz / dZ);
-        }
-    }
-    block_atomic_add((double)gb, a.grad + 1);
-}
-
-// C0 = f(C) C - I on every cell (halo included), f = (L^2 - 3)/(L^2 - tr C):
-// adds the adjoint of C^{n+1} and the L^2, beta, Wi terms (the stress
-// coefficient (1-beta)/(Re Wi) enters through sum C0 . lC0).
-template <typename T>
-__global__ void k_c0_adj(const T *C, const T *lC0, T *lC, int cs, T lp2, T inv_1mb, T inv_wi, double *grad) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    T g_coef = T(0), g_l2 = T(0);
-    if (t < cs) {
-        T c[6], l[6];
-        bool any = false;
-        for (int m = 0; m < 6; ++m) {
-            l[m] = lC0[(size_t)m * cs + t];
-            any = any || l[m] != T(0);
-        }
-        if (any) {
-            const T E[6] = {T(1), T(0), T(0), T(1), T(0), T(1)};
-            for (int m = 0; m < 6; ++m) c[m] = C[(size_t)m * cs + t];
-            // tr C - 3 from the diagonal deviations (exact differences near
-            // C = I), f - 1 = (tr C - 3)/(L^2 - tr C): the parameter terms
-            // below then carry no cancellation of the O(1) parts
-            const T tr3 = (c[0] - T(1)) + (c[3] - T(1)) + (c[5] - T(1));
-            const T den = (lp2 - 3) - tr3;
-            const T f = (lp2 - 3) / den;
-            const T fm1 = tr3 / den;
-            T lf = T(0);
-            for (int m = 0; m < 6; ++m) {
-                lC[(size_t)m * cs + t] += f * l[m];
-                lf += c[m] * l[m];
-                g_coef += (fm1 * c[m] + (c[m] - E[m])) * l[m];   // (f C - I) . lC0
-            }
-            const T dfdtr = f / den;
-            lC[t] += lf * dfdtr;
-            lC[(size_t)3 * cs + t] += lf * dfdtr;
-            lC[(size_t)5 * cs + t] += lf * dfdtr;
-            g_l2 = -lf * tr3 / (den * den);
-        }
-    }
-    block_atomic_add((double)(-g_coef * inv_1mb), grad + 1);
-    block_atomic_add((double)(-g_coef * inv_wi), grad + 0);
-    block_atomic_add((double)g_l2, grad + 2);
-}
 
 // ---------------------------------------------------------------------------
 // Polymer update transposed: implicit-function adjoint of the Lyapunov Newton
@@ -662,8 +418,6 @@ struct PolyAdjArgs {
     const uint8_t *codes, *codes_g;
     const T *U, *V, *W;               // U^n (halo)
     const T *lX;                      // adjoint of C^{n+1} (interior)
-    T *lC;                            // out: adjoint of C^n (full halo box, scattered)
-    T *lU, *lV, *lW;
     int cs;
     T dt, wi, lp2;
     double *grad;
@@ -680,10 +434,387 @@ __device__ inline int code_of(const uint8_t *codes, const uint8_t *codes_g, cons
     return (j >= 1 && j <= g.ny) ? codes[qix(g, i, j, k)] : codes_g[gcix(g, i, j, k)];
 }
 
-// Rows: the cells of the polymer update (with walls also the ghost rows,
-// whose faces towards the outside rows carry zero C)
+// mu = J^-T lx for the Jacobian J = dG/dx of the Lyapunov residual
+// G(x) = A x + x A^T + (1 + f(x) dt/Wi) x - b at the Newton solution x
+// (fenep.f90:588-605, component order xx, xy, xz, yy, yz, zz): Gaussian
+// elimination with partial pivoting on the 6 x 7 augmented transpose.  The
+// pivot row is found by compare-and-exchange with each lower row, so every
+// index is a compile-time constant and the matrix stays in registers.
 template <typename T>
-__global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
+__device__ inline void solve_jt6(const T (&A)[3][3], T dd2, T cf, const T (&x)[6], const T (&lx)[6], T (&mu)[6]) {
+    T J[6][6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) J[r][q] = T(0);
+    J[0][0] = 2 * A[0][0]; J[0][1] = 2 * A[0][1]; J[0][2] = 2 * A[0][2];
+    J[1][0] = A[1][0]; J[1][1] = A[1][1] + A[0][0]; J[1][2] = A[1][2]; J[1][3] = A[0][1]; J[1][4] = A[0][2];
+    J[2][0] = A[2][0]; J[2][1] = A[2][1]; J[2][2] = A[2][2] + A[0][0]; J[2][4] = A[0][1]; J[2][5] = A[0][2];
+    J[3][1] = 2 * A[1][0]; J[3][3] = 2 * A[1][1]; J[3][4] = 2 * A[1][2];
+    J[4][1] = A[2][0]; J[4][2] = A[1][0]; J[4][3] = A[2][1]; J[4][4] = A[2][2] + A[1][1]; J[4][5] = A[1][2];
+    J[5][2] = 2 * A[2][0]; J[5][4] = 2 * A[2][1]; J[5][5] = 2 * A[2][2];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        J[r][r] += dd2;
+        J[r][0] += cf * x[r];
+        J[r][3] += cf * x[r];
+        J[r][5] += cf * x[r];
+    }
+    T M[6][7];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) M[r][q] = J[q][r];
+        M[r][6] = lx[r];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+#pragma unroll
+        for (int r = c + 1; r < 6; ++r) {
+            const bool sw = fabs(M[r][c]) > fabs(M[c][c]);
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                if (q < c) continue;
+                const T u0 = M[c][q], u1 = M[r][q];
+                M[c][q] = sw ? u1 : u0;
+                M[r][q] = sw ? u0 : u1;
+            }
+        }
+        const T inv = T(1) / M[c][c];
+#pragma unroll
+        for (int r = c + 1; r < 6; ++r) {
+            const T fr = M[r][c] * inv;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                if (q < c) continue;
+                M[r][q] -= fr * M[c][q];
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 5; r >= 0; --r) {
+        T s = M[r][6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+            if (q > r) s -= M[r][q] * mu[q];
+        mu[r] = s / M[r][r];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gather forms of the momentum and polymer transposes (no atomics; the result
+// at each position is a fixed-order sum, so those stages are deterministic).
+// Pass 1 of each writes per-cell sources; pass 2 gathers, at every position,
+// the contributions of the cells whose stencils read that position.  The
+// coefficients are those of the momentum stencils (fenep.f90:645-770), of
+// C0 = f(C) C - I, and of Cstar and the Lyapunov update (fenep.f90:464-643),
+// regrouped by target position.
+
+constexpr int MOM_SRC = 12;    // lua (3), ga = -lA (3), vis lB (3), coef_t lT (3)
+constexpr int POLY_SRC = 34;   // mu (6), Cstar weights (13), A0 adjoint (9), upwind-face adjoint (6)
+enum { PS_MU = 0, PS_KC = 6, PS_KX = 7, PS_KY = 11, PS_KZ = 15, PS_GU = 19, PS_GV = 22, PS_GW = 25, PS_SF = 28 };
+
+// Momentum, pass 1 (interior cells): the sources, the history adjoints
+// lA0 / lT0 (updated in place: each cell reads and writes only its own) and
+// the beta terms of the viscous and Helmholtz coefficients.
+template <typename T>
+__global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    T gb = T(0);
+    if (i <= g.nx && j <= g.ny) {
+        const T dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz), dt = T(g.dt);
+        const T h2 = T(0.5), h15 = T(1.5);
+        const int o = qix(g, i, j, k), h = hix(g, i, j, k);
+        const size_t cs = (size_t)a.cs;
+        const T *F[3] = {a.U, a.V, a.W};
+        for (int c = 0; c < 3; ++c) {
+            const T lq = a.lQ[c][h];
+            const T lua = lq + a.lUa[c][h];
+            T lA = h15 * dt * lua + a.lA0[c][o];
+            T lT = h2 * dt * lua + a.lT0[c][o];
+            if (a.ab2_first) {
+                lA += -h2 * dt * lua;
+                lT += h2 * dt * lua;
+                a.lA0[c][o] = T(0);
+                a.lT0[c][o] = T(0);
+            } else {
+                a.lA0[c][o] = -h2 * dt * lua;
+                a.lT0[c][o] = h2 * dt * lua;
+            }
+            const T lB = dt * lua - h2 * dt * lq;
+            src[(size_t)(0 + c) * cs + h] = lua;
+            src[(size_t)(3 + c) * cs + h] = -lA;
+            src[(size_t)(6 + c) * cs + h] = a.vis * lB;
+            src[(size_t)(9 + c) * cs + h] = a.polymer ? a.coef_t * lT : T(0);
+            auto lap = [&](const T *X) {
+                const T x0 = X[h];
+                return (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) / (dX * dX)
+                     + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) / (dY * dY)
+                     + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) / (dZ * dZ);
+            };
+            // Helmholtz coefficient dt beta/(2 Re) and viscous coefficient beta/Re
+            if (lq != T(0)) gb += a.c_helm * lq * lap(a.Up[c]);
+            gb += a.inv_re * lB * lap(F[c]);
+        }
+    }
+    block_atomic_add((double)gb, a.grad + 1);
+}
+
+template <typename T>
+struct MomGatherArgs {
+    const T *U, *V, *W;       // forward U^n (halo)
+    const T *src;             // MOM_SRC halo-layout arrays of k_momadj_src (interior cells)
+    T *lU, *lV, *lW;          // out: adjoint of U^n from the momentum stage (full halo box)
+    T *lP;                    // adjoint of P^n, += the pressure-gradient transpose
+    const T *C;               // C as the stress read it (6 SoA halo fields)
+    T *lC;                    // += the transpose of C0 = f(C) C - I (6 fields)
+    int cs, polymer;
+    T lp2, inv_1mb, inv_wi;
+    double *grad;
+};
+
+// Momentum, pass 2 (every position of the halo box): the adjoint of U, V, W
+// at the position from the momentum stencils of the (up to 9 per component)
+// interior cells that read it, the pressure-gradient transpose, and with the
+// polymer the adjoint of C0 (stress divergence) followed by the C0 = f(C) C - I
+// linearisation.
+template <typename T>
+__global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cs = a.cs;
+    T g_coef = T(0), g_l2 = T(0);
+    if (t < cs) {
+        const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
+        const T dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz), dt = T(g.dt);
+        const T ix2 = T(1) / (dX * dX), iy2 = T(1) / (dY * dY), iz2 = T(1) / (dZ * dZ);
+        const T *U = a.U, *V = a.V, *W = a.W;
+        auto ev = [&](int x, int y, int z) { return x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz; };
+        auto S = [&](int q, int x, int y, int z) { return a.src[(size_t)q * cs + hix(g, x, y, z)]; };
+        auto u = [&](int x, int y, int z) { return U[hix(g, x, y, z)]; };
+        auto v = [&](int x, int y, int z) { return V[hix(g, x, y, z)]; };
+        auto w = [&](int x, int y, int z) { return W[hix(g, x, y, z)]; };
+        const T h = T(0.5);
+        // velocity averages of the convection stencils around source cell (x, y, z)
+        auto ax_t1 = [&](int x, int y, int z) { return (u(x - 1, y, z) + u(x, y, z)) * h; };
+        auto ax_t2 = [&](int x, int y, int z) { return (u(x, y, z) + u(x + 1, y, z)) * h; };
+        auto axy_a1 = [&](int x, int y, int z) { return (v(x, y - 1, z) + v(x + 1, y - 1, z)) * h; };
+        auto axy_b1 = [&](int x, int y, int z) { return (u(x, y - 1, z) + u(x, y, z)) * h; };
+        auto axy_a2 = [&](int x, int y, int z) { return (v(x, y, z) + v(x + 1, y, z)) * h; };
+        auto axy_b2 = [&](int x, int y, int z) { return (u(x, y, z) + u(x, y + 1, z)) * h; };
+        auto axz_c1 = [&](int x, int y, int z) { return (w(x, y, z - 1) + w(x + 1, y, z - 1)) * h; };
+        auto axz_d1 = [&](int x, int y, int z) { return (u(x, y, z - 1) + u(x, y, z)) * h; };
+        auto axz_c2 = [&](int x, int y, int z) { return (w(x, y, z) + w(x + 1, y, z)) * h; };
+        auto axz_d2 = [&](int x, int y, int z) { return (u(x, y, z) + u(x, y, z + 1)) * h; };
+        auto ayx_a1 = [&](int x, int y, int z) { return (u(x - 1, y, z) + u(x - 1, y + 1, z)) * h; };
+        auto ayx_b1 = [&](int x, int y, int z) { return (v(x - 1, y, z) + v(x, y, z)) * h; };
+        auto ayx_a2 = [&](int x, int y, int z) { return (u(x, y, z) + u(x, y + 1, z)) * h; };
+        auto ayx_b2 = [&](int x, int y, int z) { return (v(x, y, z) + v(x + 1, y, z)) * h; };
+        auto ay_t3 = [&](int x, int y, int z) { return (v(x, y - 1, z) + v(x, y, z)) * h; };
+        auto ay_t4 = [&](int x, int y, int z) { return (v(x, y, z) + v(x, y + 1, z)) * h; };
+        auto ayz_c1 = [&](int x, int y, int z) { return (w(x, y, z - 1) + w(x, y + 1, z - 1)) * h; };
+        auto ayz_d1 = [&](int x, int y, int z) { return (v(x, y, z - 1) + v(x, y, z)) * h; };
+        auto ayz_c2 = [&](int x, int y, int z) { return (w(x, y, z) + w(x, y + 1, z)) * h; };
+        auto ayz_d2 = [&](int x, int y, int z) { return (v(x, y, z) + v(x, y, z + 1)) * h; };
+        auto azx_a1 = [&](int x, int y, int z) { return (u(x - 1, y, z) + u(x - 1, y, z + 1)) * h; };
+        auto azx_b1 = [&](int x, int y, int z) { return (w(x - 1, y, z) + w(x, y, z)) * h; };
+        auto azx_a2 = [&](int x, int y, int z) { return (u(x, y, z) + u(x, y, z + 1)) * h; };
+        auto azx_b2 = [&](int x, int y, int z) { return (w(x, y, z) + w(x + 1, y, z)) * h; };
+        auto azy_c1 = [&](int x, int y, int z) { return (v(x, y - 1, z) + v(x, y - 1, z + 1)) * h; };
+        auto azy_d1 = [&](int x, int y, int z) { return (w(x, y - 1, z) + w(x, y, z)) * h; };
+        auto azy_c2 = [&](int x, int y, int z) { return (v(x, y, z) + v(x, y, z + 1)) * h; };
+        auto azy_d2 = [&](int x, int y, int z) { return (w(x, y, z) + w(x, y + 1, z)) * h; };
+        auto az_t5 = [&](int x, int y, int z) { return (w(x, y, z - 1) + w(x, y, z)) * h; };
+        auto az_t6 = [&](int x, int y, int z) { return (w(x, y, z) + w(x, y, z + 1)) * h; };
+        // sources: lua 0-2, ga 3-5 (ga, gbv, gc of the x, y, z fluxes), lb 6-8, st 9-11
+        T lu = T(0), lv = T(0), lw = T(0), lp = T(0);
+        // ---- U ----
+        if (ev(i, j, k)) {
+            const int x = i, y = j, z = k;
+            const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
+            lu += S(0, x, y, z) - 2 * S(6, x, y, z) * (ix2 + iy2 + iz2) + ga * (ax_t2(x, y, z) - ax_t1(x, y, z)) / dX
+                + ga / dY * (axy_a2(x, y, z) - axy_a1(x, y, z)) * h + ga / dZ * (axz_c2(x, y, z) - axz_c1(x, y, z)) * h
+                + gbv / dX * ayx_b2(x, y, z) * h + gc / dX * azx_b2(x, y, z) * h;
+        }
+        if (ev(i + 1, j, k)) {
+            const int x = i + 1, y = j, z = k;
+            lu += S(6, x, y, z) * ix2 - S(3, x, y, z) * ax_t1(x, y, z) / dX - S(4, x, y, z) / dX * ayx_b1(x, y, z) * h
+                - S(5, x, y, z) / dX * azx_b1(x, y, z) * h;
+        }
+        if (ev(i - 1, j, k)) {
+            const int x = i - 1, y = j, z = k;
+            lu += S(6, x, y, z) * ix2 + S(3, x, y, z) * ax_t2(x, y, z) / dX;
+        }
+        if (ev(i, j + 1, k)) {
+            const int x = i, y = j + 1, z = k;
+            lu += S(6, x, y, z) * iy2 - S(3, x, y, z) / dY * axy_a1(x, y, z) * h;
+        }
+        if (ev(i, j - 1, k)) {
+            const int x = i, y = j - 1, z = k;
+            lu += S(6, x, y, z) * iy2 + S(3, x, y, z) / dY * axy_a2(x, y, z) * h + S(4, x, y, z) / dX * ayx_b2(x, y, z) * h;
+        }
+        if (ev(i, j, k + 1)) {
+            const int x = i, y = j, z = k + 1;
+            lu += S(6, x, y, z) * iz2 - S(3, x, y, z) / dZ * axz_c1(x, y, z) * h;
+        }
+        if (ev(i, j, k - 1)) {
+            const int x = i, y = j, z = k - 1;
+            lu += S(6, x, y, z) * iz2 + S(3, x, y, z) / dZ * axz_c2(x, y, z) * h + S(5, x, y, z) / dX * azx_b2(x, y, z) * h;
+        }
+        if (ev(i + 1, j - 1, k)) {
+            const int x = i + 1, y = j - 1, z = k;
+            lu -= S(4, x, y, z) / dX * ayx_b1(x, y, z) * h;
+        }
+        if (ev(i + 1, j, k - 1)) {
+            const int x = i + 1, y = j, z = k - 1;
+            lu -= S(5, x, y, z) / dX * azx_b1(x, y, z) * h;
+        }
+        // ---- V ----
+        if (ev(i, j, k)) {
+            const int x = i, y = j, z = k;
+            const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
+            lv += S(1, x, y, z) - 2 * S(7, x, y, z) * (ix2 + iy2 + iz2) + ga / dY * axy_b2(x, y, z) * h
+                + gbv / dX * (ayx_a2(x, y, z) - ayx_a1(x, y, z)) * h + gbv * (ay_t4(x, y, z) - ay_t3(x, y, z)) / dY
+                + gbv / dZ * (ayz_c2(x, y, z) - ayz_c1(x, y, z)) * h + gc / dY * azy_d2(x, y, z) * h;
+        }
+        if (ev(i + 1, j, k)) {
+            const int x = i + 1, y = j, z = k;
+            lv += S(7, x, y, z) * ix2 - S(4, x, y, z) / dX * ayx_a1(x, y, z) * h;
+        }
+        if (ev(i - 1, j, k)) {
+            const int x = i - 1, y = j, z = k;
+            lv += S(7, x, y, z) * ix2 + S(3, x, y, z) / dY * axy_b2(x, y, z) * h + S(4, x, y, z) / dX * ayx_a2(x, y, z) * h;
+        }
+        if (ev(i, j + 1, k)) {
+            const int x = i, y = j + 1, z = k;
+            lv += S(7, x, y, z) * iy2 - S(3, x, y, z) / dY * axy_b1(x, y, z) * h - S(4, x, y, z) * ay_t3(x, y, z) / dY
+                - S(5, x, y, z) / dY * azy_d1(x, y, z) * h;
+        }
+        if (ev(i, j - 1, k)) {
+            const int x = i, y = j - 1, z = k;
+            lv += S(7, x, y, z) * iy2 + S(4, x, y, z) * ay_t4(x, y, z) / dY;
+        }
+        if (ev(i, j, k + 1)) {
+            const int x = i, y = j, z = k + 1;
+            lv += S(7, x, y, z) * iz2 - S(4, x, y, z) / dZ * ayz_c1(x, y, z) * h;
+        }
+        if (ev(i, j, k - 1)) {
+            const int x = i, y = j, z = k - 1;
+            lv += S(7, x, y, z) * iz2 + S(4, x, y, z) / dZ * ayz_c2(x, y, z) * h + S(5, x, y, z) / dY * azy_d2(x, y, z) * h;
+        }
+        if (ev(i - 1, j + 1, k)) {
+            const int x = i - 1, y = j + 1, z = k;
+            lv -= S(3, x, y, z) / dY * axy_b1(x, y, z) * h;
+        }
+        if (ev(i, j + 1, k - 1)) {
+            const int x = i, y = j + 1, z = k - 1;
+            lv -= S(5, x, y, z) / dY * azy_d1(x, y, z) * h;
+        }
+        // ---- W ----
+        if (ev(i, j, k)) {
+            const int x = i, y = j, z = k;
+            const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
+            lw += S(2, x, y, z) - 2 * S(8, x, y, z) * (ix2 + iy2 + iz2) + ga / dZ * axz_d2(x, y, z) * h
+                + gbv / dZ * ayz_d2(x, y, z) * h + gc / dX * (azx_a2(x, y, z) - azx_a1(x, y, z)) * h
+                + gc / dY * (azy_c2(x, y, z) - azy_c1(x, y, z)) * h + gc * (az_t6(x, y, z) - az_t5(x, y, z)) / dZ;
+        }
+        if (ev(i + 1, j, k)) {
+            const int x = i + 1, y = j, z = k;
+            lw += S(8, x, y, z) * ix2 - S(5, x, y, z) / dX * azx_a1(x, y, z) * h;
+        }
+        if (ev(i - 1, j, k)) {
+            const int x = i - 1, y = j, z = k;
+            lw += S(8, x, y, z) * ix2 + S(3, x, y, z) / dZ * axz_d2(x, y, z) * h + S(5, x, y, z) / dX * azx_a2(x, y, z) * h;
+        }
+        if (ev(i, j + 1, k)) {
+            const int x = i, y = j + 1, z = k;
+            lw += S(8, x, y, z) * iy2 - S(5, x, y, z) / dY * azy_c1(x, y, z) * h;
+        }
+        if (ev(i, j - 1, k)) {
+            const int x = i, y = j - 1, z = k;
+            lw += S(8, x, y, z) * iy2 + S(4, x, y, z) / dZ * ayz_d2(x, y, z) * h + S(5, x, y, z) / dY * azy_c2(x, y, z) * h;
+        }
+        if (ev(i, j, k + 1)) {
+            const int x = i, y = j, z = k + 1;
+            lw += S(8, x, y, z) * iz2 - S(3, x, y, z) / dZ * axz_d1(x, y, z) * h - S(4, x, y, z) / dZ * ayz_d1(x, y, z) * h
+                - S(5, x, y, z) * az_t5(x, y, z) / dZ;
+        }
+        if (ev(i, j, k - 1)) {
+            const int x = i, y = j, z = k - 1;
+            lw += S(8, x, y, z) * iz2 + S(5, x, y, z) * az_t6(x, y, z) / dZ;
+        }
+        if (ev(i - 1, j, k + 1)) {
+            const int x = i - 1, y = j, z = k + 1;
+            lw -= S(3, x, y, z) / dZ * axz_d1(x, y, z) * h;
+        }
+        if (ev(i, j - 1, k + 1)) {
+            const int x = i, y = j - 1, z = k + 1;
+            lw -= S(4, x, y, z) / dZ * ayz_d1(x, y, z) * h;
+        }
+        // pressure gradient gp_c = -dt (P(o + e_c) - P(o)) / d_c, transposed
+        if (ev(i, j, k)) lp += dt / dX * S(0, i, j, k) + dt / dY * S(1, i, j, k) + dt / dZ * S(2, i, j, k);
+        if (ev(i - 1, j, k)) lp -= dt / dX * S(0, i - 1, j, k);
+        if (ev(i, j - 1, k)) lp -= dt / dY * S(1, i, j - 1, k);
+        if (ev(i, j, k - 1)) lp -= dt / dZ * S(2, i, j, k - 1);
+        a.lU[t] = lu;
+        a.lV[t] = lv;
+        a.lW[t] = lw;
+        a.lP[t] += lp;
+        if (a.polymer) {
+            // adjoint of C0 from the stress divergence (fenep.f90:645-691):
+            // sT = coef_t lT of the interior cells whose stencils read C0 here
+            auto st = [&](int c, int x, int y, int z) { return ev(x, y, z) ? S(9 + c, x, y, z) : T(0); };
+            const T q4x = T(1) / (4 * dX), q4y = T(1) / (4 * dY), q4z = T(1) / (4 * dZ);
+            T l0[6];
+            l0[0] = (st(0, i - 1, j, k) - st(0, i, j, k)) / dX;
+            l0[3] = (st(1, i, j - 1, k) - st(1, i, j, k)) / dY;
+            l0[5] = (st(2, i, j, k - 1) - st(2, i, j, k)) / dZ;
+            l0[1] = q4y * (st(0, i, j - 1, k) + st(0, i - 1, j - 1, k) - st(0, i, j + 1, k) - st(0, i - 1, j + 1, k))
+                  + q4x * (st(1, i - 1, j, k) + st(1, i - 1, j - 1, k) - st(1, i + 1, j, k) - st(1, i + 1, j - 1, k));
+            l0[2] = q4z * (st(0, i, j, k - 1) + st(0, i - 1, j, k - 1) - st(0, i, j, k + 1) - st(0, i - 1, j, k + 1))
+                  + q4x * (st(2, i - 1, j, k) + st(2, i - 1, j, k - 1) - st(2, i + 1, j, k) - st(2, i + 1, j, k - 1));
+            l0[4] = q4z * (st(1, i, j, k - 1) + st(1, i, j - 1, k - 1) - st(1, i, j, k + 1) - st(1, i, j - 1, k + 1))
+                  + q4y * (st(2, i, j - 1, k) + st(2, i, j - 1, k - 1) - st(2, i, j + 1, k) - st(2, i, j + 1, k - 1));
+            bool any = false;
+            for (int m = 0; m < 6; ++m) any = any || l0[m] != T(0);
+            if (any) {
+                // C0 = f(C) C - I linearised
+                const T E[6] = {T(1), T(0), T(0), T(1), T(0), T(1)};
+                T c[6];
+                for (int m = 0; m < 6; ++m) c[m] = a.C[(size_t)m * cs + t];
+                const T tr3 = (c[0] - T(1)) + (c[3] - T(1)) + (c[5] - T(1));
+                const T den = (a.lp2 - 3) - tr3;
+                const T f = (a.lp2 - 3) / den;
+                const T fm1 = tr3 / den;
+                T lf = T(0);
+                for (int m = 0; m < 6; ++m) {
+                    a.lC[(size_t)m * cs + t] += f * l0[m];
+                    lf += c[m] * l0[m];
+                    g_coef += (fm1 * c[m] + (c[m] - E[m])) * l0[m];
+                }
+                const T dfdtr = f / den;
+                a.lC[t] += lf * dfdtr;
+                a.lC[(size_t)3 * cs + t] += lf * dfdtr;
+                a.lC[(size_t)5 * cs + t] += lf * dfdtr;
+                g_l2 = -lf * tr3 / (den * den);
+            }
+        }
+    }
+    if (a.polymer) {
+        block_atomic_add((double)(-g_coef * a.inv_1mb), a.grad + 1);
+        block_atomic_add((double)(-g_coef * a.inv_wi), a.grad + 0);
+        block_atomic_add((double)g_l2, a.grad + 2);
+    }
+}
+
+// Polymer, pass 1 (the updated cells; with walls also the ghost rows): the
+// implicit-function adjoint mu = J^-T lC^{n+1} at the Newton solution, the 13
+// Cstar weights of the cell (the same for the 6 components: centre, x/y/z at
+// offsets -2, -1, +1, +2), the adjoint of the velocity-gradient entries and
+// of the upwind coefficients, and the Wi and L^2 terms.
+template <typename T>
+__global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
@@ -692,6 +823,7 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
     if (active) {
         const size_t cs = (size_t)a.cs;
         const int h = hix(g, i, j, k);
+        auto put = [&](int q, T v) { src[(size_t)q * cs + h] = v; };
         const T dt = a.dt, wi = a.wi, lp2 = a.lp2, dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz);
         T lx[6], x[6];
         bool any = false;
@@ -701,7 +833,10 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
             x[m] = a.Cn[m * cs + h];
             any = any || lx[m] != T(0);
         }
-        if (any) {
+        if (!any) {
+#pragma unroll
+            for (int q = 0; q < POLY_SRC; ++q) put(q, T(0));
+        } else {
             const T *U = a.U, *V = a.V, *W = a.W;
             auto u = [&](int p, int q, int r) { return rowv(U, g, p, q, r); };
             auto v = [&](int p, int q, int r) { return rowv(V, g, p, q, r); };
@@ -716,92 +851,31 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
             A0[2][0] = -dt * (-u(i - 1, j, k - 1) - u(i, j, k - 1) + u(i - 1, j, k + 1) + u(i, j, k + 1)) / (4 * dZ);
             A0[2][1] = -dt * (-v(i, j - 1, k - 1) - v(i, j, k - 1) + v(i, j - 1, k + 1) + v(i, j, k + 1)) / (4 * dZ);
             A0[2][2] = -dt * (-w(i, j, k - 1) + w(i, j, k)) / dZ;
-            // A = A0^T (the matrix the Newton solve uses)
             T A[3][3];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
                 for (int q = 0; q < 3; ++q) A[r][q] = A0[q][r];
-            // tr C - 3 from the diagonal deviations and f - 1 = (tr C - 3)/den,
-            // so that the parameter terms carry no cancellation of O(1) parts
             const T tr3 = (x[0] - T(1)) + (x[3] - T(1)) + (x[5] - T(1));
             const T den = (lp2 - 3) - tr3;
             const T f = (lp2 - 3) / den;
             const T fm1 = tr3 / den;
             const T dd2 = T(1) + f * dt / wi;
-            const T cf = dt / wi * f / den;    // (dt/Wi) df/dx_d, d in {0, 3, 5}
-            // M = J^T, augmented with the right-hand side lx
-            T M[6][7];
-            {
-                T J[6][6];
-#pragma unroll
-                for (int r = 0; r < 6; ++r)
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) J[r][q] = T(0);
-                J[0][0] = 2 * A[0][0]; J[0][1] = 2 * A[0][1]; J[0][2] = 2 * A[0][2];
-                J[1][0] = A[1][0]; J[1][1] = A[1][1] + A[0][0]; J[1][2] = A[1][2]; J[1][3] = A[0][1]; J[1][4] = A[0][2];
-                J[2][0] = A[2][0]; J[2][1] = A[2][1]; J[2][2] = A[2][2] + A[0][0]; J[2][4] = A[0][1]; J[2][5] = A[0][2];
-                J[3][1] = 2 * A[1][0]; J[3][3] = 2 * A[1][1]; J[3][4] = 2 * A[1][2];
-                J[4][1] = A[2][0]; J[4][2] = A[1][0]; J[4][3] = A[2][1]; J[4][4] = A[2][2] + A[1][1]; J[4][5] = A[1][2];
-                J[5][2] = 2 * A[2][0]; J[5][4] = 2 * A[2][1]; J[5][5] = 2 * A[2][2];
-#pragma unroll
-                for (int r = 0; r < 6; ++r) {
-                    J[r][r] += dd2;
-                    J[r][0] += cf * x[r];
-                    J[r][3] += cf * x[r];
-                    J[r][5] += cf * x[r];
-                }
-#pragma unroll
-                for (int r = 0; r < 6; ++r) {
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) M[r][q] = J[q][r];
-                    M[r][6] = lx[r];
-                }
-            }
-            // Gaussian elimination with partial pivoting.  The pivot row is found
-            // by compare-and-exchange with each lower row (a running maximum),
-            // so every index is a compile-time constant and M stays in registers.
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-#pragma unroll
-                for (int r = c + 1; r < 6; ++r) {
-                    const bool sw = fabs(M[r][c]) > fabs(M[c][c]);
-#pragma unroll
-                    for (int q = c; q < 7; ++q) {
-                        const T u0 = M[c][q], u1 = M[r][q];
-                        M[c][q] = sw ? u1 : u0;
-                        M[r][q] = sw ? u0 : u1;
-                    }
-                }
-                const T inv = T(1) / M[c][c];
-#pragma unroll
-                for (int r = c + 1; r < 6; ++r) {
-                    const T fr = M[r][c] * inv;
-#pragma unroll
-                    for (int q = c; q < 7; ++q) M[r][q] -= fr * M[c][q];
-                }
-            }
+            const T cf = dt / wi * f / den;
             T mu[6];
-#pragma unroll
-            for (int r = 5; r >= 0; --r) {
-                T s = M[r][6];
-#pragma unroll
-                for (int q = r + 1; q < 6; ++q) s -= M[r][q] * mu[q];
-                mu[r] = s / M[r][r];
-            }
-            // parameters: G = L(x) + (1 + f dt/Wi) x - b, b includes dt/Wi on
-            // the diagonal: dG/dWi = -dt/Wi^2 (f x - I), formed as
-            // (f - 1) x + (x - I); dG/dL^2 = dt/Wi df/dL^2 x
+            solve_jt6(A, dd2, cf, x, lx, mu);
             T mx = T(0), mxe = T(0);
             const T E[6] = {T(1), T(0), T(0), T(1), T(0), T(1)};
 #pragma unroll
             for (int m = 0; m < 6; ++m) {
                 mx += mu[m] * x[m];
                 mxe += mu[m] * (x[m] - E[m]);
+                put(PS_MU + m, mu[m]);
             }
             gwi = dt / (wi * wi) * (fm1 * mx + mxe);
             gl2 = dt / wi * tr3 / (den * den) * mx;
-            // adjoint of A = A0^T, then of the velocity-gradient stencils
+            // adjoint of the velocity-gradient entries, each scaled by the
+            // coefficient of its stencil (A0 entries / dt d or dt 4d)
             T lAt[3][3];
             lAt[0][0] = -(2 * mu[0] * x[0] + mu[1] * x[1] + mu[2] * x[2]);
             lAt[0][1] = -(2 * mu[0] * x[1] + mu[1] * x[3] + mu[2] * x[4]);
@@ -812,53 +886,26 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
             lAt[2][0] = -(mu[2] * x[0] + mu[4] * x[1] + 2 * mu[5] * x[2]);
             lAt[2][1] = -(mu[2] * x[1] + mu[4] * x[3] + 2 * mu[5] * x[4]);
             lAt[2][2] = -(mu[2] * x[2] + mu[4] * x[4] + 2 * mu[5] * x[5]);
-            // scatters to rows beyond the ghost rows are dropped (constant zeros)
-            auto inrow = [&](int q) { return q >= 0 && q <= g.ny + 1; };
-            auto addu = [&](int p, int q, int r, T val) { if (inrow(q)) atomicAdd(&a.lU[hix(g, p, q, r)], val); };
-            auto addv = [&](int p, int q, int r, T val) { if (inrow(q)) atomicAdd(&a.lV[hix(g, p, q, r)], val); };
-            auto addw = [&](int p, int q, int r, T val) { if (inrow(q)) atomicAdd(&a.lW[hix(g, p, q, r)], val); };
-            {
-                T l = lAt[0][0] * dt / dX;   // A0[0][0]
-                addu(i - 1, j, k, l); addu(i, j, k, -l);
-                l = lAt[1][0] * dt / (4 * dX);    // A0[0][1]
-                addv(i - 1, j - 1, k, l); addv(i + 1, j - 1, k, -l); addv(i - 1, j, k, l); addv(i + 1, j, k, -l);
-                l = lAt[2][0] * dt / (4 * dX);    // A0[0][2]
-                addw(i - 1, j, k - 1, l); addw(i + 1, j, k - 1, -l); addw(i - 1, j, k, l); addw(i + 1, j, k, -l);
-                l = lAt[0][1] * dt / (4 * dY);    // A0[1][0]
-                addu(i - 1, j - 1, k, l); addu(i, j - 1, k, l); addu(i - 1, j + 1, k, -l); addu(i, j + 1, k, -l);
-                l = lAt[1][1] * dt / dY;          // A0[1][1]
-                addv(i, j - 1, k, l); addv(i, j, k, -l);
-                l = lAt[2][1] * dt / (4 * dY);    // A0[1][2]
-                addw(i, j - 1, k - 1, l); addw(i, j + 1, k - 1, -l); addw(i, j - 1, k, l); addw(i, j + 1, k, -l);
-                l = lAt[0][2] * dt / (4 * dZ);    // A0[2][0]
-                addu(i - 1, j, k - 1, l); addu(i, j, k - 1, l); addu(i - 1, j, k + 1, -l); addu(i, j, k + 1, -l);
-                l = lAt[1][2] * dt / (4 * dZ);    // A0[2][1]
-                addv(i, j - 1, k - 1, l); addv(i, j, k - 1, l); addv(i, j - 1, k + 1, -l); addv(i, j, k + 1, -l);
-                l = lAt[2][2] * dt / dZ;          // A0[2][2]
-                addw(i, j, k - 1, l); addw(i, j, k, -l);
-            }
-            // Cstar: b = s3 pxm + s1 pxp + s4 nxm + s2 nxp + (y: s7 s5 s8 s6) + (z: s11 s9 s12 s10)
+            put(PS_GU + 0, lAt[0][0] * dt / dX);
+            put(PS_GU + 1, lAt[0][1] * dt / (4 * dY));
+            put(PS_GU + 2, lAt[0][2] * dt / (4 * dZ));
+            put(PS_GV + 0, lAt[1][0] * dt / (4 * dX));
+            put(PS_GV + 1, lAt[1][1] * dt / dY);
+            put(PS_GV + 2, lAt[1][2] * dt / (4 * dZ));
+            put(PS_GW + 0, lAt[2][0] * dt / (4 * dX));
+            put(PS_GW + 1, lAt[2][1] * dt / (4 * dY));
+            put(PS_GW + 2, lAt[2][2] * dt / dZ);
+            // Cstar: upwind coefficients s1..s12 and the selection codes
             const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
             const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
             const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
             const T sixth = T(1) / T(6);
-            T s[13];
-            s[1] = (-u2 + fabs(u2)) * dt / (2 * dX);
-            s[2] = sixth + (-u2 - fabs(u2)) * dt / (2 * dX);
-            s[3] = sixth + (u1 - fabs(u1)) * dt / (2 * dX);
-            s[4] = (u1 + fabs(u1)) * dt / (2 * dX);
-            s[5] = (-v2 + fabs(v2)) * dt / (2 * dY);
-            s[6] = sixth + (-v2 - fabs(v2)) * dt / (2 * dY);
-            s[7] = sixth + (v1 - fabs(v1)) * dt / (2 * dY);
-            s[8] = (v1 + fabs(v1)) * dt / (2 * dY);
-            s[9] = (-w2 + fabs(w2)) * dt / (2 * dZ);
-            s[10] = sixth + (-w2 - fabs(w2)) * dt / (2 * dZ);
-            s[11] = sixth + (w1 - fabs(w1)) * dt / (2 * dZ);
-            s[12] = (w1 + fabs(w1)) * dt / (2 * dZ);
-            T ls[13];
-#pragma unroll
-            for (int q = 0; q < 13; ++q) ls[q] = T(0);
-            // selection codes (as the forward kernel reads them)
+            const T s1 = (-u2 + fabs(u2)) * dt / (2 * dX), s2 = sixth + (-u2 - fabs(u2)) * dt / (2 * dX);
+            const T s3 = sixth + (u1 - fabs(u1)) * dt / (2 * dX), s4 = (u1 + fabs(u1)) * dt / (2 * dX);
+            const T s5 = (-v2 + fabs(v2)) * dt / (2 * dY), s6 = sixth + (-v2 - fabs(v2)) * dt / (2 * dY);
+            const T s7 = sixth + (v1 - fabs(v1)) * dt / (2 * dY), s8 = (v1 + fabs(v1)) * dt / (2 * dY);
+            const T s9 = (-w2 + fabs(w2)) * dt / (2 * dZ), s10 = sixth + (-w2 - fabs(w2)) * dt / (2 * dZ);
+            const T s11 = sixth + (w1 - fabs(w1)) * dt / (2 * dZ), s12 = (w1 + fabs(w1)) * dt / (2 * dZ);
             const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
             const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
             const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
@@ -869,101 +916,151 @@ __global__ void __launch_bounds__(128) k_polymer_adj3(PolyAdjArgs<T> a, Geo g) {
             const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
             const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
             const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
-            const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-            const int hym = g.walls ? h : hix(g, i, jm, k), hyp = g.walls ? h : hix(g, i, jp, k);
-            const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
-            const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-            // face weights of the cell's own faces and of the neighbours' faces,
-            // by selection code
             const W3<T> wpx = wface_p<T>(isx), wnx = wface_n<T>(isx), wpy = wface_p<T>(isy), wny = wface_n<T>(isy);
             const W3<T> wpz = wface_p<T>(isz), wnz = wface_n<T>(isz);
             const W3<T> qx = wface_p<T>(cxp + 1), rx = wface_n<T>(cxm + 1), qy = wface_p<T>(cyp + 1), ry = wface_n<T>(cym + 1);
             const W3<T> qz = wface_p<T>(czp + 1), rz = wface_n<T>(czm + 1);
+            // weights of one direction: own p / n faces (coefficients sp, sn),
+            // the + neighbour's p face (sq) and the - neighbour's n face (sr),
+            // at offsets -2, -1, +1, +2; the centre weights are summed in kc
+            T kc = T(0);
+            auto dirw = [&](W3<T> wp_, W3<T> wn_, W3<T> wq, W3<T> wr, T sp, T sn, T sq, T sr, int base) {
+                put(base + 0, sr * wr.m);
+                put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
+                put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
+                put(base + 3, sq * wq.p);
+                kc += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
+            };
+            dirw(wpx, wnx, qx, rx, s3, s2, s1, s4, PS_KX);
+            dirw(wpy, wny, qy, ry, s7, s6, s5, s8, PS_KY);
+            dirw(wpz, wnz, qz, rz, s11, s10, s9, s12, PS_KZ);
+            put(PS_KC, kc);
+            // adjoints of s1..s12: mu . (face value), faces rebuilt from C^n
+            const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+            const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+            const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
+            T l1 = T(0), l2 = T(0), l3 = T(0), l4 = T(0), l5 = T(0), l6 = T(0);
+            T l7 = T(0), l8 = T(0), l9 = T(0), l10 = T(0), l11 = T(0), l12 = T(0);
+            auto face = [](W3<T> wt, T cmv, T c0v, T cpv) { return wt.m * cmv + wt.c * c0v + wt.p * cpv; };
 #pragma unroll
             for (int m = 0; m < 6; ++m) {
                 const T *Cm = a.C + m * cs;
-                T *Lm = a.lC + m * cs;
                 const T mum = mu[m];
-                T lc0 = T(0);   // accumulated weight at the cell itself
-                // one direction: own faces (code is, coefficients sp on the p face, sn on the n face),
-                // the + neighbour's p face (code cp_, coefficient sq), the - neighbour's n face (code cm_, sr)
-                auto dir = [&](W3<T> wp_, W3<T> wn_, int off, int hp, W3<T> wq, int hm, W3<T> wr, T sp, T sn,
-                               T sq, T sr, T &lsp, T &lsn, T &lsq, T &lsr) {
-                    const T cmv = Cm[h - off], c0v = Cm[h], cpv = Cm[h + off];
-                    lsp += mum * (wp_.m * cmv + wp_.c * c0v + wp_.p * cpv);
-                    lsn += mum * (wn_.m * cmv + wn_.c * c0v + wn_.p * cpv);
-                    const T am = mum * (sp * wp_.m + sn * wn_.m);
-                    const T ap = mum * (sp * wp_.p + sn * wn_.p);
-                    lc0 += mum * (sp * wp_.c + sn * wn_.c);
-                    if (am != T(0)) atomicAdd(&Lm[h - off], am);
-                    if (ap != T(0)) atomicAdd(&Lm[h + off], ap);
-                    // + neighbour's p face
-                    lsq += mum * (wq.m * Cm[hp - off] + wq.c * Cm[hp] + wq.p * Cm[hp + off]);
-                    {
-                        const T b = mum * sq;
-                        if (b != T(0)) {
-                            if (wq.m != T(0)) atomicAdd(&Lm[hp - off], b * wq.m);
-                            atomicAdd(&Lm[hp], b * wq.c);
-                            if (wq.p != T(0)) atomicAdd(&Lm[hp + off], b * wq.p);
-                        }
-                    }
-                    // - neighbour's n face
-                    lsr += mum * (wr.m * Cm[hm - off] + wr.c * Cm[hm] + wr.p * Cm[hm + off]);
-                    {
-                        const T b = mum * sr;
-                        if (b != T(0)) {
-                            if (wr.m != T(0)) atomicAdd(&Lm[hm - off], b * wr.m);
-                            atomicAdd(&Lm[hm], b * wr.c);
-                            if (wr.p != T(0)) atomicAdd(&Lm[hm + off], b * wr.p);
-                        }
-                    }
-                };
-                // x: pxm (s3, own p), nxp (s2, own n), pxp (s1, neighbour i+1), nxm (s4, neighbour i-1)
-                dir(wpx, wnx, ox, hxp, qx, hxm, rx, s[3], s[2], s[1], s[4], ls[3], ls[2], ls[1], ls[4]);
-                if (!g.walls) {
-                    dir(wpy, wny, oy, hyp, qy, hym, ry, s[7], s[6], s[5], s[8], ls[7], ls[6], ls[5], ls[8]);
-                } else {
-                    // rows j-2 .. j+2 of the column, zero beyond the ghost rows
-                    auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
-                    auto yadd = [&](int jj, T val) {
-                        if (val != T(0) && jj >= 0 && jj <= g.ny + 1) atomicAdd(&Lm[hix(g, i, jj, k)], val);
-                    };
-                    const T cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
-                    ls[7] += mum * (wpy.m * cmv + wpy.c * c0v + wpy.p * cpv);
-                    ls[6] += mum * (wny.m * cmv + wny.c * c0v + wny.p * cpv);
-                    yadd(j - 1, mum * (s[7] * wpy.m + s[6] * wny.m));
-                    yadd(j + 1, mum * (s[7] * wpy.p + s[6] * wny.p));
-                    lc0 += mum * (s[7] * wpy.c + s[6] * wny.c);
-                    // the p face of cell j+1 (rows j .. j+2), the n face of cell j-1 (rows j-2 .. j)
-                    ls[5] += mum * (qy.m * c0v + qy.c * cpv + qy.p * yv(j + 2));
-                    const T bq = mum * s[5];
-                    lc0 += bq * qy.m;
-                    yadd(j + 1, bq * qy.c);
-                    yadd(j + 2, bq * qy.p);
-                    ls[8] += mum * (ry.m * yv(j - 2) + ry.c * cmv + ry.p * c0v);
-                    const T br = mum * s[8];
-                    yadd(j - 2, br * ry.m);
-                    yadd(j - 1, br * ry.c);
-                    lc0 += br * ry.p;
+                {
+                    const T cmv = Cm[h - ox], c0v = Cm[h], cpv = Cm[h + ox];
+                    l3 += mum * face(wpx, cmv, c0v, cpv);
+                    l2 += mum * face(wnx, cmv, c0v, cpv);
+                    l1 += mum * face(qx, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+                    l4 += mum * face(rx, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
                 }
-                dir(wpz, wnz, oz, hzp, qz, hzm, rz, s[11], s[10], s[9], s[12], ls[11], ls[10], ls[9], ls[12]);
-                atomicAdd(&Lm[h], lc0);
+                if (!g.walls) {
+                    const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+                    const T cmv = Cm[h - oy], c0v = Cm[h], cpv = Cm[h + oy];
+                    l7 += mum * face(wpy, cmv, c0v, cpv);
+                    l6 += mum * face(wny, cmv, c0v, cpv);
+                    l5 += mum * face(qy, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+                    l8 += mum * face(ry, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+                } else {
+                    auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
+                    const T cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
+                    l7 += mum * face(wpy, cmv, c0v, cpv);
+                    l6 += mum * face(wny, cmv, c0v, cpv);
+                    l5 += mum * face(qy, c0v, cpv, yv(j + 2));
+                    l8 += mum * face(ry, yv(j - 2), cmv, c0v);
+                }
+                {
+                    const T cmv = Cm[h - oz], c0v = Cm[h], cpv = Cm[h + oz];
+                    l11 += mum * face(wpz, cmv, c0v, cpv);
+                    l10 += mum * face(wnz, cmv, c0v, cpv);
+                    l9 += mum * face(qz, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
+                    l12 += mum * face(rz, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
+                }
             }
-            // s coefficients -> velocities
-            {
-                const T cx = dt / (2 * dX), cy = dt / (2 * dY), cz = dt / (2 * dZ);
-                const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
-                addu(i, j, k, (ls[1] * (T(-1) + su2) + ls[2] * (T(-1) - su2)) * cx);
-                addu(i - 1, j, k, (ls[3] * (T(1) - su1) + ls[4] * (T(1) + su1)) * cx);
-                addv(i, j, k, (ls[5] * (T(-1) + sv2) + ls[6] * (T(-1) - sv2)) * cy);
-                addv(i, j - 1, k, (ls[7] * (T(1) - sv1) + ls[8] * (T(1) + sv1)) * cy);
-                addw(i, j, k, (ls[9] * (T(-1) + sw2) + ls[10] * (T(-1) - sw2)) * cz);
-                addw(i, j, k - 1, (ls[11] * (T(1) - sw1) + ls[12] * (T(1) + sw1)) * cz);
-            }
+            const T cx = dt / (2 * dX), cy = dt / (2 * dY), cz = dt / (2 * dZ);
+            const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
+            put(PS_SF + 0, (l1 * (T(-1) + su2) + l2 * (T(-1) - su2)) * cx);    // -> u(i)
+            put(PS_SF + 1, (l3 * (T(1) - su1) + l4 * (T(1) + su1)) * cx);      // -> u(i-1)
+            put(PS_SF + 2, (l5 * (T(-1) + sv2) + l6 * (T(-1) - sv2)) * cy);    // -> v(j)
+            put(PS_SF + 3, (l7 * (T(1) - sv1) + l8 * (T(1) + sv1)) * cy);      // -> v(j-1)
+            put(PS_SF + 4, (l9 * (T(-1) + sw2) + l10 * (T(-1) - sw2)) * cz);   // -> w(k)
+            put(PS_SF + 5, (l11 * (T(1) - sw1) + l12 * (T(1) + sw1)) * cz);    // -> w(k-1)
         }
     }
     block_atomic_add((double)gwi, a.grad + 0);
     block_atomic_add((double)gl2, a.grad + 2);
+}
+
+template <typename T>
+struct PolyGatherArgs {
+    const T *src;             // POLY_SRC halo-layout arrays of k_polyadj_src (updated cells)
+    T *lC;                    // out: adjoint of C^n (updated cells; zero elsewhere)
+    T *lU, *lV, *lW;          // += the velocity adjoint (full halo box)
+    int cs;
+};
+
+// Polymer, pass 2 (every position of the halo box): the adjoint of C^n at the
+// updated cells from the Cstar weights of the cells whose upwind sums read it
+// (periodic directions wrapped, as the forward reads them; with walls the
+// rows beyond the ghost rows hold zero C and are not read), and the adjoint
+// of U, V, W from the velocity-gradient and upwind-coefficient entries.
+template <typename T>
+__global__ void __launch_bounds__(256) k_polyadj_gather(PolyGatherArgs<T> a, Geo g) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cs = a.cs;
+    if (t >= cs) return;
+    const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
+    const int r0 = prow0(g), r1 = prow0(g) + prows(g) - 1;
+    auto upd = [&](int x, int y, int z) { return x >= 1 && x <= g.nx && y >= r0 && y <= r1 && z >= 1 && z <= g.nz; };
+    auto S = [&](int q, int x, int y, int z) { return a.src[(size_t)q * cs + hix(g, x, y, z)]; };
+    // velocity adjoint
+    T lu = T(0), lv = T(0), lw = T(0);
+    auto add = [&](T &acc, int q, int x, int y, int z, T sign) { if (upd(x, y, z)) acc += sign * S(q, x, y, z); };
+    add(lu, PS_GU + 0, i, j, k, T(-1));        add(lu, PS_GU + 0, i + 1, j, k, T(1));
+    add(lu, PS_GU + 1, i + 1, j + 1, k, T(1));  add(lu, PS_GU + 1, i, j + 1, k, T(1));
+    add(lu, PS_GU + 1, i + 1, j - 1, k, T(-1)); add(lu, PS_GU + 1, i, j - 1, k, T(-1));
+    add(lu, PS_GU + 2, i + 1, j, k + 1, T(1));  add(lu, PS_GU + 2, i, j, k + 1, T(1));
+    add(lu, PS_GU + 2, i + 1, j, k - 1, T(-1)); add(lu, PS_GU + 2, i, j, k - 1, T(-1));
+    add(lu, PS_SF + 0, i, j, k, T(1));          add(lu, PS_SF + 1, i + 1, j, k, T(1));
+    add(lv, PS_GV + 0, i + 1, j + 1, k, T(1));  add(lv, PS_GV + 0, i - 1, j + 1, k, T(-1));
+    add(lv, PS_GV + 0, i + 1, j, k, T(1));      add(lv, PS_GV + 0, i - 1, j, k, T(-1));
+    add(lv, PS_GV + 1, i, j + 1, k, T(1));      add(lv, PS_GV + 1, i, j, k, T(-1));
+    add(lv, PS_GV + 2, i, j + 1, k + 1, T(1));  add(lv, PS_GV + 2, i, j, k + 1, T(1));
+    add(lv, PS_GV + 2, i, j + 1, k - 1, T(-1)); add(lv, PS_GV + 2, i, j, k - 1, T(-1));
+    add(lv, PS_SF + 2, i, j, k, T(1));          add(lv, PS_SF + 3, i, j + 1, k, T(1));
+    add(lw, PS_GW + 0, i + 1, j, k + 1, T(1));  add(lw, PS_GW + 0, i - 1, j, k + 1, T(-1));
+    add(lw, PS_GW + 0, i + 1, j, k, T(1));      add(lw, PS_GW + 0, i - 1, j, k, T(-1));
+    add(lw, PS_GW + 1, i, j + 1, k + 1, T(1));  add(lw, PS_GW + 1, i, j - 1, k + 1, T(-1));
+    add(lw, PS_GW + 1, i, j + 1, k, T(1));      add(lw, PS_GW + 1, i, j - 1, k, T(-1));
+    add(lw, PS_GW + 2, i, j, k + 1, T(1));      add(lw, PS_GW + 2, i, j, k, T(-1));
+    add(lw, PS_SF + 4, i, j, k, T(1));          add(lw, PS_SF + 5, i, j, k + 1, T(1));
+    a.lU[t] += lu;
+    a.lV[t] += lv;
+    a.lW[t] += lw;
+    // adjoint of C^n at the updated cells
+    if (!upd(i, j, k)) {
+        for (int m = 0; m < 6; ++m) a.lC[(size_t)m * cs + t] = T(0);
+        return;
+    }
+    T l[6];
+    {
+        const T kc = S(PS_KC, i, j, k);
+        for (int m = 0; m < 6; ++m) l[m] = kc * S(PS_MU + m, i, j, k);
+    }
+    // source cell n = p - o e reads p with its offset-o weight
+    auto line = [&](int base, int x, int y, int z, int oq) {
+        const T kw = S(base + oq, x, y, z);
+        for (int m = 0; m < 6; ++m) l[m] += kw * S(PS_MU + m, x, y, z);
+    };
+    const int offs[4] = {-2, -1, 1, 2};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int o = offs[q];
+        line(PS_KX, wrapx(g, i - o), j, k, q);
+        line(PS_KZ, i, j, wrapz(g, k - o), q);
+        if (!g.walls) line(PS_KY, i, wrapy(g, j - o), k, q);
+        else if (j - o >= r0 && j - o <= r1) line(PS_KY, i, j - o, k, q);
+    }
+    for (int m = 0; m < 6; ++m) a.lC[(size_t)m * cs + t] = l[m];
 }
 
 // interior of a halo field (reference layout) into an adjoint field, zero halo

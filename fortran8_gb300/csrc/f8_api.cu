@@ -905,7 +905,7 @@ int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
     if (!G.A.grad) {
         AdjState &A = G.A;
         for (double **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(0, p, cs));
-        for (double **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(0, p, 6 * cs));
+        for (double **p : {&A.lC, &A.lC2}) API_CUDA(c, G.get(0, p, 6 * cs));
         for (int q = 0; q < 3; ++q) {
             API_CUDA(c, G.get(0, &A.lA0[q], ni));
             API_CUDA(c, G.get(0, &A.lT0[q], ni));
@@ -914,6 +914,7 @@ int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
             API_CUDA(c, G.get(0, &A.lQ[q], cs));
         }
         API_CUDA(c, G.get(0, &A.pack, ni));
+        API_CUDA(c, G.get(0, &A.work, ADJ_WORK_FIELDS * cs));
         API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
     }
     if (K > G.K) {
@@ -1019,7 +1020,7 @@ int grad_alloc_mixed(f8_ctx *c, int K, int nck, int nsteps) {
     if (!G.AF.grad) {
         AdjStateF &A = G.AF;
         for (float **p : {&A.lU, &A.lV, &A.lW, &A.lP, &A.lPhi}) API_CUDA(c, G.get(0, p, cs));
-        for (float **p : {&A.lC, &A.lC2, &A.lC0}) API_CUDA(c, G.get(0, p, 6 * cs));
+        for (float **p : {&A.lC, &A.lC2}) API_CUDA(c, G.get(0, p, 6 * cs));
         for (int q = 0; q < 3; ++q) {
             API_CUDA(c, G.get(0, &A.lA0[q], ni));
             API_CUDA(c, G.get(0, &A.lT0[q], ni));
@@ -1031,6 +1032,7 @@ int grad_alloc_mixed(f8_ctx *c, int K, int nck, int nsteps) {
         API_CUDA(c, G.get(0, &A.qlo, cs));
         API_CUDA(c, G.get(0, &A.zero, ni));
         API_CUDA(c, G.get(0, &A.rdef, ni));
+        API_CUDA(c, G.get(0, &A.work, ADJ_WORK_FIELDS * cs));
         API_CUDA(c, cudaMemsetAsync(A.zero, 0, ni * sizeof(float), c->s));
         API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
     }

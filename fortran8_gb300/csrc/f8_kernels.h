@@ -169,12 +169,14 @@ cudaError_t device_slice(Dev &d, bool mixed, int axis, int variant, double *dev_
 cudaError_t device_diagnostics(Dev &d, bool mixed, double *part, double *out, DiagValues *res, cudaStream_t s);
 // Discrete adjoint of the FP64 3D step (f8_adjoint.cu).  Adjoint fields are
 // full halo arrays whose halo cells are zero between stages.
+constexpr int ADJ_WORK_FIELDS = 34;   // the largest per-cell source set of the gather kernels
 struct AdjState {
     double *lU, *lV, *lW, *lP, *lPhi;      // state U, V, W, P and the pressure correction
-    double *lC, *lC2, *lC0;                // C, a second C buffer, C0 = f C - I (6 fields each)
+    double *lC, *lC2;                      // C and a second C buffer (6 fields each)
     double *lA0[3], *lT0[3];               // AB2 histories (interior)
     double *lUa[3], *lUp[3], *lQ[3];       // explicit velocity, Helmholtz solution, right-hand side
     double *pack;                          // one packed interior field
+    double *work;                          // per-cell sources of the gather kernels (ADJ_WORK_FIELDS halo fields)
     double *grad;                          // dJ/d(Wi, beta, L^2, (xc, yc) per cylinder), accumulated
 };
 // what the reverse of one step reads from its forward step
@@ -195,12 +197,13 @@ cudaError_t take_interior(const double *src, double *dst, const Geo &g, int n, c
 // stage transposes as the FP64 adjoint in FP32, reading a MixTape.
 struct AdjStateF {
     float *lU, *lV, *lW, *lP, *lPhi;
-    float *lC, *lC2, *lC0;
+    float *lC, *lC2;
     float *lA0[3], *lT0[3];
     float *lUa[3], *lUp[3], *lQ[3];
     float *pack;
     float *qlo;              // low part of the refined pressure adjoint (halo, with lQ[0] its high part)
     float *zero, *rdef;      // interior: zeros (the right-hand side's low part), the defect
+    float *work;             // per-cell sources of the gather kernels (ADJ_WORK_FIELDS halo fields)
     double *grad;
 };
 // FP32 solves of the mixed step (f8_step_mixed.cu); mode 0 writes dst, mode 2

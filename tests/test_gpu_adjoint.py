@@ -156,6 +156,37 @@ def _adjoint_workload(beta=None):
     return w, configs.initial_state(w)
 
 
+def _workload_fd(gpu, w, st, n, qs_rel):
+    """Central differences of the mean x drag over n steps from st, with the
+    relative step h_q = rel * |p_q| for each parameter index q in qs_rel."""
+    base = param_vector(w)
+    fds = {}
+    for q, rel in qs_rel.items():
+        h = rel * max(abs(base[q]), 1.0)
+        vals = []
+        for sgn in (1, -1):
+            b = base.copy()
+            b[q] += sgn * h
+            wq = with_params(w, b)
+            with Solver(gpu, wq.grid, wq.phys, wq.cyls) as s:
+                s.load(st, 0)
+                _, drag = s.step(n)
+            vals.append(drag[:, :, 0].sum() / n)
+        fds[q] = (vals[0] - vals[1]) / (2 * h)
+    return fds
+
+
+def _adjoint_workload(beta=None):
+    from dataclasses import replace
+    from fortran8_gb300 import configs
+    w = configs.c4_adjoint()
+    assert (w.grid.nx, w.grid.ny, w.grid.nz, w.steps) == (128, 64, 64, 400)
+    w = replace(w, cyls=tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls))
+    if beta is not None:
+        w = replace(w, phys=replace(w.phys, beta=beta))
+    return w, configs.initial_state(w)
+
+
 def test_grad_adjoint_workload_matches_central_differences(gpu):
     """The 128 x 64 x 64 channel with 2 cylinders (r = 0.3), Re 300, Wi 3,
     beta 0.85, L^2 400, dt 5e-4, from its seeded initial state (seed 3, C = I):
@@ -186,12 +217,14 @@ def test_grad_adjoint_workload_matches_central_differences(gpu):
 
 def test_grad_newtonian_adjoint_workload_matches_central_differences(gpu):
     """The same workload with beta = 1 (no polymer stage, hence no candidate
-    choice): beta and the centre gradients over 400 steps within 1e-4 of
-    central differences with h = 1e-4 |beta| and 1e-5 |centre|."""
+    choice): the centre gradients over 400 steps within 1e-4 of central
+    differences with h = 1e-5 |centre|.  beta is not differenced here: at
+    beta = 1 the step zeroes C and skips the polymer stage (fenep.f90:2479-2485),
+    while any beta != 1 runs it, so J is not differentiable in beta there."""
     w, st = _adjoint_workload(beta=1.0)
     n, K = w.steps, 20
     J, dp, _, _, _ = gpu_grad(gpu, w, st, 0, n, K=K)
-    fds = _workload_fd(gpu, w, st, n, {1: 1e-4, 3: 1e-5, 4: 1e-5, 5: 1e-5, 6: 1e-5})
+    fds = _workload_fd(gpu, w, st, n, {3: 1e-5, 4: 1e-5, 5: 1e-5, 6: 1e-5})
     print("adjoint", list(dp), "central differences", fds)
     for q, fd in fds.items():
         assert abs(dp[q] - fd) <= 1e-4 * abs(fd), (q, dp[q], fd)
