@@ -32,8 +32,9 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
     const double kap = dt * beta / re / 2.0;
     const unsigned nb = (unsigned)((cs + 255) / 256);
     dim3 blk(32, 8);
+    const AdjCoef<double> kc = adj_coef<double>(g);
     // 6. projection / pressure update
-    k_march_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lP, A.lPhi, t.Phi, g, kap, dt / (2.0 * re), A.grad); count_launch();
+    k_march_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lP, A.lPhi, t.Phi, g, kap, dt / (2.0 * re), kc, A.grad); count_launch();
     F8_CUDA_RET(fold(fold_set<double>({{A.lPhi, BC_P}}), g, s));
     // 5. Poisson
     k_pack<double><<<adj_cells(g, blk), blk, 0, s>>>(A.lPhi, A.pack, g); count_launch();
@@ -72,6 +73,7 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
         ma.vis = beta / re; ma.coef_t = (1.0 - beta) / (re * wi);
         ma.c_helm = dt / (2.0 * re); ma.inv_re = 1.0 / re;
         ma.grad = A.grad;
+        ma.kc = kc;
         k_momadj_src<double><<<adj_cells(g, blk), blk, 0, s>>>(ma, A.work, g); count_launch();
         MomGatherArgs<double> mg{};
         mg.U = t.U; mg.V = t.V; mg.W = t.W; mg.src = A.work;
@@ -79,6 +81,7 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
         mg.cs = cs; mg.polymer = polymer ? 1 : 0;
         mg.lp2 = d.ph.lp2; mg.inv_1mb = 1.0 / (1.0 - beta); mg.inv_wi = 1.0 / wi;
         mg.grad = A.grad;
+        mg.kc = kc;
         k_momadj_gather<double><<<nb, 256, 0, s>>>(mg, g); count_launch();
     }
     // 1. polymer: per-cell implicit-function adjoint and Cstar weights, then
@@ -92,6 +95,7 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
         pa.C = t.C; pa.Cn = t.Cn; pa.codes = t.codes; pa.codes_g = t.codes_g; pa.U = t.U; pa.V = t.V; pa.W = t.W;
         pa.lX = A.lC;
         pa.cs = cs; pa.dt = dt; pa.wi = wi; pa.lp2 = d.ph.lp2; pa.grad = A.grad;
+        pa.kc = kc; pa.dtwi = dt / wi; pa.dtwi2 = dt / (wi * wi);
         dim3 pb(32, 4);
         const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
         k_polyadj_src<double><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();

@@ -53,6 +53,35 @@ __device__ inline T lin(const T *A, const Geo &g, int i, int j, int k) {
 template <typename T>
 __device__ inline T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0)); }
 
+// Grid coefficients of the adjoint stencils in the arithmetic type T,
+// formed once on the host in FP64, so the kernels multiply instead of divide.
+template <typename T>
+struct AdjCoef {
+    T dt;
+    T id[3];     // 1/dX, 1/dY, 1/dZ
+    T id2[3];    // 1/dX^2, ...
+    T i4[3];     // 1/(4 dX), ...
+    T dtd[3];    // dt/dX, ...
+    T dt2d[3];   // dt/(2 dX), ...
+    T dt4d[3];   // dt/(4 dX), ...
+};
+
+template <typename T>
+inline AdjCoef<T> adj_coef(const Geo &g) {
+    AdjCoef<T> c{};
+    const double d[3] = {g.dx, g.dy, g.dz};
+    c.dt = T(g.dt);
+    for (int q = 0; q < 3; ++q) {
+        c.id[q] = T(1.0 / d[q]);
+        c.id2[q] = T(1.0 / (d[q] * d[q]));
+        c.i4[q] = T(1.0 / (4.0 * d[q]));
+        c.dtd[q] = T(g.dt / d[q]);
+        c.dt2d[q] = T(g.dt / (2.0 * d[q]));
+        c.dt4d[q] = T(g.dt / (4.0 * d[q]));
+    }
+    return c;
+}
+
 // Block sum of v added to *dst in FP64 (every thread of the block calls it).
 __device__ inline void block_atomic_add(double v, double *dst) {
     __shared__ double sh[32];
@@ -182,26 +211,25 @@ FoldSet<T> fold_c(T *C, int cs) {
 
 template <typename T>
 __global__ void k_march_adj(const T *lU, const T *lV, const T *lW, const T *lP, T *lPhi, const T *Phi, Geo g, T pc,
-                            T c_beta, double *grad) {
+                            T c_beta, AdjCoef<T> kc, double *grad) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int cs = g.sx * g.sy * g.sz;
     T gb = T(0);
     if (t < cs) {
         const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
-        const T dt = T(g.dt), dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz);
-        T lam = dt / dX * (lin(lU, g, i, j, k) - lin(lU, g, i - 1, j, k))
-              + dt / dY * (lin(lV, g, i, j, k) - lin(lV, g, i, j - 1, k))
-              + dt / dZ * (lin(lW, g, i, j, k) - lin(lW, g, i, j, k - 1));
+        T lam = kc.dtd[0] * (lin(lU, g, i, j, k) - lin(lU, g, i - 1, j, k))
+              + kc.dtd[1] * (lin(lV, g, i, j, k) - lin(lV, g, i, j - 1, k))
+              + kc.dtd[2] * (lin(lW, g, i, j, k) - lin(lW, g, i, j, k - 1));
         const T p0 = lin(lP, g, i, j, k);
-        const T lap = (lin(lP, g, i - 1, j, k) - 2 * p0 + lin(lP, g, i + 1, j, k)) / (dX * dX)
-                    + (lin(lP, g, i, j - 1, k) - 2 * p0 + lin(lP, g, i, j + 1, k)) / (dY * dY)
-                    + (lin(lP, g, i, j, k - 1) - 2 * p0 + lin(lP, g, i, j, k + 1)) / (dZ * dZ);
+        const T lap = (lin(lP, g, i - 1, j, k) - 2 * p0 + lin(lP, g, i + 1, j, k)) * kc.id2[0]
+                    + (lin(lP, g, i, j - 1, k) - 2 * p0 + lin(lP, g, i, j + 1, k)) * kc.id2[1]
+                    + (lin(lP, g, i, j, k - 1) - 2 * p0 + lin(lP, g, i, j, k + 1)) * kc.id2[2];
         lPhi[t] = lam + p0 - pc * lap;
         if (adj_inner(g, i, j, k) && p0 != T(0)) {
             const T ph = Phi[t];
-            const T lf = (Phi[hix(g, i - 1, j, k)] - 2 * ph + Phi[hix(g, i + 1, j, k)]) / (dX * dX)
-                       + (Phi[hix(g, i, j - 1, k)] - 2 * ph + Phi[hix(g, i, j + 1, k)]) / (dY * dY)
-                       + (Phi[hix(g, i, j, k - 1)] - 2 * ph + Phi[hix(g, i, j, k + 1)]) / (dZ * dZ);
+            const T lf = (Phi[hix(g, i - 1, j, k)] - 2 * ph + Phi[hix(g, i + 1, j, k)]) * kc.id2[0]
+                       + (Phi[hix(g, i, j - 1, k)] - 2 * ph + Phi[hix(g, i, j + 1, k)]) * kc.id2[1]
+                       + (Phi[hix(g, i, j, k - 1)] - 2 * ph + Phi[hix(g, i, j, k + 1)]) * kc.id2[2];
             gb = -c_beta * p0 * lf;
         }
     }
@@ -378,6 +406,7 @@ struct MomAdjArgs {
     const T *lQ[3];                   // adjoint of Q (interior of halo arrays)
     const T *lUa[3];                  // adjoint of Ua from the interpolation (interior)
     T *lA0[3], *lT0[3];               // in: adjoint of the new history; out: of the old
+    AdjCoef<T> kc;
     int cs, ab2_first, polymer;
     T vis, coef_t, c_helm;            // beta/Re, (1-beta)/(Re Wi), dt/(2 Re)
     T inv_re;
@@ -418,8 +447,10 @@ struct PolyAdjArgs {
     const uint8_t *codes, *codes_g;
     const T *U, *V, *W;               // U^n (halo)
     const T *lX;                      // adjoint of C^{n+1} (interior)
+    AdjCoef<T> kc;
     int cs;
     T dt, wi, lp2;
+    T dtwi, dtwi2;                    // dt/Wi, dt/Wi^2
     double *grad;
 };
 
@@ -467,6 +498,7 @@ __device__ inline void solve_jt6(const T (&A)[3][3], T dd2, T cf, const T (&x)[6
         for (int q = 0; q < 6; ++q) M[r][q] = J[q][r];
         M[r][6] = lx[r];
     }
+    T inv[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
 #pragma unroll
@@ -480,10 +512,10 @@ __device__ inline void solve_jt6(const T (&A)[3][3], T dd2, T cf, const T (&x)[6
                 M[r][q] = sw ? u0 : u1;
             }
         }
-        const T inv = T(1) / M[c][c];
+        inv[c] = T(1) / M[c][c];
 #pragma unroll
         for (int r = c + 1; r < 6; ++r) {
-            const T fr = M[r][c] * inv;
+            const T fr = M[r][c] * inv[c];
 #pragma unroll
             for (int q = 0; q < 7; ++q) {
                 if (q < c) continue;
@@ -497,7 +529,7 @@ __device__ inline void solve_jt6(const T (&A)[3][3], T dd2, T cf, const T (&x)[6
 #pragma unroll
         for (int q = 0; q < 6; ++q)
             if (q > r) s -= M[r][q] * mu[q];
-        mu[r] = s / M[r][r];
+        mu[r] = s * inv[r];
     }
 }
 
@@ -524,7 +556,8 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
     const int k = blockIdx.z + 1;
     T gb = T(0);
     if (i <= g.nx && j <= g.ny) {
-        const T dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz), dt = T(g.dt);
+        const AdjCoef<T> &kc = a.kc;
+        const T dt = kc.dt;
         const T h2 = T(0.5), h15 = T(1.5);
         const int o = qix(g, i, j, k), h = hix(g, i, j, k);
         const size_t cs = (size_t)a.cs;
@@ -550,9 +583,9 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
             src[(size_t)(9 + c) * cs + h] = a.polymer ? a.coef_t * lT : T(0);
             auto lap = [&](const T *X) {
                 const T x0 = X[h];
-                return (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) / (dX * dX)
-                     + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) / (dY * dY)
-                     + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) / (dZ * dZ);
+                return (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) * kc.id2[0]
+                     + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) * kc.id2[1]
+                     + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) * kc.id2[2];
             };
             // Helmholtz coefficient dt beta/(2 Re) and viscous coefficient beta/Re
             if (lq != T(0)) gb += a.c_helm * lq * lap(a.Up[c]);
@@ -570,6 +603,7 @@ struct MomGatherArgs {
     T *lP;                    // adjoint of P^n, += the pressure-gradient transpose
     const T *C;               // C as the stress read it (6 SoA halo fields)
     T *lC;                    // += the transpose of C0 = f(C) C - I (6 fields)
+    AdjCoef<T> kc;
     int cs, polymer;
     T lp2, inv_1mb, inv_wi;
     double *grad;
@@ -587,8 +621,9 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
     T g_coef = T(0), g_l2 = T(0);
     if (t < cs) {
         const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
-        const T dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz), dt = T(g.dt);
-        const T ix2 = T(1) / (dX * dX), iy2 = T(1) / (dY * dY), iz2 = T(1) / (dZ * dZ);
+        const AdjCoef<T> &kc = a.kc;
+        const T iX = kc.id[0], iY = kc.id[1], iZ = kc.id[2];
+        const T ix2 = kc.id2[0], iy2 = kc.id2[1], iz2 = kc.id2[2];
         const T *U = a.U, *V = a.V, *W = a.W;
         auto ev = [&](int x, int y, int z) { return x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz; };
         auto S = [&](int q, int x, int y, int z) { return a.src[(size_t)q * cs + hix(g, x, y, z)]; };
@@ -633,130 +668,130 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
         if (ev(i, j, k)) {
             const int x = i, y = j, z = k;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
-            lu += S(0, x, y, z) - 2 * S(6, x, y, z) * (ix2 + iy2 + iz2) + ga * (ax_t2(x, y, z) - ax_t1(x, y, z)) / dX
-                + ga / dY * (axy_a2(x, y, z) - axy_a1(x, y, z)) * h + ga / dZ * (axz_c2(x, y, z) - axz_c1(x, y, z)) * h
-                + gbv / dX * ayx_b2(x, y, z) * h + gc / dX * azx_b2(x, y, z) * h;
+            lu += S(0, x, y, z) - 2 * S(6, x, y, z) * (ix2 + iy2 + iz2) + ga * (ax_t2(x, y, z) - ax_t1(x, y, z)) * iX
+                + ga * iY * (axy_a2(x, y, z) - axy_a1(x, y, z)) * h + ga * iZ * (axz_c2(x, y, z) - axz_c1(x, y, z)) * h
+                + gbv * iX * ayx_b2(x, y, z) * h + gc * iX * azx_b2(x, y, z) * h;
         }
         if (ev(i + 1, j, k)) {
             const int x = i + 1, y = j, z = k;
-            lu += S(6, x, y, z) * ix2 - S(3, x, y, z) * ax_t1(x, y, z) / dX - S(4, x, y, z) / dX * ayx_b1(x, y, z) * h
-                - S(5, x, y, z) / dX * azx_b1(x, y, z) * h;
+            lu += S(6, x, y, z) * ix2 - S(3, x, y, z) * ax_t1(x, y, z) * iX - S(4, x, y, z) * iX * ayx_b1(x, y, z) * h
+                - S(5, x, y, z) * iX * azx_b1(x, y, z) * h;
         }
         if (ev(i - 1, j, k)) {
             const int x = i - 1, y = j, z = k;
-            lu += S(6, x, y, z) * ix2 + S(3, x, y, z) * ax_t2(x, y, z) / dX;
+            lu += S(6, x, y, z) * ix2 + S(3, x, y, z) * ax_t2(x, y, z) * iX;
         }
         if (ev(i, j + 1, k)) {
             const int x = i, y = j + 1, z = k;
-            lu += S(6, x, y, z) * iy2 - S(3, x, y, z) / dY * axy_a1(x, y, z) * h;
+            lu += S(6, x, y, z) * iy2 - S(3, x, y, z) * iY * axy_a1(x, y, z) * h;
         }
         if (ev(i, j - 1, k)) {
             const int x = i, y = j - 1, z = k;
-            lu += S(6, x, y, z) * iy2 + S(3, x, y, z) / dY * axy_a2(x, y, z) * h + S(4, x, y, z) / dX * ayx_b2(x, y, z) * h;
+            lu += S(6, x, y, z) * iy2 + S(3, x, y, z) * iY * axy_a2(x, y, z) * h + S(4, x, y, z) * iX * ayx_b2(x, y, z) * h;
         }
         if (ev(i, j, k + 1)) {
             const int x = i, y = j, z = k + 1;
-            lu += S(6, x, y, z) * iz2 - S(3, x, y, z) / dZ * axz_c1(x, y, z) * h;
+            lu += S(6, x, y, z) * iz2 - S(3, x, y, z) * iZ * axz_c1(x, y, z) * h;
         }
         if (ev(i, j, k - 1)) {
             const int x = i, y = j, z = k - 1;
-            lu += S(6, x, y, z) * iz2 + S(3, x, y, z) / dZ * axz_c2(x, y, z) * h + S(5, x, y, z) / dX * azx_b2(x, y, z) * h;
+            lu += S(6, x, y, z) * iz2 + S(3, x, y, z) * iZ * axz_c2(x, y, z) * h + S(5, x, y, z) * iX * azx_b2(x, y, z) * h;
         }
         if (ev(i + 1, j - 1, k)) {
             const int x = i + 1, y = j - 1, z = k;
-            lu -= S(4, x, y, z) / dX * ayx_b1(x, y, z) * h;
+            lu -= S(4, x, y, z) * iX * ayx_b1(x, y, z) * h;
         }
         if (ev(i + 1, j, k - 1)) {
             const int x = i + 1, y = j, z = k - 1;
-            lu -= S(5, x, y, z) / dX * azx_b1(x, y, z) * h;
+            lu -= S(5, x, y, z) * iX * azx_b1(x, y, z) * h;
         }
         // ---- V ----
         if (ev(i, j, k)) {
             const int x = i, y = j, z = k;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
-            lv += S(1, x, y, z) - 2 * S(7, x, y, z) * (ix2 + iy2 + iz2) + ga / dY * axy_b2(x, y, z) * h
-                + gbv / dX * (ayx_a2(x, y, z) - ayx_a1(x, y, z)) * h + gbv * (ay_t4(x, y, z) - ay_t3(x, y, z)) / dY
-                + gbv / dZ * (ayz_c2(x, y, z) - ayz_c1(x, y, z)) * h + gc / dY * azy_d2(x, y, z) * h;
+            lv += S(1, x, y, z) - 2 * S(7, x, y, z) * (ix2 + iy2 + iz2) + ga * iY * axy_b2(x, y, z) * h
+                + gbv * iX * (ayx_a2(x, y, z) - ayx_a1(x, y, z)) * h + gbv * (ay_t4(x, y, z) - ay_t3(x, y, z)) * iY
+                + gbv * iZ * (ayz_c2(x, y, z) - ayz_c1(x, y, z)) * h + gc * iY * azy_d2(x, y, z) * h;
         }
         if (ev(i + 1, j, k)) {
             const int x = i + 1, y = j, z = k;
-            lv += S(7, x, y, z) * ix2 - S(4, x, y, z) / dX * ayx_a1(x, y, z) * h;
+            lv += S(7, x, y, z) * ix2 - S(4, x, y, z) * iX * ayx_a1(x, y, z) * h;
         }
         if (ev(i - 1, j, k)) {
             const int x = i - 1, y = j, z = k;
-            lv += S(7, x, y, z) * ix2 + S(3, x, y, z) / dY * axy_b2(x, y, z) * h + S(4, x, y, z) / dX * ayx_a2(x, y, z) * h;
+            lv += S(7, x, y, z) * ix2 + S(3, x, y, z) * iY * axy_b2(x, y, z) * h + S(4, x, y, z) * iX * ayx_a2(x, y, z) * h;
         }
         if (ev(i, j + 1, k)) {
             const int x = i, y = j + 1, z = k;
-            lv += S(7, x, y, z) * iy2 - S(3, x, y, z) / dY * axy_b1(x, y, z) * h - S(4, x, y, z) * ay_t3(x, y, z) / dY
-                - S(5, x, y, z) / dY * azy_d1(x, y, z) * h;
+            lv += S(7, x, y, z) * iy2 - S(3, x, y, z) * iY * axy_b1(x, y, z) * h - S(4, x, y, z) * ay_t3(x, y, z) * iY
+                - S(5, x, y, z) * iY * azy_d1(x, y, z) * h;
         }
         if (ev(i, j - 1, k)) {
             const int x = i, y = j - 1, z = k;
-            lv += S(7, x, y, z) * iy2 + S(4, x, y, z) * ay_t4(x, y, z) / dY;
+            lv += S(7, x, y, z) * iy2 + S(4, x, y, z) * ay_t4(x, y, z) * iY;
         }
         if (ev(i, j, k + 1)) {
             const int x = i, y = j, z = k + 1;
-            lv += S(7, x, y, z) * iz2 - S(4, x, y, z) / dZ * ayz_c1(x, y, z) * h;
+            lv += S(7, x, y, z) * iz2 - S(4, x, y, z) * iZ * ayz_c1(x, y, z) * h;
         }
         if (ev(i, j, k - 1)) {
             const int x = i, y = j, z = k - 1;
-            lv += S(7, x, y, z) * iz2 + S(4, x, y, z) / dZ * ayz_c2(x, y, z) * h + S(5, x, y, z) / dY * azy_d2(x, y, z) * h;
+            lv += S(7, x, y, z) * iz2 + S(4, x, y, z) * iZ * ayz_c2(x, y, z) * h + S(5, x, y, z) * iY * azy_d2(x, y, z) * h;
         }
         if (ev(i - 1, j + 1, k)) {
             const int x = i - 1, y = j + 1, z = k;
-            lv -= S(3, x, y, z) / dY * axy_b1(x, y, z) * h;
+            lv -= S(3, x, y, z) * iY * axy_b1(x, y, z) * h;
         }
         if (ev(i, j + 1, k - 1)) {
             const int x = i, y = j + 1, z = k - 1;
-            lv -= S(5, x, y, z) / dY * azy_d1(x, y, z) * h;
+            lv -= S(5, x, y, z) * iY * azy_d1(x, y, z) * h;
         }
         // ---- W ----
         if (ev(i, j, k)) {
             const int x = i, y = j, z = k;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
-            lw += S(2, x, y, z) - 2 * S(8, x, y, z) * (ix2 + iy2 + iz2) + ga / dZ * axz_d2(x, y, z) * h
-                + gbv / dZ * ayz_d2(x, y, z) * h + gc / dX * (azx_a2(x, y, z) - azx_a1(x, y, z)) * h
-                + gc / dY * (azy_c2(x, y, z) - azy_c1(x, y, z)) * h + gc * (az_t6(x, y, z) - az_t5(x, y, z)) / dZ;
+            lw += S(2, x, y, z) - 2 * S(8, x, y, z) * (ix2 + iy2 + iz2) + ga * iZ * axz_d2(x, y, z) * h
+                + gbv * iZ * ayz_d2(x, y, z) * h + gc * iX * (azx_a2(x, y, z) - azx_a1(x, y, z)) * h
+                + gc * iY * (azy_c2(x, y, z) - azy_c1(x, y, z)) * h + gc * (az_t6(x, y, z) - az_t5(x, y, z)) * iZ;
         }
         if (ev(i + 1, j, k)) {
             const int x = i + 1, y = j, z = k;
-            lw += S(8, x, y, z) * ix2 - S(5, x, y, z) / dX * azx_a1(x, y, z) * h;
+            lw += S(8, x, y, z) * ix2 - S(5, x, y, z) * iX * azx_a1(x, y, z) * h;
         }
         if (ev(i - 1, j, k)) {
             const int x = i - 1, y = j, z = k;
-            lw += S(8, x, y, z) * ix2 + S(3, x, y, z) / dZ * axz_d2(x, y, z) * h + S(5, x, y, z) / dX * azx_a2(x, y, z) * h;
+            lw += S(8, x, y, z) * ix2 + S(3, x, y, z) * iZ * axz_d2(x, y, z) * h + S(5, x, y, z) * iX * azx_a2(x, y, z) * h;
         }
         if (ev(i, j + 1, k)) {
             const int x = i, y = j + 1, z = k;
-            lw += S(8, x, y, z) * iy2 - S(5, x, y, z) / dY * azy_c1(x, y, z) * h;
+            lw += S(8, x, y, z) * iy2 - S(5, x, y, z) * iY * azy_c1(x, y, z) * h;
         }
         if (ev(i, j - 1, k)) {
             const int x = i, y = j - 1, z = k;
-            lw += S(8, x, y, z) * iy2 + S(4, x, y, z) / dZ * ayz_d2(x, y, z) * h + S(5, x, y, z) / dY * azy_c2(x, y, z) * h;
+            lw += S(8, x, y, z) * iy2 + S(4, x, y, z) * iZ * ayz_d2(x, y, z) * h + S(5, x, y, z) * iY * azy_c2(x, y, z) * h;
         }
         if (ev(i, j, k + 1)) {
             const int x = i, y = j, z = k + 1;
-            lw += S(8, x, y, z) * iz2 - S(3, x, y, z) / dZ * axz_d1(x, y, z) * h - S(4, x, y, z) / dZ * ayz_d1(x, y, z) * h
-                - S(5, x, y, z) * az_t5(x, y, z) / dZ;
+            lw += S(8, x, y, z) * iz2 - S(3, x, y, z) * iZ * axz_d1(x, y, z) * h - S(4, x, y, z) * iZ * ayz_d1(x, y, z) * h
+                - S(5, x, y, z) * az_t5(x, y, z) * iZ;
         }
         if (ev(i, j, k - 1)) {
             const int x = i, y = j, z = k - 1;
-            lw += S(8, x, y, z) * iz2 + S(5, x, y, z) * az_t6(x, y, z) / dZ;
+            lw += S(8, x, y, z) * iz2 + S(5, x, y, z) * az_t6(x, y, z) * iZ;
         }
         if (ev(i - 1, j, k + 1)) {
             const int x = i - 1, y = j, z = k + 1;
-            lw -= S(3, x, y, z) / dZ * axz_d1(x, y, z) * h;
+            lw -= S(3, x, y, z) * iZ * axz_d1(x, y, z) * h;
         }
         if (ev(i, j - 1, k + 1)) {
             const int x = i, y = j - 1, z = k + 1;
-            lw -= S(4, x, y, z) / dZ * ayz_d1(x, y, z) * h;
+            lw -= S(4, x, y, z) * iZ * ayz_d1(x, y, z) * h;
         }
         // pressure gradient gp_c = -dt (P(o + e_c) - P(o)) / d_c, transposed
-        if (ev(i, j, k)) lp += dt / dX * S(0, i, j, k) + dt / dY * S(1, i, j, k) + dt / dZ * S(2, i, j, k);
-        if (ev(i - 1, j, k)) lp -= dt / dX * S(0, i - 1, j, k);
-        if (ev(i, j - 1, k)) lp -= dt / dY * S(1, i, j - 1, k);
-        if (ev(i, j, k - 1)) lp -= dt / dZ * S(2, i, j, k - 1);
+        if (ev(i, j, k)) lp += kc.dtd[0] * S(0, i, j, k) + kc.dtd[1] * S(1, i, j, k) + kc.dtd[2] * S(2, i, j, k);
+        if (ev(i - 1, j, k)) lp -= kc.dtd[0] * S(0, i - 1, j, k);
+        if (ev(i, j - 1, k)) lp -= kc.dtd[1] * S(1, i, j - 1, k);
+        if (ev(i, j, k - 1)) lp -= kc.dtd[2] * S(2, i, j, k - 1);
         a.lU[t] = lu;
         a.lV[t] = lv;
         a.lW[t] = lw;
@@ -765,11 +800,11 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
             // adjoint of C0 from the stress divergence (fenep.f90:645-691):
             // sT = coef_t lT of the interior cells whose stencils read C0 here
             auto st = [&](int c, int x, int y, int z) { return ev(x, y, z) ? S(9 + c, x, y, z) : T(0); };
-            const T q4x = T(1) / (4 * dX), q4y = T(1) / (4 * dY), q4z = T(1) / (4 * dZ);
+            const T q4x = kc.i4[0], q4y = kc.i4[1], q4z = kc.i4[2];
             T l0[6];
-            l0[0] = (st(0, i - 1, j, k) - st(0, i, j, k)) / dX;
-            l0[3] = (st(1, i, j - 1, k) - st(1, i, j, k)) / dY;
-            l0[5] = (st(2, i, j, k - 1) - st(2, i, j, k)) / dZ;
+            l0[0] = (st(0, i - 1, j, k) - st(0, i, j, k)) * iX;
+            l0[3] = (st(1, i, j - 1, k) - st(1, i, j, k)) * iY;
+            l0[5] = (st(2, i, j, k - 1) - st(2, i, j, k)) * iZ;
             l0[1] = q4y * (st(0, i, j - 1, k) + st(0, i - 1, j - 1, k) - st(0, i, j + 1, k) - st(0, i - 1, j + 1, k))
                   + q4x * (st(1, i - 1, j, k) + st(1, i - 1, j - 1, k) - st(1, i + 1, j, k) - st(1, i + 1, j - 1, k));
             l0[2] = q4z * (st(0, i, j, k - 1) + st(0, i - 1, j, k - 1) - st(0, i, j, k + 1) - st(0, i - 1, j, k + 1))
@@ -785,19 +820,20 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
                 for (int m = 0; m < 6; ++m) c[m] = a.C[(size_t)m * cs + t];
                 const T tr3 = (c[0] - T(1)) + (c[3] - T(1)) + (c[5] - T(1));
                 const T den = (a.lp2 - 3) - tr3;
-                const T f = (a.lp2 - 3) / den;
-                const T fm1 = tr3 / den;
+                const T iden = T(1) / den;
+                const T f = (a.lp2 - 3) * iden;
+                const T fm1 = tr3 * iden;
                 T lf = T(0);
                 for (int m = 0; m < 6; ++m) {
                     a.lC[(size_t)m * cs + t] += f * l0[m];
                     lf += c[m] * l0[m];
                     g_coef += (fm1 * c[m] + (c[m] - E[m])) * l0[m];
                 }
-                const T dfdtr = f / den;
+                const T dfdtr = f * iden;
                 a.lC[t] += lf * dfdtr;
                 a.lC[(size_t)3 * cs + t] += lf * dfdtr;
                 a.lC[(size_t)5 * cs + t] += lf * dfdtr;
-                g_l2 = -lf * tr3 / (den * den);
+                g_l2 = -lf * tr3 * (iden * iden);
             }
         }
     }
@@ -824,7 +860,8 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
         const size_t cs = (size_t)a.cs;
         const int h = hix(g, i, j, k);
         auto put = [&](int q, T v) { src[(size_t)q * cs + h] = v; };
-        const T dt = a.dt, wi = a.wi, lp2 = a.lp2, dX = T(g.dx), dY = T(g.dy), dZ = T(g.dz);
+        const AdjCoef<T> &kc = a.kc;
+        const T lp2 = a.lp2;
         T lx[6], x[6];
         bool any = false;
 #pragma unroll
@@ -842,15 +879,15 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
             auto v = [&](int p, int q, int r) { return rowv(V, g, p, q, r); };
             auto w = [&](int p, int q, int r) { return rowv(W, g, p, q, r); };
             T A0[3][3];
-            A0[0][0] = -dt * (-u(i - 1, j, k) + u(i, j, k)) / dX;
-            A0[0][1] = -dt * (-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) / (4 * dX);
-            A0[0][2] = -dt * (-w(i - 1, j, k - 1) + w(i + 1, j, k - 1) - w(i - 1, j, k) + w(i + 1, j, k)) / (4 * dX);
-            A0[1][0] = -dt * (-u(i - 1, j - 1, k) - u(i, j - 1, k) + u(i - 1, j + 1, k) + u(i, j + 1, k)) / (4 * dY);
-            A0[1][1] = -dt * (-v(i, j - 1, k) + v(i, j, k)) / dY;
-            A0[1][2] = -dt * (-w(i, j - 1, k - 1) + w(i, j + 1, k - 1) - w(i, j - 1, k) + w(i, j + 1, k)) / (4 * dY);
-            A0[2][0] = -dt * (-u(i - 1, j, k - 1) - u(i, j, k - 1) + u(i - 1, j, k + 1) + u(i, j, k + 1)) / (4 * dZ);
-            A0[2][1] = -dt * (-v(i, j - 1, k - 1) - v(i, j, k - 1) + v(i, j - 1, k + 1) + v(i, j, k + 1)) / (4 * dZ);
-            A0[2][2] = -dt * (-w(i, j, k - 1) + w(i, j, k)) / dZ;
+            A0[0][0] = -(-u(i - 1, j, k) + u(i, j, k)) * kc.dtd[0];
+            A0[0][1] = -(-v(i - 1, j - 1, k) + v(i + 1, j - 1, k) - v(i - 1, j, k) + v(i + 1, j, k)) * kc.dt4d[0];
+            A0[0][2] = -(-w(i - 1, j, k - 1) + w(i + 1, j, k - 1) - w(i - 1, j, k) + w(i + 1, j, k)) * kc.dt4d[0];
+            A0[1][0] = -(-u(i - 1, j - 1, k) - u(i, j - 1, k) + u(i - 1, j + 1, k) + u(i, j + 1, k)) * kc.dt4d[1];
+            A0[1][1] = -(-v(i, j - 1, k) + v(i, j, k)) * kc.dtd[1];
+            A0[1][2] = -(-w(i, j - 1, k - 1) + w(i, j + 1, k - 1) - w(i, j - 1, k) + w(i, j + 1, k)) * kc.dt4d[1];
+            A0[2][0] = -(-u(i - 1, j, k - 1) - u(i, j, k - 1) + u(i - 1, j, k + 1) + u(i, j, k + 1)) * kc.dt4d[2];
+            A0[2][1] = -(-v(i, j - 1, k - 1) - v(i, j, k - 1) + v(i, j - 1, k + 1) + v(i, j, k + 1)) * kc.dt4d[2];
+            A0[2][2] = -(-w(i, j, k - 1) + w(i, j, k)) * kc.dtd[2];
             T A[3][3];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
@@ -858,10 +895,11 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
                 for (int q = 0; q < 3; ++q) A[r][q] = A0[q][r];
             const T tr3 = (x[0] - T(1)) + (x[3] - T(1)) + (x[5] - T(1));
             const T den = (lp2 - 3) - tr3;
-            const T f = (lp2 - 3) / den;
-            const T fm1 = tr3 / den;
-            const T dd2 = T(1) + f * dt / wi;
-            const T cf = dt / wi * f / den;
+            const T iden = T(1) / den;
+            const T f = (lp2 - 3) * iden;
+            const T fm1 = tr3 * iden;
+            const T dd2 = T(1) + f * a.dtwi;
+            const T cf = a.dtwi * f * iden;
             T mu[6];
             solve_jt6(A, dd2, cf, x, lx, mu);
             T mx = T(0), mxe = T(0);
@@ -872,8 +910,8 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
                 mxe += mu[m] * (x[m] - E[m]);
                 put(PS_MU + m, mu[m]);
             }
-            gwi = dt / (wi * wi) * (fm1 * mx + mxe);
-            gl2 = dt / wi * tr3 / (den * den) * mx;
+            gwi = a.dtwi2 * (fm1 * mx + mxe);
+            gl2 = a.dtwi * tr3 * (iden * iden) * mx;
             // adjoint of the velocity-gradient entries, each scaled by the
             // coefficient of its stencil (A0 entries / dt d or dt 4d)
             T lAt[3][3];
@@ -886,26 +924,26 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
             lAt[2][0] = -(mu[2] * x[0] + mu[4] * x[1] + 2 * mu[5] * x[2]);
             lAt[2][1] = -(mu[2] * x[1] + mu[4] * x[3] + 2 * mu[5] * x[4]);
             lAt[2][2] = -(mu[2] * x[2] + mu[4] * x[4] + 2 * mu[5] * x[5]);
-            put(PS_GU + 0, lAt[0][0] * dt / dX);
-            put(PS_GU + 1, lAt[0][1] * dt / (4 * dY));
-            put(PS_GU + 2, lAt[0][2] * dt / (4 * dZ));
-            put(PS_GV + 0, lAt[1][0] * dt / (4 * dX));
-            put(PS_GV + 1, lAt[1][1] * dt / dY);
-            put(PS_GV + 2, lAt[1][2] * dt / (4 * dZ));
-            put(PS_GW + 0, lAt[2][0] * dt / (4 * dX));
-            put(PS_GW + 1, lAt[2][1] * dt / (4 * dY));
-            put(PS_GW + 2, lAt[2][2] * dt / dZ);
+            put(PS_GU + 0, lAt[0][0] * kc.dtd[0]);
+            put(PS_GU + 1, lAt[0][1] * kc.dt4d[1]);
+            put(PS_GU + 2, lAt[0][2] * kc.dt4d[2]);
+            put(PS_GV + 0, lAt[1][0] * kc.dt4d[0]);
+            put(PS_GV + 1, lAt[1][1] * kc.dtd[1]);
+            put(PS_GV + 2, lAt[1][2] * kc.dt4d[2]);
+            put(PS_GW + 0, lAt[2][0] * kc.dt4d[0]);
+            put(PS_GW + 1, lAt[2][1] * kc.dt4d[1]);
+            put(PS_GW + 2, lAt[2][2] * kc.dtd[2]);
             // Cstar: upwind coefficients s1..s12 and the selection codes
             const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
             const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
             const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
             const T sixth = T(1) / T(6);
-            const T s1 = (-u2 + fabs(u2)) * dt / (2 * dX), s2 = sixth + (-u2 - fabs(u2)) * dt / (2 * dX);
-            const T s3 = sixth + (u1 - fabs(u1)) * dt / (2 * dX), s4 = (u1 + fabs(u1)) * dt / (2 * dX);
-            const T s5 = (-v2 + fabs(v2)) * dt / (2 * dY), s6 = sixth + (-v2 - fabs(v2)) * dt / (2 * dY);
-            const T s7 = sixth + (v1 - fabs(v1)) * dt / (2 * dY), s8 = (v1 + fabs(v1)) * dt / (2 * dY);
-            const T s9 = (-w2 + fabs(w2)) * dt / (2 * dZ), s10 = sixth + (-w2 - fabs(w2)) * dt / (2 * dZ);
-            const T s11 = sixth + (w1 - fabs(w1)) * dt / (2 * dZ), s12 = (w1 + fabs(w1)) * dt / (2 * dZ);
+            const T s1 = (-u2 + fabs(u2)) * kc.dt2d[0], s2 = sixth + (-u2 - fabs(u2)) * kc.dt2d[0];
+            const T s3 = sixth + (u1 - fabs(u1)) * kc.dt2d[0], s4 = (u1 + fabs(u1)) * kc.dt2d[0];
+            const T s5 = (-v2 + fabs(v2)) * kc.dt2d[1], s6 = sixth + (-v2 - fabs(v2)) * kc.dt2d[1];
+            const T s7 = sixth + (v1 - fabs(v1)) * kc.dt2d[1], s8 = (v1 + fabs(v1)) * kc.dt2d[1];
+            const T s9 = (-w2 + fabs(w2)) * kc.dt2d[2], s10 = sixth + (-w2 - fabs(w2)) * kc.dt2d[2];
+            const T s11 = sixth + (w1 - fabs(w1)) * kc.dt2d[2], s12 = (w1 + fabs(w1)) * kc.dt2d[2];
             const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
             const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
             const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
@@ -922,19 +960,19 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
             const W3<T> qz = wface_p<T>(czp + 1), rz = wface_n<T>(czm + 1);
             // weights of one direction: own p / n faces (coefficients sp, sn),
             // the + neighbour's p face (sq) and the - neighbour's n face (sr),
-            // at offsets -2, -1, +1, +2; the centre weights are summed in kc
-            T kc = T(0);
+            // at offsets -2, -1, +1, +2; the centre weights are summed in kcen
+            T kcen = T(0);
             auto dirw = [&](W3<T> wp_, W3<T> wn_, W3<T> wq, W3<T> wr, T sp, T sn, T sq, T sr, int base) {
                 put(base + 0, sr * wr.m);
                 put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
                 put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
                 put(base + 3, sq * wq.p);
-                kc += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
+                kcen += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
             };
             dirw(wpx, wnx, qx, rx, s3, s2, s1, s4, PS_KX);
             dirw(wpy, wny, qy, ry, s7, s6, s5, s8, PS_KY);
             dirw(wpz, wnz, qz, rz, s11, s10, s9, s12, PS_KZ);
-            put(PS_KC, kc);
+            put(PS_KC, kcen);
             // adjoints of s1..s12: mu . (face value), faces rebuilt from C^n
             const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
             const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
@@ -976,7 +1014,7 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
                     l12 += mum * face(rz, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
                 }
             }
-            const T cx = dt / (2 * dX), cy = dt / (2 * dY), cz = dt / (2 * dZ);
+            const T cx = kc.dt2d[0], cy = kc.dt2d[1], cz = kc.dt2d[2];
             const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
             put(PS_SF + 0, (l1 * (T(-1) + su2) + l2 * (T(-1) - su2)) * cx);    // -> u(i)
             put(PS_SF + 1, (l3 * (T(1) - su1) + l4 * (T(1) + su1)) * cx);      // -> u(i-1)

@@ -77,9 +77,10 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
     const double kap = dt * beta / re / 2.0;
     const unsigned nb = (unsigned)((cs + 255) / 256);
     dim3 blk(32, 8);
+    const AdjCoef<float> kc = adj_coef<float>(g);
     // 6. projection / pressure update
     k_march_adj<float><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lP, A.lPhi, t.Phi, g, (float)kap, (float)(dt / (2.0 * re)),
-                                          A.grad); count_launch();
+                                          kc, A.grad); count_launch();
     F8_CUDA_RET(fold(fold_set<float>({{A.lPhi, BC_P}}), g, s));
     // 5. Poisson, refined as the forward's pressure solve: q0 = L^-1 r in FP32,
     // the defect r - L_h q0 in df64, q = q0 + L^-1 (defect) as a df64 pair
@@ -123,6 +124,7 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         ma.vis = (float)(beta / re); ma.coef_t = (float)((1.0 - beta) / (re * wi));
         ma.c_helm = (float)(dt / (2.0 * re)); ma.inv_re = (float)(1.0 / re);
         ma.grad = A.grad;
+        ma.kc = kc;
         k_momadj_src<float><<<adj_cells(g, blk), blk, 0, s>>>(ma, A.work, g); count_launch();
         MomGatherArgs<float> mg{};
         mg.U = t.U; mg.V = t.V; mg.W = t.W; mg.src = A.work;
@@ -130,6 +132,7 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         mg.cs = cs; mg.polymer = polymer ? 1 : 0;
         mg.lp2 = (float)(d.ph.lp2); mg.inv_1mb = (float)(1.0 / (1.0 - beta)); mg.inv_wi = (float)(1.0 / wi);
         mg.grad = A.grad;
+        mg.kc = kc;
         k_momadj_gather<float><<<nb, 256, 0, s>>>(mg, g); count_launch();
     }
     // 1. polymer: per-cell implicit-function adjoint and Cstar weights, then
@@ -143,6 +146,7 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         pa.C = t.C; pa.Cn = t.Cn; pa.codes = t.codes; pa.codes_g = t.codes_g; pa.U = t.U; pa.V = t.V; pa.W = t.W;
         pa.lX = A.lC;
         pa.cs = cs; pa.dt = (float)(dt); pa.wi = (float)(wi); pa.lp2 = (float)(d.ph.lp2); pa.grad = A.grad;
+        pa.kc = kc; pa.dtwi = (float)(dt / wi); pa.dtwi2 = (float)(dt / (wi * wi));
         dim3 pb(32, 4);
         const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
         k_polyadj_src<float><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
