@@ -28,6 +28,7 @@ module f8_gpu
     integer(c_int), parameter :: F8_FP64 = 0, F8_MIXED = 1
     integer(c_int), parameter :: F8_POISSON_FFT = 0, F8_POISSON_SOR = 1
     integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1
+    integer(c_int), parameter :: F8_IBM_CELL_VOLUME = 0, F8_IBM_ARC_VOLUME = 1
 
     type, bind(C) :: f8_grid
         integer(c_int) :: dim, nx, ny, nz
@@ -43,6 +44,8 @@ module f8_gpu
         real(c_double) :: sor_omega, sor_eps
         integer(c_int) :: sor_itrmax
         integer(c_int) :: ab2_start
+        integer(c_int) :: ibm_volume     ! 0: dX*dY*dZ (fenep), 1: pi*DC/NL*dX*dX (smac.f90:1129)
+        integer(c_int) :: ibm_repeats    ! NS of smac.f90:20 (1 in fenep)
     end type f8_phys
 
     type, bind(C) :: f8_cyl
@@ -109,7 +112,7 @@ module f8_gpu
         end function f8_store
 
         ! Gradient of J = sum(drag_weights * drag) + <seed, final state> by the
-        ! discrete adjoint (FP64 3D contexts).  drag_weights: real(8)
+        ! discrete adjoint (3D contexts, FP64 or mixed).  drag_weights: real(8)
         ! (3, ncyl, nsteps) or c_null_ptr (time-averaged total x drag); seed,
         ! dJ_dstate: c_loc of an f8_fields or c_null_ptr; J: real(8) or
         ! c_null_ptr; dJ_dparams: real(8) (3 + 2*ncyl) = dWi, dbeta, dL^2,

@@ -26,6 +26,8 @@ F8_POISSON_FFT = 0
 F8_POISSON_SOR = 1
 F8_BC_PERIODIC = 0
 F8_BC_WALLS = 1
+F8_IBM_CELL_VOLUME = 0
+F8_IBM_ARC_VOLUME = 1
 
 _dp = C.POINTER(C.c_double)
 
@@ -41,7 +43,7 @@ class Phys(C.Structure):
                 ("lp2", C.c_double), ("dt", C.c_double),
                 ("newton_dc", C.c_double), ("newton_eps", C.c_double), ("newton_itrmax", C.c_int),
                 ("sor_omega", C.c_double), ("sor_eps", C.c_double), ("sor_itrmax", C.c_int),
-                ("ab2_start", C.c_int)]
+                ("ab2_start", C.c_int), ("ibm_volume", C.c_int), ("ibm_repeats", C.c_int)]
 
 
 class Cyl(C.Structure):

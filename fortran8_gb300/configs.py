@@ -20,6 +20,14 @@ chosen so that dX = dY = dZ, which the IBM requires, fenep.f90:1808-1810):
                 beta 0.85, L^2 400, dt 5e-4.
 * ``c5_large``  512 x 256 x 256 channel, 4 x 2 cylinders r = 0.25, Re 1000,
                 Wi 8, beta 0.9, L^2 1600, dt 1e-4.
+* ``smac_rotating`` the Newtonian IBM case of smac.f90 (smac.f90:13-27,
+                1156-1196): (2pi)^3 periodic box, 64^3 (smac.f90 uses 144^3,
+                which the radix-2 transforms do not take), four rotating
+                surface-ring cylinders of diameter 2pi/6 at (pi/2 | 3pi/2)^2
+                with unit surface speed and alternating sense, Re =
+                U_C L_C / nu = 5400 for f_C = 2 rps, D_C = 0.03 m, nu = 1e-6,
+                dt 8e-5, markers spread with the arc element of their ring
+                (smac.f90:1129), noise 1e-3 on a fluid at rest.
 
 The channel is driven by the uniform body force Fx = 2 / (Re h^2), h = Ly/2,
 under which the laminar Newtonian profile is the Poiseuille base flow with
@@ -98,8 +106,20 @@ def c5_large(nx=512, ny=256, nz=256):
     return _channel("c5_large", nx, ny, nz, 1000.0, 8.0, 0.9, 1600.0, 1.0e-4, cyls, 200, 4, 1.0e-2)
 
 
+def smac_rotating(n=64, repeats=1):
+    g = GridSpec(3, n, n, n, 2 * PI, 2 * PI, 2 * PI)
+    dc = 2 * PI / 6.0
+    f_c, d_c, nu = 2.0, 0.03, 1.0e-6
+    re = (f_c * PI * d_c) * (d_c / dc) / nu
+    ph = PhysSpec(re=re, wi=1.0, beta=1.0, lp2=100.0, dt=8.0e-5, ibm_volume=abi.F8_IBM_ARC_VOLUME,
+                  ibm_repeats=repeats)
+    pos = ((PI / 2, PI / 2, 1.0), (3 * PI / 2, PI / 2, -1.0), (PI / 2, 3 * PI / 2, -1.0), (3 * PI / 2, 3 * PI / 2, 1.0))
+    cyls = tuple(CylSpec(x, y, dc / 2, spin=s, filled=0) for x, y, s in pos)
+    return Workload("smac_rotating", g, ph, cyls, 10, 5, 1.0e-3, "rest")
+
+
 WORKLOADS = {"c1_2d": c1_2d, "c2_3d": c2_3d, "c3_channel": c3_channel,
-             "c4_adjoint": c4_adjoint, "c5_large": c5_large}
+             "c4_adjoint": c4_adjoint, "c5_large": c5_large, "smac_rotating": smac_rotating}
 
 
 def initial_state(w: Workload) -> State:
@@ -119,6 +139,8 @@ def initial_state(w: Workload) -> State:
     u = np.zeros(shp); v = np.zeros(shp); wv = np.zeros(shp)
     if w.flow == "uniform":
         u[:] = 1.0
+    elif w.flow == "rest":
+        pass
     elif w.flow == "taylor_green":
         # u at (i dX, (j-1/2) dY, (k-1/2) dZ), v at ((i-1/2) dX, j dY, (k-1/2) dZ)
         u[:] = np.sin(i * dX) * np.cos((j - 0.5) * dY) * np.cos((k - 0.5) * dZ)

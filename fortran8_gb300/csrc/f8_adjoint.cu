@@ -51,7 +51,7 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
     if (d.nm > 0) {
         IbmAdjArgs<double> ia{};
         ia.mx = d.mx; ia.my = d.my; ia.mcyl = d.mcyl; ia.nm = d.nm; ia.ncyl = d.ncyl;
-        ia.dvol = (g.dx * g.dy) * g.dz; ia.dxn = g.dx * g.dx * g.dx; ia.dv = (g.dx * g.dy) * g.dz;
+        ia.dvol = (g.dx * g.dy) * g.dz; ia.dxn = g.dx * g.dx * g.dx; ia.mvol = d.mvol; ia.cylvol = d.cylvol;
         for (int c = 0; c < 3; ++c) {
             ia.Ua[c] = t.Ua[c]; ia.Fc[c] = t.Fc[c]; ia.lQ[c] = A.lQ[c]; ia.lUa[c] = A.lUa[c];
         }

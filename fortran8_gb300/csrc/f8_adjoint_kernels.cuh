@@ -290,7 +290,9 @@ struct IbmAdjArgs {
     const double *mx, *my;
     const int *mcyl;
     int nm, ncyl;
-    double dvol, dxn, dv;
+    double dvol, dxn;
+    const double *mvol;      // per marker: spreading volume
+    const double *cylvol;    // per cylinder: drag volume
     const T *Ua[3];          // forward Ua (halo, with boundary values)
     const double *Fc[3];     // forward marker forces
     const T *lQ[3];          // adjoint of the Helmholtz right-hand sides (interior)
@@ -325,7 +327,8 @@ __global__ void k_ibm_adj(IbmAdjArgs<T> a, Geo g) {
         const T fc = T(a.Fc[comp][fo]);
         const T *lQ = a.lQ[comp];
         const T *Ua = a.Ua[comp];
-        const T dvn = T(a.dxn / a.dvol);    // dX^3 / (dX dY dZ)
+        const T dvn = T(a.dxn / a.dvol);          // interpolation: dX^3 / (dX dY dZ)
+        const T svn = T(a.mvol[m] / a.dvol);      // spreading: marker volume / (dX dY dZ)
         T wxs[3], wys[3], wzs[3], dwx[3], dwy[3];
         for (int q = 0; q < 3; ++q) {
             double x = (i0 + q - 0.5) * dX, y = (j0 + q - 0.5) * dY, z = (n - 1 + q - 0.5) * dZ;
@@ -340,7 +343,7 @@ __global__ void k_ibm_adj(IbmAdjArgs<T> a, Geo g) {
             dwy[q] = -droma_t(ry) / T(dY);
         }
         // adjoint of Fc: drag weight + the folded spreading
-        T lfc = T(-a.dv * a.w[3 * l + comp]);
+        T lfc = T(-a.cylvol[l] * a.w[3 * l + comp]);
         T gx = T(0), gy = T(0);
         for (int kk = 0; kk < 3; ++kk) {
             const int k = n - 1 + kk;
@@ -358,9 +361,9 @@ __global__ void k_ibm_adj(IbmAdjArgs<T> a, Geo g) {
                     const int fi = i == 0 ? g.nx : (i == g.nx + 1 ? 1 : i);
                     const T lf = drop ? T(0) : dt * lQ[hix(g, fi, fj, fk)];
                     const T del = wxs[ii] * wys[jj] * wzs[kk];
-                    lfc += lf * del * dvn;
-                    gx += lf * fc * dvn * (dwx[ii] * wys[jj] * wzs[kk]);
-                    gy += lf * fc * dvn * (wxs[ii] * dwy[jj] * wzs[kk]);
+                    lfc += lf * del * svn;
+                    gx += lf * fc * svn * (dwx[ii] * wys[jj] * wzs[kk]);
+                    gy += lf * fc * svn * (wxs[ii] * dwy[jj] * wzs[kk]);
                 }
             }
         }

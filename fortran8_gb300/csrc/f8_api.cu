@@ -121,6 +121,7 @@ struct f8_ctx {
     f8_grid grid{};
     f8_phys phys{};
     std::vector<f8_cyl> cyl;
+    std::vector<double> cyl_vol;      // drag / spreading volume of each cylinder's markers
     std::vector<Marker> mk;
     int precision = 0, poisson = 0;
     Dev d{};
@@ -250,6 +251,14 @@ int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, in
     if (!(ph->dt > 0) || !(ph->re > 0) || !(ph->wi > 0)) return F8_ERR_ARG;
     if (ph->newton_itrmax < 1 || ph->sor_itrmax < 1) return F8_ERR_ARG;
     if (ncyl < 0 || (ncyl > 0 && !cy)) return F8_ERR_ARG;
+    if (ph->ibm_repeats < 1 || ph->ibm_repeats > 64) return F8_ERR_ARG;
+    if (ph->ibm_volume != F8_IBM_CELL_VOLUME && ph->ibm_volume != F8_IBM_ARC_VOLUME) return F8_ERR_ARG;
+    if (ph->ibm_volume == F8_IBM_ARC_VOLUME) {
+        // the arc element of a surface ring (smac.f90:1128-1129), 3D
+        if (g->dim != 3) return F8_ERR_UNSUPPORTED;
+        for (int l = 0; l < ncyl; ++l)
+            if (cy[l].filled) return F8_ERR_UNSUPPORTED;
+    }
     return F8_OK;
 }
 
@@ -303,6 +312,7 @@ int setup(f8_ctx *c) {
     g.dt = c->phys.dt; g.uwall = G.uwall;
     d.ph = Phys{c->phys.re, c->phys.wi, c->phys.beta, c->phys.lp2, c->phys.dt,
                 c->phys.newton_dc, c->phys.newton_eps, c->phys.newton_itrmax};
+    d.ibm_repeats = c->phys.ibm_repeats;
     d.ncomp = G.dim == 3 ? 6 : 3;
     d.cs = g.sx * g.sy * g.sz;
     d.ni = g.nx * g.ny * g.nz;
@@ -334,6 +344,8 @@ int setup(f8_ctx *c) {
         for (float **p : {&d.Uf, &d.Vf, &d.Wf, &d.Ul, &d.Vl, &d.Wl, &d.Pf, &d.Pl, &d.Phif, &d.Phil,
                           &d.dUf[0], &d.dUf[1], &d.dUf[2]})
             API_CUDA(c, c->alloc(p, cs));
+        if (c->phys.ibm_repeats > 1 && !c->cyl.empty())
+            for (int q = 0; q < 3; ++q) API_CUDA(c, c->alloc(&d.Qpre[q], ni));
         API_CUDA(c, c->alloc(&d.Cnf, cs * d.ncomp));
         c->cf_base = d.Cf;
         API_CUDA(c, c->alloc(&d.fpetf, cs));
@@ -485,6 +497,26 @@ int setup(f8_ctx *c) {
         if (int st = upload(c, &d.my, my)) return st;
         if (int st = upload(c, &d.mu, mu)) return st;
         if (int st = upload(c, &d.mv, mv)) return st;
+        {
+            // spreading volume of each marker and the drag volume of each
+            // cylinder: dX^3 (fenep.f90:2166-2187) with the cell volume as the
+            // drag's, or the arc element pi*DC/NL * dX * dX of the cylinder's
+            // ring (smac.f90:1128-1129, 1428-1446) for both
+            const double dxn = g.dim == 3 ? g.dx * g.dx * g.dx : g.dx * g.dx;
+            const double dvol = g.dim == 3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy;
+            std::vector<double> cv(c->cyl.size(), dvol), mvol(nm, dxn);
+            if (c->phys.ibm_volume == F8_IBM_ARC_VOLUME)
+                for (size_t l = 0; l < c->cyl.size(); ++l) {
+                    const double DC = 2.0 * c->cyl[l].r;
+                    const int NL = std::max(1, (int)std::lround(PI * DC / g.dx));
+                    cv[l] = PI * DC / NL * g.dx * g.dx;
+                }
+            if (c->phys.ibm_volume == F8_IBM_ARC_VOLUME)
+                for (int m = 0; m < nm; ++m) mvol[m] = cv[c->mk[m].cyl];
+            c->cyl_vol = cv;
+            if (int st = upload(c, &d.mvol, mvol)) return st;
+            if (int st = upload(c, &d.cylvol, cv)) return st;
+        }
         API_CUDA(c, c->alloc(&d.mcyl, nm));
         API_CUDA(c, cudaMemcpyAsync(d.mcyl, mc.data(), nm * sizeof(int), cudaMemcpyHostToDevice, c->s));
         {
@@ -551,6 +583,8 @@ int setup(f8_ctx *c) {
                         const float fx = (float)wx[3 * (size_t)m + (ii - i0v[m])];
                         const float fy = (float)wy[3 * (size_t)m + (jj - j0v[m])];
                         cw[e] = (double)(fx * fy);
+                        if (c->phys.ibm_volume == F8_IBM_ARC_VOLUME)   // spreading volume / dX^3
+                            cw[e] = (double)(fx * fy * (float)(c->cyl_vol[mc[m]] / (g.dx * g.dx * g.dx)));
                     }
                 }
                 if (int st = upload_f(c, &d.csr_w[comp], cw)) return st;
@@ -625,6 +659,8 @@ void f8_default_phys(f8_phys *ph) {
     ph->newton_dc = 1.0e-5; ph->newton_eps = 1.0e-6; ph->newton_itrmax = 10000;
     ph->sor_omega = 1.8; ph->sor_eps = 1.0e-5; ph->sor_itrmax = 10000;
     ph->ab2_start = 1;
+    ph->ibm_volume = F8_IBM_CELL_VOLUME;
+    ph->ibm_repeats = 1;
 }
 
 int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *cy, int ncyl, int prec, int poisson) {
@@ -1282,7 +1318,7 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
             double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
-    if (c->grid.dim != 3 || c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
+    if (c->grid.dim != 3 || c->poisson != F8_POISSON_FFT || c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
     if (c->precision == F8_MIXED) return grad_mixed(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
     Dev &d = c->d;
     const int ncyl = (int)c->cyl.size();

@@ -37,6 +37,10 @@ struct Dev {
     int *csr_off[3], *csr_idx[3];          // per component over (SX*SY) columns
     int *mperm, *moff;                     // markers grouped by cylinder (drag reduction)
     double *dragpart;                      // ncyl * nz * 3 partial sums
+    double *mvol;                          // per marker: the volume its force is spread with
+    double *cylvol;                        // per cylinder: the marker volume of its drag
+    int ibm_repeats;                       // direct-forcing iterations per step (NS)
+    float *Qpre[3];                        // mixed, NS > 1: the right-hand sides before spreading
     // mixed-precision state and work (F8_MIXED): the state as df64 pairs
     // (hi, lo) of FP32 halo fields
     float *Uf, *Vf, *Wf, *Ul, *Vl, *Wl;    // velocity hi / lo

@@ -734,6 +734,8 @@ struct IbmArgs {
     const int *mcyl;
     int nm, ncomp, d3;
     double dvol, dxn;
+    const double *mvol;        // per marker: spreading volume (dX^3, or the ring's arc element)
+    int accumulate;            // forcing iteration > 1: Fc += (Uc - Ub)/dt (smac.f90:1345-1353)
     const double *Uf[3];
     double *Fc[3];
     const int *off[3], *idx[3];
@@ -801,7 +803,8 @@ __global__ void k_ibm_interp(IbmArgs a, Geo g) {
                 ub = ub + Uf[hix(g, i, j, k)] * del * a.dxn;
             }
     const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
-    a.Fc[comp][m + (size_t)a.nm * (n - 1)] = 0.0 + (uc - ub) / g.dt;
+    double *fc = &a.Fc[comp][m + (size_t)a.nm * (n - 1)];
+    *fc = (a.accumulate ? *fc : 0.0) + (uc - ub) / g.dt;
 }
 
 // pre-fold spreading sum of extended cell (ie, je, ke) (ftmp of ibm_Helmholtz)
@@ -817,7 +820,7 @@ __device__ inline double spread_at(const IbmArgs &a, const Geo &g, int comp, int
             const int m = a.idx[comp][q];
             const double del = ibm_delta(a, comp, m, n, ie - a.i0[comp][m], je - a.j0[comp][m], kc);
             double fcv = a.Fc[comp][m + (size_t)a.nm * (n - 1)];
-            acc = acc + fcv * del * a.dxn;
+            acc = acc + fcv * del * a.mvol[m];
         }
     }
     return acc;
@@ -883,7 +886,7 @@ __global__ void k_drag_part(const double *Fx, const double *Fy, const double *Fz
         for (int c = 0; c < 3; ++c) part[((size_t)l * nz + n) * 3 + c] = sh[c][0];
 }
 
-__global__ void k_drag_final(const double *part, int nz, int ncomp, double dv, double *out) {
+__global__ void k_drag_final(const double *part, int nz, int ncomp, const double *cylvol, double *out) {
     const int l = blockIdx.x;
     __shared__ double sh[3][256];
     double s[3] = {0.0, 0.0, 0.0};
@@ -897,7 +900,7 @@ __global__ void k_drag_final(const double *part, int nz, int ncomp, double dv, d
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        for (int c = 0; c < 3; ++c) out[3 * l + c] = c < ncomp ? -sh[c][0] * dv : 0.0;
+        for (int c = 0; c < 3; ++c) out[3 * l + c] = c < ncomp ? -sh[c][0] * cylvol[l] : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1238,7 +1241,7 @@ cudaError_t launch_drag(Dev &d, double *out, cudaStream_t s) {
     const Geo &g = d.g;
     const bool d3 = g.dim == 3;
     k_drag_part<<<dim3(d.ncyl, g.nz), 256, 0, s>>>(d.Fc[0], d.Fc[1], d.Fc[2], d.mperm, d.moff, d.nm, d3 ? 3 : 2, d.dragpart); count_launch();
-    k_drag_final<<<d.ncyl, 256, 0, s>>>(d.dragpart, g.nz, d3 ? 3 : 2, d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy, out); count_launch();
+    k_drag_final<<<d.ncyl, 256, 0, s>>>(d.dragpart, g.nz, d3 ? 3 : 2, d.cylvol, out); count_launch();
     return cudaGetLastError();
 }
 
@@ -1299,17 +1302,22 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
         if ((e = cudaGetLastError())) return e;
     }
     mark(3);
-    // 3. IBM direct forcing
+    // 3. IBM direct forcing and 4. Helmholtz (CN viscous) solves; with NS > 1
+    // forcing iterations (smac.f90:1607-1611) each further iteration
+    // interpolates from the last Helmholtz solution, adds to the marker
+    // forces, spreads them and solves again
+    double *outs[3] = {d.Up, d.Vp, d.Wp};
+    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+    IbmArgs ia{};
     if (o.ibm) {
         if ((e = bc(d.Ua, g, BC_U, s))) return e;
         if ((e = bc(d.Va, g, BC_V, s))) return e;
         if (d3 && (e = bc(d.Wa, g, BC_W, s))) return e;
-        IbmArgs ia{};
         ia.mx = d.mx; ia.my = d.my; ia.mu = d.mu; ia.mv = d.mv; ia.mcyl = d.mcyl;
         ia.nm = d.nm; ia.ncomp = d3 ? 3 : 2; ia.d3 = d3;
         ia.dvol = d3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy;
         ia.dxn = d3 ? g.dx * g.dx * g.dx : g.dx * g.dx;
-        ia.Uf[0] = d.Ua; ia.Uf[1] = d.Va; ia.Uf[2] = d.Wa;
+        ia.mvol = d.mvol;
         for (int c = 0; c < 3; ++c) {
             ia.Fc[c] = d.Fc[c]; ia.off[c] = d.csr_off[c]; ia.idx[c] = d.csr_idx[c];
             ia.Q[c] = d.Q[c]; ia.B[c] = (c == 0 ? d.Bx : c == 1 ? d.By : d.Bz);
@@ -1319,25 +1327,31 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
             ia.wx[c] = d.mwxd[c]; ia.wy[c] = d.mwyd[c]; ia.wz[c] = d.mwzd[c];
             ia.i0[c] = d.mi0d[c]; ia.j0[c] = d.mj0d[c];
         }
-        dim3 gi((d.nm + 127) / 128, g.nz, ia.ncomp);
-        k_ibm_interp<<<gi, 128, 0, s>>>(ia, g); count_launch();
-        dim3 blk(32, 8);
-        k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g); count_launch();
-        if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
-        if ((e = cudaGetLastError())) return e;
     }
-    mark(4);
-    // 4. Helmholtz (CN viscous) solves
-    double *outs[3] = {d.Up, d.Vp, d.Wp};
-    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
-    for (int c = 0; c < (d3 ? 3 : 2); ++c) {
-        if (!g.walls) e = fft_solve_periodic(d, d.Q[c], outs[c], 1.0, lhs1, s);
-        else e = wall_solve(d, d.Q[c], outs[c], c == 1 ? SYS_V : SYS_U, c == 0 ? g.uwall : 0.0, s);
-        if (e) return e;
+    const int repeats = o.ibm ? std::max(1, d.ibm_repeats) : 1;
+    for (int r = 0; r < repeats; ++r) {
+        if (o.ibm) {
+            // the first iteration interpolates Ua (Up = Ua, ibm_preliminary)
+            const double *src[3] = {d.Ua, d.Va, d.Wa}, *srcp[3] = {d.Up, d.Vp, d.Wp};
+            for (int c = 0; c < 3; ++c) ia.Uf[c] = r == 0 ? src[c] : srcp[c];
+            ia.accumulate = r > 0;
+            dim3 gi((d.nm + 127) / 128, g.nz, ia.ncomp);
+            k_ibm_interp<<<gi, 128, 0, s>>>(ia, g); count_launch();
+            dim3 blk(32, 8);
+            k_ibm_spread_q<<<cell_grid(g, blk), blk, 0, s>>>(ia, g); count_launch();
+            if (r == repeats - 1 && drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
+            if ((e = cudaGetLastError())) return e;
+        }
+        if (r == 0) mark(4);
+        for (int c = 0; c < (d3 ? 3 : 2); ++c) {
+            if (!g.walls) e = fft_solve_periodic(d, d.Q[c], outs[c], 1.0, lhs1, s);
+            else e = wall_solve(d, d.Q[c], outs[c], c == 1 ? SYS_V : SYS_U, c == 0 ? g.uwall : 0.0, s);
+            if (e) return e;
+        }
+        if ((e = bc(d.Up, g, BC_U, s))) return e;
+        if ((e = bc(d.Vp, g, BC_V, s))) return e;
+        if (d3 && (e = bc(d.Wp, g, BC_W, s))) return e;
     }
-    if ((e = bc(d.Up, g, BC_U, s))) return e;
-    if ((e = bc(d.Vp, g, BC_V, s))) return e;
-    if (d3 && (e = bc(d.Wp, g, BC_W, s))) return e;
     mark(5);
     // 5. Poisson
     {

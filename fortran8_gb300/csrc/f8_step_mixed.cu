@@ -908,7 +908,36 @@ __device__ inline df ua_at(const Geo &g, const float *Uh, const float *Ul, const
     return (comp == 0 && j != 0) ? df_sub(uw2, inner) : df_neg(inner);
 }
 
+// U* = U^n + dU (the last Helmholtz solution) at the stencil points, with the
+// boundary values the FP64 step gives Up (the increments have no halo pass:
+// x and z wrap, the wall solves write the ghost rows of dU)
+__device__ inline df ustar_at(const Geo &g, const float *Uh, const float *Ul, const float *D, int comp, int i, int j,
+                              int k, df uw2) {
+    const int ii = wrapx(g, i), kk = wrapz(g, k);
+    auto us = [&](int jj) {
+        const int h = hix(g, i, jj, k);
+        return df_add_f(df{Uh[h], Ul[h]}, D[hix(g, ii, jj, kk)]);
+    };
+    if (j >= 1 && j <= g.ny) {
+        if (g.walls && comp == 1 && j == g.ny) return df{0.0f, 0.0f};
+        return us(j);
+    }
+    if (!g.walls) {
+        const int jw = wrapy(g, j), h = hix(g, i, j, k);
+        return df_add_f(df{Uh[h], Ul[h]}, D[hix(g, ii, jw, kk)]);
+    }
+    if (comp == 1) return df{0.0f, 0.0f};
+    const int jj = j == 0 ? 1 : g.ny;
+    const df inner = us(jj);
+    return (comp == 0 && j != 0) ? df_sub(uw2, inner) : df_neg(inner);
+}
+
 struct IbmArgsF {
+    const float *D[3];               // forcing iteration > 1: the increments dU of the last solve
+    int mode;                        // 0: interpolate Ua = U + Q; 1: interpolate U* = U + dU
+    int accumulate;                  // forcing iteration > 1: Fc += (Uc - Ub)/dt
+    const float *Qb[3];              // base of the spread: Q itself (first iteration) or the
+                                     // right-hand sides saved before the first spread
     const double *mu, *mv;
     const int *mcyl;
     int nm;
@@ -948,7 +977,9 @@ __global__ void __launch_bounds__(96) k_ibm_interp_f(IbmArgsF a, Geo g) {
 #pragma unroll
             for (int di = 0; di < 3; ++di) {
                 const float w = wx[di] * wy[dj] * wz;
-                ub = df_add(ub, df_mul_f(ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2), w));
+                const df uv = a.mode ? ustar_at(g, a.Uh[comp], a.Ul[comp], a.D[comp], comp, i0 + di, j0 + dj, k, a.uw2)
+                                     : ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2);
+                ub = df_add(ub, df_mul_f(uv, w));
             }
     }
     part[dk][threadIdx.x] = ub;
@@ -956,7 +987,8 @@ __global__ void __launch_bounds__(96) k_ibm_interp_f(IbmArgsF a, Geo g) {
     if (dk == 0 && m < a.nm) {
         const df s3 = df_add(df_add(part[0][threadIdx.x], part[1][threadIdx.x]), part[2][threadIdx.x]);
         const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
-        a.Fc[comp][m + (size_t)a.nm * (n - 1)] = (uc - ((double)s3.hi + (double)s3.lo)) * a.idt;
+        double *fc = &a.Fc[comp][m + (size_t)a.nm * (n - 1)];
+        *fc = (a.accumulate ? *fc : 0.0) + (uc - ((double)s3.hi + (double)s3.lo)) * a.idt;
     }
 }
 
@@ -1006,7 +1038,7 @@ __global__ void k_ibm_spread_f(IbmArgsF a, Geo g) {
         }
     }
     const int o = qix(g, i, j, k);
-    a.Q[comp][o] = fmaf(a.dtf, f, a.Q[comp][o]);
+    a.Q[comp][o] = fmaf(a.dtf, f, a.Qb[comp][o]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1821,76 +1853,93 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
                                       tp->Ua[1], tp->Ua[2], g, df_from_d(2.0 * g.uwall)); count_launch();
     }
     mark(3);
-    if (o.ibm) {
-        IbmArgsF a{};
-        a.mu = d.mu; a.mv = d.mv; a.mcyl = d.mcyl; a.nm = d.nm;
-        const float *Uh[3] = {d.Uf, d.Vf, d.Wf}, *Ul[3] = {d.Ul, d.Vl, d.Wl};
-        // z weights of the stencil offset k - n = -1, 0, 1 (marker plane at
-        // (n - 1/4) dZ; u, v at (k - 1/2) dZ, w at k dZ)
-        auto roma = [](double r) {
-            double ar = std::fabs(r);
-            if (ar < 1.5 && ar >= 0.5) return (5.0 - 3.0 * ar - std::sqrt(-3.0 * ((1 - ar) * (1 - ar)) + 1.0)) / 6.0;
-            if (ar < 0.5) return (1.0 + std::sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
-            return 0.0;
-        };
+    // IBM direct forcing and the Helmholtz solves; with NS > 1 forcing
+    // iterations (smac.f90:1607-1611) each further iteration interpolates
+    // U* = U^n + dU of the last solve, adds to the marker forces, spreads them
+    // onto the right-hand sides saved before the first spread and solves again
+    const int repeats = o.ibm ? std::max(1, d.ibm_repeats) : 1;
+    for (int r = 0; r < repeats; ++r) {
+        if (o.ibm) {
+            IbmArgsF a{};
+            a.mu = d.mu; a.mv = d.mv; a.mcyl = d.mcyl; a.nm = d.nm;
+            const float *Uh[3] = {d.Uf, d.Vf, d.Wf}, *Ul[3] = {d.Ul, d.Vl, d.Wl};
+            // z weights of the stencil offset k - n = -1, 0, 1 (marker plane at
+            // (n - 1/4) dZ; u, v at (k - 1/2) dZ, w at k dZ)
+            auto roma = [](double r) {
+                double ar = std::fabs(r);
+                if (ar < 1.5 && ar >= 0.5) return (5.0 - 3.0 * ar - std::sqrt(-3.0 * ((1 - ar) * (1 - ar)) + 1.0)) / 6.0;
+                if (ar < 0.5) return (1.0 + std::sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
+                return 0.0;
+            };
+            for (int c = 0; c < 3; ++c) {
+                a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
+                a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
+                a.idx[c] = d.csr_idx[c]; a.cw[c] = d.csr_w[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
+                for (int dk = 0; dk < 3; ++dk) {
+                    double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
+                    a.wz[c][dk] = (float)roma(zg);
+                }
+            }
+            a.uw2 = df_from_d(2.0 * g.uwall);
+            a.idt = 1.0 / g.dt;
+            a.dtf = (float)g.dt;
+            const bool last = r == repeats - 1;
+            a.mode = r > 0 ? 1 : 0;
+            a.accumulate = r > 0 ? 1 : 0;
+            for (int c = 0; c < 3; ++c) {
+                a.D[c] = d.dUf[c];
+                a.Qb[c] = (r > 0 && d.Qpre[c]) ? d.Qpre[c] : d.Qf[c];
+            }
+            if (r == 0 && repeats > 1)
+                for (int c = 0; c < 3; ++c)
+                    F8_CUDA_RET(cudaMemcpyAsync(d.Qpre[c], d.Qf[c], (size_t)d.ni * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            dim3 gi((d.nm + 31) / 32, g.nz, 3);
+            k_ibm_interp_f<<<gi, dim3(32, 3), 0, s>>>(a, g); count_launch();
+            int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
+            if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
+            if (last && drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
+            if ((e = cudaGetLastError())) return e;
+            if (tp && last)
+                for (int c = 0; c < 3; ++c)
+                    F8_CUDA_RET(cudaMemcpyAsync(tp->Fc[c], d.Fc[c], (size_t)d.nm * g.nz * sizeof(double),
+                                                cudaMemcpyDeviceToDevice, s));
+        }
+        if (r == 0) mark(4);
+        // Helmholtz solves for the FP32 increments dU (U* = U^n + dU).  On the
+        // fused spectral path the three solves are independent branches: V and W
+        // run on side streams with their own spectra, forked from and joined to
+        // the step's stream (parallel branches of the captured graph), so their
+        // x transforms fill the SMs that one solve's kernels leave idle.
+        const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+        const bool branches = d.fused_planes && d.aux[0] && d.aux[1];
+        if (branches) {
+            F8_CUDA_RET(cudaEventRecord(d.ev_fork, s));
+            for (int b = 0; b < 2; ++b) F8_CUDA_RET(cudaStreamWaitEvent(d.aux[b], d.ev_fork, 0));
+        }
         for (int c = 0; c < 3; ++c) {
-            a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
-            a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
-            a.idx[c] = d.csr_idx[c]; a.cw[c] = d.csr_w[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
-            for (int dk = 0; dk < 3; ++dk) {
-                double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
-                a.wz[c][dk] = (float)roma(zg);
+            const XOutF out{d.dUf[c], nullptr, 0};
+            if (branches) {
+                cudaStream_t sc = c == 0 ? s : d.aux[c - 1];
+                float *spec = c == 0 ? d.Hf : d.HfB[c - 1];
+                if (!g.walls) e = solve_periodic_fused<float>(d, d.Qf[c], out, 1.0f, (float)lhs1, sc, spec);
+                else e = solve_walls_fused<float>(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, sc, spec);
+            } else if (!g.walls) {
+                e = solve_periodic_f(d, d.Qf[c], out, 1.0, lhs1, s);
+            } else {
+                e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
+            }
+            if (e) return e;
+        }
+        if (branches) {
+            for (int b = 0; b < 2; ++b) {
+                F8_CUDA_RET(cudaEventRecord(d.ev_join[b], d.aux[b]));
+                F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_join[b], 0));
             }
         }
-        a.uw2 = df_from_d(2.0 * g.uwall);
-        a.idt = 1.0 / g.dt;
-        a.dtf = (float)g.dt;
-        dim3 gi((d.nm + 31) / 32, g.nz, 3);
-        k_ibm_interp_f<<<gi, dim3(32, 3), 0, s>>>(a, g); count_launch();
-        int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
-        if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
-        if (drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
-        if ((e = cudaGetLastError())) return e;
-        if (tp)
-            for (int c = 0; c < 3; ++c)
-                F8_CUDA_RET(cudaMemcpyAsync(tp->Fc[c], d.Fc[c], (size_t)d.nm * g.nz * sizeof(double),
-                                            cudaMemcpyDeviceToDevice, s));
-    }
-    mark(4);
-    // Helmholtz solves for the FP32 increments dU (U* = U^n + dU).  On the
-    // fused spectral path the three solves are independent branches: V and W
-    // run on side streams with their own spectra, forked from and joined to
-    // the step's stream (parallel branches of the captured graph), so their
-    // x transforms fill the SMs that one solve's kernels leave idle.
-    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
-    const bool branches = d.fused_planes && d.aux[0] && d.aux[1];
-    if (branches) {
-        F8_CUDA_RET(cudaEventRecord(d.ev_fork, s));
-        for (int b = 0; b < 2; ++b) F8_CUDA_RET(cudaStreamWaitEvent(d.aux[b], d.ev_fork, 0));
-    }
-    for (int c = 0; c < 3; ++c) {
-        const XOutF out{d.dUf[c], nullptr, 0};
-        if (branches) {
-            cudaStream_t sc = c == 0 ? s : d.aux[c - 1];
-            float *spec = c == 0 ? d.Hf : d.HfB[c - 1];
-            if (!g.walls) e = solve_periodic_fused<float>(d, d.Qf[c], out, 1.0f, (float)lhs1, sc, spec);
-            else e = solve_walls_fused<float>(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, sc, spec);
-        } else if (!g.walls) {
-            e = solve_periodic_f(d, d.Qf[c], out, 1.0, lhs1, s);
-        } else {
-            e = solve_walls_f(d, d.Qf[c], out, c == 1 ? SYS_V : SYS_U, s);
+        if (tp) {
+            const float *uh[3] = {d.Uf, d.Vf, d.Wf};
+            for (int c = 0; c < 3; ++c) { k_tape_up<<<tnb, 256, 0, s>>>(uh[c], d.dUf[c], tp->Up[c], g); count_launch(); }
         }
-        if (e) return e;
-    }
-    if (branches) {
-        for (int b = 0; b < 2; ++b) {
-            F8_CUDA_RET(cudaEventRecord(d.ev_join[b], d.aux[b]));
-            F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_join[b], 0));
-        }
-    }
-    if (tp) {
-        const float *uh[3] = {d.Uf, d.Vf, d.Wf};
-        for (int c = 0; c < 3; ++c) { k_tape_up<<<tnb, 256, 0, s>>>(uh[c], d.dUf[c], tp->Up[c], g); count_launch(); }
     }
     mark(5);
     // Poisson: FP32 solve + one df64 defect correction.  The increments and

@@ -73,11 +73,13 @@ class PhysSpec:
     sor_eps: float = 1.0e-5
     sor_itrmax: int = 10000
     ab2_start: int = 1
+    ibm_volume: int = abi.F8_IBM_CELL_VOLUME
+    ibm_repeats: int = 1
 
     def to_c(self) -> abi.Phys:
         return abi.Phys(self.re, self.wi, self.beta, self.lp2, self.dt, self.newton_dc,
                         self.newton_eps, self.newton_itrmax, self.sor_omega, self.sor_eps,
-                        self.sor_itrmax, self.ab2_start)
+                        self.sor_itrmax, self.ab2_start, self.ibm_volume, self.ibm_repeats)
 
 
 @dataclass

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define F8_ABI_VERSION 1
+#define F8_ABI_VERSION 2
 
 /* Status codes.  F8_WARN_* are non-fatal: the step completed. */
 enum f8_status {
@@ -94,7 +94,19 @@ typedef struct f8_phys {
     int sor_itrmax;         /* fenep.f90:857                                           */
     int ab2_start;          /* 1: the first step copies A->A0, T->T0 (input_type == 0,
                                fenep.f90:1445-1452)                                    */
+    int ibm_volume;         /* volume a marker force is spread with: F8_IBM_CELL_VOLUME
+                               (dX*dY*dZ, fenep.f90 / fenep_mpi.f90:1870-1898) or
+                               F8_IBM_ARC_VOLUME (pi*DC/NL * dX*dX of the cylinder's
+                               ring, smac.f90:1129, 1428-1446; 3D, surface rings)       */
+    int ibm_repeats;        /* direct-forcing iterations per step, NS of smac.f90:20,
+                               1607-1611 (interpolate from the last Helmholtz solution,
+                               add to the marker force, spread, solve again); 1 = fenep */
 } f8_phys;
+
+enum f8_ibm_volume {
+    F8_IBM_CELL_VOLUME = 0,
+    F8_IBM_ARC_VOLUME = 1
+};
 
 typedef struct f8_cyl {
     double xc, yc;  /* centre in the x-y plane; the cylinder spans z            */
@@ -164,8 +176,10 @@ int f8_load(f8_ctx *ctx, const f8_fields *in, int step0);
 
 /* Advance nsteps time steps.  drag may be NULL; otherwise it receives
  * nsteps * ncyl * 3 doubles: for each step and cylinder the force of the
- * fluid on the body, -sum_markers(Fc) * dV (x, y, z), dV = dX*dY*dZ (3D) or
- * dX*dY (2D).  Returns the worst status of the steps.
+ * fluid on the body, -sum_markers(Fc) * dV (x, y, z), dV the spreading volume
+ * of a marker (dX*dY*dZ in 3D, dX*dY in 2D, or the ring's arc element with
+ * F8_IBM_ARC_VOLUME), from the marker force after the last forcing iteration.
+ * Returns the worst status of the steps.
  * Replaces: the body of the step loop (fenep.f90:2477-2527). */
 int f8_step(f8_ctx *ctx, int nsteps, double *drag);
 
@@ -195,9 +209,10 @@ int f8_store(f8_ctx *ctx, f8_fields *out);
  * segment with its intermediate fields stored, then runs the adjoint of its
  * steps.  The selection of the SPD face candidates is held fixed (its
  * derivative is zero almost everywhere); the Newton solution is
- * differentiated through the implicit-function theorem.  Requires an F8_FP64
- * 3D context with the FFT Poisson solver (F8_ERR_UNSUPPORTED otherwise).  The
- * context's state advances by nsteps as with f8_step. */
+ * differentiated through the implicit-function theorem.  Requires a 3D
+ * context (F8_FP64 or F8_MIXED) with the FFT Poisson solver and one forcing
+ * iteration per step (F8_ERR_UNSUPPORTED otherwise).  The context's state
+ * advances by nsteps as with f8_step. */
 int f8_grad(f8_ctx *ctx, int nsteps, int checkpoint_every, const double *drag_weights,
             const f8_fields *seed, double *J, double *dJ_dparams, f8_fields *dJ_dstate, double *drag);
 

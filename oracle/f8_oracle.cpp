@@ -1108,9 +1108,20 @@ inline void grid_pos(int comp, int i, int j, int k, double dX, double dY, double
     else z = z + 0.5 * dZ;
 }
 
-// ibm_Helmholtz of fenep_mpi.f90:1794-1929 (3D, no debug override) and
-// fenep_2d.f90:1726-1819 (2D).  Up/Vp/Wp = Ua.. (halo); writes fint and Fc.
-void ibm_force(OCtx &c) {
+// Spreading (and drag) volume of a marker of cylinder l: dX**3 (fenep.f90:
+// 2166-2187; the drag uses dX*dY*dZ) or, with F8_IBM_ARC_VOLUME, the arc
+// element dV = PI*DC/NL * dX * dX of the cylinder's ring (smac.f90:1128-1129).
+double arc_volume(const OCtx &c, int l) {
+    const double DC = 2.0 * c.cyl[l].r;
+    const int NL = std::max(1, (int)std::lround(PI * DC / c.dX));
+    return PI * DC / NL * c.dX * c.dX;
+}
+
+// ibm_Helmholtz of fenep_mpi.f90:1794-1929 (3D, no debug override),
+// fenep_2d.f90:1726-1819 (2D) and smac.f90:1303-1488 (the arc-element
+// spreading volume).  Interpolates Up/Vp/Wp (halo); writes fint and Fc; with
+// accumulate (a further forcing iteration, smac.f90:1345-1353) adds to Fc.
+void ibm_force(OCtx &c, bool accumulate) {
     const int NX = c.NX, NY = c.NY, NZ = c.NZ;
     const double dX = c.dX, dY = c.dY, dZ = c.dZ, dt = c.ph.dt;
     const bool d3 = c.dim == 3;
@@ -1142,10 +1153,14 @@ void ibm_force(OCtx &c) {
                         }
                 double uc = comp == 0 ? mk.u : (comp == 1 ? mk.v : 0.0);
                 size_t o = m + nm * (size_t)(n - 1);
-                Fc[o] = 0.0 + (uc - ub) / dt;  // Fc reset in ibm_preliminary, then += (fenep.f90:2028, 2114)
+                // Fc reset in ibm_preliminary, then += (fenep.f90:2028, 2114)
+                Fc[o] = (accumulate ? Fc[o] : 0.0) + (uc - ub) / dt;
             }
     }
     // spreading into a halo-extended temporary, then periodic fold (ibm_PBM)
+    std::vector<double> mvol(c.cyl.size(), dxn);
+    if (c.ph.ibm_volume == F8_IBM_ARC_VOLUME)
+        for (size_t l = 0; l < c.cyl.size(); ++l) mvol[l] = arc_volume(c, (int)l);
     std::vector<double> ftmp(c.nh());
     for (int comp = 0; comp < ncomp; ++comp) {
         std::fill(ftmp.begin(), ftmp.end(), 0.0);
@@ -1165,7 +1180,7 @@ void ibm_force(OCtx &c) {
                             grid_pos(comp, i, j, k, dX, dY, dZ, x, y, z);
                             double del = d3 ? roma((x - mk.x) / dX) * roma((y - mk.y) / dY) * roma((z - zc) / dZ) / dvol
                                             : roma((x - mk.x) / dX) * roma((y - mk.y) / dY) / dvol;
-                            ftmp[c.hidx(i, j, k)] = ftmp[c.hidx(i, j, k)] + fcv * del * dxn;
+                            ftmp[c.hidx(i, j, k)] = ftmp[c.hidx(i, j, k)] + fcv * del * mvol[mk.cyl];
                         }
             }
         // fold (fenep.f90:2195-2205); y is folded only when periodic
@@ -1400,22 +1415,28 @@ int do_step(OCtx &c, double *drag) {
         if (d3) interior_copy(c, c.Wa.data(), Qz);
     } else {
         // Up = Ua with boundary values (ibm_preliminary), force, then
-        // Q = Ua + dt*f - dt*B/2 (ibm_predict, fenep.f90:2229)
+        // Q = Ua + dt*f - dt*B/2 (ibm_predict, fenep.f90:2229); with NS > 1
+        // (smac.f90:1607-1611) further iterations interpolate the last
+        // Helmholtz solution, add to Fc, spread and solve again
         bc_scalar(c, c.Ua.data(), BC_U);
         bc_scalar(c, c.Va.data(), BC_V);
         if (d3) bc_scalar(c, c.Wa.data(), BC_W);
         c.Up = c.Ua; c.Vp = c.Va; c.Wp = c.Wa;
-        ibm_force(c);
         const std::vector<double> *B[3] = {&c.Bx, &c.By, &c.Bz};
         const std::vector<double> *Ua[3] = {&c.Ua, &c.Va, &c.Wa};
-        for (int comp = 0; comp < (d3 ? 3 : 2); ++comp) {
-            Qs[comp]->resize(c.ni());
-            for (int k = 1; k <= c.NZ; ++k)
-                for (int j = 1; j <= c.NY; ++j)
-                    for (int i = 1; i <= c.NX; ++i) {
-                        size_t o = c.iidx(i, j, k);
-                        (*Qs[comp])[o] = (*Ua[comp])[c.hidx(i, j, k)] + dt * c.fint[comp][o] - dt * (*B[comp])[o] / 2;
-                    }
+        const int repeats = std::max(1, c.ph.ibm_repeats);
+        for (int r = 0; r < repeats; ++r) {
+            ibm_force(c, r > 0);
+            for (int comp = 0; comp < (d3 ? 3 : 2); ++comp) {
+                Qs[comp]->resize(c.ni());
+                for (int k = 1; k <= c.NZ; ++k)
+                    for (int j = 1; j <= c.NY; ++j)
+                        for (int i = 1; i <= c.NX; ++i) {
+                            size_t o = c.iidx(i, j, k);
+                            (*Qs[comp])[o] = (*Ua[comp])[c.hidx(i, j, k)] + dt * c.fint[comp][o] - dt * (*B[comp])[o] / 2;
+                        }
+            }
+            if (r < repeats - 1) helmholtz(c, Qs);
         }
         if (drag) {
             const size_t nm = c.mk.size();
@@ -1426,7 +1447,8 @@ int do_step(OCtx &c, double *drag) {
                 std::vector<double> s(ncyl, 0.0);
                 for (int n = 0; n < c.NZ; ++n)
                     for (size_t m = 0; m < nm; ++m) s[c.mk[m].cyl] = s[c.mk[m].cyl] + c.Fc[comp][m + nm * n];
-                for (int l = 0; l < ncyl; ++l) drag[3 * l + comp] = -s[l] * dv;
+                for (int l = 0; l < ncyl; ++l)
+                    drag[3 * l + comp] = -s[l] * (c.ph.ibm_volume == F8_IBM_ARC_VOLUME ? arc_volume(c, l) : dv);
             }
         }
     }
@@ -1479,6 +1501,14 @@ int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, in
     if (!(ph->dt > 0) || !(ph->re > 0) || !(ph->wi > 0)) return F8_ERR_ARG;
     if (ph->newton_itrmax < 1 || ph->sor_itrmax < 1) return F8_ERR_ARG;
     if (ncyl < 0 || (ncyl > 0 && !cy)) return F8_ERR_ARG;
+    if (ph->ibm_repeats < 1 || ph->ibm_repeats > 64) return F8_ERR_ARG;
+    if (ph->ibm_volume != F8_IBM_CELL_VOLUME && ph->ibm_volume != F8_IBM_ARC_VOLUME) return F8_ERR_ARG;
+    if (ph->ibm_volume == F8_IBM_ARC_VOLUME) {
+        // the arc element of a surface ring (smac.f90:1128-1129), 3D
+        if (g->dim != 3) return F8_ERR_UNSUPPORTED;
+        for (int l = 0; l < ncyl; ++l)
+            if (cy[l].filled) return F8_ERR_UNSUPPORTED;
+    }
     return F8_OK;
 }
 
@@ -1527,6 +1557,8 @@ void f8o_default_phys(f8_phys *ph) {
     ph->newton_dc = 1.0e-5; ph->newton_eps = 1.0e-6; ph->newton_itrmax = 10000;
     ph->sor_omega = 1.8; ph->sor_eps = 1.0e-5; ph->sor_itrmax = 10000;
     ph->ab2_start = 1;
+    ph->ibm_volume = F8_IBM_CELL_VOLUME;
+    ph->ibm_repeats = 1;
 }
 
 int f8o_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *cy, int ncyl, int prec, int poisson) {

@@ -508,8 +508,10 @@ def marker_geometry(cyls, dX):
     return out
 
 
-def ibm(Uas, centres, geom, g: TGrid, dt):
-    """Marker forces Fc[comp] (NZ, nm) and the folded spread forces (interior)."""
+def ibm(Uas, centres, geom, g: TGrid, dt, cylvol=None):
+    """Marker forces Fc[comp] (NZ, nm) and the folded spread forces (interior).
+    Markers spread over dX^3 (fenep_mpi.f90:1794-1929), or over their
+    cylinder's cylvol[l] when given."""
     dX, dY, dZ = g.dx, g.dy, g.dz
     NX, NY, NZ = g.nx, g.ny, g.nz
     SX, SY, SZ = NX + 2, NY + 2, NZ + 2
@@ -521,6 +523,8 @@ def ibm(Uas, centres, geom, g: TGrid, dt):
     mv = torch.tensor([m[4] for m in geom], dtype=F64)
     dvol = (dX * dY) * dZ
     dxn = dX * dX * dX
+    mvol = (torch.full((nm,), dxn, dtype=F64) if cylvol is None
+            else torch.tensor([cylvol[m[0]] for m in geom], dtype=F64))
     n = torch.arange(1, NZ + 1, dtype=F64)
     zc = (n - 0.25) * dZ                                   # (NZ,)
     Fcs, fints = [], []
@@ -553,7 +557,8 @@ def ibm(Uas, centres, geom, g: TGrid, dt):
         Fc = 0.0 + (uc[None, :] - ub) / dt
         Fcs.append(Fc)
         ftmp = torch.zeros(SZ * SY * SX, dtype=F64).index_add(
-            0, flat.reshape(-1), (Fc[:, :, None, None, None] * dlt * dxn).reshape(-1)).reshape(SZ, SY, SX)
+            0, flat.reshape(-1), (Fc[:, :, None, None, None] * dlt * mvol[None, :, None, None, None]).reshape(-1)
+        ).reshape(SZ, SY, SX)
         # periodic fold (fenep.f90:2195-2205); y only when periodic
         ftmp = torch.cat([ftmp[:, :, 0:1], ftmp[:, :, 1:2] + ftmp[:, :, NX + 1:NX + 2], ftmp[:, :, 2:NX],
                           ftmp[:, :, NX:NX + 1] + ftmp[:, :, 0:1], ftmp[:, :, NX + 1:]], dim=2)
@@ -576,6 +581,25 @@ class TPhys:
     newton_dc: float = 1.0e-5
     newton_eps: float = 1.0e-6
     newton_itrmax: int = 10000
+    cylvol: tuple | None = None    # per-cylinder spreading volume; None: the cell volume
+
+
+def arc_volumes(cyls, dX):
+    """Spreading volume of each cylinder's markers under the arc element of
+    smac.f90 (smac.f90:1128-1129, 1428-1446): dV = pi*DC/NL * dX * dX."""
+    out = []
+    for cy in cyls:
+        DC = 2.0 * cy.r
+        NL = max(int(round(PI * DC / dX)), 1)
+        out.append(PI * DC / NL * dX * dX)
+    return tuple(out)
+
+
+def tphys(phys_spec, cyls, dX):
+    """TPhys of a PhysSpec, with the arc-element volumes when it selects them."""
+    arc = getattr(phys_spec, "ibm_volume", 0) == 1
+    return TPhys(phys_spec.re, phys_spec.dt, phys_spec.newton_dc, phys_spec.newton_eps, phys_spec.newton_itrmax,
+                 arc_volumes(cyls, dX) if arc else None)
 
 
 def step(st: dict, prm: dict, g: TGrid, ph: TPhys, geom, first: bool):
@@ -612,9 +636,10 @@ def step(st: dict, prm: dict, g: TGrid, ph: TPhys, geom, first: bool):
         val = (sh(Us[c], g) + gp + dt * (3.0 * A[c] - A0[c]) / 2.0 + dt * B[c]
                + dt * (T[c] + T0[c]) / 2.0 + dt * st["F"][c])
         Ua.append(bc(embed(val, g), kinds[c], g))
-    Fc, fint, cyl = ibm(Ua, prm["centres"], geom, g, dt)
-    dv = (g.dx * g.dy) * g.dz
+    Fc, fint, cyl = ibm(Ua, prm["centres"], geom, g, dt, ph.cylvol)
     ncyl = prm["centres"].shape[0]
+    dv = (torch.full((ncyl,), (g.dx * g.dy) * g.dz, dtype=F64) if ph.cylvol is None
+          else torch.tensor(ph.cylvol, dtype=F64))
     drag = torch.stack([-torch.zeros(ncyl, dtype=F64).index_add(0, cyl, Fc[c].sum(0)) * dv for c in range(3)], 1)
     Q = [sh(Ua[c], g) + dt * fint[c] - dt * B[c] / 2 for c in range(3)]
     kap = dt * beta / re / 2.0
@@ -667,7 +692,9 @@ def run(arrs: dict, grid_spec, phys_spec, cyls, params: dict, nsteps: int, weigh
     require grad.  J = sum(weights * drag); by default the time-averaged total
     x-drag, J = (1/nsteps) sum_n sum_l drag[n, l, 0]."""
     g = TGrid.from_spec(grid_spec)
-    ph = TPhys(phys_spec.re, phys_spec.dt, phys_spec.newton_dc, phys_spec.newton_eps, phys_spec.newton_itrmax)
+    if getattr(phys_spec, "ibm_repeats", 1) != 1:
+        raise ValueError("the torch step has one direct-forcing iteration")
+    ph = tphys(phys_spec, cyls, g.dx)
     geom = marker_geometry(cyls, g.dx)
     st = state_from_numpy(arrs, g)
     drags = []

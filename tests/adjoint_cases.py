@@ -26,18 +26,22 @@ if str(ROOT / "oracle") not in sys.path:
 def case(name: str, oracle_fns, spinup: int = 10):
     """(workload, state, step0) of a gradient case: 'channel' (32x16x16, y walls,
     two filled cylinders), 'periodic' (16^3, one cylinder), 'moving' (the channel
-    with surface-ring cylinders spinning and the upper wall moving) or
+    with surface-ring cylinders spinning and the upper wall moving), 'arc' (the
+    moving case with markers spread over the arc element of their ring) or
     'newtonian' (the channel with beta = 1: no polymer stage)."""
-    if name in ("channel", "moving", "newtonian"):
+    if name in ("channel", "moving", "newtonian", "arc"):
         w = configs.scaled(configs.c4_adjoint(), 32, 16, 16)
     else:
         w = configs.scaled(configs.c2_3d(), 16, 16, 16)
     cyls = tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls)
-    if name == "moving":
+    if name in ("moving", "arc"):
         cyls = tuple(replace(c, filled=0, spin=0.4 * (1 - 2 * l)) for l, c in enumerate(cyls))
         w = replace(w, grid=replace(w.grid, uwall=0.3))
     if name == "newtonian":
         w = replace(w, phys=replace(w.phys, beta=1.0))
+    if name == "arc":
+        from fortran8_gb300 import abi
+        w = replace(w, phys=replace(w.phys, ibm_volume=abi.F8_IBM_ARC_VOLUME))
     w = replace(w, cyls=cyls)
     st = configs.initial_state(w)
     g = w.grid
@@ -105,7 +109,7 @@ def torch_grad(w, st, step0, nsteps, weights=None, seed=None):
     st_t["A0"] = [leaves[n] for n in ("ax0", "ay0", "az0")]
     st_t["T0"] = [leaves[n] for n in ("tx0", "ty0", "tz0")]
     st_t["F"] = [t(arrs[n]) for n in ("fx", "fy", "fz")]
-    ph = ft.TPhys(w.phys.re, w.phys.dt, w.phys.newton_dc, w.phys.newton_eps, w.phys.newton_itrmax)
+    ph = ft.tphys(w.phys, w.cyls, g.dx)
     geom = ft.marker_geometry(w.cyls, g.dx)
     drags = []
     cur = st_t

@@ -42,7 +42,7 @@ def close(a, b, rel):
     return np.all(np.abs(a - b) <= rel * np.abs(b) + 1e-3 * rel * scale)
 
 
-@pytest.mark.parametrize("name,spinup", [("channel", 10), ("channel", 0), ("periodic", 10), ("moving", 10),
+@pytest.mark.parametrize("name,spinup", [("channel", 10), ("channel", 0), ("periodic", 10), ("moving", 10), ("arc", 10),
                                          ("newtonian", 10)])
 def test_grad_matches_torch(gpu, oracle, name, spinup):
     w, st, step0 = case(name, oracle, spinup=spinup)
@@ -123,37 +123,6 @@ def test_grad_matches_gpu_central_differences(gpu, oracle):
             vals.append(drag[:, :, 0].sum() / n)
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(dp[q] - fd) <= 1e-4 * abs(fd) + 1e-8, (q, dp[q], fd)
-
-
-def _workload_fd(gpu, w, st, n, qs_rel):
-    """Central differences of the mean x drag over n steps from st, with the
-    relative step h_q = rel * |p_q| for each parameter index q in qs_rel."""
-    base = param_vector(w)
-    fds = {}
-    for q, rel in qs_rel.items():
-        h = rel * max(abs(base[q]), 1.0)
-        vals = []
-        for sgn in (1, -1):
-            b = base.copy()
-            b[q] += sgn * h
-            wq = with_params(w, b)
-            with Solver(gpu, wq.grid, wq.phys, wq.cyls) as s:
-                s.load(st, 0)
-                _, drag = s.step(n)
-            vals.append(drag[:, :, 0].sum() / n)
-        fds[q] = (vals[0] - vals[1]) / (2 * h)
-    return fds
-
-
-def _adjoint_workload(beta=None):
-    from dataclasses import replace
-    from fortran8_gb300 import configs
-    w = configs.c4_adjoint()
-    assert (w.grid.nx, w.grid.ny, w.grid.nz, w.steps) == (128, 64, 64, 400)
-    w = replace(w, cyls=tuple(replace(c, xc=c.xc + 0.0123, yc=c.yc + 0.0371) for c in w.cyls))
-    if beta is not None:
-        w = replace(w, phys=replace(w.phys, beta=beta))
-    return w, configs.initial_state(w)
 
 
 def _workload_fd(gpu, w, st, n, qs_rel):

@@ -21,7 +21,7 @@ from .conftest import interior, rel_l2
 import f8_torch as ft  # noqa: E402  (path set by adjoint_cases)
 
 
-@pytest.mark.parametrize("name", ["channel", "periodic", "moving", "newtonian"])
+@pytest.mark.parametrize("name", ["channel", "periodic", "moving", "newtonian", "arc"])
 def test_forward_matches_oracle(oracle, name):
     w, st, step0 = case(name, oracle, spinup=0)
     n = 3
