@@ -8,6 +8,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <tuple>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -235,6 +238,24 @@ int fail(f8_ctx *c, cudaError_t e, const char *where) {
         if (e__ != cudaSuccess) return fail(ctx, e__, #call); \
     } while (0)
 
+// wall_plane_cluster searches a few thousand candidate layouts
+// (milliseconds); contexts of the same grid reuse the result
+int cached_wall_plane(int ny, int nz, int optin, WallLayout *wl) {
+    struct Entry { int cl; WallLayout wl; };
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, Entry> memo;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(ny, nz, optin);
+    auto it = memo.find(key);
+    if (it == memo.end()) {
+        Entry e{0, WallLayout{0, 0, 0}};
+        e.cl = wall_plane_cluster(ny, nz, (size_t)optin, &e.wl);
+        it = memo.emplace(key, e).first;
+    }
+    *wl = it->second.wl;
+    return it->second.cl;
+}
+
 int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, int prec, int poisson) {
     if (!g || !ph) return F8_ERR_ARG;
     if (g->dim != 2 && g->dim != 3) return F8_ERR_ARG;
@@ -413,7 +434,8 @@ int setup(f8_ctx *c) {
         int dev = 0, optin = 0;
         API_CUDA(c, cudaGetDevice(&dev));
         API_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-        d.plane_cl = g.walls ? wall_plane_cluster(g.ny, g.nz, (size_t)optin) : 0;
+        d.plane_cl = g.walls ? cached_wall_plane(g.ny, g.nz, optin, &d.plane_wl) : 0;
+        API_CUDA(c, setup_staged_projection(d));
         if (g.walls) d.fused_planes = (d.plane_cl > 0 || (size_t)12 * ((g.ny + 2) | 1) * g.nz <= (size_t)optin) ? 1 : 0;
         else d.fused_planes = (size_t)8 * (g.ny + 1) * g.nz <= (size_t)optin ? 1 : 0;
         if (d.fused_planes) {
@@ -427,18 +449,21 @@ int setup(f8_ctx *c) {
             for (int q = 0; q < 4; ++q) API_CUDA(c, cudaEventCreateWithFlags(&d.ev_g[q], cudaEventDisableTiming));
         }
         {
-            std::vector<float2> t2(std::max(1, g.nz / 2));
-            for (int t = 0; t < g.nz / 2; ++t) {
-                double a = 2.0 * PI * t / g.nz;
-                t2[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
-            }
+            // stage-major twiddles of the warp transforms: stage span m holds
+            // w^(p N / (2m)), p < m, at m - 1 + p (N entries, the last unused)
+            auto stage_table = [](int n) {
+                std::vector<float2> t(std::max(1, n));
+                for (int m = 1; m < n; m <<= 1)
+                    for (int p = 0; p < m; ++p) {
+                        const int q = p * (n / (2 * m));
+                        const double a = 2.0 * PI * q / n;
+                        t[m - 1 + p] = make_float2((float)std::cos(a), (float)-std::sin(a));
+                    }
+                return t;
+            };
+            const std::vector<float2> t2 = stage_table(g.nz), tx = stage_table(g.nx);
             API_CUDA(c, c->alloc(&d.twz2, t2.size()));
             API_CUDA(c, cudaMemcpyAsync(d.twz2, t2.data(), t2.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
-            std::vector<float2> tx(std::max(1, g.nx / 2));
-            for (int t = 0; t < g.nx / 2; ++t) {
-                double a = 2.0 * PI * t / g.nx;
-                tx[t] = make_float2((float)std::cos(a), (float)-std::sin(a));
-            }
             API_CUDA(c, c->alloc(&d.twx2, tx.size()));
             API_CUDA(c, cudaMemcpyAsync(d.twx2, tx.data(), tx.size() * sizeof(float2), cudaMemcpyHostToDevice, c->s));
             API_CUDA(c, cudaStreamSynchronize(c->s));
@@ -856,7 +881,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     std::memcpy(&now, c->res_host, sizeof(now));
     const StepCounters cnt{now.newton_iters - c->cnt_prev.newton_iters,
                            now.newton_unconverged - c->cnt_prev.newton_unconverged,
-                           now.nan_cells - c->cnt_prev.nan_cells};
+                           now.nan_cells - c->cnt_prev.nan_cells, now.copy_timeouts - c->cnt_prev.copy_timeouts};
     c->cnt_prev = now;
     const unsigned long long nan = *c->nan_host;
     if (drag && ncyl)
@@ -884,6 +909,10 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     }
     c->last_newton_iters = (long long)cnt.newton_iters;
     c->last_newton_unconv = (long long)cnt.newton_unconverged;
+    if (cnt.copy_timeouts) {
+        c->last_error = "a bulk-copy wait of the projection kernel ran out; the step is incomplete";
+        return F8_ERR_CUDA;
+    }
     if (nan || cnt.nan_cells) return F8_ERR_NAN;
     if (cnt.newton_unconverged) worst = std::max(worst, (int)F8_WARN_NEWTON);
     return worst;
@@ -1284,10 +1313,14 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
     if (drag && nw) std::copy(hd.begin(), hd.begin() + nw, drag);
     if (dJ_dparams) std::copy(gr.begin(), gr.end(), dJ_dparams);
     const StepCounters dc{cnt.newton_iters - cnt0.newton_iters, cnt.newton_unconverged - cnt0.newton_unconverged,
-                          cnt.nan_cells - cnt0.nan_cells};
+                          cnt.nan_cells - cnt0.nan_cells, cnt.copy_timeouts - cnt0.copy_timeouts};
     c->cnt_prev = cnt;
     c->last_newton_iters = (long long)dc.newton_iters;
     c->last_newton_unconv = (long long)dc.newton_unconverged;
+    if (dc.copy_timeouts) {
+        c->last_error = "a bulk-copy wait of the projection kernel ran out; the step is incomplete";
+        return F8_ERR_CUDA;
+    }
     if (dc.nan_cells) return F8_ERR_NAN;
     if (dc.newton_unconverged) return F8_WARN_NEWTON;
     return F8_OK;

@@ -59,15 +59,12 @@ enum BcKind { BC_U = 0, BC_V = 1, BC_W = 2, BC_P = 3, BC_C = 4, BC_CODE = 5 };
 inline std::atomic<long long> g_kernel_launches{0};
 inline void count_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
-// Per-step device counters (status words read by the host after a step).
 // Shared memory of the scan-Thomas wall plane kernel, whose (z, y) plane of
 // one kx is split over a cluster of cl CTAs, each holding R = ceil(lj / cl)
-// y rows: the rows (complex, odd row stride), the 1/den table of its systems
-// (row stride >= R and = T (mod 32), T = 1024 / nz threads per system, so
-// that the systems x chunks of a warp read distinct banks), the z twiddles,
-// and the composed forward / backward maps of its systems (3 floats each).
+// y rows: the rows (complex, odd row stride), the 1/den table of its systems,
+// the z twiddles, and the composed forward / backward maps of its systems
+// (3 floats each); the strides come from wall_layout below.
 __host__ __device__ inline int wall_rows_per_cta(int lj, int cl) { return (lj + cl - 1) / cl; }
-__host__ __device__ inline int wall_rd_stride(int r, int t) { return r + (((t - r) % 32) + 32) % 32; }
 
 // Halo cells of a field with one halo layer, numbered face by face.
 __host__ __device__ inline long halo_count(const Geo &g) {
@@ -107,18 +104,89 @@ __device__ inline bool halo_cell(const Geo &g, long tl, int &i, int &j, int &k) 
     return true;
 }
 
-__host__ __device__ inline size_t wall_plane_smem(int ny, int nz, int cl) {
-    const int r = wall_rows_per_cta(ny + 2, cl);
-    return (size_t)8 * (r | 1) * nz + (size_t)4 * wall_rd_stride(r, 1024 / nz) * nz + (size_t)(nz / 2) * 8
-           + (size_t)24 * nz;
+// Shared-memory layout of the wall-plane kernel for R rows per CTA and T
+// threads per (kx, kz) system: the row stride ps (float2) of the spectrum
+// tile, the row stride rs (float) of the pivot table and the rows L per
+// thread of the scan-parallel Thomas solve (L >= ceil(R / T)).  The thread
+// (row, t) = (lane / T, lane % T) of the solve touches row * stride + t * L +
+// it at step it; the layout minimises the wavefronts of those accesses: a
+// 64-bit access takes one wavefront per half-warp whose 16 lanes hit distinct
+// 8-byte bank pairs, a 32-bit access one per warp on 32 distinct banks.  ps
+// stays odd, which keeps the z transforms' accesses (lane stride ps) free of
+// conflicts.  Evaluated once per context on the host.
+struct WallLayout {
+    int ps, rs, L;
+};
+
+inline int wl_max_per_bank(const int *word, int n) {
+    int cnt[32] = {0}, seen[32][32];
+    int best = 0;
+    for (int q = 0; q < n; ++q) {
+        const int b = word[q] & 31;
+        bool dup = false;
+        for (int r = 0; r < cnt[b]; ++r) dup = dup || seen[b][r] == word[q];
+        if (dup) continue;
+        seen[b][cnt[b]++] = word[q];
+        best = cnt[b] > best ? cnt[b] : best;
+    }
+    return best;
+}
+
+inline long wl_cost(int R, int T, int ps, int rs, int L) {
+    long tot = 0;
+    int w2[32], w1[32];
+    for (int it = 0; it < L; ++it) {
+        int n1 = 0;
+        for (int h = 0; h < 32; h += 16) {
+            int n2 = 0;
+            for (int lane = h; lane < h + 16; ++lane) {
+                const int row = lane / T, t = lane % T;
+                const int c0 = t * L < R ? t * L : R, c1 = c0 + L < R ? c0 + L : R;
+                const int jl = c0 + it;
+                if (jl >= c1) continue;
+                const int q = row * ps + jl;
+                w2[n2++] = 2 * q;
+                w2[n2++] = 2 * q + 1;
+                w1[n1++] = row * rs + jl;
+            }
+            tot += wl_max_per_bank(w2, n2);
+        }
+        tot += wl_max_per_bank(w1, n1);
+    }
+    return tot;
+}
+
+inline size_t wall_plane_smem(const WallLayout &wl, int nz) {
+    return (size_t)8 * wl.ps * nz + (size_t)4 * wl.rs * nz + (size_t)nz * 8 + (size_t)24 * nz;
+}
+
+// the layout of least cost whose shared memory fits in `limit` bytes (ps = 0:
+// none fits)
+inline WallLayout wall_layout(int R, int T, int nz, size_t limit) {
+    const int L0 = (R + T - 1) / T;
+    WallLayout best{0, 0, 0};
+    long bc = -1;
+    for (int L = L0; L < L0 + 12; ++L)
+        for (int ps = R | 1; ps < (R | 1) + 16; ps += 2)      // ps matters modulo 16 (8-byte pairs)
+            for (int rs = R; rs < R + 32; ++rs) {             // rs modulo 32
+                if (wall_plane_smem(WallLayout{ps, rs, L}, nz) > limit) continue;
+                const long c = wl_cost(R, T, ps, rs, L);
+                if (bc < 0 || c < bc) { bc = c; best = WallLayout{ps, rs, L}; }
+            }
+    return best;
 }
 
 // smallest cluster (<= 8 CTAs) whose per-CTA share of the plane fits in
-// `limit` bytes of shared memory, or 0
-inline int wall_plane_cluster(int ny, int nz, size_t limit) {
+// `limit` bytes of shared memory with some layout (its best layout in *wl), or 0
+inline int wall_plane_cluster(int ny, int nz, size_t limit, WallLayout *wl) {
     if (nz != 32 && nz != 64 && nz != 128 && nz != 256) return 0;
-    for (int cl = 1; cl <= 8; ++cl)
-        if (wall_plane_smem(ny, nz, cl) <= limit) return cl;
+    for (int cl = 1; cl <= 8; ++cl) {
+        const int r = wall_rows_per_cta(ny + 2, cl);
+        // the most compact layout first: skip the search where even it does not fit
+        if (wall_plane_smem(WallLayout{r | 1, r, 0}, nz) > limit) continue;
+        *wl = wall_layout(r, 1024 / nz, nz, limit);
+        if (wl->ps > 0) return cl;
+    }
     return 0;
 }
 
@@ -126,6 +194,7 @@ struct StepCounters {
     unsigned long long newton_iters;
     unsigned long long newton_unconverged;
     unsigned long long nan_cells;
+    unsigned long long copy_timeouts;   // bulk-copy waits that ran out (the kernel stopped early)
 };
 
 }  // namespace f8

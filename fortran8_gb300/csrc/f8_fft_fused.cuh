@@ -300,10 +300,13 @@ namespace f8 {
 // ---------------------------------------------------------------------------
 // Warp-level radix-2 transform of one line of N = 32*V points: lane t holds
 // elements t + 32 s (s < V).  Spans >= 32 are butterflies inside the lane,
-// spans < 32 exchange with lane t ^ span.  tw: forward twiddles
-// (cos, -sin)(2 pi p / N), p < N/2, in shared memory.  The complex arithmetic
-// uses packed FP32x2 operations; the cross-lane butterflies are branch-free
-// (the lanes holding the first element of a pair multiply by 1).
+// spans < 32 exchange with lane t ^ span.  tw: forward twiddles in shared
+// memory, stage-major: the stage of span m reads w^(p N / (2m)), p < m, at
+// tw[m - 1 + p], w = (cos, -sin)(2 pi / N), so the lanes of a stage read
+// consecutive entries (no bank conflicts, where a table indexed by p N/(2m)
+// has lane stride N/(2m)).  The complex arithmetic uses packed FP32x2
+// operations; the cross-lane butterflies are branch-free (the lanes holding
+// the first element of a pair multiply by 1).
 __device__ __forceinline__ float2 cmul_p(float2 a, float2 w) {
     return __ffma2_rn(make_float2(a.x, a.x), w, __fmul2_rn(make_float2(a.y, a.y), make_float2(-w.y, w.x)));
 }
@@ -313,21 +316,21 @@ __device__ inline void warp_dif_fwd(float2 (&v)[V], const float2 *tw, int lane) 
     constexpr int N = 32 * V;
 #pragma unroll
     for (int m = N / 2; m >= 1; m >>= 1) {
-        const int ts = N / (2 * m);
+        const float2 *tm = tw + (m - 1);
         if (m >= 32) {
             const int sm = m / 32;
 #pragma unroll
             for (int s = 0; s < V; ++s) {
                 if ((s / sm) % 2) continue;          // upper element of the pair
                 const int pos = (lane + 32 * s) % (2 * m);
-                const float2 w = tw[pos * ts];
+                const float2 w = tm[pos];
                 const float2 a = v[s], b = v[s + sm];
                 v[s] = __fadd2_rn(a, b);
                 v[s + sm] = cmul_p(__ffma2_rn(b, make_float2(-1.0f, -1.0f), a), w);
             }
         } else {
             const bool second = lane & m;            // this lane holds the second element
-            const float2 w = second ? tw[((lane % (2 * m)) - m) * ts] : make_float2(1.0f, 0.0f);
+            const float2 w = second ? tm[(lane % (2 * m)) - m] : make_float2(1.0f, 0.0f);
             const float sg = second ? -1.0f : 1.0f;
 #pragma unroll
             for (int s = 0; s < V; ++s) {
@@ -347,14 +350,14 @@ __device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) 
     constexpr int N = 32 * V;
 #pragma unroll
     for (int m = 1; m < N; m <<= 1) {
-        const int ts = N / (2 * m);
+        const float2 *tm = tw + (m - 1);
         if (m >= 32) {
             const int sm = m / 32;
 #pragma unroll
             for (int s = 0; s < V; ++s) {
                 if ((s / sm) % 2) continue;
                 const int pos = (lane + 32 * s) % (2 * m);
-                const float2 w = tw[pos * ts];
+                const float2 w = tm[pos];
                 const float2 t = cmul_p(v[s + sm], make_float2(w.x, -w.y));
                 const float2 a = v[s];
                 v[s] = __fadd2_rn(a, t);
@@ -364,7 +367,7 @@ __device__ inline void warp_dit_inv(float2 (&v)[V], const float2 *tw, int lane) 
             const bool second = lane & m;
             float2 w = make_float2(1.0f, 0.0f);
             if (second) {
-                const float2 tv = tw[((lane % (2 * m)) - m) * ts];
+                const float2 tv = tm[(lane % (2 * m)) - m];
                 w = make_float2(tv.x, -tv.y);
             }
             const float sg = second ? -1.0f : 1.0f;
@@ -393,6 +396,7 @@ struct WallTables {
     float b_first;       // b of row 0 (1 U, -1 P, 0 V)
     float nxz_inv;
     int sys;
+    WallLayout wl;       // shared-memory strides and Thomas rows per thread (wall_layout)
 };
 
 // ---------------------------------------------------------------------------
@@ -421,7 +425,7 @@ constexpr int XW_RB = 16;     // rows per block of the x passes (a constant: the
 
 inline size_t xw_smem(int nx, int rb) {
     const int nh = nx / 2;
-    return ((size_t)nh + (size_t)(nh + 1) * (rb + 1) + (size_t)XW_WARPS * (nx + 32)) * sizeof(float2);
+    return ((size_t)nx + (size_t)(nh + 1) * (rb + 1) + (size_t)XW_WARPS * (nx + 32)) * sizeof(float2);
 }
 
 template <int E, typename TS>
@@ -431,9 +435,9 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xfwd_w(const TS *__restrict__
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float2 *tws = reinterpret_cast<float2 *>(smem_raw);
-    float2 *tile = tws + NH;
+    float2 *tile = tws + N;
     float2 *zb = tile + (size_t)(NH + 1) * (rb + 1) + (size_t)warp * (N + 32);
-    for (int q = threadIdx.x; q < NH; q += blockDim.x) tws[q] = twx[q];
+    for (int q = threadIdx.x; q < N; q += blockDim.x) tws[q] = twx[q];
     const int bpp = (ny + rb - 1) / rb;
     const int k = blockIdx.x / bpp;
     const int r0 = (blockIdx.x % bpp) * rb;
@@ -472,9 +476,9 @@ __global__ void __launch_bounds__(32 * XW_WARPS) k_xinv_w(const float2 *__restri
     extern __shared__ unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float2 *tws = reinterpret_cast<float2 *>(smem_raw);
-    float2 *tile = tws + NH;
+    float2 *tile = tws + N;
     float2 *zb = tile + (size_t)(NH + 1) * (rb + 1) + (size_t)warp * (N + 32);
-    for (int q = threadIdx.x; q < NH; q += blockDim.x) tws[q] = twx[q];
+    for (int q = threadIdx.x; q < N; q += blockDim.x) tws[q] = twx[q];
     const int bpp = (nrow + rb - 1) / rb;
     const int k = blockIdx.x / bpp;
     const int r0 = (blockIdx.x % bpp) * rb;
@@ -549,17 +553,17 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_c(float2 *S, int ny, in
     const int kx = blockIdx.x / cl;
     const int jlo = rank * R;
     const int nr = max(0, min(R, lj - jlo));   // rows held by this CTA
-    const int ps = R | 1;
-    const int rs = wall_rd_stride(R, T);
+    const int ps = wt.wl.ps;
+    const int rs = wt.wl.rs;
     float2 *P = reinterpret_cast<float2 *>(smem_raw);                 // [k][jl]
     float *Rs = reinterpret_cast<float *>(P + (size_t)ps * NZ);       // [row][jl], row = bitrev(kz)
-    float2 *tws = reinterpret_cast<float2 *>(Rs + (size_t)rs * NZ);   // NZ/2 twiddles
-    float *mapF = reinterpret_cast<float *>(tws + NZ / 2);            // [3][NZ]: A, Bx, By
+    float2 *tws = reinterpret_cast<float2 *>(Rs + (size_t)rs * NZ);   // NZ stage-major twiddles
+    float *mapF = reinterpret_cast<float *>(tws + NZ);                // [3][NZ]: A, Bx, By
     float *mapB = mapF + 3 * NZ;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     float2 *Sp = S + (size_t)kx * NZ * lj;
     const float *Rg = wt.rden + (size_t)kx * NZ * lj;
-    for (int q = threadIdx.x; q < NZ / 2; q += blockDim.x) tws[q] = twz[q];
+    for (int q = threadIdx.x; q < NZ; q += blockDim.x) tws[q] = twz[q];
     for (int k = warp; k < NZ; k += nwarp) {
         float *rrow = Rs + (size_t)(__brev((unsigned)k) >> (32 - LG)) * rs;
         for (int jl0 = lane; jl0 < nr; jl0 += 128) {   // four loads of each array in flight per lane
@@ -595,7 +599,7 @@ __global__ void __launch_bounds__(1024, 1) k_plane_walls_c(float2 *S, int ny, in
         const int row = threadIdx.x / T, t = threadIdx.x % T;
         float2 *x = P + (size_t)row * ps;
         const float *rd = Rs + (size_t)row * rs;
-        const int L = (nr + T - 1) / T;
+        const int L = wt.wl.L;
         const int c0 = min(nr, t * L), c1 = min(nr, c0 + L);
         const bool sysv = wt.sys == SYS_V;
         auto fwd_coef = [&](int jl, float &al, float2 &be) {

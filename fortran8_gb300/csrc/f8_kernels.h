@@ -65,8 +65,11 @@ struct Dev {
     float *kx2f, *ky2f, *kz2f;             // FP32 copies of the modified wavenumbers
     int fused_planes;                      // 1: (z, y) plane of one kx fits in shared memory
     int plane_cl;                          // walls: CTAs per cluster holding one (z, y) plane (0: none)
-    float2 *twz2;                          // (cos, -sin)(2 pi p/NZ), p < NZ/2
-    float2 *twx2;                          // (cos, -sin)(2 pi p/NX), p < NX/2
+    WallLayout plane_wl;                   // its shared-memory layout (wall_layout)
+    int march_runs, march_ctas;            // staged projection: z runs per y tile, persistent CTAs (0: direct loads)
+    int march_depth;                       // its steps of copies in flight
+    float2 *twz2;                          // stage-major twiddles of the warp z transforms (NZ entries)
+    float2 *twx2;                          // and of the warp x transforms (NX entries)
     float *wtR[3];                         // Thomas 1/den tables of the U, V, P wall systems
     float *mwx[3], *mwy[3];                // per-marker 1D kernel weights (3 each)
     float *csr_w[3];                       // per column-list entry: the marker's x weight times y weight there
@@ -216,6 +219,7 @@ cudaError_t mixed_solve_periodic(Dev &d, const float *src, float *dst, float *lo
                                  cudaStream_t s);
 cudaError_t mixed_solve_walls(Dev &d, const float *src, float *dst, float *lo, int mode, int sys, cudaStream_t s);
 cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float *rl, float *rd, cudaStream_t s);
+cudaError_t setup_staged_projection(Dev &d);
 cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const double *drag_w, bool ab2_first,
                                bool polymer, cudaStream_t s);
 cudaError_t adjoint_fold_state_f(AdjStateF &A, const Dev &d, cudaStream_t s);

@@ -21,12 +21,14 @@
 // is divergence-free to the df64 rounding level.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include "../../include/f8.h"
 #include "f8_common.cuh"
 #include "f8_df64.cuh"
 #include "f8_fft.cuh"
 #include "f8_fft_fused.cuh"
 #include "f8_kernels.h"
+#include "f8_tma.cuh"
 
 namespace f8 {
 namespace {
@@ -1162,7 +1164,39 @@ __global__ void k_defect_df(const float *__restrict__ Phi, const float *__restri
 // projection and SMAC pressure update (fenep.f90:1562-1604):
 // U^{n+1} = U^n + (dU - dt/dX (Phi_{+1} - Phi)) in df64, and
 // P^{n+1} = P^n + Phi - dt beta/(2 Re) L_h Phi with the small Laplacian term
-// in FP32; NaN watch on the new U.
+// in FP32, for the two cells (k, k + 1) of a pair, from their loaded values:
+// c0 = Phi at the cells, pp / pm = Phi at their +1 / -1 neighbours along x,
+// y, z; Fv = U, V, W, Dv = dU, dV, dW, Pv = P at the cells.  Shared by the
+// direct-load kernel and the staged (bulk-copy) kernel, so both give the
+// same bits.
+__device__ __forceinline__ void march_pair_math(const df2 &c0, const df2 (&pp)[3], const df2 (&pm)[3],
+                                                const df2 (&Fv)[3], const float2 (&Dv)[3], const df2 &Pv,
+                                                const MixConst &mc, df2 (&nu)[3], df2 &pn) {
+    const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
+    // the FP32 Laplacian of Phi, per lane as the scalar expression
+    float lapx = 0.0f, lapy = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const df2 dp = df2_sub(pp[c], c0);
+        const df2 inc = df2_add_f(df2_mul(dp, bcast(df_neg(mc.dtd[c]))), Dv[c]);
+        nu[c] = df2_add(Fv[c], inc);
+        const float2 dpf = add2_rn(sub2_rn(pp[c].hi, c0.hi), sub2_rn(pp[c].lo, c0.lo));
+        const float2 dmf = add2_rn(sub2_rn(c0.hi, pm[c].hi), sub2_rn(c0.lo, pm[c].lo));
+        lapx = __fadd_rn(lapx, __fmul_rn(__fsub_rn(dpf.x, dmf.x), i2[c]));
+        lapy = __fadd_rn(lapy, __fmul_rn(__fsub_rn(dpf.y, dmf.y), i2[c]));
+    }
+    pn = df2_add_f(df2_add(Pv, c0), make_float2(__fmul_rn(-mc.pcf, lapx), __fmul_rn(-mc.pcf, lapy)));
+}
+
+// NaN watch on the new U (the reference stops on a NaN velocity,
+// fenep_2d.f90:1974), counted in the projection kernels instead of in a
+// separate pass
+__device__ __forceinline__ void count_nonfinite(float2 unew, StepCounters *cnt) {
+    const unsigned act = __activemask();
+    const unsigned nb = __ballot_sync(act, !isfinite(unew.x) || !isfinite(unew.y));
+    if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
+}
+
 __global__ void __launch_bounds__(256, 4) k_march_df(DfF U, DfF V, DfF W, DfF P, const float *__restrict__ dU, const float *__restrict__ dV,
                            const float *__restrict__ dW, DfF Phi, Geo g, MixConst mc, StepCounters *cnt) {
     int i, j, k;
@@ -1192,21 +1226,8 @@ __global__ void __launch_bounds__(256, 4) k_march_df(DfF U, DfF V, DfF W, DfF P,
             Dv[c] = at2f(D[c], h, hb);
         }
         const df2 Pv = at2(P, h, hb);
-        const float i2[3] = {mc.ix2, mc.iy2, mc.iz2};
-        df2 nu[3];
-        // the FP32 Laplacian of Phi, per lane as the scalar expression
-        float lapx = 0.0f, lapy = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const df2 dp = df2_sub(pp[c], c0);
-            const df2 inc = df2_add_f(df2_mul(dp, bcast(df_neg(mc.dtd[c]))), Dv[c]);
-            nu[c] = df2_add(Fv[c], inc);
-            const float2 dpf = add2_rn(sub2_rn(pp[c].hi, c0.hi), sub2_rn(pp[c].lo, c0.lo));
-            const float2 dmf = add2_rn(sub2_rn(c0.hi, pm[c].hi), sub2_rn(c0.lo, pm[c].lo));
-            lapx += (dpf.x - dmf.x) * i2[c];
-            lapy += (dpf.y - dmf.y) * i2[c];
-        }
-        const df2 pn = df2_add_f(df2_add(Pv, c0), make_float2(-mc.pcf * lapx, -mc.pcf * lapy));
+        df2 nu[3], pn;
+        march_pair_math(c0, pp, pm, Fv, Dv, Pv, mc, nu, pn);
 #pragma unroll
         for (int c = 0; c < 3; ++c) F[c].set(h, df2_x(nu[c]));
         P.set(h, df2_x(pn));
@@ -1217,11 +1238,197 @@ __global__ void __launch_bounds__(256, 4) k_march_df(DfF U, DfF V, DfF W, DfF P,
         }
         unew = make_float2(nu[0].hi.x, p.two ? nu[0].hi.y : 0.0f);
     }
-    // NaN watch on the new U (the reference stops on a NaN velocity,
-    // fenep_2d.f90:1974), counted here instead of in a separate pass
-    const unsigned act = __activemask();
-    const unsigned nb = __ballot_sync(act, !isfinite(unew.x) || !isfinite(unew.y));
-    if (nb && (threadIdx.x & 31) == (unsigned)(__ffs(act) - 1)) atomicAdd(&cnt->nan_cells, (unsigned long long)__popc(nb));
+    count_nonfinite(unew, cnt);
+}
+
+// ---------------------------------------------------------------------------
+// The projection with its inputs staged in shared memory by bulk copies.
+//
+// A work unit is a tile of two y rows [jb, jb + 2) (jb even) over a run of z
+// planes; the two rows of a plane are the two lanes of the pair arithmetic
+// (march_pair_math is lane-wise the scalar arithmetic, so any pairing gives
+// the same bits).  A step of a unit is one plane k: the 11 point-wise arrays
+// (U, V, W, P hi / lo, dU, dV, dW) on the tile's rows, and Phi (hi / lo) on
+// planes k - 1, k, k + 1, each on the tile's rows and on the row pairs holding
+// the rows below and above them (periodic wrap or the Neumann copy at the
+// walls, as nbr_p).  Full rows are copied (x halo included), a row pair per
+// bulk copy of 8 SX bytes.
+//
+// The CTA is persistent: it walks its units (blockIdx.x, + gridDim.x, ...)
+// as one sequence of steps, and thread 0 keeps the copies of the next D steps
+// in flight: D + 1 buffers of point-wise planes, each with its mbarrier, and a
+// ring of D + 5 Phi planes (a step uses three; a unit's first step loads three
+// planes, the others one; runs are at least D + 1 planes long, so at most one
+// unit starts among any D + 1 consecutive steps).
+constexpr int MT_PW = 11;   // point-wise arrays
+constexpr int MT_THREADS = 256;
+constexpr int MT_MAXD = 4;
+
+struct MarchTmaArgs {
+    const float *pw[MT_PW];      // U.hi, U.lo, V.hi, V.lo, W.hi, W.lo, P.hi, P.lo, dU, dV, dW
+    float *out[8];               // U.hi .. P.lo (written in place)
+    const float *phi[2];         // Phi hi, lo
+    int zruns;                   // z runs per tile
+    int depth;                   // D: steps whose copies are in flight ahead of the one computed
+};
+
+inline size_t march_tma_smem(const Geo &g, int depth) {
+    return 128 + (size_t)((depth + 1) * MT_PW + (depth + 5) * 6) * 2 * g.sx * sizeof(float);
+}
+
+// units of the CTA, as a cursor over (unit, plane step)
+struct MtCursor {
+    int unit, s, S, k0;
+    __device__ void set(const Geo &g, int zruns, int u) {
+        const int ntiles = g.sy / 2, nunits = ntiles * zruns;
+        for (unit = u; unit < nunits; unit += gridDim.x) {
+            const int run = unit / ntiles;
+            const int q0 = (int)((long)run * g.nz / zruns), q1 = (int)((long)(run + 1) * g.nz / zruns);
+            S = q1 - q0;
+            k0 = 1 + q0;
+            s = 0;
+            if (S > 0) return;
+        }
+        S = 0;
+    }
+    __device__ bool valid(const Geo &g, int zruns) const { return unit < (g.sy / 2) * zruns; }
+    __device__ void next(const Geo &g, int zruns) {
+        if (++s >= S) set(g, zruns, unit + gridDim.x);
+    }
+};
+
+__global__ void __launch_bounds__(MT_THREADS, 1) k_march_tma(MarchTmaArgs a, Geo g, MixConst mc, StepCounters *cnt) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);          // D + 1 barriers
+    __shared__ int abort_flag;
+    const int D = a.depth, NB = D + 1, RING = D + 5;
+    const int rowp = 2 * g.sx;                                        // floats per row pair
+    float *pwb = reinterpret_cast<float *>(smem_raw + 128);           // [NB][MT_PW][rowp]
+    float *phb = pwb + (size_t)NB * MT_PW * rowp;                     // [RING][2][3 pairs][rowp]
+    const uint32_t pair_bytes = (uint32_t)(rowp * sizeof(float));
+    const size_t plane = (size_t)g.sx * g.sy;
+    const int ntiles = g.sy / 2;
+    auto ynb = [&](int j, int d) { return g.walls ? max(1, min(g.ny, j + d)) : wrapy(g, j + d); };
+    // row pairs of the rows below / above the computed rows of tile jb
+    auto pairs_of = [&](int jb, int &jlo, int &jhi) {
+        const int jc0 = max(jb, 1), jc1 = min(jb + 1, g.ny);
+        jlo = ynb(jc0, -1) & ~1;
+        jhi = ynb(jc1, 1) & ~1;
+    };
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < NB; ++q) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+        abort_flag = 0;
+    }
+    __syncthreads();
+    // producer (thread 0): cursor, groups issued, Phi planes loaded
+    MtCursor pc;
+    unsigned pg = 0, pphi = 0;
+    auto issue = [&]() {
+        const int jb = 2 * (pc.unit % ntiles);
+        int jlo, jhi;
+        pairs_of(jb, jlo, jhi);
+        uint64_t *b = &bar[pg % NB];
+        const int k = pc.k0 + pc.s;
+        const int nphi = pc.s == 0 ? 3 : 1;
+        mbar_expect(b, pair_bytes * (uint32_t)(MT_PW + 6 * nphi));
+        float *dst = pwb + (size_t)(pg % NB) * MT_PW * rowp;
+        for (int arr = 0; arr < MT_PW; ++arr)
+            bulk_load(dst + (size_t)arr * rowp, a.pw[arr] + (size_t)k * plane + (size_t)jb * g.sx, pair_bytes, b);
+        const int rows[3] = {jlo, jb, jhi};
+        for (int kk = pc.s == 0 ? k - 1 : k + 1; kk <= k + 1; ++kk) {
+            const size_t zo = (size_t)wrapz(g, kk) * plane;
+            float *ps = phb + (size_t)(pphi % RING) * 6 * rowp;
+            for (int arr = 0; arr < 2; ++arr)
+                for (int r = 0; r < 3; ++r)
+                    bulk_load(ps + (size_t)(arr * 3 + r) * rowp, a.phi[arr] + zo + (size_t)rows[r] * g.sx, pair_bytes, b);
+            ++pphi;
+        }
+        ++pg;
+        pc.next(g, a.zruns);
+    };
+    if (threadIdx.x == 0) {
+        pc.set(g, a.zruns, blockIdx.x);
+        for (int q = 0; q < D && pc.valid(g, a.zruns); ++q) issue();
+    }
+    // consumers: cursor, step count, Phi planes consumed through this step
+    MtCursor cc;
+    cc.set(g, a.zruns, blockIdx.x);
+    unsigned t = 0, cphi = 0;
+    for (; cc.valid(g, a.zruns); cc.next(g, a.zruns), ++t) {
+        if (threadIdx.x == 0 && pc.valid(g, a.zruns)) {
+            fence_async_smem();
+            issue();
+        }
+        cphi += cc.s == 0 ? 3 : 1;
+        if (!mbar_wait(&bar[t % NB], (t / NB) & 1)) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) {
+            // let the copies already issued finish before the CTA leaves
+            if (threadIdx.x == 0) {
+                for (unsigned q = t; q < pg; ++q) mbar_wait(&bar[q % NB], (q / NB) & 1, 200000000LL);
+                atomicAdd(&cnt->copy_timeouts, 1ULL);
+            }
+            return;
+        }
+        const int jb = 2 * (cc.unit % ntiles);
+        int jlo, jhi;
+        pairs_of(jb, jlo, jhi);
+        const int k = cc.k0 + cc.s;
+        const float *pw = pwb + (size_t)(t % NB) * MT_PW * rowp;
+        const float *sm = phb + (size_t)((cphi - 3) % RING) * 6 * rowp;   // plane k - 1
+        const float *s0 = phb + (size_t)((cphi - 2) % RING) * 6 * rowp;   // plane k
+        const float *sp = phb + (size_t)((cphi - 1) % RING) * 6 * rowp;   // plane k + 1
+        // shared-memory row (of the six of a Phi slot) of the y neighbour of row j
+        auto nrow = [&](int j, int d) {
+            const int jn = ynb(j, d);
+            if (jn >= jb && jn < jb + 2) return 2 + jn - jb;
+            if (jn >= jlo && jn < jlo + 2) return jn - jlo;
+            return 4 + jn - jhi;
+        };
+        const bool in0 = jb >= 1, in1 = jb + 1 <= g.ny;   // the two rows (lanes) computed
+        // rows outside 1..NY are evaluated on the loaded halo values and not stored
+        const int j0 = in0 ? jb : jb + 1, j1 = in1 ? jb + 1 : jb;
+        const int ym0 = nrow(j0, -1) * g.sx, yp0 = nrow(j0, 1) * g.sx;
+        const int ym1 = nrow(j1, -1) * g.sx, yp1 = nrow(j1, 1) * g.sx;
+        for (int i = 1 + (int)threadIdx.x; i <= g.nx; i += blockDim.x) {
+            const int xm = wrapx(g, i - 1), xp = wrapx(g, i + 1);
+            // Phi (hi, lo) of both rows at row offset ro0 / ro1 of a slot
+            auto ph2 = [&](const float *sl, int o0, int o1) {
+                return df2_pack(df{sl[o0], sl[o0 + 3 * rowp]}, df{sl[o1], sl[o1 + 3 * rowp]});
+            };
+            const int c0o = 2 * g.sx + i, c1o = 3 * g.sx + i;   // the tile rows in a slot
+            const df2 c0 = ph2(s0, c0o, c1o);
+            const df2 pp[3] = {ph2(s0, 2 * g.sx + xp, 3 * g.sx + xp), ph2(s0, yp0 + i, yp1 + i), ph2(sp, c0o, c1o)};
+            const df2 pm[3] = {ph2(s0, 2 * g.sx + xm, 3 * g.sx + xm), ph2(s0, ym0 + i, ym1 + i), ph2(sm, c0o, c1o)};
+            auto pv = [&](int arr, int r) { return pw[(size_t)arr * rowp + r * g.sx + i]; };
+            df2 Fv[3];
+            float2 Dv[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                Fv[q] = df2_pack(df{pv(2 * q, 0), pv(2 * q + 1, 0)}, df{pv(2 * q, 1), pv(2 * q + 1, 1)});
+                Dv[q] = make_float2(pv(8 + q, 0), pv(8 + q, 1));
+            }
+            const df2 Pv = df2_pack(df{pv(6, 0), pv(7, 0)}, df{pv(6, 1), pv(7, 1)});
+            df2 nu[3], pn;
+            march_pair_math(c0, pp, pm, Fv, Dv, Pv, mc, nu, pn);
+            const size_t h0 = (size_t)hix(g, i, jb, k), h1 = h0 + g.sx;
+            if (in0) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) { a.out[2 * q][h0] = nu[q].hi.x; a.out[2 * q + 1][h0] = nu[q].lo.x; }
+                a.out[6][h0] = pn.hi.x; a.out[7][h0] = pn.lo.x;
+            }
+            if (in1) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) { a.out[2 * q][h1] = nu[q].hi.y; a.out[2 * q + 1][h1] = nu[q].lo.y; }
+                a.out[6][h1] = pn.hi.y; a.out[7][h1] = pn.lo.y;
+            }
+            if ((in0 && !isfinite(nu[0].hi.x)) || (in1 && !isfinite(nu[0].hi.y))) atomicAdd(&cnt->nan_cells, 1ULL);
+        }
+        // every thread is done with this step's buffers before later copies
+        // may overwrite them
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1494,12 +1701,12 @@ cudaError_t solve_walls_fused(Dev &d, const TS *src, XOutF out, int sys, cudaStr
     if (d.plane_cl > 0 && d.wtR[0]) {
         const int t = sys == SYS_P ? 2 : (sys == SYS_V ? 1 : 0);
         const float b_first = sys == SYS_P ? -1.0f : (sys == SYS_V ? 0.0f : 1.0f);
-        WallTables wt{d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, b_first, ps.nxz_inv, sys};
+        WallTables wt{d.wtR[t], ps.bc, sys == SYS_P ? -1.0f : 1.0f, b_first, ps.nxz_inv, sys, d.plane_wl};
         const int cl = d.plane_cl;
         cudaLaunchConfig_t cfg{};
         cfg.gridDim = dim3((unsigned)(nxh * cl));
         cfg.blockDim = dim3(1024);
-        cfg.dynamicSmemBytes = wall_plane_smem(ny, nz, cl);
+        cfg.dynamicSmemBytes = wall_plane_smem(d.plane_wl, nz);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1590,6 +1797,54 @@ cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float 
     const dim3 pblk(32, 8), pgrid((g.nx + pblk.x - 1) / pblk.x, (g.ny + pblk.y - 1) / pblk.y, (g.nz + 1) / 2);
     k_defect_df<<<pgrid, pblk, 0, s>>>(phi, rh, rl, rd, g, make_const(g, d.ph)); count_launch();
     return cudaGetLastError();
+}
+
+// The staged projection (k_march_tma) needs row pairs that are contiguous,
+// 16-byte aligned blocks: NX a multiple of 4, NY even, 3D; and its shared
+// memory for at least one step in flight within the opt-in limit (the
+// deepest of D = 1 .. 4 that fits is taken).  The z runs per y tile are
+// chosen so that the units (tile, run) spread evenly over the persistent CTAs
+// (one per SM), each run at least D + 1 planes.
+//
+// Measured on the 256 x 128 x 128 channel (GB300): 134 us against the
+// direct-load kernel's 82 us.  The df64 arithmetic costs about 2.6
+// instructions per byte, and the staged kernel's 8 warps per SM (one step of
+// 256 cell pairs per CTA at a time, the shared memory holding D + 1 steps)
+// issue too slowly to keep up with the copies, where the direct-load kernel
+// keeps 32 warps per SM.  The direct-load kernel is therefore the default;
+// F8_STAGED_PROJECTION=1 in the environment, read when a context is
+// created, selects the staged one.
+cudaError_t setup_staged_projection(Dev &d) {
+    const Geo &g = d.g;
+    d.march_runs = 0;
+    d.march_ctas = 0;
+    d.march_depth = 0;
+    const char *env = std::getenv("F8_STAGED_PROJECTION");
+    if (!env || env[0] != '1') return cudaSuccess;
+    if (g.dim != 3 || g.nx % 4 != 0 || g.ny % 2 != 0) return cudaSuccess;
+    int dev = 0, optin = 0;
+    F8_CUDA_RET(cudaGetDevice(&dev));
+    F8_CUDA_RET(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    int depth = 0;
+    for (int dd = MT_MAXD; dd >= 1 && !depth; --dd)
+        if (march_tma_smem(g, dd) <= (size_t)optin) depth = dd;
+    if (!depth || g.nz < depth + 1) return cudaSuccess;
+    F8_CUDA_RET(cudaFuncSetAttribute(k_march_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)march_tma_smem(g, depth)));
+    const int nsm = device_sm_count(), ntiles = g.sy / 2;
+    int best = 1;
+    double bestc = 1e30;
+    for (int runs = 1; runs <= g.nz / (depth + 1); ++runs) {
+        const int units = ntiles * runs;
+        const int ctas = std::min(nsm, units);
+        // planes on the busiest CTA (the copies stream across its units)
+        const double c = (double)((units + ctas - 1) / ctas) * ((g.nz + runs - 1) / runs) + 2.0 * runs / g.nz;
+        if (c < bestc) { bestc = c; best = runs; }
+    }
+    d.march_runs = best;
+    d.march_ctas = std::min(nsm, ntiles * best);
+    d.march_depth = depth;
+    return cudaSuccess;
 }
 
 cudaError_t init_kernels_mixed() {
@@ -1972,7 +2227,19 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     if (tp) { k_tape_phi<<<tnb, 256, 0, s>>>(d.Phif, tp->Phi, g); count_launch(); }
     mark(6);
     kmark(F8_KERNEL_MARCH, 0);
-    k_march_df<<<pgrid, pblk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
+    if (d.march_runs > 0) {
+        MarchTmaArgs ma{};
+        const float *pw[MT_PW] = {U.hi, U.lo, V.hi, V.lo, W.hi, W.lo, P.hi, P.lo, d.dUf[0], d.dUf[1], d.dUf[2]};
+        float *ou[8] = {U.hi, U.lo, V.hi, V.lo, W.hi, W.lo, P.hi, P.lo};
+        for (int q = 0; q < MT_PW; ++q) ma.pw[q] = pw[q];
+        for (int q = 0; q < 8; ++q) ma.out[q] = ou[q];
+        ma.phi[0] = Phi.hi; ma.phi[1] = Phi.lo;
+        ma.zruns = d.march_runs;
+        ma.depth = d.march_depth;
+        k_march_tma<<<d.march_ctas, MT_THREADS, march_tma_smem(g, d.march_depth), s>>>(ma, g, mc, d.cnt);
+    } else {
+        k_march_df<<<pgrid, pblk, 0, s>>>(U, V, W, P, d.dUf[0], d.dUf[1], d.dUf[2], Phi, g, mc, d.cnt);
+    }
     count_launch();
     kmark(F8_KERNEL_MARCH, 1);
     F8_CUDA_RET(launch_bc_set(state_bc_set(d), g, s));
