@@ -36,10 +36,23 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
     // 6. projection / pressure update
     k_march_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lP, A.lPhi, t.Phi, g, kap, dt / (2.0 * re), kc, A.grad); count_launch();
     F8_CUDA_RET(fold(fold_set<double>({{A.lPhi, BC_P}}), g, s));
-    // 5. Poisson
+    // 5. Poisson.  The solve maps the right-hand side to the zero-mean Phi
+    // through the pseudo-inverse of the symmetric Laplacian, so its transpose
+    // is the same map applied to the zero-mean part of the adjoint: the FFT
+    // solve (which drops the mean mode), or, for the SOR variant, the same
+    // red-black SOR to the same tolerance (then shifted to zero mean)
     k_pack<double><<<adj_cells(g, blk), blk, 0, s>>>(A.lPhi, A.pack, g); count_launch();
-    F8_CUDA_RET(poisson_solve_fp64(d, A.pack, A.lQ[0], s));
-    k_div_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, A.lQ[0], A.lUp[0], A.lUp[1], A.lUp[2], g); count_launch();
+    double *lq = A.lQ[0];
+    if (A.sor) {
+        F8_CUDA_RET(remove_mean_fp64(d, A.pack, d.ni, s));
+        int it = 0;
+        F8_CUDA_RET(sor_solve_fp64(d, A.pack, A.lsor, A.work, A.sor_omega, A.sor_eps, A.sor_itrmax, &it, s));
+        if (it > A.sor_itrmax) ++A.sor_capped;
+        lq = A.lsor;
+    } else {
+        F8_CUDA_RET(poisson_solve_fp64(d, A.pack, A.lQ[0], s));
+    }
+    k_div_adj<double><<<nb, 256, 0, s>>>(A.lU, A.lV, A.lW, lq, A.lUp[0], A.lUp[1], A.lUp[2], g); count_launch();
     F8_CUDA_RET(fold(fold_set<double>({{A.lUp[0], BC_U}, {A.lUp[1], BC_V}, {A.lUp[2], BC_W}}), g, s));
     // 4. Helmholtz
     for (int c = 0; c < 3; ++c) {

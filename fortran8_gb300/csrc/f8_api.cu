@@ -86,6 +86,7 @@ struct GradMem {
     std::vector<void *> mem[4];
     AdjState A{};
     int K = 0, nck = 0, nsteps = 0;
+    int sor_capped = 0;                     // forward SOR solves of the call that reached sor_itrmax
     size_t ck_slot = 0;                     // doubles per checkpoint
     double *tU = nullptr, *tV = nullptr, *tW = nullptr, *tC = nullptr;
     double *tUa = nullptr, *tUp = nullptr, *tPhi = nullptr, *tFc = nullptr, *tCm = nullptr;
@@ -1001,7 +1002,7 @@ int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
     if (nck > G.nck) {
         G.free_group(2);
         G.nck = 0;
-        G.ck_slot = 10 * cs + 6 * ni;
+        G.ck_slot = 11 * cs + 6 * ni;
         API_CUDA(c, G.get(2, &G.ck, nck * G.ck_slot));
         G.nck = nck;
     }
@@ -1020,10 +1021,12 @@ cudaError_t ck_copy(f8_ctx *c, int slot, bool save) {
     GradMem &G = c->gm;
     const size_t cs = d.cs, ni = d.ni;
     double *base = G.ck + (size_t)slot * G.ck_slot;
-    double *f[11] = {d.U, d.V, d.W, d.P, d.C, d.Ax0, d.Ay0, d.Az0, d.Tx0, d.Ty0, d.Tz0};
-    const size_t n[11] = {cs, cs, cs, cs, 6 * cs, ni, ni, ni, ni, ni, ni};
+    // Phi is the SOR variant's start value of the next solve, so a recomputed
+    // segment repeats the SOR iterates exactly
+    double *f[12] = {d.U, d.V, d.W, d.P, d.C, d.Ax0, d.Ay0, d.Az0, d.Tx0, d.Ty0, d.Tz0, d.Phi};
+    const size_t n[12] = {cs, cs, cs, cs, 6 * cs, ni, ni, ni, ni, ni, ni, cs};
     size_t off = 0;
-    for (int q = 0; q < 11; ++q) {
+    for (int q = 0; q < 12; ++q) {
         const size_t b = n[q] * sizeof(double);
         cudaError_t e = save ? cudaMemcpyAsync(base + off, f[q], b, cudaMemcpyDeviceToDevice, c->s)
                              : cudaMemcpyAsync(f[q], base + off, b, cudaMemcpyDeviceToDevice, c->s);
@@ -1044,7 +1047,8 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
     o.polymer = c->phys.beta != 1.0;
     o.ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
     o.ibm = ncyl > 0;
-    o.poisson = F8_POISSON_FFT;
+    o.poisson = c->poisson;
+    o.sor_omega = c->phys.sor_omega; o.sor_eps = c->phys.sor_eps; o.sor_itrmax = c->phys.sor_itrmax;
     if (!o.polymer) F8_CUDA_RET(cudaMemsetAsync(d.C, 0, 6 * hb, c->s));
     auto cp = [&](void *dst, const void *src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->s);
@@ -1058,6 +1062,7 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
     int sor = -1;
     if (rec >= 0) o.c_mid = G.tCm + (size_t)rec * 6 * cs;
     F8_CUDA_RET(step_fp64(d, o, ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr, &sor, c->s));
+    if (c->poisson == F8_POISSON_SOR && sor > c->phys.sor_itrmax) ++G.sor_capped;
     if (rec >= 0) {
         const size_t ng = 2 * (size_t)d.g.nx * d.g.nz;
         F8_CUDA_RET(cp(G.tC + (size_t)(rec + 1) * 6 * cs, d.C, 6 * hb));
@@ -1351,8 +1356,11 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
             double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
-    if (c->grid.dim != 3 || c->poisson != F8_POISSON_FFT || c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
-    if (c->precision == F8_MIXED) return grad_mixed(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
+    if (c->grid.dim != 3 || c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
+    if (c->precision == F8_MIXED) {
+        if (c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
+        return grad_mixed(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
+    }
     Dev &d = c->d;
     const int ncyl = (int)c->cyl.size();
     const size_t cs = d.cs, ni = d.ni;
@@ -1372,6 +1380,7 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
     API_CUDA(c, cudaMemsetAsync(d.cnt, 0, sizeof(StepCounters), c->s));
     c->cnt_prev = StepCounters{};   // f8_step reports differences from this
     API_CUDA(c, cudaMemsetAsync(c->nan_dev, 0, sizeof(unsigned long long), c->s));
+    G.sor_capped = 0;
     const int step0 = c->step;
     // forward: checkpoints at the segment starts, the tape of the last segment
     for (int seg = 0; seg < nseg; ++seg) {
@@ -1409,6 +1418,14 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
         for (int q = 0; q < 6; ++q)
             if (is[q]) API_CUDA(c, cudaMemcpyAsync(id[q], is[q], ni * sizeof(double), cudaMemcpyHostToDevice, c->s));
         API_CUDA(c, cudaStreamSynchronize(c->s));
+    }
+    // the SOR variant's adjoint pressure solves, warm started from zero
+    A.sor = c->poisson == F8_POISSON_SOR;
+    A.sor_omega = c->phys.sor_omega; A.sor_eps = c->phys.sor_eps; A.sor_itrmax = c->phys.sor_itrmax;
+    A.sor_capped = 0;
+    if (A.sor) {
+        if (!A.lsor) API_CUDA(c, G.get(0, &A.lsor, cs));
+        API_CUDA(c, cudaMemsetAsync(A.lsor, 0, cs * sizeof(double), c->s));
     }
     // reverse sweep over the segments
     const bool polymer = c->phys.beta != 1.0;
@@ -1470,6 +1487,7 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
     c->last_newton_unconv = (long long)cnt.newton_unconverged;
     if (nan) return F8_ERR_NAN;
     if (cnt.newton_unconverged) return F8_WARN_NEWTON;
+    if (G.sor_capped || A.sor_capped) return F8_WARN_SOR;
     return F8_OK;
 }
 

@@ -135,6 +135,10 @@ cudaError_t marker_weights_fp64(Dev &d, cudaStream_t s);
 // pressure Poisson L x = q; src interior, dst halo layout (interior written)
 cudaError_t helmholtz_solve_fp64(Dev &d, int comp, const double *src, double *dst, cudaStream_t s);
 cudaError_t poisson_solve_fp64(Dev &d, const double *src, double *dst, cudaStream_t s);
+// red-black SOR of Q (interior) into the halo field Phi (start value), residuals in E (interior)
+cudaError_t sor_solve_fp64(Dev &d, const double *Q, double *Phi, double *E, double omega, double eps, int itrmax,
+                           int *iters, cudaStream_t s);
+cudaError_t remove_mean_fp64(Dev &d, double *A, int n, cudaStream_t s);
 // On-device diagnostics (f8_diag.cu)
 struct DiagValues {
     double ke, cfl, trc_min, trc_max, trc_mean, trc_std, div_max;
@@ -185,6 +189,13 @@ struct AdjState {
     double *pack;                          // one packed interior field
     double *work;                          // per-cell sources of the gather kernels (ADJ_WORK_FIELDS halo fields)
     double *grad;                          // dJ/d(Wi, beta, L^2, (xc, yc) per cylinder), accumulated
+    // SOR variant: the adjoint pressure solve by the same red-black SOR, warm
+    // started from the previous adjoint step's solution (lsor, halo)
+    int sor;
+    double sor_omega, sor_eps;
+    int sor_itrmax;
+    double *lsor;
+    int sor_capped;                        // adjoint solves that reached sor_itrmax
 };
 // what the reverse of one step reads from its forward step
 struct TapeStep {

@@ -968,13 +968,14 @@ __global__ void k_bc_scalar_flag(double *A, Geo g, int kind, const int *flag) {
 
 // Deterministic two-level reductions: partial sums per block in a fixed order,
 // then one block sums the partials.
-template <int OP>  // 0: sum of squares, 1: sum of interior values of a halo field
+template <int OP>  // 0: sum of squares, 1: sum of interior values of a halo field, 2: sum of values
 __global__ void k_reduce_part(const double *A, int n, double *part, Geo g, const int *flag) {
     if (flag && flag[0]) return;
     __shared__ double sh[256];
     double s = 0.0;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         if (OP == 0) { double v = A[q]; s += v * v; }
+        else if (OP == 2) s += A[q];
         else {
             int i = 1 + (int)(q % g.nx), j = 1 + (int)((q / g.nx) % g.ny), k = 1 + (int)(q / ((long)g.nx * g.ny));
             s += A[hix(g, i, j, k)];
@@ -1145,37 +1146,56 @@ cudaError_t reduce_sumsq(const double *A, int n, double *part, double *scal, int
     return cudaGetLastError();
 }
 
-cudaError_t sor_solve(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
+// Red-black SOR (the reference's poisson, fenep.f90:848-905) of the
+// right-hand side Q (interior) into the halo field Phi, which holds the start
+// value; E (interior) receives the residuals.  Stops when
+// sqrt(sum E^2 / sum Q^2) < eps or after itrmax sweeps (*iters = itrmax + 1),
+// then shifts Phi to zero mean (fenep_2d.f90:577-579).
+cudaError_t sor_solve_on(Dev &d, const double *Q, double *Phi, double *E, double omega, double eps, int itrmax,
+                         int *iters, cudaStream_t s) {
     const Geo &g = d.g;
     dim3 blk(32, 8);
     dim3 grd = cell_grid(g, blk);
     // er0 = sum(Q^2) (+1e-16 guard); flag reset
     F8_CUDA_RET(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), s));
-    F8_CUDA_RET(reduce_sumsq(d.Q[0], d.ni, d.red, d.scal, 0, 2, d.flag, 0.0, 0, g, s));
+    F8_CUDA_RET(reduce_sumsq(Q, d.ni, d.red, d.scal, 0, 2, d.flag, 0.0, 0, g, s));
     const long nh = halo_count(g);
     const unsigned hb = (unsigned)((nh + 255) / 256);
     int done = 0, it_host[2] = {0, 0};
     const int chunk = 25;
-    for (int it0 = 1; it0 <= o.sor_itrmax && !done; it0 += chunk) {
-        int last = std::min(o.sor_itrmax, it0 + chunk - 1);
+    for (int it0 = 1; it0 <= itrmax && !done; it0 += chunk) {
+        int last = std::min(itrmax, it0 + chunk - 1);
         for (int it = it0; it <= last; ++it) {
             for (int color = 0; color < 2; ++color) {
-                k_sor_color<<<grd, blk, 0, s>>>(d.Phi, d.E, d.Q[0], g, color, o.sor_omega, d.flag); count_launch();
-                k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag); count_launch();
+                k_sor_color<<<grd, blk, 0, s>>>(Phi, E, Q, g, color, omega, d.flag); count_launch();
+                k_bc_scalar_flag<<<hb, 256, 0, s>>>(Phi, g, BC_P, d.flag); count_launch();
             }
-            k_bc_scalar_flag<<<hb, 256, 0, s>>>(d.Phi, g, BC_P, d.flag); count_launch();
-            F8_CUDA_RET(reduce_sumsq(d.E, d.ni, d.red, d.scal, 1, 1, d.flag, o.sor_eps, it, g, s));
+            k_bc_scalar_flag<<<hb, 256, 0, s>>>(Phi, g, BC_P, d.flag); count_launch();
+            F8_CUDA_RET(reduce_sumsq(E, d.ni, d.red, d.scal, 1, 1, d.flag, eps, it, g, s));
         }
         F8_CUDA_RET(cudaMemcpyAsync(it_host, d.flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
         F8_CUDA_RET(cudaStreamSynchronize(s));
         done = it_host[0];
     }
-    *iters = done ? it_host[1] : o.sor_itrmax + 1;
+    *iters = done ? it_host[1] : itrmax + 1;
     // zero-mean shift (fenep_2d.f90:577-579)
     int nb = std::min(1024, (d.ni + 255) / 256);
-    k_reduce_part<1><<<nb, 256, 0, s>>>(d.Phi, d.ni, d.red, g, nullptr); count_launch();
+    k_reduce_part<1><<<nb, 256, 0, s>>>(Phi, d.ni, d.red, g, nullptr); count_launch();
     k_reduce_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 2, 0, d.flag, 0.0, 0); count_launch();
-    k_shift<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Phi, d.cs, d.scal, 2, 1.0 / ((double)g.nx * g.ny * g.nz)); count_launch();
+    k_shift<<<(d.cs + 255) / 256, 256, 0, s>>>(Phi, d.cs, d.scal, 2, 1.0 / ((double)g.nx * g.ny * g.nz)); count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t sor_solve(Dev &d, const StepOpts &o, int *iters, cudaStream_t s) {
+    return sor_solve_on(d, d.Q[0], d.Phi, d.E, o.sor_omega, o.sor_eps, o.sor_itrmax, iters, s);
+}
+
+// subtract the mean of an interior field (n values)
+cudaError_t remove_mean(Dev &d, double *A, int n, cudaStream_t s) {
+    int nb = std::min(1024, (n + 255) / 256);
+    k_reduce_part<2><<<nb, 256, 0, s>>>(A, n, d.red, d.g, nullptr); count_launch();
+    k_reduce_final<<<1, 256, 0, s>>>(d.red, nb, d.scal, 3, 0, d.flag, 0.0, 0); count_launch();
+    k_shift<<<(n + 255) / 256, 256, 0, s>>>(A, n, d.scal, 3, 1.0 / n); count_launch();
     return cudaGetLastError();
 }
 
@@ -1208,6 +1228,13 @@ cudaError_t helmholtz_solve_fp64(Dev &d, int comp, const double *src, double *ds
     if (!d.g.walls) return fft_solve_periodic(d, src, dst, 1.0, d.ph.dt * d.ph.beta / d.ph.re / 2.0, s);
     return wall_solve(d, src, dst, comp == 1 ? SYS_V : SYS_U, 0.0, s);
 }
+
+cudaError_t sor_solve_fp64(Dev &d, const double *Q, double *Phi, double *E, double omega, double eps, int itrmax,
+                           int *iters, cudaStream_t s) {
+    return sor_solve_on(d, Q, Phi, E, omega, eps, itrmax, iters, s);
+}
+
+cudaError_t remove_mean_fp64(Dev &d, double *A, int n, cudaStream_t s) { return remove_mean(d, A, n, s); }
 
 cudaError_t poisson_solve_fp64(Dev &d, const double *src, double *dst, cudaStream_t s) {
     if (!d.g.walls) return fft_solve_periodic(d, src, dst, 0.0, -1.0, s);
