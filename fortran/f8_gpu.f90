@@ -27,7 +27,7 @@ module f8_gpu
                                  F8_WARN_SOR = 17
     integer(c_int), parameter :: F8_FP64 = 0, F8_MIXED = 1
     integer(c_int), parameter :: F8_POISSON_FFT = 0, F8_POISSON_SOR = 1
-    integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1
+    integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1, F8_BC_WALLS_Z = 2
     integer(c_int), parameter :: F8_IBM_CELL_VOLUME = 0, F8_IBM_ARC_VOLUME = 1
 
     type, bind(C) :: f8_grid

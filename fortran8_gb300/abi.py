@@ -26,6 +26,7 @@ F8_POISSON_FFT = 0
 F8_POISSON_SOR = 1
 F8_BC_PERIODIC = 0
 F8_BC_WALLS = 1
+F8_BC_WALLS_Z = 2
 F8_IBM_CELL_VOLUME = 0
 F8_IBM_ARC_VOLUME = 1
 

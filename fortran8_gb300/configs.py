@@ -28,6 +28,12 @@ chosen so that dX = dY = dZ, which the IBM requires, fenep.f90:1808-1810):
                 U_C L_C / nu = 5400 for f_C = 2 rps, D_C = 0.03 m, nu = 1e-6,
                 dt 8e-5, markers spread with the arc element of their ring
                 (smac.f90:1129), noise 1e-3 on a fluid at rest.
+* ``smac_kabe``  the z-walled Newtonian channel of smac_kabe.f90
+                (smac_kabe.f90:4-37): 16^3 cells in the box normalised by
+                Xmax (1 x 1 x 1), walls normal to z, Re 5, dt = dt_C U_C / Xmax
+                with dt_C = 0.01 and U_C = Zmax^2 Re / 8, noise 1e-3 on a fluid
+                at rest; the upper wall speed is a parameter (0 in the
+                reference).
 
 The channel is driven by the uniform body force Fx = 2 / (Re h^2), h = Ly/2,
 under which the laminar Newtonian profile is the Poiseuille base flow with
@@ -118,8 +124,16 @@ def smac_rotating(n=64, repeats=1):
     return Workload("smac_rotating", g, ph, cyls, 10, 5, 1.0e-3, "rest")
 
 
+def smac_kabe(n=16, uwall=0.0):
+    g = GridSpec(3, n, n, n, 1.0, 1.0, 1.0, bc_y=abi.F8_BC_WALLS_Z, uwall=uwall)
+    re = 5.0
+    u_c = (2 * PI) ** 2 * re / 8.0
+    ph = PhysSpec(re=re, wi=1.0, beta=1.0, lp2=100.0, dt=0.01 * u_c / (2 * PI))
+    return Workload("smac_kabe", g, ph, (), 10, 11, 1.0e-3, "rest")
+
+
 WORKLOADS = {"c1_2d": c1_2d, "c2_3d": c2_3d, "c3_channel": c3_channel,
-             "c4_adjoint": c4_adjoint, "c5_large": c5_large, "smac_rotating": smac_rotating}
+             "c4_adjoint": c4_adjoint, "c5_large": c5_large, "smac_rotating": smac_rotating, "smac_kabe": smac_kabe}
 
 
 def initial_state(w: Workload) -> State:

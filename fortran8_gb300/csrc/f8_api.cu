@@ -122,7 +122,11 @@ struct GradMem {
 }  // namespace
 
 struct f8_ctx {
-    f8_grid grid{};
+    f8_grid grid{};                   // the grid the step runs on (y and z exchanged for F8_BC_WALLS_Z)
+    f8_grid user_grid{};              // the caller's grid
+    bool zwalls = false;              // F8_BC_WALLS_Z: fields are exchanged at the boundary
+    std::vector<double> zbuf[15];     // host staging of the exchanged fields
+    std::vector<double> zbuf2[15];    // a second set (f8_grad: seed and state adjoint)
     f8_phys phys{};
     std::vector<f8_cyl> cyl;
     std::vector<double> cyl_vol;      // drag / spreading volume of each cylinder's markers
@@ -264,7 +268,8 @@ int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, in
     if (g->dim == 2 && g->nz != 1) return F8_ERR_ARG;
     if (g->dim == 3 && g->nz < 4) return F8_ERR_ARG;
     if (!(g->lx > 0 && g->ly > 0 && g->lz > 0)) return F8_ERR_ARG;
-    if (g->bc_y != F8_BC_PERIODIC && g->bc_y != F8_BC_WALLS) return F8_ERR_ARG;
+    if (g->bc_y != F8_BC_PERIODIC && g->bc_y != F8_BC_WALLS && g->bc_y != F8_BC_WALLS_Z) return F8_ERR_ARG;
+    if (g->bc_y == F8_BC_WALLS_Z && (g->dim != 3 || ncyl > 0)) return F8_ERR_UNSUPPORTED;
     if (!is_pow2(g->nx) || !is_pow2(g->ny) || !is_pow2(g->nz)) return F8_ERR_ARG;  // spectral solves
     if (g->nx > 1024 || g->ny > 1024 || g->nz > 1024) return F8_ERR_ARG;
     if ((long)(g->nx + 2) * (g->ny + 2) * (g->nz + 2) > (1L << 31) / 8) return F8_ERR_ARG;
@@ -675,6 +680,93 @@ int ensure_drag(f8_ctx *c, int nsteps) {
     return F8_OK;
 }
 
+// ---- walls normal to z (smac_kabe.f90) --------------------------------------
+// The caller's fields (x, y, z) are the step's fields (x, y', z') = (x, z, y):
+// halo and interior arrays are transposed in (y, z), the velocity-like
+// components exchange y and z (u' = u, v' = w, w' = v), and the tensor C
+// (xx, xy, xz, yy, yz, zz) becomes (xx, xz, xy, zz, zy, yy).
+struct ZSwap {
+    int nx, ny, nz;   // the caller's extents
+    // caller (i, j, k) <-> step (i, k, j); halo = 1 with the halo layers
+    template <bool Back>
+    void move(const double *src, double *dst, int halo, int ncomp, const int *perm) const {
+        const int sx = nx + 2 * halo, sy = ny + 2 * halo, sz = nz + 2 * halo;
+        for (int k = 0; k < sz; ++k)
+            for (int j = 0; j < sy; ++j)
+                for (int i = 0; i < sx; ++i) {
+                    const size_t u = (size_t)i + (size_t)sx * (j + (size_t)sy * k);   // caller
+                    const size_t t = (size_t)i + (size_t)sx * (k + (size_t)sz * j);   // step
+                    for (int m = 0; m < ncomp; ++m) {
+                        const int mu = perm ? perm[m] : m;   // caller component of step component m
+                        if (Back) dst[u * ncomp + mu] = src[t * ncomp + m];
+                        else dst[t * ncomp + m] = src[u * ncomp + mu];
+                    }
+                }
+    }
+};
+
+constexpr int C_SWAP[6] = {0, 2, 1, 5, 4, 3};
+
+// pointers of the fields in the order below, with the halo flag and the
+// source field of each step field (velocity-like triples exchange y and z)
+void zwall_slots(f8_fields *f, double **slot[15]) {
+    double **p[15] = {&f->u, &f->v, &f->w, &f->p, &f->phi, &f->c, &f->ax0, &f->ay0, &f->az0,
+                      &f->tx0, &f->ty0, &f->tz0, &f->fx, &f->fy, &f->fz};
+    for (int q = 0; q < 15; ++q) slot[q] = p[q];
+}
+constexpr int Z_SRC[15] = {0, 2, 1, 3, 4, 5, 6, 8, 7, 9, 11, 10, 12, 14, 13};   // step field q <- caller field Z_SRC[q]
+
+// caller fields -> step fields in the context's staging buffers
+void zwall_in(f8_ctx *c, const f8_fields *in, f8_fields *out, std::vector<double> (&buf)[15]) {
+    const ZSwap zs{c->user_grid.nx, c->user_grid.ny, c->user_grid.nz};
+    f8_fields src = *in;
+    *out = f8_fields{};
+    double **ps[15], **pd[15];
+    zwall_slots(&src, ps);
+    zwall_slots(out, pd);
+    const size_t cs = (size_t)(zs.nx + 2) * (zs.ny + 2) * (zs.nz + 2), ni = (size_t)zs.nx * zs.ny * zs.nz;
+    for (int q = 0; q < 15; ++q) {
+        const double *from = *ps[Z_SRC[q]];
+        if (!from) continue;
+        const bool halo = q < 6, tensor = q == 5;
+        buf[q].resize((halo ? cs : ni) * (tensor ? 6 : 1));
+        zs.move<false>(from, buf[q].data(), halo ? 1 : 0, tensor ? 6 : 1, tensor ? C_SWAP : nullptr);
+        *pd[q] = buf[q].data();
+    }
+}
+
+// step fields (in the staging buffers) -> the caller's non-null arrays
+void zwall_out(f8_ctx *c, const f8_fields *stepf, f8_fields *user) {
+    const ZSwap zs{c->user_grid.nx, c->user_grid.ny, c->user_grid.nz};
+    f8_fields sf = *stepf;
+    double **ps[15], **pu[15];
+    zwall_slots(&sf, ps);
+    zwall_slots(user, pu);
+    for (int q = 0; q < 15; ++q) {
+        double *to = *pu[Z_SRC[q]];
+        if (!to || !*ps[q]) continue;
+        const bool halo = q < 6, tensor = q == 5;
+        zs.move<true>(*ps[q], to, halo ? 1 : 0, tensor ? 6 : 1, tensor ? C_SWAP : nullptr);
+    }
+}
+
+// staging buffers of the step fields a caller asked for
+void zwall_stage(f8_ctx *c, const f8_fields *user, f8_fields *stepf, std::vector<double> (&buf)[15]) {
+    const ZSwap zs{c->user_grid.nx, c->user_grid.ny, c->user_grid.nz};
+    f8_fields u = *user;
+    *stepf = f8_fields{};
+    double **pu[15], **pd[15];
+    zwall_slots(&u, pu);
+    zwall_slots(stepf, pd);
+    const size_t cs = (size_t)(zs.nx + 2) * (zs.ny + 2) * (zs.nz + 2), ni = (size_t)zs.nx * zs.ny * zs.nz;
+    for (int q = 0; q < 15; ++q) {
+        if (!*pu[Z_SRC[q]]) continue;
+        const bool halo = q < 6, tensor = q == 5;
+        buf[q].resize((halo ? cs : ni) * (tensor ? 6 : 1));
+        *pd[q] = buf[q].data();
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -702,7 +794,14 @@ int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *c
     }
     f8_ctx *c = new (std::nothrow) f8_ctx();
     if (!c) return F8_ERR_NOMEM;
-    c->grid = *g; c->phys = *ph; c->precision = prec; c->poisson = poisson;
+    c->grid = *g; c->user_grid = *g; c->phys = *ph; c->precision = prec; c->poisson = poisson;
+    if (g->bc_y == F8_BC_WALLS_Z) {
+        // the walls-normal-to-z box is the y-walled box with y and z exchanged
+        c->zwalls = true;
+        c->grid.ny = g->nz; c->grid.nz = g->ny;
+        c->grid.ly = g->lz; c->grid.lz = g->ly;
+        c->grid.bc_y = F8_BC_WALLS;
+    }
     if (ncyl > 0) c->cyl.assign(cy, cy + ncyl);
     st = setup(c);
     if (st) {
@@ -714,7 +813,7 @@ int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *c
     return F8_OK;
 }
 
-int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
+static int load_impl(f8_ctx *c, const f8_fields *in, int step0) {
     if (!c || !in || !in->u || !in->v || !in->p || !in->c || step0 < 0) return F8_ERR_ARG;
     if (c->grid.dim == 3 && !in->w) return F8_ERR_ARG;
     Dev &d = c->d;
@@ -919,7 +1018,7 @@ int f8_step(f8_ctx *c, int nsteps, double *drag) {
     return worst;
 }
 
-int f8_store(f8_ctx *c, f8_fields *out) {
+static int store_impl(f8_ctx *c, f8_fields *out) {
     if (!c || !out) return F8_ERR_ARG;
     Dev &d = c->d;
     const size_t cs = d.cs, ni = d.ni;
@@ -959,6 +1058,26 @@ int f8_store(f8_ctx *c, f8_fields *out) {
     API_CUDA(c, cudaStreamSynchronize(c->s));
     return F8_OK;
 }
+
+int f8_load(f8_ctx *c, const f8_fields *in, int step0) {
+    if (!c || !in) return F8_ERR_ARG;
+    if (!c->zwalls) return load_impl(c, in, step0);
+    if (!in->u || !in->v || !in->w || !in->p || !in->c || step0 < 0) return F8_ERR_ARG;
+    f8_fields t;
+    zwall_in(c, in, &t, c->zbuf);
+    return load_impl(c, &t, step0);
+}
+
+int f8_store(f8_ctx *c, f8_fields *out) {
+    if (!c || !out) return F8_ERR_ARG;
+    if (!c->zwalls) return store_impl(c, out);
+    f8_fields t;
+    zwall_stage(c, out, &t, c->zbuf);
+    const int st = store_impl(c, &t);
+    if (st == F8_OK) zwall_out(c, &t, out);
+    return st;
+}
+
 
 }  // extern "C"
 
@@ -1352,8 +1471,8 @@ TapeStep tape_step(f8_ctx *c, int rec) {
 
 extern "C" {
 
-int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed, double *J,
-            double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
+static int grad_impl(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed,
+                     double *J, double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
     if (c->grid.dim != 3 || c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
@@ -1491,6 +1610,18 @@ int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, c
     return F8_OK;
 }
 
+int f8_grad(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed, double *J,
+            double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
+    if (!c || !c->zwalls) return grad_impl(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
+    f8_fields si{}, so{};
+    if (seed) zwall_in(c, seed, &si, c->zbuf);
+    if (dJ_dstate) zwall_stage(c, dJ_dstate, &so, c->zbuf2);
+    const int st = grad_impl(c, nsteps, checkpoint_every, drag_w, seed ? &si : nullptr, J, dJ_dparams,
+                             dJ_dstate ? &so : nullptr, drag);
+    if (dJ_dstate && (st == F8_OK || st >= 16)) zwall_out(c, &so, dJ_dstate);
+    return st;
+}
+
 int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
     if (!c || !dg) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
@@ -1511,6 +1642,7 @@ int f8_diagnostics(f8_ctx *c, f8_diag *dg) {
 }
 
 int f8_slice(f8_ctx *c, int axis, int variant, double *out) {
+    if (c && c->zwalls) return F8_ERR_UNSUPPORTED;   // the exchanged axes are not mapped back here
     if (!c || !out || axis < 0 || axis > 2 || variant < 0 || variant > 1) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
     if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
@@ -1539,6 +1671,7 @@ int upload_means(f8_ctx *c, const double *mu, const double *mv, const double *mw
 }  // namespace
 
 int f8_turbulence(f8_ctx *c, const double *mu, const double *mv, const double *mw, f8_turb *out) {
+    if (c && c->zwalls) return F8_ERR_UNSUPPORTED;   // the exchanged axes are not mapped back here
     if (!c || !out) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
     if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
@@ -1558,6 +1691,7 @@ int f8_turbulence(f8_ctx *c, const double *mu, const double *mv, const double *m
 }
 
 int f8_spectrum(f8_ctx *c, const double *mu, const double *mv, const double *mw, double *energy) {
+    if (c && c->zwalls) return F8_ERR_UNSUPPORTED;   // the exchanged axes are not mapped back here
     if (!c || !energy) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
     if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
@@ -1586,6 +1720,7 @@ int f8_spectrum(f8_ctx *c, const double *mu, const double *mv, const double *mw,
 }
 
 int f8_stats_begin(f8_ctx *c, int mode, const double *mu, const double *mv, const double *mw, int max_steps) {
+    if (c && c->zwalls) return F8_ERR_UNSUPPORTED;   // the exchanged axes are not mapped back here
     if (!c || mode < 0 || mode > 2 || max_steps < 0) return F8_ERR_ARG;
     if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
     if (mode == 2 && (!mu || !mv || !mw)) return F8_ERR_ARG;
@@ -1631,6 +1766,7 @@ int f8_stats_read(f8_ctx *c, double *su, double *sv, double *sw, double *probes,
 }
 
 int f8_selection_codes(f8_ctx *c, unsigned char *codes) {
+    if (c && c->zwalls) return F8_ERR_UNSUPPORTED;   // the exchanged axes are not mapped back here
     if (!c || !codes) return F8_ERR_ARG;
     if (!c->loaded || c->step == c->step0 || c->phys.beta == 1.0) return F8_ERR_STATE;
     const f8::Geo &g = c->d.g;

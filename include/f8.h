@@ -67,8 +67,17 @@ enum f8_poisson {
 
 enum f8_bc_y {
     F8_BC_PERIODIC = 0, /* PBM (fenep.f90:147-166)                         */
-    F8_BC_WALLS = 1     /* no-slip walls at y = 0 and y = NY*dY
+    F8_BC_WALLS = 1,    /* no-slip walls at y = 0 and y = NY*dY
                            (fenep_2d.f90:1098-1143 with NA = 0, NB = NY)  */
+    F8_BC_WALLS_Z = 2   /* no-slip walls at z = 0 and z = NZ*dZ, x and y
+                           periodic: the channel of smac_kabe.f90
+                           (U_kabe .. P_kabe, smac_kabe.f90:118-157; the
+                           upper wall moves at uwall in x).  3D, no
+                           cylinders; f8_slice, f8_spectrum, f8_turbulence,
+                           f8_stats_* and f8_selection_codes return
+                           F8_ERR_UNSUPPORTED.  Fields keep the caller's
+                           (x, y, z) layouts; the library runs the y-walled
+                           step with y and z exchanged                   */
 };
 
 typedef struct f8_grid {
@@ -76,7 +85,7 @@ typedef struct f8_grid {
     int nx, ny, nz;     /* cell counts; powers of two for the FFT solver;
                            nz = 1 when dim == 2                           */
     double lx, ly, lz;  /* box lengths: dX = lx/nx ... (fenep.f90:13)     */
-    int bc_y;           /* enum f8_bc_y                                   */
+    int bc_y;           /* enum f8_bc_y: the box's boundary conditions    */
     double uwall;       /* upper-wall speed when bc_y == F8_BC_WALLS
                            (fenep_2d.f90:1084, 1103)                      */
 } f8_grid;
