@@ -36,6 +36,7 @@
 #include <initializer_list>
 #include <utility>
 #include "f8_common.cuh"
+#include "f8_df64.cuh"
 
 namespace f8 {
 namespace {
@@ -83,6 +84,28 @@ inline AdjCoef<T> adj_coef(const Geo &g) {
 }
 
 // Block sum of v added to *dst in FP64 (every thread of the block calls it).
+// Block sum of a float partial added to *dst: the partials are summed as
+// double-float pairs (two-sums on the FP32 pipes), converted to double once
+// per block.  A double reduction tree would run on GB300's FP64 pipe, a small
+// fraction of its FP32 rate, and cost more than the FP32 kernels around it.
+__device__ inline void block_atomic_add(float v, double *dst) {
+    __shared__ float shh[32], shl[32];
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    df s{v, 0.0f};
+    for (int o = 16; o > 0; o >>= 1)
+        s = df_add(s, df{__shfl_down_sync(0xffffffffu, s.hi, o), __shfl_down_sync(0xffffffffu, s.lo, o)});
+    __syncthreads();
+    if ((t & 31) == 0) { shh[t >> 5] = s.hi; shl[t >> 5] = s.lo; }
+    __syncthreads();
+    if (t < 32) {
+        df r = t < (nt >> 5) ? df{shh[t], shl[t]} : df{0.0f, 0.0f};
+        for (int o = 16; o > 0; o >>= 1)
+            r = df_add(r, df{__shfl_down_sync(0xffffffffu, r.hi, o), __shfl_down_sync(0xffffffffu, r.lo, o)});
+        if (t == 0 && (r.hi != 0.0f || r.lo != 0.0f)) atomicAdd(dst, (double)r.hi + (double)r.lo);
+    }
+}
+
 __device__ inline void block_atomic_add(double v, double *dst) {
     __shared__ double sh[32];
     const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
@@ -233,7 +256,7 @@ __global__ void k_march_adj(const T *lU, const T *lV, const T *lW, const T *lP, 
             gb = -c_beta * p0 * lf;
         }
     }
-    block_atomic_add((double)gb, grad + 1);
+    block_atomic_add(gb, grad + 1);
 }
 
 // interior of a halo field -> packed interior array
@@ -565,6 +588,7 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
         const int o = qix(g, i, j, k), h = hix(g, i, j, k);
         const size_t cs = (size_t)a.cs;
         const T *F[3] = {a.U, a.V, a.W};
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
             const T lq = a.lQ[c][h];
             const T lua = lq + a.lUa[c][h];
@@ -595,7 +619,7 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
             gb += a.inv_re * lB * lap(F[c]);
         }
     }
-    block_atomic_add((double)gb, a.grad + 1);
+    block_atomic_add(gb, a.grad + 1);
 }
 
 template <typename T>
@@ -841,9 +865,9 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
         }
     }
     if (a.polymer) {
-        block_atomic_add((double)(-g_coef * a.inv_1mb), a.grad + 1);
-        block_atomic_add((double)(-g_coef * a.inv_wi), a.grad + 0);
-        block_atomic_add((double)g_l2, a.grad + 2);
+        block_atomic_add(-g_coef * a.inv_1mb, a.grad + 1);
+        block_atomic_add(-g_coef * a.inv_wi, a.grad + 0);
+        block_atomic_add(g_l2, a.grad + 2);
     }
 }
 
@@ -1027,8 +1051,8 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, G
             put(PS_SF + 5, (l11 * (T(1) - sw1) + l12 * (T(1) + sw1)) * cz);    // -> w(k-1)
         }
     }
-    block_atomic_add((double)gwi, a.grad + 0);
-    block_atomic_add((double)gl2, a.grad + 2);
+    block_atomic_add(gwi, a.grad + 0);
+    block_atomic_add(gl2, a.grad + 2);
 }
 
 template <typename T>
