@@ -213,23 +213,36 @@ def oracle_fns():
 
 
 def cpu_baseline(w, steps_cap=2, budget_s=30.0):
-    """Oracle on the host cores (all threads) on a bounded sample of the workload."""
+    """Oracle on the host cores (all threads) on a bounded sample of the workload,
+    and one step on a single thread (the reference's code is serial)."""
     fns, lib = oracle_fns()
     threads = int(lib.f8o_max_threads())
     st0 = configs.initial_state(w)
-    with Solver(fns, w.grid, w.phys, w.cyls) as s:
-        s.load(st0)
-        t0 = time.perf_counter()
-        n = 0
-        while n < steps_cap:
-            s.step(1, want_drag=True)
-            n += 1
-            if time.perf_counter() - t0 > budget_s:
-                break
-        el = time.perf_counter() - t0
-    return {"value": w.cells * n / el / 1e6, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} full step(s) of {w.grid.nx}x{w.grid.ny}x{w.grid.nz} from the seeded initial state, "
-                      f"FP64, {threads} OpenMP threads, {el:.1f} s"}
+
+    def sample(cap, budget):
+        with Solver(fns, w.grid, w.phys, w.cyls) as s:
+            s.load(st0)
+            t0 = time.perf_counter()
+            n = 0
+            while n < cap:
+                s.step(1, want_drag=True)
+                n += 1
+                if time.perf_counter() - t0 > budget:
+                    break
+            return n, time.perf_counter() - t0
+
+    n, el = sample(steps_cap, budget_s)
+    out = {"value": w.cells * n / el / 1e6, "unit": "Mcell-steps/s", "cores": threads, "kind": "port",
+           "sample": f"{n} full step(s) of {w.grid.nx}x{w.grid.ny}x{w.grid.nz} from the seeded initial state, "
+                     f"FP64, {threads} OpenMP threads, {el:.1f} s"}
+    lib.f8o_set_threads(1)
+    try:
+        n1, el1 = sample(1, budget_s)
+    finally:
+        lib.f8o_set_threads(threads)
+    out["one_thread"] = {"value": w.cells * n1 / el1 / 1e6, "unit": "Mcell-steps/s", "cores": 1,
+                         "sample": f"{n1} full step(s), FP64, 1 thread, {el1:.1f} s"}
+    return out
 
 
 def run_reference(args, w, budget_s=90.0):

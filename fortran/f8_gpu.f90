@@ -112,7 +112,7 @@ module f8_gpu
         end function f8_store
 
         ! Gradient of J = sum(drag_weights * drag) + <seed, final state> by the
-        ! discrete adjoint (3D contexts, FP64 or mixed).  drag_weights: real(8)
+        ! discrete adjoint (FP64 2D/3D, mixed 3D).  drag_weights: real(8)
         ! (3, ncyl, nsteps) or c_null_ptr (time-averaged total x drag); seed,
         ! dJ_dstate: c_loc of an f8_fields or c_null_ptr; J: real(8) or
         ! c_null_ptr; dJ_dparams: real(8) (3 + 2*ncyl) = dWi, dbeta, dL^2,

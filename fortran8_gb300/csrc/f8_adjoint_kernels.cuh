@@ -221,10 +221,10 @@ FoldSet<T> fold_set(std::initializer_list<std::pair<T *, int>> fields) {
 }
 
 template <typename T>
-FoldSet<T> fold_c(T *C, int cs) {
+FoldSet<T> fold_c(T *C, int cs, int ncomp = 6) {
     FoldSet<T> f{};
-    for (int m = 0; m < 6; ++m) { f.A[m] = C + (size_t)m * cs; f.kind[m] = BC_C; }
-    f.n = 6;
+    for (int m = 0; m < ncomp; ++m) { f.A[m] = C + (size_t)m * cs; f.kind[m] = BC_C; }
+    f.n = ncomp;
     return f;
 }
 
@@ -322,6 +322,7 @@ struct IbmAdjArgs {
     T *lUa[3];               // out: adjoint of Ua (full halo box, scattered)
     const double *w;         // drag weights of this step (ncyl x 3)
     double *grad;            // grad[3 + 2 l], grad[4 + 2 l]: cylinder centre
+    int d3;                  // 0: the 2D step (one marker plane, no z weight, fenep_2d.f90:1726-1819)
 };
 
 // One thread per (marker, plane, component).  Forward: Ub = sum Ua delta dX^3,
@@ -361,7 +362,7 @@ __global__ void k_ibm_adj(IbmAdjArgs<T> a, Geo g) {
             const T rx = T((x - xc) / dX), ry = T((y - yc) / dY), rz = T((z - zc) / dZ);
             wxs[q] = roma_t(rx);
             wys[q] = roma_t(ry);
-            wzs[q] = roma_t(rz);
+            wzs[q] = a.d3 ? roma_t(rz) : (q == 1 ? T(1) : T(0));
             dwx[q] = -droma_t(rx) / T(dX);   // d/dxc
             dwy[q] = -droma_t(ry) / T(dY);
         }

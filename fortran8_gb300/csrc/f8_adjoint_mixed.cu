@@ -108,6 +108,7 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         }
         ia.w = drag_w;
         ia.grad = A.grad;
+        ia.d3 = 1;
         k_ibm_adj<float><<<dim3((d.nm + 127) / 128, g.nz, 3), 128, 0, s>>>(ia, g); count_launch();
         F8_CUDA_RET(fold(fold_set<float>({{A.lUa[0], BC_U}, {A.lUa[1], BC_V}, {A.lUa[2], BC_W}}), g, s));
     }

@@ -1143,7 +1143,7 @@ cudaError_t ck_copy(f8_ctx *c, int slot, bool save) {
     // Phi is the SOR variant's start value of the next solve, so a recomputed
     // segment repeats the SOR iterates exactly
     double *f[12] = {d.U, d.V, d.W, d.P, d.C, d.Ax0, d.Ay0, d.Az0, d.Tx0, d.Ty0, d.Tz0, d.Phi};
-    const size_t n[12] = {cs, cs, cs, cs, 6 * cs, ni, ni, ni, ni, ni, ni, cs};
+    const size_t n[12] = {cs, cs, cs, cs, (size_t)d.ncomp * cs, ni, ni, ni, ni, ni, ni, cs};
     size_t off = 0;
     for (int q = 0; q < 12; ++q) {
         const size_t b = n[q] * sizeof(double);
@@ -1168,7 +1168,7 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
     o.ibm = ncyl > 0;
     o.poisson = c->poisson;
     o.sor_omega = c->phys.sor_omega; o.sor_eps = c->phys.sor_eps; o.sor_itrmax = c->phys.sor_itrmax;
-    if (!o.polymer) F8_CUDA_RET(cudaMemsetAsync(d.C, 0, 6 * hb, c->s));
+    if (!o.polymer) F8_CUDA_RET(cudaMemsetAsync(d.C, 0, d.ncomp * hb, c->s));
     auto cp = [&](void *dst, const void *src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->s);
     };
@@ -1176,7 +1176,7 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
         F8_CUDA_RET(cp(G.tU + rec * cs, d.U, hb));
         F8_CUDA_RET(cp(G.tV + rec * cs, d.V, hb));
         F8_CUDA_RET(cp(G.tW + rec * cs, d.W, hb));
-        if (rec == 0) F8_CUDA_RET(cp(G.tC, d.C, 6 * hb));
+        if (rec == 0) F8_CUDA_RET(cp(G.tC, d.C, d.ncomp * hb));
     }
     int sor = -1;
     if (rec >= 0) o.c_mid = G.tCm + (size_t)rec * 6 * cs;
@@ -1184,7 +1184,7 @@ cudaError_t grad_forward_step(f8_ctx *c, int step0, int s, int rec) {
     if (c->poisson == F8_POISSON_SOR && sor > c->phys.sor_itrmax) ++G.sor_capped;
     if (rec >= 0) {
         const size_t ng = 2 * (size_t)d.g.nx * d.g.nz;
-        F8_CUDA_RET(cp(G.tC + (size_t)(rec + 1) * 6 * cs, d.C, 6 * hb));
+        F8_CUDA_RET(cp(G.tC + (size_t)(rec + 1) * 6 * cs, d.C, d.ncomp * hb));
         F8_CUDA_RET(cp(G.tcodes + rec * ni, d.codes, ni));
         F8_CUDA_RET(cp(G.tcodes_g + rec * ng, d.codes_g, ng));
         const double *ua[3] = {d.Ua, d.Va, d.Wa}, *up[3] = {d.Up, d.Vp, d.Wp};
@@ -1475,8 +1475,9 @@ static int grad_impl(f8_ctx *c, int nsteps, int checkpoint_every, const double *
                      double *J, double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     if (!c || nsteps < 1 || checkpoint_every < 0) return F8_ERR_ARG;
     if (!c->loaded) return F8_ERR_STATE;
-    if (c->grid.dim != 3 || c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
+    if (c->phys.ibm_repeats != 1) return F8_ERR_UNSUPPORTED;
     if (c->precision == F8_MIXED) {
+        if (c->grid.dim != 3) return F8_ERR_UNSUPPORTED;
         if (c->poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
         return grad_mixed(c, nsteps, checkpoint_every, drag_w, seed, J, dJ_dparams, dJ_dstate, drag);
     }
@@ -1528,9 +1529,9 @@ static int grad_impl(f8_ctx *c, int nsteps, int checkpoint_every, const double *
             API_CUDA(c, take_interior(tmp, hd[q], d.g, (int)cs, c->s));
         }
         if (seed->c) {
-            API_CUDA(c, cudaMemcpyAsync(tmp, seed->c, 6 * cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
-            API_CUDA(c, aos_to_soa(tmp, A.lC2, 6, (int)cs, c->s));
-            API_CUDA(c, take_interior(A.lC2, A.lC, d.g, (int)(6 * cs), c->s));
+            API_CUDA(c, cudaMemcpyAsync(tmp, seed->c, d.ncomp * cs * sizeof(double), cudaMemcpyHostToDevice, c->s));
+            API_CUDA(c, aos_to_soa(tmp, A.lC2, d.ncomp, (int)cs, c->s));
+            API_CUDA(c, take_interior(A.lC2, A.lC, d.g, (int)(d.ncomp * cs), c->s));
         }
         const double *is[6] = {seed->ax0, seed->ay0, seed->az0, seed->tx0, seed->ty0, seed->tz0};
         double *id[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};
@@ -1557,7 +1558,8 @@ static int grad_impl(f8_ctx *c, int nsteps, int checkpoint_every, const double *
         for (int s = s1 - 1; s >= s0; --s) {
             const TapeStep t = tape_step(c, s - s0);
             const bool ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
-            API_CUDA(c, step_fp64_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
+            if (d.g.dim == 3) API_CUDA(c, step_fp64_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
+            else API_CUDA(c, step_fp64_adjoint2(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
         }
     }
     if (nseg > 1) API_CUDA(c, ck_copy(c, nseg - 1, false));
@@ -1581,8 +1583,8 @@ static int grad_impl(f8_ctx *c, int nsteps, int checkpoint_every, const double *
         API_CUDA(c, get(dJ_dstate->w, A.lW, cs));
         API_CUDA(c, get(dJ_dstate->p, A.lP, cs));
         if (dJ_dstate->c) {
-            API_CUDA(c, soa_to_aos(A.lC, c->scratch_aos, 6, (int)cs, c->s));
-            API_CUDA(c, get(dJ_dstate->c, c->scratch_aos, 6 * cs));
+            API_CUDA(c, soa_to_aos(A.lC, c->scratch_aos, d.ncomp, (int)cs, c->s));
+            API_CUDA(c, get(dJ_dstate->c, c->scratch_aos, d.ncomp * cs));
         }
         double *od[6] = {dJ_dstate->ax0, dJ_dstate->ay0, dJ_dstate->az0, dJ_dstate->tx0, dJ_dstate->ty0, dJ_dstate->tz0};
         const double *os[6] = {A.lA0[0], A.lA0[1], A.lA0[2], A.lT0[0], A.lT0[1], A.lT0[2]};

@@ -208,6 +208,8 @@ struct TapeStep {
 };
 cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const double *drag_w, bool ab2_first,
                               bool polymer, cudaStream_t s);
+cudaError_t step_fp64_adjoint2(Dev &d, AdjState &A, const TapeStep &t, const double *drag_w, bool ab2_first,
+                              bool polymer, cudaStream_t s);
 cudaError_t adjoint_fold_state(AdjState &A, const Dev &d, cudaStream_t s);
 // dst[q] = src[q] on interior cells of n / cs stacked halo fields, 0 on halo cells
 cudaError_t take_interior(const double *src, double *dst, const Geo &g, int n, cudaStream_t s);

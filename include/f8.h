@@ -199,9 +199,9 @@ int f8_store(f8_ctx *ctx, f8_fields *out);
 /* Advance nsteps steps like f8_step and return the gradient of
  *     J = sum_{n,l,c} drag_weights[n][l][c] * drag[n][l][c]
  *       + <seed, state after the nsteps> (interior values)
- * from the discrete adjoint of the FP64 3D step.  The reference has no
- * adjoint; the forward it differentiates is the step of f8_step
- * (fenep.f90:2477-2527 with the IBM of fenep_mpi.f90:1794-1929).
+ * from the discrete adjoint of the step.  The reference has no adjoint; the
+ * forward it differentiates is the step of f8_step (fenep.f90:2477-2527 with
+ * the IBM of fenep_mpi.f90:1794-1929; 2D fenep_2d.f90:1912-1966).
  *   drag_weights : nsteps * ncyl * 3 doubles, or NULL for the time-averaged
  *                  total drag J = (1/nsteps) sum_n sum_l drag_x[n][l];
  *   seed         : adjoint of the final state (interior cells of u, v, w, p,
@@ -218,10 +218,12 @@ int f8_store(f8_ctx *ctx, f8_fields *out);
  * segment with its intermediate fields stored, then runs the adjoint of its
  * steps.  The selection of the SPD face candidates is held fixed (its
  * derivative is zero almost everywhere); the Newton solution is
- * differentiated through the implicit-function theorem.  Requires a 3D
- * context (F8_FP64 or F8_MIXED) with the FFT Poisson solver and one forcing
- * iteration per step (F8_ERR_UNSUPPORTED otherwise).  The context's state
- * advances by nsteps as with f8_step. */
+ * differentiated through the implicit-function theorem.  Requires one
+ * forcing iteration per step and either an F8_FP64 context (2D or 3D, FFT or
+ * SOR Poisson solver; the SOR variant's adjoint solve is the same SOR to the
+ * same tolerance) or a 3D F8_MIXED context with the FFT solver
+ * (F8_ERR_UNSUPPORTED otherwise).  The context's state advances by nsteps as
+ * with f8_step. */
 int f8_grad(f8_ctx *ctx, int nsteps, int checkpoint_every, const double *drag_weights,
             const f8_fields *seed, double *J, double *dJ_dparams, f8_fields *dJ_dstate, double *drag);
 
