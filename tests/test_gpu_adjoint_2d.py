@@ -10,7 +10,8 @@ the cylinder off the grid lines; the FENE-P step and the Newtonian one
 against central differences (relative step 1e-4, 1e-6 for the centres) within
 1e-4; the adjoint of
 the initial state along a random direction against the directional central
-difference; checkpoint intervals agree and the state left equals f8_step's.
+difference; checkpoint intervals agree and the state left equals f8_step's;
+the SOR variant's gradient equals the FFT one at a tight SOR tolerance.
 """
 from __future__ import annotations
 
@@ -136,3 +137,19 @@ def test_2d_checkpoints_agree_and_state_advances(gpu, oracle):
             assert np.array_equal(final[name], out[name]), name
         for q, (a, b) in enumerate(zip(dp, res[0][1])):
             assert abs(a - b) <= 1e-9 * abs(b) + 1e-12, (q, a, b)
+
+
+def test_2d_sor_gradient_matches_fft_gradient(gpu, oracle):
+    """The SOR variant's adjoint in 2D: at a tight SOR tolerance the gradient
+    equals the FFT + tridiagonal one (the same discrete Laplacian)."""
+    w, st, step0 = case2d("channel", oracle)
+    w = replace(w, phys=replace(w.phys, sor_eps=1e-13, sor_itrmax=20000))
+    out = []
+    for poisson in (abi.F8_POISSON_SOR, abi.F8_POISSON_FFT):
+        with Solver(gpu, w.grid, w.phys, w.cyls, poisson=poisson) as s:
+            s.load(st, step0)
+            status, J, dp, _, _ = s.grad(3, 0)
+        assert status == abi.F8_OK
+        out.append(dp)
+    for q, (a, b) in enumerate(zip(*out)):
+        assert abs(a - b) <= 1e-7 * abs(b) + 1e-11, (q, a, b)
