@@ -974,15 +974,47 @@ __global__ void __launch_bounds__(96) k_ibm_interp_f(IbmArgsF a, Geo g) {
         const float *wx = a.wx[comp] + 3 * m, *wy = a.wy[comp] + 3 * m;
         const int k = n - 1 + dk;
         const float wz = a.wz[comp][dk];
+        // a stencil inside the interior columns and rows (no x wrap, no wall
+        // rule) reads its 9 points at fixed offsets from one base index; the
+        // values and their order of summation are those of ua_at / ustar_at
+        const bool inner = i0 >= 1 && i0 + 2 <= g.nx && j0 >= 1 && j0 + 2 <= g.ny &&
+                           !(g.walls && comp == 1 && j0 + 2 == g.ny);
+        if (inner) {
+            const int kk = wrapz(g, k);
+            const int hb = hix(g, i0, j0, k);
+            const float *Uh = a.Uh[comp], *Ul = a.Ul[comp];
+            const float *X = a.mode ? a.D[comp] : a.Qc[comp];
+            const int xb = a.mode ? hix(g, i0, j0, kk) : qix(g, i0, j0, kk);
+            const int xs = a.mode ? g.sx : g.nx;
+            float uh[9], ul[9], xv[9];
 #pragma unroll
-        for (int dj = 0; dj < 3; ++dj)
+            for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
-            for (int di = 0; di < 3; ++di) {
-                const float w = wx[di] * wy[dj] * wz;
-                const df uv = a.mode ? ustar_at(g, a.Uh[comp], a.Ul[comp], a.D[comp], comp, i0 + di, j0 + dj, k, a.uw2)
-                                     : ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2);
-                ub = df_add(ub, df_mul_f(uv, w));
-            }
+                for (int di = 0; di < 3; ++di) {
+                    const int h = hb + di + g.sx * dj;
+                    uh[3 * dj + di] = Uh[h];
+                    ul[3 * dj + di] = Ul[h];
+                    xv[3 * dj + di] = X[xb + di + xs * dj];
+                }
+#pragma unroll
+            for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+                for (int di = 0; di < 3; ++di) {
+                    const float w = wx[di] * wy[dj] * wz;
+                    const int q = 3 * dj + di;
+                    ub = df_add(ub, df_mul_f(df_add_f(df{uh[q], ul[q]}, xv[q]), w));
+                }
+        } else {
+#pragma unroll
+            for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+                for (int di = 0; di < 3; ++di) {
+                    const float w = wx[di] * wy[dj] * wz;
+                    const df uv = a.mode ? ustar_at(g, a.Uh[comp], a.Ul[comp], a.D[comp], comp, i0 + di, j0 + dj, k, a.uw2)
+                                         : ua_at(g, a.Uh[comp], a.Ul[comp], a.Qc[comp], comp, i0 + di, j0 + dj, k, a.uw2);
+                    ub = df_add(ub, df_mul_f(uv, w));
+                }
+        }
     }
     part[dk][threadIdx.x] = ub;
     __syncthreads();
