@@ -1031,15 +1031,17 @@ __device__ inline float spread_at_f(const IbmArgsF &a, const Geo &g, int comp, i
     const int col = ie + g.sx * je;
     const int b = a.off[comp][col], e = a.off[comp][col + 1];
     if (b == e) return 0.0f;
+    // each list entry (marker, x y weight) is read once for the (up to) three
+    // marker planes whose z stencil covers plane ke
     float acc = 0.0f;
     const int nlo = max(ke - 1, 1), nhi = min(ke + 1, g.nz);
-    for (int n = nlo; n <= nhi; ++n) {
-        const float wz = a.wz[comp][ke - n + 1];
-        for (int q = b; q < e; ++q) {
-            const int m = a.idx[comp][q];
-            const float w = a.cw[comp][q] * wz;
-            acc = fmaf((float)a.Fc[comp][m + (size_t)a.nm * (n - 1)], w, acc);
-        }
+    const double *Fc = a.Fc[comp];
+    const size_t nm = (size_t)a.nm;
+    for (int q = b; q < e; ++q) {
+        const int m = a.idx[comp][q];
+        const float cw = a.cw[comp][q];
+        for (int n = nlo; n <= nhi; ++n)
+            acc = fmaf((float)Fc[m + nm * (n - 1)], cw * a.wz[comp][ke - n + 1], acc);
     }
     return acc;
 }
