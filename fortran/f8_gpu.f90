@@ -29,6 +29,7 @@ module f8_gpu
     integer(c_int), parameter :: F8_POISSON_FFT = 0, F8_POISSON_SOR = 1
     integer(c_int), parameter :: F8_BC_PERIODIC = 0, F8_BC_WALLS = 1, F8_BC_WALLS_Z = 2
     integer(c_int), parameter :: F8_IBM_CELL_VOLUME = 0, F8_IBM_ARC_VOLUME = 1
+    integer(c_int), parameter :: F8_EIGEN_VIETA = 0, F8_EIGEN_CARDANO = 1, F8_EIGEN_SYLVESTER = 2, F8_EIGEN_SYMMETRIC = 3
 
     type, bind(C) :: f8_grid
         integer(c_int) :: dim, nx, ny, nz
@@ -46,6 +47,7 @@ module f8_gpu
         integer(c_int) :: ab2_start
         integer(c_int) :: ibm_volume     ! 0: dX*dY*dZ (fenep), 1: pi*DC/NL*dX*dX (smac.f90:1129)
         integer(c_int) :: ibm_repeats    ! NS of smac.f90:20 (1 in fenep)
+        integer(c_int) :: eigen_test     ! F8_EIGEN_*: the reference's eigen_method (fenep.f90:21)
     end type f8_phys
 
     type, bind(C) :: f8_cyl

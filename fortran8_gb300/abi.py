@@ -29,6 +29,10 @@ F8_BC_WALLS = 1
 F8_BC_WALLS_Z = 2
 F8_IBM_CELL_VOLUME = 0
 F8_IBM_ARC_VOLUME = 1
+F8_EIGEN_VIETA = 0
+F8_EIGEN_CARDANO = 1
+F8_EIGEN_SYLVESTER = 2
+F8_EIGEN_SYMMETRIC = 3
 
 _dp = C.POINTER(C.c_double)
 
@@ -44,7 +48,8 @@ class Phys(C.Structure):
                 ("lp2", C.c_double), ("dt", C.c_double),
                 ("newton_dc", C.c_double), ("newton_eps", C.c_double), ("newton_itrmax", C.c_int),
                 ("sor_omega", C.c_double), ("sor_eps", C.c_double), ("sor_itrmax", C.c_int),
-                ("ab2_start", C.c_int), ("ibm_volume", C.c_int), ("ibm_repeats", C.c_int)]
+                ("ab2_start", C.c_int), ("ibm_volume", C.c_int), ("ibm_repeats", C.c_int),
+                ("eigen_test", C.c_int)]
 
 
 class Cyl(C.Structure):

@@ -279,6 +279,8 @@ int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, in
     if (ph->newton_itrmax < 1 || ph->sor_itrmax < 1) return F8_ERR_ARG;
     if (ncyl < 0 || (ncyl > 0 && !cy)) return F8_ERR_ARG;
     if (ph->ibm_repeats < 1 || ph->ibm_repeats > 64) return F8_ERR_ARG;
+    if (ph->eigen_test < F8_EIGEN_VIETA || ph->eigen_test > F8_EIGEN_SYMMETRIC) return F8_ERR_ARG;
+    if (ph->eigen_test != F8_EIGEN_VIETA && (g->dim != 3 || prec != F8_FP64)) return F8_ERR_UNSUPPORTED;
     if (ph->ibm_volume != F8_IBM_CELL_VOLUME && ph->ibm_volume != F8_IBM_ARC_VOLUME) return F8_ERR_ARG;
     if (ph->ibm_volume == F8_IBM_ARC_VOLUME) {
         // the arc element of a surface ring (smac.f90:1128-1129), 3D
@@ -338,7 +340,7 @@ int setup(f8_ctx *c) {
     g.dx = G.lx / G.nx; g.dy = G.ly / G.ny; g.dz = G.dim == 3 ? G.lz / G.nz : g.dx;
     g.dt = c->phys.dt; g.uwall = G.uwall;
     d.ph = Phys{c->phys.re, c->phys.wi, c->phys.beta, c->phys.lp2, c->phys.dt,
-                c->phys.newton_dc, c->phys.newton_eps, c->phys.newton_itrmax};
+                c->phys.newton_dc, c->phys.newton_eps, c->phys.newton_itrmax, c->phys.eigen_test};
     d.ibm_repeats = c->phys.ibm_repeats;
     d.ncomp = G.dim == 3 ? 6 : 3;
     d.cs = g.sx * g.sy * g.sz;

@@ -49,6 +49,7 @@ struct Phys {
     double re, wi, beta, lp2, dt;
     double newton_dc, newton_eps;
     int newton_itrmax;
+    int eigen_test;      // f8_eigen_test (3D FP64 step)
 };
 
 // Boundary-condition kinds of the halo fill kernel.

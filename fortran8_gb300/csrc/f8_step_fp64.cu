@@ -158,7 +158,70 @@ __device__ inline double face_n(int idx, double cm, double c0, double cp) {
     }
 }
 
-__device__ inline int select3(const double *cm, const double *c0, const double *cp) {
+// The reference's other eigen tests (its compile-time eigen_method,
+// fenep.f90:187-212).  Cardano (fenep.f90:384-423): the three roots from the
+// complex cube roots of u3 = -q/2 + i sqrt(-t) and its conjugate; with
+// u3 = rho e^(i th) the principal cube roots give 2 rho^(1/3) cos(th/3 + 2 pi
+// k/3) - a2/3, k = 0, 1, -1.  The reference sets -1 when t >= 0 (and then
+// reads u3, v3 unset; the evident intent, -1, is kept here).
+__device__ inline void cardano(const double *a, double *e) {
+    double a2 = -(a[0] + a[3] + a[5]);
+    double a1 = a[0] * a[3] + a[3] * a[5] + a[5] * a[0] - a[4] * a[4] - a[2] * a[2] - a[1] * a[1];
+    double a0 = -(a[0] * a[3] * a[5] + a[1] * a[4] * a[2] + a[1] * a[4] * a[2] - a[0] * a[4] * a[4]
+                  - a[1] * a[1] * a[5] - a[2] * a[3] * a[2]);
+    double p = a1 - (a2 * a2) / 3.0;
+    double q = a0 - a1 * a2 / 3.0 + 2.0 * (a2 * a2 * a2) / 27.0;
+    double qh = q / 2.0, p3 = p / 3.0;
+    double t = qh * qh + p3 * p3 * p3;
+    if (t >= 0.0) { e[0] = e[1] = e[2] = -1.0; return; }
+    const double rho = sqrt(qh * qh - t), th = atan2(sqrt(-t), -qh);
+    const double r3 = cbrt(rho), two_pi_3 = 2.0 * PI_D / 3.0;
+    e[0] = 2.0 * r3 * cos(th / 3.0) - a2 / 3.0;
+    e[1] = 2.0 * r3 * cos(th / 3.0 + two_pi_3) - a2 / 3.0;
+    e[2] = 2.0 * r3 * cos(th / 3.0 - two_pi_3) - a2 / 3.0;
+}
+
+// Sylvester's criterion (fenep.f90:446-461): 1 for positive leading minors, else -1
+__device__ inline double sylvester(const double *a) {
+    if (a[0] > 0 && a[3] > 0 && a[5] > 0)
+        if (a[0] * a[3] - a[1] * a[1] > 0)
+            if (a[0] * a[3] * a[5] + a[1] * a[4] * a[2] + a[1] * a[4] * a[2] - a[0] * a[4] * a[4]
+                - a[1] * a[1] * a[5] - a[2] * a[3] * a[2] > 0)
+                return 1.0;
+    return -1.0;
+}
+
+// The smallest eigenvalue of the symmetric matrix, repeated roots included
+// (the reference's dsyev, fenep.f90:197-212): the trigonometric form of the
+// deviator B = A - m I, p2 = |B|^2/6, r = det(B)/2 / p2^(3/2) clamped to
+// [-1, 1] (Smith, Comm. ACM 4 (1961) 168).
+__device__ inline double symmetric_min(const double *a) {
+    const double m = (a[0] + a[3] + a[5]) / 3.0;
+    const double b0 = a[0] - m, b3 = a[3] - m, b5 = a[5] - m;
+    const double p2 = (b0 * b0 + b3 * b3 + b5 * b5 + 2.0 * (a[1] * a[1] + a[2] * a[2] + a[4] * a[4])) / 6.0;
+    if (!(p2 > 0.0)) return p2 == 0.0 ? m : p2;   // p2 NaN: NaN
+    const double det = b0 * (b3 * b5 - a[4] * a[4]) - a[1] * (a[1] * b5 - a[4] * a[2]) + a[2] * (a[1] * a[4] - b3 * a[2]);
+    double r = det / 2.0 / (p2 * sqrt(p2));
+    r = r < -1.0 ? -1.0 : (r > 1.0 ? 1.0 : r);
+    return m + 2.0 * sqrt(p2) * cos(acos(r) / 3.0 + 2.0 * PI_D / 3.0);
+}
+
+// minval over the values of one candidate's two faces (fenep.f90:186-241)
+__device__ inline double face_test(int method, const double *pt, const double *nt) {
+    if (method == 1) {
+        double e[6];
+        cardano(pt, e);
+        cardano(nt, e + 3);
+        double v = e[0];
+        for (int q = 1; q < 6; ++q) v = nanmin2(v, e[q]);
+        return v;
+    }
+    if (method == 2) return nanmin2(sylvester(pt), sylvester(nt));
+    if (method == 3) return nanmin2(symmetric_min(pt), symmetric_min(nt));
+    return nanmin2(vieta(pt), vieta(nt));
+}
+
+__device__ inline int select3(const double *cm, const double *c0, const double *cp, int method) {
     double minlist[4];
     for (int l = 1; l <= 3; ++l) {
         double pt[6], nt[6];
@@ -166,7 +229,7 @@ __device__ inline int select3(const double *cm, const double *c0, const double *
             pt[m] = face_p(l, cm[m], c0[m], cp[m]);
             nt[m] = face_n(l, cm[m], c0[m], cp[m]);
         }
-        minlist[l - 1] = nanmin2(vieta(pt), vieta(nt));
+        minlist[l - 1] = face_test(method, pt, nt);
     }
     minlist[3] = 0.0;
     return maxloc4(minlist);
@@ -184,7 +247,7 @@ __device__ inline int code_at(const uint8_t *codes, const uint8_t *codes_g, cons
 }
 
 __global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict__ C, uint8_t *__restrict__ codes,
-                                                        uint8_t *__restrict__ codes_g, Geo g, int cs) {
+                                                        uint8_t *__restrict__ codes_g, Geo g, int cs, int method) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
@@ -204,7 +267,7 @@ __global__ void __launch_bounds__(128) k_polymer_codes3(const double *__restrict
                 cp[m] = C[(size_t)m * cs + h + off[d]];
             }
         }
-        code |= (select3(cm, c0, cp) - 1) << (2 * d);
+        code |= (select3(cm, c0, cp, method) - 1) << (2 * d);
     }
     if (j >= 1 && j <= g.ny) codes[qix(g, i, j, k)] = (uint8_t)code;
     else codes_g[gcix(g, i, j, k)] = (uint8_t)code;
@@ -1296,7 +1359,7 @@ cudaError_t step_fp64(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor_
         dim3 blk(32, 4);
         // the rows of the polymer update (with walls the ghost rows too)
         dim3 grd((g.nx + blk.x - 1) / blk.x, (prows(g) + blk.y - 1) / blk.y, g.nz);
-        if (d3) { k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, d.codes_g, g, d.cs); count_launch(); }
+        if (d3) { k_polymer_codes3<<<grd, blk, 0, s>>>(d.C, d.codes, d.codes_g, g, d.cs, d.ph.eigen_test); count_launch(); }
         else { k_polymer_codes2<<<grd, blk, 0, s>>>(d.C, d.codes, d.codes_g, g, d.cs); count_launch(); }
         mark(1);
         if (d3) { k_polymer_update3<<<grd, blk, 0, s>>>(d.C, d.Cn, d.fpet, d.codes, d.codes_g, d.U, d.V, d.W, g, d.ph, d.cs, d.cnt); count_launch(); }

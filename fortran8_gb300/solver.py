@@ -75,11 +75,12 @@ class PhysSpec:
     ab2_start: int = 1
     ibm_volume: int = abi.F8_IBM_CELL_VOLUME
     ibm_repeats: int = 1
+    eigen_test: int = abi.F8_EIGEN_VIETA
 
     def to_c(self) -> abi.Phys:
         return abi.Phys(self.re, self.wi, self.beta, self.lp2, self.dt, self.newton_dc,
                         self.newton_eps, self.newton_itrmax, self.sor_omega, self.sor_eps,
-                        self.sor_itrmax, self.ab2_start, self.ibm_volume, self.ibm_repeats)
+                        self.sor_itrmax, self.ab2_start, self.ibm_volume, self.ibm_repeats, self.eigen_test)
 
 
 @dataclass

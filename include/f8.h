@@ -110,7 +110,25 @@ typedef struct f8_phys {
     int ibm_repeats;        /* direct-forcing iterations per step, NS of smac.f90:20,
                                1607-1611 (interpolate from the last Helmholtz solution,
                                add to the marker force, spread, solve again); 1 = fenep */
+    int eigen_test;         /* enum f8_eigen_test: the SPD test of the face candidates
+                               (the reference's compile-time eigen_method,
+                               fenep.f90:21, 187-212); 3D FP64 only, F8_EIGEN_VIETA
+                               elsewhere                                              */
 } f8_phys;
+
+enum f8_eigen_test {
+    F8_EIGEN_VIETA = 0,      /* eigen_method 3, the default: smallest eigenvalue by the
+                                trigonometric cubic formula, -100 on repeated roots
+                                (Vieta, fenep.f90:425-444)                            */
+    F8_EIGEN_CARDANO = 1,    /* eigen_method 0: the three eigenvalues by Cardano's
+                                complex cube roots, -1 when the discriminant is not
+                                negative (Cardano, fenep.f90:384-423)                 */
+    F8_EIGEN_SYLVESTER = 2,  /* eigen_method 1: +1 when Sylvester's leading minors are
+                                positive, else -1 (Sylvester, fenep.f90:446-461)      */
+    F8_EIGEN_SYMMETRIC = 3   /* eigen_method 2: the three eigenvalues of the symmetric
+                                matrix, repeated roots included (LAPACK dsyev in the
+                                reference, fenep.f90:197-212; here the closed form)   */
+};
 
 enum f8_ibm_volume {
     F8_IBM_CELL_VOLUME = 0,

@@ -27,6 +27,7 @@
 // Build: oracle/Makefile (g++ -O2 -ffp-contract=off -fopenmp -shared).
 
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <cstdint>
@@ -221,6 +222,91 @@ inline double nanmin2(double a, double b) {
     return b < a ? b : a;
 }
 
+// fenep.f90:384-423 (eigen_method == 0): the three roots of the cubic from
+// the complex cube roots of u3 = -q/2 + i sqrt(-t) and of its conjugate v3,
+// e_k = w_k u3^(1/3) + conj(w_k) v3^(1/3) - a2/3 with w_k the cube roots of
+// unity (principal branch, as Fortran's complex power).  For t >= 0 the
+// reference sets -1 and then reads u3, v3 unset; -1 is kept here.
+inline void cardano(const double *a, double *e) {
+    double a2 = -(a[0] + a[3] + a[5]);
+    double a1 = a[0] * a[3] + a[3] * a[5] + a[5] * a[0] - a[4] * a[4] - a[2] * a[2] - a[1] * a[1];
+    double a0 = -(a[0] * a[3] * a[5] + a[1] * a[4] * a[2] + a[1] * a[4] * a[2] - a[0] * a[4] * a[4]
+                  - a[1] * a[1] * a[5] - a[2] * a[3] * a[2]);
+    double p = a1 - (a2 * a2) / 3.0;
+    double q = a0 - a1 * a2 / 3.0 + 2.0 * (a2 * a2 * a2) / 27.0;
+    double qh = q / 2.0, p3 = p / 3.0;
+    double t = qh * qh + p3 * p3 * p3;
+    if (t >= 0.0) { e[0] = e[1] = e[2] = -1.0; return; }
+    const std::complex<double> u3(-qh, std::sqrt(-t)), v3(-qh, -std::sqrt(-t));
+    const std::complex<double> cu = std::pow(u3, 1.0 / 3.0), cv = std::pow(v3, 1.0 / 3.0);
+    const std::complex<double> w1(-0.5, std::sqrt(3.0) / 2.0), w2(-0.5, -std::sqrt(3.0) / 2.0);
+    e[0] = (cu + cv).real() - a2 / 3.0;
+    e[1] = (w1 * cu + w2 * cv).real() - a2 / 3.0;
+    e[2] = (w2 * cu + w1 * cv).real() - a2 / 3.0;
+}
+
+// fenep.f90:446-461 (eigen_method == 1): 1 when the leading minors are positive
+inline double sylvester(const double *a) {
+    if (a[0] > 0 && a[3] > 0 && a[5] > 0)
+        if (a[0] * a[3] - a[1] * a[1] > 0)
+            if (a[0] * a[3] * a[5] + a[1] * a[4] * a[2] + a[1] * a[4] * a[2] - a[0] * a[4] * a[4]
+                - a[1] * a[1] * a[5] - a[2] * a[3] * a[2] > 0)
+                return 1.0;
+    return -1.0;
+}
+
+// eigen_method == 2 (LAPACK dsyev, fenep.f90:197-212): the three eigenvalues
+// of the symmetric matrix by Jacobi rotations (the oracle's own method; the
+// library evaluates the closed form), ascending
+inline void symmetric_eig(const double *a, double *e) {
+    double A[3][3] = {{a[0], a[1], a[2]}, {a[1], a[3], a[4]}, {a[2], a[4], a[5]}};
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        if (off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (A[p][q] == 0.0) continue;
+                const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                const double tt = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double cc = 1.0 / std::sqrt(tt * tt + 1.0), ss = tt * cc;
+                for (int k = 0; k < 3; ++k) {   // columns p, q
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = cc * akp - ss * akq;
+                    A[k][q] = ss * akp + cc * akq;
+                }
+                for (int k = 0; k < 3; ++k) {   // rows p, q
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = cc * apk - ss * aqk;
+                    A[q][k] = ss * apk + cc * aqk;
+                }
+            }
+    }
+    e[0] = A[0][0]; e[1] = A[1][1]; e[2] = A[2][2];
+    std::sort(e, e + 3);
+}
+
+// minval over the values of one candidate's two faces (fenep.f90:186-241)
+inline double face_test(int method, const double *pt, const double *nt) {
+    if (method == F8_EIGEN_CARDANO) {
+        double e[6];
+        cardano(pt, e);
+        cardano(nt, e + 3);
+        double v = e[0];
+        for (int q = 1; q < 6; ++q) v = nanmin2(v, e[q]);
+        return v;
+    }
+    if (method == F8_EIGEN_SYLVESTER) return nanmin2(sylvester(pt), sylvester(nt));
+    if (method == F8_EIGEN_SYMMETRIC) {
+        double e[6];
+        symmetric_eig(pt, e);
+        symmetric_eig(nt, e + 3);
+        double v = e[0];
+        for (int q = 1; q < 6; ++q) v = nanmin2(v, e[q]);
+        return v;
+    }
+    return nanmin2(vieta(pt), vieta(nt));
+}
+
 // Fortran maxloc(minlist(1:4), 1): first position of the largest non-NaN value.
 inline int maxloc4(const double *m) {
     int idx = 0; double best = 0; bool found = false;
@@ -245,10 +331,10 @@ inline void candidates3(const double *cm, const double *c0, const double *cp, do
 
 // One direction of CpxCnx (fenep.f90:169-242): fills the two face values of
 // cell (i,j,k) in direction d.  Returns the chosen index (1..4).
-int reconstruct3(const double *cm, const double *c0, const double *cp, double *fp, double *fn) {
+int reconstruct3(const double *cm, const double *c0, const double *cp, double *fp, double *fn, int method) {
     double pt[3][6], nt[3][6], minlist[4];
     candidates3(cm, c0, cp, pt, nt);
-    for (int l = 0; l < 3; ++l) minlist[l] = nanmin2(vieta(pt[l]), vieta(nt[l]));
+    for (int l = 0; l < 3; ++l) minlist[l] = face_test(method, pt[l], nt[l]);
     minlist[3] = 0.0;
     int index = maxloc4(minlist);
     if (index == 4) {
@@ -303,11 +389,11 @@ void polymer_faces3(OCtx &c) {
             for (int i = 1; i <= NX; ++i) {
                 const double *c0 = cval(c, C, 6, i, j, k);
                 const int ix = reconstruct3(cval(c, C, 6, i - 1, j, k), c0, cval(c, C, 6, i + 1, j, k),
-                                            &c.Cpx[F.x(i - 1, j, k)], &c.Cnx[F.x(i, j, k)]);
+                                            &c.Cpx[F.x(i - 1, j, k)], &c.Cnx[F.x(i, j, k)], c.ph.eigen_test);
                 const int iy = reconstruct3(cval(c, C, 6, i, j - 1, k), c0, cval(c, C, 6, i, j + 1, k),
-                                            &c.Cpy[F.y(i, j - 1, k)], &c.Cny[F.y(i, j, k)]);
+                                            &c.Cpy[F.y(i, j - 1, k)], &c.Cny[F.y(i, j, k)], c.ph.eigen_test);
                 const int iz = reconstruct3(cval(c, C, 6, i, j, k - 1), c0, cval(c, C, 6, i, j, k + 1),
-                                            &c.Cpz[F.z(i, j, k - 1)], &c.Cnz[F.z(i, j, k)]);
+                                            &c.Cpz[F.z(i, j, k - 1)], &c.Cnz[F.z(i, j, k)], c.ph.eigen_test);
                 c.codes[(size_t)(i - 1) + (size_t)NX * ((size_t)(j - jlo) + (size_t)F.nr * (k - 1))] =
                     (unsigned char)((ix - 1) | ((iy - 1) << 2) | ((iz - 1) << 4));
             }
@@ -1503,6 +1589,8 @@ int validate(const f8_grid *g, const f8_phys *ph, int ncyl, const f8_cyl *cy, in
     if (ncyl < 0 || (ncyl > 0 && !cy)) return F8_ERR_ARG;
     if (ph->ibm_repeats < 1 || ph->ibm_repeats > 64) return F8_ERR_ARG;
     if (ph->ibm_volume != F8_IBM_CELL_VOLUME && ph->ibm_volume != F8_IBM_ARC_VOLUME) return F8_ERR_ARG;
+    if (ph->eigen_test < F8_EIGEN_VIETA || ph->eigen_test > F8_EIGEN_SYMMETRIC) return F8_ERR_ARG;
+    if (ph->eigen_test != F8_EIGEN_VIETA && g->dim != 3) return F8_ERR_UNSUPPORTED;
     if (ph->ibm_volume == F8_IBM_ARC_VOLUME) {
         // the arc element of a surface ring (smac.f90:1128-1129), 3D
         if (g->dim != 3) return F8_ERR_UNSUPPORTED;
@@ -2005,6 +2093,8 @@ int f8o_set_sor_order(f8_ctx *ctx, int order) {
 }
 
 double f8o_vieta(const double *a) { return vieta(a); }
+// the value the eigen test gives one symmetric matrix (face_test on a pair of equal faces)
+double f8o_eigen_test(int method, const double *a) { return face_test(method, a, a); }
 void f8o_eig2(const double *a, double *out) { eig2(a, out[0], out[1]); }
 double f8o_roma(double r) { return roma(r); }
 
