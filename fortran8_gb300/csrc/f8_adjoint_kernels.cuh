@@ -587,14 +587,37 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
         const T dt = kc.dt;
         const T h2 = T(0.5), h15 = T(1.5);
         const int o = qix(g, i, j, k), h = hix(g, i, j, k);
+        const int sx = g.sx, sxy = g.sx * g.sy;
         const size_t cs = (size_t)a.cs;
         const T *F[3] = {a.U, a.V, a.W};
+        // every load of the three components precedes the first store: the
+        // stores may alias the inputs as far as the compiler knows, so loads
+        // after a store would each wait for their own round trip
+        T lq[3], lu0[3], la0[3], lt0[3], xp[3][7], xf[3][7];
+        auto load7 = [&](const T *X, T (&x)[7]) {
+            x[0] = X[h];
+            x[1] = X[h - 1]; x[2] = X[h + 1];
+            x[3] = X[h - sx]; x[4] = X[h + sx];
+            x[5] = X[h - sxy]; x[6] = X[h + sxy];
+        };
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const T lq = a.lQ[c][h];
-            const T lua = lq + a.lUa[c][h];
-            T lA = h15 * dt * lua + a.lA0[c][o];
-            T lT = h2 * dt * lua + a.lT0[c][o];
+            lq[c] = a.lQ[c][h];
+            lu0[c] = a.lUa[c][h];
+            la0[c] = a.lA0[c][o];
+            lt0[c] = a.lT0[c][o];
+            load7(a.Up[c], xp[c]);
+            load7(F[c], xf[c]);
+        }
+        auto lap = [&](const T (&x)[7]) {
+            return (x[1] - 2 * x[0] + x[2]) * kc.id2[0] + (x[3] - 2 * x[0] + x[4]) * kc.id2[1]
+                 + (x[5] - 2 * x[0] + x[6]) * kc.id2[2];
+        };
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T lua = lq[c] + lu0[c];
+            T lA = h15 * dt * lua + la0[c];
+            T lT = h2 * dt * lua + lt0[c];
             if (a.ab2_first) {
                 lA += -h2 * dt * lua;
                 lT += h2 * dt * lua;
@@ -604,20 +627,14 @@ __global__ void __launch_bounds__(256) k_momadj_src(MomAdjArgs<T> a, T *src, Geo
                 a.lA0[c][o] = -h2 * dt * lua;
                 a.lT0[c][o] = h2 * dt * lua;
             }
-            const T lB = dt * lua - h2 * dt * lq;
+            const T lB = dt * lua - h2 * dt * lq[c];
             src[(size_t)(0 + c) * cs + h] = lua;
             src[(size_t)(3 + c) * cs + h] = -lA;
             src[(size_t)(6 + c) * cs + h] = a.vis * lB;
             src[(size_t)(9 + c) * cs + h] = a.polymer ? a.coef_t * lT : T(0);
-            auto lap = [&](const T *X) {
-                const T x0 = X[h];
-                return (X[hix(g, i - 1, j, k)] - 2 * x0 + X[hix(g, i + 1, j, k)]) * kc.id2[0]
-                     + (X[hix(g, i, j - 1, k)] - 2 * x0 + X[hix(g, i, j + 1, k)]) * kc.id2[1]
-                     + (X[hix(g, i, j, k - 1)] - 2 * x0 + X[hix(g, i, j, k + 1)]) * kc.id2[2];
-            };
             // Helmholtz coefficient dt beta/(2 Re) and viscous coefficient beta/Re
-            if (lq != T(0)) gb += a.c_helm * lq * lap(a.Up[c]);
-            gb += a.inv_re * lB * lap(F[c]);
+            if (lq[c] != T(0)) gb += a.c_helm * lq[c] * lap(xp[c]);
+            gb += a.inv_re * lB * lap(xf[c]);
         }
     }
     block_atomic_add(gb, a.grad + 1);
@@ -653,11 +670,19 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
         const T iX = kc.id[0], iY = kc.id[1], iZ = kc.id[2];
         const T ix2 = kc.id2[0], iy2 = kc.id2[1], iz2 = kc.id2[2];
         const T *U = a.U, *V = a.V, *W = a.W;
-        auto ev = [&](int x, int y, int z) { return x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz; };
-        auto S = [&](int q, int x, int y, int z) { return a.src[(size_t)q * cs + hix(g, x, y, z)]; };
-        auto u = [&](int x, int y, int z) { return U[hix(g, x, y, z)]; };
-        auto v = [&](int x, int y, int z) { return V[hix(g, x, y, z)]; };
-        auto w = [&](int x, int y, int z) { return W[hix(g, x, y, z)]; };
+        // all stencil coordinates below are offsets (x, y, z) from this
+        // position; a source cell at offset (x, y, z) with |x|, |y|, |z| <= 1
+        // is an interior cell when ex[x + 1] && ey[y + 1] && ez[z + 1]
+        const int sx = g.sx, sxy = g.sx * g.sy;
+        const bool ex[3] = {i - 1 >= 1 && i - 1 <= g.nx, i >= 1 && i <= g.nx, i + 1 >= 1 && i + 1 <= g.nx};
+        const bool ey[3] = {j - 1 >= 1 && j - 1 <= g.ny, j >= 1 && j <= g.ny, j + 1 >= 1 && j + 1 <= g.ny};
+        const bool ez[3] = {k - 1 >= 1 && k - 1 <= g.nz, k >= 1 && k <= g.nz, k + 1 >= 1 && k + 1 <= g.nz};
+        auto ev = [&](int x, int y, int z) { return ex[x + 1] && ey[y + 1] && ez[z + 1]; };
+        auto at = [&](int x, int y, int z) { return t + x + sx * y + sxy * z; };
+        auto S = [&](int q, int x, int y, int z) { return a.src[(size_t)q * cs + at(x, y, z)]; };
+        auto u = [&](int x, int y, int z) { return U[at(x, y, z)]; };
+        auto v = [&](int x, int y, int z) { return V[at(x, y, z)]; };
+        auto w = [&](int x, int y, int z) { return W[at(x, y, z)]; };
         const T h = T(0.5);
         // velocity averages of the convection stencils around source cell (x, y, z)
         auto ax_t1 = [&](int x, int y, int z) { return (u(x - 1, y, z) + u(x, y, z)) * h; };
@@ -693,177 +718,186 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
         // sources: lua 0-2, ga 3-5 (ga, gbv, gc of the x, y, z fluxes), lb 6-8, st 9-11
         T lu = T(0), lv = T(0), lw = T(0), lp = T(0);
         // ---- U ----
-        if (ev(i, j, k)) {
-            const int x = i, y = j, z = k;
+        if (ev(0, 0, 0)) {
+            const int x = 0, y = 0, z = 0;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
             lu += S(0, x, y, z) - 2 * S(6, x, y, z) * (ix2 + iy2 + iz2) + ga * (ax_t2(x, y, z) - ax_t1(x, y, z)) * iX
                 + ga * iY * (axy_a2(x, y, z) - axy_a1(x, y, z)) * h + ga * iZ * (axz_c2(x, y, z) - axz_c1(x, y, z)) * h
                 + gbv * iX * ayx_b2(x, y, z) * h + gc * iX * azx_b2(x, y, z) * h;
         }
-        if (ev(i + 1, j, k)) {
-            const int x = i + 1, y = j, z = k;
+        if (ev(1, 0, 0)) {
+            const int x = 1, y = 0, z = 0;
             lu += S(6, x, y, z) * ix2 - S(3, x, y, z) * ax_t1(x, y, z) * iX - S(4, x, y, z) * iX * ayx_b1(x, y, z) * h
                 - S(5, x, y, z) * iX * azx_b1(x, y, z) * h;
         }
-        if (ev(i - 1, j, k)) {
-            const int x = i - 1, y = j, z = k;
+        if (ev(-1, 0, 0)) {
+            const int x = -1, y = 0, z = 0;
             lu += S(6, x, y, z) * ix2 + S(3, x, y, z) * ax_t2(x, y, z) * iX;
         }
-        if (ev(i, j + 1, k)) {
-            const int x = i, y = j + 1, z = k;
+        if (ev(0, 1, 0)) {
+            const int x = 0, y = 1, z = 0;
             lu += S(6, x, y, z) * iy2 - S(3, x, y, z) * iY * axy_a1(x, y, z) * h;
         }
-        if (ev(i, j - 1, k)) {
-            const int x = i, y = j - 1, z = k;
+        if (ev(0, -1, 0)) {
+            const int x = 0, y = -1, z = 0;
             lu += S(6, x, y, z) * iy2 + S(3, x, y, z) * iY * axy_a2(x, y, z) * h + S(4, x, y, z) * iX * ayx_b2(x, y, z) * h;
         }
-        if (ev(i, j, k + 1)) {
-            const int x = i, y = j, z = k + 1;
+        if (ev(0, 0, 1)) {
+            const int x = 0, y = 0, z = 1;
             lu += S(6, x, y, z) * iz2 - S(3, x, y, z) * iZ * axz_c1(x, y, z) * h;
         }
-        if (ev(i, j, k - 1)) {
-            const int x = i, y = j, z = k - 1;
+        if (ev(0, 0, -1)) {
+            const int x = 0, y = 0, z = -1;
             lu += S(6, x, y, z) * iz2 + S(3, x, y, z) * iZ * axz_c2(x, y, z) * h + S(5, x, y, z) * iX * azx_b2(x, y, z) * h;
         }
-        if (ev(i + 1, j - 1, k)) {
-            const int x = i + 1, y = j - 1, z = k;
+        if (ev(1, -1, 0)) {
+            const int x = 1, y = -1, z = 0;
             lu -= S(4, x, y, z) * iX * ayx_b1(x, y, z) * h;
         }
-        if (ev(i + 1, j, k - 1)) {
-            const int x = i + 1, y = j, z = k - 1;
+        if (ev(1, 0, -1)) {
+            const int x = 1, y = 0, z = -1;
             lu -= S(5, x, y, z) * iX * azx_b1(x, y, z) * h;
         }
         // ---- V ----
-        if (ev(i, j, k)) {
-            const int x = i, y = j, z = k;
+        if (ev(0, 0, 0)) {
+            const int x = 0, y = 0, z = 0;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
             lv += S(1, x, y, z) - 2 * S(7, x, y, z) * (ix2 + iy2 + iz2) + ga * iY * axy_b2(x, y, z) * h
                 + gbv * iX * (ayx_a2(x, y, z) - ayx_a1(x, y, z)) * h + gbv * (ay_t4(x, y, z) - ay_t3(x, y, z)) * iY
                 + gbv * iZ * (ayz_c2(x, y, z) - ayz_c1(x, y, z)) * h + gc * iY * azy_d2(x, y, z) * h;
         }
-        if (ev(i + 1, j, k)) {
-            const int x = i + 1, y = j, z = k;
+        if (ev(1, 0, 0)) {
+            const int x = 1, y = 0, z = 0;
             lv += S(7, x, y, z) * ix2 - S(4, x, y, z) * iX * ayx_a1(x, y, z) * h;
         }
-        if (ev(i - 1, j, k)) {
-            const int x = i - 1, y = j, z = k;
+        if (ev(-1, 0, 0)) {
+            const int x = -1, y = 0, z = 0;
             lv += S(7, x, y, z) * ix2 + S(3, x, y, z) * iY * axy_b2(x, y, z) * h + S(4, x, y, z) * iX * ayx_a2(x, y, z) * h;
         }
-        if (ev(i, j + 1, k)) {
-            const int x = i, y = j + 1, z = k;
+        if (ev(0, 1, 0)) {
+            const int x = 0, y = 1, z = 0;
             lv += S(7, x, y, z) * iy2 - S(3, x, y, z) * iY * axy_b1(x, y, z) * h - S(4, x, y, z) * ay_t3(x, y, z) * iY
                 - S(5, x, y, z) * iY * azy_d1(x, y, z) * h;
         }
-        if (ev(i, j - 1, k)) {
-            const int x = i, y = j - 1, z = k;
+        if (ev(0, -1, 0)) {
+            const int x = 0, y = -1, z = 0;
             lv += S(7, x, y, z) * iy2 + S(4, x, y, z) * ay_t4(x, y, z) * iY;
         }
-        if (ev(i, j, k + 1)) {
-            const int x = i, y = j, z = k + 1;
+        if (ev(0, 0, 1)) {
+            const int x = 0, y = 0, z = 1;
             lv += S(7, x, y, z) * iz2 - S(4, x, y, z) * iZ * ayz_c1(x, y, z) * h;
         }
-        if (ev(i, j, k - 1)) {
-            const int x = i, y = j, z = k - 1;
+        if (ev(0, 0, -1)) {
+            const int x = 0, y = 0, z = -1;
             lv += S(7, x, y, z) * iz2 + S(4, x, y, z) * iZ * ayz_c2(x, y, z) * h + S(5, x, y, z) * iY * azy_d2(x, y, z) * h;
         }
-        if (ev(i - 1, j + 1, k)) {
-            const int x = i - 1, y = j + 1, z = k;
+        if (ev(-1, 1, 0)) {
+            const int x = -1, y = 1, z = 0;
             lv -= S(3, x, y, z) * iY * axy_b1(x, y, z) * h;
         }
-        if (ev(i, j + 1, k - 1)) {
-            const int x = i, y = j + 1, z = k - 1;
+        if (ev(0, 1, -1)) {
+            const int x = 0, y = 1, z = -1;
             lv -= S(5, x, y, z) * iY * azy_d1(x, y, z) * h;
         }
         // ---- W ----
-        if (ev(i, j, k)) {
-            const int x = i, y = j, z = k;
+        if (ev(0, 0, 0)) {
+            const int x = 0, y = 0, z = 0;
             const T ga = S(3, x, y, z), gbv = S(4, x, y, z), gc = S(5, x, y, z);
             lw += S(2, x, y, z) - 2 * S(8, x, y, z) * (ix2 + iy2 + iz2) + ga * iZ * axz_d2(x, y, z) * h
                 + gbv * iZ * ayz_d2(x, y, z) * h + gc * iX * (azx_a2(x, y, z) - azx_a1(x, y, z)) * h
                 + gc * iY * (azy_c2(x, y, z) - azy_c1(x, y, z)) * h + gc * (az_t6(x, y, z) - az_t5(x, y, z)) * iZ;
         }
-        if (ev(i + 1, j, k)) {
-            const int x = i + 1, y = j, z = k;
+        if (ev(1, 0, 0)) {
+            const int x = 1, y = 0, z = 0;
             lw += S(8, x, y, z) * ix2 - S(5, x, y, z) * iX * azx_a1(x, y, z) * h;
         }
-        if (ev(i - 1, j, k)) {
-            const int x = i - 1, y = j, z = k;
+        if (ev(-1, 0, 0)) {
+            const int x = -1, y = 0, z = 0;
             lw += S(8, x, y, z) * ix2 + S(3, x, y, z) * iZ * axz_d2(x, y, z) * h + S(5, x, y, z) * iX * azx_a2(x, y, z) * h;
         }
-        if (ev(i, j + 1, k)) {
-            const int x = i, y = j + 1, z = k;
+        if (ev(0, 1, 0)) {
+            const int x = 0, y = 1, z = 0;
             lw += S(8, x, y, z) * iy2 - S(5, x, y, z) * iY * azy_c1(x, y, z) * h;
         }
-        if (ev(i, j - 1, k)) {
-            const int x = i, y = j - 1, z = k;
+        if (ev(0, -1, 0)) {
+            const int x = 0, y = -1, z = 0;
             lw += S(8, x, y, z) * iy2 + S(4, x, y, z) * iZ * ayz_d2(x, y, z) * h + S(5, x, y, z) * iY * azy_c2(x, y, z) * h;
         }
-        if (ev(i, j, k + 1)) {
-            const int x = i, y = j, z = k + 1;
+        if (ev(0, 0, 1)) {
+            const int x = 0, y = 0, z = 1;
             lw += S(8, x, y, z) * iz2 - S(3, x, y, z) * iZ * axz_d1(x, y, z) * h - S(4, x, y, z) * iZ * ayz_d1(x, y, z) * h
                 - S(5, x, y, z) * az_t5(x, y, z) * iZ;
         }
-        if (ev(i, j, k - 1)) {
-            const int x = i, y = j, z = k - 1;
+        if (ev(0, 0, -1)) {
+            const int x = 0, y = 0, z = -1;
             lw += S(8, x, y, z) * iz2 + S(5, x, y, z) * az_t6(x, y, z) * iZ;
         }
-        if (ev(i - 1, j, k + 1)) {
-            const int x = i - 1, y = j, z = k + 1;
+        if (ev(-1, 0, 1)) {
+            const int x = -1, y = 0, z = 1;
             lw -= S(3, x, y, z) * iZ * axz_d1(x, y, z) * h;
         }
-        if (ev(i, j - 1, k + 1)) {
-            const int x = i, y = j - 1, z = k + 1;
+        if (ev(0, -1, 1)) {
+            const int x = 0, y = -1, z = 1;
             lw -= S(4, x, y, z) * iZ * ayz_d1(x, y, z) * h;
         }
         // pressure gradient gp_c = -dt (P(o + e_c) - P(o)) / d_c, transposed
-        if (ev(i, j, k)) lp += kc.dtd[0] * S(0, i, j, k) + kc.dtd[1] * S(1, i, j, k) + kc.dtd[2] * S(2, i, j, k);
-        if (ev(i - 1, j, k)) lp -= kc.dtd[0] * S(0, i - 1, j, k);
-        if (ev(i, j - 1, k)) lp -= kc.dtd[1] * S(1, i, j - 1, k);
-        if (ev(i, j, k - 1)) lp -= kc.dtd[2] * S(2, i, j, k - 1);
-        a.lU[t] = lu;
-        a.lV[t] = lv;
-        a.lW[t] = lw;
-        a.lP[t] += lp;
+        if (ev(0, 0, 0)) lp += kc.dtd[0] * S(0, 0, 0, 0) + kc.dtd[1] * S(1, 0, 0, 0) + kc.dtd[2] * S(2, 0, 0, 0);
+        if (ev(-1, 0, 0)) lp -= kc.dtd[0] * S(0, -1, 0, 0);
+        if (ev(0, -1, 0)) lp -= kc.dtd[1] * S(1, 0, -1, 0);
+        if (ev(0, 0, -1)) lp -= kc.dtd[2] * S(2, 0, 0, -1);
+        const T lp0 = a.lP[t];
         if (a.polymer) {
             // adjoint of C0 from the stress divergence (fenep.f90:645-691):
             // sT = coef_t lT of the interior cells whose stencils read C0 here
             auto st = [&](int c, int x, int y, int z) { return ev(x, y, z) ? S(9 + c, x, y, z) : T(0); };
             const T q4x = kc.i4[0], q4y = kc.i4[1], q4z = kc.i4[2];
             T l0[6];
-            l0[0] = (st(0, i - 1, j, k) - st(0, i, j, k)) * iX;
-            l0[3] = (st(1, i, j - 1, k) - st(1, i, j, k)) * iY;
-            l0[5] = (st(2, i, j, k - 1) - st(2, i, j, k)) * iZ;
-            l0[1] = q4y * (st(0, i, j - 1, k) + st(0, i - 1, j - 1, k) - st(0, i, j + 1, k) - st(0, i - 1, j + 1, k))
-                  + q4x * (st(1, i - 1, j, k) + st(1, i - 1, j - 1, k) - st(1, i + 1, j, k) - st(1, i + 1, j - 1, k));
-            l0[2] = q4z * (st(0, i, j, k - 1) + st(0, i - 1, j, k - 1) - st(0, i, j, k + 1) - st(0, i - 1, j, k + 1))
-                  + q4x * (st(2, i - 1, j, k) + st(2, i - 1, j, k - 1) - st(2, i + 1, j, k) - st(2, i + 1, j, k - 1));
-            l0[4] = q4z * (st(1, i, j, k - 1) + st(1, i, j - 1, k - 1) - st(1, i, j, k + 1) - st(1, i, j - 1, k + 1))
-                  + q4y * (st(2, i, j - 1, k) + st(2, i, j - 1, k - 1) - st(2, i, j + 1, k) - st(2, i, j + 1, k - 1));
+            l0[0] = (st(0, -1, 0, 0) - st(0, 0, 0, 0)) * iX;
+            l0[3] = (st(1, 0, -1, 0) - st(1, 0, 0, 0)) * iY;
+            l0[5] = (st(2, 0, 0, -1) - st(2, 0, 0, 0)) * iZ;
+            l0[1] = q4y * (st(0, 0, -1, 0) + st(0, -1, -1, 0) - st(0, 0, 1, 0) - st(0, -1, 1, 0))
+                  + q4x * (st(1, -1, 0, 0) + st(1, -1, -1, 0) - st(1, 1, 0, 0) - st(1, 1, -1, 0));
+            l0[2] = q4z * (st(0, 0, 0, -1) + st(0, -1, 0, -1) - st(0, 0, 0, 1) - st(0, -1, 0, 1))
+                  + q4x * (st(2, -1, 0, 0) + st(2, -1, 0, -1) - st(2, 1, 0, 0) - st(2, 1, 0, -1));
+            l0[4] = q4z * (st(1, 0, 0, -1) + st(1, 0, -1, -1) - st(1, 0, 0, 1) - st(1, 0, -1, 1))
+                  + q4y * (st(2, 0, -1, 0) + st(2, 0, -1, -1) - st(2, 0, 1, 0) - st(2, 0, 1, -1));
             bool any = false;
             for (int m = 0; m < 6; ++m) any = any || l0[m] != T(0);
             if (any) {
                 // C0 = f(C) C - I linearised
                 const T E[6] = {T(1), T(0), T(0), T(1), T(0), T(1)};
-                T c[6];
-                for (int m = 0; m < 6; ++m) c[m] = a.C[(size_t)m * cs + t];
+                T c[6], lc[6];
+#pragma unroll
+                for (int m = 0; m < 6; ++m) {
+                    c[m] = a.C[(size_t)m * cs + t];
+                    lc[m] = a.lC[(size_t)m * cs + t];
+                }
                 const T tr3 = (c[0] - T(1)) + (c[3] - T(1)) + (c[5] - T(1));
                 const T den = (a.lp2 - 3) - tr3;
                 const T iden = T(1) / den;
                 const T f = (a.lp2 - 3) * iden;
                 const T fm1 = tr3 * iden;
                 T lf = T(0);
+#pragma unroll
                 for (int m = 0; m < 6; ++m) {
-                    a.lC[(size_t)m * cs + t] += f * l0[m];
+                    lc[m] += f * l0[m];
                     lf += c[m] * l0[m];
                     g_coef += (fm1 * c[m] + (c[m] - E[m])) * l0[m];
                 }
                 const T dfdtr = f * iden;
-                a.lC[t] += lf * dfdtr;
-                a.lC[(size_t)3 * cs + t] += lf * dfdtr;
-                a.lC[(size_t)5 * cs + t] += lf * dfdtr;
+                lc[0] += lf * dfdtr;
+                lc[3] += lf * dfdtr;
+                lc[5] += lf * dfdtr;
+#pragma unroll
+                for (int m = 0; m < 6; ++m) a.lC[(size_t)m * cs + t] = lc[m];
                 g_l2 = -lf * tr3 * (iden * iden);
             }
         }
+        // the stores last: loads after a store could not be moved ahead of it
+        a.lU[t] = lu;
+        a.lV[t] = lv;
+        a.lW[t] = lw;
+        a.lP[t] = lp0 + lp;
     }
     if (a.polymer) {
         block_atomic_add(-g_coef * a.inv_1mb, a.grad + 1);
@@ -878,7 +912,7 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
 // offsets -2, -1, +1, +2), the adjoint of the velocity-gradient entries and
 // of the upwind coefficients, and the Wi and L^2 terms.
 template <typename T>
-__global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *src, Geo g) {
+__global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
@@ -1099,11 +1133,12 @@ __global__ void __launch_bounds__(256) k_polyadj_gather(PolyGatherArgs<T> a, Geo
     add(lw, PS_GW + 1, i, j + 1, k, T(1));      add(lw, PS_GW + 1, i, j - 1, k, T(-1));
     add(lw, PS_GW + 2, i, j, k + 1, T(1));      add(lw, PS_GW + 2, i, j, k, T(-1));
     add(lw, PS_SF + 4, i, j, k, T(1));          add(lw, PS_SF + 5, i, j, k + 1, T(1));
-    a.lU[t] += lu;
-    a.lV[t] += lv;
-    a.lW[t] += lw;
+    const T lu0 = a.lU[t], lv0 = a.lV[t], lw0 = a.lW[t];
     // adjoint of C^n at the updated cells
     if (!upd(i, j, k)) {
+        a.lU[t] = lu0 + lu;
+        a.lV[t] = lv0 + lv;
+        a.lW[t] = lw0 + lw;
         for (int m = 0; m < 6; ++m) a.lC[(size_t)m * cs + t] = T(0);
         return;
     }
@@ -1126,6 +1161,10 @@ __global__ void __launch_bounds__(256) k_polyadj_gather(PolyGatherArgs<T> a, Geo
         if (!g.walls) line(PS_KY, i, wrapy(g, j - o), k, q);
         else if (j - o >= r0 && j - o <= r1) line(PS_KY, i, j - o, k, q);
     }
+    // the stores last: loads after a store could not be moved ahead of it
+    a.lU[t] = lu0 + lu;
+    a.lV[t] = lv0 + lv;
+    a.lW[t] = lw0 + lw;
     for (int m = 0; m < 6; ++m) a.lC[(size_t)m * cs + t] = l[m];
 }
 

@@ -39,11 +39,6 @@ cudaError_t poisson_solve_f(Dev &d, const float *src, float *dst, float *lo, int
                      : mixed_solve_periodic(d, src, dst, lo, mode, 0.0, -1.0, s);
 }
 
-cudaError_t helmholtz_solve_f(Dev &d, int comp, const float *src, float *dst, cudaStream_t s) {
-    if (d.g.walls) return mixed_solve_walls(d, src, dst, nullptr, 0, comp == 1 ? 1 : 0, s);
-    return mixed_solve_periodic(d, src, dst, nullptr, 0, 1.0, d.ph.dt * d.ph.beta / d.ph.re / 2.0, s);
-}
-
 // k_div_adj with the pressure adjoint q as a double-float pair (qh, ql): the
 // adjoint projection lUp = lU + (q - q(+e))/(d dt) cancels the gradient part of
 // lU, so the difference and its scaling are formed in df64 and only the
@@ -92,10 +87,15 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
                                     df_from_d(1.0 / (g.dx * dt)), df_from_d(1.0 / (g.dy * dt)),
                                     df_from_d(1.0 / (g.dz * dt))); count_launch();
     F8_CUDA_RET(fold(fold_set<float>({{A.lUp[0], BC_U}, {A.lUp[1], BC_V}, {A.lUp[2], BC_W}}), g, s));
-    // 4. Helmholtz
-    for (int c = 0; c < 3; ++c) {
-        k_pack<float><<<adj_cells(g, blk), blk, 0, s>>>(A.lUp[c], A.pack, g); count_launch();
-        F8_CUDA_RET(helmholtz_solve_f(d, c, A.pack, A.lQ[c], s));
+    // 4. Helmholtz: the three solves as the forward's parallel branches
+    {
+        const float *src[3];
+        for (int c = 0; c < 3; ++c) {
+            float *pk = A.pack + (size_t)c * d.ni;
+            k_pack<float><<<adj_cells(g, blk), blk, 0, s>>>(A.lUp[c], pk, g); count_launch();
+            src[c] = pk;
+        }
+        F8_CUDA_RET(mixed_helmholtz3(d, src, A.lQ, s));
     }
     // 3. IBM
     for (int c = 0; c < 3; ++c) F8_CUDA_RET(cudaMemsetAsync(A.lUa[c], 0, hb, s));

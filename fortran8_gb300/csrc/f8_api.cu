@@ -1100,7 +1100,7 @@ int grad_alloc(f8_ctx *c, int K, int nck, int nsteps) {
             API_CUDA(c, G.get(0, &A.lUp[q], cs));
             API_CUDA(c, G.get(0, &A.lQ[q], cs));
         }
-        API_CUDA(c, G.get(0, &A.pack, ni));
+        API_CUDA(c, G.get(0, &A.pack, 3 * ni));   // one interior array per Helmholtz solve
         API_CUDA(c, G.get(0, &A.work, ADJ_WORK_FIELDS * cs));
         API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
     }
@@ -1219,7 +1219,7 @@ int grad_alloc_mixed(f8_ctx *c, int K, int nck, int nsteps) {
             API_CUDA(c, G.get(0, &A.lUp[q], cs));
             API_CUDA(c, G.get(0, &A.lQ[q], cs));
         }
-        API_CUDA(c, G.get(0, &A.pack, ni));
+        API_CUDA(c, G.get(0, &A.pack, 3 * ni));   // one interior array per Helmholtz solve
         API_CUDA(c, G.get(0, &A.qlo, cs));
         API_CUDA(c, G.get(0, &A.zero, ni));
         API_CUDA(c, G.get(0, &A.rdef, ni));

@@ -220,7 +220,7 @@ struct AdjStateF {
     float *lC, *lC2;
     float *lA0[3], *lT0[3];
     float *lUa[3], *lUp[3], *lQ[3];
-    float *pack;
+    float *pack;             // interior arrays of the solves' right-hand sides (3 * ni)
     float *qlo;              // low part of the refined pressure adjoint (halo, with lQ[0] its high part)
     float *zero, *rdef;      // interior: zeros (the right-hand side's low part), the defect
     float *work;             // per-cell sources of the gather kernels (ADJ_WORK_FIELDS halo fields)
@@ -231,6 +231,7 @@ struct AdjStateF {
 cudaError_t mixed_solve_periodic(Dev &d, const float *src, float *dst, float *lo, int mode, double lhs0, double lhs1,
                                  cudaStream_t s);
 cudaError_t mixed_solve_walls(Dev &d, const float *src, float *dst, float *lo, int mode, int sys, cudaStream_t s);
+cudaError_t mixed_helmholtz3(Dev &d, const float *const src[3], float *const dst[3], cudaStream_t s);
 cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float *rl, float *rd, cudaStream_t s);
 cudaError_t setup_staged_projection(Dev &d);
 cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const double *drag_w, bool ab2_first,

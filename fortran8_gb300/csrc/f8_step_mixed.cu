@@ -1824,6 +1824,42 @@ cudaError_t mixed_solve_walls(Dev &d, const float *src, float *dst, float *lo, i
     return solve_walls_f(d, src, XOutF{dst, lo, mode}, sys, s);
 }
 
+// the three Helmholtz solves of one step (dst[c] = v of component c, mode 0),
+// the V and W solves forked onto the side streams with their own spectra on
+// the fused spectral path, as in the forward step
+cudaError_t mixed_helmholtz3(Dev &d, const float *const src[3], float *const dst[3], cudaStream_t s) {
+    const Geo &g = d.g;
+    const double lhs1 = d.ph.dt * d.ph.beta / d.ph.re / 2.0;
+    const bool branches = d.fused_planes && d.aux[0] && d.aux[1];
+    if (branches) {
+        F8_CUDA_RET(cudaEventRecord(d.ev_fork, s));
+        for (int b = 0; b < 2; ++b) F8_CUDA_RET(cudaStreamWaitEvent(d.aux[b], d.ev_fork, 0));
+    }
+    for (int c = 0; c < 3; ++c) {
+        const XOutF out{dst[c], nullptr, 0};
+        const int sys = c == 1 ? SYS_V : SYS_U;
+        cudaError_t e;
+        if (branches) {
+            cudaStream_t sc = c == 0 ? s : d.aux[c - 1];
+            float *spec = c == 0 ? d.Hf : d.HfB[c - 1];
+            if (!g.walls) e = solve_periodic_fused<float>(d, src[c], out, 1.0f, (float)lhs1, sc, spec);
+            else e = solve_walls_fused<float>(d, src[c], out, sys, sc, spec);
+        } else if (!g.walls) {
+            e = solve_periodic_f(d, src[c], out, 1.0, lhs1, s);
+        } else {
+            e = solve_walls_f(d, src[c], out, sys, s);
+        }
+        if (e) return e;
+    }
+    if (branches) {
+        for (int b = 0; b < 2; ++b) {
+            F8_CUDA_RET(cudaEventRecord(d.ev_join[b], d.aux[b]));
+            F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_join[b], 0));
+        }
+    }
+    return cudaGetLastError();
+}
+
 // defect rd = (rh + rl) - L_h phi of an FP32 pressure-type field in df64, the
 // operator of the mixed step's Poisson solve (interior arrays rh, rl, rd)
 cudaError_t mixed_defect(Dev &d, const float *phi, const float *rh, const float *rl, float *rd, cudaStream_t s) {
