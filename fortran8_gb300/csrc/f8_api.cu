@@ -100,6 +100,21 @@ struct GradMem {
     uint8_t *fcodes = nullptr, *fcodes_g = nullptr;
     double *fFc = nullptr;
     size_t fck_slot = 0;                    // floats per mixed checkpoint
+    // CUDA graphs of the mixed gradient's steps, [2 * rec + parity]: the
+    // forward step writing tape slot rec and the reverse step reading it
+    // (parity: which buffer of the C pair, or of the adjoint C pair, is
+    // current); kernels per replay of each kind
+    std::vector<cudaGraphExec_t> gfwd, grev;
+    long long gfwd_launches = 0, grev_launches = 0;
+    double *dw_slot = nullptr;              // drag weights of the step a replayed reverse step reads
+    float *lc_base = nullptr;               // the adjoint C buffer of parity 0
+    void drop_graphs() {
+        for (auto *v : {&gfwd, &grev}) {
+            for (cudaGraphExec_t &ge : *v)
+                if (ge) cudaGraphExecDestroy(ge);
+            v->clear();
+        }
+    }
     template <typename T>
     cudaError_t get(int grp, T **p, size_t n) {
         void *q = nullptr;
@@ -114,6 +129,7 @@ struct GradMem {
         mem[grp].clear();
     }
     void free_all() {
+        drop_graphs();
         for (int q = 0; q < 4; ++q) free_group(q);
         *this = GradMem{};
     }
@@ -195,6 +211,7 @@ struct f8_ctx {
     void drop_graphs() {
         for (cudaGraphExec_t &ge : gexec)
             if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+        gm.drop_graphs();
     }
     void release() {
         for (cudaEvent_t e : evpool) cudaEventDestroy(e);
@@ -1226,8 +1243,11 @@ int grad_alloc_mixed(f8_ctx *c, int K, int nck, int nsteps) {
         API_CUDA(c, G.get(0, &A.work, ADJ_WORK_FIELDS * cs));
         API_CUDA(c, cudaMemsetAsync(A.zero, 0, ni * sizeof(float), c->s));
         API_CUDA(c, G.get(0, &A.grad, 3 + 2 * ncyl));
+        API_CUDA(c, G.get(0, &G.dw_slot, 3 * std::max<size_t>(ncyl, 1)));
+        G.lc_base = A.lC;
     }
     if (K > G.K) {
+        G.drop_graphs();   // they hold tape addresses
         G.free_group(1);
         G.K = 0;
         API_CUDA(c, G.get(1, &G.ftape, (size_t)K * MIXED_TAPE_FIELDS * cs));
@@ -1291,10 +1311,39 @@ MixTape tape_slot_mixed(f8_ctx *c, int rec) {
     return t;
 }
 
+// Launch graph ge on the context's stream, capturing it first from record()
+// (which enqueues the work and undoes any host-side buffer swap it makes:
+// the capture runs nothing).  nl: kernels per replay.
+template <typename F>
+cudaError_t replay_graph(f8_ctx *c, cudaGraphExec_t &ge, long long &nl, F &&record) {
+    if (!ge) {
+        const long long l0 = g_kernel_launches.load();
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        e = record();
+        const cudaError_t e2 = cudaStreamEndCapture(c->s, &gr);
+        nl = g_kernel_launches.load() - l0;
+        g_kernel_launches -= nl;
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+        if (e != cudaSuccess) {
+            ge = nullptr;
+            return e;
+        }
+    }
+    g_kernel_launches += nl;
+    return cudaGraphLaunch(ge, c->s);
+}
+
 // one forward step of f8_grad on a mixed context (absolute step index s of
-// the call); rec >= 0 writes the tape of the step into segment slot rec
+// the call); rec >= 0 writes the tape of the step into segment slot rec.
+// Replayed from a CUDA graph (the step's own without a tape, one per tape
+// slot and C parity with one) except for the AB2 start step.
 cudaError_t grad_forward_step_mixed(f8_ctx *c, int step0, int s, int rec) {
     Dev &d = c->d;
+    GradMem &G = c->gm;
     const int ncyl = (int)c->cyl.size();
     StepOpts o{};
     o.polymer = c->phys.beta != 1.0;
@@ -1308,7 +1357,22 @@ cudaError_t grad_forward_step_mixed(f8_ctx *c, int step0, int s, int rec) {
         o.tape = &t;
     }
     int sor = -1;
-    return step_mixed(d, o, ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr, &sor, c->s);
+    double *dg = ncyl ? c->drag_dev + (size_t)s * ncyl * 3 : nullptr;
+    if (o.ab2_first) return step_mixed(d, o, dg, &sor, c->s);
+    const int p = d.Cf == c->cf_base ? 0 : 1;
+    if (rec >= 0 && G.gfwd.size() < 2 * (size_t)G.K) G.gfwd.resize(2 * (size_t)G.K, nullptr);
+    cudaGraphExec_t &ge = rec < 0 ? c->gexec[p] : G.gfwd[2 * rec + p];
+    long long &nl = rec < 0 ? c->graph_launches : G.gfwd_launches;
+    F8_CUDA_RET(replay_graph(c, ge, nl, [&] {
+        float *cf0 = d.Cf, *cn0 = d.Cnf;
+        const cudaError_t e = step_mixed(d, o, ncyl ? c->drag_slot : nullptr, &sor, c->s);
+        d.Cf = cf0;
+        d.Cnf = cn0;
+        return e;
+    }));
+    if (o.polymer) std::swap(d.Cf, d.Cnf);
+    if (dg) F8_CUDA_RET(cudaMemcpyAsync(dg, c->drag_slot, (size_t)ncyl * 3 * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+    return cudaSuccess;
 }
 
 // f8_grad on an FP32-mixed 3D context with the FFT solvers: the same
@@ -1388,9 +1452,28 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
             for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step_mixed(c, step0, s, s - s0));
         }
         for (int s = s1 - 1; s >= s0; --s) {
-            const MixTape t = tape_slot_mixed(c, s - s0);
+            const int rec = s - s0;
+            const MixTape t = tape_slot_mixed(c, rec);
             const bool ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
-            API_CUDA(c, step_mixed_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, ab2_first, polymer, c->s));
+            if (ab2_first) {
+                API_CUDA(c, step_mixed_adjoint(d, A, t, G.dw + (size_t)s * ncyl * 3, true, polymer, c->s));
+                continue;
+            }
+            // replayed from the graph of tape slot rec and adjoint C parity,
+            // reading this step's drag weights from a fixed slot
+            if (ncyl)
+                API_CUDA(c, cudaMemcpyAsync(G.dw_slot, G.dw + (size_t)s * ncyl * 3, (size_t)ncyl * 3 * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, c->s));
+            if (G.grev.size() < 2 * (size_t)G.K) G.grev.resize(2 * (size_t)G.K, nullptr);
+            const int p = A.lC == G.lc_base ? 0 : 1;
+            API_CUDA(c, replay_graph(c, G.grev[2 * rec + p], G.grev_launches, [&] {
+                float *l0 = A.lC, *l1 = A.lC2;
+                const cudaError_t e = step_mixed_adjoint(d, A, t, G.dw_slot, false, polymer, c->s);
+                A.lC = l0;
+                A.lC2 = l1;
+                return e;
+            }));
+            if (polymer) std::swap(A.lC, A.lC2);
         }
     }
     if (nseg > 1) API_CUDA(c, ck_copy_mixed(c, nseg - 1, false));
