@@ -14,8 +14,7 @@ namespace f8 {
 
 cudaError_t adjoint_fold_state(AdjState &A, const Dev &d, cudaStream_t s) {
     const Geo &g = d.g;
-    F8_CUDA_RET(fold(fold_set<double>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lW, BC_W}, {A.lP, BC_P}}), g, s));
-    return fold(fold_c(A.lC, d.cs), g, s);
+    return fold(fold_with_c(fold_set<double>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lW, BC_W}, {A.lP, BC_P}}), A.lC, d.cs, 6), g, s);
 }
 
 cudaError_t take_interior(const double *src, double *dst, const Geo &g, int n, cudaStream_t s) {
@@ -112,7 +111,9 @@ cudaError_t step_fp64_adjoint(Dev &d, AdjState &A, const TapeStep &t, const doub
         pa.kc = kc; pa.dtwi = dt / wi; pa.dtwi2 = dt / (wi * wi);
         dim3 pb(32, 4);
         const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
-        k_polyadj_src<double><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
+        k_polyadj_mu<double><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
+        const dim3 pb2(32, 8), pg2((g.nx + pb2.x - 1) / pb2.x, (prows(g) + pb2.y - 1) / pb2.y, g.nz);
+        k_polyadj_cstar<double><<<pg2, pb2, 0, s>>>(pa, A.work, g); count_launch();
         PolyGatherArgs<double> pga{};
         pga.src = A.work; pga.lC = A.lC2; pga.lU = A.lU; pga.lV = A.lV; pga.lW = A.lW; pga.cs = cs;
         k_polyadj_gather<double><<<nb, 256, 0, s>>>(pga, g); count_launch();
@@ -565,8 +566,7 @@ cudaError_t step_fp64_adjoint2(Dev &d, AdjState &A, const TapeStep &t, const dou
     } else {
         F8_CUDA_RET(cudaMemsetAsync(A.lC, 0, 3 * hb, s));
     }
-    F8_CUDA_RET(fold(fold_set<double>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lP, BC_P}}), g, s));
-    return fold(fold_c(A.lC, cs, 3), g, s);
+    return fold(fold_with_c(fold_set<double>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lP, BC_P}}), A.lC, cs, 3), g, s);
 }
 
 }  // namespace f8

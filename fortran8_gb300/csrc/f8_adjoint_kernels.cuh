@@ -16,7 +16,8 @@
 //   Helmholtz solves               (1430-1527) the forward solves again
 //   IBM direct forcing             (fenep_mpi.f90:1794-1929)   k_ibm_adj
 //   momentum right-hand side       (fenep.f90:645-770, 1469)   k_momadj_src, k_momadj_gather
-//   Lyapunov Newton + Cstar        (fenep.f90:464-643)         k_polyadj_src, k_polyadj_gather
+//   Lyapunov Newton + Cstar        (fenep.f90:464-643)         k_polyadj_mu, k_polyadj_cstar,
+//                                                               k_polyadj_gather
 // Halo fills (fenep.f90:147-166, fenep_2d.f90:1098-1143) are linear maps of
 // the interior; their transposes (k_fold_*) move the adjoint gathered on halo
 // cells back to the interior cells they were copied from.
@@ -128,8 +129,8 @@ __device__ inline void block_atomic_add(double v, double *dst) {
 
 template <typename T>
 struct FoldSet {
-    T *A[8];
-    int kind[8];
+    T *A[12];
+    int kind[12];
     int n;
 };
 
@@ -139,14 +140,12 @@ __global__ void k_fold_z(FoldSet<T> f, Geo g) {
     if (t >= g.sx * g.sy) return;
     const int i = t % g.sx, j = t / g.sx;
     const int lo = hix(g, i, j, 0), hi = hix(g, i, j, g.sz - 1), top = hix(g, i, j, g.nz), bot = hix(g, i, j, 1);
-    for (int q = 0; q < f.n; ++q) {
-        T *A = f.A[q];
-        const T a = A[lo], b = A[hi];
-        A[top] += a;
-        A[bot] += b;
-        A[lo] = T(0);
-        A[hi] = T(0);
-    }
+    T *A = f.A[blockIdx.y];
+    const T a = A[lo], b = A[hi];
+    A[top] += a;
+    A[bot] += b;
+    A[lo] = T(0);
+    A[hi] = T(0);
 }
 
 template <typename T>
@@ -155,26 +154,25 @@ __global__ void k_fold_y(FoldSet<T> f, Geo g) {
     if (t >= g.sx * g.nz) return;
     const int i = t % g.sx, k = 1 + t / g.sx;
     const int g0 = hix(g, i, 0, k), g1 = hix(g, i, g.ny + 1, k), r1 = hix(g, i, 1, k), rn = hix(g, i, g.ny, k);
-    for (int q = 0; q < f.n; ++q) {
-        T *A = f.A[q];
-        const T a = A[g0], b = A[g1];
-        if (!g.walls) {
-            A[rn] += a;
-            A[r1] += b;
-        } else {
-            switch (f.kind[q]) {
-            case BC_U:
-            case BC_W: A[r1] -= a; A[rn] -= b; break;     // ghost = -U (2 Uwall - U)
-            case BC_V: A[rn] = T(0); break;               // V(:,0) = V(:,NY) = V(:,NY+1) = 0
-            case BC_P: A[r1] += a; A[rn] += b; break;     // Neumann copies
-            default:                                      // C: 2 C(1) - C(2), 2 C(NY) - C(NY-1)
-                A[r1] += T(2) * a; A[hix(g, i, 2, k)] -= a;
-                A[rn] += T(2) * b; A[hix(g, i, g.ny - 1, k)] -= b;
-            }
+    const int q = blockIdx.y;
+    T *A = f.A[q];
+    const T a = A[g0], b = A[g1];
+    if (!g.walls) {
+        A[rn] += a;
+        A[r1] += b;
+    } else {
+        switch (f.kind[q]) {
+        case BC_U:
+        case BC_W: A[r1] -= a; A[rn] -= b; break;     // ghost = -U (2 Uwall - U)
+        case BC_V: A[rn] = T(0); break;               // V(:,0) = V(:,NY) = V(:,NY+1) = 0
+        case BC_P: A[r1] += a; A[rn] += b; break;     // Neumann copies
+        default:                                      // C: 2 C(1) - C(2), 2 C(NY) - C(NY-1)
+            A[r1] += T(2) * a; A[hix(g, i, 2, k)] -= a;
+            A[rn] += T(2) * b; A[hix(g, i, g.ny - 1, k)] -= b;
         }
-        A[g0] = T(0);
-        A[g1] = T(0);
     }
+    A[g0] = T(0);
+    A[g1] = T(0);
 }
 
 // rows: 1..NY, or every row 0..NY+1 (rows_all) for the periodic x/z fill of
@@ -186,21 +184,22 @@ __global__ void k_fold_x(FoldSet<T> f, Geo g, int rows_all) {
     if (t >= ny * g.nz) return;
     const int j = j0 + t % ny, k = 1 + t / ny;
     const int lo = hix(g, 0, j, k), hi = hix(g, g.sx - 1, j, k);
-    for (int q = 0; q < f.n; ++q) {
-        T *A = f.A[q];
-        const T a = A[lo], b = A[hi];
-        A[hix(g, g.nx, j, k)] += a;
-        A[hix(g, 1, j, k)] += b;
-        A[lo] = T(0);
-        A[hi] = T(0);
-    }
+    T *A = f.A[blockIdx.y];
+    const T a = A[lo], b = A[hi];
+    A[hix(g, g.nx, j, k)] += a;
+    A[hix(g, 1, j, k)] += b;
+    A[lo] = T(0);
+    A[hi] = T(0);
 }
 
+// one block row (blockIdx.y) per field of the set: the fields are independent
 template <typename T>
 cudaError_t fold(const FoldSet<T> &f, const Geo &g, cudaStream_t s) {
-    k_fold_z<T><<<(g.sx * g.sy + 255) / 256, 256, 0, s>>>(f, g); count_launch();
-    k_fold_y<T><<<(g.sx * g.nz + 255) / 256, 256, 0, s>>>(f, g); count_launch();
-    k_fold_x<T><<<(g.ny * g.nz + 255) / 256, 256, 0, s>>>(f, g, 0); count_launch();
+    const unsigned n = (unsigned)f.n;
+    if (n == 0) return cudaSuccess;
+    k_fold_z<T><<<dim3((g.sx * g.sy + 255) / 256, n), 256, 0, s>>>(f, g); count_launch();
+    k_fold_y<T><<<dim3((g.sx * g.nz + 255) / 256, n), 256, 0, s>>>(f, g); count_launch();
+    k_fold_x<T><<<dim3((g.ny * g.nz + 255) / 256, n), 256, 0, s>>>(f, g, 0); count_launch();
     return cudaGetLastError();
 }
 
@@ -208,8 +207,10 @@ cudaError_t fold(const FoldSet<T> &f, const Geo &g, cudaStream_t s) {
 // wall ghost rows stay (they are updated cells)
 template <typename T>
 cudaError_t fold_xz(const FoldSet<T> &f, const Geo &g, cudaStream_t s) {
-    k_fold_z<T><<<(g.sx * g.sy + 255) / 256, 256, 0, s>>>(f, g); count_launch();
-    k_fold_x<T><<<(g.sy * g.nz + 255) / 256, 256, 0, s>>>(f, g, 1); count_launch();
+    const unsigned n = (unsigned)f.n;
+    if (n == 0) return cudaSuccess;
+    k_fold_z<T><<<dim3((g.sx * g.sy + 255) / 256, n), 256, 0, s>>>(f, g); count_launch();
+    k_fold_x<T><<<dim3((g.sy * g.nz + 255) / 256, n), 256, 0, s>>>(f, g, 1); count_launch();
     return cudaGetLastError();
 }
 
@@ -226,6 +227,13 @@ FoldSet<T> fold_c(T *C, int cs, int ncomp = 6) {
     for (int m = 0; m < ncomp; ++m) { f.A[m] = C + (size_t)m * cs; f.kind[m] = BC_C; }
     f.n = ncomp;
     return f;
+}
+
+// the fields of a and then those of C (ncomp components), folded in one pass
+template <typename T>
+FoldSet<T> fold_with_c(FoldSet<T> a, T *C, int cs, int ncomp) {
+    for (int m = 0; m < ncomp; ++m) { a.A[a.n] = C + (size_t)m * cs; a.kind[a.n] = BC_C; ++a.n; }
+    return a;
 }
 
 // ---------------------------------------------------------------------------
@@ -906,13 +914,12 @@ __global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g
     }
 }
 
-// Polymer, pass 1 (the updated cells; with walls also the ghost rows): the
-// implicit-function adjoint mu = J^-T lC^{n+1} at the Newton solution, the 13
-// Cstar weights of the cell (the same for the 6 components: centre, x/y/z at
-// offsets -2, -1, +1, +2), the adjoint of the velocity-gradient entries and
-// of the upwind coefficients, and the Wi and L^2 terms.
+// Polymer, pass 1 (the updated cells; with walls also the ghost rows), in two
+// kernels so that neither holds the registers of both halves.  Pass 1a: the
+// implicit-function adjoint mu = J^-T lC^{n+1} at the Newton solution, the
+// adjoint of the velocity-gradient entries and the Wi and L^2 terms.
 template <typename T>
-__global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
+__global__ void __launch_bounds__(128) k_polyadj_mu(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
@@ -934,7 +941,9 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *__rest
         }
         if (!any) {
 #pragma unroll
-            for (int q = 0; q < POLY_SRC; ++q) put(q, T(0));
+            for (int m = 0; m < 6; ++m) put(PS_MU + m, T(0));
+#pragma unroll
+            for (int q = PS_GU; q < PS_SF; ++q) put(q, T(0));
         } else {
             const T *U = a.U, *V = a.V, *W = a.W;
             auto u = [&](int p, int q, int r) { return rowv(U, g, p, q, r); };
@@ -995,104 +1004,137 @@ __global__ void __launch_bounds__(128) k_polyadj_src(PolyAdjArgs<T> a, T *__rest
             put(PS_GW + 0, lAt[2][0] * kc.dt4d[0]);
             put(PS_GW + 1, lAt[2][1] * kc.dt4d[1]);
             put(PS_GW + 2, lAt[2][2] * kc.dtd[2]);
-            // Cstar: upwind coefficients s1..s12 and the selection codes
-            const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
-            const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
-            const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
-            const T sixth = T(1) / T(6);
-            const T s1 = (-u2 + fabs(u2)) * kc.dt2d[0], s2 = sixth + (-u2 - fabs(u2)) * kc.dt2d[0];
-            const T s3 = sixth + (u1 - fabs(u1)) * kc.dt2d[0], s4 = (u1 + fabs(u1)) * kc.dt2d[0];
-            const T s5 = (-v2 + fabs(v2)) * kc.dt2d[1], s6 = sixth + (-v2 - fabs(v2)) * kc.dt2d[1];
-            const T s7 = sixth + (v1 - fabs(v1)) * kc.dt2d[1], s8 = (v1 + fabs(v1)) * kc.dt2d[1];
-            const T s9 = (-w2 + fabs(w2)) * kc.dt2d[2], s10 = sixth + (-w2 - fabs(w2)) * kc.dt2d[2];
-            const T s11 = sixth + (w1 - fabs(w1)) * kc.dt2d[2], s12 = (w1 + fabs(w1)) * kc.dt2d[2];
-            const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
-            const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
-            const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
-            const int czm = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
-            const int czp = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
-            int jm = j - 1, jp = j + 1;
-            if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-            const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
-            const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
-            const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
-            const W3<T> wpx = wface_p<T>(isx), wnx = wface_n<T>(isx), wpy = wface_p<T>(isy), wny = wface_n<T>(isy);
-            const W3<T> wpz = wface_p<T>(isz), wnz = wface_n<T>(isz);
-            const W3<T> qx = wface_p<T>(cxp + 1), rx = wface_n<T>(cxm + 1), qy = wface_p<T>(cyp + 1), ry = wface_n<T>(cym + 1);
-            const W3<T> qz = wface_p<T>(czp + 1), rz = wface_n<T>(czm + 1);
-            // weights of one direction: own p / n faces (coefficients sp, sn),
-            // the + neighbour's p face (sq) and the - neighbour's n face (sr),
-            // at offsets -2, -1, +1, +2; the centre weights are summed in kcen
-            T kcen = T(0);
-            auto dirw = [&](W3<T> wp_, W3<T> wn_, W3<T> wq, W3<T> wr, T sp, T sn, T sq, T sr, int base) {
-                put(base + 0, sr * wr.m);
-                put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
-                put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
-                put(base + 3, sq * wq.p);
-                kcen += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
-            };
-            dirw(wpx, wnx, qx, rx, s3, s2, s1, s4, PS_KX);
-            dirw(wpy, wny, qy, ry, s7, s6, s5, s8, PS_KY);
-            dirw(wpz, wnz, qz, rz, s11, s10, s9, s12, PS_KZ);
-            put(PS_KC, kcen);
-            // adjoints of s1..s12: mu . (face value), faces rebuilt from C^n
-            const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-            const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-            const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
-            T l1 = T(0), l2 = T(0), l3 = T(0), l4 = T(0), l5 = T(0), l6 = T(0);
-            T l7 = T(0), l8 = T(0), l9 = T(0), l10 = T(0), l11 = T(0), l12 = T(0);
-            auto face = [](W3<T> wt, T cmv, T c0v, T cpv) { return wt.m * cmv + wt.c * c0v + wt.p * cpv; };
-#pragma unroll
-            for (int m = 0; m < 6; ++m) {
-                const T *Cm = a.C + m * cs;
-                const T mum = mu[m];
-                {
-                    const T cmv = Cm[h - ox], c0v = Cm[h], cpv = Cm[h + ox];
-                    l3 += mum * face(wpx, cmv, c0v, cpv);
-                    l2 += mum * face(wnx, cmv, c0v, cpv);
-                    l1 += mum * face(qx, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
-                    l4 += mum * face(rx, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
-                }
-                if (!g.walls) {
-                    const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
-                    const T cmv = Cm[h - oy], c0v = Cm[h], cpv = Cm[h + oy];
-                    l7 += mum * face(wpy, cmv, c0v, cpv);
-                    l6 += mum * face(wny, cmv, c0v, cpv);
-                    l5 += mum * face(qy, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-                    l8 += mum * face(ry, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
-                } else {
-                    auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
-                    const T cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
-                    l7 += mum * face(wpy, cmv, c0v, cpv);
-                    l6 += mum * face(wny, cmv, c0v, cpv);
-                    l5 += mum * face(qy, c0v, cpv, yv(j + 2));
-                    l8 += mum * face(ry, yv(j - 2), cmv, c0v);
-                }
-                {
-                    const T cmv = Cm[h - oz], c0v = Cm[h], cpv = Cm[h + oz];
-                    l11 += mum * face(wpz, cmv, c0v, cpv);
-                    l10 += mum * face(wnz, cmv, c0v, cpv);
-                    l9 += mum * face(qz, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
-                    l12 += mum * face(rz, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
-                }
-            }
-            const T cx = kc.dt2d[0], cy = kc.dt2d[1], cz = kc.dt2d[2];
-            const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
-            put(PS_SF + 0, (l1 * (T(-1) + su2) + l2 * (T(-1) - su2)) * cx);    // -> u(i)
-            put(PS_SF + 1, (l3 * (T(1) - su1) + l4 * (T(1) + su1)) * cx);      // -> u(i-1)
-            put(PS_SF + 2, (l5 * (T(-1) + sv2) + l6 * (T(-1) - sv2)) * cy);    // -> v(j)
-            put(PS_SF + 3, (l7 * (T(1) - sv1) + l8 * (T(1) + sv1)) * cy);      // -> v(j-1)
-            put(PS_SF + 4, (l9 * (T(-1) + sw2) + l10 * (T(-1) - sw2)) * cz);   // -> w(k)
-            put(PS_SF + 5, (l11 * (T(1) - sw1) + l12 * (T(1) + sw1)) * cz);    // -> w(k-1)
         }
     }
     block_atomic_add(gwi, a.grad + 0);
     block_atomic_add(gl2, a.grad + 2);
 }
 
+// Pass 1b: the 13 Cstar weights of the cell (the same for the 6 components:
+// centre, x/y/z at offsets -2, -1, +1, +2) and the adjoint of the upwind
+// coefficients, from the mu of pass 1a.  Where mu vanishes the gather reads
+// the weights only multiplied by it, and they are stored as zero.
+template <typename T>
+__global__ void __launch_bounds__(256) k_polyadj_cstar(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
+    const int k = blockIdx.z + 1;
+    if (i > g.nx || j >= prow0(g) + prows(g)) return;
+    const size_t cs = (size_t)a.cs;
+    const int h = hix(g, i, j, k);
+    auto put = [&](int q, T v) { src[(size_t)q * cs + h] = v; };
+    const AdjCoef<T> &kc = a.kc;
+    T mu[6];
+    bool any = false;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        mu[m] = src[(size_t)(PS_MU + m) * cs + h];
+        any = any || mu[m] != T(0);
+    }
+    if (!any) {
+#pragma unroll
+        for (int q = PS_KC; q < PS_GU; ++q) put(q, T(0));
+#pragma unroll
+        for (int q = PS_SF; q < POLY_SRC; ++q) put(q, T(0));
+        return;
+    }
+    const T *U = a.U, *V = a.V, *W = a.W;
+    {
+        // Cstar: upwind coefficients s1..s12 and the selection codes
+        const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
+        const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
+        const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
+        const T sixth = T(1) / T(6);
+        const T s1 = (-u2 + fabs(u2)) * kc.dt2d[0], s2 = sixth + (-u2 - fabs(u2)) * kc.dt2d[0];
+        const T s3 = sixth + (u1 - fabs(u1)) * kc.dt2d[0], s4 = (u1 + fabs(u1)) * kc.dt2d[0];
+        const T s5 = (-v2 + fabs(v2)) * kc.dt2d[1], s6 = sixth + (-v2 - fabs(v2)) * kc.dt2d[1];
+        const T s7 = sixth + (v1 - fabs(v1)) * kc.dt2d[1], s8 = (v1 + fabs(v1)) * kc.dt2d[1];
+        const T s9 = (-w2 + fabs(w2)) * kc.dt2d[2], s10 = sixth + (-w2 - fabs(w2)) * kc.dt2d[2];
+        const T s11 = sixth + (w1 - fabs(w1)) * kc.dt2d[2], s12 = (w1 + fabs(w1)) * kc.dt2d[2];
+        const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
+        const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
+        const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
+        const int czm = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
+        const int czp = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
+        int jm = j - 1, jp = j + 1;
+        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+        const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
+        const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
+        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
+        const W3<T> wpx = wface_p<T>(isx), wnx = wface_n<T>(isx), wpy = wface_p<T>(isy), wny = wface_n<T>(isy);
+        const W3<T> wpz = wface_p<T>(isz), wnz = wface_n<T>(isz);
+        const W3<T> qx = wface_p<T>(cxp + 1), rx = wface_n<T>(cxm + 1), qy = wface_p<T>(cyp + 1), ry = wface_n<T>(cym + 1);
+        const W3<T> qz = wface_p<T>(czp + 1), rz = wface_n<T>(czm + 1);
+        // weights of one direction: own p / n faces (coefficients sp, sn),
+        // the + neighbour's p face (sq) and the - neighbour's n face (sr),
+        // at offsets -2, -1, +1, +2; the centre weights are summed in kcen
+        T kcen = T(0);
+        auto dirw = [&](W3<T> wp_, W3<T> wn_, W3<T> wq, W3<T> wr, T sp, T sn, T sq, T sr, int base) {
+            put(base + 0, sr * wr.m);
+            put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
+            put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
+            put(base + 3, sq * wq.p);
+            kcen += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
+        };
+        dirw(wpx, wnx, qx, rx, s3, s2, s1, s4, PS_KX);
+        dirw(wpy, wny, qy, ry, s7, s6, s5, s8, PS_KY);
+        dirw(wpz, wnz, qz, rz, s11, s10, s9, s12, PS_KZ);
+        put(PS_KC, kcen);
+        // adjoints of s1..s12: mu . (face value), faces rebuilt from C^n
+        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+        const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
+        T l1 = T(0), l2 = T(0), l3 = T(0), l4 = T(0), l5 = T(0), l6 = T(0);
+        T l7 = T(0), l8 = T(0), l9 = T(0), l10 = T(0), l11 = T(0), l12 = T(0);
+        auto face = [](W3<T> wt, T cmv, T c0v, T cpv) { return wt.m * cmv + wt.c * c0v + wt.p * cpv; };
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            const T *Cm = a.C + m * cs;
+            const T mum = mu[m];
+            {
+                const T cmv = Cm[h - ox], c0v = Cm[h], cpv = Cm[h + ox];
+                l3 += mum * face(wpx, cmv, c0v, cpv);
+                l2 += mum * face(wnx, cmv, c0v, cpv);
+                l1 += mum * face(qx, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+                l4 += mum * face(rx, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            }
+            if (!g.walls) {
+                const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+                const T cmv = Cm[h - oy], c0v = Cm[h], cpv = Cm[h + oy];
+                l7 += mum * face(wpy, cmv, c0v, cpv);
+                l6 += mum * face(wny, cmv, c0v, cpv);
+                l5 += mum * face(qy, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+                l8 += mum * face(ry, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            } else {
+                auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
+                const T cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
+                l7 += mum * face(wpy, cmv, c0v, cpv);
+                l6 += mum * face(wny, cmv, c0v, cpv);
+                l5 += mum * face(qy, c0v, cpv, yv(j + 2));
+                l8 += mum * face(ry, yv(j - 2), cmv, c0v);
+            }
+            {
+                const T cmv = Cm[h - oz], c0v = Cm[h], cpv = Cm[h + oz];
+                l11 += mum * face(wpz, cmv, c0v, cpv);
+                l10 += mum * face(wnz, cmv, c0v, cpv);
+                l9 += mum * face(qz, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
+                l12 += mum * face(rz, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
+            }
+        }
+        const T cx = kc.dt2d[0], cy = kc.dt2d[1], cz = kc.dt2d[2];
+        const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
+        put(PS_SF + 0, (l1 * (T(-1) + su2) + l2 * (T(-1) - su2)) * cx);    // -> u(i)
+        put(PS_SF + 1, (l3 * (T(1) - su1) + l4 * (T(1) + su1)) * cx);      // -> u(i-1)
+        put(PS_SF + 2, (l5 * (T(-1) + sv2) + l6 * (T(-1) - sv2)) * cy);    // -> v(j)
+        put(PS_SF + 3, (l7 * (T(1) - sv1) + l8 * (T(1) + sv1)) * cy);      // -> v(j-1)
+        put(PS_SF + 4, (l9 * (T(-1) + sw2) + l10 * (T(-1) - sw2)) * cz);   // -> w(k)
+        put(PS_SF + 5, (l11 * (T(1) - sw1) + l12 * (T(1) + sw1)) * cz);    // -> w(k-1)
+    }
+}
+
 template <typename T>
 struct PolyGatherArgs {
-    const T *src;             // POLY_SRC halo-layout arrays of k_polyadj_src (updated cells)
+    const T *src;             // POLY_SRC halo-layout arrays of k_polyadj_mu / _cstar (updated cells)
     T *lC;                    // out: adjoint of C^n (updated cells; zero elsewhere)
     T *lU, *lV, *lW;          // += the velocity adjoint (full halo box)
     int cs;

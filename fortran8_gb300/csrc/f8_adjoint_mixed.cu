@@ -23,8 +23,7 @@ namespace f8 {
 
 cudaError_t adjoint_fold_state_f(AdjStateF &A, const Dev &d, cudaStream_t s) {
     const Geo &g = d.g;
-    F8_CUDA_RET(fold(fold_set<float>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lW, BC_W}, {A.lP, BC_P}}), g, s));
-    return fold(fold_c(A.lC, d.cs), g, s);
+    return fold(fold_with_c(fold_set<float>({{A.lU, BC_U}, {A.lV, BC_V}, {A.lW, BC_W}, {A.lP, BC_P}}), A.lC, d.cs, 6), g, s);
 }
 
 cudaError_t take_interior_f(const float *src, float *dst, const Geo &g, int n, cudaStream_t s) {
@@ -150,7 +149,9 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         pa.kc = kc; pa.dtwi = (float)(dt / wi); pa.dtwi2 = (float)(dt / (wi * wi));
         dim3 pb(32, 4);
         const dim3 pg((g.nx + pb.x - 1) / pb.x, (prows(g) + pb.y - 1) / pb.y, g.nz);
-        k_polyadj_src<float><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
+        k_polyadj_mu<float><<<pg, pb, 0, s>>>(pa, A.work, g); count_launch();
+        const dim3 pb2(32, 8), pg2((g.nx + pb2.x - 1) / pb2.x, (prows(g) + pb2.y - 1) / pb2.y, g.nz);
+        k_polyadj_cstar<float><<<pg2, pb2, 0, s>>>(pa, A.work, g); count_launch();
         PolyGatherArgs<float> pga{};
         pga.src = A.work; pga.lC = A.lC2; pga.lU = A.lU; pga.lV = A.lV; pga.lW = A.lW; pga.cs = cs;
         k_polyadj_gather<float><<<nb, 256, 0, s>>>(pga, g); count_launch();

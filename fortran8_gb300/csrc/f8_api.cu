@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -187,6 +188,7 @@ struct f8_ctx {
     int stats_mode = 0, stats_n = 0, stats_max = 0;   // running statistics (f8_stats_begin)
     double *stats_sum = nullptr, *stats_probe = nullptr;
     GradMem gm;                        // f8_grad buffers
+    int grad_kept_segments = 0;        // mixed f8_grad: segments of the last call kept from its first pass
     long long last_newton_iters = 0, last_newton_unconv = 0;
     int last_poisson_iters = -1;
     std::string last_error;
@@ -1375,9 +1377,37 @@ cudaError_t grad_forward_step_mixed(f8_ctx *c, int step0, int s, int rec) {
     return cudaSuccess;
 }
 
+// Segments (the last R >= 1) whose tape the first forward pass keeps, so
+// that the reverse sweep recomputes only the nseg - R before them: as many as
+// fit, together with the checkpoints those others need, in the memory the
+// gradient's tape and checkpoints already hold plus 60 % of the device's free
+// memory.  F8_GRAD_KEEP_TAPE=0 in the environment keeps the last segment only.
+int kept_segments_mixed(f8_ctx *c, int K, int nseg) {
+    const char *env = std::getenv("F8_GRAD_KEEP_TAPE");
+    if (env && env[0] == '0') return 1;
+    const GradMem &G = c->gm;
+    const Dev &d = c->d;
+    const double cs = (double)d.cs, ni = (double)d.ni;
+    const double nfc = std::max(1.0, (double)d.nm * d.g.nz);
+    const double slot = MIXED_TAPE_FIELDS * cs * 4 + ni + 2.0 * d.g.nx * d.g.nz + 3 * nfc * 8;
+    const double ck = (15 * cs + 6 * ni) * 4;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return 1;
+    const double avail = G.K * slot + G.nck * ck + 0.6 * (double)fr;
+    for (int r = nseg; r > 1; --r) {
+        const int nck = r < nseg ? nseg - r + 1 : 0;
+        if ((double)r * K * slot + nck * ck <= avail) return r;
+    }
+    return 1;
+}
+
 // f8_grad on an FP32-mixed 3D context with the FFT solvers: the same
 // checkpointed schedule as the FP64 gradient, with the mixed forward step
-// (its tape written by the step itself) and the FP32 adjoint step.
+// (its tape written by the step itself) and the FP32 adjoint step.  The
+// first forward pass keeps the tape of the last R segments (slots
+// (seg - (nseg - R)) K ..); the segments before them are recomputed from
+// their checkpoints into slots 0 .. K-1, whose first owner has been swept
+// by then.
 int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w, const f8_fields *seed, double *J,
                double *dJ_dparams, f8_fields *dJ_dstate, double *drag) {
     Dev &d = c->d;
@@ -1385,7 +1415,10 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
     const size_t cs = d.cs, ni = d.ni;
     const int K = checkpoint_every == 0 ? nsteps : std::min(checkpoint_every, nsteps);
     const int nseg = (nsteps + K - 1) / K;
-    if (int st = grad_alloc_mixed(c, K, nseg, nsteps)) return st;
+    const int R = kept_segments_mixed(c, K, nseg);
+    const int nrec = nseg - R;                       // segments recomputed from a checkpoint
+    if (int st = grad_alloc_mixed(c, R * K, nrec > 0 ? nrec + 1 : 0, nsteps)) return st;
+    c->grad_kept_segments = R;
     if (int st = ensure_drag(c, nsteps)) return st;
     GradMem &G = c->gm;
     AdjStateF &A = G.AF;
@@ -1402,14 +1435,16 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
     API_CUDA(c, cudaMemcpyAsync(&cnt0, d.cnt, sizeof(cnt0), cudaMemcpyDeviceToHost, c->s));
     API_CUDA(c, cudaStreamSynchronize(c->s));
     const int step0 = c->step;
-    // forward: checkpoints at the segment starts, the tape of the last segment
+    // forward: checkpoints at the starts of the segments to recompute, the
+    // tape of the kept ones
     for (int seg = 0; seg < nseg; ++seg) {
         const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
-        const bool last = seg == nseg - 1;
-        if (!last) API_CUDA(c, ck_copy_mixed(c, seg, true));
-        for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step_mixed(c, step0, s, last ? s - s0 : -1));
+        const bool kept = seg >= nrec;
+        if (!kept) API_CUDA(c, ck_copy_mixed(c, seg, true));
+        for (int s = s0; s < s1; ++s)
+            API_CUDA(c, grad_forward_step_mixed(c, step0, s, kept ? (seg - nrec) * K + s - s0 : -1));
     }
-    if (nseg > 1) API_CUDA(c, ck_copy_mixed(c, nseg - 1, true));   // final state
+    if (nrec > 0) API_CUDA(c, ck_copy_mixed(c, nrec, true));   // final state
     // adjoint of the final state
     for (float *p : {A.lU, A.lV, A.lW, A.lP}) API_CUDA(c, cudaMemsetAsync(p, 0, cs * sizeof(float), c->s));
     API_CUDA(c, cudaMemsetAsync(A.lC, 0, 6 * cs * sizeof(float), c->s));
@@ -1447,12 +1482,13 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
     const bool polymer = c->phys.beta != 1.0;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int s0 = seg * K, s1 = std::min(nsteps, s0 + K);
-        if (seg != nseg - 1) {
+        const int base = seg >= nrec ? (seg - nrec) * K : 0;
+        if (seg < nrec) {
             API_CUDA(c, ck_copy_mixed(c, seg, false));
             for (int s = s0; s < s1; ++s) API_CUDA(c, grad_forward_step_mixed(c, step0, s, s - s0));
         }
         for (int s = s1 - 1; s >= s0; --s) {
-            const int rec = s - s0;
+            const int rec = base + s - s0;
             const MixTape t = tape_slot_mixed(c, rec);
             const bool ab2_first = (step0 + s + 1 == 1) && c->phys.ab2_start;
             if (ab2_first) {
@@ -1476,7 +1512,7 @@ int grad_mixed(f8_ctx *c, int nsteps, int checkpoint_every, const double *drag_w
             if (polymer) std::swap(A.lC, A.lC2);
         }
     }
-    if (nseg > 1) API_CUDA(c, ck_copy_mixed(c, nseg - 1, false));
+    if (nrec > 0) API_CUDA(c, ck_copy_mixed(c, nrec, false));
     c->step = step0 + nsteps;
     // results
     std::vector<double> hd((size_t)std::max<size_t>(nw, 1));

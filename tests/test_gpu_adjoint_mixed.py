@@ -19,8 +19,9 @@ itself, the 128 x 64 x 64 channel over 400 steps from C = I, at 1e-4:
   adjoint, per parameter, with and without the AB2 start step, on the channel
   and the periodic box, and at full size on the adjoint workload;
 * the adjoint of the whole initial state (seeded final-state adjoints);
-* checkpoint intervals agree, and the state f8_grad leaves equals f8_step's
-  bit for bit;
+* checkpoint intervals agree, with the tapes of the earlier segments kept
+  from the first forward pass or recomputed, and the state f8_grad leaves
+  equals f8_step's bit for bit;
 * central differences of the FP64 forward (relative step 1e-4).
 """
 from __future__ import annotations
@@ -103,10 +104,16 @@ def test_mixed_state_vjp_matches_fp64(gpu, oracle):
     assert max(errs.values()) < TOL_STATE, errs
 
 
-def test_mixed_checkpoints_agree_and_state_advances(gpu, oracle):
+def test_mixed_checkpoints_agree_and_state_advances(gpu, oracle, monkeypatch):
     w, st, step0 = case("channel", oracle)
     n = 6
+    # the first forward pass keeps the tape of every segment that fits in
+    # memory (here all of them); F8_GRAD_KEEP_TAPE=0 keeps the last one only,
+    # so that the others are recomputed from their checkpoints
     res = [grad(gpu, w, st, step0, n, abi.F8_MIXED, K=K) for K in (1, 4, 0)]
+    monkeypatch.setenv("F8_GRAD_KEEP_TAPE", "0")
+    res += [grad(gpu, w, st, step0, n, abi.F8_MIXED, K=K) for K in (1, 4)]
+    monkeypatch.delenv("F8_GRAD_KEEP_TAPE")
     with Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED) as s:
         s.load(st, step0)
         _, drag = s.step(n)
