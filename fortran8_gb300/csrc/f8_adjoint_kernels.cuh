@@ -668,7 +668,7 @@ struct MomGatherArgs {
 // polymer the adjoint of C0 (stress divergence) followed by the C0 = f(C) C - I
 // linearisation.
 template <typename T>
-__global__ void __launch_bounds__(256) k_momadj_gather(MomGatherArgs<T> a, Geo g) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_momadj_gather(MomGatherArgs<T> a, Geo g) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int cs = a.cs;
     T g_coef = T(0), g_l2 = T(0);
@@ -1015,7 +1015,7 @@ __global__ void __launch_bounds__(128) k_polyadj_mu(PolyAdjArgs<T> a, T *__restr
 // coefficients, from the mu of pass 1a.  Where mu vanishes the gather reads
 // the weights only multiplied by it, and they are stored as zero.
 template <typename T>
-__global__ void __launch_bounds__(256) k_polyadj_cstar(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_polyadj_cstar(PolyAdjArgs<T> a, T *__restrict__ src, Geo g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
     const int k = blockIdx.z + 1;
@@ -1039,97 +1039,84 @@ __global__ void __launch_bounds__(256) k_polyadj_cstar(PolyAdjArgs<T> a, T *__re
         return;
     }
     const T *U = a.U, *V = a.V, *W = a.W;
-    {
-        // Cstar: upwind coefficients s1..s12 and the selection codes
-        const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
-        const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
-        const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
-        const T sixth = T(1) / T(6);
-        const T s1 = (-u2 + fabs(u2)) * kc.dt2d[0], s2 = sixth + (-u2 - fabs(u2)) * kc.dt2d[0];
-        const T s3 = sixth + (u1 - fabs(u1)) * kc.dt2d[0], s4 = (u1 + fabs(u1)) * kc.dt2d[0];
-        const T s5 = (-v2 + fabs(v2)) * kc.dt2d[1], s6 = sixth + (-v2 - fabs(v2)) * kc.dt2d[1];
-        const T s7 = sixth + (v1 - fabs(v1)) * kc.dt2d[1], s8 = (v1 + fabs(v1)) * kc.dt2d[1];
-        const T s9 = (-w2 + fabs(w2)) * kc.dt2d[2], s10 = sixth + (-w2 - fabs(w2)) * kc.dt2d[2];
-        const T s11 = sixth + (w1 - fabs(w1)) * kc.dt2d[2], s12 = (w1 + fabs(w1)) * kc.dt2d[2];
-        const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
-        const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
-        const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
-        const int czm = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
-        const int czp = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
-        int jm = j - 1, jp = j + 1;
-        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
-        const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
-        const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
-        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
-        const W3<T> wpx = wface_p<T>(isx), wnx = wface_n<T>(isx), wpy = wface_p<T>(isy), wny = wface_n<T>(isy);
-        const W3<T> wpz = wface_p<T>(isz), wnz = wface_n<T>(isz);
-        const W3<T> qx = wface_p<T>(cxp + 1), rx = wface_n<T>(cxm + 1), qy = wface_p<T>(cyp + 1), ry = wface_n<T>(cym + 1);
-        const W3<T> qz = wface_p<T>(czp + 1), rz = wface_n<T>(czm + 1);
-        // weights of one direction: own p / n faces (coefficients sp, sn),
-        // the + neighbour's p face (sq) and the - neighbour's n face (sr),
-        // at offsets -2, -1, +1, +2; the centre weights are summed in kcen
-        T kcen = T(0);
-        auto dirw = [&](W3<T> wp_, W3<T> wn_, W3<T> wq, W3<T> wr, T sp, T sn, T sq, T sr, int base) {
-            put(base + 0, sr * wr.m);
-            put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
-            put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
-            put(base + 3, sq * wq.p);
-            kcen += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
-        };
-        dirw(wpx, wnx, qx, rx, s3, s2, s1, s4, PS_KX);
-        dirw(wpy, wny, qy, ry, s7, s6, s5, s8, PS_KY);
-        dirw(wpz, wnz, qz, rz, s11, s10, s9, s12, PS_KZ);
-        put(PS_KC, kcen);
-        // adjoints of s1..s12: mu . (face value), faces rebuilt from C^n
-        const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
-        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
-        const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
-        T l1 = T(0), l2 = T(0), l3 = T(0), l4 = T(0), l5 = T(0), l6 = T(0);
-        T l7 = T(0), l8 = T(0), l9 = T(0), l10 = T(0), l11 = T(0), l12 = T(0);
+    // Cstar: upwind coefficients s1..s12 and the selection codes
+    const T u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
+    const T v1 = rowv(V, g, i, j - 1, k), v2 = V[h];
+    const T w1 = W[hix(g, i, j, k - 1)], w2 = W[h];
+    const T sixth = T(1) / T(6);
+    const int cself = code_of(a.codes, a.codes_g, g, i, j, k);
+    const int cxm = code_of(a.codes, a.codes_g, g, wrapx(g, i - 1), j, k) & 3;
+    const int cxp = code_of(a.codes, a.codes_g, g, wrapx(g, i + 1), j, k) & 3;
+    const int czm = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k - 1)) >> 4) & 3;
+    const int czp = (code_of(a.codes, a.codes_g, g, i, j, wrapz(g, k + 1)) >> 4) & 3;
+    int jm = j - 1, jp = j + 1;
+    if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+    const int cym = jm < 0 ? 3 : (code_of(a.codes, a.codes_g, g, i, jm, k) >> 2) & 3;
+    const int cyp = jp > g.ny + 1 ? 3 : (code_of(a.codes, a.codes_g, g, i, jp, k) >> 2) & 3;
+    const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1, isz = ((cself >> 4) & 3) + 1;
+    // One direction at a time (x, y, z), so that only its face weights and
+    // sums are live: the weights of the cell's own p / n faces (coefficients
+    // sp, sn), of the + neighbour's p face (sq) and of the - neighbour's n
+    // face (sr) at offsets -2, -1, +1, +2, the centre weights summed in kcen;
+    // then the adjoints of the direction's four upwind coefficients,
+    // mu . (face value) with the faces rebuilt from C^n at positions
+    // cm, c0, cp (own faces), q-, q0, q+ (+ neighbour's) and r-, r0, r+.
+    T kcen = T(0);
+    auto direction = [&](int isd, int cq, int cr, T vel2, T vel1, T dt2d, int base, int sf, auto &&cval) {
+        const T sq = (-vel2 + fabs(vel2)) * dt2d, sn = sixth + (-vel2 - fabs(vel2)) * dt2d;
+        const T sp = sixth + (vel1 - fabs(vel1)) * dt2d, sr = (vel1 + fabs(vel1)) * dt2d;
+        const W3<T> wp_ = wface_p<T>(isd), wn_ = wface_n<T>(isd);
+        const W3<T> wq = wface_p<T>(cq + 1), wr = wface_n<T>(cr + 1);
+        put(base + 0, sr * wr.m);
+        put(base + 1, sp * wp_.m + sn * wn_.m + sr * wr.c);
+        put(base + 2, sp * wp_.p + sn * wn_.p + sq * wq.c);
+        put(base + 3, sq * wq.p);
+        kcen += sp * wp_.c + sn * wn_.c + sq * wq.m + sr * wr.p;
         auto face = [](W3<T> wt, T cmv, T c0v, T cpv) { return wt.m * cmv + wt.c * c0v + wt.p * cpv; };
+        T lq = T(0), ln = T(0), lp_ = T(0), lr = T(0);
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
-            const T *Cm = a.C + m * cs;
+            T v[9];
+            cval(a.C + m * cs, v);
             const T mum = mu[m];
-            {
-                const T cmv = Cm[h - ox], c0v = Cm[h], cpv = Cm[h + ox];
-                l3 += mum * face(wpx, cmv, c0v, cpv);
-                l2 += mum * face(wnx, cmv, c0v, cpv);
-                l1 += mum * face(qx, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
-                l4 += mum * face(rx, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
-            }
-            if (!g.walls) {
-                const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
-                const T cmv = Cm[h - oy], c0v = Cm[h], cpv = Cm[h + oy];
-                l7 += mum * face(wpy, cmv, c0v, cpv);
-                l6 += mum * face(wny, cmv, c0v, cpv);
-                l5 += mum * face(qy, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
-                l8 += mum * face(ry, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
-            } else {
-                auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
-                const T cmv = yv(j - 1), c0v = Cm[h], cpv = yv(j + 1);
-                l7 += mum * face(wpy, cmv, c0v, cpv);
-                l6 += mum * face(wny, cmv, c0v, cpv);
-                l5 += mum * face(qy, c0v, cpv, yv(j + 2));
-                l8 += mum * face(ry, yv(j - 2), cmv, c0v);
-            }
-            {
-                const T cmv = Cm[h - oz], c0v = Cm[h], cpv = Cm[h + oz];
-                l11 += mum * face(wpz, cmv, c0v, cpv);
-                l10 += mum * face(wnz, cmv, c0v, cpv);
-                l9 += mum * face(qz, Cm[hzp - oz], Cm[hzp], Cm[hzp + oz]);
-                l12 += mum * face(rz, Cm[hzm - oz], Cm[hzm], Cm[hzm + oz]);
-            }
+            lp_ += mum * face(wp_, v[0], v[1], v[2]);
+            ln += mum * face(wn_, v[0], v[1], v[2]);
+            lq += mum * face(wq, v[3], v[4], v[5]);
+            lr += mum * face(wr, v[6], v[7], v[8]);
         }
-        const T cx = kc.dt2d[0], cy = kc.dt2d[1], cz = kc.dt2d[2];
-        const T su2 = sgn(u2), su1 = sgn(u1), sv2 = sgn(v2), sv1 = sgn(v1), sw2 = sgn(w2), sw1 = sgn(w1);
-        put(PS_SF + 0, (l1 * (T(-1) + su2) + l2 * (T(-1) - su2)) * cx);    // -> u(i)
-        put(PS_SF + 1, (l3 * (T(1) - su1) + l4 * (T(1) + su1)) * cx);      // -> u(i-1)
-        put(PS_SF + 2, (l5 * (T(-1) + sv2) + l6 * (T(-1) - sv2)) * cy);    // -> v(j)
-        put(PS_SF + 3, (l7 * (T(1) - sv1) + l8 * (T(1) + sv1)) * cy);      // -> v(j-1)
-        put(PS_SF + 4, (l9 * (T(-1) + sw2) + l10 * (T(-1) - sw2)) * cz);   // -> w(k)
-        put(PS_SF + 5, (l11 * (T(1) - sw1) + l12 * (T(1) + sw1)) * cz);    // -> w(k-1)
+        const T s2 = sgn(vel2), s1 = sgn(vel1);
+        put(sf + 0, (lq * (T(-1) + s2) + ln * (T(-1) - s2)) * dt2d);    // -> the + face velocity
+        put(sf + 1, (lp_ * (T(1) - s1) + lr * (T(1) + s1)) * dt2d);     // -> the - face velocity
+    };
+    const int ox = 1, oy = g.sx, oz = g.sx * g.sy;
+    const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+    direction(isx, cxp, cxm, u2, u1, kc.dt2d[0], PS_KX, PS_SF + 0, [&](const T *Cm, T (&v)[9]) {
+        v[0] = Cm[h - ox]; v[1] = Cm[h]; v[2] = Cm[h + ox];
+        v[3] = Cm[hxp - ox]; v[4] = Cm[hxp]; v[5] = Cm[hxp + ox];
+        v[6] = Cm[hxm - ox]; v[7] = Cm[hxm]; v[8] = Cm[hxm + ox];
+    });
+    if (!g.walls) {
+        const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k);
+        direction(isy, cyp, cym, v2, v1, kc.dt2d[1], PS_KY, PS_SF + 2, [&](const T *Cm, T (&v)[9]) {
+            v[0] = Cm[h - oy]; v[1] = Cm[h]; v[2] = Cm[h + oy];
+            v[3] = Cm[hyp - oy]; v[4] = Cm[hyp]; v[5] = Cm[hyp + oy];
+            v[6] = Cm[hym - oy]; v[7] = Cm[hym]; v[8] = Cm[hym + oy];
+        });
+    } else {
+        direction(isy, cyp, cym, v2, v1, kc.dt2d[1], PS_KY, PS_SF + 2, [&](const T *Cm, T (&v)[9]) {
+            auto yv = [&](int jj) { return rowv(Cm, g, i, jj, k); };
+            v[0] = yv(j - 1); v[1] = Cm[h]; v[2] = yv(j + 1);
+            v[3] = v[1]; v[4] = v[2]; v[5] = yv(j + 2);
+            v[6] = yv(j - 2); v[7] = v[0]; v[8] = v[1];
+        });
     }
+    const int hzm = hix(g, i, j, wrapz(g, k - 1)), hzp = hix(g, i, j, wrapz(g, k + 1));
+    direction(isz, czp, czm, w2, w1, kc.dt2d[2], PS_KZ, PS_SF + 4, [&](const T *Cm, T (&v)[9]) {
+        v[0] = Cm[h - oz]; v[1] = Cm[h]; v[2] = Cm[h + oz];
+        v[3] = Cm[hzp - oz]; v[4] = Cm[hzp]; v[5] = Cm[hzp + oz];
+        v[6] = Cm[hzm - oz]; v[7] = Cm[hzm]; v[8] = Cm[hzm + oz];
+    });
+    put(PS_KC, kcen);
 }
 
 template <typename T>
