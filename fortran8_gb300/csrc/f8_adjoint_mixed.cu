@@ -88,12 +88,11 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
     F8_CUDA_RET(fold(fold_set<float>({{A.lUp[0], BC_U}, {A.lUp[1], BC_V}, {A.lUp[2], BC_W}}), g, s));
     // 4. Helmholtz: the three solves as the forward's parallel branches
     {
-        const float *src[3];
-        for (int c = 0; c < 3; ++c) {
-            float *pk = A.pack + (size_t)c * d.ni;
-            k_pack<float><<<adj_cells(g, blk), blk, 0, s>>>(A.lUp[c], pk, g); count_launch();
-            src[c] = pk;
-        }
+        float *pk[3];
+        for (int c = 0; c < 3; ++c) pk[c] = A.pack + (size_t)c * d.ni;
+        k_pack3<float><<<adj_cells(g, blk), blk, 0, s>>>(A.lUp[0], A.lUp[1], A.lUp[2], pk[0], pk[1], pk[2], g);
+        count_launch();
+        const float *src[3] = {pk[0], pk[1], pk[2]};
         F8_CUDA_RET(mixed_helmholtz3(d, src, A.lQ, s));
     }
     // 3. IBM

@@ -2041,7 +2041,8 @@ cudaError_t count_nonfinite_f(const float *a, int n, unsigned long long *out, cu
 __global__ void k_tape_ua(const float *__restrict__ Uh, const float *__restrict__ Ul, const float *__restrict__ Vh,
                           const float *__restrict__ Vl, const float *__restrict__ Wh, const float *__restrict__ Wl,
                           const float *__restrict__ Qu, const float *__restrict__ Qv, const float *__restrict__ Qw,
-                          float *__restrict__ ou, float *__restrict__ ov, float *__restrict__ ow, Geo g, df uw2) {
+                          float *__restrict__ ou, float *__restrict__ ov, float *__restrict__ ow,
+                          float *__restrict__ tu, float *__restrict__ tv, float *__restrict__ tw, Geo g, df uw2) {
     const int cs = g.sx * g.sy * g.sz;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cs) return;
@@ -2052,17 +2053,28 @@ __global__ void k_tape_ua(const float *__restrict__ Uh, const float *__restrict_
     ou[t] = a.hi + a.lo;
     ov[t] = b.hi + b.lo;
     ow[t] = c.hi + c.lo;
+    // the velocity of the start of the step (high parts; unchanged until the
+    // projection)
+    tu[t] = Uh[t];
+    tv[t] = Vh[t];
+    tw[t] = Wh[t];
 }
 
 // U* = U^n + dU: the increments have no halo pass; their readers wrap x and z
 // (and y when periodic), and the wall solves write the ghost rows
-__global__ void k_tape_up(const float *__restrict__ U, const float *__restrict__ D, float *__restrict__ out, Geo g) {
+struct TapeUp {
+    const float *U[3], *D[3];
+    float *out[3];
+};
+// the three Helmholtz solutions U^n + dU (blockIdx.y: component)
+__global__ void k_tape_up(TapeUp a, Geo g) {
     const int cs = g.sx * g.sy * g.sz;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cs) return;
+    const int c = blockIdx.y;
     const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
     const int jj = g.walls ? j : wrapy(g, j);
-    out[t] = U[t] + D[hix(g, wrapx(g, i), jj, wrapz(g, k))];
+    a.out[c][t] = a.U[c][t] + a.D[c][hix(g, wrapx(g, i), jj, wrapz(g, k))];
 }
 
 // Phi (hi part) with the periodic wrap and the Neumann copy at the walls
@@ -2086,12 +2098,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     const MixTape *tp = o.tape;
     const size_t hbf = (size_t)d.cs * sizeof(float);
     const unsigned tnb = (unsigned)((d.cs + 255) / 256);
-    if (tp) {
-        F8_CUDA_RET(cudaMemcpyAsync(tp->U, d.Uf, hbf, cudaMemcpyDeviceToDevice, s));
-        F8_CUDA_RET(cudaMemcpyAsync(tp->V, d.Vf, hbf, cudaMemcpyDeviceToDevice, s));
-        F8_CUDA_RET(cudaMemcpyAsync(tp->W, d.Wf, hbf, cudaMemcpyDeviceToDevice, s));
-        if (o.polymer) F8_CUDA_RET(cudaMemcpyAsync(tp->C, d.Cf, 6 * hbf, cudaMemcpyDeviceToDevice, s));
-    }
+    if (tp && o.polymer) F8_CUDA_RET(cudaMemcpyAsync(tp->C, d.Cf, 6 * hbf, cudaMemcpyDeviceToDevice, s));
     mark(0);
     // wall channel: the ghost rows' codes and update run on a side stream
     // beside the interior kernels (they read the state and the interior codes
@@ -2175,7 +2182,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     }
     if (tp) {
         k_tape_ua<<<tnb, 256, 0, s>>>(d.Uf, d.Ul, d.Vf, d.Vl, d.Wf, d.Wl, d.Qf[0], d.Qf[1], d.Qf[2], tp->Ua[0],
-                                      tp->Ua[1], tp->Ua[2], g, df_from_d(2.0 * g.uwall)); count_launch();
+                                      tp->Ua[1], tp->Ua[2], tp->U, tp->V, tp->W, g, df_from_d(2.0 * g.uwall));
+        count_launch();
     }
     mark(3);
     // IBM direct forcing and the Helmholtz solves; with NS > 1 forcing
@@ -2262,8 +2270,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             }
         }
         if (tp) {
-            const float *uh[3] = {d.Uf, d.Vf, d.Wf};
-            for (int c = 0; c < 3; ++c) { k_tape_up<<<tnb, 256, 0, s>>>(uh[c], d.dUf[c], tp->Up[c], g); count_launch(); }
+            const TapeUp a{{d.Uf, d.Vf, d.Wf}, {d.dUf[0], d.dUf[1], d.dUf[2]}, {tp->Up[0], tp->Up[1], tp->Up[2]}};
+            k_tape_up<<<dim3(tnb, 3), 256, 0, s>>>(a, g); count_launch();
         }
     }
     mark(5);
