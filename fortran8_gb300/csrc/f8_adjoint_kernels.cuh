@@ -203,6 +203,17 @@ cudaError_t fold(const FoldSet<T> &f, const Geo &g, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// the z pass of fold alone: for a set whose values outside the z faces'
+// planes lie only in interior columns below row NY, where the y and x passes
+// would move and zero nothing
+template <typename T>
+cudaError_t fold_z_only(const FoldSet<T> &f, const Geo &g, cudaStream_t s) {
+    const unsigned n = (unsigned)f.n;
+    if (n == 0) return cudaSuccess;
+    k_fold_z<T><<<dim3((g.sx * g.sy + 255) / 256, n), 256, 0, s>>>(f, g); count_launch();
+    return cudaGetLastError();
+}
+
 // transpose of the periodic x and z copies of every row (k_bc_c_pet_xz): the
 // wall ghost rows stay (they are updated cells)
 template <typename T>

@@ -108,7 +108,11 @@ cudaError_t step_mixed_adjoint(Dev &d, AdjStateF &A, const MixTape &t, const dou
         ia.grad = A.grad;
         ia.d3 = 1;
         k_ibm_adj<float><<<dim3((d.nm + 127) / 128, g.nz, 3), 128, 0, s>>>(ia, g); count_launch();
-        F8_CUDA_RET(fold(fold_set<float>({{A.lUa[0], BC_U}, {A.lUa[1], BC_V}, {A.lUa[2], BC_W}}), g, s));
+        // the markers' stencils reach the ghost planes in z; where they reach
+        // no ghost column or row (nor row NY, which the V wall rule zeroes)
+        // the y and x passes have nothing to do
+        const FoldSet<float> fa = fold_set<float>({{A.lUa[0], BC_U}, {A.lUa[1], BC_V}, {A.lUa[2], BC_W}});
+        F8_CUDA_RET(d.ibm_edge ? fold(fa, g, s) : fold_z_only(fa, g, s));
     }
     // 2. momentum right-hand side: per-cell sources, then the gather of the
     // velocity, pressure and (with the polymer) C0 / C adjoints

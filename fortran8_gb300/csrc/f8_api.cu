@@ -596,6 +596,7 @@ int setup(f8_ctx *c) {
                         for (int ii = i0; ii <= i0 + 2; ++ii) {
                             if (ii < 0 || ii >= g.sx || jj < 0 || jj >= g.sy) return F8_ERR_ARG;  // marker too close to the edge
                             lists[ii + g.sx * jj].push_back(m);
+                            if (ii == 0 || ii == g.sx - 1 || jj == 0 || jj >= g.ny) d.ibm_edge = 1;
                         }
                 }
             for (int q = 0; q < ncol; ++q) off[q + 1] = off[q] + (int)lists[q].size();

@@ -40,6 +40,7 @@ struct Dev {
     double *mvol;                          // per marker: the volume its force is spread with
     double *cylvol;                        // per cylinder: the marker volume of its drag
     int ibm_repeats;                       // direct-forcing iterations per step (NS)
+    int ibm_edge;                          // some marker stencil reaches a ghost column, a ghost row or row NY
     float *Qpre[3];                        // mixed, NS > 1: the right-hand sides before spreading
     // mixed-precision state and work (F8_MIXED): the state as df64 pairs
     // (hi, lo) of FP32 halo fields
