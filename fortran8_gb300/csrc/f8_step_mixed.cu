@@ -2071,10 +2071,15 @@ __global__ void k_tape_up(TapeUp a, Geo g) {
     const int cs = g.sx * g.sy * g.sz;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cs) return;
+    // the component's pointers by selects (an index into the parameter
+    // arrays would copy them to local memory)
     const int c = blockIdx.y;
+    const float *U = c == 0 ? a.U[0] : (c == 1 ? a.U[1] : a.U[2]);
+    const float *D = c == 0 ? a.D[0] : (c == 1 ? a.D[1] : a.D[2]);
+    float *out = c == 0 ? a.out[0] : (c == 1 ? a.out[1] : a.out[2]);
     const int i = t % g.sx, j = (t / g.sx) % g.sy, k = t / (g.sx * g.sy);
     const int jj = g.walls ? j : wrapy(g, j);
-    a.out[c][t] = a.U[c][t] + a.D[c][hix(g, wrapx(g, i), jj, wrapz(g, k))];
+    out[t] = U[t] + D[hix(g, wrapx(g, i), jj, wrapz(g, k))];
 }
 
 // Phi (hi part) with the periodic wrap and the Neumann copy at the walls
