@@ -465,6 +465,7 @@ int setup(f8_ctx *c) {
         API_CUDA(c, setup_staged_projection(d));
         if (g.walls) d.fused_planes = (d.plane_cl > 0 || (size_t)12 * ((g.ny + 2) | 1) * g.nz <= (size_t)optin) ? 1 : 0;
         else d.fused_planes = (size_t)8 * (g.ny + 1) * g.nz <= (size_t)optin ? 1 : 0;
+        if (g.dim == 2) d.fused_planes = 0;   // 2D: the line transforms and tridiagonal sweeps
         if (d.fused_planes) {
             // side streams and spectra of the V and W Helmholtz solves
             for (int b = 0; b < 2; ++b) {
@@ -584,6 +585,7 @@ int setup(f8_ctx *c) {
         }
         const int ncomp = g.dim == 3 ? 3 : 2;
         const int ncol = g.sx * g.sy;
+        const double dvol_m = g.dim == 3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy;   // cell volume
         for (int comp = 0; comp < 3; ++comp) {
             API_CUDA(c, c->alloc(&d.Fc[comp], (size_t)nm * g.nz));
             std::vector<int> off(ncol + 1, 0), idx;
@@ -636,8 +638,8 @@ int setup(f8_ctx *c) {
                         const float fx = (float)wx[3 * (size_t)m + (ii - i0v[m])];
                         const float fy = (float)wy[3 * (size_t)m + (jj - j0v[m])];
                         cw[e] = (double)(fx * fy);
-                        if (c->phys.ibm_volume == F8_IBM_ARC_VOLUME)   // spreading volume / dX^3
-                            cw[e] = (double)(fx * fy * (float)(c->cyl_vol[mc[m]] / (g.dx * g.dx * g.dx)));
+                        if (c->phys.ibm_volume == F8_IBM_ARC_VOLUME)   // spreading volume / cell volume
+                            cw[e] = (double)(fx * fy * (float)(c->cyl_vol[mc[m]] / dvol_m));
                     }
                 }
                 if (int st = upload_f(c, &d.csr_w[comp], cw)) return st;
@@ -808,7 +810,8 @@ int f8_create(f8_ctx **out, const f8_grid *g, const f8_phys *ph, const f8_cyl *c
     *out = nullptr;
     int st = validate(g, ph, ncyl, cy, prec, poisson);
     if (st) return st;
-    if (prec == F8_MIXED && g->dim != 3) return F8_ERR_UNSUPPORTED;
+    // the 2D mixed step solves its pressure with the FFT solvers only
+    if (prec == F8_MIXED && g->dim == 2 && poisson != F8_POISSON_FFT) return F8_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();

@@ -20,6 +20,7 @@
 // with a df64 residual (iterative refinement), so that the projected velocity
 // is divergence-free to the df64 rounding level.
 #include <algorithm>
+#include <cfloat>
 #include <cstdio>
 #include <cstdlib>
 #include "../../include/f8.h"
@@ -84,7 +85,25 @@ __device__ inline float peterlin_f(float x0, float x3, float x5, float lp2f, dou
     return (float)((lp2 - 3.0) / (lp2 - trd));
 }
 
+// The 2D model's Peterlin factor (L^2 - 2)/(L^2 - tr C), tr C = c11 + c22
+// (fenep_2d.f90), FP64 near the limit as peterlin_f
+__device__ inline float peterlin2_f(float x0, float x2, float lp2f, double lp2) {
+    float tr = x0 + x2;
+    float den = lp2f - tr;
+    if (den > 0.01f * lp2f) return (lp2f - 2.0f) / den;
+    double trd = (double)x0 + (double)x2;
+    return (float)((lp2 - 2.0) / (lp2 - trd));
+}
+
+// f of NC stored components: 6 (3D: xx xy xz yy yz zz) or 3 (2D: xx xy yy)
+template <int NC>
+__device__ inline float peterlin_nc(const float (&x)[NC], float lp2f, double lp2) {
+    if constexpr (NC == 6) return peterlin_f(x[0], x[3], x[5], lp2f, lp2);
+    else return peterlin2_f(x[0], x[2], lp2f, lp2);
+}
+
 // C halo (C_PBM / linear extrapolation at walls) and f on the halo cells
+template <int NC>
 __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
@@ -99,37 +118,39 @@ __global__ void k_bc_c_pet_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     else if (j == 0) { s1 = hix(g, ii, 1, kk); s2 = hix(g, ii, 2, kk); }
     else { s1 = hix(g, ii, g.ny, kk); s2 = hix(g, ii, g.ny - 1, kk); }
     // every component's sources before the first store
-    float x[6];
+    float x[NC];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) {
+    for (int m = 0; m < NC; ++m) {
         const float *A = C + (size_t)m * cs;
         x[m] = s2 < 0 ? A[s1] : 2.0f * A[s1] - A[s2];
     }
 #pragma unroll
-    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
-    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+    for (int m = 0; m < NC; ++m) C[(size_t)m * cs + h] = x[m];
+    fpet[h] = peterlin_nc<NC>(x, (float)lp2, lp2);
 }
 
 // After the polymer update of a wall channel: the x and z halo cells of every
 // row (ghost rows included) as periodic copies, with their Peterlin factor;
 // the updated ghost rows are kept (extrapolated at the end of the step).
+template <int NC>
 __global__ void k_bc_c_pet_xz_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     int i, j, k;
     if (!halo_cell(g, t, i, j, k)) return;
     if ((j == 0 || j == g.sy - 1) && i >= 1 && i <= g.nx && k >= 1 && k <= g.nz) return;   // updated ghost cell
     const int h = hix(g, i, j, k), src = hix(g, wrapx(g, i), j, wrapz(g, k));
-    float x[6];
+    float x[NC];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) x[m] = C[(size_t)m * cs + src];
+    for (int m = 0; m < NC; ++m) x[m] = C[(size_t)m * cs + src];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
-    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+    for (int m = 0; m < NC; ++m) C[(size_t)m * cs + h] = x[m];
+    fpet[h] = peterlin_nc<NC>(x, (float)lp2, lp2);
 }
 
 // The wall extrapolation of the C ghost rows (C_kabe, fenep_2d.f90:1131-1143)
 // and their Peterlin factor, every x and z (the x/z halo copies of rows 1, 2,
 // NY-1, NY are already in place).
+template <int NC>
 __global__ void k_extrap_ghost_f(float *C, float *fpet, Geo g, int cs, double lp2) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * g.sx * g.sz) return;
@@ -137,15 +158,15 @@ __global__ void k_extrap_ghost_f(float *C, float *fpet, Geo g, int cs, double lp
     const int i = r % g.sx, k = r / g.sx;
     const int j = side ? g.ny + 1 : 0, j1 = side ? g.ny : 1, j2 = side ? g.ny - 1 : 2;
     const int h = hix(g, i, j, k), h1 = hix(g, i, j1, k), h2 = hix(g, i, j2, k);
-    float x[6];
+    float x[NC];
 #pragma unroll
-    for (int m = 0; m < 6; ++m) {
+    for (int m = 0; m < NC; ++m) {
         const float *A = C + (size_t)m * cs;
         x[m] = 2.0f * A[h1] - A[h2];
     }
 #pragma unroll
-    for (int m = 0; m < 6; ++m) C[(size_t)m * cs + h] = x[m];
-    fpet[h] = peterlin_f(x[0], x[3], x[5], (float)lp2, lp2);
+    for (int m = 0; m < NC; ++m) C[(size_t)m * cs + h] = x[m];
+    fpet[h] = peterlin_nc<NC>(x, (float)lp2, lp2);
 }
 
 // halo values (PBM / wall rules, fenep_2d.f90:1098-1129) of a df64 field;
@@ -227,10 +248,12 @@ __global__ void k_join_df(const float *hi, const float *lo, double *dst, int n) 
     dst[q] = (double)hi[q] + (double)lo[q];
 }
 
+template <int NC>
 __global__ void k_pet_all_f(const float *C, float *fpet, int cs, double lp2) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= cs) return;
-    fpet[h] = peterlin_f(C[h], C[3 * (size_t)cs + h], C[5 * (size_t)cs + h], (float)lp2, lp2);
+    if constexpr (NC == 6) fpet[h] = peterlin_f(C[h], C[3 * (size_t)cs + h], C[5 * (size_t)cs + h], (float)lp2, lp2);
+    else fpet[h] = peterlin2_f(C[h], C[2 * (size_t)cs + h], (float)lp2, lp2);
 }
 
 // ---------------------------------------------------------------------------
@@ -793,6 +816,235 @@ __global__ void __launch_bounds__(128) k_update_ghost3_f(const float *__restrict
 }
 
 // ---------------------------------------------------------------------------
+// Polymer, 2D (fenep_2d.f90:138-393) in FP32: the closed-form eigenvalues of
+// the 2 x 2 candidate faces, the "last candidate >= running best" rule, Cstar
+// with 1/4 weights, and the Newton iteration of the 3-unknown Lyapunov system
+// with its Jacobian assembled analytically (the FP64 step differentiates by
+// finite differences, which FP32 cannot resolve).
+
+__device__ inline float face_p_f(int idx, float cm, float c0, float cp) {
+    switch (idx) {
+    case 1: return c0 * 1.5f - cp * 0.5f;
+    case 2: return cm * 0.5f + c0 * 0.5f;
+    case 3: return cm * 0.25f + c0 - cp * 0.25f;
+    default: return c0;
+    }
+}
+__device__ inline float face_n_f(int idx, float cm, float c0, float cp) {
+    switch (idx) {
+    case 1: return c0 * 0.5f + cp * 0.5f;
+    case 2: return -cm * 0.5f + c0 * 1.5f;
+    case 3: return -cm * 0.25f + c0 + cp * 0.25f;
+    default: return c0;
+    }
+}
+
+// smaller eigenvalue of the symmetric 2 x 2 (a0 a1; a1 a2)
+__device__ inline float eig2_min_f(float a0, float a1, float a2) {
+    const float d = (a0 - a2) * (a0 - a2) + 4.0f * (a1 * a1);
+    return (a0 + a2 - sqrtf(d)) * 0.5f;
+}
+
+// the reference's index (0: no candidate qualified, the cell value)
+__device__ inline int select2_f(const float (&cm)[3], const float (&c0)[3], const float (&cp)[3]) {
+    int index = 0;
+    float best = 0.0f;
+#pragma unroll
+    for (int l = 1; l <= 3; ++l) {
+        float pt[3], nt[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            pt[m] = face_p_f(l, cm[m], c0[m], cp[m]);
+            nt[m] = face_n_f(l, cm[m], c0[m], cp[m]);
+        }
+        const float ep = eig2_min_f(pt[0], pt[1], pt[2]), en = eig2_min_f(nt[0], nt[1], nt[2]);
+        // NaN eigenvalues are skipped, as in the reference's minval
+        float mv = ep;
+        bool found = !isnan(ep);
+        if (!isnan(en) && (!found || en < mv)) { mv = en; found = true; }
+        if (found && mv >= best) { index = l; best = mv; }
+    }
+    return index;
+}
+
+// value of a C component at row jj of column (i, k): zero beyond the ghost
+// rows of a wall channel
+__device__ inline float crow_f(const float *A, const Geo &g, int i, int jj, int k) {
+    return (jj < 0 || jj > g.ny + 1) ? 0.0f : A[hix(g, i, jj, k)];
+}
+
+__global__ void k_codes2_f(const float *__restrict__ C, uint8_t *__restrict__ codes, uint8_t *__restrict__ codes_g,
+                           Geo g, int cs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
+    if (i > g.nx || j >= prow0(g) + prows(g)) return;
+    const int k = 1, h = hix(g, i, j, k);
+    float c0[3], cm[3], cp[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) c0[m] = C[(size_t)m * cs + h];
+    int code = 0;
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const float *Cm = C + (size_t)m * cs;
+            if (d == 1 && g.walls) {
+                cm[m] = crow_f(Cm, g, i, j - 1, k);
+                cp[m] = crow_f(Cm, g, i, j + 1, k);
+            } else {
+                const int od = d == 0 ? 1 : g.sx;
+                cm[m] = Cm[h - od];
+                cp[m] = Cm[h + od];
+            }
+        }
+        const int idx = select2_f(cm, c0, cp);   // 0..3; 0 -> the cell value (code 3)
+        code |= (idx == 0 ? 3 : idx - 1) << (2 * d);
+    }
+    if (j >= 1 && j <= g.ny) codes[qix(g, i, j, k)] = (uint8_t)code;
+    else codes_g[gcix(g, i, j, k)] = (uint8_t)code;
+}
+
+__device__ inline int code2_at(const uint8_t *codes, const uint8_t *codes_g, const Geo &g, int i, int j) {
+    return (j >= 1 && j <= g.ny) ? codes[qix(g, i, j, 1)] : codes_g[gcix(g, i, j, 1)];
+}
+
+// Newton for G(x) = M x + a(x) x - b = 0, x = (c11, c12, c22), with M the 2D
+// Lyapunov operator of A = (grad u)^T and a = 1 + f(x) dt/Wi (lyap_func2 of
+// the FP64 step); the Jacobian is M + a I + (da/dtr) x (e1 + e3)^T.  The
+// relative step test uses the larger of eps^2 and (8 ulp)^2: the 2D
+// reference's eps (1e-10, fenep_2d.f90:291-293) is below FP32 resolution,
+// and once the step is a few ulp of x the quadratic iteration has converged
+// to FP32 rounding.  Returns the iterations taken, > itrmax when not
+// converged.
+__device__ __forceinline__ int newton2_f(float (&x)[3], const float (&b)[3], float a00, float a01, float a10, float a11,
+                                const MixConst &mc, double lp2, int itrmax) {
+    const float M[3][3] = {{2.0f * a00, 2.0f * a01, 0.0f}, {a10, a00 + a11, a01}, {0.0f, 2.0f * a10, 2.0f * a11}};
+    const float ulp8 = 8.0f * FLT_EPSILON;
+    const float eps2 = fmaxf(mc.eps2f, ulp8 * ulp8);
+    int itr;
+#pragma unroll 1
+    for (itr = 1; itr <= itrmax; ++itr) {
+        const float f = peterlin2_f(x[0], x[2], mc.lp2f, lp2);
+        const float a = 1.0f + f * mc.dtwi;
+        const float den = mc.lp2f - (x[0] + x[2]);
+        const float cc = mc.dtwi * (mc.lp2f - 2.0f) / (den * den);
+        float J[3][4];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            J[q][3] = M[q][0] * x[0] + M[q][1] * x[1] + M[q][2] * x[2] + a * x[q] - b[q];
+#pragma unroll
+            for (int w = 0; w < 3; ++w) J[q][w] = M[q][w] + (w != 1 ? cc * x[q] : 0.0f) + (w == q ? a : 0.0f);
+        }
+        // Gauss-Jordan without pivoting: J is dominated by its diagonal a >= 1
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float inv = 1.0f / J[k][k];
+#pragma unroll
+            for (int q = k + 1; q < 4; ++q) J[k][q] *= inv;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q == k) continue;
+                const float fr = J[q][k];
+#pragma unroll
+                for (int w = k + 1; w < 4; ++w) J[q][w] -= fr * J[k][w];
+            }
+        }
+        float sr = 0.0f, sx = 0.0f;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            x[m] -= J[m][3];
+            sr = fmaf(J[m][3], J[m][3], sr);
+            sx = fmaf(x[m], x[m], sx);
+        }
+        if (!(sr > eps2 * sx)) break;   // the relative step test, also ends on NaN
+    }
+    return itr;
+}
+
+__global__ void __launch_bounds__(128) k_update2_f(const float *__restrict__ C, float *__restrict__ Cn,
+                                                   float *__restrict__ fpet, const uint8_t *__restrict__ codes,
+                                                   const uint8_t *__restrict__ codes_g, const float *__restrict__ U,
+                                                   const float *__restrict__ V, Geo g, Phys ph, MixConst mc, int cs,
+                                                   StepCounters *cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + prow0(g);
+    const int k = 1;
+    const bool active = i <= g.nx && j < prow0(g) + prows(g);
+    unsigned long long my_itr = 0, my_unconv = 0;
+    if (active) {
+        const int h = hix(g, i, j, k);
+        const int cself = code2_at(codes, codes_g, g, i, j);
+        const int cxm = code2_at(codes, codes_g, g, wrapx(g, i - 1), j) & 3;
+        const int cxp = code2_at(codes, codes_g, g, wrapx(g, i + 1), j) & 3;
+        int jm = j - 1, jp = j + 1;
+        if (!g.walls) { jm = wrapy(g, jm); jp = wrapy(g, jp); }
+        const int cym = jm < 0 ? 3 : (code2_at(codes, codes_g, g, i, jm) >> 2) & 3;
+        const int cyp = jp > g.ny + 1 ? 3 : (code2_at(codes, codes_g, g, i, jp) >> 2) & 3;
+        const int isx = (cself & 3) + 1, isy = ((cself >> 2) & 3) + 1;
+        const int hxm = hix(g, wrapx(g, i - 1), j, k), hxp = hix(g, wrapx(g, i + 1), j, k);
+        const int ox = 1;
+        const float u1 = U[hix(g, i - 1, j, k)], u2 = U[h];
+        const float v1 = crow_f(V, g, i, j - 1, k), v2 = V[h];
+        // Cstar upwind coefficients with the 2D weight 1/4 (fenep_2d.f90)
+        const float s1 = (-u2 + fabsf(u2)) * mc.sx, s2 = 0.25f + (-u2 - fabsf(u2)) * mc.sx;
+        const float s3 = 0.25f + (u1 - fabsf(u1)) * mc.sx, s4 = (u1 + fabsf(u1)) * mc.sx;
+        const float s5 = (-v2 + fabsf(v2)) * mc.sy, s6 = 0.25f + (-v2 - fabsf(v2)) * mc.sy;
+        const float s7 = 0.25f + (v1 - fabsf(v1)) * mc.sy, s8 = (v1 + fabsf(v1)) * mc.sy;
+        float b[3], x[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const float *Cm = C + (size_t)m * cs;
+            const float c0 = Cm[h];
+            const float pxm = face_p_f(isx, Cm[h - ox], c0, Cm[h + ox]);
+            const float nxp = face_n_f(isx, Cm[h - ox], c0, Cm[h + ox]);
+            const float pxp = face_p_f(cxp + 1, Cm[hxp - ox], Cm[hxp], Cm[hxp + ox]);
+            const float nxm = face_n_f(cxm + 1, Cm[hxm - ox], Cm[hxm], Cm[hxm + ox]);
+            float pym, nyp, pyp, nym;
+            if (!g.walls) {
+                const int hym = hix(g, i, jm, k), hyp = hix(g, i, jp, k), oy = g.sx;
+                pym = face_p_f(isy, Cm[h - oy], c0, Cm[h + oy]);
+                nyp = face_n_f(isy, Cm[h - oy], c0, Cm[h + oy]);
+                pyp = face_p_f(cyp + 1, Cm[hyp - oy], Cm[hyp], Cm[hyp + oy]);
+                nym = face_n_f(cym + 1, Cm[hym - oy], Cm[hym], Cm[hym + oy]);
+            } else {
+                const float ym2 = crow_f(Cm, g, i, j - 2, k), ym1 = crow_f(Cm, g, i, j - 1, k);
+                const float yp1 = crow_f(Cm, g, i, j + 1, k), yp2 = crow_f(Cm, g, i, j + 2, k);
+                pym = face_p_f(isy, ym1, c0, yp1);
+                nyp = face_n_f(isy, ym1, c0, yp1);
+                pyp = face_p_f(cyp + 1, c0, yp1, yp2);
+                nym = face_n_f(cym + 1, ym2, ym1, c0);
+            }
+            b[m] = s3 * pxm + s1 * pxp + s4 * nxm + s2 * nxp + s7 * pym + s5 * pyp + s8 * nym + s6 * nyp;
+            x[m] = c0;
+        }
+        b[0] += mc.dtwi;
+        b[2] += mc.dtwi;
+        auto u = [&](int a, int bb) { return crow_f(U, g, a, bb, k); };
+        auto v = [&](int a, int bb) { return crow_f(V, g, a, bb, k); };
+        // the velocity gradient of fenep_2d.f90 (A0) and its transpose A
+        const float g00 = mc.gx1 * (u(i, j) - u(i - 1, j));
+        const float g01 = mc.gx4 * (-v(i - 1, j - 1) + v(i + 1, j - 1) - v(i - 1, j) + v(i + 1, j));
+        const float g10 = mc.gy4 * (-u(i - 1, j - 1) - u(i, j - 1) + u(i - 1, j + 1) + u(i, j + 1));
+        const float g11 = mc.gy1 * (v(i, j) - v(i, j - 1));
+        const int itr = newton2_f(x, b, g00, g10, g01, g11, mc, ph.lp2, ph.newton_itrmax);
+        my_itr = (unsigned long long)itr;
+        my_unconv = itr > ph.newton_itrmax ? 1ull : 0ull;
+#pragma unroll
+        for (int m = 0; m < 3; ++m) Cn[(size_t)m * cs + h] = x[m];
+        fpet[h] = peterlin2_f(x[0], x[2], mc.lp2f, ph.lp2);
+    }
+    unsigned long long a = my_itr, b2 = my_unconv;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b2 += __shfl_down_sync(0xffffffffu, b2, o);
+    }
+    if (((threadIdx.x + blockDim.x * threadIdx.y) & 31) == 0) {
+        if (a) atomicAdd(&cnt->newton_iters, a);
+        if (b2) atomicAdd(&cnt->newton_unconverged, b2);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Momentum right-hand side in increment form: Q_c = dt * R_c (FP32).
 struct MomArgsF {
     const float *U, *V, *W;   // hi parts of the velocity
@@ -808,7 +1060,9 @@ struct MomArgsF {
     double dt;
 };
 
-__global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixConst mc) {
+// DIM 2: the 2D stress of C = (xx, xy, yy) and no z terms (W = 0)
+template <int DIM>
+__device__ __forceinline__ void momentum_f(const MomArgsF &a, const Geo &g, const MixConst &mc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k = blockIdx.z + 1;
@@ -821,46 +1075,65 @@ __global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixCo
         // polymer_stress (fenep.f90:645-691) with C0 = f(C) C - I on the fly
         const int cs = a.cs;
         const float *C = a.C, *fp = a.fpet;
-        auto c0 = [&](int m, int hh) {
-            const float e = (m == 1 || m == 4 || m == 6) ? 1.0f : 0.0f;
-            return fp[hh] * C[(size_t)(m - 1) * cs + hh] - e;
-        };
-        const float sx = (c0(1, h + ox) - c0(1, h)) * ix
-                       + (-c0(2, h - oy) - c0(2, h + ox - oy) + c0(2, h + oy) + c0(2, h + ox + oy)) * (0.25f * iy)
-                       + (-c0(3, h - oz) - c0(3, h + ox - oz) + c0(3, h + oz) + c0(3, h + ox + oz)) * (0.25f * iz);
-        const float sy = (-c0(2, h - ox) + c0(2, h + ox) - c0(2, h - ox + oy) + c0(2, h + ox + oy)) * (0.25f * ix)
-                       + (c0(4, h + oy) - c0(4, h)) * iy
-                       + (-c0(5, h - oz) - c0(5, h + oy - oz) + c0(5, h + oz) + c0(5, h + oy + oz)) * (0.25f * iz);
-        const float sz = (-c0(3, h - ox) + c0(3, h + ox) - c0(3, h - ox + oz) + c0(3, h + ox + oz)) * (0.25f * ix)
-                       + (-c0(5, h - oy) + c0(5, h + oy) - c0(5, h - oy + oz) + c0(5, h + oy + oz)) * (0.25f * iy)
-                       + (c0(6, h + oz) - c0(6, h)) * iz;
-        tx = a.coef_t * sx; ty = a.coef_t * sy; tz = a.coef_t * sz;
+        if constexpr (DIM == 3) {
+            auto c0 = [&](int m, int hh) {
+                const float e = (m == 1 || m == 4 || m == 6) ? 1.0f : 0.0f;
+                return fp[hh] * C[(size_t)(m - 1) * cs + hh] - e;
+            };
+            const float sx = (c0(1, h + ox) - c0(1, h)) * ix
+                           + (-c0(2, h - oy) - c0(2, h + ox - oy) + c0(2, h + oy) + c0(2, h + ox + oy)) * (0.25f * iy)
+                           + (-c0(3, h - oz) - c0(3, h + ox - oz) + c0(3, h + oz) + c0(3, h + ox + oz)) * (0.25f * iz);
+            const float sy = (-c0(2, h - ox) + c0(2, h + ox) - c0(2, h - ox + oy) + c0(2, h + ox + oy)) * (0.25f * ix)
+                           + (c0(4, h + oy) - c0(4, h)) * iy
+                           + (-c0(5, h - oz) - c0(5, h + oy - oz) + c0(5, h + oz) + c0(5, h + oy + oz)) * (0.25f * iz);
+            const float sz = (-c0(3, h - ox) + c0(3, h + ox) - c0(3, h - ox + oz) + c0(3, h + ox + oz)) * (0.25f * ix)
+                           + (-c0(5, h - oy) + c0(5, h + oy) - c0(5, h - oy + oz) + c0(5, h + oy + oz)) * (0.25f * iy)
+                           + (c0(6, h + oz) - c0(6, h)) * iz;
+            tx = a.coef_t * sx; ty = a.coef_t * sy; tz = a.coef_t * sz;
+        } else {
+            auto c0 = [&](int m, int hh) {
+                const float e = (m == 1 || m == 3) ? 1.0f : 0.0f;
+                return fp[hh] * C[(size_t)(m - 1) * cs + hh] - e;
+            };
+            const float sx = (c0(1, h + ox) - c0(1, h)) * ix
+                           + (-c0(2, h - oy) - c0(2, h + ox - oy) + c0(2, h + oy) + c0(2, h + ox + oy)) * (0.25f * iy);
+            const float sy = (-c0(2, h - ox) + c0(2, h + ox) - c0(2, h - ox + oy) + c0(2, h + ox + oy)) * (0.25f * ix)
+                           + (c0(3, h + oy) - c0(3, h)) * iy;
+            tx = a.coef_t * sx; ty = a.coef_t * sy;
+        }
     }
     const float *U = a.U, *V = a.V, *W = a.W;
     auto u = [&](int hh) { return U[hh]; };
     auto v = [&](int hh) { return V[hh]; };
     auto w = [&](int hh) { return W[hh]; };
-    // convection (fenep.f90:694-734), divergence form
-    const float uc = u(h), vc = v(h), wc = w(h);
-    const float uxm = u(h - ox), uxp = u(h + ox), uym = u(h - oy), uyp = u(h + oy), uzm = u(h - oz), uzp = u(h + oz);
-    const float vxm = v(h - ox), vxp = v(h + ox), vym = v(h - oy), vyp = v(h + oy), vzm = v(h - oz), vzp = v(h + oz);
-    const float wxm = w(h - ox), wxp = w(h + ox), wym = w(h - oy), wyp = w(h + oy), wzm = w(h - oz), wzp = w(h + oz);
+    // convection (fenep.f90:694-734), divergence form, and viscous
+    // (fenep.f90:736-770)
+    const float uc = u(h), vc = v(h);
+    const float uxm = u(h - ox), uxp = u(h + ox), uym = u(h - oy), uyp = u(h + oy);
+    const float vxm = v(h - ox), vxp = v(h + ox), vym = v(h - oy), vyp = v(h + oy);
     float t1 = 0.5f * (uxm + uc), t2 = 0.5f * (uc + uxp);
     float ax = (t2 * t2 - t1 * t1) * ix
-             + (0.25f * (vc + v(h + ox)) * (uc + uyp) - 0.25f * (vym + v(h + ox - oy)) * (uym + uc)) * iy
-             + (0.25f * (wc + w(h + ox)) * (uc + uzp) - 0.25f * (wzm + w(h + ox - oz)) * (uzm + uc)) * iz;
+             + (0.25f * (vc + v(h + ox)) * (uc + uyp) - 0.25f * (vym + v(h + ox - oy)) * (uym + uc)) * iy;
     float t3 = 0.5f * (vym + vc), t4 = 0.5f * (vc + vyp);
     float ay = (0.25f * (uc + uyp) * (vc + vxp) - 0.25f * (uxm + u(h - ox + oy)) * (vxm + vc)) * ix
-             + (t4 * t4 - t3 * t3) * iy
-             + (0.25f * (wc + w(h + oy)) * (vc + vzp) - 0.25f * (wzm + w(h + oy - oz)) * (vzm + vc)) * iz;
-    float t5 = 0.5f * (wzm + wc), t6 = 0.5f * (wc + wzp);
-    float az = (0.25f * (uc + uzp) * (wc + wxp) - 0.25f * (uxm + u(h - ox + oz)) * (wxm + wc)) * ix
-             + (0.25f * (vc + vzp) * (wc + wyp) - 0.25f * (vym + v(h - oy + oz)) * (wym + wc)) * iy
-             + (t6 * t6 - t5 * t5) * iz;
-    // viscous (fenep.f90:736-770)
-    const float bx = (uxm - 2.0f * uc + uxp) * mc.ix2 + (uym - 2.0f * uc + uyp) * mc.iy2 + (uzm - 2.0f * uc + uzp) * mc.iz2;
-    const float by = (vxm - 2.0f * vc + vxp) * mc.ix2 + (vym - 2.0f * vc + vyp) * mc.iy2 + (vzm - 2.0f * vc + vzp) * mc.iz2;
-    const float bz = (wxm - 2.0f * wc + wxp) * mc.ix2 + (wym - 2.0f * wc + wyp) * mc.iy2 + (wzm - 2.0f * wc + wzp) * mc.iz2;
+             + (t4 * t4 - t3 * t3) * iy;
+    float bx = (uxm - 2.0f * uc + uxp) * mc.ix2 + (uym - 2.0f * uc + uyp) * mc.iy2;
+    float by = (vxm - 2.0f * vc + vxp) * mc.ix2 + (vym - 2.0f * vc + vyp) * mc.iy2;
+    float az = 0.0f, bz = 0.0f;
+    if constexpr (DIM == 3) {
+        const float wc = w(h);
+        const float uzm = u(h - oz), uzp = u(h + oz), vzm = v(h - oz), vzp = v(h + oz);
+        const float wxm = w(h - ox), wxp = w(h + ox), wym = w(h - oy), wyp = w(h + oy), wzm = w(h - oz), wzp = w(h + oz);
+        ax += (0.25f * (wc + w(h + ox)) * (uc + uzp) - 0.25f * (wzm + w(h + ox - oz)) * (uzm + uc)) * iz;
+        ay += (0.25f * (wc + w(h + oy)) * (vc + vzp) - 0.25f * (wzm + w(h + oy - oz)) * (vzm + vc)) * iz;
+        float t5 = 0.5f * (wzm + wc), t6 = 0.5f * (wc + wzp);
+        az = (0.25f * (uc + uzp) * (wc + wxp) - 0.25f * (uxm + u(h - ox + oz)) * (wxm + wc)) * ix
+           + (0.25f * (vc + vzp) * (wc + wyp) - 0.25f * (vym + v(h - oy + oz)) * (wym + wc)) * iy
+           + (t6 * t6 - t5 * t5) * iz;
+        bx += (uzm - 2.0f * uc + uzp) * mc.iz2;
+        by += (vzm - 2.0f * vc + vzp) * mc.iz2;
+        bz = (wxm - 2.0f * wc + wxp) * mc.ix2 + (wym - 2.0f * wc + wyp) * mc.iy2 + (wzm - 2.0f * wc + wzp) * mc.iz2;
+    }
     const float A[3] = {-ax, -ay, -az};
     const float B[3] = {a.vis * bx, a.vis * by, a.vis * bz};
     const float T[3] = {tx, ty, tz};
@@ -868,11 +1141,11 @@ __global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixCo
     const float id[3] = {ix, iy, iz};
     const float ph0 = a.Ph[h], pl0 = a.Pl[h];
     const float dt = (float)a.dt;
-    // every load of the three components before the first store (the
-    // history arrays are read and written in place)
-    float a0[3], t0[3], php[3], plp[3], fb[3];
+    // every load of the components before the first store (the history
+    // arrays are read and written in place)
+    float a0[DIM], t0[DIM], php[DIM], plp[DIM], fb[DIM];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < DIM; ++c) {
         a0[c] = a.ab2_first ? A[c] : a.A0[c][o];
         t0[c] = a.ab2_first ? T[c] : a.T0[c][o];
         php[c] = a.Ph[hp[c]];
@@ -880,7 +1153,7 @@ __global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixCo
         fb[c] = a.F[c] ? a.F[c][o] : a.Fu[c];
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < DIM; ++c) {
         // pressure difference from the df64 pair: the hi difference is
         // correctly rounded, the lo difference carries the rest
         const float gp = -((php[c] - ph0) + (plp[c] - pl0)) * id[c];
@@ -890,6 +1163,9 @@ __global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixCo
         a.T0[c][o] = T[c];
     }
 }
+
+__global__ void __launch_bounds__(256, 6) k_momentum3_f(MomArgsF a, Geo g, MixConst mc) { momentum_f<3>(a, g, mc); }
+__global__ void __launch_bounds__(256, 6) k_momentum2_f(MomArgsF a, Geo g, MixConst mc) { momentum_f<2>(a, g, mc); }
 
 // ---------------------------------------------------------------------------
 // IBM (fenep_mpi.f90:1794-1929).  Ua = U + dt R at the stencil points with the
@@ -1599,6 +1875,14 @@ cudaError_t solve_periodic_mp(Dev &d, const TS *src, XOutF out, double lhs0, dou
     DivideSpec none{};
     const int txy = std::max(1, std::min(32, 4096 / ny));
     const size_t smy = (size_t)2 * ny * txy * sizeof(Cx<float>);
+    if (nz == 1) {
+        // 2D: the y lines transform, divide and transform back in one pass
+        DivideSpec dv{d.kx2, d.ky2, d.kz2, lhs0, lhs1, (double)nx * ny * nz, 0};
+        k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, -1, 1, dv); count_launch();
+        int npp = ny / 2, total = npp * nz;
+        k_fft_x_inv<float, XOutF><<<(total + ppc - 1) / ppc, ppc * tpp, smx, s>>>(d.Hf, out, nx, ny, npp, nz, 1, g.sx, g.sy, d.twxf_r, d.twxf_i); count_launch();
+        return cudaGetLastError();
+    }
     k_fft_lines<float><<<dim3((nxh + txy - 1) / txy, nz), 256, smy, s>>>(d.Hf, ny, nxh, nxh, nxh * ny, txy, d.twyf_r, d.twyf_i, -1, 0, none); count_launch();
     {
         DivideSpec dv{d.kx2, d.ky2, d.kz2, lhs0, lhs1, (double)nx * ny * nz, 1};
@@ -2005,8 +2289,14 @@ cudaError_t bc_all_state_mixed(Dev &d, cudaStream_t s) {
     F8_CUDA_RET(bc_field(d.W, d.g, BC_W, s));
     F8_CUDA_RET(bc_field(d.P, d.g, BC_P, s));
     long n = halo_count(d.g);
-    k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
-    k_pet_all_f<<<(d.cs + 255) / 256, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
+    const unsigned nb = (unsigned)((n + 255) / 256), cb = (unsigned)((d.cs + 255) / 256);
+    if (d.g.dim == 3) {
+        k_bc_c_pet_f<6><<<nb, 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
+        k_pet_all_f<6><<<cb, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
+    } else {
+        k_bc_c_pet_f<3><<<nb, 256, 0, s>>>(d.Cf, d.fpetf, d.g, d.cs, d.ph.lp2); count_launch();
+        k_pet_all_f<3><<<cb, 256, 0, s>>>(d.Cf, d.fpetf, d.cs, d.ph.lp2); count_launch();
+    }
     const double *src[5] = {d.U, d.V, d.W, d.P, d.Phi};
     float *hi[5] = {d.Uf, d.Vf, d.Wf, d.Pf, d.Phif}, *lo[5] = {d.Ul, d.Vl, d.Wl, d.Pl, d.Phil};
     for (int q = 0; q < 5; ++q) {
@@ -2108,10 +2398,28 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     // wall channel: the ghost rows' codes and update run on a side stream
     // beside the interior kernels (they read the state and the interior codes
     // of rows 1 and NY, and write only ghost-row cells)
-    const bool gbranch = o.polymer && g.walls && d.aux[0];
+    const bool d3 = g.dim == 3;
+    const bool gbranch = o.polymer && g.walls && d.aux[0] && d3;
     const dim3 gg((g.nx + 127) / 128, 2, g.nz);
     cudaStream_t sg = gbranch ? d.aux[0] : s;
-    if (o.polymer) {
+    if (o.polymer && !d3) {
+        // 2D (fenep_2d.f90:138-393): codes and update over the rows of the
+        // update (with walls the ghost rows too), then the C halo
+        const dim3 blk(32, 4), grd((g.nx + blk.x - 1) / blk.x, (prows(g) + blk.y - 1) / blk.y, 1);
+        kmark(F8_KERNEL_CODES, 0);
+        k_codes2_f<<<grd, blk, 0, s>>>(d.Cf, d.codes, d.codes_g, g, d.cs); count_launch();
+        kmark(F8_KERNEL_CODES, 1);
+        mark(1);
+        kmark(F8_KERNEL_UPDATE, 0);
+        k_update2_f<<<grd, blk, 0, s>>>(d.Cf, d.Cnf, d.fpetf, d.codes, d.codes_g, d.Uf, d.Vf, g, d.ph, mc, d.cs,
+                                        d.cnt); count_launch();
+        kmark(F8_KERNEL_UPDATE, 1);
+        std::swap(d.Cf, d.Cnf);
+        const long n = halo_count(g);
+        if (g.walls) { k_bc_c_pet_xz_f<3><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch(); }
+        else { k_bc_c_pet_f<3><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch(); }
+        if ((e = cudaGetLastError())) return e;
+    } else if (o.polymer) {
         dim3 blk(32, 4);
         if (g.walls) {
             if (gbranch) {
@@ -2143,10 +2451,10 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         if (g.walls) {
             if (gbranch) F8_CUDA_RET(cudaStreamWaitEvent(s, d.ev_g[2], 0));
             std::swap(d.Cf, d.Cnf);
-            k_bc_c_pet_xz_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+            k_bc_c_pet_xz_f<6><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
         } else {
             std::swap(d.Cf, d.Cnf);
-            k_bc_c_pet_f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+            k_bc_c_pet_f<6><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
         }
         if (tp) F8_CUDA_RET(cudaMemcpyAsync(tp->Cn, d.Cf, 6 * hbf, cudaMemcpyDeviceToDevice, s));
         if ((e = cudaGetLastError())) return e;
@@ -2170,7 +2478,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         a.dt = d.ph.dt;
         dim3 blk(32, 8);
         kmark(F8_KERNEL_MOMENTUM, 0);
-        k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch();
+        if (d3) { k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch(); }
+        else { k_momentum2_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch(); }
         kmark(F8_KERNEL_MOMENTUM, 1);
         if ((e = cudaGetLastError())) return e;
     }
@@ -2183,7 +2492,8 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             F8_CUDA_RET(cudaEventRecord(d.ev_g[3], s));
             F8_CUDA_RET(cudaStreamWaitEvent(sg, d.ev_g[3], 0));
         }
-        k_extrap_ghost_f<<<(ng + 255) / 256, 256, 0, sg>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch();
+        if (d3) { k_extrap_ghost_f<6><<<(ng + 255) / 256, 256, 0, sg>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch(); }
+        else { k_extrap_ghost_f<3><<<(ng + 255) / 256, 256, 0, sg>>>(d.Cf, d.fpetf, g, d.cs, d.ph.lp2); count_launch(); }
     }
     if (tp) {
         k_tape_ua<<<tnb, 256, 0, s>>>(d.Uf, d.Ul, d.Vf, d.Vl, d.Wf, d.Wl, d.Qf[0], d.Qf[1], d.Qf[2], tp->Ua[0],
@@ -2196,6 +2506,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
     // U* = U^n + dU of the last solve, adds to the marker forces, spreads them
     // onto the right-hand sides saved before the first spread and solves again
     const int repeats = o.ibm ? std::max(1, d.ibm_repeats) : 1;
+    const int nvc = d3 ? 3 : 2;   // velocity components
     for (int r = 0; r < repeats; ++r) {
         if (o.ibm) {
             IbmArgsF a{};
@@ -2209,13 +2520,14 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
                 if (ar < 0.5) return (1.0 + std::sqrt(-3.0 * (r * r) + 1.0)) / 3.0;
                 return 0.0;
             };
-            for (int c = 0; c < 3; ++c) {
+            for (int c = 0; c < nvc; ++c) {
                 a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
                 a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
                 a.idx[c] = d.csr_idx[c]; a.cw[c] = d.csr_w[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
                 for (int dk = 0; dk < 3; ++dk) {
                     double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
-                    a.wz[c][dk] = (float)roma(zg);
+                    // 2D: one marker plane and no z weight (fenep_2d.f90:1726-1819)
+                    a.wz[c][dk] = d3 ? (float)roma(zg) : (dk == 1 ? 1.0f : 0.0f);
                 }
             }
             a.uw2 = df_from_d(2.0 * g.uwall);
@@ -2224,17 +2536,18 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             const bool last = r == repeats - 1;
             a.mode = r > 0 ? 1 : 0;
             a.accumulate = r > 0 ? 1 : 0;
-            for (int c = 0; c < 3; ++c) {
+            for (int c = 0; c < nvc; ++c) {
                 a.D[c] = d.dUf[c];
                 a.Qb[c] = (r > 0 && d.Qpre[c]) ? d.Qpre[c] : d.Qf[c];
             }
             if (r == 0 && repeats > 1)
-                for (int c = 0; c < 3; ++c)
+                for (int c = 0; c < nvc; ++c)
                     F8_CUDA_RET(cudaMemcpyAsync(d.Qpre[c], d.Qf[c], (size_t)d.ni * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            dim3 gi((d.nm + 31) / 32, g.nz, 3);
+            dim3 gi((d.nm + 31) / 32, g.nz, nvc);
             k_ibm_interp_f<<<gi, dim3(32, 3), 0, s>>>(a, g); count_launch();
-            int maxact = std::max(d.nact[0], std::max(d.nact[1], d.nact[2]));
-            if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, 3), 128, 0, s>>>(a, g); count_launch(); }
+            int maxact = 0;
+            for (int c = 0; c < nvc; ++c) maxact = std::max(maxact, d.nact[c]);
+            if (maxact > 0) { k_ibm_spread_f<<<dim3((maxact + 127) / 128, g.nz, nvc), 128, 0, s>>>(a, g); count_launch(); }
             if (last && drag_out_dev) F8_CUDA_RET(launch_drag(d, drag_out_dev, s));
             if ((e = cudaGetLastError())) return e;
             if (tp && last)
@@ -2254,7 +2567,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             F8_CUDA_RET(cudaEventRecord(d.ev_fork, s));
             for (int b = 0; b < 2; ++b) F8_CUDA_RET(cudaStreamWaitEvent(d.aux[b], d.ev_fork, 0));
         }
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < nvc; ++c) {
             const XOutF out{d.dUf[c], nullptr, 0};
             if (branches) {
                 cudaStream_t sc = c == 0 ? s : d.aux[c - 1];

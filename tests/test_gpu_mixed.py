@@ -84,10 +84,12 @@ def test_mixed_newtonian_no_ibm(gpu, oracle):
         assert rel_l2(interior(om[f]), interior(oo[f])) <= VEL_TOL, f
 
 
-def test_mixed_rejects_2d(gpu):
+def test_mixed_2d_rejects_sor(gpu):
+    """The 2D mixed step solves its pressure with the FFT solvers only."""
     w = configs.scaled(configs.c1_2d(), 32, 32, 1)
-    with pytest.raises(Exception):
-        Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED)
+    with pytest.raises(F8Error) as err:
+        Solver(gpu, w.grid, w.phys, w.cyls, precision=abi.F8_MIXED, poisson=abi.F8_POISSON_SOR)
+    assert err.value.status == abi.F8_ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("precision", [abi.F8_MIXED, abi.F8_FP64])
