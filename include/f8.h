@@ -55,7 +55,7 @@ enum f8_status {
 enum f8_precision {
     F8_FP64 = 0,   /* every operation in FP64, same operation order as the oracle */
     F8_MIXED = 1   /* FP32 bulk stencils, FP64 state / Peterlin / reductions /
-                      Poisson defect correction                                  */
+                      Poisson defect correction; 2D with the FFT solver only     */
 };
 
 enum f8_poisson {
