@@ -457,8 +457,11 @@ def fp64_compare(fns, w, pois, nsteps, mixed_value):
         return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
     inner = (slice(1, -1), slice(1, -1), slice(1, -1))
-    errs = {f: rel(om[f][inner], o64[f][inner]) for f in ("u", "v", "w", "p")}
-    tr = lambda o: o["c"][inner][..., 0] + o["c"][inner][..., 3] + o["c"][inner][..., 5]
+    vel = ("u", "v", "w", "p") if w.grid.dim == 3 else ("u", "v", "p")
+    errs = {f: rel(om[f][inner], o64[f][inner]) for f in vel}
+    # trace of C: (xx, xy, xz, yy, yz, zz) in 3D, (xx, xy, yy) in 2D
+    tq = (0, 3, 5) if w.grid.dim == 3 else (0, 2)
+    tr = lambda o: sum(o["c"][inner][..., q] for q in tq)
     errs["trC"] = rel(tr(om), tr(o64))
     out = {"steps_compared": nsteps, "field_rel_l2": errs}
     if d64 is not None:
