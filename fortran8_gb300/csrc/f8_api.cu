@@ -588,6 +588,7 @@ int setup(f8_ctx *c) {
         const double dvol_m = g.dim == 3 ? (g.dx * g.dy) * g.dz : g.dx * g.dy;   // cell volume
         for (int comp = 0; comp < 3; ++comp) {
             API_CUDA(c, c->alloc(&d.Fc[comp], (size_t)nm * g.nz));
+            if (mixed) API_CUDA(c, c->alloc(&d.Fcf[comp], (size_t)nm * g.nz));
             std::vector<int> off(ncol + 1, 0), idx;
             std::vector<std::vector<int>> lists(ncol);
             if (comp < ncomp)

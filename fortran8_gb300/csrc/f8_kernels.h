@@ -42,6 +42,7 @@ struct Dev {
     int ibm_repeats;                       // direct-forcing iterations per step (NS)
     int ibm_edge;                          // some marker stencil reaches a ghost column, a ghost row or row NY
     float *Qpre[3];                        // mixed, NS > 1: the right-hand sides before spreading
+    float *Fcf[3];                         // mixed: FP32 copies of the marker forces (the spreading's)
     // mixed-precision state and work (F8_MIXED): the state as df64 pairs
     // (hi, lo) of FP32 halo fields
     float *Uf, *Vf, *Wf, *Ul, *Vl, *Wl;    // velocity hi / lo

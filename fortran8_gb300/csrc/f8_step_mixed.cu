@@ -78,21 +78,32 @@ MixConst make_const(const Geo &g, const Phys &ph) {
 // Peterlin factor (fenep.f90:510-515) from FP32 components: FP32 normally, FP64
 // when the denominator L^2 - tr C is within 1% of L^2 of the limit.
 __device__ inline float peterlin_f(float x0, float x3, float x5, float lp2f, double lp2) {
-    float tr = x0 + x3 + x5;
-    float den = lp2f - tr;
-    if (den > 0.01f * lp2f) return (lp2f - 3.0f) / den;
-    double trd = (double)x0 + (double)x3 + (double)x5;
-    return (float)((lp2 - 3.0) / (lp2 - trd));
+    const float tr = x0 + x3 + x5;
+    const float den = lp2f - tr;
+    const bool near = !(den > 0.01f * lp2f);
+    float f = (lp2f - 3.0f) / den;
+    // the FP64 branch is entered only by warps that hold a cell near the
+    // limit (a warp-uniform test, so that it is a branch, not a predicated
+    // FP64 sequence that every warp issues)
+    if (__any_sync(__activemask(), near) && near) {
+        const double trd = (double)x0 + (double)x3 + (double)x5;
+        f = (float)((lp2 - 3.0) / (lp2 - trd));
+    }
+    return f;
 }
 
 // The 2D model's Peterlin factor (L^2 - 2)/(L^2 - tr C), tr C = c11 + c22
 // (fenep_2d.f90), FP64 near the limit as peterlin_f
 __device__ inline float peterlin2_f(float x0, float x2, float lp2f, double lp2) {
-    float tr = x0 + x2;
-    float den = lp2f - tr;
-    if (den > 0.01f * lp2f) return (lp2f - 2.0f) / den;
-    double trd = (double)x0 + (double)x2;
-    return (float)((lp2 - 2.0) / (lp2 - trd));
+    const float tr = x0 + x2;
+    const float den = lp2f - tr;
+    const bool near = !(den > 0.01f * lp2f);
+    float f = (lp2f - 2.0f) / den;
+    if (__any_sync(__activemask(), near) && near) {
+        const double trd = (double)x0 + (double)x2;
+        f = (float)((lp2 - 2.0) / (lp2 - trd));
+    }
+    return f;
 }
 
 // f of NC stored components: 6 (3D: xx xy xz yy yz zz) or 3 (2D: xx xy yy)
@@ -490,7 +501,9 @@ __device__ inline int newton_fast_f(float (&x)[6], const float (&b)[6], const Ly
     for (itr = 1; itr <= maxit; ++itr) {
         const float tr = x[0] + x[3] + x[5];
         const float den = lp2f - tr;
-        const float f = den > 0.01f * lp2f ? __fdividef(lp2f - 3.0f, den) : peterlin_f(x[0], x[3], x[5], lp2f, lp2);
+        float f = __fdividef(lp2f - 3.0f, den);
+        if (__any_sync(__activemask(), !(den > 0.01f * lp2f)) && !(den > 0.01f * lp2f))
+            f = peterlin_f(x[0], x[3], x[5], lp2f, lp2);
         const float a = fmaf(f, dtwi, 1.0f);
         const float ia = __fdividef(1.0f, a);
         const float cc = __fdividef(mc.cpet, den * den);
@@ -1057,7 +1070,7 @@ struct MomArgsF {
     int cs;
     int polymer, ab2_first;
     float coef_t, vis;
-    double dt;
+    float dt;                 // dt rounded on the host (a per-thread FP64 conversion used the FP64 pipe)
 };
 
 // DIM 2: the 2D stress of C = (xx, xy, yy) and no z terms (W = 0)
@@ -1140,7 +1153,7 @@ __device__ __forceinline__ void momentum_f(const MomArgsF &a, const Geo &g, cons
     const int hp[3] = {h + ox, h + oy, h + oz};
     const float id[3] = {ix, iy, iz};
     const float ph0 = a.Ph[h], pl0 = a.Pl[h];
-    const float dt = (float)a.dt;
+    const float dt = a.dt;
     // every load of the components before the first store (the history
     // arrays are read and written in place)
     float a0[DIM], t0[DIM], php[DIM], plp[DIM], fb[DIM];
@@ -1225,6 +1238,7 @@ struct IbmArgsF {
     const float *Uh[3], *Ul[3];      // velocity (df64)
     const float *Qc[3];
     double *Fc[3];
+    float *Fcf[3];                   // FP32 copies of Fc, read by the spreading
     const int *off[3], *idx[3];
     const float *cw[3];              // per list entry: x weight * y weight
     const int *act[3];
@@ -1297,8 +1311,14 @@ __global__ void __launch_bounds__(96) k_ibm_interp_f(IbmArgsF a, Geo g) {
     if (dk == 0 && m < a.nm) {
         const df s3 = df_add(df_add(part[0][threadIdx.x], part[1][threadIdx.x]), part[2][threadIdx.x]);
         const double uc = comp == 0 ? a.mu[m] : (comp == 1 ? a.mv[m] : 0.0);
-        double *fc = &a.Fc[comp][m + (size_t)a.nm * (n - 1)];
-        *fc = (a.accumulate ? *fc : 0.0) + (uc - ((double)s3.hi + (double)s3.lo)) * a.idt;
+        const size_t q = m + (size_t)a.nm * (n - 1);
+        double *fc = &a.Fc[comp][q];
+        const double v = (a.accumulate ? *fc : 0.0) + (uc - ((double)s3.hi + (double)s3.lo)) * a.idt;
+        *fc = v;
+        // one conversion per marker and plane: the spreading reads each
+        // force once per list entry and plane, and a double-to-float
+        // conversion there ran on the FP64 pipe
+        a.Fcf[comp][q] = (float)v;
     }
 }
 
@@ -1311,13 +1331,13 @@ __device__ inline float spread_at_f(const IbmArgsF &a, const Geo &g, int comp, i
     // marker planes whose z stencil covers plane ke
     float acc = 0.0f;
     const int nlo = max(ke - 1, 1), nhi = min(ke + 1, g.nz);
-    const double *Fc = a.Fc[comp];
+    const float *Fc = a.Fcf[comp];
     const size_t nm = (size_t)a.nm;
     for (int q = b; q < e; ++q) {
         const int m = a.idx[comp][q];
         const float cw = a.cw[comp][q];
         for (int n = nlo; n <= nhi; ++n)
-            acc = fmaf((float)Fc[m + nm * (n - 1)], cw * a.wz[comp][ke - n + 1], acc);
+            acc = fmaf(Fc[m + nm * (n - 1)], cw * a.wz[comp][ke - n + 1], acc);
     }
     return acc;
 }
@@ -2475,7 +2495,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
         a.cs = d.cs; a.polymer = o.polymer; a.ab2_first = o.ab2_first;
         a.coef_t = (float)((1.0 - d.ph.beta) / (d.ph.re * d.ph.wi));
         a.vis = (float)(d.ph.beta / d.ph.re);
-        a.dt = d.ph.dt;
+        a.dt = (float)d.ph.dt;
         dim3 blk(32, 8);
         kmark(F8_KERNEL_MOMENTUM, 0);
         if (d3) { k_momentum3_f<<<cell_grid_m(g, blk), blk, 0, s>>>(a, g, mc); count_launch(); }
@@ -2522,7 +2542,7 @@ cudaError_t step_mixed(Dev &d, const StepOpts &o, double *drag_out_dev, int *sor
             };
             for (int c = 0; c < nvc; ++c) {
                 a.wx[c] = d.mwx[c]; a.wy[c] = d.mwy[c]; a.i0[c] = d.mi0[c]; a.j0[c] = d.mj0[c];
-                a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.off[c] = d.csr_off[c];
+                a.Uh[c] = Uh[c]; a.Ul[c] = Ul[c]; a.Qc[c] = d.Qf[c]; a.Fc[c] = d.Fc[c]; a.Fcf[c] = d.Fcf[c]; a.off[c] = d.csr_off[c];
                 a.idx[c] = d.csr_idx[c]; a.cw[c] = d.csr_w[c]; a.act[c] = d.act_cols[c]; a.nact[c] = d.nact[c]; a.Q[c] = d.Qf[c];
                 for (int dk = 0; dk < 3; ++dk) {
                     double zg = (dk - 1) + (c == 2 ? 0.5 : 0.0) - 0.5 + 0.25;  // (k - 1/2 [+1/2]) - (n - 1/4), k = n - 1 + dk
