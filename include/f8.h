@@ -319,9 +319,9 @@ enum f8_stage {
 /* Kernels of the FP32-mixed step launched once per step, each bracketed by
  * its own pair of CUDA events on its stream while timing is enabled: */
 enum f8_kernel {
-    F8_KERNEL_CODES = 0,       /* k_codes3_f: candidate faces + eigen test       */
-    F8_KERNEL_UPDATE = 1,      /* k_update3_f: Cstar + Newton + f(C)             */
-    F8_KERNEL_MOMENTUM = 2,    /* k_momentum3_f: stress, convection, viscous, RHS */
+    F8_KERNEL_CODES = 0,       /* k_codes3_f (2D: k_codes2_f): candidate faces + eigen test */
+    F8_KERNEL_UPDATE = 1,      /* k_update3_f (k_update2_f): Cstar + Newton + f(C)          */
+    F8_KERNEL_MOMENTUM = 2,    /* k_momentum3_f (k_momentum2_f): stress, convection, RHS   */
     F8_KERNEL_POISSON_RHS = 3, /* k_poisson_rhs_df: div(U + dU)/dt               */
     F8_KERNEL_DEFECT = 4,      /* k_defect_df: Poisson defect                    */
     F8_KERNEL_MARCH = 5,       /* k_march_df: projection + pressure update       */
@@ -333,7 +333,7 @@ int f8_timing(f8_ctx *ctx, double *total_ms, double *stage_ms /* F8_NSTAGE or NU
 int f8_timing_reset(f8_ctx *ctx);
 /* Accumulated device milliseconds of each enum f8_kernel launch (F8_NKERNEL
  * doubles) and the number of steps they cover, since the last timing reset.
- * FP32-mixed 3D contexts only (F8_ERR_UNSUPPORTED otherwise). */
+ * FP32-mixed contexts only (F8_ERR_UNSUPPORTED otherwise). */
 int f8_kernel_timing(f8_ctx *ctx, double *kernel_ms, long long *steps_timed);
 
 /* Stand-alone periodic spectral solve, the reference's fft_solve
