@@ -366,6 +366,11 @@ def run_ours(args, w):
             # the same gradient in FP64 (the parity path), for its own ratio
             adj["fp64"] = adjoint_cost(fns, args.adjoint_steps, args.adjoint_every, None, args.adjoint_workload,
                                        0, "fp64")
+        if args.adjoint_precision == "mixed" and not args.adjoint_grid and ws == 1 and not args.no_adjoint_large:
+            # the mixed gradient of the 512 x 256 x 256 channel over a 100-step
+            # window with a checkpoint every 10 steps (one GPU only: it holds
+            # about 170 GB of tape and checkpoints)
+            adj["large"] = adjoint_cost(fns, 100, 10, None, "c5_large", 0, "mixed")
     sb = state_bytes(st0)
     ncyl = len(w.cyls)
     e2e = {"value": cells * args.steps * ws / e2e_s / 1e6, "unit": "Mcell-steps/s", "repetitions": len(reps),
@@ -612,6 +617,8 @@ def main():
     ap.add_argument("--compare-steps", type=int, default=0,
                     help="steps of the mixed-vs-FP64 comparison (default: the workload's horizon, 2000)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward cost measurement")
+    ap.add_argument("--no-adjoint-large", action="store_true",
+                    help="skip the gradient of the 512 x 256 x 256 channel in the adjoint measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-every", type=int, default=20, help="checkpoint interval of the adjoint run")
     ap.add_argument("--adjoint-only", action="store_true",
