@@ -1398,12 +1398,7 @@ int kept_segments_mixed(f8_ctx *c, int K, int nseg) {
     const double ck = (15 * cs + 6 * ni) * 4;
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return 1;
-    const double avail = G.K * slot + G.nck * ck + 0.6 * (double)fr;
-    for (int r = nseg; r > 1; --r) {
-        const int nck = r < nseg ? nseg - r + 1 : 0;
-        if ((double)r * K * slot + nck * ck <= avail) return r;
-    }
-    return 1;
+    return kept_segments(G.K * slot + G.nck * ck + 0.6 * (double)fr, slot, ck, K, nseg);
 }
 
 // f8_grad on an FP32-mixed 3D context with the FFT solvers: the same

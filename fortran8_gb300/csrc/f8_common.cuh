@@ -191,6 +191,18 @@ inline int wall_plane_cluster(int ny, int nz, size_t limit, WallLayout *wl) {
     return 0;
 }
 
+// Segments (the last R >= 1 of nseg segments of K steps) whose tape the first
+// forward pass of a gradient keeps: the largest R whose tapes (slot_bytes per
+// step) and the checkpoints of the nseg - R segments before them plus one for
+// the final state (ck_bytes each) fit in avail bytes; 1 when none does.
+inline int kept_segments(double avail, double slot_bytes, double ck_bytes, int K, int nseg) {
+    for (int r = nseg; r > 1; --r) {
+        const int nck = r < nseg ? nseg - r + 1 : 0;
+        if ((double)r * K * slot_bytes + nck * ck_bytes <= avail) return r;
+    }
+    return 1;
+}
+
 struct StepCounters {
     unsigned long long newton_iters;
     unsigned long long newton_unconverged;
